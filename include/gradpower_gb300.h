@@ -1,0 +1,198 @@
+/*
+ * gradpower_gb300.h — C ABI of the GB300-native batched backward-Euler
+ * Newton step of GradPower.jl.
+ *
+ * The library integrates M independent fault scenarios of one power system
+ * on one GPU.  Every scenario follows the reference's CPU semantics
+ * (`integrate!`, src/dynamics.jl:502-655, and `newton_step!`,
+ * src/numerics.jl:55-176): backward Euler with step dt, a Newton solve per
+ * step that stops when the residual infinity norm drops below `newton_tol`,
+ * fault events toggled after step k's solve with an extra dt = 0 solve, and
+ * the state stored before that re-solve.
+ *
+ * Conventions
+ *  - All indices are 0-based.  z is the per-scenario state vector of length
+ *    n_sys = n_diff + n_alg + 2*n_bus, laid out as the reference lays it
+ *    after `reorder_state!` (src/clusters.jl:225-319): the states of each
+ *    generator cluster contiguously, then (vr, vi) per bus.
+ *  - Host arrays of per-scenario data are scenario-major: z[m*n_sys + i].
+ *  - Every function returns 0 on success or a negative GP_E* code; the
+ *    message of the last error is available from gp_last_error().
+ *  - The library owns its device memory.  A layout is used by one host
+ *    thread at a time; it runs on its own CUDA stream.
+ *
+ * Reference interfaces replaced (file:line in GradPower.jl):
+ *  - GpuBatchedLayout(dp, ps, M)           ext/GradPowerCUDAExt/GradPowerCUDAExt.jl:466
+ *      -> gp_layout_create
+ *  - integrate_gpu_schur_cudss!(gbl, ps, tf; dt, newton_tol)
+ *                                          ext/GradPowerCUDAExt/GradPowerCUDAExt.jl:3008-3080
+ *      -> gp_integrate(..., solver = GP_SOLVER_SCHUR_FP64)
+ *  - integrate_gpu_cudss!(gbl, ps, tf; dt, newton_tol)
+ *                                          ext/GradPowerCUDAExt/GradPowerCUDAExt.jl:2924-2996
+ *      -> gp_integrate(..., solver = GP_SOLVER_SCHUR_FP64): the monolithic
+ *         LU of J is the same exact Newton step; the library eliminates the
+ *         cluster blocks first, which is one elimination order of that LU
+ *  - _beuler_all_scenarios_gpu!            ext/GradPowerCUDAExt/GradPowerCUDAExt.jl:1522-1542
+ *      -> gp_residual (parity probe)
+ */
+#ifndef GRADPOWER_GB300_H
+#define GRADPOWER_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GP_ABI_VERSION 1
+
+/* error codes */
+#define GP_OK            0
+#define GP_E_INVALID    -1   /* bad argument or inconsistent problem */
+#define GP_E_CUDA       -2   /* CUDA runtime error */
+#define GP_E_NOMEM      -3   /* allocation failed */
+#define GP_E_NUMERIC    -4   /* zero pivot / non-finite values */
+#define GP_E_TIMEOUT    -5   /* a device wait ran out its iteration limit */
+
+/* device types, in the reference's DEVICE_REGISTRY order (src/layout.jl) */
+enum {
+    GP_GENROU = 0,      /* GENROU and GENSAL (src/kernels/genrou.jl)      */
+    GP_IEESGO = 1,      /* src/kernels/ieesgo.jl                           */
+    GP_TGOV1 = 2,       /* src/kernels/tgov1.jl                            */
+    GP_SEXS = 3,        /* src/kernels/sexs.jl                             */
+    GP_ESDC1A = 4,      /* src/kernels/esdc1a.jl                           */
+    GP_IEEEST = 5,      /* src/kernels/ieeest.jl                           */
+    GP_ZIPLOAD = 6,     /* src/kernels/zipload.jl                          */
+    GP_STATIC_GEN = 7,  /* src/kernels/static_gen.jl                       */
+    GP_NTYPES = 8
+};
+
+/*
+ * One struct-of-arrays device table (the reference's *Table structs,
+ * src/layout.jl:61-179).  Arrays have length n.  Absent pointers are -1.
+ *   bus      internal bus index
+ *   diff_ptr z index of the first differential state
+ *   alg_ptr  z index of the first algebraic state
+ *   ctrl_ptr index into u of the first control slot
+ *   par_ptr  index into p of the first parameter (fill_pvec! order)
+ *   link0    GENROU: z index of the governor's p_m (pm_idx)
+ *            IEESGO/TGOV1/IEEEST: z index of the machine speed w (w_idx)
+ *            SEXS/ESDC1A: z index of the stabiliser output v_s (vs_idx)
+ *            STATIC_GEN: bus type (1 PQ, 2 PV, 3 slack)
+ *   link1    GENROU: z index of the exciter's e_fd (efd_idx); else unused
+ *   online   0 = device skipped (may be NULL: all online)
+ */
+typedef struct gp_device_table {
+    int32_t n;
+    const int32_t *bus;
+    const int32_t *diff_ptr;
+    const int32_t *alg_ptr;
+    const int32_t *ctrl_ptr;
+    const int32_t *par_ptr;
+    const int32_t *link0;
+    const int32_t *link1;
+    const uint8_t *online;
+} gp_device_table;
+
+/*
+ * The problem, shared by all scenarios.  Values that differ per scenario
+ * (z0, u0, p) are passed to gp_layout_create separately.
+ */
+typedef struct gp_problem {
+    int32_t n_bus, n_diff, n_alg, n_ctrl, n_par;
+    /* complex bus admittance matrix in CSR form (src/network.jl:29-85) */
+    int32_t y_nnz;
+    const int32_t *y_rowptr;     /* [n_bus+1] */
+    const int32_t *y_colidx;     /* [y_nnz]   */
+    const double *y_re, *y_im;   /* [y_nnz]   */
+    /* bus adjacency without self loops, CSR (src/network.jl:15-27) */
+    const int32_t *adj_rowptr;   /* [n_bus+1] */
+    const int32_t *adj_colidx;
+    gp_device_table dev[GP_NTYPES];
+    const uint8_t *is_diff;      /* [n_diff+n_alg]: 1 for differential states */
+    /* generator clusters (src/clusters.jl:16-57), in z order */
+    int32_t n_clusters;
+    const int32_t *cl_w_start, *cl_w_size, *cl_bus;
+    const int32_t *cl_gen;       /* GENROU table index, -1 for a static generator */
+    const int32_t *cl_sg;        /* STATIC_GEN table index or -1 */
+    const int32_t *cl_gov_type;  /* GP_IEESGO, GP_TGOV1 or -1 */
+    const int32_t *cl_gov;
+    const int32_t *cl_exc_type;  /* GP_SEXS, GP_ESDC1A or -1 */
+    const int32_t *cl_exc;
+    const int32_t *cl_pss;       /* IEEEST table index or -1 */
+} gp_problem;
+
+/* A three-phase bus fault (ContingencyEvent, src/GradPower.jl:117-128).
+ * on_step/off_step are round(ton/dt), round(toff/dt) with ties to even. */
+typedef struct gp_fault {
+    int32_t scenario;            /* -1: every scenario (the reference's global events) */
+    int32_t bus;
+    double rfault;
+    int32_t on_step;
+    int32_t off_step;
+} gp_fault;
+
+#define GP_SOLVER_SCHUR_FP64   0   /* exact Newton, FP64 factors every iteration */
+#define GP_SOLVER_SCHUR_MIXED  1   /* FP32 factors reused across iterations + FP64 refinement */
+
+typedef struct gp_options {
+    double dt;
+    int32_t n_steps;             /* Int(round(tf/dt)) */
+    double newton_tol;           /* infinity-norm tolerance, reference default 1e-10 */
+    int32_t itermax;             /* reference batched default 30 */
+    int32_t solver;              /* GP_SOLVER_* */
+} gp_options;
+
+typedef struct gp_layout gp_layout;
+
+/* Library version and the message of the last failed call (thread-local). */
+int32_t gp_abi_version(void);
+int32_t gp_last_error(char *buf, int32_t len);
+
+/* Build the device-resident layout for M scenarios: uploads the problem,
+ * runs the host-once symbolic analysis of the reduced network matrix and
+ * allocates all work buffers.  z0 [M*n_sys], u0 [M*n_ctrl], p [M*n_par].
+ * Replaces GpuBatchedLayout(dp, ps, M). */
+int32_t gp_layout_create(const gp_problem *prob, int32_t M, const double *z0,
+                         const double *u0, const double *p, gp_layout **out);
+int32_t gp_layout_destroy(gp_layout *L);
+
+/* Sizes of the host-once symbolic analysis, for reporting:
+ * out[0] n_red, out[1] nnz of the reduced matrix, out[2] nnz(L+U) of its
+ * supernodal factor, out[3] supernodes, out[4] elimination-tree levels,
+ * out[5] factor flops per scenario (rounded), out[6] sum of w_k^2. */
+int32_t gp_layout_stats(const gp_layout *L, int64_t out[8]);
+
+/* Copy the current state of all scenarios in or out: z [M*n_sys]. */
+int32_t gp_set_state(gp_layout *L, const double *z);
+int32_t gp_get_state(const gp_layout *L, double *z);
+
+/* Integrate every scenario for opt->n_steps backward-Euler steps from the
+ * current state.  Replaces integrate_gpu_schur_cudss! / integrate_gpu_cudss!.
+ *   traj    [M][n_steps+1][n_sys] host output, or NULL
+ *   iters   [M][2*n_steps] Newton iterations: slot 2k the step solve of
+ *           step k+1, slot 2k+1 its event re-solve (0 if none); or NULL
+ *   status  [M] 0 converged everywhere, 1 some solve hit itermax,
+ *           2 non-finite values; or NULL
+ * On return the layout holds the final state. */
+int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults,
+                     const gp_fault *faults, double *traj, int32_t *iters,
+                     int32_t *status);
+
+/* Parity probe: the backward-Euler residual of every scenario at the
+ * current state against zold [M*n_sys] (src/dynamics.jl:366-391), with the
+ * faults whose flag in fault_on [n_faults] is 1 applied.  f [M*n_sys]. */
+int32_t gp_residual(gp_layout *L, const double *zold, double dt, int32_t n_faults,
+                    const gp_fault *faults, const uint8_t *fault_on, double *f);
+
+/* Time of the last gp_integrate call split by phase, milliseconds on the
+ * device clock: out[0] total, out[1] cluster kernels, out[2] network
+ * kernels, out[3] factorisation, out[4] triangular solves, out[5] Newton
+ * iterations summed over steps (max over scenarios), out[6] kernel launches. */
+int32_t gp_last_timing(const gp_layout *L, double out[8]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GRADPOWER_GB300_H */
