@@ -1,0 +1,962 @@
+// C-ABI entry points and host orchestration of the batched backward-Euler
+// Newton step (see include/gradpower_gb300.h).
+//
+// Host side of the reference's GpuBatchedLayout constructor
+// (ext/GradPowerCUDAExt/GradPowerCUDAExt.jl:466-945) and of the time loops of
+// integrate_gpu_schur_cudss! / integrate_gpu_cudss!
+// (ext/GradPowerCUDAExt/GradPowerCUDAExt.jl:2924-3080): everything is
+// uploaded once, the symbolic analysis of the reduced network matrix runs
+// once, and each Newton iteration is two captured CUDA graphs (evaluate,
+// solve) with one 4-byte readback of the number of scenarios still
+// iterating.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/gradpower_gb300.h"
+#include "gp_internal.h"
+#include "gp_symbolic.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct gp_error : std::runtime_error {
+    int code;
+    gp_error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] void fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    throw gp_error(code, buf);
+}
+
+void ck(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) fail(GP_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+struct DeviceArena {
+    std::vector<void *> ptrs;
+    template <class T>
+    T *alloc(size_t n) {
+        void *p = nullptr;
+        if (n == 0) n = 1;
+        cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+        if (e != cudaSuccess) fail(GP_E_NOMEM, "cudaMalloc of %zu bytes: %s", n * sizeof(T), cudaGetErrorString(e));
+        ptrs.push_back(p);
+        return (T *)p;
+    }
+    template <class T>
+    T *upload(const std::vector<T> &v) {
+        T *p = alloc<T>(v.size());
+        if (!v.empty()) ck(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "upload");
+        return p;
+    }
+    template <class T>
+    T *upload(const T *v, size_t n) {
+        T *p = alloc<T>(n);
+        if (n && v) ck(cudaMemcpy(p, v, n * sizeof(T), cudaMemcpyHostToDevice), "upload");
+        return p;
+    }
+    void release() {
+        for (void *p : ptrs) cudaFree(p);
+        ptrs.clear();
+    }
+};
+
+std::vector<int> vec(const int32_t *p, int n) {
+    std::vector<int> v(n > 0 ? n : 0);
+    if (n > 0 && p) std::copy(p, p + n, v.begin());
+    return v;
+}
+
+}  // namespace
+
+struct gp_layout {
+    int M = 0;
+    int n_sys = 0, n_da = 0, n_red = 0, n_bus = 0, n_ctrl = 0, n_par = 0;
+    gp::DevProblem P{};
+    gp::DevWork W{};
+    gp::DevSym S{};
+    gp::Symbolic sym;
+    DeviceArena arena;     // lifetime of the layout
+    DeviceArena call;      // lifetime of one gp_integrate call
+    cudaStream_t st = nullptr;
+    int *d_state_maps = nullptr;   // state_bus then red_of
+    int *h_flag = nullptr;         // pinned
+    double *h_dt = nullptr;        // pinned
+    std::vector<int> lvl_max_front;
+    int smem_limit = 0;
+    // faults of the current call
+    int n_fl = 0;
+    int *d_fl_on_step = nullptr, *d_fl_off_step = nullptr, *d_fl_scen = nullptr;
+    uint8_t *d_fl_on = nullptr;
+    std::vector<int> h_fl_on_step, h_fl_off_step, h_fl_scen;
+    // graphs
+    cudaGraphExec_t g_eval = nullptr, g_solve = nullptr;
+    double graph_tol = -1.0;
+    int graph_itermax = -1;
+    // timing of the last integrate call
+    double t_total_ms = 0.0, iters_total = 0.0, launches = 0.0;
+    int64_t sum_w2 = 0;
+};
+
+namespace {
+
+// Host-side plan of a layout: everything derived from the problem before
+// any device allocation (validated cluster tables, reduced-system maps,
+// symbolic analysis, front assembly lists).  Also used, without a GPU, by
+// gp_reduced_selftest.
+struct Plan {
+    int nb = 0, net = 0, n_sys = 0, n_red = 0, n_var = 0;
+    std::vector<int> ws, wsz, gen, gvt, gv, ext, ex, pss, cbus;
+    std::vector<int> state_bus, red_of, sg_red, sg_var;
+    std::vector<int> var_r, var_c;          // (row, col) of every variable entry of S
+    gp::Symbolic sym;
+    std::vector<int> acp, acpos, avp, avpos, avidx;
+    std::vector<double> acval;
+    std::vector<int> lvl_max_front;
+    int64_t sum_w2 = 0;
+};
+
+void check_in_cluster(int c, int w0, int w, int idx, const char *what) {
+    if (idx < w0 || idx >= w0 + w)
+        fail(GP_E_INVALID, "cluster %d: %s index %d outside the cluster states [%d, %d)", c, what, idx, w0, w0 + w);
+}
+
+void make_plan(const gp_problem *pr, Plan &pl) {
+    const int nb = pr->n_bus;
+    if (nb <= 0 || pr->n_diff < 0 || pr->n_alg < 0 || pr->n_ctrl < 0 || pr->n_par < 0)
+        fail(GP_E_INVALID, "bad problem sizes");
+    pl.nb = nb;
+    pl.net = pr->n_diff + pr->n_alg;
+    pl.n_sys = pl.net + 2 * nb;
+    const int net = pl.net;
+    for (int t = 0; t < GP_NTYPES; t++) {
+        const gp_device_table &T = pr->dev[t];
+        for (int k = 0; k < T.n; k++) {
+            if (T.online && !T.online[k]) fail(GP_E_INVALID, "offline devices are not supported (type %d, row %d)", t, k);
+            if (T.bus[k] < 0 || T.bus[k] >= nb) fail(GP_E_INVALID, "type %d row %d: bus out of range", t, k);
+            if (T.par_ptr[k] < 0 || T.par_ptr[k] >= pr->n_par) fail(GP_E_INVALID, "type %d row %d: par_ptr out of range", t, k);
+        }
+    }
+    for (int q = 0; q < pr->y_nnz; q++)
+        if (pr->y_colidx[q] < 0 || pr->y_colidx[q] >= nb) fail(GP_E_INVALID, "Ybus column out of range");
+    // ---- clusters: non-trivial ones go to the cluster kernel ----
+    pl.state_bus.assign(net, -2);
+    pl.red_of.assign(net, -1);
+    const gp_device_table &G = pr->dev[GP_GENROU];
+    for (int c = 0; c < pr->n_clusters; c++) {
+        const int w0 = pr->cl_w_start[c], w = pr->cl_w_size[c];
+        if (w0 < 0 || w < 0 || w0 + w > net) fail(GP_E_INVALID, "cluster %d outside the state vector", c);
+        if (pr->cl_gen[c] < 0) continue;   // static generator: reduced unknowns
+        if (w > 29) fail(GP_E_INVALID, "cluster %d has %d states; at most 29 are supported", c, w);
+        const int g = pr->cl_gen[c];
+        if (g >= G.n) fail(GP_E_INVALID, "cluster %d: generator index out of range", c);
+        if (G.bus[g] != pr->cl_bus[c]) fail(GP_E_INVALID, "cluster %d: bus differs from its machine's", c);
+        check_in_cluster(c, w0, w, G.diff_ptr[g], "GENROU diff");
+        check_in_cluster(c, w0, w, G.diff_ptr[g] + 5, "GENROU diff");
+        check_in_cluster(c, w0, w, G.alg_ptr[g], "GENROU alg");
+        check_in_cluster(c, w0, w, G.alg_ptr[g] + 3, "GENROU alg");
+        if (G.link0[g] >= 0) check_in_cluster(c, w0, w, G.link0[g], "GENROU p_m");
+        else if (G.ctrl_ptr[g] < 0 || G.ctrl_ptr[g] + 1 >= pr->n_ctrl) fail(GP_E_INVALID, "cluster %d: GENROU ctrl_ptr", c);
+        if (G.link1 && G.link1[g] >= 0) check_in_cluster(c, w0, w, G.link1[g], "GENROU e_fd");
+        else if (G.ctrl_ptr[g] < 0 || G.ctrl_ptr[g] >= pr->n_ctrl) fail(GP_E_INVALID, "cluster %d: GENROU ctrl_ptr", c);
+        const int gt = pr->cl_gov_type[c], gi = pr->cl_gov[c];
+        if (gt == GP_IEESGO || gt == GP_TGOV1) {
+            const gp_device_table &T = pr->dev[gt];
+            if (gi < 0 || gi >= T.n) fail(GP_E_INVALID, "cluster %d: governor index", c);
+            const int nd = gt == GP_IEESGO ? 5 : 2;
+            check_in_cluster(c, w0, w, T.diff_ptr[gi], "governor diff");
+            check_in_cluster(c, w0, w, T.diff_ptr[gi] + nd - 1, "governor diff");
+            check_in_cluster(c, w0, w, T.alg_ptr[gi], "governor alg");
+            if (T.link0[gi] >= 0) check_in_cluster(c, w0, w, T.link0[gi], "governor w");
+        } else if (gt != -1) fail(GP_E_INVALID, "cluster %d: bad governor type", c);
+        const int et = pr->cl_exc_type[c], ei = pr->cl_exc[c];
+        if (et == GP_SEXS || et == GP_ESDC1A) {
+            const gp_device_table &T = pr->dev[et];
+            if (ei < 0 || ei >= T.n) fail(GP_E_INVALID, "cluster %d: exciter index", c);
+            const int nd = et == GP_SEXS ? 2 : 3;
+            check_in_cluster(c, w0, w, T.diff_ptr[ei], "exciter diff");
+            check_in_cluster(c, w0, w, T.diff_ptr[ei] + nd - 1, "exciter diff");
+            if (T.link0[ei] >= 0) check_in_cluster(c, w0, w, T.link0[ei], "exciter v_s");
+            if (T.bus[ei] != pr->cl_bus[c]) fail(GP_E_INVALID, "cluster %d: exciter on another bus", c);
+        } else if (et != -1) fail(GP_E_INVALID, "cluster %d: bad exciter type", c);
+        const int si = pr->cl_pss[c];
+        if (si >= 0) {
+            const gp_device_table &T = pr->dev[GP_IEEEST];
+            if (si >= T.n) fail(GP_E_INVALID, "cluster %d: stabiliser index", c);
+            check_in_cluster(c, w0, w, T.diff_ptr[si], "stabiliser diff");
+            check_in_cluster(c, w0, w, T.diff_ptr[si] + 6, "stabiliser diff");
+            check_in_cluster(c, w0, w, T.alg_ptr[si], "stabiliser alg");
+            if (T.link0[si] >= 0) check_in_cluster(c, w0, w, T.link0[si], "stabiliser w");
+        }
+        pl.ws.push_back(w0);
+        pl.wsz.push_back(w);
+        pl.gen.push_back(g);
+        pl.gvt.push_back(gt);
+        pl.gv.push_back(gi);
+        pl.ext.push_back(et);
+        pl.ex.push_back(ei);
+        pl.pss.push_back(si);
+        pl.cbus.push_back(pr->cl_bus[c]);
+        for (int j = 0; j < w; j++) pl.state_bus[w0 + j] = pr->cl_bus[c];
+        pl.sum_w2 += (int64_t)w * w;
+    }
+    // ---- reduced system: bus voltages then static-generator states ----
+    const gp_device_table &SG = pr->dev[GP_STATIC_GEN];
+    pl.sg_red.assign(SG.n, -1);
+    pl.sg_var.assign(SG.n, 0);
+    int n_red = 2 * nb, n_var = 4 * nb;
+    pl.var_r.clear();
+    pl.var_c.clear();
+    for (int b = 0; b < nb; b++)
+        for (int q = 0; q < 4; q++) {
+            pl.var_r.push_back(2 * b + q / 2);
+            pl.var_c.push_back(2 * b + q % 2);
+        }
+    for (int k = 0; k < SG.n; k++) {
+        const int bt = SG.link0[k];
+        const int na = bt == 2 ? 1 : (bt == 3 ? 2 : 0);
+        if (na) {
+            pl.sg_red[k] = n_red;
+            for (int j = 0; j < na; j++) {
+                const int zi = SG.alg_ptr[k] + j;
+                if (zi < 0 || zi >= net) fail(GP_E_INVALID, "static generator %d state outside the state vector", k);
+                pl.state_bus[zi] = -1;
+                pl.red_of[zi] = n_red + j;
+            }
+        }
+        pl.sg_var[k] = n_var;
+        const int vr = 2 * SG.bus[k], vi = vr + 1, a0 = n_red;
+        if (bt == 2) {
+            const int rr[4] = {a0, a0, vr, vi}, cc[4] = {vr, vi, a0, a0};
+            for (int q = 0; q < 4; q++) { pl.var_r.push_back(rr[q]); pl.var_c.push_back(cc[q]); }
+            n_var += 4;
+        } else if (bt == 3) {
+            const int rr[6] = {a0, a0 + 1, vr, vi, vr, vi}, cc[6] = {vr, vi, a0, a0, a0 + 1, a0 + 1};
+            for (int q = 0; q < 6; q++) { pl.var_r.push_back(rr[q]); pl.var_c.push_back(cc[q]); }
+            n_var += 6;
+        }
+        n_red += na;
+    }
+    for (int i = 0; i < net; i++)
+        if (pl.state_bus[i] == -2) fail(GP_E_INVALID, "state %d belongs to no cluster", i);
+    pl.n_red = n_red;
+    pl.n_var = n_var;
+
+    // ---- pattern of S and symbolic analysis ----
+    struct Ent { int r, c; int kind; double val; int idx; };   // kind 0 const, 1 var
+    std::vector<Ent> ents;
+    for (int v = 0; v < n_var; v++) ents.push_back({pl.var_r[v], pl.var_c[v], 1, 0.0, v});
+    for (int b = 0; b < nb; b++) {
+        for (int q = pr->y_rowptr[b]; q < pr->y_rowptr[b + 1]; q++) {
+            const int j = pr->y_colidx[q];
+            if (j == b) continue;
+            const double g = pr->y_re[q], bb = pr->y_im[q];
+            ents.push_back({2 * b, 2 * j, 0, -g, 0});
+            ents.push_back({2 * b, 2 * j + 1, 0, bb, 0});
+            ents.push_back({2 * b + 1, 2 * j, 0, -bb, 0});
+            ents.push_back({2 * b + 1, 2 * j + 1, 0, -g, 0});
+        }
+        for (int q = pr->adj_rowptr[b]; q < pr->adj_rowptr[b + 1]; q++) {
+            const int j = pr->adj_colidx[q];
+            if (j < 0 || j >= nb) fail(GP_E_INVALID, "adjacency out of range");
+            for (int t = 0; t < 4; t++) ents.push_back({2 * b + t / 2, 2 * j + t % 2, 0, 0.0, 0});
+        }
+    }
+    for (int k = 0; k < SG.n; k++) {
+        const int a0 = pl.sg_red[k];
+        if (a0 < 0) continue;
+        const int na = SG.link0[k] == 2 ? 1 : 2;
+        for (int i = 0; i < na; i++)
+            for (int j = 0; j < na; j++) ents.push_back({a0 + i, a0 + j, 0, 0.0, 0});
+    }
+    std::vector<std::vector<int>> adjr(n_red);
+    for (const Ent &e : ents) {
+        adjr[e.r].push_back(e.c);
+        adjr[e.c].push_back(e.r);
+    }
+    std::vector<int> rp(n_red + 1, 0), ci;
+    for (int i = 0; i < n_red; i++) {
+        std::sort(adjr[i].begin(), adjr[i].end());
+        adjr[i].erase(std::unique(adjr[i].begin(), adjr[i].end()), adjr[i].end());
+        rp[i + 1] = rp[i] + (int)adjr[i].size();
+        ci.insert(ci.end(), adjr[i].begin(), adjr[i].end());
+    }
+    std::vector<int> group(n_red);
+    for (int i = 0; i < 2 * nb; i++) group[i] = i / 2;
+    for (int k = 0; k < SG.n; k++) {
+        const int a0 = pl.sg_red[k];
+        if (a0 < 0) continue;
+        const int na = SG.link0[k] == 2 ? 1 : 2;
+        for (int j = 0; j < na; j++) group[a0 + j] = SG.bus[k];
+    }
+    gp::Symbolic &sym = pl.sym;
+    gp::analyse(n_red, rp, ci, group, nb, sym);
+    // ---- assembly lists ----
+    auto fpos = [&](int s, int k) -> int {
+        const int st0 = sym.sup_start[s], en = sym.sup_start[s + 1];
+        if (k >= st0 && k < en) return k - st0;
+        auto b = sym.rows.begin() + sym.row_ptr[s], e = sym.rows.begin() + sym.row_ptr[s + 1];
+        auto it = std::lower_bound(b, e, k);
+        if (it == e || *it != k) fail(GP_E_INVALID, "entry outside the symbolic structure");
+        return (en - st0) + (int)(it - b);
+    };
+    std::vector<std::vector<std::pair<int, double>>> ac(sym.nsup);
+    std::vector<std::vector<std::pair<int, int>>> av(sym.nsup);
+    for (const Ent &e : ents) {
+        if (e.kind == 0 && e.val == 0.0) continue;
+        const int pi = sym.iperm[e.r], pj = sym.iperm[e.c];
+        const int s = sym.sup_of[std::min(pi, pj)];
+        const int m = sym.front_m(s);
+        const int lin = fpos(s, pi) + fpos(s, pj) * m;
+        if (lin < 0 || lin >= m * m) fail(GP_E_INVALID, "assembly position outside its front");
+        if (e.kind == 0) ac[s].push_back({lin, e.val});
+        else av[s].push_back({lin, e.idx});
+    }
+    // merge duplicate constant positions (parallel branches share a Ybus entry)
+    pl.acp.assign(sym.nsup + 1, 0);
+    pl.avp.assign(sym.nsup + 1, 0);
+    for (int s = 0; s < sym.nsup; s++) {
+        std::sort(ac[s].begin(), ac[s].end());
+        for (size_t q = 0; q < ac[s].size(); q++) {
+            if (q > 0 && ac[s][q].first == ac[s][q - 1].first) pl.acval.back() += ac[s][q].second;
+            else { pl.acpos.push_back(ac[s][q].first); pl.acval.push_back(ac[s][q].second); }
+        }
+        pl.acp[s + 1] = (int)pl.acpos.size();
+        std::sort(av[s].begin(), av[s].end());
+        for (size_t q = 0; q < av[s].size(); q++) {
+            if (q > 0 && av[s][q].first == av[s][q - 1].first) fail(GP_E_INVALID, "duplicate variable entry of S");
+            pl.avpos.push_back(av[s][q].first);
+            pl.avidx.push_back(av[s][q].second);
+        }
+        pl.avp[s + 1] = (int)pl.avpos.size();
+    }
+    pl.lvl_max_front.assign(sym.nlevels, 0);
+    for (int l = 0; l < sym.nlevels; l++)
+        for (int q = sym.level_ptr[l]; q < sym.level_ptr[l + 1]; q++)
+            pl.lvl_max_front[l] = std::max(pl.lvl_max_front[l], sym.front_m(sym.level_sups[q]));
+}
+
+// Host emulation of the device factorisation and solves, same data layout
+// and the same operation order as factor_kernel / fwd_kernel / bwd_kernel.
+// x: right-hand side in permuted order on entry, solution on exit.
+int host_factor_solve(const Plan &pl, const std::vector<double> &svar, std::vector<double> &x) {
+    const gp::Symbolic &S = pl.sym;
+    std::vector<double> fronts(S.front_off[S.nsup]), uvec(std::max<int64_t>(1, S.uvec_off[S.nsup]));
+    std::vector<int> ipiv(S.n);
+    int zero_pivots = 0;
+    for (int l = 0; l < S.nlevels; l++)
+        for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+            const int s = S.level_sups[q];
+            const int ns = S.front_n(s), mm = S.front_m(s), start = S.sup_start[s];
+            double *F = fronts.data() + S.front_off[s];
+            std::fill(F, F + (size_t)mm * mm, 0.0);
+            for (int e = pl.acp[s]; e < pl.acp[s + 1]; e++) F[pl.acpos[e]] += pl.acval[e];
+            for (int e = pl.avp[s]; e < pl.avp[s + 1]; e++) F[pl.avpos[e]] += svar[pl.avidx[e]];
+            for (int cq = S.child_ptr[s]; cq < S.child_ptr[s + 1]; cq++) {
+                const int c = S.children[cq];
+                const int nc = S.front_n(c), rc = S.front_r(c), mc = S.front_m(c);
+                const int *rel = S.relmap.data() + S.relmap_ptr[c];
+                const double *Fc = fronts.data() + S.front_off[c];
+                for (int b = 0; b < rc; b++)
+                    for (int a = 0; a < rc; a++) F[rel[a] + rel[b] * mm] += Fc[(nc + a) + (size_t)(nc + b) * mc];
+            }
+            for (int k = 0; k < ns; k++) {
+                double best = -1.0;
+                int bi = k;
+                for (int i = k; i < ns; i++) {
+                    const double v = std::fabs(F[i + k * mm]);
+                    if (v > best) { best = v; bi = i; }
+                }
+                if (best == 0.0) zero_pivots++;
+                ipiv[start + k] = bi;
+                if (bi != k)
+                    for (int j = 0; j < mm; j++) std::swap(F[k + j * mm], F[bi + j * mm]);
+                const double inv = 1.0 / F[k + k * mm];
+                for (int i = k + 1; i < mm; i++) F[i + k * mm] *= inv;
+                for (int j = k + 1; j < mm; j++)
+                    for (int i = k + 1; i < mm; i++) F[i + j * mm] -= F[i + k * mm] * F[k + j * mm];
+            }
+        }
+    for (int l = 0; l < S.nlevels; l++)
+        for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+            const int s = S.level_sups[q];
+            const int ns = S.front_n(s), r = S.front_r(s), mm = S.front_m(s), start = S.sup_start[s];
+            std::vector<double> t(x.begin() + start, x.begin() + start + ns), u(r, 0.0);
+            for (int cq = S.child_ptr[s]; cq < S.child_ptr[s + 1]; cq++) {
+                const int c = S.children[cq];
+                const int *rel = S.relmap.data() + S.relmap_ptr[c];
+                const double *uc = uvec.data() + S.uvec_off[c];
+                for (int a = 0; a < S.front_r(c); a++) {
+                    if (rel[a] < ns) t[rel[a]] += uc[a];
+                    else u[rel[a] - ns] += uc[a];
+                }
+            }
+            const double *F = fronts.data() + S.front_off[s];
+            for (int k = 0; k < ns; k++)
+                if (ipiv[start + k] != k) std::swap(t[k], t[ipiv[start + k]]);
+            for (int k = 0; k < ns; k++)
+                for (int i = k + 1; i < ns; i++) t[i] -= F[i + k * mm] * t[k];
+            for (int i = 0; i < r; i++) {
+                double acc = 0.0;
+                for (int k = 0; k < ns; k++) acc += F[(ns + i) + (size_t)k * mm] * t[k];
+                u[i] -= acc;
+            }
+            std::copy(t.begin(), t.end(), x.begin() + start);
+            std::copy(u.begin(), u.end(), uvec.begin() + S.uvec_off[s]);
+        }
+    for (int l = S.nlevels - 1; l >= 0; l--)
+        for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
+            const int s = S.level_sups[q];
+            const int ns = S.front_n(s), r = S.front_r(s), mm = S.front_m(s), start = S.sup_start[s];
+            const double *F = fronts.data() + S.front_off[s];
+            const int *rows = S.rows.data() + S.row_ptr[s];
+            std::vector<double> t(ns);
+            for (int i = 0; i < ns; i++) {
+                double acc = 0.0;
+                for (int a = 0; a < r; a++) acc += F[i + (size_t)(ns + a) * mm] * x[rows[a]];
+                t[i] = x[start + i] - acc;
+            }
+            for (int k = ns - 1; k >= 0; k--) {
+                t[k] /= F[k + k * mm];
+                for (int i = 0; i < k; i++) t[i] -= F[i + k * mm] * t[k];
+            }
+            std::copy(t.begin(), t.end(), x.begin() + start);
+        }
+    return zero_pivots;
+}
+
+void build_problem(gp_layout *L, const gp_problem *pr) {
+    using namespace gp;
+    Plan &pl = *new Plan();
+    std::unique_ptr<Plan> own(&pl);
+    make_plan(pr, pl);
+    DeviceArena &A = L->arena;
+    DevProblem &P = L->P;
+    const int nb = pl.nb;
+    P.n_bus = nb;
+    P.n_diff = pr->n_diff;
+    P.n_alg = pr->n_alg;
+    P.n_ctrl = pr->n_ctrl;
+    P.n_par = pr->n_par;
+    P.net = pl.net;
+    P.n_sys = pl.n_sys;
+    P.M = L->M;
+    L->n_sys = P.n_sys;
+    L->n_da = P.net;
+    L->n_bus = nb;
+    L->n_ctrl = pr->n_ctrl;
+    L->n_par = pr->n_par;
+    P.y_rowptr = A.upload(pr->y_rowptr, nb + 1);
+    P.y_colidx = A.upload(pr->y_colidx, pr->y_nnz);
+    P.y_re = A.upload(pr->y_re, pr->y_nnz);
+    P.y_im = A.upload(pr->y_im, pr->y_nnz);
+    for (int t = 0; t < GP_NTYPES; t++) {
+        const gp_device_table &T = pr->dev[t];
+        DTab &D = P.dev[t];
+        D.n = T.n;
+        auto up = [&](const int32_t *a) -> const int * {
+            if (T.n == 0) return A.alloc<int>(1);
+            if (!a) {
+                std::vector<int> m1(T.n, -1);
+                return A.upload(m1);
+            }
+            return A.upload(a, T.n);
+        };
+        D.bus = up(T.bus);
+        D.diff_ptr = up(T.diff_ptr);
+        D.alg_ptr = up(T.alg_ptr);
+        D.ctrl_ptr = up(T.ctrl_ptr);
+        D.par_ptr = up(T.par_ptr);
+        D.link0 = up(T.link0);
+        D.link1 = up(T.link1);
+    }
+    P.is_diff = A.upload(pr->is_diff, P.net);
+    L->sum_w2 = pl.sum_w2;
+    P.n_cl = (int)pl.ws.size();
+    P.cl_w_start = A.upload(pl.ws);
+    P.cl_w_size = A.upload(pl.wsz);
+    P.cl_gen = A.upload(pl.gen);
+    P.cl_gov_type = A.upload(pl.gvt);
+    P.cl_gov = A.upload(pl.gv);
+    P.cl_exc_type = A.upload(pl.ext);
+    P.cl_exc = A.upload(pl.ex);
+    P.cl_pss = A.upload(pl.pss);
+    P.n_red = pl.n_red;
+    P.n_var = pl.n_var;
+    L->n_red = pl.n_red;
+    P.sg_red = A.upload(pl.sg_red);
+    P.sg_var = A.upload(pl.sg_var);
+    {
+        std::vector<int> maps(2 * P.net);
+        std::copy(pl.state_bus.begin(), pl.state_bus.end(), maps.begin());
+        std::copy(pl.red_of.begin(), pl.red_of.end(), maps.begin() + P.net);
+        L->d_state_maps = A.upload(maps);
+    }
+    // ---- per-bus device lists (deterministic summation order) ----
+    auto bus_csr = [&](const std::vector<int> &bus_of, const int **ptr, const int **lst) {
+        std::vector<int> cnt(nb + 1, 0);
+        for (int b : bus_of) cnt[b + 1]++;
+        for (int b = 0; b < nb; b++) cnt[b + 1] += cnt[b];
+        std::vector<int> l(bus_of.size()), fill(cnt.begin(), cnt.end() - 1);
+        for (size_t k = 0; k < bus_of.size(); k++) l[fill[bus_of[k]]++] = (int)k;
+        *ptr = A.upload(cnt);
+        *lst = A.upload(l);
+    };
+    bus_csr(pl.cbus, &P.bus_cl_ptr, &P.bus_cl);
+    bus_csr(vec(pr->dev[GP_ZIPLOAD].bus, pr->dev[GP_ZIPLOAD].n), &P.bus_zl_ptr, &P.bus_zl);
+    bus_csr(vec(pr->dev[GP_STATIC_GEN].bus, pr->dev[GP_STATIC_GEN].n), &P.bus_sg_ptr, &P.bus_sg);
+    const gp::Symbolic &sym = pl.sym;
+    P.iperm = A.upload(sym.iperm);
+    DevSym &S = L->S;
+    S.n = pl.n_red;
+    S.nsup = sym.nsup;
+    S.nlevels = sym.nlevels;
+    S.sup_start = A.upload(sym.sup_start);
+    S.row_ptr = A.upload(sym.row_ptr);
+    S.rows = A.upload(sym.rows);
+    S.child_ptr = A.upload(sym.child_ptr);
+    S.children = A.upload(sym.children);
+    S.relmap_ptr = A.upload(sym.relmap_ptr);
+    S.relmap = A.upload(sym.relmap);
+    S.front_off = A.upload(sym.front_off);
+    S.uvec_off = A.upload(sym.uvec_off);
+    S.level_sups = A.upload(sym.level_sups);
+    S.front_total = sym.front_off[sym.nsup];
+    S.uvec_total = sym.uvec_off[sym.nsup];
+    S.asmc_ptr = A.upload(pl.acp);
+    S.asmc_pos = A.upload(pl.acpos);
+    S.asmc_val = A.upload(pl.acval);
+    S.asmv_ptr = A.upload(pl.avp);
+    S.asmv_pos = A.upload(pl.avpos);
+    S.asmv_idx = A.upload(pl.avidx);
+    L->lvl_max_front = pl.lvl_max_front;
+    L->sym = pl.sym;
+    L->smem_limit = gp::factor_smem_limit();
+    if (L->smem_limit < 0) fail(GP_E_CUDA, "could not configure the factorisation kernel's shared memory");
+    if ((size_t)sym.max_front * sym.max_front * sizeof(double) > (size_t)L->smem_limit)
+        fail(GP_E_INVALID, "largest front (%d) exceeds shared memory (%d bytes)", sym.max_front, L->smem_limit);
+}
+
+void build_work(gp_layout *L, const double *z0, const double *u0, const double *p) {
+    using namespace gp;
+    DeviceArena &A = L->arena;
+    DevProblem &P = L->P;
+    DevWork &W = L->W;
+    const size_t M = L->M;
+    W.z = A.upload(z0, M * P.n_sys);
+    W.zold = A.alloc<double>(M * P.n_sys);
+    W.u0 = A.upload(u0, M * std::max(1, P.n_ctrl));
+    W.p = A.upload(p, M * std::max(1, P.n_par));
+    W.yx = A.alloc<double>(M * 3 * std::max(1, P.net));
+    W.clout = A.alloc<double>(M * 8 * std::max(1, P.n_cl));
+    W.svar = A.alloc<double>(M * P.n_var);
+    W.xperm = A.alloc<double>(M * P.n_red);
+    W.f = A.alloc<double>(M * P.n_sys);
+    W.norm = A.alloc<unsigned long long>(M);
+    W.active = A.alloc<uint8_t>(M);
+    W.iters = A.alloc<int>(M);
+    W.status = A.alloc<int>(M);
+    W.flag = A.alloc<int>(1);
+    W.dt = A.alloc<double>(1);
+    DevSym &S = L->S;
+    S.fronts = A.alloc<double>(M * S.front_total);
+    S.uvec = A.alloc<double>(M * std::max<int64_t>(1, S.uvec_total));
+    S.ipiv = A.alloc<int>(M * S.n);
+    ck(cudaMemset(W.status, 0, M * sizeof(int)), "memset");
+    ck(cudaMallocHost(&L->h_flag, sizeof(int)), "cudaMallocHost");
+    ck(cudaMallocHost(&L->h_dt, sizeof(double)), "cudaMallocHost");
+    ck(cudaStreamCreateWithFlags(&L->st, cudaStreamNonBlocking), "stream");
+}
+
+void set_faults(gp_layout *L, int n_faults, const gp_fault *faults) {
+    using namespace gp;
+    L->call.release();
+    const int M = L->M;
+    std::vector<std::vector<int>> per(M);
+    for (int e = 0; e < n_faults; e++) {
+        const gp_fault &f = faults[e];
+        if (f.bus < 0 || f.bus >= L->n_bus) fail(GP_E_INVALID, "fault %d: bus %d out of range", e, f.bus);
+        if (!(f.rfault > 0.0)) fail(GP_E_INVALID, "fault %d: rfault must be positive", e);
+        if (f.scenario >= M) fail(GP_E_INVALID, "fault %d: scenario %d out of range", e, f.scenario);
+        if (f.scenario < 0)
+            for (int m = 0; m < M; m++) per[m].push_back(e);
+        else
+            per[f.scenario].push_back(e);
+    }
+    std::vector<int> ptr(M + 1, 0), bus, on, off, scen;
+    std::vector<double> yf;
+    for (int m = 0; m < M; m++) {
+        for (int e : per[m]) {
+            bus.push_back(faults[e].bus);
+            yf.push_back(1.0 / faults[e].rfault);
+            on.push_back(faults[e].on_step);
+            off.push_back(faults[e].off_step);
+            scen.push_back(m);
+        }
+        ptr[m + 1] = (int)bus.size();
+    }
+    L->n_fl = (int)bus.size();
+    L->P.fl_ptr = L->call.upload(ptr);
+    L->P.fl_bus = L->call.upload(bus);
+    L->P.fl_yf = L->call.upload(yf);
+    L->d_fl_on = L->call.alloc<uint8_t>(std::max(1, L->n_fl));
+    ck(cudaMemset(L->d_fl_on, 0, std::max(1, L->n_fl)), "memset");
+    L->P.fl_on = L->d_fl_on;
+    L->d_fl_on_step = L->call.upload(on);
+    L->d_fl_off_step = L->call.upload(off);
+    L->d_fl_scen = L->call.upload(scen);
+    L->h_fl_on_step = on;
+    L->h_fl_off_step = off;
+    L->h_fl_scen = scen;
+    // graphs capture the fault pointers: rebuild them
+    if (L->g_eval) { cudaGraphExecDestroy(L->g_eval); L->g_eval = nullptr; }
+    if (L->g_solve) { cudaGraphExecDestroy(L->g_solve); L->g_solve = nullptr; }
+}
+
+void enqueue_solve(gp_layout *L) {
+    const gp::Symbolic &sym = L->sym;
+    for (int l = 0; l < sym.nlevels; l++)
+        gp::launch_factor_level(L->P, L->W, L->S, sym.level_ptr[l], sym.level_ptr[l + 1] - sym.level_ptr[l],
+                                L->lvl_max_front[l], L->st);
+    for (int l = 0; l < sym.nlevels; l++)
+        gp::launch_fwd_level(L->P, L->W, L->S, sym.level_ptr[l], sym.level_ptr[l + 1] - sym.level_ptr[l],
+                             L->lvl_max_front[l], L->st);
+    for (int l = sym.nlevels - 1; l >= 0; l--)
+        gp::launch_bwd_level(L->P, L->W, L->S, sym.level_ptr[l], sym.level_ptr[l + 1] - sym.level_ptr[l],
+                             L->lvl_max_front[l], L->st);
+    gp::launch_update(L->P, L->W, L->S, L->d_state_maps, L->st);
+}
+
+void enqueue_eval(gp_layout *L, double tol, int itermax) {
+    gp::launch_reset_norm(L->P, L->W, L->st);
+    gp::launch_cluster(L->P, L->W, 0, L->st);
+    gp::launch_network(L->P, L->W, 0, L->st);
+    gp::launch_check(L->P, L->W, tol, itermax, L->st);
+    ck(cudaMemcpyAsync(L->h_flag, L->W.flag, sizeof(int), cudaMemcpyDeviceToHost, L->st), "flag copy");
+}
+
+cudaGraphExec_t capture(gp_layout *L, bool eval, double tol, int itermax) {
+    cudaGraph_t g;
+    ck(cudaStreamBeginCapture(L->st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    if (eval) enqueue_eval(L, tol, itermax);
+    else enqueue_solve(L);
+    ck(cudaStreamEndCapture(L->st, &g), "end capture");
+    cudaGraphExec_t ex;
+    ck(cudaGraphInstantiate(&ex, g, 0), "graph instantiate");
+    cudaGraphDestroy(g);
+    return ex;
+}
+
+void ensure_graphs(gp_layout *L, double tol, int itermax) {
+    if (L->g_eval && (L->graph_tol != tol || L->graph_itermax != itermax)) {
+        cudaGraphExecDestroy(L->g_eval);
+        L->g_eval = nullptr;
+    }
+    if (!L->g_eval) {
+        L->g_eval = capture(L, true, tol, itermax);
+        L->graph_tol = tol;
+        L->graph_itermax = itermax;
+    }
+    if (!L->g_solve) L->g_solve = capture(L, false, tol, itermax);
+}
+
+// One Newton solve for the scenarios marked active; returns after every
+// scenario converged, diverged or used itermax updates.
+void newton(gp_layout *L, double dt, double tol, int itermax) {
+    *L->h_dt = dt;
+    ck(cudaMemcpyAsync(L->W.dt, L->h_dt, sizeof(double), cudaMemcpyHostToDevice, L->st), "dt");
+    ck(cudaMemsetAsync(L->W.iters, 0, L->M * sizeof(int), L->st), "memset");
+    for (int guard = 0; guard <= itermax + 1; guard++) {
+        ck(cudaGraphLaunch(L->g_eval, L->st), "graph launch");
+        ck(cudaStreamSynchronize(L->st), "newton sync");
+        L->launches += 4;
+        if (*L->h_flag == 0) return;
+        ck(cudaGraphLaunch(L->g_solve, L->st), "graph launch");
+        L->launches += 3 * L->sym.nlevels + 1;
+    }
+    fail(GP_E_NUMERIC, "Newton loop did not terminate");
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// exported API
+// ---------------------------------------------------------------------------
+
+#define API_BEGIN try {
+#define API_END                                  \
+    }                                            \
+    catch (const gp_error &e) {                  \
+        g_last_error = e.what();                 \
+        return e.code;                           \
+    }                                            \
+    catch (const std::exception &e) {            \
+        g_last_error = e.what();                 \
+        return GP_E_INVALID;                     \
+    }                                            \
+    return GP_OK;
+
+extern "C" {
+
+int32_t gp_abi_version(void) { return GP_ABI_VERSION; }
+
+int32_t gp_last_error(char *buf, int32_t len) {
+    if (!buf || len <= 0) return (int32_t)g_last_error.size();
+    snprintf(buf, (size_t)len, "%s", g_last_error.c_str());
+    return (int32_t)g_last_error.size();
+}
+
+int32_t gp_layout_create(const gp_problem *prob, int32_t M, const double *z0, const double *u0, const double *p,
+                         gp_layout **out) {
+    gp_layout *L = nullptr;
+    API_BEGIN
+    if (!prob || !out || !z0 || M <= 0) fail(GP_E_INVALID, "gp_layout_create: null argument or M <= 0");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) fail(GP_E_CUDA, "no CUDA device available");
+    L = new gp_layout();
+    L->M = M;
+    build_problem(L, prob);
+    build_work(L, z0, u0, p);
+    ck(cudaDeviceSynchronize(), "layout create");
+    *out = L;
+    L = nullptr;
+    }
+    catch (const gp_error &e) {
+        g_last_error = e.what();
+        if (L) { L->arena.release(); delete L; }
+        return e.code;
+    }
+    catch (const std::exception &e) {
+        g_last_error = e.what();
+        if (L) { L->arena.release(); delete L; }
+        return GP_E_INVALID;
+    }
+    return GP_OK;
+}
+
+int32_t gp_layout_destroy(gp_layout *L) {
+    API_BEGIN
+    if (!L) return GP_OK;
+    if (L->g_eval) cudaGraphExecDestroy(L->g_eval);
+    if (L->g_solve) cudaGraphExecDestroy(L->g_solve);
+    if (L->st) cudaStreamSynchronize(L->st);
+    L->call.release();
+    L->arena.release();
+    if (L->h_flag) cudaFreeHost(L->h_flag);
+    if (L->h_dt) cudaFreeHost(L->h_dt);
+    if (L->st) cudaStreamDestroy(L->st);
+    delete L;
+    API_END
+}
+
+int32_t gp_layout_stats(const gp_layout *L, int64_t out[8]) {
+    API_BEGIN
+    if (!L || !out) fail(GP_E_INVALID, "null argument");
+    const gp::Symbolic &s = L->sym;
+    int64_t nnz_s = 0;
+    out[0] = L->n_red;
+    out[1] = nnz_s;
+    out[2] = s.nnz_lu;
+    out[3] = s.nsup;
+    out[4] = s.nlevels;
+    out[5] = (int64_t)std::llround(s.flops);
+    out[6] = L->sum_w2;
+    out[7] = s.max_front;
+    API_END
+}
+
+int32_t gp_set_state(gp_layout *L, const double *z) {
+    API_BEGIN
+    if (!L || !z) fail(GP_E_INVALID, "null argument");
+    ck(cudaMemcpy(L->W.z, z, (size_t)L->M * L->n_sys * sizeof(double), cudaMemcpyHostToDevice), "set state");
+    API_END
+}
+
+int32_t gp_get_state(const gp_layout *L, double *z) {
+    API_BEGIN
+    if (!L || !z) fail(GP_E_INVALID, "null argument");
+    ck(cudaMemcpy(z, L->W.z, (size_t)L->M * L->n_sys * sizeof(double), cudaMemcpyDeviceToHost), "get state");
+    API_END
+}
+
+int32_t gp_residual(gp_layout *L, const double *zold, double dt, int32_t n_faults, const gp_fault *faults,
+                    const uint8_t *fault_on, double *f) {
+    API_BEGIN
+    if (!L || !zold || !f) fail(GP_E_INVALID, "null argument");
+    set_faults(L, n_faults, faults);
+    // expanded fault status from the per-input flags
+    {
+        std::vector<uint8_t> on;
+        for (int m = 0; m < L->M; m++)
+            for (int e = 0; e < n_faults; e++)
+                if (faults[e].scenario < 0 || faults[e].scenario == m) on.push_back(fault_on ? fault_on[e] : 0);
+        if (!on.empty()) ck(cudaMemcpy(L->d_fl_on, on.data(), on.size(), cudaMemcpyHostToDevice), "fault flags");
+    }
+    const size_t n = (size_t)L->M * L->n_sys;
+    ck(cudaMemcpy(L->W.zold, zold, n * sizeof(double), cudaMemcpyHostToDevice), "zold");
+    *L->h_dt = dt;
+    ck(cudaMemcpy(L->W.dt, L->h_dt, sizeof(double), cudaMemcpyHostToDevice), "dt");
+    ck(cudaMemset(L->W.active, 1, L->M), "memset");
+    gp::launch_reset_norm(L->P, L->W, L->st);
+    gp::launch_cluster(L->P, L->W, 1, L->st);
+    gp::launch_network(L->P, L->W, 1, L->st);
+    ck(cudaGetLastError(), "residual launch");
+    ck(cudaStreamSynchronize(L->st), "residual");
+    ck(cudaMemcpy(f, L->W.f, n * sizeof(double), cudaMemcpyDeviceToHost), "residual copy");
+    API_END
+}
+
+int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, const gp_fault *faults, double *traj,
+                     int32_t *iters, int32_t *status) {
+    API_BEGIN
+    if (!L || !opt) fail(GP_E_INVALID, "null argument");
+    if (opt->n_steps < 0 || !(opt->dt > 0.0) || opt->itermax <= 0) fail(GP_E_INVALID, "bad options");
+    if (opt->solver != GP_SOLVER_SCHUR_FP64) fail(GP_E_INVALID, "solver %d is not available", opt->solver);
+    const int M = L->M, ns = opt->n_steps, nsys = L->n_sys;
+    set_faults(L, n_faults, faults);
+    ensure_graphs(L, opt->newton_tol, opt->itermax);
+    ck(cudaMemsetAsync(L->W.status, 0, M * sizeof(int), L->st), "memset");
+    // event steps
+    std::map<int, int> ev_steps;
+    for (int e = 0; e < L->n_fl; e++) {
+        ev_steps[L->h_fl_on_step[e]] = 1;
+        ev_steps[L->h_fl_off_step[e]] = 1;
+    }
+    double *d_traj = nullptr;
+    int *d_iters = L->call.alloc<int>((size_t)2 * std::max(ns, 1) * M);
+    ck(cudaMemsetAsync(d_iters, 0, (size_t)2 * std::max(ns, 1) * M * sizeof(int), L->st), "memset");
+    if (traj) {
+        d_traj = L->call.alloc<double>((size_t)M * (ns + 1) * nsys);
+        ck(cudaMemcpy2DAsync(d_traj, (size_t)(ns + 1) * nsys * sizeof(double), L->W.z, nsys * sizeof(double),
+                             nsys * sizeof(double), M, cudaMemcpyDeviceToDevice, L->st),
+           "snapshot");
+    }
+    cudaEvent_t e0, e1;
+    ck(cudaEventCreate(&e0), "event");
+    ck(cudaEventCreate(&e1), "event");
+    ck(cudaEventRecord(e0, L->st), "event");
+    L->launches = 0;
+    for (int k = 1; k <= ns; k++) {
+        ck(cudaMemcpyAsync(L->W.zold, L->W.z, (size_t)M * nsys * sizeof(double), cudaMemcpyDeviceToDevice, L->st),
+           "zold");
+        ck(cudaMemsetAsync(L->W.active, 1, M, L->st), "memset");
+        newton(L, opt->dt, opt->newton_tol, opt->itermax);
+        ck(cudaMemcpyAsync(d_iters + (size_t)(2 * (k - 1)) * M, L->W.iters, M * sizeof(int),
+                           cudaMemcpyDeviceToDevice, L->st),
+           "iters");
+        if (d_traj)
+            ck(cudaMemcpy2DAsync(d_traj + (size_t)k * nsys, (size_t)(ns + 1) * nsys * sizeof(double), L->W.z,
+                                 nsys * sizeof(double), nsys * sizeof(double), M, cudaMemcpyDeviceToDevice, L->st),
+               "snapshot");
+        if (ev_steps.count(k)) {
+            ck(cudaMemsetAsync(L->W.active, 0, M, L->st), "memset");
+            gp::launch_events(L->P, L->W, L->d_fl_on_step, L->d_fl_off_step, L->d_fl_scen, L->d_fl_on, L->n_fl, k,
+                              L->st);
+            ck(cudaMemcpyAsync(L->W.zold, L->W.z, (size_t)M * nsys * sizeof(double), cudaMemcpyDeviceToDevice,
+                               L->st),
+               "zold");
+            newton(L, 0.0, opt->newton_tol, opt->itermax);
+            ck(cudaMemcpyAsync(d_iters + (size_t)(2 * (k - 1) + 1) * M, L->W.iters, M * sizeof(int),
+                               cudaMemcpyDeviceToDevice, L->st),
+               "iters");
+        }
+    }
+    ck(cudaEventRecord(e1, L->st), "event");
+    ck(cudaStreamSynchronize(L->st), "integrate");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    L->t_total_ms = ms;
+    if (traj)
+        ck(cudaMemcpy(traj, d_traj, (size_t)M * (ns + 1) * nsys * sizeof(double), cudaMemcpyDeviceToHost),
+           "trajectory copy");
+    std::vector<int> hi((size_t)2 * std::max(ns, 1) * M);
+    ck(cudaMemcpy(hi.data(), d_iters, hi.size() * sizeof(int), cudaMemcpyDeviceToHost), "iters copy");
+    double tot = 0.0;
+    for (int m = 0; m < M; m++) {
+        double s = 0.0;
+        for (int q = 0; q < 2 * ns; q++) {
+            const int v = hi[(size_t)q * M + m];
+            if (iters) iters[(size_t)m * 2 * ns + q] = v;
+            s += v;
+        }
+        tot = std::max(tot, s);
+    }
+    L->iters_total = tot;
+    if (status) ck(cudaMemcpy(status, L->W.status, M * sizeof(int), cudaMemcpyDeviceToHost), "status copy");
+    ck(cudaGetLastError(), "integrate");
+    API_END
+}
+
+int32_t gp_reduced_selftest(const gp_problem *prob, const int32_t *s_rowptr, const int32_t *s_colidx,
+                            const double *s_val, const double *rhs, double *x, double out[4]) {
+    API_BEGIN
+    if (!prob || !s_rowptr || !s_colidx || !s_val || !rhs || !x || !out) fail(GP_E_INVALID, "null argument");
+    Plan pl;
+    make_plan(prob, pl);
+    const int n = pl.n_red;
+    auto find = [&](int r, int c, bool &hit) -> double {
+        const int32_t *b = s_colidx + s_rowptr[r], *e = s_colidx + s_rowptr[r + 1];
+        const int32_t *it = std::lower_bound(b, e, c);
+        hit = it != e && *it == c;
+        return hit ? s_val[s_rowptr[r] + (it - s_colidx - s_rowptr[r])] : 0.0;
+    };
+    std::vector<double> svar(pl.n_var);
+    for (int v = 0; v < pl.n_var; v++) {
+        bool hit;
+        svar[v] = find(pl.var_r[v], pl.var_c[v], hit);
+    }
+    // the constant part must reproduce S off the diagonal blocks
+    double mism = 0.0;
+    for (int b = 0; b < pl.nb; b++)
+        for (int q = prob->y_rowptr[b]; q < prob->y_rowptr[b + 1]; q++) {
+            const int j = prob->y_colidx[q];
+            if (j == b) continue;
+            const double g = prob->y_re[q], bb = prob->y_im[q];
+            const double want[4] = {-g, bb, -bb, -g};
+            for (int t = 0; t < 4; t++) {
+                bool hit;
+                const double got = find(2 * b + t / 2, 2 * j + t % 2, hit);
+                mism = std::max(mism, std::fabs(got - want[t]));
+            }
+        }
+    std::vector<double> xp(n);
+    for (int k = 0; k < n; k++) xp[k] = rhs[pl.sym.perm[k]];
+    const int zp = host_factor_solve(pl, svar, xp);
+    for (int k = 0; k < n; k++) x[pl.sym.perm[k]] = xp[k];
+    out[0] = mism;
+    out[1] = zp;
+    out[2] = (double)pl.sym.nnz_lu;
+    out[3] = pl.sym.nlevels;
+    API_END
+}
+
+int32_t gp_last_timing(const gp_layout *L, double out[8]) {
+    API_BEGIN
+    if (!L || !out) fail(GP_E_INVALID, "null argument");
+    for (int i = 0; i < 8; i++) out[i] = 0.0;
+    out[0] = L->t_total_ms;
+    out[5] = L->iters_total;
+    out[6] = L->launches;
+    API_END
+}
+
+}  // extern "C"

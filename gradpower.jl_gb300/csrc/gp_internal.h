@@ -1,0 +1,91 @@
+// Internal declarations shared by the host orchestration (gp_api.cu) and
+// the device kernels (gp_kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gp {
+
+// Struct-of-arrays device table on the GPU (see gp_device_table).
+struct DTab {
+    int n;
+    const int *bus, *diff_ptr, *alg_ptr, *ctrl_ptr, *par_ptr, *link0, *link1;
+};
+
+// Everything the kernels read about the problem.  All pointers are device
+// pointers; per-scenario arrays are scenario-major.
+struct DevProblem {
+    int n_bus, n_diff, n_alg, n_ctrl, n_par, n_sys, net, n_red;
+    int M;
+    // complex Ybus, CSR
+    const int *y_rowptr, *y_colidx;
+    const double *y_re, *y_im;
+    DTab dev[8];
+    const uint8_t *is_diff;
+    // clusters (non-trivial only are processed by the cluster kernel)
+    int n_cl;
+    const int *cl_w_start, *cl_w_size, *cl_gen, *cl_gov_type, *cl_gov, *cl_exc_type, *cl_exc, *cl_pss;
+    // per bus: non-trivial clusters, ZIP loads, static generators
+    const int *bus_cl_ptr, *bus_cl, *bus_zl_ptr, *bus_zl, *bus_sg_ptr, *bus_sg;
+    // static generators in the reduced system
+    const int *sg_red;     // [n_sg] reduced index of the first alg state (or -1)
+    const int *sg_var;     // [n_sg] first index of its coupling entries in the var block
+    int n_var;             // per-scenario variable entries of S: 4*n_bus + sg entries
+    // faults expanded per scenario
+    const int *fl_ptr;     // [M+1]
+    const int *fl_bus;
+    const double *fl_yf;   // 1/rfault
+    const uint8_t *fl_on;  // current status
+    // symbolic permutation of the reduced system
+    const int *iperm;      // reduced index -> permuted position
+};
+
+// Per-scenario work arrays of the Newton iteration.
+struct DevWork {
+    double *z, *zold, *u0, *p;      // [M][n_sys], [M][n_sys], [M][n_ctrl], [M][n_par]
+    double *yx;                     // [M][3][n_da]: A^-1 f, A^-1 B(:,1), A^-1 B(:,2)
+    double *clout;                  // [M][n_cl][8]: D (4), C y (2), injection (2)
+    double *svar;                   // [M][n_var]: diagonal blocks and static-generator couplings
+    double *xperm;                  // [M][n_red]: right-hand side / solution, permuted
+    double *f;                      // [M][n_sys] residual (written when want_f)
+    unsigned long long *norm;       // [M] residual infinity norm as ordered bits
+    uint8_t *active;                // [M] scenario takes part in this iteration
+    int *iters;                     // [M] Newton updates in the current solve
+    int *status;                    // [M] 0 ok, 1 itermax reached, 2 non-finite, 4 zero pivot
+    int *flag;                      // [1] number of scenarios still iterating
+    double *dt;                     // [1] time step of the current solve
+};
+
+// Symbolic factor layout on the GPU.
+struct DevSym {
+    int n, nsup, nlevels;
+    const int *sup_start, *row_ptr, *rows, *child_ptr, *children, *relmap_ptr, *relmap;
+    const int64_t *front_off, *uvec_off;
+    const int *level_sups;
+    int64_t front_total, uvec_total;
+    const int *asmc_ptr, *asmc_pos;   // constant entries: front position, value
+    const double *asmc_val;
+    const int *asmv_ptr, *asmv_pos, *asmv_idx;   // variable entries: front position, svar index
+    double *fronts;                   // [M][front_total]
+    double *uvec;                     // [M][uvec_total]
+    int *ipiv;                        // [M][n] pivot row within the supernode, per column
+};
+
+// launches (gp_kernels.cu)
+void launch_cluster(const DevProblem &P, const DevWork &W, int want_f, cudaStream_t st);
+void launch_network(const DevProblem &P, const DevWork &W, int want_f, cudaStream_t st);
+void launch_check(const DevProblem &P, const DevWork &W, double tol, int itermax, cudaStream_t st);
+void launch_reset_norm(const DevProblem &P, const DevWork &W, cudaStream_t st);
+void launch_factor_level(const DevProblem &P, const DevWork &W, const DevSym &S, int lvl_begin, int lvl_count,
+                         int max_front, cudaStream_t st);
+void launch_fwd_level(const DevProblem &P, const DevWork &W, const DevSym &S, int lvl_begin, int lvl_count,
+                      int max_front, cudaStream_t st);
+void launch_bwd_level(const DevProblem &P, const DevWork &W, const DevSym &S, int lvl_begin, int lvl_count,
+                      int max_front, cudaStream_t st);
+void launch_update(const DevProblem &P, const DevWork &W, const DevSym &S, const int *perm, cudaStream_t st);
+void launch_events(const DevProblem &P, const DevWork &W, const int *fl_on_step, const int *fl_off_step,
+                   const int *fl_scen, uint8_t *fl_on, int n_fl, int step, cudaStream_t st);
+void launch_snapshot(const double *z, double *traj, int M, int n_sys, int n_steps, int k, cudaStream_t st);
+int factor_smem_limit();
+
+}  // namespace gp

@@ -1,0 +1,166 @@
+"""Python mirror of the reference's GPU entry points, over the C ABI.
+
+    gbl = GpuBatchedLayout(dp, ps, M)                     # ext/...:466
+    tvec, trajs = integrate_gpu_schur_cudss(gbl, ps, tf)   # ext/...:3008-3080
+    tvec, trajs = integrate_gpu_cudss(gbl, ps, tf)         # ext/...:2924-2996
+
+`trajs[m]` is an (n_sys, n_steps+1) array per scenario, like the reference's
+`Vector{Matrix{Float64}}`.  Events come from `ps.dynamic.events` (applied to
+every scenario, the reference's semantics); `scenario_faults` adds one event
+list per scenario.  There is no CPU fallback: a missing or failing library
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import layout as LY
+from . import model as Mdl
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libgradpower_gb300.so")
+_lib = None
+
+
+class GradPowerError(RuntimeError):
+    pass
+
+
+def library():
+    """Load libgradpower_gb300.so (built by build.py / __graft_entry__.build)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            raise GradPowerError("libgradpower_gb300.so is not built (%s); run build()" % _LIB_PATH)
+        L = C.CDLL(_LIB_PATH)
+        vp = C.c_void_p
+        L.gp_abi_version.restype = C.c_int32
+        L.gp_last_error.argtypes = [C.c_char_p, C.c_int32]
+        L.gp_last_error.restype = C.c_int32
+        L.gp_layout_create.argtypes = [vp, C.c_int32, vp, vp, vp, C.POINTER(C.c_void_p)]
+        L.gp_layout_destroy.argtypes = [vp]
+        L.gp_layout_stats.argtypes = [vp, vp]
+        L.gp_set_state.argtypes = [vp, vp]
+        L.gp_get_state.argtypes = [vp, vp]
+        L.gp_integrate.argtypes = [vp, vp, C.c_int32, vp, vp, vp, vp]
+        L.gp_residual.argtypes = [vp, vp, C.c_double, C.c_int32, vp, vp, vp]
+        L.gp_last_timing.argtypes = [vp, vp]
+        for f in ("gp_layout_create", "gp_layout_destroy", "gp_layout_stats", "gp_set_state",
+                  "gp_get_state", "gp_integrate", "gp_residual", "gp_last_timing"):
+            getattr(L, f).restype = C.c_int32
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        buf = C.create_string_buffer(1024)
+        library().gp_last_error(buf, 1024)
+        raise GradPowerError("libgradpower_gb300 error %d: %s" % (rc, buf.value.decode(errors="replace")))
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+class GpuBatchedLayout:
+    """Device-resident batch of M scenarios (ext/GradPowerCUDAExt/
+    GradPowerCUDAExt.jl:303-945).  Owns all device memory; `close()` or
+    garbage collection releases it."""
+
+    def __init__(self, dp: Mdl.DynamicProblem, ps: Mdl.PowerSystem, M: int,
+                 z0: Optional[np.ndarray] = None, p: Optional[np.ndarray] = None):
+        self.ps = ps
+        self.M = int(M)
+        self.arrays = LY.ProblemArrays(ps)
+        z, u, pp = LY.replicate(dp, self.M)
+        if z0 is not None:
+            z = np.ascontiguousarray(z0, dtype=np.float64).reshape(self.M, -1)
+        if p is not None:
+            pp = np.ascontiguousarray(p, dtype=np.float64).reshape(self.M, -1)
+        self.n_sys = self.arrays.n_sys
+        self._keep = (z, u, pp)
+        h = C.c_void_p()
+        P = self.arrays.as_ctypes()
+        _check(library().gp_layout_create(C.addressof(P), self.M, _p(z), _p(u), _p(pp), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            library().gp_layout_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def z(self) -> np.ndarray:
+        out = np.empty((self.M, self.n_sys))
+        _check(library().gp_get_state(self._h, _p(out)))
+        return out
+
+    @z.setter
+    def z(self, value):
+        v = np.ascontiguousarray(value, dtype=np.float64).reshape(self.M, self.n_sys)
+        _check(library().gp_set_state(self._h, _p(v)))
+
+    def stats(self) -> dict:
+        out = np.zeros(8, dtype=np.int64)
+        _check(library().gp_layout_stats(self._h, _p(out)))
+        keys = ("n_red", "nnz_S", "nnz_LU", "supernodes", "levels", "factor_flops", "sum_w2", "max_front")
+        return dict(zip(keys, (int(v) for v in out)))
+
+    def timing(self) -> dict:
+        out = np.zeros(8)
+        _check(library().gp_last_timing(self._h, _p(out)))
+        return dict(total_ms=out[0], newton_iters=out[5], launches=out[6])
+
+    def residual(self, zold, dt, faults=(), fault_on=()):
+        """Backward-Euler residual at the current state (parity probe)."""
+        fa, nf = LY.fault_array([[] for _ in range(self.M)], dt, faults)
+        on = np.ascontiguousarray(np.asarray(fault_on, dtype=np.uint8).reshape(-1)) if nf else np.zeros(1, np.uint8)
+        f = np.empty((self.M, self.n_sys))
+        zo = np.ascontiguousarray(zold, dtype=np.float64).reshape(self.M, self.n_sys)
+        _check(library().gp_residual(self._h, _p(zo), float(dt), nf, C.addressof(fa), _p(on), _p(f)))
+        return f
+
+    def integrate(self, tf: float, dt: float = 1.0 / 120.0, newton_tol: float = 1e-10,
+                  itermax: int = 30, events: Sequence[Mdl.ContingencyEvent] = (),
+                  scenario_faults: Optional[Sequence[Sequence[Mdl.ContingencyEvent]]] = None,
+                  want_traj: bool = True, solver: int = LY.SOLVER_SCHUR_FP64):
+        nsteps = LY.jl_round(tf / dt)
+        per = scenario_faults if scenario_faults is not None else [[] for _ in range(self.M)]
+        fa, nf = LY.fault_array(per, dt, events)
+        opt = LY.GpOptions(dt, nsteps, newton_tol, itermax, solver)
+        traj = np.empty((self.M, nsteps + 1, self.n_sys)) if want_traj else None
+        iters = np.zeros((self.M, 2 * max(nsteps, 1)), dtype=np.int32)
+        status = np.zeros(self.M, dtype=np.int32)
+        _check(library().gp_integrate(self._h, C.byref(opt), nf, C.addressof(fa), _p(traj), _p(iters),
+                                      _p(status)))
+        tvec = np.arange(nsteps + 1) * dt
+        return dict(tvec=tvec, traj=traj, iters=iters[:, :2 * nsteps], status=status)
+
+
+def integrate_gpu_schur_cudss(gbl: GpuBatchedLayout, ps: Mdl.PowerSystem, tf: float,
+                              dt: float = 1.0 / 120.0, newton_tol: float = 1e-10,
+                              scenario_faults=None):
+    """(tvec, trajs): the reference's GPU Schur integrator
+    (ext/GradPowerCUDAExt/GradPowerCUDAExt.jl:3008-3080)."""
+    r = gbl.integrate(tf, dt, newton_tol, 30, ps.dynamic.events, scenario_faults)
+    return r["tvec"], [r["traj"][m].T for m in range(gbl.M)]
+
+
+def integrate_gpu_cudss(gbl: GpuBatchedLayout, ps: Mdl.PowerSystem, tf: float,
+                        dt: float = 1.0 / 120.0, newton_tol: float = 1e-10,
+                        scenario_faults=None):
+    """(tvec, trajs): the reference's monolithic GPU integrator
+    (ext/GradPowerCUDAExt/GradPowerCUDAExt.jl:2924-2996).  The library runs
+    the same exact Newton step with the cluster blocks eliminated first."""
+    return integrate_gpu_schur_cudss(gbl, ps, tf, dt, newton_tol, scenario_faults)

@@ -191,6 +191,18 @@ int32_t gp_residual(gp_layout *L, const double *zold, double dt, int32_t n_fault
  * iterations summed over steps (max over scenarios), out[6] kernel launches. */
 int32_t gp_last_timing(const gp_layout *L, double out[8]);
 
+/* Host-only check of the reduced-system machinery, needs no GPU: builds the
+ * same symbolic analysis and front assembly lists as gp_layout_create, takes
+ * the diagonal blocks and static-generator couplings of S from the given
+ * CSR matrix (reduced indexing: 2b, 2b+1 for bus b, then static-generator
+ * states), factors and solves S x = rhs on the host with the operation order
+ * of the device kernels.  out[0] max |S - (-Ybus)| over off-diagonal blocks,
+ * out[1] zero pivots, out[2] nnz(L+U), out[3] elimination-tree levels.
+ * No counterpart in the reference: a test hook for the analysis that
+ * replaces cuDSS's. */
+int32_t gp_reduced_selftest(const gp_problem *prob, const int32_t *s_rowptr, const int32_t *s_colidx,
+                            const double *s_val, const double *rhs, double *x, double out[4]);
+
 #ifdef __cplusplus
 }
 #endif
