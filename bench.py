@@ -1,0 +1,350 @@
+#!/usr/bin/env python
+"""Benchmark: scenario-steps/s of the batched backward-Euler Newton step.
+
+Workload: the 70,000-bus planar grid (235,109 unknowns per scenario, 5,000
+machine clusters), 8 fault scenarios per GPU (seeded faults on top-decile
+degree buses), 1 s horizon at dt = 1/120 s.  One benchmark step = one
+integration of the whole horizon for every scenario: 120 backward-Euler
+steps, their Newton iterations and the two dt = 0 event re-solves, i.e.
+8 x 120 scenario-steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+The GPU arm prints one JSON line with `value` measured with inputs resident
+on the device (device-clock CUDA events recorded by the library), `e2e`
+measured through the public API with the state uploaded from pinned host
+memory and the full trajectory read back every step, the roofline of the
+dominant kernel phase, the CPU oracle baseline and the SM clocks sampled
+during the timed region.  `--impl reference` times the CPU restatement of
+the reference's integrate! path (the oracle, OpenMP over scenarios) on the
+same workload.
+"""
+import argparse
+import importlib.util
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+WORKLOAD = "planar70k"
+SCEN_PER_GPU = 8
+TF = 1.0
+DT = 1.0 / 120.0
+
+
+def load_package():
+    if "gradpower_gb300" in sys.modules:
+        return sys.modules["gradpower_gb300"]
+    pkg = os.path.join(ROOT, "gradpower.jl_gb300")
+    spec = importlib.util.spec_from_file_location("gradpower_gb300", os.path.join(pkg, "__init__.py"),
+                                                  submodule_search_locations=[pkg])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["gradpower_gb300"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def load_oracle():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    return oracle
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.gpu = gpu_index
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_baseline(gp, orc, w):
+    """The oracle (restatement of the reference's integrate! KLU path), one
+    thread, one scenario over the full 1 s horizon (~10 s of CPU work)."""
+    from gradpower_gb300 import layout as LY
+    PA = LY.ProblemArrays(w.ps)
+    z, u, p = LY.replicate(w.dp, 1)
+    fa, nf = LY.fault_array(w.faults[:1], DT)
+    ns = LY.jl_round(TF / DT)
+    t0 = time.perf_counter()
+    orc.integrate(PA, z, u, p, fa, nf, DT, ns, itermax=50, solver=0, nthreads=1, want_traj=False)
+    t = time.perf_counter() - t0
+    return {"value": ns / t, "unit": "scenario-steps/s", "cores": 1, "kind": "port",
+            "sample": "1 scenario x %d steps of the %s workload, monolithic sparse-LU Newton, 1 thread"
+                      % (ns, WORKLOAD)}
+
+
+def gpu_arm(args):
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    gp = load_package()
+    from gradpower_gb300 import build, gpu, synthetic
+    if rank == 0 or world > 1:
+        build.build()
+    M_total = SCEN_PER_GPU * world
+    w = synthetic.planar70k(n_scenarios=M_total)
+    lo, hi = gpu.scenario_shard(M_total, rank, world)
+    faults = w.faults[lo:hi]
+    Mloc = hi - lo
+    gbl = gpu.GpuBatchedLayout(w.dp, w.ps, Mloc)
+    stats = gbl.stats()
+    nsteps = int(round(TF / DT))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def one(want_traj=False):
+        gbl.restore_initial_state()
+        return gbl.integrate(TF, DT, scenario_faults=faults, want_traj=want_traj)
+
+    for _ in range(args.warmup):
+        one()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident timed region ----
+    clk = ClockSampler(local)
+    barrier()
+    clk.start()
+    acc = dict(total_ms=0.0, cluster_ms=0.0, network_ms=0.0, factor_ms=0.0, solve_ms=0.0, update_ms=0.0,
+               launches=0.0, factor_launches=0.0, linear_solves=0.0, newton_iters=0.0)
+    statuses = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)                      # L2 flush between steps (buffer > 129 MB L2)
+        torch.cuda.synchronize()
+        r = one()
+        statuses.append(int(r["status"].max()))
+        t = gbl.timing()
+        for k in acc:
+            acc[k] += t[k]
+    barrier()
+    clocks = clk.stop()
+    dev_ms = acc["total_ms"]
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([dev_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        dev_ms = float(tt.item())
+    units = M_total * nsteps * args.steps
+    value = units / (dev_ms / 1e3)
+
+    # ---- end to end through the public API (host buffers) ----
+    z_host = torch.empty((Mloc, gbl.n_sys), dtype=torch.float64, pin_memory=True).numpy()
+    z_host[:] = w.dp.zvec[None, :]
+    traj_host = torch.empty((Mloc, nsteps + 1, gbl.n_sys), dtype=torch.float64, pin_memory=True).numpy()
+    gbl.z = z_host
+    gbl.integrate(TF, DT, scenario_faults=faults, traj_out=traj_host)      # warm the trajectory buffer
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        gbl.z = z_host                                                     # H2D of the inputs
+        gbl.integrate(TF, DT, scenario_faults=faults, traj_out=traj_host)  # D2H of the trajectories
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e = {"value": units / e2e_s, "unit": "scenario-steps/s",
+           "h2d_bytes_per_step": int(z_host.nbytes * world),
+           "d2h_bytes_per_step": int(traj_host.nbytes * world)}
+
+    if rank != 0:
+        gbl.close()
+        return
+
+    # ---- roofline of the dominant phase ----
+    peak, peak_kind = peaks()
+    n_red = stats["n_red"]
+    nnz_lu = stats["nnz_LU"]
+    # algorithmic bytes (FP64) per scenario, documented in the design doc:
+    #   factorisation: read S (4 per 2x2 block entry ~ nnz of the reduced
+    #   pattern) + write L and U;  solves: read L and U twice + vectors;
+    #   cluster kernel: read 2w+4 state/voltage values + 50 parameters,
+    #   write 3w solution columns + 8 Schur terms
+    nnz_s = 4 * (w.ps.nbus + 2 * len(w.ps.branches))
+    sum_w = int(w.ps.dynamic.diff_dim + w.ps.dynamic.alg_dim)
+    n_cl = len(w.ps.dynamic.clusters)
+    phases = {
+        "factor": (acc["factor_ms"], 8.0 * (nnz_s + nnz_lu)),
+        "solve": (acc["solve_ms"], 8.0 * (2 * nnz_lu + 4 * n_red)),
+        "cluster": (acc["cluster_ms"], 8.0 * (5 * sum_w + n_cl * (4 + 50 + 8))),
+        "network": (acc["network_ms"], 8.0 * (4 * w.ps.nbus + 2 * len(ps_branches(w)) * 2 + 8 * w.ps.nbus)),
+    }
+    dom = max(phases, key=lambda k: phases[k][0])
+    ms, bytes_per_scen = phases[dom]
+    # scenario-passes of the dominant phase in the timed region: every
+    # linear solve covers all scenarios still iterating; count Mloc per solve
+    # for the solve phases, per evaluation for the evaluation phases
+    passes = acc["linear_solves"] * Mloc if dom in ("factor", "solve") else acc["newton_iters"] * Mloc
+    achieved = bytes_per_scen * passes / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None, "kernel": dom,
+                "peak_source": peak_kind,
+                "phase_ms": {k: round(v[0], 3) for k, v in phases.items()}}
+
+    oracle = load_oracle()
+    base = cpu_baseline(gp, oracle, w)
+    line = {
+        "metric": "scenario-steps/s at 70k-bus (FP64 Schur path)",
+        "value": value,
+        "unit": "scenario-steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dev_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded 70,000-bus planar grid, random-parameter machine mix)",
+        "config": {"workload": "%s: %d buses, %d unknowns, %d clusters, %d scenarios/GPU, tf=%gs, dt=1/120s"
+                               % (WORKLOAD, w.ps.nbus, gbl.n_sys, n_cl, SCEN_PER_GPU, TF),
+                   "scenarios": M_total, "time_steps": nsteps, "solver": "schur_fp64",
+                   "l2": "flushed between steps (256 MB write); working set > 129 MB L2",
+                   "parallelism": "scenario shards, %d GPU(s)" % world,
+                   "nnz_LU": nnz_lu, "levels": stats["levels"], "supernodes": stats["supernodes"],
+                   "sum_w2": stats["sum_w2"], "newton_iters_per_run": acc["newton_iters"] / args.steps,
+                   "status_max": max(statuses) if statuses else None},
+        "e2e": e2e,
+        "gpu_launches": int(acc["launches"]),
+        "roofline": roofline,
+        "cpu_baseline": base,
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    gbl.close()
+
+
+def ps_branches(w):
+    return w.ps.branches
+
+
+def reference_arm(args):
+    """CPU restatement of the reference's integrate! path on the same
+    workload, OpenMP over the 8 scenarios with every host thread."""
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    gp = load_package()
+    orc = load_oracle()
+    from gradpower_gb300 import layout as LY, synthetic
+    w = synthetic.planar70k(n_scenarios=SCEN_PER_GPU * world)
+    PA = LY.ProblemArrays(w.ps)
+    Ms = SCEN_PER_GPU
+    z, u, p = LY.replicate(w.dp, Ms)
+    fa, nf = LY.fault_array(w.faults[:Ms], DT)
+    cores = os.cpu_count() or 1
+    threads = min(cores, Ms)
+    ns = 30           # bounded sample: 0.25 s of the 1 s horizon, covers fault on (step 12) and off (24)
+    for _ in range(args.warmup):
+        orc.integrate(PA, z, u, p, fa, nf, DT, 12, itermax=50, solver=0, nthreads=threads, want_traj=False)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        orc.integrate(PA, z, u, p, fa, nf, DT, ns, itermax=50, solver=0, nthreads=threads, want_traj=False)
+    t = time.perf_counter() - t0
+    v = Ms * ns * args.steps / t
+    line = {
+        "impl": "reference",
+        "metric": "scenario-steps/s at 70k-bus (FP64 Schur path)",
+        "value": v, "unit": "scenario-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded 70,000-bus planar grid)",
+        "config": {"workload": "%s: %d buses, %d scenarios, first %d of 120 steps per sample"
+                               % (WORKLOAD, w.ps.nbus, Ms, ns)},
+        "cpu_baseline": {"value": v, "unit": "scenario-steps/s", "cores": threads, "kind": "port",
+                         "sample": "%d scenarios x %d steps per step, monolithic sparse-LU Newton, "
+                                   "OpenMP over scenarios" % (Ms, ns)},
+        "e2e": {"value": v, "unit": "scenario-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

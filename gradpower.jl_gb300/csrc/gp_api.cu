@@ -111,6 +111,13 @@ struct gp_layout {
     int graph_itermax = -1;
     // timing of the last integrate call
     double t_total_ms = 0.0, iters_total = 0.0, launches = 0.0;
+    // phase timing: events recorded as nodes of the captured graphs
+    // 0 before cluster, 1 after cluster, 2 after network,
+    // 3 before factor, 4 after factor, 5 after forward, 6 after backward, 7 after update
+    cudaEvent_t pev[8] = {};
+    double ph_ms[8] = {};        // 0 cluster, 1 network, 2 factor, 3 forward, 4 backward, 5 update
+    double factor_launches = 0.0, solves = 0.0;
+    double *z_init = nullptr;    // z0 as given to gp_layout_create
     int64_t sum_w2 = 0;
 };
 
@@ -582,6 +589,10 @@ void build_work(gp_layout *L, const double *z0, const double *u0, const double *
     ck(cudaMallocHost(&L->h_flag, sizeof(int)), "cudaMallocHost");
     ck(cudaMallocHost(&L->h_dt, sizeof(double)), "cudaMallocHost");
     ck(cudaStreamCreateWithFlags(&L->st, cudaStreamNonBlocking), "stream");
+    for (int i = 0; i < 8; i++) ck(cudaEventCreate(&L->pev[i]), "event");
+    // keep the initial state for gp_restore_initial_state
+    L->z_init = A.alloc<double>(M * P.n_sys);
+    ck(cudaMemcpy(L->z_init, W.z, M * P.n_sys * sizeof(double), cudaMemcpyDeviceToDevice), "z0 copy");
 }
 
 void set_faults(gp_layout *L, int n_faults, const gp_fault *faults) {
@@ -629,24 +640,36 @@ void set_faults(gp_layout *L, int n_faults, const gp_fault *faults) {
     if (L->g_solve) { cudaGraphExecDestroy(L->g_solve); L->g_solve = nullptr; }
 }
 
+void mark(gp_layout *L, int i) {
+    ck(cudaEventRecordWithFlags(L->pev[i], L->st, cudaEventRecordExternal), "event record");
+}
+
 void enqueue_solve(gp_layout *L) {
     const gp::Symbolic &sym = L->sym;
+    mark(L, 3);
     for (int l = 0; l < sym.nlevels; l++)
         gp::launch_factor_level(L->P, L->W, L->S, sym.level_ptr[l], sym.level_ptr[l + 1] - sym.level_ptr[l],
                                 L->lvl_max_front[l], L->st);
+    mark(L, 4);
     for (int l = 0; l < sym.nlevels; l++)
         gp::launch_fwd_level(L->P, L->W, L->S, sym.level_ptr[l], sym.level_ptr[l + 1] - sym.level_ptr[l],
                              L->lvl_max_front[l], L->st);
+    mark(L, 5);
     for (int l = sym.nlevels - 1; l >= 0; l--)
         gp::launch_bwd_level(L->P, L->W, L->S, sym.level_ptr[l], sym.level_ptr[l + 1] - sym.level_ptr[l],
                              L->lvl_max_front[l], L->st);
+    mark(L, 6);
     gp::launch_update(L->P, L->W, L->S, L->d_state_maps, L->st);
+    mark(L, 7);
 }
 
 void enqueue_eval(gp_layout *L, double tol, int itermax) {
     gp::launch_reset_norm(L->P, L->W, L->st);
+    mark(L, 0);
     gp::launch_cluster(L->P, L->W, 0, L->st);
+    mark(L, 1);
     gp::launch_network(L->P, L->W, 0, L->st);
+    mark(L, 2);
     gp::launch_check(L->P, L->W, tol, itermax, L->st);
     ck(cudaMemcpyAsync(L->h_flag, L->W.flag, sizeof(int), cudaMemcpyDeviceToHost, L->st), "flag copy");
 }
@@ -678,17 +701,36 @@ void ensure_graphs(gp_layout *L, double tol, int itermax) {
 
 // One Newton solve for the scenarios marked active; returns after every
 // scenario converged, diverged or used itermax updates.
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0.f;
+    ck(cudaEventElapsedTime(&ms, a, b), "event elapsed");
+    return ms;
+}
+
 void newton(gp_layout *L, double dt, double tol, int itermax) {
     *L->h_dt = dt;
     ck(cudaMemcpyAsync(L->W.dt, L->h_dt, sizeof(double), cudaMemcpyHostToDevice, L->st), "dt");
     ck(cudaMemsetAsync(L->W.iters, 0, L->M * sizeof(int), L->st), "memset");
+    bool solve_pending = false;
     for (int guard = 0; guard <= itermax + 1; guard++) {
         ck(cudaGraphLaunch(L->g_eval, L->st), "graph launch");
         ck(cudaStreamSynchronize(L->st), "newton sync");
         L->launches += 4;
+        L->ph_ms[0] += elapsed(L->pev[0], L->pev[1]);
+        L->ph_ms[1] += elapsed(L->pev[1], L->pev[2]);
+        if (solve_pending) {
+            L->ph_ms[2] += elapsed(L->pev[3], L->pev[4]);
+            L->ph_ms[3] += elapsed(L->pev[4], L->pev[5]);
+            L->ph_ms[4] += elapsed(L->pev[5], L->pev[6]);
+            L->ph_ms[5] += elapsed(L->pev[6], L->pev[7]);
+            solve_pending = false;
+        }
         if (*L->h_flag == 0) return;
         ck(cudaGraphLaunch(L->g_solve, L->st), "graph launch");
+        solve_pending = true;
         L->launches += 3 * L->sym.nlevels + 1;
+        L->factor_launches += L->sym.nlevels;
+        L->solves += 1;
     }
     fail(GP_E_NUMERIC, "Newton loop did not terminate");
 }
@@ -761,6 +803,8 @@ int32_t gp_layout_destroy(gp_layout *L) {
     L->arena.release();
     if (L->h_flag) cudaFreeHost(L->h_flag);
     if (L->h_dt) cudaFreeHost(L->h_dt);
+    for (int i = 0; i < 8; i++)
+        if (L->pev[i]) cudaEventDestroy(L->pev[i]);
     if (L->st) cudaStreamDestroy(L->st);
     delete L;
     API_END
@@ -786,6 +830,16 @@ int32_t gp_set_state(gp_layout *L, const double *z) {
     API_BEGIN
     if (!L || !z) fail(GP_E_INVALID, "null argument");
     ck(cudaMemcpy(L->W.z, z, (size_t)L->M * L->n_sys * sizeof(double), cudaMemcpyHostToDevice), "set state");
+    API_END
+}
+
+int32_t gp_restore_initial_state(gp_layout *L) {
+    API_BEGIN
+    if (!L) fail(GP_E_INVALID, "null argument");
+    ck(cudaMemcpyAsync(L->W.z, L->z_init, (size_t)L->M * L->n_sys * sizeof(double), cudaMemcpyDeviceToDevice,
+                       L->st),
+       "restore state");
+    ck(cudaStreamSynchronize(L->st), "restore state");
     API_END
 }
 
@@ -853,6 +907,9 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
     ck(cudaEventCreate(&e1), "event");
     ck(cudaEventRecord(e0, L->st), "event");
     L->launches = 0;
+    L->factor_launches = 0;
+    L->solves = 0;
+    for (int i = 0; i < 8; i++) L->ph_ms[i] = 0.0;
     for (int k = 1; k <= ns; k++) {
         ck(cudaMemcpyAsync(L->W.zold, L->W.z, (size_t)M * nsys * sizeof(double), cudaMemcpyDeviceToDevice, L->st),
            "zold");
@@ -949,13 +1006,20 @@ int32_t gp_reduced_selftest(const gp_problem *prob, const int32_t *s_rowptr, con
     API_END
 }
 
-int32_t gp_last_timing(const gp_layout *L, double out[8]) {
+int32_t gp_last_timing(const gp_layout *L, double out[16]) {
     API_BEGIN
     if (!L || !out) fail(GP_E_INVALID, "null argument");
-    for (int i = 0; i < 8; i++) out[i] = 0.0;
+    for (int i = 0; i < 16; i++) out[i] = 0.0;
     out[0] = L->t_total_ms;
+    out[1] = L->ph_ms[0];
+    out[2] = L->ph_ms[1];
+    out[3] = L->ph_ms[2];
+    out[4] = L->ph_ms[3] + L->ph_ms[4];
     out[5] = L->iters_total;
     out[6] = L->launches;
+    out[7] = L->ph_ms[5];
+    out[8] = L->factor_launches;
+    out[9] = L->solves;
     API_END
 }
 

@@ -49,8 +49,11 @@ def library():
         L.gp_integrate.argtypes = [vp, vp, C.c_int32, vp, vp, vp, vp]
         L.gp_residual.argtypes = [vp, vp, C.c_double, C.c_int32, vp, vp, vp]
         L.gp_last_timing.argtypes = [vp, vp]
+        L.gp_restore_initial_state.argtypes = [vp]
+        L.gp_reduced_selftest.argtypes = [vp] * 7
         for f in ("gp_layout_create", "gp_layout_destroy", "gp_layout_stats", "gp_set_state",
-                  "gp_get_state", "gp_integrate", "gp_residual", "gp_last_timing"):
+                  "gp_get_state", "gp_integrate", "gp_residual", "gp_last_timing",
+                  "gp_restore_initial_state", "gp_reduced_selftest"):
             getattr(L, f).restype = C.c_int32
         _lib = L
     return _lib
@@ -118,9 +121,17 @@ class GpuBatchedLayout:
         return dict(zip(keys, (int(v) for v in out)))
 
     def timing(self) -> dict:
-        out = np.zeros(8)
+        """Device time of the last integrate call by phase (CUDA events on
+        the library's stream, recorded inside its graphs)."""
+        out = np.zeros(16)
         _check(library().gp_last_timing(self._h, _p(out)))
-        return dict(total_ms=out[0], newton_iters=out[5], launches=out[6])
+        return dict(total_ms=float(out[0]), cluster_ms=float(out[1]), network_ms=float(out[2]),
+                    factor_ms=float(out[3]), solve_ms=float(out[4]), update_ms=float(out[7]),
+                    newton_iters=float(out[5]), launches=float(out[6]),
+                    factor_launches=float(out[8]), linear_solves=float(out[9]))
+
+    def restore_initial_state(self):
+        _check(library().gp_restore_initial_state(self._h))
 
     def residual(self, zold, dt, faults=(), fault_on=()):
         """Backward-Euler residual at the current state (parity probe)."""
@@ -134,18 +145,38 @@ class GpuBatchedLayout:
     def integrate(self, tf: float, dt: float = 1.0 / 120.0, newton_tol: float = 1e-10,
                   itermax: int = 30, events: Sequence[Mdl.ContingencyEvent] = (),
                   scenario_faults: Optional[Sequence[Sequence[Mdl.ContingencyEvent]]] = None,
-                  want_traj: bool = True, solver: int = LY.SOLVER_SCHUR_FP64):
+                  want_traj: bool = True, solver: int = LY.SOLVER_SCHUR_FP64,
+                  traj_out: Optional[np.ndarray] = None):
+        """Integrate every scenario from the current state.  `traj_out`, if
+        given, is a C-contiguous float64 array [M, n_steps+1, n_sys] (for
+        example a pinned buffer) that receives the trajectories."""
         nsteps = LY.jl_round(tf / dt)
         per = scenario_faults if scenario_faults is not None else [[] for _ in range(self.M)]
         fa, nf = LY.fault_array(per, dt, events)
         opt = LY.GpOptions(dt, nsteps, newton_tol, itermax, solver)
-        traj = np.empty((self.M, nsteps + 1, self.n_sys)) if want_traj else None
+        if traj_out is not None:
+            if (traj_out.shape != (self.M, nsteps + 1, self.n_sys) or traj_out.dtype != np.float64
+                    or not traj_out.flags.c_contiguous):
+                raise ValueError("traj_out must be a C-contiguous float64 array of shape %s"
+                                 % ((self.M, nsteps + 1, self.n_sys),))
+            traj = traj_out
+        else:
+            traj = np.empty((self.M, nsteps + 1, self.n_sys)) if want_traj else None
         iters = np.zeros((self.M, 2 * max(nsteps, 1)), dtype=np.int32)
         status = np.zeros(self.M, dtype=np.int32)
         _check(library().gp_integrate(self._h, C.byref(opt), nf, C.addressof(fa), _p(traj), _p(iters),
                                       _p(status)))
         tvec = np.arange(nsteps + 1) * dt
         return dict(tvec=tvec, traj=traj, iters=iters[:, :2 * nsteps], status=status)
+
+
+def scenario_shard(M: int, rank: int, world: int):
+    """Contiguous scenario range [lo, hi) of one rank.  Scenarios never
+    exchange data during a run, so sharding needs no collective until the
+    trajectories are gathered at the end."""
+    base, extra = divmod(M, world)
+    lo = rank * base + min(rank, extra)
+    return lo, lo + base + (1 if rank < extra else 0)
 
 
 def integrate_gpu_schur_cudss(gbl: GpuBatchedLayout, ps: Mdl.PowerSystem, tf: float,

@@ -166,6 +166,9 @@ int32_t gp_layout_stats(const gp_layout *L, int64_t out[8]);
 /* Copy the current state of all scenarios in or out: z [M*n_sys]. */
 int32_t gp_set_state(gp_layout *L, const double *z);
 int32_t gp_get_state(const gp_layout *L, double *z);
+/* Reset the state to the z0 given to gp_layout_create (device-side copy;
+ * reruns a batch without host traffic). */
+int32_t gp_restore_initial_state(gp_layout *L);
 
 /* Integrate every scenario for opt->n_steps backward-Euler steps from the
  * current state.  Replaces integrate_gpu_schur_cudss! / integrate_gpu_cudss!.
@@ -185,11 +188,14 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults,
 int32_t gp_residual(gp_layout *L, const double *zold, double dt, int32_t n_faults,
                     const gp_fault *faults, const uint8_t *fault_on, double *f);
 
-/* Time of the last gp_integrate call split by phase, milliseconds on the
- * device clock: out[0] total, out[1] cluster kernels, out[2] network
- * kernels, out[3] factorisation, out[4] triangular solves, out[5] Newton
- * iterations summed over steps (max over scenarios), out[6] kernel launches. */
-int32_t gp_last_timing(const gp_layout *L, double out[8]);
+/* Time of the last gp_integrate call split by phase, milliseconds between
+ * CUDA events recorded on the library's stream inside the captured graphs:
+ * out[0] total, out[1] cluster kernel, out[2] network kernel, out[3]
+ * factorisation (all levels), out[4] triangular solves, out[5] Newton
+ * iterations summed over steps (max over scenarios), out[6] kernel launches,
+ * out[7] update kernel, out[8] factorisation-level launches, out[9] linear
+ * solves (batched over scenarios); out[10..15] zero. */
+int32_t gp_last_timing(const gp_layout *L, double out[16]);
 
 /* Host-only check of the reduced-system machinery, needs no GPU: builds the
  * same symbolic analysis and front assembly lists as gp_layout_create, takes

@@ -1174,10 +1174,16 @@ static double inf_norm(const double *f, int n) {
     return m;
 }
 
-/* newton_step! (src/numerics.jl:55-176).  Returns iterations (linear
- * solves); *ok = 1 when converged. */
+/* Newton solve on the full Jacobian.  Returns iterations (linear solves);
+ * *ok = 1 when converged.  fresh_first = 1 follows the batched CPU path
+ * _newton_step_batched! (src/batched.jl:389-402): a new pivoting
+ * factorisation (klu) at the first iteration of every Newton call and
+ * klu! refactorisations after it.  fresh_first = 0 follows integrate! /
+ * newton_step! (src/numerics.jl:138-167): the pivot sequence of the
+ * factorisation made at z0 is reused for the whole run, with a fresh
+ * factorisation only when a pivot is exactly zero. */
 static int newton_mono(newton_ws *W, double *z, const double *zold, const double *u0, const double *p,
-                       const faults_t *F, double dt, double tol, int itermax, int *ok) {
+                       const faults_t *F, double dt, double tol, int itermax, int *ok, int fresh_first) {
     sym_t *S = W->S;
     int n = S->nsys;
     memcpy(W->zb, z, sizeof(double) * n);
@@ -1189,7 +1195,7 @@ static int newton_mono(newton_ws *W, double *z, const double *zold, const double
         if (nf < tol) { *ok = 1; break; }
         if (!isfinite(nf)) break;
         assemble_J(S, W->zb, u0, p, F, dt, &W->t);
-        if (factor_or_refactor(W, &S->J, 0) != 0) break;
+        if (factor_or_refactor(W, &S->J, fresh_first && it == 0) != 0) break;
         memcpy(W->dx, W->f, sizeof(double) * n);
         splu_solve(&W->LU, W->dx, W->work);
         for (int i = 0; i < n; i++) W->zb[i] -= W->dx[i];
@@ -1347,15 +1353,15 @@ static int integrate_one(const gp_problem *P, const double *z0, const double *u0
     uint8_t *on = (uint8_t *)calloc(nf > 0 ? nf : 1, 1);
     faults_t F = {nf, faults, on};
     int status = 0;
-    if (solver == 0) {
-        /* the reference factors J at z0 once before the loop (src/dynamics.jl:572-580) */
+    if (solver == 2) {
+        /* integrate! factors J at z0 once before the loop (src/dynamics.jl:572-580) */
         assemble_J(&S, z, u0, p, &F, dt, &W.t);
         if (factor_or_refactor(&W, &S.J, 1) != 0) status = 2;
     }
     for (int k = 1; k <= nsteps && status != 2; k++) {
         int ok;
         memcpy(zold, z, sizeof(double) * n);
-        int it = solver == 0 ? newton_mono(&W, z, zold, u0, p, &F, dt, tol, itermax, &ok)
+        int it = solver != 1 ? newton_mono(&W, z, zold, u0, p, &F, dt, tol, itermax, &ok, solver == 0)
                              : newton_schur(&W, z, zold, u0, p, &F, dt, tol, itermax, &ok);
         if (!ok) status = isfinite(inf_norm(z, n)) ? 1 : 2;
         if (iters) { iters[2 * (k - 1)] = it; iters[2 * (k - 1) + 1] = 0; }
@@ -1367,7 +1373,7 @@ static int integrate_one(const gp_problem *P, const double *z0, const double *u0
         }
         if (any) {
             memcpy(zold, z, sizeof(double) * n);
-            it = solver == 0 ? newton_mono(&W, z, zold, u0, p, &F, 0.0, tol, itermax, &ok)
+            it = solver != 1 ? newton_mono(&W, z, zold, u0, p, &F, 0.0, tol, itermax, &ok, solver == 0)
                              : newton_schur(&W, z, zold, u0, p, &F, 0.0, tol, itermax, &ok);
             if (!ok) status = isfinite(inf_norm(z, n)) ? 1 : 2;
             if (iters) iters[2 * (k - 1) + 1] = it;
@@ -1394,9 +1400,11 @@ static int integrate_one(const gp_problem *P, const double *z0, const double *u0
 /* exported entry points (called through ctypes by the test harness)   */
 /* ------------------------------------------------------------------ */
 
-/* Integrate M scenarios, each as an independent integrate! run.  Faults
- * with scenario == -1 apply to every scenario.  solver: 0 monolithic KLU
- * path, 1 Schur path.  traj [M][nsteps+1][n_sys] or NULL; zfinal [M][n_sys]
+/* Integrate M scenarios, each as an independent run.  Faults with
+ * scenario == -1 apply to every scenario.  solver: 0 monolithic sparse LU
+ * with the batched path's factorisation schedule (integrate_batched!),
+ * 1 Schur path (newton_step_schur!), 2 monolithic with integrate!'s
+ * schedule (one pivoting factorisation at z0, refactorisations after).  traj [M][nsteps+1][n_sys] or NULL; zfinal [M][n_sys]
  * or NULL; iters [M][2*nsteps] or NULL; status [M]; stats [M][6] or NULL. */
 int gpo_integrate(const gp_problem *P, int M, const double *z0, const double *u0, const double *p, int nf,
                   const gp_fault *faults, double dt, int nsteps, double tol, int itermax, int solver,

@@ -1,0 +1,157 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the CPU oracle.
+
+Bar: identical Newton iteration counts per step and every state within
+|gpu - oracle| <= 1e-9 * max(1, |oracle|) (the FP64 tolerance of the path:
+trajectories match the reference's CPU path to <= 1e-9 relative per state).
+"""
+import numpy as np
+import pytest
+
+from helpers import DT, Case, M, psse_case, run_oracle, synthetic_case
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-9
+
+
+@pytest.fixture(scope="module")
+def G():
+    from gradpower_gb300 import build, gpu
+    build.build()
+    return gpu
+
+
+def _close(a, b):
+    return np.max(np.abs(a - b) / np.maximum(1.0, np.abs(b)))
+
+
+def _gpu_run(G, c, nsteps, itermax=30, dt=DT):
+    gbl = G.GpuBatchedLayout(c.dp, c.ps, c.M)
+    try:
+        r = gbl.integrate(nsteps * dt, dt, itermax=itermax, events=c.events, scenario_faults=c.faults)
+    finally:
+        gbl.close()
+    return r
+
+
+def _parity(G, orc, c, nsteps, itermax=30):
+    g = _gpu_run(G, c, nsteps, itermax)
+    o = run_oracle(orc, c, nsteps, itermax=itermax)
+    assert np.array_equal(g["status"], o["status"])
+    ok = o["status"] == 0
+    assert np.array_equal(g["iters"][ok], o["iters"][ok])
+    if ok.any():
+        assert _close(g["traj"][ok], o["traj"][ok]) <= RTOL
+    return g, o
+
+
+CASES = [("2bus.raw", "2bus.dyr"), ("2bus.raw", "2bus_ESDC1A.dyr"), ("2bus.raw", "2bus_SEXS.dyr"),
+         ("2bus.raw", "2bus_TGOV1.dyr"), ("2bus.raw", "2bus_IEESGO.dyr"),
+         ("ieee9_v33.raw", "ieee9bus_gov.dyr"), ("ieee9_v33.raw", "ieee9bus_SEXS.dyr"),
+         ("ieee9_v33.raw", "ieee9bus_TGOV1.dyr"), ("IEEE39.raw", "IEEE39_gov.dyr")]
+
+
+@pytest.mark.parametrize("raw,dyr", CASES)
+def test_residual_parity_psse_cases(G, orc, golden_cases, raw, dyr):
+    ps, dp = psse_case(golden_cases, raw, dyr)
+    c = Case(ps, dp, [[M.ContingencyEvent(0, 0.05, 0.1, 0.2)]], 1)
+    gbl = G.GpuBatchedLayout(dp, ps, 1)
+    rng = np.random.default_rng(4)
+    z = dp.zvec + 1e-3 * rng.normal(size=dp.zvec.size)
+    gbl.z = z[None]
+    fa, nf = c.fault_array()
+    for on in (0, 1):
+        f = gbl.residual(dp.zvec[None], DT, faults=c.faults[0], fault_on=[on])
+        fo = orc.residual(c.PA, z, dp.zvec, dp.uvec, dp.pvec, fa, nf, np.array([on], np.uint8), DT)
+        assert np.max(np.abs(f[0] - fo)) <= 1e-12 * max(1.0, np.max(np.abs(fo)))
+    gbl.close()
+
+
+@pytest.mark.parametrize("raw,dyr", CASES[:8])
+def test_trajectory_parity_psse_cases(G, orc, golden_cases, raw, dyr):
+    """Reference-style events: one global fault applied to every scenario
+    (ps.dynamic.events), M = 2."""
+    ps, dp = psse_case(golden_cases, raw, dyr)
+    c = Case(ps, dp, None, 2, events=[M.ContingencyEvent(0, 0.02, 0.1, 0.2)])
+    _parity(G, orc, c, 90)
+
+
+def test_static_generators(G, orc, golden_cases):
+    """Machines without a dynamic model become StaticGenerator stand-ins
+    (slack: p, q states; PV: q state) inside the reduced network system."""
+    ps, dp = psse_case(golden_cases, "ieee9_v33.raw", "ieee9bus_gov.dyr", drop_dyr_gens=(1, 2))
+    c = Case(ps, dp, [[M.ContingencyEvent(4, 0.05, 0.1, 0.2)], [M.ContingencyEvent(6, 0.1, 0.1, 0.25)]], 2)
+    _parity(G, orc, c, 60)
+
+
+def test_two_bus_full_horizon(G, orc):
+    """The 2-bus GENROU+IEESGO workload over its full 10 s horizon."""
+    c, w = synthetic_case("two_bus", 1)
+    _parity(G, orc, c, 1200)
+
+
+def test_uqgrid_golden_trajectory_on_gpu(G, golden_cases, golden_known):
+    """The GPU path against the reference's golden rotor-speed trajectory
+    (examples/refs/2bus_esdc1a.npz)."""
+    uq = golden_known["uqgrid_2bus_esdc1a"]
+    ps, dp = psse_case(golden_cases, "2bus.raw", "2bus_ESDC1A.dyr", alpha=uq["zipload_alpha"])
+    c = Case(ps, dp, [[M.ContingencyEvent(uq["fault_bus_index"], uq["rfault"], uq["ton"], uq["toff"])]], 1)
+    g = _gpu_run(G, c, int(round(uq["tend"] / uq["dt"])), dt=uq["dt"])
+    w = g["traj"][0, ::5, ps.dynamic.devices[0].diff_ptr + 4]
+    assert np.max(np.abs(w - np.array(uq["speed"]))) < 1e-9
+
+
+def test_ring39_all_scenarios(G, orc):
+    """39-bus batch, M=64, one seeded fault bus per scenario, 1 s."""
+    c, w = synthetic_case("ring39", 64)
+    g, o = _parity(G, orc, c, 120)
+    assert (o["status"] == 0).mean() > 0.9
+
+
+def test_planar2k_batch(G, orc):
+    c, w = synthetic_case("planar2k", 8)
+    _parity(G, orc, c, 40)
+
+
+def test_planar70k_short(G, orc):
+    """The 70,000-bus grid, two scenarios, 15 steps around the fault onset."""
+    c, w = synthetic_case("planar70k", 2)
+    _parity(G, orc, c, 15)
+
+
+def test_reproducible(G):
+    """Deterministic reductions: two GPU runs are bit-identical."""
+    c, w = synthetic_case("planar2k", 4)
+    a = _gpu_run(G, c, 30)
+    b = _gpu_run(G, c, 30)
+    assert np.array_equal(a["traj"], b["traj"])
+
+
+def test_itermax_reports_status(G, orc):
+    """A solve that runs out of iterations is reported (status bit 1), not
+    hidden; the oracle agrees."""
+    c, w = synthetic_case("ring39", 4)
+    _parity(G, orc, c, 20, itermax=1)
+
+
+def test_invalid_fault_raises(G):
+    c, w = synthetic_case("two_bus", 1)
+    gbl = G.GpuBatchedLayout(c.dp, c.ps, 1)
+    with pytest.raises(G.GradPowerError):
+        gbl.integrate(0.1, scenario_faults=[[M.ContingencyEvent(99, 0.1, 0.0, 0.05)]])
+    gbl.close()
+
+
+def test_reference_api_signatures(G):
+    """integrate_gpu_schur_cudss / integrate_gpu_cudss return (tvec, trajs)
+    with trajs[m] of shape (n_sys, n_steps+1), like the reference."""
+    c, w = synthetic_case("two_bus", 1)
+    w.ps.dynamic.events[:] = [M.ContingencyEvent(1, 0.2, 0.05, 0.1)]
+    gbl = G.GpuBatchedLayout(w.dp, w.ps, 3)
+    tvec, trajs = G.integrate_gpu_schur_cudss(gbl, w.ps, 0.2)
+    assert len(trajs) == 3 and trajs[0].shape == (len(w.dp.zvec), 25) and len(tvec) == 25
+    gbl.z = np.tile(w.dp.zvec, (3, 1))
+    tvec2, trajs2 = G.integrate_gpu_cudss(gbl, w.ps, 0.2)
+    assert np.array_equal(trajs[1], trajs2[1])
+    gbl.close()
+    w.ps.dynamic.events[:] = []

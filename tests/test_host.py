@@ -1,0 +1,207 @@
+"""CPU tests of the host side: setup, descriptor export, the C-ABI library's
+symbols and its host-only symbolic analysis, and scenario sharding across
+ranks (gloo)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+from conftest import ROOT
+from helpers import LY, Case, M, psse, psse_case, synthetic
+
+HEADER = os.path.join(ROOT, "include", "gradpower_gb300.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import subprocess
+    import shutil
+    if shutil.which(os.environ.get("NVCC", "nvcc")) is None:
+        pytest.skip("nvcc not available")
+    from gradpower_gb300 import build, gpu
+    build.build()
+    return gpu.library()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = re.findall(r"^\w[\w\s\*]*?\b(gp_\w+)\(", open(HEADER).read(), re.M)
+    assert len(names) >= 10
+    for n in names:
+        assert hasattr(lib, n), n
+    assert lib.gp_abi_version() == 1
+
+
+def _reduced_S(ps, rng):
+    """A reduced matrix with the structure the library expects: -Ybus off the
+    diagonal blocks, random well-conditioned diagonal blocks."""
+    Y = ps.ybus.tocoo()
+    nb = ps.nbus
+    r, c, v = [], [], []
+    for i, j, y in zip(Y.row, Y.col, Y.data):
+        r += [2 * i, 2 * i, 2 * i + 1, 2 * i + 1]
+        c += [2 * j, 2 * j + 1, 2 * j, 2 * j + 1]
+        v += [-y.real, y.imag, -y.imag, -y.real]
+    for i in range(nb):
+        for a in range(2):
+            for b in range(2):
+                r.append(2 * i + a)
+                c.append(2 * i + b)
+                v.append(0.5 * rng.normal() + (3.0 if a == b else 0.0))
+    S = sp.csr_matrix((v, (r, c)), shape=(2 * nb, 2 * nb))
+    S.sum_duplicates()
+    S.sort_indices()
+    return S
+
+
+@pytest.mark.parametrize("name", ["two_bus", "ring39", "planar2k"])
+def test_reduced_factorisation_matches_scipy(lib, name):
+    """Symbolic analysis + front assembly + multifrontal LU/solves (host
+    emulation of the device kernels) against scipy's sparse LU."""
+    w = synthetic.WORKLOADS[name]()
+    PA = LY.ProblemArrays(w.ps)
+    P = PA.as_ctypes()
+    rng = np.random.default_rng(0)
+    S = _reduced_S(w.ps, rng)
+    rhs = rng.normal(size=S.shape[0])
+    x = np.zeros_like(rhs)
+    out = np.zeros(4)
+    rp, ci, sv = S.indptr.astype(np.int32), S.indices.astype(np.int32), S.data.astype(np.float64)
+    lib.gp_reduced_selftest.argtypes = [C.c_void_p] * 7
+    rc = lib.gp_reduced_selftest(C.addressof(P), rp.ctypes.data, ci.ctypes.data, sv.ctypes.data,
+                                 rhs.ctypes.data, x.ctypes.data, out.ctypes.data)
+    assert rc == 0
+    assert out[0] == 0.0 and out[1] == 0
+    xr = spla.spsolve(S.tocsc(), rhs)
+    assert np.max(np.abs(x - xr)) <= 1e-12 * np.max(np.abs(xr))
+
+
+def test_reduced_factorisation_with_static_generators(lib, golden_cases, orc):
+    """IEEE 9-bus with the slack machine (bus 1) and one PV machine (bus 2)
+    left without a dynamic model: StaticGenerator stand-ins add algebraic
+    states to the reduced system (PV: q; slack: p, q)."""
+    ps, dp = psse_case(golden_cases, "ieee9_v33.raw", "ieee9bus_gov.dyr", drop_dyr_gens=(1, 2))
+    PA = LY.ProblemArrays(ps)
+    kinds = [ps.dynamic.devices[i].dtype.bus_type for i in PA.tables[7].device_index]
+    assert sorted(kinds) == [2, 3]
+    # true reduced matrix from the oracle's Jacobian at a perturbed state
+    fa, nf = LY.fault_array([[]], 1 / 120)
+    z = dp.zvec + 1e-3 * np.random.default_rng(1).normal(size=dp.zvec.size)
+    J = orc.jacobian_dense(PA, z, dp.uvec, dp.pvec, fa, nf, np.zeros(1, np.uint8), 1 / 120)
+    net = PA.n_diff + PA.n_alg
+    red = [i for i in range(PA.n_sys) if i >= net]
+    sg_states = []
+    for k, i in enumerate(PA.tables[7].device_index):
+        rec = ps.dynamic.devices[i]
+        sg_states += list(range(rec.alg_ptr, rec.alg_ptr + rec.dtype.alg_size))
+    red_global = [net + j for j in range(2 * PA.n_bus)] + sg_states
+    w_idx = [i for i in range(net) if i not in set(sg_states)]
+    A = J[np.ix_(w_idx, w_idx)]
+    S = J[np.ix_(red_global, red_global)] - J[np.ix_(red_global, w_idx)] @ np.linalg.solve(A, J[np.ix_(w_idx, red_global)])
+    Ssp = sp.csr_matrix(np.where(np.abs(S) > 0, S, 0.0))
+    # keep the structural entries of the static generator coupling
+    Ssp.sort_indices()
+    rhs = np.random.default_rng(2).normal(size=len(red_global))
+    x = np.zeros_like(rhs)
+    out = np.zeros(4)
+    P = PA.as_ctypes()
+    rp, ci, sv = Ssp.indptr.astype(np.int32), Ssp.indices.astype(np.int32), Ssp.data.astype(np.float64)
+    lib.gp_reduced_selftest.argtypes = [C.c_void_p] * 7
+    assert lib.gp_reduced_selftest(C.addressof(P), rp.ctypes.data, ci.ctypes.data, sv.ctypes.data,
+                                   rhs.ctypes.data, x.ctypes.data, out.ctypes.data) == 0
+    assert out[0] < 1e-12
+    xr = np.linalg.solve(S, rhs)
+    assert np.max(np.abs(x - xr)) <= 1e-10 * np.max(np.abs(xr))
+
+
+def test_synthetic_sizes():
+    """Sizes of the benchmark grids (ring39: 228 unknowns, 461 parameters;
+    planar2k: cluster widths 15..27)."""
+    w = synthetic.ring39()
+    assert len(w.dp.zvec) == 228 and w.ps.dynamic.par_dim == 461 and len(w.faults) == 64
+    w2 = synthetic.planar2k()
+    widths = {c.w_size for c in w2.ps.dynamic.clusters}
+    assert widths == {15, 16, 18, 19, 23, 24, 26, 27}
+    assert len(w2.ps.branches) == 2700 and w2.n_scenarios == 256
+
+
+def test_julia_round_ties_to_even():
+    assert LY.jl_round(2.5) == 2 and LY.jl_round(3.5) == 4 and LY.jl_round(0.1 / (1 / 120)) == 12
+
+
+def test_fault_array_expansion():
+    evs = [[M.ContingencyEvent(1, 0.1, 0.1, 0.2)], [], [M.ContingencyEvent(0, 0.2, 0.05, 0.3)]]
+    arr, n = LY.fault_array(evs, 1 / 120, [M.ContingencyEvent(2, 0.5, 0.5, 0.6)])
+    rows = [(arr[k].scenario, arr[k].bus, arr[k].on_step, arr[k].off_step) for k in range(n)]
+    assert rows == [(-1, 2, 60, 72), (0, 1, 12, 24), (2, 0, 6, 36)]
+
+
+def test_psse_reader(golden_cases):
+    ps = psse.ps_from_records(golden_cases["raw"]["ieee9_v33.raw"])
+    assert ps.nbus == 9 and len(ps.gens) == 3 and len(ps.loads) == 3
+    assert len(ps.branches) == 9          # 6 lines + 3 transformers
+    assert ps.loads[0].qd < 0             # stored negated (src/parse.jl:384)
+    assert ps.buses[0].type == M.SLACK and ps.buses[0].v0m == 1.04
+
+
+def test_cluster_layout_matches_reference_order(golden_cases):
+    """Cluster-contiguous z: generator diff, generator alg, governor diff,
+    governor alg, ... then (vr, vi) per bus (src/clusters.jl:218-223)."""
+    ps, dp = psse_case(golden_cases, "ieee9_v33.raw", "ieee9bus_gov.dyr")
+    d = ps.dynamic
+    cl = d.clusters[0]
+    g, gv = d.devices[cl.gen], d.devices[cl.gov]
+    assert g.diff_ptr == cl.w_start and g.alg_ptr == cl.w_start + 6
+    assert gv.diff_ptr == cl.w_start + 10 and gv.alg_ptr == cl.w_start + 15
+    assert d.uvec_idx[g.ctrl_ptr + 1] == gv.alg_ptr       # p_m <- governor output
+    assert d.uvec_idx[gv.ctrl_ptr] == g.diff_ptr + 4      # governor reads w
+
+
+def _gloo_worker(rank, world, port, out_q):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from conftest import load_oracle, load_package
+    gp = load_package()
+    orc = load_oracle()
+    from gradpower_gb300 import gpu as G
+    w = gp.synthetic.ring39()
+    Mtot = 6
+    lo, hi = G.scenario_shard(Mtot, rank, world)
+    c = Case(w.ps, w.dp, w.faults[lo:hi], hi - lo)
+    z, u, p = c.arrays()
+    fa, nf = c.fault_array()
+    r = orc.integrate(c.PA, z, u, p, fa, nf, 1 / 120, 30, itermax=30)
+    parts = [None] * world
+    dist.all_gather_object(parts, (lo, hi, r["z"], r["iters"]))
+    if rank == 0:
+        out_q.put(parts)
+    dist.destroy_process_group()
+
+
+def test_scenario_sharding_gloo(orc):
+    """Scenarios shard across ranks with no exchange during the run; the
+    gathered result equals the single-process run (world size 2, gloo)."""
+    import multiprocessing as mp
+    import random
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = random.randint(20000, 40000)
+    procs = [ctx.Process(target=_gloo_worker, args=(r, 2, port, q)) for r in range(2)]
+    for pr in procs:
+        pr.start()
+    parts = q.get(timeout=240)
+    for pr in procs:
+        pr.join(timeout=60)
+    w = synthetic.ring39()
+    c = Case(w.ps, w.dp, w.faults[:6], 6)
+    z, u, p = c.arrays()
+    fa, nf = c.fault_array()
+    full = orc.integrate(c.PA, z, u, p, fa, nf, 1 / 120, 30, itermax=30)
+    for lo, hi, zf, it in parts:
+        assert np.array_equal(zf, full["z"][lo:hi])
+        assert np.array_equal(it, full["iters"][lo:hi])

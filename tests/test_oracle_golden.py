@@ -1,0 +1,184 @@
+"""Pin the CPU oracle against the reference's own tests and golden data.
+
+Each test names the reference test or fixture it restates.  These run on CPU
+only and gate every GPU parity test (which compares against this oracle).
+"""
+import numpy as np
+import pytest
+
+from helpers import DT, Case, M, case9_system, psse_case, run_oracle
+
+
+def test_case9_powerflow_vs_matpower(golden_known):
+    """test/test_pflow.jl:1-28: |V| and angle within rtol 1e-2 of MATPOWER."""
+    ps = case9_system(golden_known)
+    vm, va, _, _ = M.runpf(ps)
+    vmat = np.array([complex(a, b) for a, b in golden_known["case9_vmatpower"]])
+    assert np.allclose(np.abs(vmat), vm, rtol=1e-2)
+    assert np.allclose(np.angle(vmat), va, rtol=1e-2, atol=1e-4)
+    # the published MATPOWER values carry 4 decimals
+    assert np.max(np.abs(np.abs(vmat) - vm)) < 1e-4
+
+
+@pytest.mark.parametrize("raw,dyr", [("2bus.raw", "2bus.dyr"), ("ieee9_v33.raw", "ieee9bus_gov.dyr"),
+                                     ("2bus.raw", "2bus_ESDC1A.dyr"), ("2bus.raw", "2bus_SEXS.dyr"),
+                                     ("2bus.raw", "2bus_TGOV1.dyr"), ("2bus.raw", "2bus_IEESGO.dyr"),
+                                     ("ieee9_v33.raw", "ieee9bus_SEXS.dyr"),
+                                     ("ieee9_v33.raw", "ieee9bus_TGOV1.dyr")])
+def test_init_residual(orc, golden_cases, raw, dyr):
+    """test/test_integrate.jl:27-47 (and src/dynamics.jl:58): |f(z0)| < 1e-9."""
+    ps, dp = psse_case(golden_cases, raw, dyr)
+    c = Case(ps, dp)
+    fa, nf = c.fault_array()
+    f = orc.residual(c.PA, dp.zvec, dp.zvec, dp.uvec, dp.pvec, fa, nf, np.zeros(1), DT)
+    assert np.max(np.abs(f)) < 1e-9
+
+
+def test_ieee39_slack_generation_quirk(orc, golden_cases):
+    """runpf! sets slack generation to P_inj - P_load (src/pflow.jl:397-417);
+    IEEE39 has a load on its slack bus 39, so its z0 is not an equilibrium
+    there.  The restatement keeps that behaviour: the residual is non-zero
+    only on the slack bus rows."""
+    ps, dp = psse_case(golden_cases, "IEEE39.raw", "IEEE39.dyr")
+    c = Case(ps, dp)
+    fa, nf = c.fault_array()
+    f = orc.residual(c.PA, dp.zvec, dp.zvec, dp.uvec, dp.pvec, fa, nf, np.zeros(1), DT)
+    slack = ps.busmap[39]
+    net = c.PA.n_diff + c.PA.n_alg
+    rows = np.where(np.abs(f) > 1e-9)[0]
+    assert set(rows.tolist()) <= {net + 2 * slack, net + 2 * slack + 1}
+
+
+@pytest.mark.parametrize("raw,dyr", [("2bus.raw", "2bus.dyr"), ("ieee9_v33.raw", "ieee9bus_gov.dyr")])
+def test_flat_line(orc, golden_cases, raw, dyr):
+    """test/test_integrate.jl:49-66: no fault, 0.5 s, drift < 1e-5."""
+    ps, dp = psse_case(golden_cases, raw, dyr)
+    r = run_oracle(orc, Case(ps, dp), 60)
+    assert np.max(np.abs(r["traj"][0, -1] - dp.zvec)) < 1e-5
+    assert r["status"][0] == 0
+
+
+def test_reproducible(orc, golden_cases):
+    """test/test_integrate.jl:68-84: two identical runs are bit-identical."""
+    ps, dp = psse_case(golden_cases, "2bus.raw", "2bus.dyr")
+    c = Case(ps, dp, [[M.ContingencyEvent(0, 0.02, 0.1, 0.2)]])
+    a = run_oracle(orc, c, 120)
+    b = run_oracle(orc, c, 120)
+    assert np.array_equal(a["traj"], b["traj"])
+
+
+def test_fault_voltage_dip_and_spot_checks(orc, golden_cases):
+    """test/test_integrate.jl:86-155."""
+    ps, dp = psse_case(golden_cases, "2bus.raw", "2bus.dyr")
+    c = Case(ps, dp, [[M.ContingencyEvent(0, 0.02, 0.1, 0.2)]])
+    r = run_oracle(orc, c, 120)
+    nf = run_oracle(orc, Case(ps, dp), 60)
+    assert np.max(np.abs(r["traj"][0, :61] - nf["traj"][0])) > 0.01
+    net = c.PA.n_diff + c.PA.n_alg
+    t = np.arange(121) * DT
+    k = int(np.argmax(t >= 0.15))
+    vm = np.hypot(r["traj"][0, :, net], r["traj"][0, :, net + 1])
+    assert vm[k] < 0.9 * vm[0]
+    g = ps.dynamic.devices[0]
+    assert 0.5 < abs(r["traj"][0, -1, g.diff_ptr]) < 2.0
+    assert abs(r["traj"][0, -1, g.diff_ptr + 4]) < 0.1
+    ps9, dp9 = psse_case(golden_cases, "ieee9_v33.raw", "ieee9bus_gov.dyr")
+    c9 = Case(ps9, dp9, [[M.ContingencyEvent(0, 0.02, 0.1, 0.2)]])
+    r9 = run_oracle(orc, c9, 120)
+    for rec in ps9.dynamic.devices:
+        if rec.dtype.kind == "genrou":
+            assert abs(r9["traj"][0, -1, rec.diff_ptr + 4]) < 0.1
+        if rec.dtype.kind == "ieesgo":
+            assert r9["traj"][0, -1, rec.alg_ptr] > 0.0
+
+
+def test_dynamics_known_answers(orc, golden_cases, golden_known):
+    """test/test_dynamics.jl:21-28 (2-bus, fault on bus 2, r=0.2, 0.2-0.3 s,
+    final state at t = 1 s).  The reference asserts rtol 1e-2; the oracle
+    reproduces entries 1, 4 and 10 to better than 1e-9.  Entry 14 was
+    recorded with an earlier state layout (the test is no longer part of the
+    reference's suite) and is only checked to 3 %."""
+    kd = golden_known["dynamics_2bus"]
+    ps, dp = psse_case(golden_cases, "testdata/2bus.raw", "testdata/2bus.dyr", alpha=1.0)
+    bus, rf, ton, toff = kd["event"]
+    c = Case(ps, dp, [[M.ContingencyEvent(ps.busmap[bus], rf, ton, toff)]])
+    r = run_oracle(orc, c, int(round(kd["tfinal"] / DT)))
+    res = r["traj"][0, -1]
+    vals = {int(k): v for k, v in kd["values_1based"].items()}
+    for k in (1, 4, 10):
+        assert abs(res[k - 1] - vals[k]) <= 1e-9 * abs(vals[k])
+    assert abs(res[13] - vals[14]) <= 0.03 * abs(vals[14])
+
+
+def test_uqgrid_golden_trajectory(orc, golden_cases, golden_known):
+    """examples/refs/2bus_esdc1a.npz (scripts/gen_ref_2bus_esdc1a.py): an
+    independent simulator's rotor-speed trajectory for 2-bus GENROU+ESDC1A,
+    fault on bus 1, r=0.02, 0.2-0.3 s, alpha=0.5, 5 s."""
+    uq = golden_known["uqgrid_2bus_esdc1a"]
+    ps, dp = psse_case(golden_cases, "2bus.raw", "2bus_ESDC1A.dyr", alpha=uq["zipload_alpha"])
+    c = Case(ps, dp, [[M.ContingencyEvent(uq["fault_bus_index"], uq["rfault"], uq["ton"], uq["toff"])]])
+    ns = int(round(uq["tend"] / uq["dt"]))
+    r = run_oracle(orc, c, ns, dt=uq["dt"])
+    w = r["traj"][0, ::5, ps.dynamic.devices[0].diff_ptr + 4]
+    assert np.max(np.abs(w - np.array(uq["speed"]))) < 1e-9
+
+
+@pytest.mark.parametrize("raw,dyr", [("2bus.raw", "2bus_ESDC1A.dyr"), ("2bus.raw", "2bus_SEXS.dyr"),
+                                     ("2bus.raw", "2bus_TGOV1.dyr"), ("ieee9_v33.raw", "ieee9bus_gov.dyr")])
+def test_fd_jacobian(orc, golden_cases, raw, dyr):
+    """test/test_fd_jacobian.jl: analytic backward-Euler Jacobian against
+    central differences of the residual (< 1e-5), at a perturbed state with a
+    fault on."""
+    ps, dp = psse_case(golden_cases, raw, dyr)
+    c = Case(ps, dp, [[M.ContingencyEvent(0, 0.05, 0.1, 0.2)]])
+    fa, nf = c.fault_array()
+    on = np.ones(nf, dtype=np.uint8)
+    rng = np.random.default_rng(3)
+    z = dp.zvec + 1e-2 * rng.normal(size=dp.zvec.size)
+    J = orc.jacobian_dense(c.PA, z, dp.uvec, dp.pvec, fa, nf, on, DT)
+    n = z.size
+    Jfd = np.zeros((n, n))
+    for j in range(n):
+        h = 1e-6 * max(1.0, abs(z[j]))
+        zp = z.copy(); zp[j] += h
+        zm = z.copy(); zm[j] -= h
+        Jfd[:, j] = (orc.residual(c.PA, zp, dp.zvec, dp.uvec, dp.pvec, fa, nf, on, DT)
+                     - orc.residual(c.PA, zm, dp.zvec, dp.uvec, dp.pvec, fa, nf, on, DT)) / (2 * h)
+    assert np.max(np.abs(J - Jfd)) < 1e-5 * max(1.0, np.max(np.abs(J)))
+
+
+def test_fd_jacobian_synthetic_mix(orc):
+    """Same check on a small planar grid with the full model mix of the
+    benchmark grids (GENROU, GENSAL, SEXS, ESDC1A, IEEEST, IEESGO, TGOV1,
+    ZIP loads)."""
+    from helpers import synthetic
+    w = synthetic._planar("mix", 11, 120, 24, 0.6, 1, 0.5, "random")
+    kinds = {r.dtype.kind for r in w.ps.dynamic.devices}
+    assert {"genrou", "sexs", "esdc1a", "ieeest", "ieesgo", "tgov1", "zipload"} <= kinds
+    c = Case(w.ps, w.dp, w.faults)
+    fa, nf = c.fault_array()
+    on = np.ones(nf, dtype=np.uint8)
+    rng = np.random.default_rng(5)
+    z0 = w.dp.zvec
+    z = z0 + 1e-3 * rng.normal(size=z0.size)
+    J = orc.jacobian_dense(c.PA, z, w.dp.uvec, w.dp.pvec, fa, nf, on, DT)
+    n = z.size
+    Jfd = np.zeros((n, n))
+    for j in range(n):
+        h = 1e-6 * max(1.0, abs(z[j]))
+        zp = z.copy(); zp[j] += h
+        zm = z.copy(); zm[j] -= h
+        Jfd[:, j] = (orc.residual(c.PA, zp, z0, w.dp.uvec, w.dp.pvec, fa, nf, on, DT)
+                     - orc.residual(c.PA, zm, z0, w.dp.uvec, w.dp.pvec, fa, nf, on, DT)) / (2 * h)
+    assert np.max(np.abs(J - Jfd)) < 1e-5 * max(1.0, np.max(np.abs(J)))
+
+
+def test_monolithic_equals_schur(orc):
+    """Monolithic KLU path and Schur path give the same trajectories and the
+    same Newton counts (reference: integrate!(solver=:monolithic|:schur))."""
+    from helpers import synthetic_case
+    c, w = synthetic_case("planar2k", 2)
+    a = run_oracle(orc, c, 40, solver=0)
+    b = run_oracle(orc, c, 40, solver=1)
+    assert np.array_equal(a["iters"], b["iters"])
+    assert np.max(np.abs(a["traj"] - b["traj"])) < 1e-9
