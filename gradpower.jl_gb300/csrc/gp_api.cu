@@ -25,6 +25,7 @@
 #include "../../include/gradpower_gb300.h"
 #include "gp_internal.h"
 #include "gp_symbolic.h"
+#include "gp_cluster_plan.h"
 
 namespace {
 
@@ -119,6 +120,9 @@ struct gp_layout {
     double factor_launches = 0.0, solves = 0.0;
     double *z_init = nullptr;    // z0 as given to gp_layout_create
     int64_t sum_w2 = 0;
+    // sparse cluster factorisation
+    gp::ClusterPlan cplan;
+    gp::DevClu C{};
 };
 
 namespace {
@@ -595,6 +599,38 @@ void build_work(gp_layout *L, const double *z0, const double *u0, const double *
     ck(cudaMemcpy(L->z_init, W.z, M * P.n_sys * sizeof(double), cudaMemcpyDeviceToDevice), "z0 copy");
 }
 
+// Sparse cluster programs (gp_cluster_plan.cpp), uploaded with the cluster
+// indices translated to the compacted non-trivial cluster arrays.
+void build_clusters(gp_layout *L, const gp_problem *pr, const double *z0, const double *u0, const double *p) {
+    gp::ClusterPlan &cp = L->cplan;
+    gp::make_cluster_plan(pr, z0, u0, p, cp);
+    std::vector<int> compact(pr->n_clusters, -1);
+    int k = 0;
+    for (int c = 0; c < pr->n_clusters; c++)
+        if (pr->cl_gen[c] >= 0) compact[c] = k++;
+    std::vector<int> order(cp.order.size());
+    for (size_t q = 0; q < cp.order.size(); q++) order[q] = compact[cp.order[q]];
+    DeviceArena &A = L->arena;
+    gp::DevClu &C = L->C;
+    C.n_tasks = (int)cp.task_class.size();
+    C.task_class = A.upload(cp.task_class);
+    C.task_first = A.upload(cp.task_first);
+    C.task_count = A.upload(cp.task_count);
+    C.order = A.upload(order);
+    C.slot_of = A.upload(cp.slot_of);
+    C.prog_ptr = A.upload(cp.prog_ptr);
+    C.prog_mid = A.upload(cp.prog_mid);
+    C.ops = A.upload(cp.ops);
+    C.rhs_base = A.upload(cp.rhs_base);
+    C.nslot = A.upload(cp.nslot);
+    C.perm_col = A.upload(cp.perm_col);
+    C.pos3 = A.upload(cp.pos3);
+    C.max_slots = cp.max_slots;
+    const int bytes = cp.max_slots * 32 * (int)sizeof(double);
+    if (bytes > 48 * 1024 && gp::cluster_smem_optin(bytes) < 0)
+        fail(GP_E_CUDA, "cluster kernel needs %d bytes of shared memory", bytes);
+}
+
 void set_faults(gp_layout *L, int n_faults, const gp_fault *faults) {
     using namespace gp;
     L->call.release();
@@ -666,7 +702,7 @@ void enqueue_solve(gp_layout *L) {
 void enqueue_eval(gp_layout *L, double tol, int itermax) {
     gp::launch_reset_norm(L->P, L->W, L->st);
     mark(L, 0);
-    gp::launch_cluster(L->P, L->W, 0, L->st);
+    gp::launch_cluster(L->P, L->W, L->C, 0, L->st);
     mark(L, 1);
     gp::launch_network(L->P, L->W, 0, L->st);
     mark(L, 2);
@@ -776,6 +812,7 @@ int32_t gp_layout_create(const gp_problem *prob, int32_t M, const double *z0, co
     L->M = M;
     build_problem(L, prob);
     build_work(L, z0, u0, p);
+    build_clusters(L, prob, z0, u0, p);
     ck(cudaDeviceSynchronize(), "layout create");
     *out = L;
     L = nullptr;
@@ -869,7 +906,7 @@ int32_t gp_residual(gp_layout *L, const double *zold, double dt, int32_t n_fault
     ck(cudaMemcpy(L->W.dt, L->h_dt, sizeof(double), cudaMemcpyHostToDevice), "dt");
     ck(cudaMemset(L->W.active, 1, L->M), "memset");
     gp::launch_reset_norm(L->P, L->W, L->st);
-    gp::launch_cluster(L->P, L->W, 1, L->st);
+    gp::launch_cluster(L->P, L->W, L->C, 1, L->st);
     gp::launch_network(L->P, L->W, 1, L->st);
     ck(cudaGetLastError(), "residual launch");
     ck(cudaStreamSynchronize(L->st), "residual");
@@ -960,6 +997,38 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
     L->iters_total = tot;
     if (status) ck(cudaMemcpy(status, L->W.status, M * sizeof(int), cudaMemcpyDeviceToHost), "status copy");
     ck(cudaGetLastError(), "integrate");
+    API_END
+}
+
+int32_t gp_cluster_selftest(const gp_problem *prob, const double *z, const double *zold, const double *u0,
+                            const double *p, double dt, double *yx, double *clout, double *f, double out[4]) {
+    API_BEGIN
+    if (!prob || !z || !zold || !u0 || !p || !yx || !clout || !out) fail(GP_E_INVALID, "null argument");
+    Plan pl;
+    make_plan(prob, pl);
+    gp::ClusterPlan cp;
+    gp::make_cluster_plan(prob, z, u0, p, cp);
+    const int n_da = prob->n_diff + prob->n_alg;
+    double fmax = 0.0;
+    int k = 0;
+    std::vector<double> buf(96), fl(32);
+    for (int c = 0; c < prob->n_clusters; c++) {
+        if (prob->cl_gen[c] < 0) continue;
+        const int W = prob->cl_w_size[c], ws = prob->cl_w_start[c];
+        const double fm = gp::host_cluster_run(prob, cp, c, z, zold, u0, p, dt, buf.data(), clout + 8 * k, fl.data());
+        fmax = std::max(fmax, fm);
+        for (int j = 0; j < W; j++) {
+            yx[ws + j] = buf[j];
+            yx[n_da + ws + j] = buf[W + j];
+            yx[2 * n_da + ws + j] = buf[2 * W + j];
+            if (f) f[ws + j] = fl[j];
+        }
+        k++;
+    }
+    out[0] = fmax;
+    out[1] = cp.n_class;
+    out[2] = (double)cp.lu_flops;
+    out[3] = cp.max_slots;
     API_END
 }
 

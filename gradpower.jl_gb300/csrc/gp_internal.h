@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "gp_devices.cuh"
+
 namespace gp {
 
 // Struct-of-arrays device table on the GPU (see gp_device_table).
@@ -71,8 +73,26 @@ struct DevSym {
     int *ipiv;                        // [M][n] pivot row within the supernode, per column
 };
 
+// Sparse cluster factorisation plan: clusters grouped into classes with
+// identical local Jacobian pattern; each class carries a straight-line
+// program (backward-Euler scaling, static-pivot LU, three solves).
+struct DevClu {
+    int n_tasks;                // warp tasks: up to 32 clusters of one class
+    const int *task_class, *task_first, *task_count;
+    const int *order;           // cluster indices (into the P.cl_* arrays) grouped by class
+    const short *slot_of;       // [class][32*32] slot of local entry (r, c); c = 29/30 B, 31 f
+    const int *prog_ptr;        // [n_class+1]
+    const int *prog_mid;        // [n_class] first op of the factorisation part
+    const CluOp *ops;
+    const int *rhs_base;        // [n_class] first right-hand-side slot
+    const int *nslot;           // [n_class] slots used (values + pivots + 3 W)
+    const int *perm_col;        // [class][32] state (local) of solution position j
+    const int *pos3;            // [class][3] solution positions of delta, i_q, i_d
+    int max_slots;
+};
+
 // launches (gp_kernels.cu)
-void launch_cluster(const DevProblem &P, const DevWork &W, int want_f, cudaStream_t st);
+void launch_cluster(const DevProblem &P, const DevWork &W, const DevClu &C, int want_f, cudaStream_t st);
 void launch_network(const DevProblem &P, const DevWork &W, int want_f, cudaStream_t st);
 void launch_check(const DevProblem &P, const DevWork &W, double tol, int itermax, cudaStream_t st);
 void launch_reset_norm(const DevProblem &P, const DevWork &W, cudaStream_t st);
@@ -87,5 +107,6 @@ void launch_events(const DevProblem &P, const DevWork &W, const int *fl_on_step,
                    const int *fl_scen, uint8_t *fl_on, int n_fl, int step, cudaStream_t st);
 void launch_snapshot(const double *z, double *traj, int M, int n_sys, int n_steps, int k, cudaStream_t st);
 int factor_smem_limit();
+int cluster_smem_optin(int bytes);
 
 }  // namespace gp

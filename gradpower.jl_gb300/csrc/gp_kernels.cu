@@ -28,12 +28,12 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "gp_devices.cuh"
 #include "gp_internal.h"
 
 namespace gp {
 
 #define FULL_MASK 0xffffffffu
-constexpr double TWOPI60 = 2.0 * 3.14159265358979323846 * 60.0;
 
 // ---------------------------------------------------------------------------
 // helpers
@@ -45,448 +45,174 @@ __device__ __forceinline__ unsigned long long norm_bits(double v) {
     return (unsigned long long)__double_as_longlong(fabs(v));
 }
 
-// Cluster matrix in shared memory: row = state - ws, columns 0..28 the
-// cluster states, 29/30 the bus voltage (vr, vi), 31 the residual.
-constexpr int LDM = 32;
-constexpr int WMAX = 29;
-constexpr int COL_VR = 29, COL_VI = 30, COL_F = 31;
-constexpr int CK_WARPS = 4;
+// ---------------------------------------------------------------------------
+// cluster kernel: one lane per (cluster, scenario), 32 clusters of one
+// pattern class per warp; the class program does the backward-Euler scaling,
+// the static-pivot sparse LU and the solves for [B(:,vr) B(:,vi) f].
+// ---------------------------------------------------------------------------
 
-struct CMat {
-    double *A;
-    int ws;
-    __device__ __forceinline__ void put(int r, int c, double v) const { A[(r - ws) * LDM + (c - ws)] = v; }
-    __device__ __forceinline__ void putv(int r, int which, double v) const { A[(r - ws) * LDM + COL_VR + which] = v; }
-    __device__ __forceinline__ void putf(int r, double v) const { A[(r - ws) * LDM + COL_F] = v; }
+struct LaneSink {
+    double *v;             // vals[slot * 32 + lane]
+    const short *slot_of;  // class map, local (r, c) -> slot
+    int ws, lane;
+    __device__ __forceinline__ void put(int r, int c, double x) {
+        v[(int)slot_of[(r - ws) * 32 + (c - ws)] * 32 + lane] = x;
+    }
+    __device__ __forceinline__ void putv(int r, int k, double x) {
+        v[(int)slot_of[(r - ws) * 32 + 29 + k] * 32 + lane] = x;
+    }
+    __device__ __forceinline__ void putf(int r, double x) { v[(int)slot_of[(r - ws) * 32 + 31] * 32 + lane] = x; }
 };
 
-__device__ __forceinline__ void genrou_sat_coef(double s1, double s2, double &sa, double &sb) {
-    sa = 0.0;
-    sb = 0.0;
-    if (s1 <= 0.0 || s2 <= 0.0) return;
-    const double e1 = 1.0, e2 = 1.2;
-    double a = sqrt(s1 * e1 / (s2 * e2));
-    if (a == 1.0) return;
-    sa = e2 - (e1 - e2) / (a - 1.0);
-    sb = s2 * e2 * (a - 1.0) * (a - 1.0) / ((e1 - e2) * (e1 - e2));
+__device__ __forceinline__ DevRef devref(const DTab &T, int k) {
+    DevRef d;
+    d.dp = T.diff_ptr[k];
+    d.ap = T.alg_ptr[k];
+    d.cp = T.ctrl_ptr[k];
+    d.pp = T.par_ptr[k];
+    d.bus = T.bus[k];
+    d.link0 = T.link0[k];
+    d.link1 = T.link1[k];
+    return d;
 }
 
-// GENROU residual rows + Jacobian (src/kernels/genrou.jl:48-141, 407-559).
-// Returns the network-row couplings C (d f_vr/d{delta,i_q,i_d},
-// d f_vi/d{delta,i_q,i_d}) and the injected current.
-__device__ void genrou_eval(const DevProblem &P, int k, const double *z, const double *u0, const double *p,
-                            const CMat &M, double *C, double *I, int *loc) {
-    const DTab &G = P.dev[0];
-    const int dp = G.diff_ptr[k], ap = G.alg_ptr[k], cp = G.ctrl_ptr[k], pp = G.par_ptr[k], bus = G.bus[k];
-    const double x_d = p[pp], x_q = p[pp + 1], x_dp = p[pp + 2], x_qp = p[pp + 3], x_ddp = p[pp + 4],
-                 xl = p[pp + 5], H = p[pp + 6], D = p[pp + 7], T_d0p = p[pp + 8], T_q0p = p[pp + 9],
-                 T_d0dp = p[pp + 10], T_q0dp = p[pp + 11], S1 = p[pp + 12], S2 = p[pp + 13];
-    const double x_qdp = x_ddp;
-    const double e_qp = z[dp], e_dp = z[dp + 1], phi_1d = z[dp + 2], phi_2q = z[dp + 3], w = z[dp + 4],
-                 delta = z[dp + 5];
-    const double v_q = z[ap], v_d = z[ap + 1], i_q = z[ap + 2], i_d = z[ap + 3];
-    const int vr_idx = P.net + 2 * bus;
-    const double vr = z[vr_idx], vi = z[vr_idx + 1];
-    const int pm_idx = G.link0[k], efd_idx = G.link1[k];
-    const double e_fd = efd_idx >= 0 ? z[efd_idx] : u0[cp];
-    const double p_m = pm_idx >= 0 ? z[pm_idx] : u0[cp + 1];
-    const double dpl = x_dp - xl, qpl = x_qp - xl;
-    const double psi_de = (x_ddp - xl) / dpl * e_qp + (x_dp - x_ddp) / dpl * phi_1d;
-    const double psi_qe = -(x_ddp - xl) / qpl * e_dp + (x_qp - x_ddp) / qpl * phi_2q;
-    double sa, sb;
-    genrou_sat_coef(S1, S2, sa, sb);
-    const double psi2 = sqrt(psi_de * psi_de + psi_qe * psi_qe);
-    const bool sat_on = !(sb == 0.0 || psi2 <= sa || psi2 == 0.0);
-    const double Se = sat_on ? sb * (psi2 - sa) * (psi2 - sa) / psi2 : 0.0;
-    double sd, cd;
-    sincos(delta, &sd, &cd);
-    // residual
-    M.putf(dp, (-e_qp + e_fd - (i_d - (-x_ddp + x_dp) * (-e_qp + i_d * dpl + phi_1d) / (dpl * dpl)) * (x_d - x_dp) -
-                Se * psi_de) / T_d0p);
-    M.putf(dp + 1, (-e_dp + (i_q - (-x_qdp + x_qp) * (e_dp + i_q * qpl + phi_2q) / (qpl * qpl)) * (x_q - x_qp)) / T_q0p);
-    M.putf(dp + 2, (e_qp - i_d * dpl - phi_1d) / T_d0dp);
-    M.putf(dp + 3, (-e_dp - i_q * qpl - phi_2q) / T_q0dp);
-    M.putf(dp + 4, (p_m - D * w - psi_de * i_q + psi_qe * i_d) / (2.0 * H));
-    M.putf(dp + 5, TWOPI60 * w);
-    M.putf(ap, i_d - ((x_ddp - xl) / dpl * e_qp + (x_dp - x_ddp) / dpl * phi_1d - v_q) / x_ddp);
-    M.putf(ap + 1, i_q - (-(x_qdp - xl) / qpl * e_dp + (x_qp - x_qdp) / qpl * phi_2q + v_d) / x_qdp);
-    M.putf(ap + 2, v_d - (vr * sd - vi * cd));
-    M.putf(ap + 3, v_q - (vr * cd + vi * sd));
-    // Jacobian
-    double dSe = 0.0;
-    if (sat_on) {
-        double g = psi2 - sa;
-        dSe = sb * (2.0 * g * psi2 - g * g) / (psi2 * psi2);
-    }
-    const double dpd = psi2 == 0.0 ? 0.0 : psi_de / psi2;
-    const double dpq = psi2 == 0.0 ? 0.0 : psi_qe / psi2;
-    const double a_eqp = (x_ddp - xl) / dpl, a_phi1d = (x_dp - x_ddp) / dpl;
-    const double b_edp = -(x_ddp - xl) / qpl, b_phi2q = (x_qp - x_ddp) / qpl;
-    const double dT_dde = -(dSe * dpd * psi_de + Se);
-    const double dT_dqe = -(dSe * dpq * psi_de);
-    const int c_eqp = dp, c_edp = dp + 1, c_phi1d = dp + 2, c_phi2q = dp + 3, c_w = dp + 4, c_delta = dp + 5;
-    const int c_vq = ap, c_vd = ap + 1, c_iq = ap + 2, c_id = ap + 3;
-    M.put(dp, c_eqp, (-(x_d - x_dp) * (-x_ddp + x_dp) / (dpl * dpl) - 1) / T_d0p + dT_dde * a_eqp / T_d0p);
-    M.put(dp, c_phi1d, (x_d - x_dp) * (-x_ddp + x_dp) / (dpl * dpl) / T_d0p + dT_dde * a_phi1d / T_d0p);
-    M.put(dp, c_id, -(x_d - x_dp) * (-(-x_ddp + x_dp) / dpl + 1) / T_d0p);
-    M.put(dp, c_edp, dT_dqe * b_edp / T_d0p);
-    M.put(dp, c_phi2q, dT_dqe * b_phi2q / T_d0p);
-    if (efd_idx >= 0) M.put(dp, efd_idx, 1.0 / T_d0p);
-    M.put(dp + 1, c_edp, (-(x_q - x_qp) * (-x_qdp + x_qp) / (qpl * qpl) - 1) / T_q0p);
-    M.put(dp + 1, c_phi2q, -(x_q - x_qp) * (-x_qdp + x_qp) / (qpl * qpl) / T_q0p);
-    M.put(dp + 1, c_iq, (x_q - x_qp) * (-(-x_qdp + x_qp) / qpl + 1) / T_q0p);
-    M.put(dp + 2, c_eqp, 1.0 / T_d0dp);
-    M.put(dp + 2, c_phi1d, -1.0 / T_d0dp);
-    M.put(dp + 2, c_id, (-x_dp + xl) / T_d0dp);
-    M.put(dp + 3, c_edp, -1.0 / T_q0dp);
-    M.put(dp + 3, c_phi2q, -1.0 / T_q0dp);
-    M.put(dp + 3, c_iq, (-x_qp + xl) / T_q0dp);
-    M.put(dp + 4, c_eqp, -0.5 * i_q * (x_ddp - xl) / (H * dpl));
-    M.put(dp + 4, c_edp, 0.5 * i_d * (-x_ddp + xl) / (H * qpl));
-    M.put(dp + 4, c_phi1d, -0.5 * i_q * (-x_ddp + x_dp) / (H * dpl));
-    M.put(dp + 4, c_phi2q, 0.5 * i_d * (-x_ddp + x_qp) / (H * qpl));
-    M.put(dp + 4, c_w, -0.5 * D / H);
-    if (pm_idx >= 0) M.put(dp + 4, pm_idx, 0.5 / H);
-    M.put(dp + 4, c_iq, 0.5 * (-e_qp * (x_ddp - xl) / dpl - phi_1d * (-x_ddp + x_dp) / dpl) / H);
-    M.put(dp + 4, c_id, 0.5 * (e_dp * (-x_ddp + xl) / qpl + phi_2q * (-x_ddp + x_qp) / qpl) / H);
-    M.put(dp + 5, c_w, TWOPI60);
-    M.put(ap, c_eqp, -(x_ddp - xl) / (x_ddp * dpl));
-    M.put(ap, c_phi1d, -(-x_ddp + x_dp) / (x_ddp * dpl));
-    M.put(ap, c_vq, 1.0 / x_ddp);
-    M.put(ap, c_id, 1.0);
-    M.put(ap + 1, c_edp, -(-x_qdp + xl) / (x_qdp * qpl));
-    M.put(ap + 1, c_phi2q, -(-x_qdp + x_qp) / (x_qdp * qpl));
-    M.put(ap + 1, c_vd, -1.0 / x_qdp);
-    M.put(ap + 1, c_iq, 1.0);
-    M.put(ap + 2, c_delta, -vr * cd - vi * sd);
-    M.put(ap + 2, c_vd, 1.0);
-    M.putv(ap + 2, 0, -sd);
-    M.putv(ap + 2, 1, cd);
-    M.put(ap + 3, c_delta, vr * sd - vi * cd);
-    M.put(ap + 3, c_vq, 1.0);
-    M.putv(ap + 3, 0, -cd);
-    M.putv(ap + 3, 1, -sd);
-    // network coupling (not part of the cluster block)
-    C[0] = i_d * cd - i_q * sd;
-    C[1] = cd;
-    C[2] = sd;
-    C[3] = i_d * sd + i_q * cd;
-    C[4] = sd;
-    C[5] = -cd;
-    I[0] = sd * i_d + cd * i_q;
-    I[1] = -cd * i_d + sd * i_q;
-    loc[0] = c_delta - M.ws;
-    loc[1] = c_iq - M.ws;
-    loc[2] = c_id - M.ws;
-}
-
-// IEESGO (src/kernels/ieesgo.jl:133-224)
-__device__ void ieesgo_eval(const DevProblem &P, int k, const double *z, const double *p, const CMat &M) {
-    const DTab &T = P.dev[1];
-    const int dp = T.diff_ptr[k], ap = T.alg_ptr[k], pp = T.par_ptr[k], wi = T.link0[k];
-    const double T1 = p[pp], T2 = p[pp + 1], T3 = p[pp + 2], T4 = p[pp + 3], T5 = p[pp + 4], T6 = p[pp + 5];
-    const double K1 = p[pp + 6], K2 = p[pp + 7], K3 = p[pp + 8], pref = p[pp + 11];
-    const double PF0 = z[dp], PLL = z[dp + 1], TP1 = z[dp + 2], TP2 = z[dp + 3], TP3 = z[dp + 4], p_m = z[ap];
-    const double w = wi < 0 ? 0.0 : z[wi];
-    M.putf(dp, (1.0 / T1) * (K1 * w - PF0));
-    M.putf(dp + 1, (1.0 / T3) * ((1.0 - (T2 / T3)) * PF0 - PLL));
-    const double SatP = pref - (T2 / T3) * PF0 - PLL;
-    M.putf(dp + 2, (1.0 / T4) * (SatP - TP1));
-    M.putf(dp + 3, (1.0 / T5) * (K2 * TP1 - TP2));
-    M.putf(dp + 4, (1.0 / T6) * (K3 * TP2 - TP3));
-    M.putf(ap, TP1 * (1.0 - K2) + TP2 * (1.0 - K3) + TP3 - p_m);
-    M.put(dp, dp, -1.0 / T1);
-    if (wi >= 0) M.put(dp, wi, K1 / T1);
-    M.put(dp + 1, dp, (1.0 - T2 / T3) / T3);
-    M.put(dp + 1, dp + 1, -1.0 / T3);
-    M.put(dp + 2, dp, -T2 / (T3 * T4));
-    M.put(dp + 2, dp + 1, -1.0 / T4);
-    M.put(dp + 2, dp + 2, -1.0 / T4);
-    M.put(dp + 3, dp + 2, K2 / T5);
-    M.put(dp + 3, dp + 3, -1.0 / T5);
-    M.put(dp + 4, dp + 3, K3 / T6);
-    M.put(dp + 4, dp + 4, -1.0 / T6);
-    M.put(ap, dp + 2, 1.0 - K2);
-    M.put(ap, dp + 3, 1.0 - K3);
-    M.put(ap, dp + 4, 1.0);
-    M.put(ap, ap, -1.0);
-}
-
-// TGOV1 (src/kernels/tgov1.jl:73-146)
-__device__ void tgov1_eval(const DevProblem &P, int k, const double *z, const double *p, const CMat &M) {
-    const DTab &T = P.dev[2];
-    const int dp = T.diff_ptr[k], ap = T.alg_ptr[k], pp = T.par_ptr[k], wi = T.link0[k];
-    const double R = p[pp], T1 = p[pp + 1], T2 = p[pp + 4], T3 = p[pp + 5], DT = p[pp + 6], pref = p[pp + 7];
-    const double x1 = z[dp], x2 = z[dp + 1], p_m = z[ap];
-    const double w = wi < 0 ? 0.0 : z[wi];
-    const double r23 = T2 / T3;
-    M.putf(dp, (-x1 + (1.0 - r23) * x2) / T3);
-    M.putf(dp + 1, ((pref - w) / R - x2) / T1);
-    M.putf(ap, x1 + r23 * x2 - DT * w - p_m);
-    M.put(dp, dp, -1.0 / T3);
-    M.put(dp, dp + 1, (1.0 - r23) / T3);
-    M.put(dp + 1, dp + 1, -1.0 / T1);
-    if (wi >= 0) M.put(dp + 1, wi, -1.0 / (R * T1));
-    M.put(ap, dp, 1.0);
-    M.put(ap, dp + 1, r23);
-    if (wi >= 0) M.put(ap, wi, -DT);
-    M.put(ap, ap, -1.0);
-}
-
-// SEXS (src/kernels/sexs.jl:74-156)
-__device__ void sexs_eval(const DevProblem &P, int k, const double *z, const double *p, const CMat &M) {
-    const DTab &T = P.dev[3];
-    const int dp = T.diff_ptr[k], pp = T.par_ptr[k], vsi = T.link0[k];
-    const int vr_idx = P.net + 2 * T.bus[k];
-    const double TA_TB = p[pp], TB = p[pp + 1], K = p[pp + 2], TE = p[pp + 3], vref = p[pp + 6];
-    const double x1 = z[dp], e_fd = z[dp + 1], vr = z[vr_idx], vi = z[vr_idx + 1];
-    double vm = sqrt(vr * vr + vi * vi);
-    vm = vm == 0.0 ? 1e-12 : vm;
-    const double vs = vsi >= 0 ? z[vsi] : 0.0;
-    const double err = vref - vm + vs;
-    M.putf(dp, (-x1 + (1.0 - TA_TB) * err) / TB);
-    M.putf(dp + 1, (-e_fd + K * (x1 + TA_TB * err)) / TE);
-    const double dvr = vr / vm, dvi = vi / vm;
-    M.put(dp, dp, -1.0 / TB);
-    M.putv(dp, 0, -(1.0 - TA_TB) * dvr / TB);
-    M.putv(dp, 1, -(1.0 - TA_TB) * dvi / TB);
-    if (vsi >= 0) M.put(dp, vsi, (1.0 - TA_TB) / TB);
-    M.put(dp + 1, dp, K / TE);
-    M.put(dp + 1, dp + 1, -1.0 / TE);
-    M.putv(dp + 1, 0, -K * TA_TB * dvr / TE);
-    M.putv(dp + 1, 1, -K * TA_TB * dvi / TE);
-    if (vsi >= 0) M.put(dp + 1, vsi, K * TA_TB / TE);
-}
-
-// ESDC1A (src/kernels/esdc1a.jl:97-196)
-__device__ void esdc1a_eval(const DevProblem &P, int k, const double *z, const double *p, const CMat &M) {
-    const DTab &T = P.dev[4];
-    const int dp = T.diff_ptr[k], pp = T.par_ptr[k], vsi = T.link0[k];
-    const int vr_idx = P.net + 2 * T.bus[k];
-    const double Ka = p[pp], Ta = p[pp + 1], Kf = p[pp + 2], Tf = p[pp + 3], Ke = p[pp + 4], Te = p[pp + 5];
-    const double sat_a = p[pp + 7], sat_b = p[pp + 8], vref = p[pp + 9];
-    const double vr1 = z[dp], vr2 = z[dp + 1], e_fd = z[dp + 2], vr = z[vr_idx], vi = z[vr_idx + 1];
-    double vm = sqrt(vr * vr + vi * vi);
-    vm = vm == 0.0 ? 1e-12 : vm;
-    const double vs = vsi >= 0 ? z[vsi] : 0.0;
-    const bool son = !(sat_b == 0.0 || e_fd <= sat_a);
-    const double sat = son ? sat_b * (e_fd - sat_a) * (e_fd - sat_a) : 0.0;
-    M.putf(dp, (Ka * (vref - vm + vs - vr2 - (Kf / Tf) * e_fd) - vr1) / Ta);
-    M.putf(dp + 1, -((Kf / Tf) * e_fd + vr2) / Tf);
-    M.putf(dp + 2, (vr1 - Ke * e_fd - sat) / Te);
-    const double dvr = vr / vm, dvi = vi / vm;
-    const double dsat = son ? 2.0 * sat_b * (e_fd - sat_a) : 0.0;
-    M.put(dp, dp, -1.0 / Ta);
-    M.put(dp, dp + 1, -Ka / Ta);
-    M.put(dp, dp + 2, -Ka * Kf / (Ta * Tf));
-    M.putv(dp, 0, -Ka * dvr / Ta);
-    M.putv(dp, 1, -Ka * dvi / Ta);
-    if (vsi >= 0) M.put(dp, vsi, Ka / Ta);
-    M.put(dp + 1, dp + 1, -1.0 / Tf);
-    M.put(dp + 1, dp + 2, -Kf / (Tf * Tf));
-    M.put(dp + 2, dp, 1.0 / Te);
-    M.put(dp + 2, dp + 2, -(Ke + dsat) / Te);
-}
-
-// IEEEST (src/kernels/ieeest.jl:207-359)
-__device__ void ieeest_eval(const DevProblem &P, int k, const double *z, const double *p, const CMat &M) {
-    const DTab &T = P.dev[5];
-    const int dp = T.diff_ptr[k], ap = T.alg_ptr[k], pp = T.par_ptr[k], wi = T.link0[k];
-    const double A1 = p[pp], A2 = p[pp + 1], A3 = p[pp + 2], A4 = p[pp + 3], A5 = p[pp + 4], A6 = p[pp + 5];
-    const double T1 = p[pp + 6], T2 = p[pp + 7], T3 = p[pp + 8], T4 = p[pp + 9], T5 = p[pp + 10], T6 = p[pp + 11],
-                 KS = p[pp + 12];
-    const double s0 = z[dp], s1 = z[dp + 1], s2 = z[dp + 2], s3 = z[dp + 3], s4 = z[dp + 4], s5 = z[dp + 5],
-                 s6 = z[dp + 6], vs = z[ap];
-    const double sig = wi >= 0 ? z[wi] : 0.0;
-    const double q = s1 - s3 - A3 * s2;
-    const double y2 = s3 + A5 * s2 + (A6 / A4) * q;
-    const double y3 = s4 + (T1 / T2) * (y2 - s4);
-    const double y4 = s5 + (T3 / T4) * (y3 - s5);
-    M.putf(dp, (sig - s1 - A1 * s0) / A2);
-    M.putf(dp + 1, s0);
-    M.putf(dp + 2, (s1 - s3 - A3 * s2) / A4);
-    M.putf(dp + 3, s2);
-    M.putf(dp + 4, (y2 - s4) / T2);
-    M.putf(dp + 5, (y3 - s5) / T4);
-    M.putf(dp + 6, (KS * y4 - s6) / T6);
-    M.putf(ap, vs - (T5 / T6) * (KS * y4 - s6));
-    const double rA = A6 / A4;
-    const double d2[3] = {rA, A5 - A3 * rA, 1.0 - rA};
-    const double r12 = T1 / T2;
-    const double d3[4] = {r12 * d2[0], r12 * d2[1], r12 * d2[2], 1.0 - r12};
-    const double r34 = T3 / T4;
-    const double d4[5] = {r34 * d3[0], r34 * d3[1], r34 * d3[2], r34 * d3[3], 1.0 - r34};
-    M.put(dp, dp, -A1 / A2);
-    M.put(dp, dp + 1, -1.0 / A2);
-    if (wi >= 0) M.put(dp, wi, 1.0 / A2);
-    M.put(dp + 1, dp, 1.0);
-    M.put(dp + 2, dp + 1, 1.0 / A4);
-    M.put(dp + 2, dp + 2, -A3 / A4);
-    M.put(dp + 2, dp + 3, -1.0 / A4);
-    M.put(dp + 3, dp + 2, 1.0);
-#pragma unroll
-    for (int j = 0; j < 3; j++) M.put(dp + 4, dp + 1 + j, d2[j] / T2);
-    M.put(dp + 4, dp + 4, -1.0 / T2);
-#pragma unroll
-    for (int j = 0; j < 4; j++) M.put(dp + 5, dp + 1 + j, d3[j] / T4);
-    M.put(dp + 5, dp + 5, -1.0 / T4);
-#pragma unroll
-    for (int j = 0; j < 5; j++) M.put(dp + 6, dp + 1 + j, KS * d4[j] / T6);
-    M.put(dp + 6, dp + 6, -1.0 / T6);
-    const double r56 = T5 / T6;
-#pragma unroll
-    for (int j = 0; j < 5; j++) M.put(ap, dp + 1 + j, -r56 * KS * d4[j]);
-    M.put(ap, dp + 6, r56);
-    M.put(ap, ap, 1.0);
-}
-
-// ---------------------------------------------------------------------------
-// cluster kernel
-// ---------------------------------------------------------------------------
-
-__global__ void __launch_bounds__(CK_WARPS * 32) cluster_kernel(DevProblem P, DevWork W, int want_f) {
-    __shared__ double sA[CK_WARPS][WMAX * LDM];
-    __shared__ double sC[CK_WARPS][8];
-    __shared__ int sLoc[CK_WARPS][3];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const long long task = (long long)blockIdx.x * CK_WARPS + warp;
-    if (task >= (long long)P.M * P.n_cl) return;
-    const int m = (int)(task / P.n_cl), c = (int)(task % P.n_cl);
+__global__ void __launch_bounds__(32) cluster_kernel(DevProblem P, DevWork W, DevClu Cl, int want_f) {
+    extern __shared__ double vals[];
+    const int task = blockIdx.x, m = blockIdx.y, lane = threadIdx.x;
     if (!W.active[m]) return;
+    const int cls = Cl.task_class[task];
+    const int cnt = Cl.task_count[task];
+    const bool act = lane < cnt;
+    const int c = act ? Cl.order[Cl.task_first[task] + lane] : Cl.order[Cl.task_first[task]];
     const int ws = P.cl_w_start[c], Wn = P.cl_w_size[c];
+    const int nslot = Cl.nslot[cls];
+    for (int s = 0; s < nslot; s++) vals[s * 32 + lane] = 0.0;
     const double *z = W.z + (size_t)m * P.n_sys;
     const double *zold = W.zold + (size_t)m * P.n_sys;
     const double *u0 = W.u0 + (size_t)m * P.n_ctrl;
     const double *p = W.p + (size_t)m * P.n_par;
-    double *A = sA[warp];
-    for (int i = lane; i < Wn * LDM; i += 32) A[i] = 0.0;
-    __syncwarp();
-    CMat Mx{A, ws};
-    if (lane == 0) {
-        genrou_eval(P, P.cl_gen[c], z, u0, p, Mx, sC[warp], sC[warp] + 6, sLoc[warp]);
-    } else if (lane == 1) {
+    LaneSink sink{vals, Cl.slot_of + (size_t)cls * 1024, ws, lane};
+    double Cc[6] = {0, 0, 0, 0, 0, 0}, Ic[2] = {0, 0};
+    if (act) {
+        genrou_eval(devref(P.dev[0], P.cl_gen[c]), P.net, z, u0, p, sink, Cc, Ic);
         const int gt = P.cl_gov_type[c];
-        if (gt == 1) ieesgo_eval(P, P.cl_gov[c], z, p, Mx);
-        else if (gt == 2) tgov1_eval(P, P.cl_gov[c], z, p, Mx);
-    } else if (lane == 2) {
+        if (gt == 1) ieesgo_eval(devref(P.dev[1], P.cl_gov[c]), z, p, sink);
+        else if (gt == 2) tgov1_eval(devref(P.dev[2], P.cl_gov[c]), z, p, sink);
         const int et = P.cl_exc_type[c];
-        if (et == 3) sexs_eval(P, P.cl_exc[c], z, p, Mx);
-        else if (et == 4) esdc1a_eval(P, P.cl_exc[c], z, p, Mx);
-    } else if (lane == 3) {
-        if (P.cl_pss[c] >= 0) ieeest_eval(P, P.cl_pss[c], z, p, Mx);
+        if (et == 3) sexs_eval(devref(P.dev[3], P.cl_exc[c]), P.net, z, p, sink);
+        else if (et == 4) esdc1a_eval(devref(P.dev[4], P.cl_exc[c]), P.net, z, p, sink);
+        if (P.cl_pss[c] >= 0) ieeest_eval(devref(P.dev[5], P.cl_pss[c]), z, p, sink);
+    } else {
+        // idle lanes factor an identity so that no lane divides by zero
+        const CluOp *o = Cl.ops + Cl.prog_ptr[cls];
+        for (int q = Cl.prog_mid[cls] - Cl.prog_ptr[cls]; q < Cl.prog_ptr[cls + 1] - Cl.prog_ptr[cls]; q++)
+            if (o[q].code == OP_RCP) vals[o[q].a * 32 + lane] = 1.0;
     }
-    __syncwarp();
-    const bool has_row = lane < Wn;
-    double a[LDM];
-#pragma unroll
-    for (int j = 0; j < LDM; j++) a[j] = has_row ? A[lane * LDM + j] : 0.0;
-    // backward Euler on differential rows
     const double dt = *W.dt;
-    if (has_row && P.is_diff[ws + lane]) {
-#pragma unroll
-        for (int j = 0; j < COL_F; j++) a[j] *= -dt;
-#pragma unroll
-        for (int j = 0; j < WMAX; j++)
-            if (j == lane) a[j] += 1.0;
-        a[COL_F] = z[ws + lane] - zold[ws + lane] - dt * a[COL_F];
+    const int rb = Cl.rhs_base[cls];
+    double *R0 = vals + (size_t)rb * 32, *R1 = R0 + (size_t)Wn * 32, *R2 = R1 + (size_t)Wn * 32;
+    const CluOp *ops = Cl.ops;
+    const int q0 = Cl.prog_ptr[cls], qm = Cl.prog_mid[cls], q1 = Cl.prog_ptr[cls + 1];
+    // backward-Euler scaling
+    for (int q = q0; q < qm; q++) {
+        const CluOp o = ops[q];
+        double *vd = vals + o.d * 32 + lane;
+        if (o.code == OP_SCL) *vd *= -dt;
+        else if (o.code == OP_DIAG) *vd += 1.0;
+        else if (o.code == OP_BEF) *vd = act ? z[ws + o.a] - zold[ws + o.a] - dt * *vd : 0.0;
     }
-    if (want_f && has_row) W.f[(size_t)m * P.n_sys + ws + lane] = a[COL_F];
-    // residual norm
-    unsigned long long nb = has_row ? norm_bits(a[COL_F]) : 0ull;
+    // residual norm (and the residual itself for the parity probe)
+    const int *pc = Cl.perm_col + cls * 32;
+    unsigned long long nb = 0ull;
+    for (int j = 0; j < Wn; j++) {
+        const unsigned long long t = norm_bits(R2[j * 32 + lane]);
+        nb = t > nb ? t : nb;
+    }
+    if (!act) nb = 0ull;
+    if (want_f && act) {
+        // R2 is indexed by pivot position; OP_BEF / OP_ROW name the local row
+        // whose residual each position holds
+        for (int q = q0; q < qm; q++)
+            if (ops[q].code == OP_BEF || ops[q].code == OP_ROW)
+                W.f[(size_t)m * P.n_sys + ws + ops[q].a] = vals[ops[q].d * 32 + lane];
+    }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-        unsigned long long o = __shfl_xor_sync(FULL_MASK, nb, off);
+        const unsigned long long o = __shfl_xor_sync(FULL_MASK, nb, off);
         nb = o > nb ? o : nb;
     }
     if (lane == 0) atomicMax(W.norm + m, nb);
-    // LU with partial pivoting: lane i owns row i; the three right-hand
-    // sides (B(:,vr), B(:,vi), f) ride along as columns 29..31.
-    bool pivoted = !has_row;
-    int mystep = -1;
-#pragma unroll
-    for (int k = 0; k < WMAX; k++) {
-        if (k < Wn) {
-            double cand = pivoted ? -1.0 : fabs(a[k]);
-            int cl = lane;
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                double ov = __shfl_xor_sync(FULL_MASK, cand, off);
-                int ol = __shfl_xor_sync(FULL_MASK, cl, off);
-                if (ov > cand || (ov == cand && ol < cl)) { cand = ov; cl = ol; }
-            }
-            const int pl = cl;
-            const double pk = __shfl_sync(FULL_MASK, a[k], pl);
-            const bool elim = !pivoted && lane != pl;
-            const double l = elim ? a[k] / pk : 0.0;
-            if (lane == pl) { pivoted = true; mystep = k; }
-#pragma unroll
-            for (int j = k + 1; j < LDM; j++) {
-                if (j < Wn || j >= WMAX) {
-                    const double pr = __shfl_sync(FULL_MASK, a[j], pl);
-                    if (elim) a[j] -= l * pr;
-                }
-            }
+    // factorisation and solves
+    for (int q = qm; q < q1; q++) {
+        const CluOp o = ops[q];
+        switch (o.code) {
+        case OP_RCP:
+            vals[o.d * 32 + lane] = 1.0 / vals[o.a * 32 + lane];
+            break;
+        case OP_MUL:
+            vals[o.d * 32 + lane] *= vals[o.a * 32 + lane];
+            break;
+        case OP_FMS:
+            vals[o.d * 32 + lane] -= vals[o.a * 32 + lane] * vals[o.b * 32 + lane];
+            break;
+        case OP_FMS3: {
+            const double l = vals[o.a * 32 + lane];
+            R0[o.d * 32 + lane] -= l * R0[o.b * 32 + lane];
+            R1[o.d * 32 + lane] -= l * R1[o.b * 32 + lane];
+            R2[o.d * 32 + lane] -= l * R2[o.b * 32 + lane];
+            break;
+        }
+        case OP_MUL3: {
+            const double l = vals[o.a * 32 + lane];
+            R0[o.d * 32 + lane] *= l;
+            R1[o.d * 32 + lane] *= l;
+            R2[o.d * 32 + lane] *= l;
+            break;
+        }
+        default:
+            break;
         }
     }
-    // back substitution for the three right-hand sides
-#pragma unroll
-    for (int k = WMAX - 1; k >= 0; k--) {
-        if (k < Wn) {
-            const unsigned own = __ballot_sync(FULL_MASK, mystep == k);
-            const int q = __ffs(own) - 1;
-            const double d = __shfl_sync(FULL_MASK, a[k], q);
-            const double x1 = __shfl_sync(FULL_MASK, a[COL_VR], q) / d;
-            const double x2 = __shfl_sync(FULL_MASK, a[COL_VI], q) / d;
-            const double y = __shfl_sync(FULL_MASK, a[COL_F], q) / d;
-            if (lane == q) {
-                a[COL_VR] = x1;
-                a[COL_VI] = x2;
-                a[COL_F] = y;
-            } else if (mystep >= 0 && mystep < k) {
-                const double u = a[k];
-                a[COL_VR] -= u * x1;
-                a[COL_VI] -= u * x2;
-                a[COL_F] -= u * y;
-            }
-        }
-    }
+    if (!act) return;
     const int n_da = P.n_diff + P.n_alg;
-    if (mystep >= 0) {
-        double *yx = W.yx + (size_t)m * 3 * n_da + ws + mystep;
-        yx[0] = a[COL_F];
-        yx[n_da] = a[COL_VR];
-        yx[2 * n_da] = a[COL_VI];
+    double *yx = W.yx + (size_t)m * 3 * n_da + ws;
+    for (int j = 0; j < Wn; j++) {
+        const int st = pc[j];
+        yx[st] = R2[j * 32 + lane];
+        yx[n_da + st] = R0[j * 32 + lane];
+        yx[2 * n_da + st] = R1[j * 32 + lane];
     }
-    // Schur terms: D = C X, r = C y over the three coupled states
+    const int *p3 = Cl.pos3 + cls * 3;
     double X1[3], X2[3], Y[3];
 #pragma unroll
     for (int t = 0; t < 3; t++) {
-        const int kk = sLoc[warp][t];
-        const unsigned own = __ballot_sync(FULL_MASK, mystep == kk);
-        const int q = __ffs(own) - 1;
-        X1[t] = __shfl_sync(FULL_MASK, a[COL_VR], q);
-        X2[t] = __shfl_sync(FULL_MASK, a[COL_VI], q);
-        Y[t] = __shfl_sync(FULL_MASK, a[COL_F], q);
+        X1[t] = R0[p3[t] * 32 + lane];
+        X2[t] = R1[p3[t] * 32 + lane];
+        Y[t] = R2[p3[t] * 32 + lane];
     }
-    if (lane == 0) {
-        const double *Cc = sC[warp];
-        double *o = W.clout + ((size_t)m * P.n_cl + c) * 8;
-        o[0] = Cc[0] * X1[0] + Cc[1] * X1[1] + Cc[2] * X1[2];
-        o[1] = Cc[0] * X2[0] + Cc[1] * X2[1] + Cc[2] * X2[2];
-        o[2] = Cc[3] * X1[0] + Cc[4] * X1[1] + Cc[5] * X1[2];
-        o[3] = Cc[3] * X2[0] + Cc[4] * X2[1] + Cc[5] * X2[2];
-        o[4] = Cc[0] * Y[0] + Cc[1] * Y[1] + Cc[2] * Y[2];
-        o[5] = Cc[3] * Y[0] + Cc[4] * Y[1] + Cc[5] * Y[2];
-        o[6] = Cc[6];
-        o[7] = Cc[7];
-    }
+    double *o = W.clout + ((size_t)m * P.n_cl + c) * 8;
+    o[0] = Cc[0] * X1[0] + Cc[1] * X1[1] + Cc[2] * X1[2];
+    o[1] = Cc[0] * X2[0] + Cc[1] * X2[1] + Cc[2] * X2[2];
+    o[2] = Cc[3] * X1[0] + Cc[4] * X1[1] + Cc[5] * X1[2];
+    o[3] = Cc[3] * X2[0] + Cc[4] * X2[1] + Cc[5] * X2[2];
+    o[4] = Cc[0] * Y[0] + Cc[1] * Y[1] + Cc[2] * Y[2];
+    o[5] = Cc[3] * Y[0] + Cc[4] * Y[1] + Cc[5] * Y[2];
+    o[6] = Ic[0];
+    o[7] = Ic[1];
 }
 
-void launch_cluster(const DevProblem &P, const DevWork &W, int want_f, cudaStream_t st) {
-    long long tasks = (long long)P.M * P.n_cl;
-    if (tasks == 0) return;
-    int blocks = (int)((tasks + CK_WARPS - 1) / CK_WARPS);
-    cluster_kernel<<<blocks, CK_WARPS * 32, 0, st>>>(P, W, want_f);
+void launch_cluster(const DevProblem &P, const DevWork &W, const DevClu &C, int want_f, cudaStream_t st) {
+    if (C.n_tasks == 0) return;
+    dim3 grid(C.n_tasks, P.M);
+    cluster_kernel<<<grid, 32, (size_t)C.max_slots * 32 * sizeof(double), st>>>(P, W, C, want_f);
+}
+
+int cluster_smem_optin(int bytes) {
+    if (cudaFuncSetAttribute(cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    return bytes;
 }
 
 // ---------------------------------------------------------------------------

@@ -209,6 +209,21 @@ int32_t gp_last_timing(const gp_layout *L, double out[16]);
 int32_t gp_reduced_selftest(const gp_problem *prob, const int32_t *s_rowptr, const int32_t *s_colidx,
                             const double *s_val, const double *rhs, double *x, double out[4]);
 
+/* Host-only check of the cluster factorisation, needs no GPU: builds the
+ * class plans of gp_layout_create from (z, u0, p) of one scenario and runs
+ * every non-trivial cluster's program on the host in the device kernel's
+ * operation order.  yx[3][n_diff+n_alg] receives A_k^-1 f_k, A_k^-1 B_k(:,vr),
+ * A_k^-1 B_k(:,vi) at the cluster's states; clout[n_nontrivial][8] the
+ * per-cluster outputs (C A^-1 B as 4 values, C A^-1 f as 2, bus injection
+ * as 2); f (may be NULL) the backward-Euler residual of the cluster rows.
+ * out[0] max |f| over cluster rows, out[1] classes, out[2] FMAs of all
+ * cluster factorisations, out[3] maximum slots of a class.
+ * No counterpart in the reference: a test hook for the static-pivot sparse
+ * factorisation that replaces the dense per-cluster getrf
+ * (src/schur.jl:436-493). */
+int32_t gp_cluster_selftest(const gp_problem *prob, const double *z, const double *zold, const double *u0,
+                            const double *p, double dt, double *yx, double *clout, double *f, double out[4]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -205,3 +205,64 @@ def test_scenario_sharding_gloo(orc):
     for lo, hi, zf, it in parts:
         assert np.array_equal(zf, full["z"][lo:hi])
         assert np.array_equal(it, full["iters"][lo:hi])
+
+
+CLUSTER_CASES = [("2bus.raw", "2bus_ESDC1A.dyr"), ("2bus.raw", "2bus_SEXS.dyr"), ("2bus.raw", "2bus_TGOV1.dyr"),
+                 ("2bus.raw", "2bus_IEESGO.dyr"), ("ieee9_v33.raw", "ieee9bus_gov.dyr"),
+                 ("IEEE39.raw", "IEEE39_gov.dyr"), ("IEEE39.raw", "IEEE39.dyr"), "ring39"]
+
+
+@pytest.mark.parametrize("case", CLUSTER_CASES, ids=lambda c: c if isinstance(c, str) else c[1])
+def test_cluster_factorisation_matches_dense_solves(lib, golden_cases, orc, case):
+    """Static-pivot sparse LU of every generator cluster (host run of the
+    device program) against dense solves with the oracle's Jacobian blocks:
+    A_k^-1 f_k, A_k^-1 B_k, C_k A_k^-1 B_k and C_k A_k^-1 f_k."""
+    if isinstance(case, str):
+        w = synthetic.WORKLOADS[case]()
+        ps, dp = w.ps, w.dp
+    else:
+        ps, dp = psse_case(golden_cases, *case)
+    PA = LY.ProblemArrays(ps)
+    P = PA.as_ctypes()
+    dt = 1 / 120
+    rng = np.random.default_rng(7)
+    zold = dp.zvec.copy()
+    z = zold + 1e-3 * rng.normal(size=zold.size)
+    fa, nf = LY.fault_array([[]], dt)
+    J = orc.jacobian_dense(PA, z, dp.uvec, dp.pvec, fa, nf, np.zeros(1, np.uint8), dt)
+    f = orc.residual(PA, z, zold, dp.uvec, dp.pvec, fa, nf, np.zeros(1, np.uint8), dt)
+    net = PA.n_diff + PA.n_alg
+    yx = np.zeros(3 * net)
+    nt = int((PA.cl_gen >= 0).sum())
+    clout = np.zeros((max(nt, 1), 8))
+    fc = np.zeros(net)
+    out = np.zeros(4)
+    assert lib.gp_cluster_selftest(C.addressof(P), z.ctypes.data, zold.ctypes.data, dp.uvec.ctypes.data,
+                                   dp.pvec.ctypes.data, dt, yx.ctypes.data, clout.ctypes.data,
+                                   fc.ctypes.data, out.ctypes.data) == 0
+    assert out[1] >= 1 and out[2] > 0
+    fmax = 0.0
+    k = 0
+    for c in range(PA.n_clusters):
+        if PA.cl_gen[c] < 0:
+            continue
+        w0, W, b = PA.cl_w_start[c], PA.cl_w_size[c], PA.cl_bus[c]
+        s = slice(w0, w0 + W)
+        rows = [net + 2 * b, net + 2 * b + 1]
+        A = J[s, s]
+        B = J[s][:, rows]
+        Cm = J[rows][:, s]
+        assert np.max(np.abs(fc[s] - f[s])) <= 1e-15 * max(1.0, np.max(np.abs(f[s])))
+        fmax = max(fmax, np.max(np.abs(f[s])))
+        y = np.linalg.solve(A, f[s])
+        X = np.linalg.solve(A, B)
+        got = np.stack([yx[s], yx[net:][s], yx[2 * net:][s]], axis=1)
+        ref = np.concatenate([y[:, None], X], axis=1)
+        assert np.max(np.abs(got - ref)) <= 1e-11 * max(1.0, np.max(np.abs(ref))), c
+        CX = Cm @ X
+        Cy = Cm @ y
+        assert np.allclose(clout[k, :4], CX.ravel(), rtol=1e-11, atol=1e-12), c
+        assert np.allclose(clout[k, 4:6], Cy, rtol=1e-11, atol=1e-13), c
+        k += 1
+    assert k == nt
+    assert abs(out[0] - fmax) <= 1e-15 * max(1.0, fmax)
