@@ -1093,3 +1093,92 @@ int32_t gp_last_timing(const gp_layout *L, double out[16]) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Residual with file-scope scratch (gp_residual_static)
+// ---------------------------------------------------------------------------
+
+namespace {
+
+// 16 MiB of device scratch; nothing in it is assumed to survive between calls.
+constexpr size_t kStaticScratchBytes = size_t(1) << 24;
+__device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+constexpr int kMaxDevices = 64;
+void *g_static_ptr[kMaxDevices] = {};
+
+// Address of g_static_scratch on the current device, looked up once per
+// device (the first call on a device does it; make that call before any
+// stream capture).
+unsigned char *static_scratch() {
+    int dev = 0;
+    ck(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices) fail(GP_E_INVALID, "device ordinal %d out of range", dev);
+    if (!g_static_ptr[dev]) {
+        void *ptr = nullptr;
+        ck(cudaGetSymbolAddress(&ptr, g_static_scratch), "cudaGetSymbolAddress");
+        g_static_ptr[dev] = ptr;
+    }
+    return (unsigned char *)g_static_ptr[dev];
+}
+
+// Carves 256-byte aligned pieces off the scratch array.
+struct Carver {
+    unsigned char *base;
+    size_t used = 0;
+    template <class T>
+    T *take(size_t n) {
+        T *p = (T *)(base + used);
+        used += (n * sizeof(T) + 255) & ~size_t(255);
+        return p;
+    }
+};
+
+}  // namespace
+
+extern "C" int32_t gp_residual_static(gp_layout *L, const double *zold, double dt, double *f) {
+    API_BEGIN
+    if (!L || !zold || !f) fail(GP_E_INVALID, "null argument");
+    const size_t M = L->M;
+    const gp::DevProblem &P0 = L->P;
+    // bytes the residual needs, with the same 256-byte rounding as Carver
+    auto rnd = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t need = rnd(M * P0.n_sys * 8) * 2 + rnd(M * 3 * std::max(1, P0.net) * 8) +
+                        rnd(M * 8 * std::max(1, P0.n_cl) * 8) + rnd(M * std::max(1, P0.n_var) * 8) +
+                        rnd(M * std::max(1, P0.n_red) * 8) + rnd(M * 8) + rnd(M) + rnd(4) + rnd(8) +
+                        rnd((M + 1) * 4);
+    if (need > kStaticScratchBytes)
+        fail(GP_E_INVALID, "gp_residual_static needs %zu bytes of scratch; at most %zu are available", need,
+             kStaticScratchBytes);
+    Carver cv{static_scratch()};
+    gp::DevWork W = L->W;
+    gp::DevProblem P = L->P;
+    W.zold = cv.take<double>(M * P.n_sys);
+    W.f = cv.take<double>(M * P.n_sys);
+    W.yx = cv.take<double>(M * 3 * std::max(1, P.net));
+    W.clout = cv.take<double>(M * 8 * std::max(1, P.n_cl));
+    W.svar = cv.take<double>(M * std::max(1, P.n_var));
+    W.xperm = cv.take<double>(M * std::max(1, P.n_red));
+    W.norm = cv.take<unsigned long long>(M);
+    W.active = cv.take<uint8_t>(M);
+    W.flag = cv.take<int>(1);
+    W.dt = cv.take<double>(1);
+    int *fl_ptr = cv.take<int>(M + 1);
+    // no fault applied: every scenario's fault range is empty
+    P.fl_ptr = fl_ptr;
+    P.fl_bus = fl_ptr;
+    P.fl_on = W.active;
+    P.fl_yf = W.dt;
+    cudaStream_t st = L->st;
+    ck(cudaMemsetAsync(fl_ptr, 0, (M + 1) * sizeof(int), st), "memset");
+    ck(cudaMemsetAsync(W.active, 1, M, st), "memset");
+    ck(cudaMemcpyAsync(W.zold, zold, M * P.n_sys * sizeof(double), cudaMemcpyHostToDevice, st), "zold");
+    ck(cudaMemcpyAsync(W.dt, &dt, sizeof(double), cudaMemcpyHostToDevice, st), "dt");
+    gp::launch_reset_norm(P, W, st);
+    gp::launch_cluster(P, W, L->C, 1, st);
+    gp::launch_network(P, W, 1, st);
+    ck(cudaGetLastError(), "residual launch");
+    ck(cudaMemcpyAsync(f, W.f, M * P.n_sys * sizeof(double), cudaMemcpyDeviceToHost, st), "residual copy");
+    ck(cudaStreamSynchronize(st), "residual");
+    API_END
+}

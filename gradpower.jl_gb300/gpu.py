@@ -52,9 +52,11 @@ def library():
         L.gp_restore_initial_state.argtypes = [vp]
         L.gp_reduced_selftest.argtypes = [vp] * 7
         L.gp_cluster_selftest.argtypes = [vp] * 5 + [C.c_double] + [vp] * 4
+        L.gp_residual_static.argtypes = [vp, vp, C.c_double, vp]
         for f in ("gp_layout_create", "gp_layout_destroy", "gp_layout_stats", "gp_set_state",
                   "gp_get_state", "gp_integrate", "gp_residual", "gp_last_timing",
-                  "gp_restore_initial_state", "gp_reduced_selftest", "gp_cluster_selftest"):
+                  "gp_restore_initial_state", "gp_reduced_selftest", "gp_cluster_selftest",
+                  "gp_residual_static"):
             getattr(L, f).restype = C.c_int32
         _lib = L
     return _lib

@@ -197,6 +197,17 @@ int32_t gp_residual(gp_layout *L, const double *zold, double dt, int32_t n_fault
  * solves (batched over scenarios); out[10..15] zero. */
 int32_t gp_last_timing(const gp_layout *L, double out[16]);
 
+/* gp_residual with no fault applied, computed without allocating anything:
+ * its scratch (zold, residual, cluster and network intermediates) lives in
+ * one file-scope 16 MiB device array instead of the layout's buffers.
+ * f[M][n_sys] as gp_residual(L, zold, dt, 0, NULL, NULL, f).  Returns
+ * GP_E_INVALID when M * (about 3 n_sys + 3 n_diff + 3 n_alg + 8 clusters +
+ * n_var) doubles exceed the 16 MiB.  The first call on a device looks up the
+ * array's address: make it before any stream capture.  The array is shared
+ * by every layout on the device, so overlapping calls race.
+ * No counterpart in the reference. */
+int32_t gp_residual_static(gp_layout *L, const double *zold, double dt, double *f);
+
 /* Host-only check of the reduced-system machinery, needs no GPU: builds the
  * same symbolic analysis and front assembly lists as gp_layout_create, takes
  * the diagonal blocks and static-generator couplings of S from the given
