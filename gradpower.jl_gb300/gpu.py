@@ -198,3 +198,19 @@ def integrate_gpu_cudss(gbl: GpuBatchedLayout, ps: Mdl.PowerSystem, tf: float,
     (ext/GradPowerCUDAExt/GradPowerCUDAExt.jl:2924-2996).  The library runs
     the same exact Newton step with the cluster blocks eliminated first."""
     return integrate_gpu_schur_cudss(gbl, ps, tf, dt, newton_tol, scenario_faults)
+
+
+class BatchedLayout(GpuBatchedLayout):
+    """The reference's CPU batch container (src/batched.jl:16-72), same
+    constructor `BatchedLayout(dp, ps, M)`; here the batch lives on the GPU
+    and `integrate_batched` runs the library's Newton step on it."""
+
+
+def integrate_batched(bl: GpuBatchedLayout, ps: Mdl.PowerSystem, tf: float,
+                      dt: float = 1.0 / 120.0, newton_tol: float = 1e-10,
+                      scenario_faults=None):
+    """(tvec, trajs): the reference's batched integrator
+    (src/batched.jl:417-492): exact Newton, a fresh factorisation every
+    iteration, at most 30 iterations per solve."""
+    return integrate_gpu_schur_cudss(gbl=bl, ps=ps, tf=tf, dt=dt, newton_tol=newton_tol,
+                                     scenario_faults=scenario_faults)
