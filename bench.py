@@ -9,6 +9,11 @@ steps, their Newton iterations and the two dt = 0 event re-solves, i.e.
 8 x 120 scenario-steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+  python bench.py --profile TF [--steps K] [--warmup W]
+
+`--profile TF` is the short run used under ncu: the same workload and
+layout over a TF-second horizon, no end-to-end leg and no CPU baseline;
+it prints the library's phase timing (not a benchmark line).
 
 The GPU arm prints one JSON line with `value` measured with inputs resident
 on the device (device-clock CUDA events recorded by the library), `e2e`
@@ -331,13 +336,35 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def profile_arm(args):
+    """Short integrations of the bench workload for profilers."""
+    import torch
+    torch.cuda.set_device(0)
+    load_package()
+    from gradpower_gb300 import build, gpu, synthetic
+    build.build()
+    w = synthetic.planar70k(n_scenarios=SCEN_PER_GPU)
+    gbl = gpu.GpuBatchedLayout(w.dp, w.ps, SCEN_PER_GPU)
+    for k in range(args.warmup + args.steps):
+        gbl.restore_initial_state()
+        r = gbl.integrate(args.profile, DT, scenario_faults=w.faults, want_traj=False)
+        if k >= args.warmup:
+            print(json.dumps({"profile_tf": args.profile, "status_max": int(r["status"].max()), **gbl.timing()}),
+                  flush=True)
+    gbl.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--profile", type=float, default=None, metavar="TF")
     args = ap.parse_args()
+    if args.profile is not None:
+        profile_arm(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -123,6 +123,10 @@ struct gp_layout {
     // sparse cluster factorisation
     gp::ClusterPlan cplan;
     gp::DevClu C{};
+    // dataflow schedule of the reduced-system factorisation and solves
+    gp::DevDag D{};
+    gp::DagGrid G64;
+    int solve_graph_launches = 0;
 };
 
 namespace {
@@ -452,6 +456,46 @@ int host_factor_solve(const Plan &pl, const std::vector<double> &svar, std::vect
     return zero_pivots;
 }
 
+// Task order of the dataflow kernels: supernodes whose whole subtree has
+// fronts of at most dag_small_front() rows first (by level), then the rest
+// (by level).  Both parts list children before parents.
+void build_dag(gp_layout *L, const gp::Symbolic &sym) {
+    DeviceArena &A = L->arena;
+    const int ns = sym.nsup;
+    std::vector<int> submax(ns, 0);
+    for (int l = 0; l < sym.nlevels; l++)
+        for (int q = sym.level_ptr[l]; q < sym.level_ptr[l + 1]; q++) {
+            const int s = sym.level_sups[q];
+            int mx = sym.front_m(s);
+            for (int c = sym.child_ptr[s]; c < sym.child_ptr[s + 1]; c++) mx = std::max(mx, submax[sym.children[c]]);
+            submax[s] = mx;
+        }
+    const int lim = gp::dag_small_front();
+    std::vector<int> order, rank(ns);
+    int max_big = 0;
+    for (int pass = 0; pass < 2; pass++)
+        for (int l = 0; l < sym.nlevels; l++)
+            for (int q = sym.level_ptr[l]; q < sym.level_ptr[l + 1]; q++) {
+                const int s = sym.level_sups[q];
+                const bool small = submax[s] <= lim;
+                if (small != (pass == 0)) continue;
+                rank[s] = (int)order.size();
+                order.push_back(s);
+                if (!small) max_big = std::max(max_big, sym.front_m(s));
+            }
+    int n_small = 0;
+    for (int s = 0; s < ns; s++) n_small += submax[s] <= lim;
+    gp::DevDag &D = L->D;
+    D.nsup = ns;
+    D.n_small = n_small;
+    D.max_front = sym.max_front;
+    D.max_big_front = max_big;
+    D.order = A.upload(order);
+    D.rank = A.upload(rank);
+    D.parent = A.upload(sym.parent);
+    if (gp::dag_configure(D, 0, L->G64) != 0) fail(GP_E_CUDA, "could not configure the dataflow kernels");
+}
+
 void build_problem(gp_layout *L, const gp_problem *pr) {
     using namespace gp;
     Plan &pl = *new Plan();
@@ -558,6 +602,7 @@ void build_problem(gp_layout *L, const gp_problem *pr) {
     S.asmv_idx = A.upload(pl.avidx);
     L->lvl_max_front = pl.lvl_max_front;
     L->sym = pl.sym;
+    build_dag(L, sym);
     L->smem_limit = gp::factor_smem_limit();
     if (L->smem_limit < 0) fail(GP_E_CUDA, "could not configure the factorisation kernel's shared memory");
     if ((size_t)sym.max_front * sym.max_front * sizeof(double) > (size_t)L->smem_limit)
@@ -589,6 +634,19 @@ void build_work(gp_layout *L, const double *z0, const double *u0, const double *
     S.fronts = A.alloc<double>(M * S.front_total);
     S.uvec = A.alloc<double>(M * std::max<int64_t>(1, S.uvec_total));
     S.ipiv = A.alloc<int>(M * S.n);
+    gp::DevDag &D = L->D;
+    D.ctr = A.alloc<int>(4);
+    D.epoch = A.alloc<int>(1);
+    D.err = A.alloc<int>(1);
+    D.fdone = A.alloc<int>(M * D.nsup);
+    D.xdone = A.alloc<int>(M * D.nsup);
+    D.bdone = A.alloc<int>(M * D.nsup);
+    ck(cudaMemset(D.ctr, 0, 4 * sizeof(int)), "memset");
+    ck(cudaMemset(D.epoch, 0, sizeof(int)), "memset");
+    ck(cudaMemset(D.err, 0, sizeof(int)), "memset");
+    ck(cudaMemset(D.fdone, 0, M * D.nsup * sizeof(int)), "memset");
+    ck(cudaMemset(D.xdone, 0, M * D.nsup * sizeof(int)), "memset");
+    ck(cudaMemset(D.bdone, 0, M * D.nsup * sizeof(int)), "memset");
     ck(cudaMemset(W.status, 0, M * sizeof(int)), "memset");
     ck(cudaMallocHost(&L->h_flag, sizeof(int)), "cudaMallocHost");
     ck(cudaMallocHost(&L->h_dt, sizeof(double)), "cudaMallocHost");
@@ -681,22 +739,17 @@ void mark(gp_layout *L, int i) {
 }
 
 void enqueue_solve(gp_layout *L) {
-    const gp::Symbolic &sym = L->sym;
+    const gp::DevDag &D = L->D;
     mark(L, 3);
-    for (int l = 0; l < sym.nlevels; l++)
-        gp::launch_factor_level(L->P, L->W, L->S, sym.level_ptr[l], sym.level_ptr[l + 1] - sym.level_ptr[l],
-                                L->lvl_max_front[l], L->st);
-    mark(L, 4);
-    for (int l = 0; l < sym.nlevels; l++)
-        gp::launch_fwd_level(L->P, L->W, L->S, sym.level_ptr[l], sym.level_ptr[l + 1] - sym.level_ptr[l],
-                             L->lvl_max_front[l], L->st);
+    gp::launch_dag_begin(D, L->st);
+    gp::launch_dag_factor<double>(L->P, L->W, L->S, D, L->G64, L->S.fronts, L->W.active, L->st);
+    mark(L, 4);   // the FP64 factorisation includes the forward solve
     mark(L, 5);
-    for (int l = sym.nlevels - 1; l >= 0; l--)
-        gp::launch_bwd_level(L->P, L->W, L->S, sym.level_ptr[l], sym.level_ptr[l + 1] - sym.level_ptr[l],
-                             L->lvl_max_front[l], L->st);
+    gp::launch_dag_bwd<double>(L->P, L->W, L->S, D, L->G64, L->S.fronts, L->st);
     mark(L, 6);
     gp::launch_update(L->P, L->W, L->S, L->d_state_maps, L->st);
     mark(L, 7);
+    L->solve_graph_launches = 1 + (D.n_small > 0) + (D.nsup > D.n_small) + 2;
 }
 
 void enqueue_eval(gp_layout *L, double tol, int itermax) {
@@ -764,8 +817,8 @@ void newton(gp_layout *L, double dt, double tol, int itermax) {
         if (*L->h_flag == 0) return;
         ck(cudaGraphLaunch(L->g_solve, L->st), "graph launch");
         solve_pending = true;
-        L->launches += 3 * L->sym.nlevels + 1;
-        L->factor_launches += L->sym.nlevels;
+        L->launches += L->solve_graph_launches;
+        L->factor_launches += (L->D.n_small > 0) + (L->D.nsup > L->D.n_small);
         L->solves += 1;
     }
     fail(GP_E_NUMERIC, "Newton loop did not terminate");
@@ -947,6 +1000,7 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
     L->factor_launches = 0;
     L->solves = 0;
     for (int i = 0; i < 8; i++) L->ph_ms[i] = 0.0;
+    ck(cudaMemsetAsync(L->D.err, 0, sizeof(int), L->st), "memset");
     for (int k = 1; k <= ns; k++) {
         ck(cudaMemcpyAsync(L->W.zold, L->W.z, (size_t)M * nsys * sizeof(double), cudaMemcpyDeviceToDevice, L->st),
            "zold");
@@ -979,6 +1033,11 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     L->t_total_ms = ms;
+    {
+        int err = 0;
+        ck(cudaMemcpy(&err, L->D.err, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
+        if (err) fail(GP_E_TIMEOUT, "a dataflow wait of the reduced-system solve ran out its iteration limit");
+    }
     if (traj)
         ck(cudaMemcpy(traj, d_traj, (size_t)M * (ns + 1) * nsys * sizeof(double), cudaMemcpyDeviceToHost),
            "trajectory copy");

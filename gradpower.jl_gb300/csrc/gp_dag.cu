@@ -1,0 +1,541 @@
+// Dataflow multifrontal factorisation and triangular solves of the reduced
+// network matrix S, batched over scenarios.
+//
+// This replaces cuDSS's factorization/solve of S
+// (ext/GradPowerCUDAExt/GradPowerCUDAExt.jl:2782-2799).  A task is one
+// (supernode, scenario) pair.  Tasks are numbered in a topological order of
+// the assembly tree (children before parents) and claimed in that order
+// from an atomic counter by persistent warps or CTAs.  A task waits only on
+// tasks with smaller numbers (its children; for the backward solve, its
+// parent in the reversed order), which were claimed earlier by warps or
+// CTAs that are running, so the smallest unfinished claimed task can always
+// proceed and the kernel cannot deadlock.  Every wait is bounded: after
+// kWaitLimit polls it raises the error flag, every other wait then returns
+// at once, and the kernel finishes with the scenario marked in `status`.
+//
+// Factorisation, in two launches:
+//  - factor_small_kernel: supernodes whose whole subtree has fronts of at
+//    most 32 rows, one warp per task, the front in shared memory;
+//  - factor_big_kernel: the rest, one CTA per task.
+// Partial pivoting is restricted to a supernode's pivot rows.  The front
+// (column-major, leading dimension = front rows) keeps L, U and the update
+// matrix that the parent's extend-add reads.
+//
+// Solves, one launch each, one warp per task over all supernodes:
+//  - fwd_dag_kernel: extend-add of the children's update vectors, row
+//    swaps, unit-lower solve, update vector of this supernode;
+//  - bwd_dag_kernel: gather of the ancestors' solution, upper solve.
+//
+// The factor type T is double (exact Newton) or float (factors kept and
+// reused across Newton iterations); vectors are always double.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "gp_internal.h"
+
+namespace gp {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int kWaitLimit = 1 << 20;
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kSmallFront = 32;
+
+__device__ __forceinline__ int ld_relaxed(const int *p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void fence_acquire() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
+__device__ __forceinline__ void st_release(int *p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+template <class T>
+__device__ __forceinline__ T ldcg(const T *p) {
+    return __ldcg(p);
+}
+
+// Waits until *flag == epoch; false when it gave up (error flag raised here
+// or by another task).
+__device__ bool wait_epoch(const int *flag, int epoch, int *err) {
+    for (int it = 0; it < kWaitLimit; ++it) {
+        if (ld_relaxed(flag) == epoch) {
+            fence_acquire();
+            return true;
+        }
+        if (*(volatile int *)err) return false;
+        __nanosleep(64);
+    }
+    atomicExch(err, 1);
+    return false;
+}
+
+// One warp waits for the children of supernode s (scenario m) whose
+// schedule rank is at least `from_rank`.
+__device__ bool warp_wait_children(const DevSym &S, const DevDag &D, const int *done, int s, int m, int M,
+                                   int epoch, int from_rank) {
+    const int lane = threadIdx.x & 31;
+    const int c0 = S.child_ptr[s], nc = S.child_ptr[s + 1] - c0;
+    bool ok = true;
+    for (int q = lane; q < nc; q += 32) {
+        const int c = S.children[c0 + q];
+        if (D.rank[c] >= from_rank) ok = wait_epoch(done + (size_t)c * M + m, epoch, D.err) && ok;
+    }
+    ok = __all_sync(FULL, ok);
+    __syncwarp();
+    return ok;
+}
+
+__device__ __forceinline__ void signal_done(int *flag, int epoch) {
+    __threadfence();
+    st_release(flag, epoch);
+}
+
+// Magnitude of a factor entry as an unsigned key that orders like |v|
+// (sign bit cleared; NaN above +inf), so that pivot search and reductions
+// run on the integer pipes instead of the (scarce) FP64 pipe.
+__device__ __forceinline__ unsigned long long mag_key(double v) {
+    return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
+__device__ __forceinline__ unsigned long long mag_key(float v) {
+    return (unsigned long long)(__float_as_uint(v) & 0x7fffffffu);
+}
+
+// Pivot of column k among rows [k, ns) of a front: index of the largest
+// magnitude, the smallest index on ties.  Called by a whole warp; every lane
+// returns the same result.  zero is set when the column is zero there.
+template <class T>
+__device__ __forceinline__ int warp_pivot(const T *F, int mm, int k, int ns, bool &zero) {
+    const int lane = threadIdx.x & 31;
+    unsigned long long bk = 0;
+    int bi = k;
+    for (int i = k + lane; i < ns; i += 32) {
+        const unsigned long long v = mag_key(F[i + k * mm]);
+        if (v > bk) { bk = v; bi = i; }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const unsigned long long ok = __shfl_xor_sync(FULL, bk, off);
+        const int oi = __shfl_xor_sync(FULL, bi, off);
+        if (ok > bk || (ok == bk && oi < bi)) { bk = ok; bi = oi; }
+    }
+    zero = bk == 0;
+    return bi;
+}
+
+// Next power of two >= n, for 1 <= n <= 32.
+__device__ __forceinline__ int np2(int n) { return n <= 1 ? 1 : 1 << (32 - __clz(n - 1)); }
+
+// Row dot products out_i = sum_j A[i*si + j*sj] * v(j), i < nrow, j < ncol,
+// by one warp.  Rows are spread over groups of G lanes (G = 32 / np2(nrow),
+// 1 when nrow >= 32) that split the j range and combine by shuffles in a
+// fixed order, so that short rows still fill the warp.  emit(i, acc) runs on
+// the first lane of each group.
+template <class T, class V, class E>
+__device__ __forceinline__ void warp_row_dots(const T *A, int si, int sj, int nrow, int ncol, V v, E emit) {
+    const int lane = threadIdx.x & 31;
+    const int G = nrow >= 32 ? 1 : 32 / np2(nrow);
+    const int rows_per_pass = 32 / G;
+    const int g = lane & (G - 1);
+    for (int i0 = 0; i0 < nrow; i0 += rows_per_pass) {
+        const int i = i0 + lane / G;
+        double acc = 0.0;
+        if (i < nrow)
+            for (int j = g; j < ncol; j += G) acc += (double)A[i * si + j * sj] * v(j);
+        for (int off = G >> 1; off > 0; off >>= 1) acc += __shfl_xor_sync(FULL, acc, off);
+        if (g == 0 && i < nrow) emit(i, acc);
+    }
+}
+
+// Thread groups that factor one front: a warp, or the whole CTA.
+struct WarpGroup {
+    static constexpr int size = 32;
+    __device__ int idx() const { return threadIdx.x & 31; }
+    __device__ bool lead_warp() const { return true; }
+    __device__ void sync() const { __syncwarp(); }
+};
+struct BlockGroup {
+    static constexpr int size = kThreads;
+    __device__ int idx() const { return threadIdx.x; }
+    __device__ bool lead_warp() const { return threadIdx.x < 32; }
+    __device__ void sync() const { __syncthreads(); }
+};
+
+// Factors the front of supernode s for scenario m in shared memory F
+// (leading dimension mm = front rows) and stores it to global memory.
+//  - Assembly: constant entries of S, the scenario's entries from svar, and
+//    the children's update matrices.
+//  - Partial pivoting within the pivot rows; the multipliers are stored
+//    below the diagonal, and the reciprocal of each pivot on the diagonal.
+//  - RHS: column mm carries the right-hand side (the supernode's entries of
+//    xperm plus the children's update vectors), so that the elimination is
+//    also the forward solve.  It leaves the forward-solved entries in xperm
+//    and this supernode's update vector in uvec.
+template <class T, bool RHS, class G>
+__device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym &S, T *fronts, int s, int m, T *F,
+                             G g) {
+    const int start = S.sup_start[s];
+    const int ns = S.sup_start[s + 1] - start;
+    const int mm = ns + S.row_ptr[s + 1] - S.row_ptr[s];
+    const int nc = mm + (RHS ? 1 : 0);
+    const int idx = g.idx(), step = G::size;
+    T *fr = fronts + (size_t)m * S.front_total;
+    double *x = W.xperm + (size_t)m * P.n_red;
+    double *uv = S.uvec + (size_t)m * S.uvec_total;
+    // ---- assembly ----
+    for (int i = idx; i < mm * nc; i += step) F[i] = T(0);
+    g.sync();
+    for (int e = S.asmc_ptr[s] + idx; e < S.asmc_ptr[s + 1]; e += step) F[S.asmc_pos[e]] += (T)S.asmc_val[e];
+    if (RHS)
+        for (int i = idx; i < ns; i += step) F[mm * mm + i] = (T)x[start + i];
+    g.sync();
+    const double *sv = W.svar + (size_t)m * P.n_var;
+    for (int e = S.asmv_ptr[s] + idx; e < S.asmv_ptr[s + 1]; e += step) F[S.asmv_pos[e]] += (T)sv[S.asmv_idx[e]];
+    g.sync();
+    for (int q = S.child_ptr[s]; q < S.child_ptr[s + 1]; q++) {
+        const int c = S.children[q];
+        const int ncc = S.sup_start[c + 1] - S.sup_start[c];
+        const int rc = S.row_ptr[c + 1] - S.row_ptr[c];
+        const int mc = ncc + rc;
+        const int *rel = S.relmap + S.relmap_ptr[c];
+        const T *Fc = fr + S.front_off[c];
+        for (int t = idx; t < rc * rc; t += step) {
+            const int a = t % rc, b = t / rc;
+            F[rel[a] + rel[b] * mm] += ldcg(Fc + (ncc + a) + (size_t)(ncc + b) * mc);
+        }
+        if (RHS) {
+            const double *uc = uv + S.uvec_off[c];
+            for (int a = idx; a < rc; a += step) F[mm * mm + rel[a]] += (T)ldcg(uc + a);
+        }
+        g.sync();
+    }
+    // ---- elimination ----
+    int *ipiv = S.ipiv + (size_t)m * S.n + start;
+    for (int k = 0; k < ns; k++) {
+        if (g.lead_warp()) {
+            const int lane = threadIdx.x & 31;
+            bool zero;
+            const int pv = warp_pivot(F, mm, k, ns, zero);
+            if (lane == 0) {
+                ipiv[k] = pv;
+                if (zero) atomicOr(W.status + m, 4);
+            }
+            if (pv != k)
+                for (int j = lane; j < nc; j += 32) {
+                    const T a = F[k + j * mm];
+                    F[k + j * mm] = F[pv + j * mm];
+                    F[pv + j * mm] = a;
+                }
+            __syncwarp();
+            const T inv = T(1) / F[k + k * mm];
+            for (int i = k + 1 + lane; i < mm; i += 32) F[i + k * mm] *= inv;
+            __syncwarp();
+            if (lane == 0) F[k + k * mm] = inv;
+        }
+        g.sync();
+        // rank-1 update of rows k+1.., columns k+1.. (the right-hand side too)
+        const int lr = mm - k - 1, lc = nc - k - 1;
+        if (lr > 0 && lc > 0) {
+            int i = idx % lr, j = idx / lr;
+            const int di = step % lr, dj = step / lr;
+            const T *lk = F + k * mm;
+            for (int t = idx; t < lr * lc; t += step) {
+                const int ii = k + 1 + i, jj = k + 1 + j;
+                F[ii + jj * mm] -= lk[ii] * F[k + jj * mm];
+                i += di;
+                j += dj;
+                if (i >= lr) { i -= lr; j++; }
+            }
+        }
+        g.sync();
+    }
+    // ---- store ----
+    T *out = fr + S.front_off[s];
+    for (int i = idx; i < mm * mm; i += step) out[i] = F[i];
+    if (RHS) {
+        for (int i = idx; i < ns; i += step) x[start + i] = (double)F[mm * mm + i];
+        double *us = uv + S.uvec_off[s];
+        for (int a = idx; a < mm - ns; a += step) us[a] = (double)F[mm * mm + ns + a];
+    }
+    g.sync();
+}
+
+template <class T, bool RHS>
+__global__ void __launch_bounds__(kThreads) factor_small_kernel(DevProblem P, DevWork W, DevSym S, DevDag D,
+                                                                T *fronts, const uint8_t *mask) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    T *F = reinterpret_cast<T *>(smem_raw) + warp * kSmallFront * (kSmallFront + 1);
+    const int M = P.M;
+    const int epoch = *D.epoch;
+    const int n_tasks = D.n_small * M;
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(D.ctr + 0, 1);
+        t = __shfl_sync(FULL, t, 0);
+        if (t >= n_tasks) break;
+        const int s = D.order[t / M], m = t % M;
+        if (!mask[m]) continue;
+        if (!warp_wait_children(S, D, D.fdone, s, m, M, epoch, 0) && lane == 0) atomicOr(W.status + m, 8);
+        factor_front<T, RHS>(P, W, S, fronts, s, m, F, WarpGroup{});
+        if (lane == 0) signal_done(D.fdone + (size_t)s * M + m, epoch);
+    }
+}
+
+template <class T, bool RHS>
+__global__ void __launch_bounds__(kThreads) factor_big_kernel(DevProblem P, DevWork W, DevSym S, DevDag D,
+                                                              T *fronts, const uint8_t *mask) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *F = reinterpret_cast<T *>(smem_raw);
+    __shared__ int s_task, s_ok;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int M = P.M;
+    const int epoch = *D.epoch;
+    const int n_tasks = (D.nsup - D.n_small) * M;
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) s_task = atomicAdd(D.ctr + 1, 1);
+        __syncthreads();
+        const int t = s_task;
+        if (t >= n_tasks) break;
+        const int s = D.order[D.n_small + t / M], m = t % M;
+        if (!mask[m]) continue;
+        if (tid < 32) {
+            const bool ok = warp_wait_children(S, D, D.fdone, s, m, M, epoch, D.n_small);
+            if (lane == 0) s_ok = ok;
+        }
+        __syncthreads();
+        if (!s_ok && tid == 0) atomicOr(W.status + m, 8);
+        factor_front<T, RHS>(P, W, S, fronts, s, m, F, BlockGroup{});
+        if (tid == 0) signal_done(D.fdone + (size_t)s * M + m, epoch);
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) fwd_dag_kernel(DevProblem P, DevWork W, DevSym S, DevDag D,
+                                                           const T *fronts) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double *tv = reinterpret_cast<double *>(smem_raw) + warp * D.max_front;
+    const int M = P.M;
+    const int epoch = *D.epoch;
+    const int n_tasks = D.nsup * M;
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(D.ctr + 2, 1);
+        t = __shfl_sync(FULL, t, 0);
+        if (t >= n_tasks) break;
+        const int s = D.order[t / M], m = t % M;
+        if (!W.active[m]) continue;
+        if (!warp_wait_children(S, D, D.xdone, s, m, M, epoch, 0) && lane == 0) atomicOr(W.status + m, 8);
+        const int start = S.sup_start[s];
+        const int ns = S.sup_start[s + 1] - start;
+        const int r = S.row_ptr[s + 1] - S.row_ptr[s];
+        const int mm = ns + r;
+        double *x = W.xperm + (size_t)m * P.n_red;
+        double *uv = S.uvec + (size_t)m * S.uvec_total;
+        for (int i = lane; i < ns; i += 32) tv[i] = x[start + i];
+        for (int i = lane; i < r; i += 32) tv[ns + i] = 0.0;
+        __syncwarp();
+        for (int q = S.child_ptr[s]; q < S.child_ptr[s + 1]; q++) {
+            const int c = S.children[q];
+            const int rc = S.row_ptr[c + 1] - S.row_ptr[c];
+            const int *rel = S.relmap + S.relmap_ptr[c];
+            const double *uc = uv + S.uvec_off[c];
+            for (int a = lane; a < rc; a += 32) tv[rel[a]] += ldcg(uc + a);
+            __syncwarp();
+        }
+        const T *F = fronts + (size_t)m * S.front_total + S.front_off[s];
+        const int *ipiv = S.ipiv + (size_t)m * S.n + start;
+        if (lane == 0)
+            for (int k = 0; k < ns; k++) {
+                const int pv = ipiv[k];
+                if (pv != k) { const double a = tv[k]; tv[k] = tv[pv]; tv[pv] = a; }
+            }
+        __syncwarp();
+        for (int k = 0; k < ns; k++) {
+            const double tk = tv[k];
+            for (int i = k + 1 + lane; i < ns; i += 32) tv[i] -= (double)F[i + k * mm] * tk;
+            __syncwarp();
+        }
+        double *us = uv + S.uvec_off[s];
+        warp_row_dots(F + ns, 1, mm, r, ns, [&](int k) { return tv[k]; },
+                      [&](int a, double acc) { us[a] = tv[ns + a] - acc; });
+        for (int i = lane; i < ns; i += 32) x[start + i] = tv[i];
+        __syncwarp();
+        if (lane == 0) signal_done(D.xdone + (size_t)s * M + m, epoch);
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) bwd_dag_kernel(DevProblem P, DevWork W, DevSym S, DevDag D,
+                                                           const T *fronts) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double *tv = reinterpret_cast<double *>(smem_raw) + warp * D.max_front;
+    const int M = P.M;
+    const int epoch = *D.epoch;
+    const int n_tasks = D.nsup * M;
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(D.ctr + 3, 1);
+        t = __shfl_sync(FULL, t, 0);
+        if (t >= n_tasks) break;
+        const int s = D.order[D.nsup - 1 - t / M], m = t % M;
+        if (!W.active[m]) continue;
+        const int par = D.parent[s];
+        if (par >= 0) {
+            bool ok = true;
+            if (lane == 0) ok = wait_epoch(D.bdone + (size_t)par * M + m, epoch, D.err);
+            ok = __shfl_sync(FULL, ok, 0);
+            __syncwarp();
+            if (!ok && lane == 0) atomicOr(W.status + m, 8);
+        }
+        const int start = S.sup_start[s];
+        const int ns = S.sup_start[s + 1] - start;
+        const int r = S.row_ptr[s + 1] - S.row_ptr[s];
+        const int mm = ns + r;
+        double *x = W.xperm + (size_t)m * P.n_red;
+        const T *F = fronts + (size_t)m * S.front_total + S.front_off[s];
+        const int *rows = S.rows + S.row_ptr[s];
+        warp_row_dots(F + (size_t)ns * mm, 1, mm, ns, r, [&](int a) { return ldcg(x + rows[a]); },
+                      [&](int i, double acc) { tv[i] = x[start + i] - acc; });
+        __syncwarp();
+        for (int k = ns - 1; k >= 0; k--) {
+            const double tk = tv[k] * (double)F[k + k * mm];   // reciprocal of the pivot
+            if (lane == 0) x[start + k] = tk;
+            for (int i = lane; i < k; i += 32) tv[i] -= (double)F[i + k * mm] * tk;
+            __syncwarp();
+        }
+        if (lane == 0) signal_done(D.bdone + (size_t)s * M + m, epoch);
+    }
+}
+
+// Re-arms the claim counters and moves to a new epoch: done flags of the
+// previous solve no longer match.  The error flag stays raised until the
+// host clears it.
+__global__ void dag_begin_kernel(DevDag D) {
+    if (threadIdx.x < 4) D.ctr[threadIdx.x] = 0;
+    if (threadIdx.x == 0) *D.epoch += 1;
+}
+
+// The FP64 factorisation carries the right-hand side (fused forward solve);
+// the FP32 one is reused across iterations and solved by fwd_dag_kernel.
+template <class T>
+struct FusedRhs {
+    static constexpr bool value = false;
+};
+template <>
+struct FusedRhs<double> {
+    static constexpr bool value = true;
+};
+
+template <class T>
+int configure_one(DagGrid &g, int nsm, int small_bytes, int big_bytes, int vec_bytes) {
+    constexpr bool R = FusedRhs<T>::value;
+    int occ = 0;
+    if (cudaFuncSetAttribute(factor_small_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, small_bytes) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, factor_small_kernel<T, R>, kThreads, small_bytes) !=
+            cudaSuccess || occ < 1)
+        return -1;
+    g.small = nsm * occ;
+    if (cudaFuncSetAttribute(factor_big_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, big_bytes) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, factor_big_kernel<T, R>, kThreads, big_bytes) !=
+            cudaSuccess || occ < 1)
+        return -1;
+    g.big = nsm * occ;
+    if (cudaFuncSetAttribute(fwd_dag_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, vec_bytes) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fwd_dag_kernel<T>, kThreads, vec_bytes) != cudaSuccess ||
+        occ < 1)
+        return -1;
+    g.fwd = nsm * occ;
+    if (cudaFuncSetAttribute(bwd_dag_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, vec_bytes) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bwd_dag_kernel<T>, kThreads, vec_bytes) != cudaSuccess ||
+        occ < 1)
+        return -1;
+    g.bwd = nsm * occ;
+    return 0;
+}
+
+int blocks_for(int grid_max, long long warp_tasks, int per_block) {
+    const long long need = (warp_tasks + per_block - 1) / per_block;
+    return (int)(need < grid_max ? (need > 0 ? need : 1) : grid_max);
+}
+
+}  // namespace
+
+int dag_configure(const DevDag &D, int fp32, DagGrid &g) {
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -1;
+    const int es = fp32 ? 4 : 8;
+    const int small_bytes = kWarps * kSmallFront * (kSmallFront + 1) * es;
+    const int big_bytes = std::max(1, D.max_big_front * (D.max_big_front + 1)) * es;
+    const int vec_bytes = kWarps * D.max_front * 8;
+    const int rc = fp32 ? configure_one<float>(g, nsm, small_bytes, big_bytes, vec_bytes)
+                        : configure_one<double>(g, nsm, small_bytes, big_bytes, vec_bytes);
+    if (rc != 0) {
+        cudaGetLastError();
+        return -1;
+    }
+    g.small_bytes = small_bytes;
+    g.big_bytes = big_bytes;
+    g.vec_bytes = vec_bytes;
+    return 0;
+}
+
+int dag_small_front() { return kSmallFront; }
+
+void launch_dag_begin(const DevDag &D, cudaStream_t st) { dag_begin_kernel<<<1, 32, 0, st>>>(D); }
+
+template <class T>
+void launch_dag_factor(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, const DagGrid &g,
+                       T *fronts, const uint8_t *mask, cudaStream_t st) {
+    constexpr bool R = FusedRhs<T>::value;
+    const long long ts = (long long)D.n_small * P.M, tb = (long long)(D.nsup - D.n_small) * P.M;
+    if (ts > 0)
+        factor_small_kernel<T, R><<<blocks_for(g.small, ts, kWarps), kThreads, g.small_bytes, st>>>(P, W, S, D,
+                                                                                                   fronts, mask);
+    if (tb > 0)
+        factor_big_kernel<T, R><<<blocks_for(g.big, tb, 1), kThreads, g.big_bytes, st>>>(P, W, S, D, fronts, mask);
+}
+
+template <class T>
+void launch_dag_fwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, const DagGrid &g,
+                    const T *fronts, cudaStream_t st) {
+    const long long tasks = (long long)D.nsup * P.M;
+    fwd_dag_kernel<T><<<blocks_for(g.fwd, tasks, kWarps), kThreads, g.vec_bytes, st>>>(P, W, S, D, fronts);
+}
+
+template <class T>
+void launch_dag_bwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, const DagGrid &g,
+                    const T *fronts, cudaStream_t st) {
+    const long long tasks = (long long)D.nsup * P.M;
+    bwd_dag_kernel<T><<<blocks_for(g.bwd, tasks, kWarps), kThreads, g.vec_bytes, st>>>(P, W, S, D, fronts);
+}
+
+template void launch_dag_factor<double>(const DevProblem &, const DevWork &, const DevSym &, const DevDag &,
+                                        const DagGrid &, double *, const uint8_t *, cudaStream_t);
+template void launch_dag_factor<float>(const DevProblem &, const DevWork &, const DevSym &, const DevDag &,
+                                       const DagGrid &, float *, const uint8_t *, cudaStream_t);
+template void launch_dag_fwd<double>(const DevProblem &, const DevWork &, const DevSym &, const DevDag &,
+                                     const DagGrid &, const double *, cudaStream_t);
+template void launch_dag_fwd<float>(const DevProblem &, const DevWork &, const DevSym &, const DevDag &,
+                                    const DagGrid &, const float *, cudaStream_t);
+template void launch_dag_bwd<double>(const DevProblem &, const DevWork &, const DevSym &, const DevDag &,
+                                     const DagGrid &, const double *, cudaStream_t);
+template void launch_dag_bwd<float>(const DevProblem &, const DevWork &, const DevSym &, const DevDag &,
+                                    const DagGrid &, const float *, cudaStream_t);
+
+}  // namespace gp

@@ -91,6 +91,42 @@ struct DevClu {
     int max_slots;
 };
 
+// Dataflow schedule of the multifrontal factorisation and solves
+// (gp_dag.cu).  order: supernodes of the small region (every front of the
+// subtree at most 32 rows) by level, then the others by level; a topological
+// order of the assembly tree.
+struct DevDag {
+    int nsup, n_small;
+    int max_front, max_big_front;
+    const int *order;       // [nsup]
+    const int *rank;        // [nsup] position in order
+    const int *parent;      // [nsup] parent supernode or -1
+    int *ctr;               // [4] claim counters: small factor, big factor, forward, backward
+    int *epoch;             // [1] current solve
+    int *err;               // [1] a wait gave up (sticky until the host clears it)
+    int *fdone, *xdone, *bdone;   // [nsup][M] epoch at which the task finished
+};
+
+struct DagGrid {
+    int small = 0, big = 0, fwd = 0, bwd = 0;          // resident blocks
+    int small_bytes = 0, big_bytes = 0, vec_bytes = 0; // dynamic shared memory
+};
+
+int dag_configure(const DevDag &D, int fp32, DagGrid &g);
+// launch_dag_factor<double> also does the forward solve (the right-hand side
+// rides along as an extra front column); launch_dag_factor<float> does not.
+int dag_small_front();
+void launch_dag_begin(const DevDag &D, cudaStream_t st);
+template <class T>
+void launch_dag_factor(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, const DagGrid &g,
+                       T *fronts, const uint8_t *mask, cudaStream_t st);
+template <class T>
+void launch_dag_fwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, const DagGrid &g,
+                    const T *fronts, cudaStream_t st);
+template <class T>
+void launch_dag_bwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, const DagGrid &g,
+                    const T *fronts, cudaStream_t st);
+
 // launches (gp_kernels.cu)
 void launch_cluster(const DevProblem &P, const DevWork &W, const DevClu &C, int want_f, cudaStream_t st);
 void launch_network(const DevProblem &P, const DevWork &W, int want_f, cudaStream_t st);
