@@ -99,8 +99,6 @@ struct gp_layout {
     int *d_state_maps = nullptr;   // state_bus then red_of
     int *h_flag = nullptr;         // pinned
     double *h_dt = nullptr;        // pinned
-    std::vector<int> lvl_max_front;
-    int smem_limit = 0;
     // faults of the current call
     int n_fl = 0;
     int *d_fl_on_step = nullptr, *d_fl_off_step = nullptr, *d_fl_scen = nullptr;
@@ -125,8 +123,17 @@ struct gp_layout {
     gp::DevClu C{};
     // dataflow schedule of the reduced-system factorisation and solves
     gp::DevDag D{};
-    gp::DagGrid G64;
-    int solve_graph_launches = 0;
+    gp::DagGrid G64, G32;
+    gp::DevBlk B{};
+    // mixed-precision solver: kept FP32 factors (allocated on first use)
+    gp::DevMixed Mx{};
+    bool mixed_ready = false;
+    int solver = -1;                          // solver the graphs were captured for
+    cudaGraphExec_t g_solve_keep = nullptr;   // mixed: solve with the kept factors
+    int solve_graph_launches = 0, keep_graph_launches = 0;
+    double refreshes = 0.0;                   // mixed: scenario factor refreshes in the last call
+    int mx_max_age = 1, mx_exact_after = 8;   // mixed solver policy (gp_set_mixed_policy)
+    double mx_rho_max = 0.1;
 };
 
 namespace {
@@ -143,7 +150,6 @@ struct Plan {
     gp::Symbolic sym;
     std::vector<int> acp, acpos, avp, avpos, avidx;
     std::vector<double> acval;
-    std::vector<int> lvl_max_front;
     int64_t sum_w2 = 0;
 };
 
@@ -361,26 +367,138 @@ void make_plan(const gp_problem *pr, Plan &pl) {
         }
         pl.avp[s + 1] = (int)pl.avpos.size();
     }
-    pl.lvl_max_front.assign(sym.nlevels, 0);
-    for (int l = 0; l < sym.nlevels; l++)
-        for (int q = sym.level_ptr[l]; q < sym.level_ptr[l + 1]; q++)
-            pl.lvl_max_front[l] = std::max(pl.lvl_max_front[l], sym.front_m(sym.level_sups[q]));
 }
 
-// Host emulation of the device factorisation and solves, same data layout
-// and the same operation order as factor_kernel / fwd_kernel / bwd_kernel.
-// x: right-hand side in permuted order on entry, solution on exit.
-int host_factor_solve(const Plan &pl, const std::vector<double> &svar, std::vector<double> &x) {
+// Split of the assembly tree for the triangular solves (gp_solve.cu), on
+// the host: blocks are the largest subtrees within the per-warp staging
+// budget; the supernodes above them form the top region, grouped by level.
+struct HostBlk {
+    int nblk = 0;
+    int max_n = 1, max_l = 1, max_v = 1, max_p = 1, max_map = 1, max_ext = 1;
+    std::vector<int> blk_ptr{0}, map_ptr{0}, ext_ptr{0}, map_fwd, map_bwd, ext_pos, ext_row;
+    std::vector<int4> ent0, ent1;
+    int n_top_levels = 0, top_max_front = 1;
+    std::vector<int> top_ptr, top_sups;
+};
+
+void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
+    constexpr long kLimSlices = 2048, kLimRows = 512, kLimSups = 64;
+    const int ns = sym.nsup;
+    std::vector<long> sl(ns, 0), sv(ns, 0), sn(ns, 0);
+    for (int l = 0; l < sym.nlevels; l++)
+        for (int q = sym.level_ptr[l]; q < sym.level_ptr[l + 1]; q++) {
+            const int s = sym.level_sups[q];
+            const long m = sym.front_m(s), n = sym.front_n(s), r = sym.front_r(s);
+            sl[s] = m * n + n * r;
+            sv[s] = m;
+            sn[s] = 1;
+            for (int c = sym.child_ptr[s]; c < sym.child_ptr[s + 1]; c++) {
+                const int ch = sym.children[c];
+                sl[s] += sl[ch];
+                sv[s] += sv[ch];
+                sn[s] += sn[ch];
+            }
+        }
+    auto fits = [&](int s) { return sl[s] <= kLimSlices && sv[s] <= kLimRows && sn[s] <= kLimSups; };
+    // levels run from the leaves (0) to the roots, so parents are visited
+    // before their children here
+    std::vector<int> blk_of(ns, -1);
+    int nblk = 0;
+    for (int l = sym.nlevels - 1; l >= 0; l--)
+        for (int q = sym.level_ptr[l]; q < sym.level_ptr[l + 1]; q++) {
+            const int s = sym.level_sups[q], p = sym.parent[s];
+            if (fits(s) && (p < 0 || !fits(p))) blk_of[s] = nblk++;
+            else if (p >= 0 && blk_of[p] >= 0) blk_of[s] = blk_of[p];
+        }
+    // members by level: children before parents, the block's root last
+    std::vector<std::vector<int>> members(nblk);
+    for (int l = 0; l < sym.nlevels; l++)
+        for (int q = sym.level_ptr[l]; q < sym.level_ptr[l + 1]; q++) {
+            const int s = sym.level_sups[q];
+            if (blk_of[s] >= 0) members[blk_of[s]].push_back(s);
+        }
+    std::vector<int> voff_of(ns, -1);
+    for (int b = 0; b < nblk; b++) {
+        int lo = 0, vo = 0, mo = 0, po = 0;
+        for (int s : members[b]) {
+            const int m = sym.front_m(s), n = sym.front_n(s), r = sym.front_r(s);
+            B.ent0.push_back(make_int4(s, sym.sup_start[s], n, r));
+            B.ent1.push_back(make_int4(lo, vo, mo, po));
+            voff_of[s] = vo;
+            lo += m * n + n * r;
+            vo += m;
+            mo += r;
+            po += n;
+        }
+        std::map<int, int> ext;
+        for (int s : members[b]) {
+            const int r = sym.front_r(s), p = sym.parent[s];
+            const bool root = s == members[b].back();
+            for (int a = 0; a < r; a++) {
+                B.map_fwd.push_back(root ? -1 : voff_of[p] + sym.relmap[sym.relmap_ptr[s] + a]);
+                const int g = sym.rows[sym.row_ptr[s] + a], owner = sym.sup_of[g];
+                if (blk_of[owner] == b) {
+                    B.map_bwd.push_back(voff_of[owner] + (g - sym.sup_start[owner]));
+                } else {
+                    auto it = ext.find(g);
+                    if (it == ext.end()) it = ext.emplace(g, vo + (int)ext.size()).first;
+                    B.map_bwd.push_back(it->second);
+                }
+            }
+        }
+        for (auto &kv : ext) {
+            B.ext_pos.push_back(kv.second);
+            B.ext_row.push_back(kv.first);
+        }
+        B.max_n = std::max(B.max_n, (int)members[b].size());
+        B.max_l = std::max(B.max_l, lo);
+        B.max_v = std::max(B.max_v, vo + (int)ext.size());
+        B.max_p = std::max(B.max_p, po);
+        B.max_map = std::max(B.max_map, mo);
+        B.max_ext = std::max(B.max_ext, (int)ext.size());
+        B.blk_ptr.push_back((int)B.ent0.size());
+        B.map_ptr.push_back((int)B.map_fwd.size());
+        B.ext_ptr.push_back((int)B.ext_pos.size());
+    }
+    B.nblk = nblk;
+    // top region by level (leaves of the region first)
+    std::vector<int> tlev(ns, -1);
+    int ntl = 0;
+    for (int l = 0; l < sym.nlevels; l++)
+        for (int q = sym.level_ptr[l]; q < sym.level_ptr[l + 1]; q++) {
+            const int s = sym.level_sups[q];
+            if (blk_of[s] >= 0) continue;
+            int d = 0;
+            for (int c = sym.child_ptr[s]; c < sym.child_ptr[s + 1]; c++)
+                if (blk_of[sym.children[c]] < 0) d = std::max(d, tlev[sym.children[c]] + 1);
+            tlev[s] = d;
+            ntl = std::max(ntl, d + 1);
+            B.top_max_front = std::max(B.top_max_front, sym.front_m(s));
+        }
+    B.top_ptr.assign(ntl + 1, 0);
+    B.top_sups.clear();
+    for (int d = 0; d < ntl; d++) {
+        for (int s = 0; s < ns; s++)
+            if (tlev[s] == d) B.top_sups.push_back(s);
+        B.top_ptr[d + 1] = (int)B.top_sups.size();
+    }
+    B.n_top_levels = ntl;
+}
+
+// Host emulation of the device factorisation (gp_dag.cu): the same front
+// layout, assembly order and pivot rule, supernodes by level; the diagonal
+// keeps the reciprocal of each pivot, as on the device.  Returns the number
+// of zero pivots.
+int host_factor(const Plan &pl, const std::vector<double> &svar, std::vector<double> &fronts, std::vector<int> &ipiv) {
     const gp::Symbolic &S = pl.sym;
-    std::vector<double> fronts(S.front_off[S.nsup]), uvec(std::max<int64_t>(1, S.uvec_off[S.nsup]));
-    std::vector<int> ipiv(S.n);
+    fronts.assign(S.front_off[S.nsup], 0.0);
+    ipiv.assign(S.n, 0);
     int zero_pivots = 0;
     for (int l = 0; l < S.nlevels; l++)
         for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
             const int s = S.level_sups[q];
             const int ns = S.front_n(s), mm = S.front_m(s), start = S.sup_start[s];
             double *F = fronts.data() + S.front_off[s];
-            std::fill(F, F + (size_t)mm * mm, 0.0);
             for (int e = pl.acp[s]; e < pl.acp[s + 1]; e++) F[pl.acpos[e]] += pl.acval[e];
             for (int e = pl.avp[s]; e < pl.avp[s + 1]; e++) F[pl.avpos[e]] += svar[pl.avidx[e]];
             for (int cq = S.child_ptr[s]; cq < S.child_ptr[s + 1]; cq++) {
@@ -406,8 +524,17 @@ int host_factor_solve(const Plan &pl, const std::vector<double> &svar, std::vect
                 for (int i = k + 1; i < mm; i++) F[i + k * mm] *= inv;
                 for (int j = k + 1; j < mm; j++)
                     for (int i = k + 1; i < mm; i++) F[i + j * mm] -= F[i + k * mm] * F[k + j * mm];
+                F[k + k * mm] = inv;
             }
         }
+    return zero_pivots;
+}
+
+// Level-order forward and backward solves with the factors of host_factor.
+// x: right-hand side in permuted order on entry, solution on exit.
+void host_level_solve(const gp::Symbolic &S, const std::vector<double> &fronts, const std::vector<int> &ipiv,
+                      std::vector<double> &x) {
+    std::vector<double> uvec(std::max<int64_t>(1, S.uvec_off[S.nsup]));
     for (int l = 0; l < S.nlevels; l++)
         for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
             const int s = S.level_sups[q];
@@ -448,12 +575,153 @@ int host_factor_solve(const Plan &pl, const std::vector<double> &svar, std::vect
                 t[i] = x[start + i] - acc;
             }
             for (int k = ns - 1; k >= 0; k--) {
-                t[k] /= F[k + k * mm];
+                t[k] *= F[k + k * mm];
                 for (int i = 0; i < k; i++) t[i] -= F[i + k * mm] * t[k];
             }
             std::copy(t.begin(), t.end(), x.begin() + start);
         }
-    return zero_pivots;
+}
+
+// Bounds-checked stand-in for one warp's shared-memory staging array.
+struct Staged {
+    std::vector<double> v;
+    const char *what;
+    Staged(size_t n, const char *w) : v(n, 0.0), what(w) {}
+    double &operator[](long i) {
+        if (i < 0 || i >= (long)v.size()) fail(GP_E_INTERNAL, "block solve: %s index %ld outside [0, %zu)", what, i, v.size());
+        return v[(size_t)i];
+    }
+};
+
+// Host emulation of the blocked triangular solves (gp_solve.cu) with the
+// same staging areas, sized by the block maxima, and every staged index
+// checked against them: blocks forward, top region forward by level, top
+// region backward, blocks backward.
+void host_block_solve(const gp::Symbolic &S, const HostBlk &B, const std::vector<double> &fronts,
+                      const std::vector<int> &ipiv, std::vector<double> &x) {
+    std::vector<double> uvec(std::max<int64_t>(1, S.uvec_off[S.nsup]), 0.0);
+    auto ent = [&](int e, int4 &a, int4 &b) {
+        a = B.ent0[e];
+        b = B.ent1[e];
+        if (a.z != S.front_n(a.x) || a.w != S.front_r(a.x) || a.y != S.sup_start[a.x])
+            fail(GP_E_INTERNAL, "block solve: entry %d does not describe supernode %d", e, a.x);
+    };
+    for (int blk = 0; blk < B.nblk; blk++) {
+        Staged Ls(B.max_l, "factor slice"), vs(B.max_v, "vector"), pv(B.max_p, "pivot"), mp(B.max_map, "map");
+        const int e0 = B.blk_ptr[blk], n = B.blk_ptr[blk + 1] - e0;
+        if (n > B.max_n) fail(GP_E_INTERNAL, "block solve: %d entries above max_n", n);
+        const int mb = B.map_ptr[blk], nmap = B.map_ptr[blk + 1] - mb;
+        for (int i = 0; i < nmap; i++) mp[i] = B.map_fwd[mb + i];
+        for (int q = 0; q < n; q++) {
+            int4 a, b;
+            ent(e0 + q, a, b);
+            const int ns = a.z, mm = a.z + a.w;
+            for (int i = 0; i < mm * ns; i++) Ls[b.x + i] = fronts[S.front_off[a.x] + i];
+            for (int i = 0; i < ns; i++) {
+                vs[b.y + i] = x[a.y + i];
+                pv[b.w + i] = ipiv[a.y + i];
+            }
+            for (int i = 0; i < a.w; i++) vs[b.y + ns + i] = 0.0;
+        }
+        for (int q = 0; q < n; q++) {
+            int4 a, b;
+            ent(e0 + q, a, b);
+            const int s = a.x, start = a.y, ns = a.z, r = a.w, mm = ns + r;
+            for (int k = 0; k < ns; k++) {
+                const int p = (int)pv[b.w + k];
+                if (p < k || p >= ns) fail(GP_E_INTERNAL, "block solve: pivot %d of supernode %d out of range", p, s);
+                if (p != k) std::swap(vs[b.y + k], vs[b.y + p]);
+            }
+            for (int k = 0; k < ns; k++)
+                for (int i = k + 1; i < ns; i++) vs[b.y + i] -= Ls[b.x + i + k * mm] * vs[b.y + k];
+            for (int i = 0; i < r; i++) {
+                double acc = 0.0;
+                for (int k = 0; k < ns; k++) acc += Ls[b.x + ns + i + k * mm] * vs[b.y + k];
+                vs[b.y + ns + i] -= acc;
+            }
+            if (q < n - 1) {
+                for (int i = 0; i < r; i++) vs[(long)mp[b.z + i]] += vs[b.y + ns + i];
+            } else {
+                for (int i = 0; i < r; i++) uvec[S.uvec_off[s] + i] = vs[b.y + ns + i];
+            }
+            for (int i = 0; i < ns; i++) x[start + i] = vs[b.y + i];
+        }
+    }
+    auto top_fwd = [&](int s) {
+        const int start = S.sup_start[s], ns = S.front_n(s), r = S.front_r(s), mm = ns + r;
+        Staged tv(B.top_max_front, "top vector");
+        for (int i = 0; i < ns; i++) tv[i] = x[start + i];
+        for (int cq = S.child_ptr[s]; cq < S.child_ptr[s + 1]; cq++) {
+            const int c = S.children[cq];
+            const int *rel = S.relmap.data() + S.relmap_ptr[c];
+            for (int a = 0; a < S.front_r(c); a++) tv[rel[a]] += uvec[S.uvec_off[c] + a];
+        }
+        const double *F = fronts.data() + S.front_off[s];
+        for (int k = 0; k < ns; k++)
+            if (ipiv[start + k] != k) std::swap(tv[k], tv[ipiv[start + k]]);
+        for (int k = 0; k < ns; k++)
+            for (int i = k + 1; i < ns; i++) tv[i] -= F[i + k * mm] * tv[k];
+        for (int a = 0; a < r; a++) {
+            double acc = 0.0;
+            for (int k = 0; k < ns; k++) acc += F[ns + a + (size_t)k * mm] * tv[k];
+            uvec[S.uvec_off[s] + a] = tv[ns + a] - acc;
+        }
+        for (int i = 0; i < ns; i++) x[start + i] = tv[i];
+    };
+    auto top_bwd = [&](int s) {
+        const int start = S.sup_start[s], ns = S.front_n(s), r = S.front_r(s), mm = ns + r;
+        Staged tv(B.top_max_front, "top vector");
+        const double *F = fronts.data() + S.front_off[s];
+        const int *rows = S.rows.data() + S.row_ptr[s];
+        for (int i = 0; i < ns; i++) {
+            double acc = 0.0;
+            for (int a = 0; a < r; a++) acc += F[i + (size_t)(ns + a) * mm] * x[rows[a]];
+            tv[i] = x[start + i] - acc;
+        }
+        for (int k = ns - 1; k >= 0; k--) {
+            const double tk = tv[k] * F[k + k * mm];
+            x[start + k] = tk;
+            for (int i = 0; i < k; i++) tv[i] -= F[i + k * mm] * tk;
+        }
+    };
+    for (int l = 0; l < B.n_top_levels; l++)
+        for (int q = B.top_ptr[l]; q < B.top_ptr[l + 1]; q++) top_fwd(B.top_sups[q]);
+    for (int l = B.n_top_levels - 1; l >= 0; l--)
+        for (int q = B.top_ptr[l]; q < B.top_ptr[l + 1]; q++) top_bwd(B.top_sups[q]);
+    for (int blk = 0; blk < B.nblk; blk++) {
+        Staged Ls(B.max_l, "factor slice"), vs(B.max_v, "vector"), mp(B.max_map, "map");
+        const int e0 = B.blk_ptr[blk], n = B.blk_ptr[blk + 1] - e0;
+        const int mb = B.map_ptr[blk], nmap = B.map_ptr[blk + 1] - mb;
+        for (int i = 0; i < nmap; i++) mp[i] = B.map_bwd[mb + i];
+        const int xb = B.ext_ptr[blk], next = B.ext_ptr[blk + 1] - xb;
+        if (next > B.max_ext) fail(GP_E_INTERNAL, "block solve: %d external rows above max_ext", next);
+        for (int q = 0; q < n; q++) {
+            int4 a, b;
+            ent(e0 + q, a, b);
+            const int ns = a.z, r = a.w, mm = ns + r;
+            const double *src = fronts.data() + S.front_off[a.x];
+            for (int i = 0; i < mm * ns; i++) Ls[b.x + i] = src[i];
+            for (int e = 0; e < ns * r; e++) Ls[b.x + mm * ns + e] = src[e % ns + (size_t)(ns + e / ns) * mm];
+            for (int i = 0; i < ns; i++) vs[b.y + i] = x[a.y + i];
+        }
+        for (int k = 0; k < next; k++) vs[B.ext_pos[xb + k]] = x[B.ext_row[xb + k]];
+        for (int q = n - 1; q >= 0; q--) {
+            int4 a, b;
+            ent(e0 + q, a, b);
+            const int start = a.y, ns = a.z, r = a.w, mm = ns + r;
+            for (int i = 0; i < ns; i++) {
+                double acc = 0.0;
+                for (int c = 0; c < r; c++) acc += Ls[b.x + mm * ns + i + c * ns] * vs[(long)mp[b.z + c]];
+                vs[b.y + i] -= acc;
+            }
+            for (int k = ns - 1; k >= 0; k--) {
+                const double tk = vs[b.y + k] * Ls[b.x + k + k * mm];
+                vs[b.y + k] = tk;
+                for (int i = 0; i < k; i++) vs[b.y + i] -= Ls[b.x + i + k * mm] * tk;
+            }
+            for (int i = 0; i < ns; i++) x[start + i] = vs[b.y + i];
+        }
+    }
 }
 
 // Task order of the dataflow kernels: supernodes whose whole subtree has
@@ -494,6 +762,34 @@ void build_dag(gp_layout *L, const gp::Symbolic &sym) {
     D.rank = A.upload(rank);
     D.parent = A.upload(sym.parent);
     if (gp::dag_configure(D, 0, L->G64) != 0) fail(GP_E_CUDA, "could not configure the dataflow kernels");
+}
+
+void build_blocks(gp_layout *L, const gp::Symbolic &sym) {
+    HostBlk H;
+    make_blocks(sym, H);
+    DeviceArena &A = L->arena;
+    gp::DevBlk &B = L->B;
+    B.nblk = H.nblk;
+    B.max_n = H.max_n;
+    B.max_l = H.max_l;
+    B.max_v = H.max_v;
+    B.max_p = H.max_p;
+    B.max_map = H.max_map;
+    B.max_ext = H.max_ext;
+    B.blk_ptr = A.upload(H.blk_ptr);
+    B.ent0 = A.upload(H.ent0);
+    B.ent1 = A.upload(H.ent1);
+    B.map_ptr = A.upload(H.map_ptr);
+    B.map_fwd = A.upload(H.map_fwd);
+    B.map_bwd = A.upload(H.map_bwd);
+    B.ext_ptr = A.upload(H.ext_ptr);
+    B.ext_pos = A.upload(H.ext_pos);
+    B.ext_row = A.upload(H.ext_row);
+    B.n_top_levels = H.n_top_levels;
+    B.top_max_front = H.top_max_front;
+    B.top_ptr = A.upload(H.top_ptr);
+    B.top_sups = A.upload(H.top_sups);
+    if (gp::solve_configure(B) != 0) fail(GP_E_CUDA, "could not configure the solve kernels");
 }
 
 void build_problem(gp_layout *L, const gp_problem *pr) {
@@ -591,7 +887,6 @@ void build_problem(gp_layout *L, const gp_problem *pr) {
     S.relmap = A.upload(sym.relmap);
     S.front_off = A.upload(sym.front_off);
     S.uvec_off = A.upload(sym.uvec_off);
-    S.level_sups = A.upload(sym.level_sups);
     S.front_total = sym.front_off[sym.nsup];
     S.uvec_total = sym.uvec_off[sym.nsup];
     S.asmc_ptr = A.upload(pl.acp);
@@ -600,13 +895,9 @@ void build_problem(gp_layout *L, const gp_problem *pr) {
     S.asmv_ptr = A.upload(pl.avp);
     S.asmv_pos = A.upload(pl.avpos);
     S.asmv_idx = A.upload(pl.avidx);
-    L->lvl_max_front = pl.lvl_max_front;
     L->sym = pl.sym;
     build_dag(L, sym);
-    L->smem_limit = gp::factor_smem_limit();
-    if (L->smem_limit < 0) fail(GP_E_CUDA, "could not configure the factorisation kernel's shared memory");
-    if ((size_t)sym.max_front * sym.max_front * sizeof(double) > (size_t)L->smem_limit)
-        fail(GP_E_INVALID, "largest front (%d) exceeds shared memory (%d bytes)", sym.max_front, L->smem_limit);
+    build_blocks(L, sym);
 }
 
 void build_work(gp_layout *L, const double *z0, const double *u0, const double *p) {
@@ -628,12 +919,22 @@ void build_work(gp_layout *L, const double *z0, const double *u0, const double *
     W.active = A.alloc<uint8_t>(M);
     W.iters = A.alloc<int>(M);
     W.status = A.alloc<int>(M);
-    W.flag = A.alloc<int>(1);
+    W.flag = A.alloc<int>(2);
     W.dt = A.alloc<double>(1);
     DevSym &S = L->S;
     S.fronts = A.alloc<double>(M * S.front_total);
     S.uvec = A.alloc<double>(M * std::max<int64_t>(1, S.uvec_total));
     S.ipiv = A.alloc<int>(M * S.n);
+    {
+        // no row swaps until a factorisation has run: the solves of a
+        // scenario whose factors were never computed stay in bounds
+        std::vector<int> ident((size_t)M * S.n);
+        for (size_t m = 0; m < M; m++)
+            for (int s = 0; s < L->sym.nsup; s++)
+                for (int c = L->sym.sup_start[s]; c < L->sym.sup_start[s + 1]; c++)
+                    ident[m * S.n + c] = c - L->sym.sup_start[s];
+        ck(cudaMemcpy(S.ipiv, ident.data(), ident.size() * sizeof(int), cudaMemcpyHostToDevice), "ipiv");
+    }
     gp::DevDag &D = L->D;
     D.ctr = A.alloc<int>(4);
     D.epoch = A.alloc<int>(1);
@@ -648,7 +949,7 @@ void build_work(gp_layout *L, const double *z0, const double *u0, const double *
     ck(cudaMemset(D.xdone, 0, M * D.nsup * sizeof(int)), "memset");
     ck(cudaMemset(D.bdone, 0, M * D.nsup * sizeof(int)), "memset");
     ck(cudaMemset(W.status, 0, M * sizeof(int)), "memset");
-    ck(cudaMallocHost(&L->h_flag, sizeof(int)), "cudaMallocHost");
+    ck(cudaMallocHost(&L->h_flag, 2 * sizeof(int)), "cudaMallocHost");
     ck(cudaMallocHost(&L->h_dt, sizeof(double)), "cudaMallocHost");
     ck(cudaStreamCreateWithFlags(&L->st, cudaStreamNonBlocking), "stream");
     for (int i = 0; i < 8; i++) ck(cudaEventCreate(&L->pev[i]), "event");
@@ -730,44 +1031,62 @@ void set_faults(gp_layout *L, int n_faults, const gp_fault *faults) {
     L->h_fl_off_step = off;
     L->h_fl_scen = scen;
     // graphs capture the fault pointers: rebuild them
-    if (L->g_eval) { cudaGraphExecDestroy(L->g_eval); L->g_eval = nullptr; }
-    if (L->g_solve) { cudaGraphExecDestroy(L->g_solve); L->g_solve = nullptr; }
+    for (cudaGraphExec_t *g : {&L->g_eval, &L->g_solve, &L->g_solve_keep})
+        if (*g) {
+            cudaGraphExecDestroy(*g);
+            *g = nullptr;
+        }
 }
 
 void mark(gp_layout *L, int i) {
     ck(cudaEventRecordWithFlags(L->pev[i], L->st, cudaEventRecordExternal), "event record");
 }
 
-void enqueue_solve(gp_layout *L) {
+// Solve graph.  FP64: fresh factorisation (with the forward solve fused),
+// backward solve, update.  Mixed, refresh=true: FP32 factorisation of the
+// scenarios refreshing their factors, then both solves with the kept FP32
+// factors; refresh=false: the solves alone.
+int enqueue_solve(gp_layout *L, bool mixed, bool refresh) {
     const gp::DevDag &D = L->D;
+    const int nfac = (D.n_small > 0) + (D.nsup > D.n_small);
     mark(L, 3);
     gp::launch_dag_begin(D, L->st);
-    gp::launch_dag_factor<double>(L->P, L->W, L->S, D, L->G64, L->S.fronts, L->W.active, L->st);
-    mark(L, 4);   // the FP64 factorisation includes the forward solve
-    mark(L, 5);
-    gp::launch_dag_bwd<double>(L->P, L->W, L->S, D, L->G64, L->S.fronts, L->st);
+    const gp::DevBlk &B = L->B;
+    const int nsolve = (B.nblk > 0) + (B.n_top_levels > 0);
+    if (!mixed) {
+        gp::launch_dag_factor<double>(L->P, L->W, L->S, D, L->G64, L->S.fronts, L->W.active, L->st);
+        mark(L, 4);   // the FP64 factorisation includes the forward solve
+        mark(L, 5);
+        gp::launch_solve_bwd<double>(L->P, L->W, L->S, B, L->S.fronts, L->st);
+    } else {
+        if (refresh) gp::launch_dag_factor<float>(L->P, L->W, L->S, D, L->G32, L->Mx.fronts, L->Mx.refac, L->st);
+        mark(L, 4);
+        gp::launch_solve_fwd<float>(L->P, L->W, L->S, B, L->Mx.fronts, L->st);
+        mark(L, 5);
+        gp::launch_solve_bwd<float>(L->P, L->W, L->S, B, L->Mx.fronts, L->st);
+    }
     mark(L, 6);
     gp::launch_update(L->P, L->W, L->S, L->d_state_maps, L->st);
     mark(L, 7);
-    L->solve_graph_launches = 1 + (D.n_small > 0) + (D.nsup > D.n_small) + 2;
+    return 1 + (mixed ? (refresh ? nfac : 0) + 2 * nsolve : nfac + nsolve) + 1;
 }
 
 void enqueue_eval(gp_layout *L, double tol, int itermax) {
-    gp::launch_reset_norm(L->P, L->W, L->st);
+    gp::launch_reset_norm(L->P, L->W, L->Mx, L->st);
     mark(L, 0);
-    gp::launch_cluster(L->P, L->W, L->C, 0, L->st);
+    gp::launch_cluster(L->P, L->W, L->C, L->Mx, 0, L->st);
     mark(L, 1);
     gp::launch_network(L->P, L->W, 0, L->st);
     mark(L, 2);
-    gp::launch_check(L->P, L->W, tol, itermax, L->st);
-    ck(cudaMemcpyAsync(L->h_flag, L->W.flag, sizeof(int), cudaMemcpyDeviceToHost, L->st), "flag copy");
+    gp::launch_check(L->P, L->W, L->Mx, tol, itermax, L->st);
+    ck(cudaMemcpyAsync(L->h_flag, L->W.flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, L->st), "flag copy");
 }
 
-cudaGraphExec_t capture(gp_layout *L, bool eval, double tol, int itermax) {
+template <class F>
+cudaGraphExec_t capture(gp_layout *L, F enqueue) {
     cudaGraph_t g;
     ck(cudaStreamBeginCapture(L->st, cudaStreamCaptureModeThreadLocal), "begin capture");
-    if (eval) enqueue_eval(L, tol, itermax);
-    else enqueue_solve(L);
+    enqueue();
     ck(cudaStreamEndCapture(L->st, &g), "end capture");
     cudaGraphExec_t ex;
     ck(cudaGraphInstantiate(&ex, g, 0), "graph instantiate");
@@ -775,17 +1094,59 @@ cudaGraphExec_t capture(gp_layout *L, bool eval, double tol, int itermax) {
     return ex;
 }
 
-void ensure_graphs(gp_layout *L, double tol, int itermax) {
-    if (L->g_eval && (L->graph_tol != tol || L->graph_itermax != itermax)) {
-        cudaGraphExecDestroy(L->g_eval);
-        L->g_eval = nullptr;
-    }
+void drop_graphs(gp_layout *L) {
+    for (cudaGraphExec_t *g : {&L->g_eval, &L->g_solve, &L->g_solve_keep})
+        if (*g) {
+            cudaGraphExecDestroy(*g);
+            *g = nullptr;
+        }
+}
+
+// Kept FP32 factors of the mixed solver, allocated on its first use.
+void ensure_mixed(gp_layout *L) {
+    if (L->mixed_ready) return;
+    DeviceArena &A = L->arena;
+    const size_t M = L->M;
+    gp::DevMixed &X = L->Mx;
+    int n_lu = 1;
+    for (int v : L->cplan.rhs_base) n_lu = std::max(n_lu, v);
+    X.n_lu = n_lu;
+    X.max_age = L->mx_max_age;
+    X.exact_after = L->mx_exact_after;
+    X.rho_max = L->mx_rho_max;
+    X.refac = A.alloc<uint8_t>(M);
+    X.refac_next = A.alloc<uint8_t>(M);
+    X.age = A.alloc<int>(M);
+    X.prev_norm = A.alloc<double>(M);
+    X.lu = A.alloc<float>(M * std::max(1, L->C.n_tasks) * n_lu * 32);
+    X.cc = A.alloc<float>(M * std::max(1, L->P.n_cl) * 6);
+    X.fronts = A.alloc<float>(M * L->S.front_total);
+    ck(cudaMemset(X.refac, 0, M), "memset");
+    ck(cudaMemset(X.refac_next, 0, M), "memset");
+    ck(cudaMemset(X.age, 0, M * sizeof(int)), "memset");
+    // kept factors start at zero (zero pivot reciprocals give a zero step,
+    // which the contraction test turns into a refresh)
+    ck(cudaMemset(X.lu, 0, M * std::max(1, L->C.n_tasks) * n_lu * 32 * sizeof(float)), "memset");
+    ck(cudaMemset(X.cc, 0, M * std::max(1, L->P.n_cl) * 6 * sizeof(float)), "memset");
+    ck(cudaMemset(X.fronts, 0, M * L->S.front_total * sizeof(float)), "memset");
+    if (gp::dag_configure(L->D, 1, L->G32) != 0) fail(GP_E_CUDA, "could not configure the FP32 dataflow kernels");
+    L->mixed_ready = true;
+}
+
+void ensure_graphs(gp_layout *L, double tol, int itermax, int solver) {
+    if (L->solver != solver || L->graph_tol != tol || L->graph_itermax != itermax) drop_graphs(L);
+    const bool mixed = solver == GP_SOLVER_SCHUR_MIXED;
+    if (mixed) ensure_mixed(L);
+    L->Mx.on = mixed ? 1 : 0;
     if (!L->g_eval) {
-        L->g_eval = capture(L, true, tol, itermax);
+        L->g_eval = capture(L, [&] { enqueue_eval(L, tol, itermax); });
         L->graph_tol = tol;
         L->graph_itermax = itermax;
+        L->solver = solver;
     }
-    if (!L->g_solve) L->g_solve = capture(L, false, tol, itermax);
+    if (!L->g_solve) L->g_solve = capture(L, [&] { L->solve_graph_launches = enqueue_solve(L, mixed, true); });
+    if (mixed && !L->g_solve_keep)
+        L->g_solve_keep = capture(L, [&] { L->keep_graph_launches = enqueue_solve(L, true, false); });
 }
 
 // One Newton solve for the scenarios marked active; returns after every
@@ -796,10 +1157,15 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
     return ms;
 }
 
-void newton(gp_layout *L, double dt, double tol, int itermax) {
+void newton(gp_layout *L, double dt, double tol, int itermax, bool force_refresh) {
     *L->h_dt = dt;
     ck(cudaMemcpyAsync(L->W.dt, L->h_dt, sizeof(double), cudaMemcpyHostToDevice, L->st), "dt");
     ck(cudaMemsetAsync(L->W.iters, 0, L->M * sizeof(int), L->st), "memset");
+    const bool mixed = L->Mx.on != 0;
+    if (mixed) {
+        gp::launch_mixed_start(L->P, L->W, L->Mx, force_refresh ? 1 : 0, L->st);
+        L->launches += 1;
+    }
     bool solve_pending = false;
     for (int guard = 0; guard <= itermax + 1; guard++) {
         ck(cudaGraphLaunch(L->g_eval, L->st), "graph launch");
@@ -814,11 +1180,13 @@ void newton(gp_layout *L, double dt, double tol, int itermax) {
             L->ph_ms[5] += elapsed(L->pev[6], L->pev[7]);
             solve_pending = false;
         }
-        if (*L->h_flag == 0) return;
-        ck(cudaGraphLaunch(L->g_solve, L->st), "graph launch");
+        if (L->h_flag[0] == 0) return;
+        const bool refresh = !mixed || L->h_flag[1] > 0;
+        ck(cudaGraphLaunch(refresh ? L->g_solve : L->g_solve_keep, L->st), "graph launch");
         solve_pending = true;
-        L->launches += L->solve_graph_launches;
-        L->factor_launches += (L->D.n_small > 0) + (L->D.nsup > L->D.n_small);
+        L->launches += refresh ? L->solve_graph_launches : L->keep_graph_launches;
+        if (refresh) L->factor_launches += (L->D.n_small > 0) + (L->D.nsup > L->D.n_small);
+        if (mixed) L->refreshes += L->h_flag[1];
         L->solves += 1;
     }
     fail(GP_E_NUMERIC, "Newton loop did not terminate");
@@ -888,6 +1256,7 @@ int32_t gp_layout_destroy(gp_layout *L) {
     if (!L) return GP_OK;
     if (L->g_eval) cudaGraphExecDestroy(L->g_eval);
     if (L->g_solve) cudaGraphExecDestroy(L->g_solve);
+    if (L->g_solve_keep) cudaGraphExecDestroy(L->g_solve_keep);
     if (L->st) cudaStreamSynchronize(L->st);
     L->call.release();
     L->arena.release();
@@ -958,8 +1327,9 @@ int32_t gp_residual(gp_layout *L, const double *zold, double dt, int32_t n_fault
     *L->h_dt = dt;
     ck(cudaMemcpy(L->W.dt, L->h_dt, sizeof(double), cudaMemcpyHostToDevice), "dt");
     ck(cudaMemset(L->W.active, 1, L->M), "memset");
-    gp::launch_reset_norm(L->P, L->W, L->st);
-    gp::launch_cluster(L->P, L->W, L->C, 1, L->st);
+    const gp::DevMixed exact{};
+    gp::launch_reset_norm(L->P, L->W, exact, L->st);
+    gp::launch_cluster(L->P, L->W, L->C, exact, 1, L->st);
     gp::launch_network(L->P, L->W, 1, L->st);
     ck(cudaGetLastError(), "residual launch");
     ck(cudaStreamSynchronize(L->st), "residual");
@@ -972,10 +1342,11 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
     API_BEGIN
     if (!L || !opt) fail(GP_E_INVALID, "null argument");
     if (opt->n_steps < 0 || !(opt->dt > 0.0) || opt->itermax <= 0) fail(GP_E_INVALID, "bad options");
-    if (opt->solver != GP_SOLVER_SCHUR_FP64) fail(GP_E_INVALID, "solver %d is not available", opt->solver);
+    if (opt->solver != GP_SOLVER_SCHUR_FP64 && opt->solver != GP_SOLVER_SCHUR_MIXED)
+        fail(GP_E_INVALID, "solver %d is not available", opt->solver);
     const int M = L->M, ns = opt->n_steps, nsys = L->n_sys;
     set_faults(L, n_faults, faults);
-    ensure_graphs(L, opt->newton_tol, opt->itermax);
+    ensure_graphs(L, opt->newton_tol, opt->itermax, opt->solver);
     ck(cudaMemsetAsync(L->W.status, 0, M * sizeof(int), L->st), "memset");
     // event steps
     std::map<int, int> ev_steps;
@@ -999,13 +1370,18 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
     L->launches = 0;
     L->factor_launches = 0;
     L->solves = 0;
+    L->refreshes = 0;
     for (int i = 0; i < 8; i++) L->ph_ms[i] = 0.0;
     ck(cudaMemsetAsync(L->D.err, 0, sizeof(int), L->st), "memset");
+    // the mixed solver refreshes its kept factors at the first solve and
+    // around every event (the dt = 0 re-solve and the step after it)
+    bool force = true;
     for (int k = 1; k <= ns; k++) {
         ck(cudaMemcpyAsync(L->W.zold, L->W.z, (size_t)M * nsys * sizeof(double), cudaMemcpyDeviceToDevice, L->st),
            "zold");
         ck(cudaMemsetAsync(L->W.active, 1, M, L->st), "memset");
-        newton(L, opt->dt, opt->newton_tol, opt->itermax);
+        newton(L, opt->dt, opt->newton_tol, opt->itermax, force);
+        force = false;
         ck(cudaMemcpyAsync(d_iters + (size_t)(2 * (k - 1)) * M, L->W.iters, M * sizeof(int),
                            cudaMemcpyDeviceToDevice, L->st),
            "iters");
@@ -1020,7 +1396,8 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
             ck(cudaMemcpyAsync(L->W.zold, L->W.z, (size_t)M * nsys * sizeof(double), cudaMemcpyDeviceToDevice,
                                L->st),
                "zold");
-            newton(L, 0.0, opt->newton_tol, opt->itermax);
+            newton(L, 0.0, opt->newton_tol, opt->itermax, true);
+            force = true;
             ck(cudaMemcpyAsync(d_iters + (size_t)(2 * (k - 1) + 1) * M, L->W.iters, M * sizeof(int),
                                cudaMemcpyDeviceToDevice, L->st),
                "iters");
@@ -1092,7 +1469,7 @@ int32_t gp_cluster_selftest(const gp_problem *prob, const double *z, const doubl
 }
 
 int32_t gp_reduced_selftest(const gp_problem *prob, const int32_t *s_rowptr, const int32_t *s_colidx,
-                            const double *s_val, const double *rhs, double *x, double out[4]) {
+                            const double *s_val, const double *rhs, double *x, double out[8]) {
     API_BEGIN
     if (!prob || !s_rowptr || !s_colidx || !s_val || !rhs || !x || !out) fail(GP_E_INVALID, "null argument");
     Plan pl;
@@ -1125,12 +1502,42 @@ int32_t gp_reduced_selftest(const gp_problem *prob, const int32_t *s_rowptr, con
         }
     std::vector<double> xp(n);
     for (int k = 0; k < n; k++) xp[k] = rhs[pl.sym.perm[k]];
-    const int zp = host_factor_solve(pl, svar, xp);
+    std::vector<double> fronts;
+    std::vector<int> ipiv;
+    const int zp = host_factor(pl, svar, fronts, ipiv);
+    std::vector<double> xl = xp;
+    host_level_solve(pl.sym, fronts, ipiv, xl);
+    HostBlk hb;
+    make_blocks(pl.sym, hb);
+    host_block_solve(pl.sym, hb, fronts, ipiv, xp);
+    double dmax = 0.0, xmax = 0.0;
+    for (int k = 0; k < n; k++) {
+        dmax = std::max(dmax, std::fabs(xp[k] - xl[k]));
+        xmax = std::max(xmax, std::fabs(xl[k]));
+    }
     for (int k = 0; k < n; k++) x[pl.sym.perm[k]] = xp[k];
     out[0] = mism;
     out[1] = zp;
     out[2] = (double)pl.sym.nnz_lu;
     out[3] = pl.sym.nlevels;
+    out[4] = xmax > 0.0 ? dmax / xmax : dmax;
+    out[5] = hb.nblk;
+    out[6] = hb.n_top_levels;
+    out[7] = hb.max_n;
+    API_END
+}
+
+int32_t gp_set_mixed_policy(gp_layout *L, int32_t max_age, double rho_max, int32_t exact_after) {
+    API_BEGIN
+    if (!L) fail(GP_E_INVALID, "null argument");
+    if (max_age < 1 || !(rho_max > 0.0) || exact_after < 1) fail(GP_E_INVALID, "bad mixed-solver policy");
+    L->mx_max_age = max_age;
+    L->mx_rho_max = rho_max;
+    L->mx_exact_after = exact_after;
+    L->Mx.max_age = max_age;
+    L->Mx.rho_max = rho_max;
+    L->Mx.exact_after = exact_after;
+    drop_graphs(L);   // the graphs hold the policy by value
     API_END
 }
 
@@ -1148,6 +1555,7 @@ int32_t gp_last_timing(const gp_layout *L, double out[16]) {
     out[7] = L->ph_ms[5];
     out[8] = L->factor_launches;
     out[9] = L->solves;
+    out[10] = L->refreshes;
     API_END
 }
 
@@ -1220,7 +1628,7 @@ extern "C" int32_t gp_residual_static(gp_layout *L, const double *zold, double d
     W.xperm = cv.take<double>(M * std::max(1, P.n_red));
     W.norm = cv.take<unsigned long long>(M);
     W.active = cv.take<uint8_t>(M);
-    W.flag = cv.take<int>(1);
+    W.flag = cv.take<int>(2);
     W.dt = cv.take<double>(1);
     int *fl_ptr = cv.take<int>(M + 1);
     // no fault applied: every scenario's fault range is empty
@@ -1233,8 +1641,9 @@ extern "C" int32_t gp_residual_static(gp_layout *L, const double *zold, double d
     ck(cudaMemsetAsync(W.active, 1, M, st), "memset");
     ck(cudaMemcpyAsync(W.zold, zold, M * P.n_sys * sizeof(double), cudaMemcpyHostToDevice, st), "zold");
     ck(cudaMemcpyAsync(W.dt, &dt, sizeof(double), cudaMemcpyHostToDevice, st), "dt");
-    gp::launch_reset_norm(P, W, st);
-    gp::launch_cluster(P, W, L->C, 1, st);
+    const gp::DevMixed exact{};
+    gp::launch_reset_norm(P, W, exact, st);
+    gp::launch_cluster(P, W, L->C, exact, 1, st);
     gp::launch_network(P, W, 1, st);
     ck(cudaGetLastError(), "residual launch");
     ck(cudaMemcpyAsync(f, W.f, M * P.n_sys * sizeof(double), cudaMemcpyDeviceToHost, st), "residual copy");

@@ -34,6 +34,7 @@
 #include <algorithm>
 
 #include "gp_internal.h"
+#include "gp_warp.cuh"
 
 namespace gp {
 
@@ -128,30 +129,6 @@ __device__ __forceinline__ int warp_pivot(const T *F, int mm, int k, int ns, boo
     }
     zero = bk == 0;
     return bi;
-}
-
-// Next power of two >= n, for 1 <= n <= 32.
-__device__ __forceinline__ int np2(int n) { return n <= 1 ? 1 : 1 << (32 - __clz(n - 1)); }
-
-// Row dot products out_i = sum_j A[i*si + j*sj] * v(j), i < nrow, j < ncol,
-// by one warp.  Rows are spread over groups of G lanes (G = 32 / np2(nrow),
-// 1 when nrow >= 32) that split the j range and combine by shuffles in a
-// fixed order, so that short rows still fill the warp.  emit(i, acc) runs on
-// the first lane of each group.
-template <class T, class V, class E>
-__device__ __forceinline__ void warp_row_dots(const T *A, int si, int sj, int nrow, int ncol, V v, E emit) {
-    const int lane = threadIdx.x & 31;
-    const int G = nrow >= 32 ? 1 : 32 / np2(nrow);
-    const int rows_per_pass = 32 / G;
-    const int g = lane & (G - 1);
-    for (int i0 = 0; i0 < nrow; i0 += rows_per_pass) {
-        const int i = i0 + lane / G;
-        double acc = 0.0;
-        if (i < nrow)
-            for (int j = g; j < ncol; j += G) acc += (double)A[i * si + j * sj] * v(j);
-        for (int off = G >> 1; off > 0; off >>= 1) acc += __shfl_xor_sync(FULL, acc, off);
-        if (g == 0 && i < nrow) emit(i, acc);
-    }
 }
 
 // Thread groups that factor one front: a warp, or the whole CTA.
@@ -366,7 +343,7 @@ __global__ void __launch_bounds__(kThreads) fwd_dag_kernel(DevProblem P, DevWork
             __syncwarp();
         }
         double *us = uv + S.uvec_off[s];
-        warp_row_dots(F + ns, 1, mm, r, ns, [&](int k) { return tv[k]; },
+        warp_row_dots<double>(F + ns, 1, mm, r, ns, [&](int k) { return tv[k]; },
                       [&](int a, double acc) { us[a] = tv[ns + a] - acc; });
         for (int i = lane; i < ns; i += 32) x[start + i] = tv[i];
         __syncwarp();
@@ -405,7 +382,7 @@ __global__ void __launch_bounds__(kThreads) bwd_dag_kernel(DevProblem P, DevWork
         double *x = W.xperm + (size_t)m * P.n_red;
         const T *F = fronts + (size_t)m * S.front_total + S.front_off[s];
         const int *rows = S.rows + S.row_ptr[s];
-        warp_row_dots(F + (size_t)ns * mm, 1, mm, ns, r, [&](int a) { return ldcg(x + rows[a]); },
+        warp_row_dots<double>(F + (size_t)ns * mm, 1, mm, ns, r, [&](int a) { return ldcg(x + rows[a]); },
                       [&](int i, double acc) { tv[i] = x[start + i] - acc; });
         __syncwarp();
         for (int k = ns - 1; k >= 0; k--) {

@@ -54,7 +54,7 @@ struct DevWork {
     uint8_t *active;                // [M] scenario takes part in this iteration
     int *iters;                     // [M] Newton updates in the current solve
     int *status;                    // [M] 0 ok, 1 itermax reached, 2 non-finite, 4 zero pivot
-    int *flag;                      // [1] number of scenarios still iterating
+    int *flag;                      // [2] scenarios still iterating; of those, refreshing factors
     double *dt;                     // [1] time step of the current solve
 };
 
@@ -63,7 +63,6 @@ struct DevSym {
     int n, nsup, nlevels;
     const int *sup_start, *row_ptr, *rows, *child_ptr, *children, *relmap_ptr, *relmap;
     const int64_t *front_off, *uvec_off;
-    const int *level_sups;
     int64_t front_total, uvec_total;
     const int *asmc_ptr, *asmc_pos;   // constant entries: front position, value
     const double *asmc_val;
@@ -89,6 +88,27 @@ struct DevClu {
     const int *perm_col;        // [class][32] state (local) of solution position j
     const int *pos3;            // [class][3] solution positions of delta, i_q, i_d
     int max_slots;
+};
+
+// Factor reuse of the mixed-precision solver (GP_SOLVER_SCHUR_MIXED).  The
+// cluster blocks' LU values and the reduced-system factors are kept in FP32
+// and reused across Newton iterations; every iteration evaluates the
+// residual in FP64 and applies the kept factors to it.  A scenario refreshes
+// its factors (FP64 Jacobian at the current iterate, stored in FP32) when
+// refac[m] is set.
+struct DevMixed {
+    int on;                // 0: exact Newton with fresh FP64 factors every iteration
+    int n_lu;              // LU slots kept per cluster (maximum over classes)
+    int max_age;           // Newton solves a factor set may serve before a refresh
+    int exact_after;       // iterations of one solve after which every iteration refreshes
+    double rho_max;        // residual contraction above which the factors are refreshed
+    uint8_t *refac;        // [M] this iteration refreshes the scenario's factors
+    uint8_t *refac_next;   // [M] set for the next iteration
+    int *age;              // [M] Newton solves since the last refresh
+    double *prev_norm;     // [M] residual norm of the previous iteration
+    float *lu;             // [M][n_tasks][n_lu][32] cluster LU values and pivot reciprocals
+    float *cc;             // [M][n_cl][6] coupling rows of the network equations
+    float *fronts;         // [M][front_total] reduced-system factors
 };
 
 // Dataflow schedule of the multifrontal factorisation and solves
@@ -127,22 +147,49 @@ template <class T>
 void launch_dag_bwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, const DagGrid &g,
                     const T *fronts, cudaStream_t st);
 
+// Split of the assembly tree for the triangular solves (gp_solve.cu).
+// Entries are the supernodes of all blocks, block by block, children before
+// parents; the last entry of a block is its root.
+//   ent0 = {supernode, first column, pivots ns, update rows r}
+//   ent1 = {factor-slice offset, vector offset, map offset, pivot offset}
+// (offsets within the block's shared-memory staging area; map offsets
+// relative to the block's first map entry).
+struct DevBlk {
+    int nblk;
+    int max_n, max_l, max_v, max_p, max_map, max_ext;   // per-block maxima
+    const int *blk_ptr;          // [nblk+1]
+    const int4 *ent0, *ent1;
+    const int *map_ptr;          // [nblk+1]
+    const int *map_fwd;          // per update row: parent vector position (forward push)
+    const int *map_bwd;          // per update row: vector position of that row's solution
+    const int *ext_ptr;          // [nblk+1]
+    const int *ext_pos, *ext_row;   // solution entries above the block: vector position, xperm row
+    int n_top_levels, top_max_front;
+    const int *top_ptr;          // [n_top_levels+1]
+    const int *top_sups;
+};
+
+int solve_configure(const DevBlk &B);
+int solve_block_bytes(const DevBlk &B, int fp32);
+template <class T>
+void launch_solve_fwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B, const T *fronts,
+                      cudaStream_t st);
+template <class T>
+void launch_solve_bwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B, const T *fronts,
+                      cudaStream_t st);
+
 // launches (gp_kernels.cu)
-void launch_cluster(const DevProblem &P, const DevWork &W, const DevClu &C, int want_f, cudaStream_t st);
+void launch_cluster(const DevProblem &P, const DevWork &W, const DevClu &C, const DevMixed &Mx, int want_f,
+                    cudaStream_t st);
 void launch_network(const DevProblem &P, const DevWork &W, int want_f, cudaStream_t st);
-void launch_check(const DevProblem &P, const DevWork &W, double tol, int itermax, cudaStream_t st);
-void launch_reset_norm(const DevProblem &P, const DevWork &W, cudaStream_t st);
-void launch_factor_level(const DevProblem &P, const DevWork &W, const DevSym &S, int lvl_begin, int lvl_count,
-                         int max_front, cudaStream_t st);
-void launch_fwd_level(const DevProblem &P, const DevWork &W, const DevSym &S, int lvl_begin, int lvl_count,
-                      int max_front, cudaStream_t st);
-void launch_bwd_level(const DevProblem &P, const DevWork &W, const DevSym &S, int lvl_begin, int lvl_count,
-                      int max_front, cudaStream_t st);
+void launch_check(const DevProblem &P, const DevWork &W, const DevMixed &Mx, double tol, int itermax,
+                  cudaStream_t st);
+void launch_reset_norm(const DevProblem &P, const DevWork &W, const DevMixed &Mx, cudaStream_t st);
+void launch_mixed_start(const DevProblem &P, const DevWork &W, const DevMixed &Mx, int force, cudaStream_t st);
 void launch_update(const DevProblem &P, const DevWork &W, const DevSym &S, const int *perm, cudaStream_t st);
 void launch_events(const DevProblem &P, const DevWork &W, const int *fl_on_step, const int *fl_off_step,
                    const int *fl_scen, uint8_t *fl_on, int n_fl, int step, cudaStream_t st);
 void launch_snapshot(const double *z, double *traj, int M, int n_sys, int n_steps, int k, cudaStream_t st);
-int factor_smem_limit();
 int cluster_smem_optin(int bytes);
 
 }  // namespace gp

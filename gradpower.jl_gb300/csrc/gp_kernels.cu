@@ -17,10 +17,6 @@
 //                  (src/kernels/static_gen.jl) and fault shunts
 //                  (src/dynamics.jl:314-327); writes the bus's 2x2 diagonal
 //                  block of the reduced matrix S and its right-hand side.
-//  factor/fwd/bwd  level-scheduled multifrontal LU of S (one CTA per
-//                  (supernode, scenario)) and the two triangular solves; the
-//                  replacement of cuDSS factorization/solve
-//                  (ext/GradPowerCUDAExt/GradPowerCUDAExt.jl:2782-2799).
 //  update_kernel   z += dz: network and static-generator unknowns from the
 //                  solve, cluster states by back-substitution
 //                  dw_k = -(A_k^-1 f_k + A_k^-1 B_k dv) (src/schur.jl:383-409).
@@ -76,10 +72,39 @@ __device__ __forceinline__ DevRef devref(const DTab &T, int k) {
     return d;
 }
 
-__global__ void __launch_bounds__(32) cluster_kernel(DevProblem P, DevWork W, DevClu Cl, int want_f) {
+// Sink of a residual-only evaluation: Jacobian entries are dropped (the
+// compiler removes their arithmetic), residuals go to their slots.
+struct ResidualSink {
+    double *v;
+    const short *slot_of;
+    int ws, lane;
+    __device__ __forceinline__ void put(int, int, double) {}
+    __device__ __forceinline__ void putv(int, int, double) {}
+    __device__ __forceinline__ void putf(int r, double x) { v[(int)slot_of[(r - ws) * 32 + 31] * 32 + lane] = x; }
+};
+
+template <class Sink>
+__device__ __forceinline__ void eval_cluster(const DevProblem &P, int c, const double *z, const double *u0,
+                                             const double *p, Sink &sink, double Cc[6], double Ic[2]) {
+    genrou_eval(devref(P.dev[0], P.cl_gen[c]), P.net, z, u0, p, sink, Cc, Ic);
+    const int gt = P.cl_gov_type[c];
+    if (gt == 1) ieesgo_eval(devref(P.dev[1], P.cl_gov[c]), z, p, sink);
+    else if (gt == 2) tgov1_eval(devref(P.dev[2], P.cl_gov[c]), z, p, sink);
+    const int et = P.cl_exc_type[c];
+    if (et == 3) sexs_eval(devref(P.dev[3], P.cl_exc[c]), P.net, z, p, sink);
+    else if (et == 4) esdc1a_eval(devref(P.dev[4], P.cl_exc[c]), P.net, z, p, sink);
+    if (P.cl_pss[c] >= 0) ieeest_eval(devref(P.dev[5], P.cl_pss[c]), z, p, sink);
+}
+
+// Modes per scenario: 0 exact Newton (Jacobian block, FP64 LU, three solves);
+// 1 the same, and the LU values and coupling rows are kept in FP32 for the
+// following iterations; 2 residual only, solved with the kept FP32 LU (the
+// kept A^-1 B columns and C A^-1 B terms stay as they are).
+__global__ void __launch_bounds__(32) cluster_kernel(DevProblem P, DevWork W, DevClu Cl, DevMixed Mx, int want_f) {
     extern __shared__ double vals[];
     const int task = blockIdx.x, m = blockIdx.y, lane = threadIdx.x;
     if (!W.active[m]) return;
+    const int mode = Mx.on ? (Mx.refac[m] ? 1 : 2) : 0;
     const int cls = Cl.task_class[task];
     const int cnt = Cl.task_count[task];
     const bool act = lane < cnt;
@@ -91,28 +116,25 @@ __global__ void __launch_bounds__(32) cluster_kernel(DevProblem P, DevWork W, De
     const double *zold = W.zold + (size_t)m * P.n_sys;
     const double *u0 = W.u0 + (size_t)m * P.n_ctrl;
     const double *p = W.p + (size_t)m * P.n_par;
-    LaneSink sink{vals, Cl.slot_of + (size_t)cls * 1024, ws, lane};
     double Cc[6] = {0, 0, 0, 0, 0, 0}, Ic[2] = {0, 0};
+    const CluOp *ops = Cl.ops;
+    const int q0 = Cl.prog_ptr[cls], qm = Cl.prog_mid[cls], q1 = Cl.prog_ptr[cls + 1];
     if (act) {
-        genrou_eval(devref(P.dev[0], P.cl_gen[c]), P.net, z, u0, p, sink, Cc, Ic);
-        const int gt = P.cl_gov_type[c];
-        if (gt == 1) ieesgo_eval(devref(P.dev[1], P.cl_gov[c]), z, p, sink);
-        else if (gt == 2) tgov1_eval(devref(P.dev[2], P.cl_gov[c]), z, p, sink);
-        const int et = P.cl_exc_type[c];
-        if (et == 3) sexs_eval(devref(P.dev[3], P.cl_exc[c]), P.net, z, p, sink);
-        else if (et == 4) esdc1a_eval(devref(P.dev[4], P.cl_exc[c]), P.net, z, p, sink);
-        if (P.cl_pss[c] >= 0) ieeest_eval(devref(P.dev[5], P.cl_pss[c]), z, p, sink);
-    } else {
+        if (mode == 2) {
+            ResidualSink sink{vals, Cl.slot_of + (size_t)cls * 1024, ws, lane};
+            eval_cluster(P, c, z, u0, p, sink, Cc, Ic);
+        } else {
+            LaneSink sink{vals, Cl.slot_of + (size_t)cls * 1024, ws, lane};
+            eval_cluster(P, c, z, u0, p, sink, Cc, Ic);
+        }
+    } else if (mode != 2) {
         // idle lanes factor an identity so that no lane divides by zero
-        const CluOp *o = Cl.ops + Cl.prog_ptr[cls];
-        for (int q = Cl.prog_mid[cls] - Cl.prog_ptr[cls]; q < Cl.prog_ptr[cls + 1] - Cl.prog_ptr[cls]; q++)
-            if (o[q].code == OP_RCP) vals[o[q].a * 32 + lane] = 1.0;
+        for (int q = qm; q < q1; q++)
+            if (ops[q].code == OP_RCP) vals[ops[q].a * 32 + lane] = 1.0;
     }
     const double dt = *W.dt;
     const int rb = Cl.rhs_base[cls];
     double *R0 = vals + (size_t)rb * 32, *R1 = R0 + (size_t)Wn * 32, *R2 = R1 + (size_t)Wn * 32;
-    const CluOp *ops = Cl.ops;
-    const int q0 = Cl.prog_ptr[cls], qm = Cl.prog_mid[cls], q1 = Cl.prog_ptr[cls + 1];
     // backward-Euler scaling
     for (int q = q0; q < qm; q++) {
         const CluOp o = ops[q];
@@ -142,55 +164,79 @@ __global__ void __launch_bounds__(32) cluster_kernel(DevProblem P, DevWork W, De
         nb = o > nb ? o : nb;
     }
     if (lane == 0) atomicMax(W.norm + m, nb);
-    // factorisation and solves
-    for (int q = qm; q < q1; q++) {
-        const CluOp o = ops[q];
-        switch (o.code) {
-        case OP_RCP:
-            vals[o.d * 32 + lane] = 1.0 / vals[o.a * 32 + lane];
-            break;
-        case OP_MUL:
-            vals[o.d * 32 + lane] *= vals[o.a * 32 + lane];
-            break;
-        case OP_FMS:
-            vals[o.d * 32 + lane] -= vals[o.a * 32 + lane] * vals[o.b * 32 + lane];
-            break;
-        case OP_FMS3: {
-            const double l = vals[o.a * 32 + lane];
-            R0[o.d * 32 + lane] -= l * R0[o.b * 32 + lane];
-            R1[o.d * 32 + lane] -= l * R1[o.b * 32 + lane];
-            R2[o.d * 32 + lane] -= l * R2[o.b * 32 + lane];
-            break;
+    float *keep = Mx.on ? Mx.lu + (((size_t)m * Cl.n_tasks + task) * Mx.n_lu) * 32 + lane : nullptr;
+    if (mode == 2) {
+        // kept LU values; the solve of the residual column alone
+        for (int s = 0; s < rb; s++) vals[s * 32 + lane] = (double)keep[s * 32];
+        for (int q = qm; q < q1; q++) {
+            const CluOp o = ops[q];
+            if (o.code == OP_FMS3) R2[o.d * 32 + lane] -= vals[o.a * 32 + lane] * R2[o.b * 32 + lane];
+            else if (o.code == OP_MUL3) R2[o.d * 32 + lane] *= vals[o.a * 32 + lane];
         }
-        case OP_MUL3: {
-            const double l = vals[o.a * 32 + lane];
-            R0[o.d * 32 + lane] *= l;
-            R1[o.d * 32 + lane] *= l;
-            R2[o.d * 32 + lane] *= l;
-            break;
+    } else {
+        // factorisation and solves
+        for (int q = qm; q < q1; q++) {
+            const CluOp o = ops[q];
+            switch (o.code) {
+            case OP_RCP:
+                vals[o.d * 32 + lane] = 1.0 / vals[o.a * 32 + lane];
+                break;
+            case OP_MUL:
+                vals[o.d * 32 + lane] *= vals[o.a * 32 + lane];
+                break;
+            case OP_FMS:
+                vals[o.d * 32 + lane] -= vals[o.a * 32 + lane] * vals[o.b * 32 + lane];
+                break;
+            case OP_FMS3: {
+                const double l = vals[o.a * 32 + lane];
+                R0[o.d * 32 + lane] -= l * R0[o.b * 32 + lane];
+                R1[o.d * 32 + lane] -= l * R1[o.b * 32 + lane];
+                R2[o.d * 32 + lane] -= l * R2[o.b * 32 + lane];
+                break;
+            }
+            case OP_MUL3: {
+                const double l = vals[o.a * 32 + lane];
+                R0[o.d * 32 + lane] *= l;
+                R1[o.d * 32 + lane] *= l;
+                R2[o.d * 32 + lane] *= l;
+                break;
+            }
+            default:
+                break;
+            }
         }
-        default:
-            break;
-        }
+        if (mode == 1)
+            for (int s = 0; s < rb; s++) keep[s * 32] = (float)vals[s * 32 + lane];
     }
     if (!act) return;
     const int n_da = P.n_diff + P.n_alg;
     double *yx = W.yx + (size_t)m * 3 * n_da + ws;
+    const int *p3 = Cl.pos3 + cls * 3;
+    double *o = W.clout + ((size_t)m * P.n_cl + c) * 8;
+    double Y[3];
+#pragma unroll
+    for (int t = 0; t < 3; t++) Y[t] = R2[p3[t] * 32 + lane];
+    if (mode == 2) {
+        for (int j = 0; j < Wn; j++) yx[pc[j]] = R2[j * 32 + lane];
+        const float *cc = Mx.cc + ((size_t)m * P.n_cl + c) * 6;
+        o[4] = (double)cc[0] * Y[0] + (double)cc[1] * Y[1] + (double)cc[2] * Y[2];
+        o[5] = (double)cc[3] * Y[0] + (double)cc[4] * Y[1] + (double)cc[5] * Y[2];
+        o[6] = Ic[0];
+        o[7] = Ic[1];
+        return;
+    }
     for (int j = 0; j < Wn; j++) {
         const int st = pc[j];
         yx[st] = R2[j * 32 + lane];
         yx[n_da + st] = R0[j * 32 + lane];
         yx[2 * n_da + st] = R1[j * 32 + lane];
     }
-    const int *p3 = Cl.pos3 + cls * 3;
-    double X1[3], X2[3], Y[3];
+    double X1[3], X2[3];
 #pragma unroll
     for (int t = 0; t < 3; t++) {
         X1[t] = R0[p3[t] * 32 + lane];
         X2[t] = R1[p3[t] * 32 + lane];
-        Y[t] = R2[p3[t] * 32 + lane];
     }
-    double *o = W.clout + ((size_t)m * P.n_cl + c) * 8;
     o[0] = Cc[0] * X1[0] + Cc[1] * X1[1] + Cc[2] * X1[2];
     o[1] = Cc[0] * X2[0] + Cc[1] * X2[1] + Cc[2] * X2[2];
     o[2] = Cc[3] * X1[0] + Cc[4] * X1[1] + Cc[5] * X1[2];
@@ -199,12 +245,17 @@ __global__ void __launch_bounds__(32) cluster_kernel(DevProblem P, DevWork W, De
     o[5] = Cc[3] * Y[0] + Cc[4] * Y[1] + Cc[5] * Y[2];
     o[6] = Ic[0];
     o[7] = Ic[1];
+    if (mode == 1) {
+        float *cc = Mx.cc + ((size_t)m * P.n_cl + c) * 6;
+        for (int t = 0; t < 6; t++) cc[t] = (float)Cc[t];
+    }
 }
 
-void launch_cluster(const DevProblem &P, const DevWork &W, const DevClu &C, int want_f, cudaStream_t st) {
+void launch_cluster(const DevProblem &P, const DevWork &W, const DevClu &C, const DevMixed &Mx, int want_f,
+                    cudaStream_t st) {
     if (C.n_tasks == 0) return;
     dim3 grid(C.n_tasks, P.M);
-    cluster_kernel<<<grid, 32, (size_t)C.max_slots * 32 * sizeof(double), st>>>(P, W, C, want_f);
+    cluster_kernel<<<grid, 32, (size_t)C.max_slots * 32 * sizeof(double), st>>>(P, W, C, Mx, want_f);
 }
 
 int cluster_smem_optin(int bytes) {
@@ -375,17 +426,49 @@ void launch_network(const DevProblem &P, const DevWork &W, int want_f, cudaStrea
 // convergence bookkeeping
 // ---------------------------------------------------------------------------
 
-__global__ void reset_norm_kernel(DevWork W, int M) {
+// Start of a Newton iteration: clears the residual norms and the counters;
+// the mixed solver takes the refresh decisions made at the previous check.
+__global__ void reset_norm_kernel(DevWork W, DevMixed Mx, int M) {
     int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m < M) W.norm[m] = 0ull;
-    if (m == 0) *W.flag = 0;
+    if (m < M) {
+        W.norm[m] = 0ull;
+        if (Mx.on) {
+            const uint8_t r = Mx.refac_next[m];
+            Mx.refac[m] = r;
+            Mx.refac_next[m] = 0;
+            if (r) Mx.age[m] = 0;
+        }
+    }
+    if (m == 0) {
+        W.flag[0] = 0;
+        W.flag[1] = 0;
+    }
 }
 
-void launch_reset_norm(const DevProblem &P, const DevWork &W, cudaStream_t st) {
-    reset_norm_kernel<<<(P.M + 255) / 256, 256, 0, st>>>(W, P.M);
+void launch_reset_norm(const DevProblem &P, const DevWork &W, const DevMixed &Mx, cudaStream_t st) {
+    reset_norm_kernel<<<(P.M + 255) / 256, 256, 0, st>>>(W, Mx, P.M);
 }
 
-__global__ void check_kernel(DevWork W, int M, double tol, int itermax) {
+// Start of a Newton solve of the mixed solver: scenarios whose factors have
+// served max_age solves, or every scenario when `force` (first solve, event
+// re-solves and the solve after them), refresh them at the first iteration.
+__global__ void mixed_start_kernel(DevWork W, DevMixed Mx, int M, int force) {
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M || !W.active[m]) return;
+    if (force || Mx.age[m] >= Mx.max_age) Mx.refac_next[m] = 1;
+    Mx.age[m] += 1;
+}
+
+void launch_mixed_start(const DevProblem &P, const DevWork &W, const DevMixed &Mx, int force, cudaStream_t st) {
+    mixed_start_kernel<<<(P.M + 255) / 256, 256, 0, st>>>(W, Mx, P.M, force);
+}
+
+// Convergence test (infinity norm of the FP64 residual), the itermax and
+// non-finite checks, and for the mixed solver the refresh decision: a
+// residual that fell by less than rho_max in the last iteration with kept
+// factors refreshes them at the next one, and after exact_after iterations
+// of one solve every iteration refreshes them.
+__global__ void check_kernel(DevWork W, DevMixed Mx, int M, double tol, int itermax) {
     int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M || !W.active[m]) return;
     const unsigned long long bits = W.norm[m];
@@ -399,221 +482,21 @@ __global__ void check_kernel(DevWork W, int M, double tol, int itermax) {
         W.active[m] = 0;
         W.status[m] |= 1;
     } else {
+        if (Mx.on) {
+            if (W.iters[m] >= Mx.exact_after ||
+                (W.iters[m] > 0 && !Mx.refac[m] && nrm > Mx.rho_max * Mx.prev_norm[m]))
+                Mx.refac_next[m] = 1;
+            Mx.prev_norm[m] = nrm;
+            if (Mx.refac[m]) atomicAdd(W.flag + 1, 1);
+        }
         W.iters[m] += 1;
         atomicAdd(W.flag, 1);
     }
 }
 
-void launch_check(const DevProblem &P, const DevWork &W, double tol, int itermax, cudaStream_t st) {
-    check_kernel<<<(P.M + 255) / 256, 256, 0, st>>>(W, P.M, tol, itermax);
-}
-
-// ---------------------------------------------------------------------------
-// multifrontal factorisation and solves
-// ---------------------------------------------------------------------------
-
-__global__ void factor_kernel(DevProblem P, DevWork W, DevSym S, int lvl_begin) {
-    extern __shared__ double smem[];
-    const int s = S.level_sups[lvl_begin + blockIdx.x];
-    const int m = blockIdx.y;
-    if (!W.active[m]) return;
-    const int start = S.sup_start[s];
-    const int ns = S.sup_start[s + 1] - start;
-    const int r = S.row_ptr[s + 1] - S.row_ptr[s];
-    const int mm = ns + r;
-    double *F = smem;
-    __shared__ int s_piv;
-    const int tid = threadIdx.x, nt = blockDim.x;
-    for (int i = tid; i < mm * mm; i += nt) F[i] = 0.0;
-    __syncthreads();
-    for (int e = S.asmc_ptr[s] + tid; e < S.asmc_ptr[s + 1]; e += nt) F[S.asmc_pos[e]] += S.asmc_val[e];
-    const double *sv = W.svar + (size_t)m * P.n_var;
-    for (int e = S.asmv_ptr[s] + tid; e < S.asmv_ptr[s + 1]; e += nt) F[S.asmv_pos[e]] += sv[S.asmv_idx[e]];
-    __syncthreads();
-    const double *fronts = S.fronts + (size_t)m * S.front_total;
-    for (int q = S.child_ptr[s]; q < S.child_ptr[s + 1]; q++) {
-        const int c = S.children[q];
-        const int nc = S.sup_start[c + 1] - S.sup_start[c];
-        const int rc = S.row_ptr[c + 1] - S.row_ptr[c];
-        const int mc = nc + rc;
-        const int *rel = S.relmap + S.relmap_ptr[c];
-        const double *Fc = fronts + S.front_off[c];
-        for (int t = tid; t < rc * rc; t += nt) {
-            const int a = t % rc, b = t / rc;
-            F[rel[a] + rel[b] * mm] += Fc[(nc + a) + (size_t)(nc + b) * mc];
-        }
-        __syncthreads();
-    }
-    int *ipiv = S.ipiv + (size_t)m * S.n + start;
-    for (int k = 0; k < ns; k++) {
-        if (tid < 32) {
-            double best = -1.0;
-            int bi = k;
-            for (int i = k + tid; i < ns; i += 32) {
-                const double v = fabs(F[i + k * mm]);
-                if (v > best) { best = v; bi = i; }
-            }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                const double ov = __shfl_xor_sync(FULL_MASK, best, off);
-                const int oi = __shfl_xor_sync(FULL_MASK, bi, off);
-                if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
-            }
-            if (tid == 0) {
-                s_piv = bi;
-                ipiv[k] = bi;
-                if (best == 0.0) atomicOr(W.status + m, 4);
-            }
-        }
-        __syncthreads();
-        const int pv = s_piv;
-        if (pv != k) {
-            for (int j = tid; j < mm; j += nt) {
-                const double t = F[k + j * mm];
-                F[k + j * mm] = F[pv + j * mm];
-                F[pv + j * mm] = t;
-            }
-            __syncthreads();
-        }
-        const double pk = F[k + k * mm];
-        const double inv = 1.0 / pk;
-        for (int i = k + 1 + tid; i < mm; i += nt) F[i + k * mm] *= inv;
-        __syncthreads();
-        const int len = mm - k - 1;
-        for (int t = tid; t < len * len; t += nt) {
-            const int i = k + 1 + t % len, j = k + 1 + t / len;
-            F[i + j * mm] -= F[i + k * mm] * F[k + j * mm];
-        }
-        __syncthreads();
-    }
-    double *out = S.fronts + (size_t)m * S.front_total + S.front_off[s];
-    for (int i = tid; i < mm * mm; i += nt) out[i] = F[i];
-}
-
-static int block_for(int max_front) {
-    if (max_front <= 16) return 64;
-    if (max_front <= 48) return 128;
-    return 256;
-}
-
-void launch_factor_level(const DevProblem &P, const DevWork &W, const DevSym &S, int lvl_begin, int lvl_count,
-                         int max_front, cudaStream_t st) {
-    dim3 grid(lvl_count, P.M);
-    size_t smem = (size_t)max_front * max_front * sizeof(double);
-    factor_kernel<<<grid, block_for(max_front), smem, st>>>(P, W, S, lvl_begin);
-}
-
-// Opt the factorisation kernel into the largest dynamic shared memory the
-// device allows next to its static shared memory; returns that size, or -1
-// if the runtime refused.
-int factor_smem_limit() {
-    int dev = 0, v = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
-    if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return -1;
-    cudaFuncAttributes fa;
-    if (cudaFuncGetAttributes(&fa, factor_kernel) != cudaSuccess) return -1;
-    const int dyn = v - (int)fa.sharedSizeBytes;
-    if (cudaFuncSetAttribute(factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess) {
-        cudaGetLastError();
-        return -1;
-    }
-    return dyn;
-}
-
-// forward solve: bottom-up, extend-add of the children's update vectors
-__global__ void fwd_kernel(DevProblem P, DevWork W, DevSym S, int lvl_begin) {
-    extern __shared__ double smem[];
-    const int s = S.level_sups[lvl_begin + blockIdx.x];
-    const int m = blockIdx.y;
-    if (!W.active[m]) return;
-    const int start = S.sup_start[s];
-    const int ns = S.sup_start[s + 1] - start;
-    const int r = S.row_ptr[s + 1] - S.row_ptr[s];
-    const int mm = ns + r;
-    double *t = smem, *u = smem + ns;
-    const int tid = threadIdx.x, nt = blockDim.x;
-    double *x = W.xperm + (size_t)m * P.n_red;
-    double *uv = S.uvec + (size_t)m * S.uvec_total;
-    for (int i = tid; i < ns; i += nt) t[i] = x[start + i];
-    for (int i = tid; i < r; i += nt) u[i] = 0.0;
-    __syncthreads();
-    for (int q = S.child_ptr[s]; q < S.child_ptr[s + 1]; q++) {
-        const int c = S.children[q];
-        const int rc = S.row_ptr[c + 1] - S.row_ptr[c];
-        const int *rel = S.relmap + S.relmap_ptr[c];
-        const double *uc = uv + S.uvec_off[c];
-        for (int a = tid; a < rc; a += nt) {
-            const int pos = rel[a];
-            if (pos < ns) t[pos] += uc[a];
-            else u[pos - ns] += uc[a];
-        }
-        __syncthreads();
-    }
-    const double *F = S.fronts + (size_t)m * S.front_total + S.front_off[s];
-    const int *ipiv = S.ipiv + (size_t)m * S.n + start;
-    if (tid == 0)
-        for (int k = 0; k < ns; k++) {
-            const int pv = ipiv[k];
-            if (pv != k) { const double tt = t[k]; t[k] = t[pv]; t[pv] = tt; }
-        }
-    __syncthreads();
-    for (int k = 0; k < ns; k++) {
-        const double tk = t[k];
-        for (int i = k + 1 + tid; i < ns; i += nt) t[i] -= F[i + k * mm] * tk;
-        __syncthreads();
-    }
-    for (int i = tid; i < r; i += nt) {
-        double acc = 0.0;
-        for (int k = 0; k < ns; k++) acc += F[(ns + i) + (size_t)k * mm] * t[k];
-        u[i] -= acc;
-    }
-    __syncthreads();
-    for (int i = tid; i < ns; i += nt) x[start + i] = t[i];
-    double *us = uv + S.uvec_off[s];
-    for (int i = tid; i < r; i += nt) us[i] = u[i];
-}
-
-void launch_fwd_level(const DevProblem &P, const DevWork &W, const DevSym &S, int lvl_begin, int lvl_count,
-                      int max_front, cudaStream_t st) {
-    dim3 grid(lvl_count, P.M);
-    fwd_kernel<<<grid, max_front <= 32 ? 32 : 128, (size_t)max_front * sizeof(double), st>>>(P, W, S, lvl_begin);
-}
-
-// backward solve: top-down, gathers of the ancestors' solution
-__global__ void bwd_kernel(DevProblem P, DevWork W, DevSym S, int lvl_begin) {
-    extern __shared__ double smem[];
-    const int s = S.level_sups[lvl_begin + blockIdx.x];
-    const int m = blockIdx.y;
-    if (!W.active[m]) return;
-    const int start = S.sup_start[s];
-    const int ns = S.sup_start[s + 1] - start;
-    const int r = S.row_ptr[s + 1] - S.row_ptr[s];
-    const int mm = ns + r;
-    double *t = smem;
-    const int tid = threadIdx.x, nt = blockDim.x;
-    double *x = W.xperm + (size_t)m * P.n_red;
-    const double *F = S.fronts + (size_t)m * S.front_total + S.front_off[s];
-    const int *rows = S.rows + S.row_ptr[s];
-    for (int i = tid; i < ns; i += nt) {
-        double acc = 0.0;
-        for (int a = 0; a < r; a++) acc += F[i + (size_t)(ns + a) * mm] * x[rows[a]];
-        t[i] = x[start + i] - acc;
-    }
-    __syncthreads();
-    for (int k = ns - 1; k >= 0; k--) {
-        if (tid == 0) t[k] /= F[k + k * mm];
-        __syncthreads();
-        const double tk = t[k];
-        for (int i = tid; i < k; i += nt) t[i] -= F[i + k * mm] * tk;
-        __syncthreads();
-    }
-    for (int i = tid; i < ns; i += nt) x[start + i] = t[i];
-}
-
-void launch_bwd_level(const DevProblem &P, const DevWork &W, const DevSym &S, int lvl_begin, int lvl_count,
-                      int max_front, cudaStream_t st) {
-    dim3 grid(lvl_count, P.M);
-    bwd_kernel<<<grid, max_front <= 32 ? 32 : 128, (size_t)max_front * sizeof(double), st>>>(P, W, S, lvl_begin);
+void launch_check(const DevProblem &P, const DevWork &W, const DevMixed &Mx, double tol, int itermax,
+                  cudaStream_t st) {
+    check_kernel<<<(P.M + 255) / 256, 256, 0, st>>>(W, Mx, P.M, tol, itermax);
 }
 
 // ---------------------------------------------------------------------------

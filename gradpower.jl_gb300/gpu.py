@@ -53,10 +53,11 @@ def library():
         L.gp_reduced_selftest.argtypes = [vp] * 7
         L.gp_cluster_selftest.argtypes = [vp] * 5 + [C.c_double] + [vp] * 4
         L.gp_residual_static.argtypes = [vp, vp, C.c_double, vp]
+        L.gp_set_mixed_policy.argtypes = [vp, C.c_int32, C.c_double, C.c_int32]
         for f in ("gp_layout_create", "gp_layout_destroy", "gp_layout_stats", "gp_set_state",
                   "gp_get_state", "gp_integrate", "gp_residual", "gp_last_timing",
                   "gp_restore_initial_state", "gp_reduced_selftest", "gp_cluster_selftest",
-                  "gp_residual_static"):
+                  "gp_residual_static", "gp_set_mixed_policy"):
             getattr(L, f).restype = C.c_int32
         _lib = L
     return _lib
@@ -123,6 +124,11 @@ class GpuBatchedLayout:
         keys = ("n_red", "nnz_S", "nnz_LU", "supernodes", "levels", "factor_flops", "sum_w2", "max_front")
         return dict(zip(keys, (int(v) for v in out)))
 
+    def set_mixed_policy(self, max_age: int = 1, rho_max: float = 0.1, exact_after: int = 8):
+        """Refresh policy of the mixed-precision solver (see
+        gp_set_mixed_policy in include/gradpower_gb300.h)."""
+        _check(library().gp_set_mixed_policy(self._h, int(max_age), float(rho_max), int(exact_after)))
+
     def timing(self) -> dict:
         """Device time of the last integrate call by phase (CUDA events on
         the library's stream, recorded inside its graphs)."""
@@ -131,7 +137,8 @@ class GpuBatchedLayout:
         return dict(total_ms=float(out[0]), cluster_ms=float(out[1]), network_ms=float(out[2]),
                     factor_ms=float(out[3]), solve_ms=float(out[4]), update_ms=float(out[7]),
                     newton_iters=float(out[5]), launches=float(out[6]),
-                    factor_launches=float(out[8]), linear_solves=float(out[9]))
+                    factor_launches=float(out[8]), linear_solves=float(out[9]),
+                    refreshes=float(out[10]))
 
     def restore_initial_state(self):
         _check(library().gp_restore_initial_state(self._h))

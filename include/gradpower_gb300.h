@@ -53,6 +53,7 @@ extern "C" {
 #define GP_E_NOMEM      -3   /* allocation failed */
 #define GP_E_NUMERIC    -4   /* zero pivot / non-finite values */
 #define GP_E_TIMEOUT    -5   /* a device wait ran out its iteration limit */
+#define GP_E_INTERNAL   -6   /* an internal consistency check failed */
 
 /* device types, in the reference's DEVICE_REGISTRY order (src/layout.jl) */
 enum {
@@ -132,8 +133,19 @@ typedef struct gp_fault {
     int32_t off_step;
 } gp_fault;
 
-#define GP_SOLVER_SCHUR_FP64   0   /* exact Newton, FP64 factors every iteration */
-#define GP_SOLVER_SCHUR_MIXED  1   /* FP32 factors reused across iterations + FP64 refinement */
+/* GP_SOLVER_SCHUR_FP64: exact Newton, the reference's batched schedule: the
+ *   cluster blocks and the reduced network matrix are factored in FP64 at
+ *   every iteration.
+ * GP_SOLVER_SCHUR_MIXED: the cluster blocks' LU and the reduced-system
+ *   factors are kept in FP32 and reused across Newton iterations and steps;
+ *   every iteration evaluates the residual in FP64 and corrects with the
+ *   kept factors (defect correction / iterative refinement of the nonlinear
+ *   system), the convergence test is the same FP64 infinity norm.  A
+ *   scenario refreshes its factors (FP64 Jacobian at the current iterate,
+ *   stored in FP32) at the first solve and around events, and then by the
+ *   policy of gp_set_mixed_policy. */
+#define GP_SOLVER_SCHUR_FP64   0
+#define GP_SOLVER_SCHUR_MIXED  1
 
 typedef struct gp_options {
     double dt;
@@ -193,9 +205,18 @@ int32_t gp_residual(gp_layout *L, const double *zold, double dt, int32_t n_fault
  * out[0] total, out[1] cluster kernel, out[2] network kernel, out[3]
  * factorisation (all levels), out[4] triangular solves, out[5] Newton
  * iterations summed over steps (max over scenarios), out[6] kernel launches,
- * out[7] update kernel, out[8] factorisation-level launches, out[9] linear
- * solves (batched over scenarios); out[10..15] zero. */
+ * out[7] update kernel, out[8] factorisation launches, out[9] linear
+ * solves (batched over scenarios), out[10] mixed solver: scenario factor
+ * refreshes; out[11..15] zero. */
 int32_t gp_last_timing(const gp_layout *L, double out[16]);
+
+/* Refresh policy of GP_SOLVER_SCHUR_MIXED (no counterpart in the reference,
+ * whose solvers refactor every iteration): a scenario refreshes its kept
+ * factors at the start of a solve once they have served max_age solves,
+ * after an iteration that reduced the residual by less than the factor
+ * rho_max, and at every iteration once a solve has taken exact_after
+ * iterations.  Defaults: max_age 1, rho_max 0.1, exact_after 8. */
+int32_t gp_set_mixed_policy(gp_layout *L, int32_t max_age, double rho_max, int32_t exact_after);
 
 /* gp_residual with no fault applied, computed without allocating anything:
  * its scratch (zold, residual, cluster and network intermediates) lives in
@@ -213,12 +234,18 @@ int32_t gp_residual_static(gp_layout *L, const double *zold, double dt, double *
  * the diagonal blocks and static-generator couplings of S from the given
  * CSR matrix (reduced indexing: 2b, 2b+1 for bus b, then static-generator
  * states), factors and solves S x = rhs on the host with the operation order
- * of the device kernels.  out[0] max |S - (-Ybus)| over off-diagonal blocks,
- * out[1] zero pivots, out[2] nnz(L+U), out[3] elimination-tree levels.
+ * of the device kernels: the level-order solves, and the blocked solves of
+ * the triangular-solve kernels with their shared-memory staging indices
+ * checked against the block maxima (GP_E_INTERNAL when one falls outside).
+ * x receives the blocked solve's solution.  out[0] max |S - (-Ybus)| over
+ * off-diagonal blocks, out[1] zero pivots, out[2] nnz(L+U), out[3]
+ * elimination-tree levels, out[4] max |x_blocked - x_levels| / max |x|,
+ * out[5] solve blocks, out[6] levels of the top region, out[7] most
+ * supernodes in one block.
  * No counterpart in the reference: a test hook for the analysis that
  * replaces cuDSS's. */
 int32_t gp_reduced_selftest(const gp_problem *prob, const int32_t *s_rowptr, const int32_t *s_colidx,
-                            const double *s_val, const double *rhs, double *x, double out[4]);
+                            const double *s_val, const double *rhs, double *x, double out[8]);
 
 /* Host-only check of the cluster factorisation, needs no GPU: builds the
  * class plans of gp_layout_create from (z, u0, p) of one scenario and runs

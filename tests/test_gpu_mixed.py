@@ -1,0 +1,106 @@
+"""GPU tests of the mixed-precision solver (GP_SOLVER_SCHUR_MIXED): FP32
+factors of the cluster blocks and of the reduced network matrix, kept and
+reused across Newton iterations, FP64 residuals and convergence test.
+
+Bar: every scenario converges (status 0), and the rotor angle, rotor speed
+and bus voltage magnitude stay within 1e-6 of the FP64 oracle (or of the
+FP64 GPU path, which matches the oracle to 1e-9, where the oracle is too
+slow).
+"""
+import numpy as np
+import pytest
+
+from helpers import DT, LY, Case, M, psse_case, run_oracle, synthetic_case
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-6
+
+
+@pytest.fixture(scope="module")
+def G():
+    from gradpower_gb300 import build, gpu
+    build.build()
+    return gpu
+
+
+def _watched(PA):
+    """Indices of rotor angle, rotor speed (GENROU diff states 5 and 4) and
+    the bus voltage components."""
+    g = PA.tables[0]
+    return g.diff_ptr + 5, g.diff_ptr + 4, PA.n_diff + PA.n_alg + 2 * np.arange(PA.n_bus)
+
+
+def _errors(PA, traj, ref):
+    d, w, vr = _watched(PA)
+    vm = np.hypot(traj[..., vr], traj[..., vr + 1])
+    vm_ref = np.hypot(ref[..., vr], ref[..., vr + 1])
+    return (np.max(np.abs(traj[..., d] - ref[..., d])), np.max(np.abs(traj[..., w] - ref[..., w])),
+            np.max(np.abs(vm - vm_ref)))
+
+
+def _run(G, c, nsteps, solver):
+    gbl = G.GpuBatchedLayout(c.dp, c.ps, c.M)
+    try:
+        r = gbl.integrate(nsteps * DT, DT, events=c.events, scenario_faults=c.faults, solver=solver)
+        r["timing"] = gbl.timing()
+    finally:
+        gbl.close()
+    return r
+
+
+@pytest.mark.parametrize("raw,dyr", [("2bus.raw", "2bus_ESDC1A.dyr"), ("2bus.raw", "2bus_IEESGO.dyr"),
+                                     ("ieee9_v33.raw", "ieee9bus_gov.dyr"), ("IEEE39.raw", "IEEE39_gov.dyr")])
+def test_mixed_psse_cases_against_oracle(G, orc, golden_cases, raw, dyr):
+    ps, dp = psse_case(golden_cases, raw, dyr)
+    c = Case(ps, dp, [[M.ContingencyEvent(1, 0.05, 0.1, 0.2)]], 1)
+    g = _run(G, c, 40, LY.SOLVER_SCHUR_MIXED)
+    o = run_oracle(orc, c, 40)
+    assert np.all(g["status"] == 0) and np.all(o["status"] == 0)
+    assert max(_errors(c.PA, g["traj"], o["traj"])) <= TOL
+
+
+def test_mixed_ring39_against_oracle(G, orc):
+    c, w = synthetic_case("ring39", 16)
+    g = _run(G, c, 120, LY.SOLVER_SCHUR_MIXED)
+    o = run_oracle(orc, c, 120, itermax=30, nthreads=8)
+    ok = o["status"] == 0
+    assert ok.sum() >= 12
+    assert np.all(g["status"][ok] == 0)
+    assert max(_errors(c.PA, g["traj"][ok], o["traj"][ok])) <= TOL
+    assert g["timing"]["refreshes"] > 0
+
+
+def test_mixed_planar2k_against_oracle(G, orc):
+    c, w = synthetic_case("planar2k", 8)
+    g = _run(G, c, 60, LY.SOLVER_SCHUR_MIXED)
+    o = run_oracle(orc, c, 60, itermax=30, nthreads=8)
+    assert np.all(g["status"] == 0) and np.all(o["status"] == 0)
+    assert max(_errors(c.PA, g["traj"], o["traj"])) <= TOL
+    t = g["timing"]
+    # factors are kept: fewer refreshes than scenario-iterations
+    assert t["refreshes"] < t["newton_iters"] * c.M
+
+
+def test_mixed_planar70k_against_fp64_path(G):
+    c, w = synthetic_case("planar70k", 2)
+    g = _run(G, c, 30, LY.SOLVER_SCHUR_MIXED)
+    e = _run(G, c, 30, LY.SOLVER_SCHUR_FP64)
+    assert np.all(g["status"] == 0) and np.all(e["status"] == 0)
+    assert max(_errors(c.PA, g["traj"], e["traj"])) <= TOL
+
+
+def test_mixed_then_fp64_on_one_layout(G, orc):
+    """Switching solvers on one layout recaptures its graphs; the FP64 run
+    after a mixed run still matches the oracle to 1e-9."""
+    c, w = synthetic_case("planar2k", 4)
+    gbl = G.GpuBatchedLayout(c.dp, c.ps, c.M)
+    try:
+        gbl.integrate(20 * DT, DT, scenario_faults=c.faults, solver=LY.SOLVER_SCHUR_MIXED, want_traj=False)
+        gbl.restore_initial_state()
+        r = gbl.integrate(20 * DT, DT, scenario_faults=c.faults, solver=LY.SOLVER_SCHUR_FP64)
+    finally:
+        gbl.close()
+    o = run_oracle(orc, c, 20, itermax=30)
+    assert np.array_equal(r["iters"], o["iters"])
+    assert np.max(np.abs(r["traj"] - o["traj"]) / np.maximum(1.0, np.abs(o["traj"]))) <= 1e-9
