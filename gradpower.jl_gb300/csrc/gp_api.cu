@@ -125,13 +125,18 @@ struct gp_layout {
     gp::DevDag D{};
     gp::DagGrid G64, G32;
     gp::DevBlk B{};
+    gp::SolveGrid SG;
+    int n_top_levels = 0;
     // mixed-precision solver: kept FP32 factors (allocated on first use)
     gp::DevMixed Mx{};
     bool mixed_ready = false;
     int solver = -1;                          // solver the graphs were captured for
-    cudaGraphExec_t g_solve_keep = nullptr;   // mixed: solve with the kept factors
-    int solve_graph_launches = 0, keep_graph_launches = 0;
-    double refreshes = 0.0;                   // mixed: scenario factor refreshes in the last call
+    // mixed: solve graphs by the modes present in an iteration (bit 0: some
+    // scenario refreshes its FP32 factors, bit 1: some scenario uses FP64)
+    cudaGraphExec_t g_mix[4] = {};
+    int solve_graph_launches = 0, mix_launches[4] = {}, mix_factor_launches[4] = {};
+    double refreshes = 0.0;                   // mixed: scenario FP32 factor refreshes in the last call
+    double exact_iters = 0.0;                 // mixed: scenario iterations with FP64 factors
     int mx_max_age = 1, mx_exact_after = 8;   // mixed solver policy (gp_set_mixed_policy)
     double mx_rho_max = 0.1;
 };
@@ -370,21 +375,24 @@ void make_plan(const gp_problem *pr, Plan &pl) {
 }
 
 // Split of the assembly tree for the triangular solves (gp_solve.cu), on
-// the host: blocks are the largest subtrees within the per-warp staging
-// budget; the supernodes above them form the top region, grouped by level.
+// the host: blocks are the largest subtrees within the per-warp budget
+// (factor entries, vector rows, supernodes, and no front beyond the
+// register path of the solve kernels); the supernodes above them form the
+// top region, listed children before parents.
 struct HostBlk {
     int nblk = 0;
-    int max_n = 1, max_l = 1, max_v = 1, max_p = 1, max_map = 1, max_ext = 1;
+    int max_n = 1, max_v = 1, max_p = 1, max_map = 1, max_ext = 1;
     std::vector<int> blk_ptr{0}, map_ptr{0}, ext_ptr{0}, map_fwd, map_bwd, ext_pos, ext_row;
     std::vector<int4> ent0, ent1;
     int n_top_levels = 0, top_max_front = 1;
-    std::vector<int> top_ptr, top_sups;
+    std::vector<int> top_order, top_rank;
 };
 
 void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
     constexpr long kLimSlices = 2048, kLimRows = 512, kLimSups = 64;
+    const long kLimFront = gp::solve_block_front_limit();
     const int ns = sym.nsup;
-    std::vector<long> sl(ns, 0), sv(ns, 0), sn(ns, 0);
+    std::vector<long> sl(ns, 0), sv(ns, 0), sn(ns, 0), sm(ns, 0);
     for (int l = 0; l < sym.nlevels; l++)
         for (int q = sym.level_ptr[l]; q < sym.level_ptr[l + 1]; q++) {
             const int s = sym.level_sups[q];
@@ -392,14 +400,18 @@ void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
             sl[s] = m * n + n * r;
             sv[s] = m;
             sn[s] = 1;
+            sm[s] = m;
             for (int c = sym.child_ptr[s]; c < sym.child_ptr[s + 1]; c++) {
                 const int ch = sym.children[c];
                 sl[s] += sl[ch];
                 sv[s] += sv[ch];
                 sn[s] += sn[ch];
+                sm[s] = std::max(sm[s], sm[ch]);
             }
         }
-    auto fits = [&](int s) { return sl[s] <= kLimSlices && sv[s] <= kLimRows && sn[s] <= kLimSups; };
+    auto fits = [&](int s) {
+        return sl[s] <= kLimSlices && sv[s] <= kLimRows && sn[s] <= kLimSups && sm[s] <= kLimFront;
+    };
     // levels run from the leaves (0) to the roots, so parents are visited
     // before their children here
     std::vector<int> blk_of(ns, -1);
@@ -419,13 +431,12 @@ void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
         }
     std::vector<int> voff_of(ns, -1);
     for (int b = 0; b < nblk; b++) {
-        int lo = 0, vo = 0, mo = 0, po = 0;
+        int vo = 0, mo = 0, po = 0;
         for (int s : members[b]) {
             const int m = sym.front_m(s), n = sym.front_n(s), r = sym.front_r(s);
             B.ent0.push_back(make_int4(s, sym.sup_start[s], n, r));
-            B.ent1.push_back(make_int4(lo, vo, mo, po));
+            B.ent1.push_back(make_int4(0, vo, mo, po));
             voff_of[s] = vo;
-            lo += m * n + n * r;
             vo += m;
             mo += r;
             po += n;
@@ -451,7 +462,6 @@ void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
             B.ext_row.push_back(kv.first);
         }
         B.max_n = std::max(B.max_n, (int)members[b].size());
-        B.max_l = std::max(B.max_l, lo);
         B.max_v = std::max(B.max_v, vo + (int)ext.size());
         B.max_p = std::max(B.max_p, po);
         B.max_map = std::max(B.max_map, mo);
@@ -475,20 +485,22 @@ void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
             ntl = std::max(ntl, d + 1);
             B.top_max_front = std::max(B.top_max_front, sym.front_m(s));
         }
-    B.top_ptr.assign(ntl + 1, 0);
-    B.top_sups.clear();
-    for (int d = 0; d < ntl; d++) {
+    B.top_order.clear();
+    B.top_rank.assign(ns, -1);
+    for (int d = 0; d < ntl; d++)
         for (int s = 0; s < ns; s++)
-            if (tlev[s] == d) B.top_sups.push_back(s);
-        B.top_ptr[d + 1] = (int)B.top_sups.size();
-    }
+            if (tlev[s] == d) {
+                B.top_rank[s] = (int)B.top_order.size();
+                B.top_order.push_back(s);
+            }
     B.n_top_levels = ntl;
 }
 
 // Host emulation of the device factorisation (gp_dag.cu): the same front
 // layout, assembly order and pivot rule, supernodes by level; the diagonal
-// keeps the reciprocal of each pivot, as on the device.  Returns the number
-// of zero pivots.
+// keeps the reciprocal of each pivot and ipiv the composed row permutation
+// of each supernode (pivot row i = assembled row ipiv[start + i]), as on the
+// device.  Returns the number of zero pivots.
 int host_factor(const Plan &pl, const std::vector<double> &svar, std::vector<double> &fronts, std::vector<int> &ipiv) {
     const gp::Symbolic &S = pl.sym;
     fronts.assign(S.front_off[S.nsup], 0.0);
@@ -509,6 +521,8 @@ int host_factor(const Plan &pl, const std::vector<double> &svar, std::vector<dou
                 for (int b = 0; b < rc; b++)
                     for (int a = 0; a < rc; a++) F[rel[a] + rel[b] * mm] += Fc[(nc + a) + (size_t)(nc + b) * mc];
             }
+            std::vector<int> perm(ns);
+            for (int i = 0; i < ns; i++) perm[i] = i;
             for (int k = 0; k < ns; k++) {
                 double best = -1.0;
                 int bi = k;
@@ -517,7 +531,7 @@ int host_factor(const Plan &pl, const std::vector<double> &svar, std::vector<dou
                     if (v > best) { best = v; bi = i; }
                 }
                 if (best == 0.0) zero_pivots++;
-                ipiv[start + k] = bi;
+                std::swap(perm[k], perm[bi]);
                 if (bi != k)
                     for (int j = 0; j < mm; j++) std::swap(F[k + j * mm], F[bi + j * mm]);
                 const double inv = 1.0 / F[k + k * mm];
@@ -526,6 +540,7 @@ int host_factor(const Plan &pl, const std::vector<double> &svar, std::vector<dou
                     for (int i = k + 1; i < mm; i++) F[i + j * mm] -= F[i + k * mm] * F[k + j * mm];
                 F[k + k * mm] = inv;
             }
+            for (int i = 0; i < ns; i++) ipiv[start + i] = perm[i];
         }
     return zero_pivots;
 }
@@ -539,19 +554,19 @@ void host_level_solve(const gp::Symbolic &S, const std::vector<double> &fronts, 
         for (int q = S.level_ptr[l]; q < S.level_ptr[l + 1]; q++) {
             const int s = S.level_sups[q];
             const int ns = S.front_n(s), r = S.front_r(s), mm = S.front_m(s), start = S.sup_start[s];
-            std::vector<double> t(x.begin() + start, x.begin() + start + ns), u(r, 0.0);
+            std::vector<double> a(x.begin() + start, x.begin() + start + ns), u(r, 0.0);
             for (int cq = S.child_ptr[s]; cq < S.child_ptr[s + 1]; cq++) {
                 const int c = S.children[cq];
                 const int *rel = S.relmap.data() + S.relmap_ptr[c];
                 const double *uc = uvec.data() + S.uvec_off[c];
-                for (int a = 0; a < S.front_r(c); a++) {
-                    if (rel[a] < ns) t[rel[a]] += uc[a];
-                    else u[rel[a] - ns] += uc[a];
+                for (int e = 0; e < S.front_r(c); e++) {
+                    if (rel[e] < ns) a[rel[e]] += uc[e];
+                    else u[rel[e] - ns] += uc[e];
                 }
             }
             const double *F = fronts.data() + S.front_off[s];
-            for (int k = 0; k < ns; k++)
-                if (ipiv[start + k] != k) std::swap(t[k], t[ipiv[start + k]]);
+            std::vector<double> t(ns);
+            for (int i = 0; i < ns; i++) t[i] = a[ipiv[start + i]];
             for (int k = 0; k < ns; k++)
                 for (int i = k + 1; i < ns; i++) t[i] -= F[i + k * mm] * t[k];
             for (int i = 0; i < r; i++) {
@@ -582,7 +597,7 @@ void host_level_solve(const gp::Symbolic &S, const std::vector<double> &fronts, 
         }
 }
 
-// Bounds-checked stand-in for one warp's shared-memory staging array.
+// Bounds-checked stand-in for one warp's shared-memory arrays.
 struct Staged {
     std::vector<double> v;
     const char *what;
@@ -593,10 +608,38 @@ struct Staged {
     }
 };
 
+// One front's forward elimination and backward substitution on a staged
+// vector v (offset o), in the device kernels' order (gp_solve.cu).
+void host_fwd_front(const double *F, const int *perm, int ns, int mm, Staged &v, long o) {
+    std::vector<double> t(ns);
+    for (int i = 0; i < ns; i++) {
+        if (perm[i] < 0 || perm[i] >= ns) fail(GP_E_INTERNAL, "block solve: permutation entry %d outside [0, %d)", perm[i], ns);
+        t[i] = v[o + perm[i]];
+    }
+    for (int i = 0; i < ns; i++) v[o + i] = t[i];
+    for (int k = 0; k < ns; k++) {
+        const double vk = v[o + k];
+        for (int i = k + 1; i < mm; i++) v[o + i] -= F[i + (size_t)k * mm] * vk;
+    }
+}
+
+void host_bwd_front(const double *F, int ns, int mm, Staged &v, long o) {
+    for (int i = 0; i < ns; i++) {
+        double acc = 0.0;
+        for (int a = 0; a < mm - ns; a++) acc += F[i + (size_t)(ns + a) * mm] * v[o + ns + a];
+        v[o + i] -= acc;
+    }
+    for (int k = ns - 1; k >= 0; k--) {
+        const double tk = v[o + k] * F[k + (size_t)k * mm];
+        v[o + k] = tk;
+        for (int i = 0; i < k; i++) v[o + i] -= F[i + (size_t)k * mm] * tk;
+    }
+}
+
 // Host emulation of the blocked triangular solves (gp_solve.cu) with the
-// same staging areas, sized by the block maxima, and every staged index
-// checked against them: blocks forward, top region forward by level, top
-// region backward, blocks backward.
+// same staged vectors, maps and permutations, sized by the block maxima,
+// every staged index checked against them: blocks forward, top region
+// forward in its task order, top region backward, blocks backward.
 void host_block_solve(const gp::Symbolic &S, const HostBlk &B, const std::vector<double> &fronts,
                       const std::vector<int> &ipiv, std::vector<double> &x) {
     std::vector<double> uvec(std::max<int64_t>(1, S.uvec_off[S.nsup]), 0.0);
@@ -605,9 +648,11 @@ void host_block_solve(const gp::Symbolic &S, const HostBlk &B, const std::vector
         b = B.ent1[e];
         if (a.z != S.front_n(a.x) || a.w != S.front_r(a.x) || a.y != S.sup_start[a.x])
             fail(GP_E_INTERNAL, "block solve: entry %d does not describe supernode %d", e, a.x);
+        if (S.front_m(a.x) > gp::solve_block_front_limit())
+            fail(GP_E_INTERNAL, "block solve: front of %d rows in a block", S.front_m(a.x));
     };
     for (int blk = 0; blk < B.nblk; blk++) {
-        Staged Ls(B.max_l, "factor slice"), vs(B.max_v, "vector"), pv(B.max_p, "pivot"), mp(B.max_map, "map");
+        Staged vs(B.max_v, "vector"), pv(B.max_p, "pivot"), mp(B.max_map, "map");
         const int e0 = B.blk_ptr[blk], n = B.blk_ptr[blk + 1] - e0;
         if (n > B.max_n) fail(GP_E_INTERNAL, "block solve: %d entries above max_n", n);
         const int mb = B.map_ptr[blk], nmap = B.map_ptr[blk + 1] - mb;
@@ -615,81 +660,53 @@ void host_block_solve(const gp::Symbolic &S, const HostBlk &B, const std::vector
         for (int q = 0; q < n; q++) {
             int4 a, b;
             ent(e0 + q, a, b);
-            const int ns = a.z, mm = a.z + a.w;
-            for (int i = 0; i < mm * ns; i++) Ls[b.x + i] = fronts[S.front_off[a.x] + i];
-            for (int i = 0; i < ns; i++) {
-                vs[b.y + i] = x[a.y + i];
-                pv[b.w + i] = ipiv[a.y + i];
-            }
-            for (int i = 0; i < a.w; i++) vs[b.y + ns + i] = 0.0;
+            for (int i = 0; i < a.z; i++) pv[b.w + i] = ipiv[a.y + i];
+            for (int i = 0; i < a.z + a.w; i++) vs[b.y + i] = i < a.z ? x[a.y + i] : 0.0;
         }
         for (int q = 0; q < n; q++) {
             int4 a, b;
             ent(e0 + q, a, b);
-            const int s = a.x, start = a.y, ns = a.z, r = a.w, mm = ns + r;
-            for (int k = 0; k < ns; k++) {
-                const int p = (int)pv[b.w + k];
-                if (p < k || p >= ns) fail(GP_E_INTERNAL, "block solve: pivot %d of supernode %d out of range", p, s);
-                if (p != k) std::swap(vs[b.y + k], vs[b.y + p]);
-            }
-            for (int k = 0; k < ns; k++)
-                for (int i = k + 1; i < ns; i++) vs[b.y + i] -= Ls[b.x + i + k * mm] * vs[b.y + k];
-            for (int i = 0; i < r; i++) {
-                double acc = 0.0;
-                for (int k = 0; k < ns; k++) acc += Ls[b.x + ns + i + k * mm] * vs[b.y + k];
-                vs[b.y + ns + i] -= acc;
-            }
-            if (q < n - 1) {
+            const int s = a.x, ns = a.z, r = a.w;
+            std::vector<int> perm(ns);
+            for (int i = 0; i < ns; i++) perm[i] = (int)pv[b.w + i];
+            host_fwd_front(fronts.data() + S.front_off[s], perm.data(), ns, ns + r, vs, b.y);
+            for (int i = 0; i < ns; i++) x[a.y + i] = vs[b.y + i];
+            if (q < n - 1)
                 for (int i = 0; i < r; i++) vs[(long)mp[b.z + i]] += vs[b.y + ns + i];
-            } else {
+            else
                 for (int i = 0; i < r; i++) uvec[S.uvec_off[s] + i] = vs[b.y + ns + i];
-            }
-            for (int i = 0; i < ns; i++) x[start + i] = vs[b.y + i];
         }
     }
-    auto top_fwd = [&](int s) {
+    const int ntop = (int)B.top_order.size();
+    for (int t = 0; t < ntop; t++) {
+        const int s = B.top_order[t];
+        for (int cq = S.child_ptr[s]; cq < S.child_ptr[s + 1]; cq++) {
+            const int c = S.children[cq];
+            if (B.top_rank[c] >= t) fail(GP_E_INTERNAL, "top order: child %d after parent %d", c, s);
+        }
         const int start = S.sup_start[s], ns = S.front_n(s), r = S.front_r(s), mm = ns + r;
         Staged tv(B.top_max_front, "top vector");
-        for (int i = 0; i < ns; i++) tv[i] = x[start + i];
+        for (int i = 0; i < mm; i++) tv[i] = i < ns ? x[start + i] : 0.0;
         for (int cq = S.child_ptr[s]; cq < S.child_ptr[s + 1]; cq++) {
             const int c = S.children[cq];
             const int *rel = S.relmap.data() + S.relmap_ptr[c];
             for (int a = 0; a < S.front_r(c); a++) tv[rel[a]] += uvec[S.uvec_off[c] + a];
         }
-        const double *F = fronts.data() + S.front_off[s];
-        for (int k = 0; k < ns; k++)
-            if (ipiv[start + k] != k) std::swap(tv[k], tv[ipiv[start + k]]);
-        for (int k = 0; k < ns; k++)
-            for (int i = k + 1; i < ns; i++) tv[i] -= F[i + k * mm] * tv[k];
-        for (int a = 0; a < r; a++) {
-            double acc = 0.0;
-            for (int k = 0; k < ns; k++) acc += F[ns + a + (size_t)k * mm] * tv[k];
-            uvec[S.uvec_off[s] + a] = tv[ns + a] - acc;
-        }
+        host_fwd_front(fronts.data() + S.front_off[s], ipiv.data() + start, ns, mm, tv, 0);
         for (int i = 0; i < ns; i++) x[start + i] = tv[i];
-    };
-    auto top_bwd = [&](int s) {
+        for (int a = 0; a < r; a++) uvec[S.uvec_off[s] + a] = tv[ns + a];
+    }
+    for (int t = ntop - 1; t >= 0; t--) {
+        const int s = B.top_order[t];
         const int start = S.sup_start[s], ns = S.front_n(s), r = S.front_r(s), mm = ns + r;
         Staged tv(B.top_max_front, "top vector");
-        const double *F = fronts.data() + S.front_off[s];
         const int *rows = S.rows.data() + S.row_ptr[s];
-        for (int i = 0; i < ns; i++) {
-            double acc = 0.0;
-            for (int a = 0; a < r; a++) acc += F[i + (size_t)(ns + a) * mm] * x[rows[a]];
-            tv[i] = x[start + i] - acc;
-        }
-        for (int k = ns - 1; k >= 0; k--) {
-            const double tk = tv[k] * F[k + k * mm];
-            x[start + k] = tk;
-            for (int i = 0; i < k; i++) tv[i] -= F[i + k * mm] * tk;
-        }
-    };
-    for (int l = 0; l < B.n_top_levels; l++)
-        for (int q = B.top_ptr[l]; q < B.top_ptr[l + 1]; q++) top_fwd(B.top_sups[q]);
-    for (int l = B.n_top_levels - 1; l >= 0; l--)
-        for (int q = B.top_ptr[l]; q < B.top_ptr[l + 1]; q++) top_bwd(B.top_sups[q]);
+        for (int i = 0; i < mm; i++) tv[i] = i < ns ? x[start + i] : x[rows[i - ns]];
+        host_bwd_front(fronts.data() + S.front_off[s], ns, mm, tv, 0);
+        for (int i = 0; i < ns; i++) x[start + i] = tv[i];
+    }
     for (int blk = 0; blk < B.nblk; blk++) {
-        Staged Ls(B.max_l, "factor slice"), vs(B.max_v, "vector"), mp(B.max_map, "map");
+        Staged vs(B.max_v, "vector"), mp(B.max_map, "map");
         const int e0 = B.blk_ptr[blk], n = B.blk_ptr[blk + 1] - e0;
         const int mb = B.map_ptr[blk], nmap = B.map_ptr[blk + 1] - mb;
         for (int i = 0; i < nmap; i++) mp[i] = B.map_bwd[mb + i];
@@ -698,28 +715,20 @@ void host_block_solve(const gp::Symbolic &S, const HostBlk &B, const std::vector
         for (int q = 0; q < n; q++) {
             int4 a, b;
             ent(e0 + q, a, b);
-            const int ns = a.z, r = a.w, mm = ns + r;
-            const double *src = fronts.data() + S.front_off[a.x];
-            for (int i = 0; i < mm * ns; i++) Ls[b.x + i] = src[i];
-            for (int e = 0; e < ns * r; e++) Ls[b.x + mm * ns + e] = src[e % ns + (size_t)(ns + e / ns) * mm];
-            for (int i = 0; i < ns; i++) vs[b.y + i] = x[a.y + i];
+            for (int i = 0; i < a.z; i++) vs[b.y + i] = x[a.y + i];
         }
         for (int k = 0; k < next; k++) vs[B.ext_pos[xb + k]] = x[B.ext_row[xb + k]];
         for (int q = n - 1; q >= 0; q--) {
             int4 a, b;
             ent(e0 + q, a, b);
-            const int start = a.y, ns = a.z, r = a.w, mm = ns + r;
-            for (int i = 0; i < ns; i++) {
-                double acc = 0.0;
-                for (int c = 0; c < r; c++) acc += Ls[b.x + mm * ns + i + c * ns] * vs[(long)mp[b.z + c]];
-                vs[b.y + i] -= acc;
+            const int ns = a.z, r = a.w;
+            for (int c = 0; c < r; c++) {
+                const long g = (long)mp[b.z + c];
+                if (g >= b.y && g < b.y + ns + r) fail(GP_E_INTERNAL, "block solve: map into the front's own rows");
+                vs[b.y + ns + c] = vs[g];
             }
-            for (int k = ns - 1; k >= 0; k--) {
-                const double tk = vs[b.y + k] * Ls[b.x + k + k * mm];
-                vs[b.y + k] = tk;
-                for (int i = 0; i < k; i++) vs[b.y + i] -= Ls[b.x + i + k * mm] * tk;
-            }
-            for (int i = 0; i < ns; i++) x[start + i] = vs[b.y + i];
+            host_bwd_front(fronts.data() + S.front_off[a.x], ns, ns + r, vs, b.y);
+            for (int i = 0; i < ns; i++) x[a.y + i] = vs[b.y + i];
         }
     }
 }
@@ -771,11 +780,9 @@ void build_blocks(gp_layout *L, const gp::Symbolic &sym) {
     gp::DevBlk &B = L->B;
     B.nblk = H.nblk;
     B.max_n = H.max_n;
-    B.max_l = H.max_l;
     B.max_v = H.max_v;
     B.max_p = H.max_p;
     B.max_map = H.max_map;
-    B.max_ext = H.max_ext;
     B.blk_ptr = A.upload(H.blk_ptr);
     B.ent0 = A.upload(H.ent0);
     B.ent1 = A.upload(H.ent1);
@@ -785,11 +792,12 @@ void build_blocks(gp_layout *L, const gp::Symbolic &sym) {
     B.ext_ptr = A.upload(H.ext_ptr);
     B.ext_pos = A.upload(H.ext_pos);
     B.ext_row = A.upload(H.ext_row);
-    B.n_top_levels = H.n_top_levels;
+    B.n_top = (int)H.top_order.size();
     B.top_max_front = H.top_max_front;
-    B.top_ptr = A.upload(H.top_ptr);
-    B.top_sups = A.upload(H.top_sups);
-    if (gp::solve_configure(B) != 0) fail(GP_E_CUDA, "could not configure the solve kernels");
+    B.top_order = A.upload(H.top_order);
+    B.top_rank = A.upload(H.top_rank);
+    L->n_top_levels = H.n_top_levels;
+    if (gp::solve_configure(B, L->SG) != 0) fail(GP_E_CUDA, "could not configure the solve kernels");
 }
 
 void build_problem(gp_layout *L, const gp_problem *pr) {
@@ -919,7 +927,7 @@ void build_work(gp_layout *L, const double *z0, const double *u0, const double *
     W.active = A.alloc<uint8_t>(M);
     W.iters = A.alloc<int>(M);
     W.status = A.alloc<int>(M);
-    W.flag = A.alloc<int>(2);
+    W.flag = A.alloc<int>(3);
     W.dt = A.alloc<double>(1);
     DevSym &S = L->S;
     S.fronts = A.alloc<double>(M * S.front_total);
@@ -949,7 +957,7 @@ void build_work(gp_layout *L, const double *z0, const double *u0, const double *
     ck(cudaMemset(D.xdone, 0, M * D.nsup * sizeof(int)), "memset");
     ck(cudaMemset(D.bdone, 0, M * D.nsup * sizeof(int)), "memset");
     ck(cudaMemset(W.status, 0, M * sizeof(int)), "memset");
-    ck(cudaMallocHost(&L->h_flag, 2 * sizeof(int)), "cudaMallocHost");
+    ck(cudaMallocHost(&L->h_flag, 3 * sizeof(int)), "cudaMallocHost");
     ck(cudaMallocHost(&L->h_dt, sizeof(double)), "cudaMallocHost");
     ck(cudaStreamCreateWithFlags(&L->st, cudaStreamNonBlocking), "stream");
     for (int i = 0; i < 8; i++) ck(cudaEventCreate(&L->pev[i]), "event");
@@ -988,6 +996,14 @@ void build_clusters(gp_layout *L, const gp_problem *pr, const double *z0, const 
     const int bytes = cp.max_slots * 32 * (int)sizeof(double);
     if (bytes > 48 * 1024 && gp::cluster_smem_optin(bytes) < 0)
         fail(GP_E_CUDA, "cluster kernel needs %d bytes of shared memory", bytes);
+}
+
+void drop_graphs(gp_layout *L) {
+    for (cudaGraphExec_t *g : {&L->g_eval, &L->g_solve, &L->g_mix[0], &L->g_mix[1], &L->g_mix[2], &L->g_mix[3]})
+        if (*g) {
+            cudaGraphExecDestroy(*g);
+            *g = nullptr;
+        }
 }
 
 void set_faults(gp_layout *L, int n_faults, const gp_fault *faults) {
@@ -1031,44 +1047,63 @@ void set_faults(gp_layout *L, int n_faults, const gp_fault *faults) {
     L->h_fl_off_step = off;
     L->h_fl_scen = scen;
     // graphs capture the fault pointers: rebuild them
-    for (cudaGraphExec_t *g : {&L->g_eval, &L->g_solve, &L->g_solve_keep})
-        if (*g) {
-            cudaGraphExecDestroy(*g);
-            *g = nullptr;
-        }
+    drop_graphs(L);
 }
 
 void mark(gp_layout *L, int i) {
     ck(cudaEventRecordWithFlags(L->pev[i], L->st, cudaEventRecordExternal), "event record");
 }
 
-// Solve graph.  FP64: fresh factorisation (with the forward solve fused),
-// backward solve, update.  Mixed, refresh=true: FP32 factorisation of the
-// scenarios refreshing their factors, then both solves with the kept FP32
-// factors; refresh=false: the solves alone.
-int enqueue_solve(gp_layout *L, bool mixed, bool refresh) {
+// Solve graph; returns its kernel launches and counts its factorisation
+// launches in *nfac_out.  FP64 (variant < 0): fresh factorisation with the
+// forward solve fused, backward solve, update.  Mixed, variant bits: 1 the
+// FP32 factorisation of the MX_FP32 scenarios, 2 the FP64 factorisation
+// (forward solve fused) of the MX_EXACT scenarios; then the forward solve of
+// the scenarios on FP32 factors, the backward solve of all (each with its
+// own factors), and the update.
+int enqueue_solve(gp_layout *L, int variant, int *nfac_out) {
     const gp::DevDag &D = L->D;
     const int nfac = (D.n_small > 0) + (D.nsup > D.n_small);
+    const gp::DevBlk &B = L->B;
+    const int nsolve = (B.nblk > 0) + (B.n_top > 0);
+    int launches = 2, facs = 0;   // dag_begin, update
     mark(L, 3);
     gp::launch_dag_begin(D, L->st);
-    const gp::DevBlk &B = L->B;
-    const int nsolve = (B.nblk > 0) + (B.n_top_levels > 0);
-    if (!mixed) {
-        gp::launch_dag_factor<double>(L->P, L->W, L->S, D, L->G64, L->S.fronts, L->W.active, L->st);
+    if (variant < 0) {
+        const gp::FrontSel fs{nullptr, L->S.fronts, nullptr, 1};
+        gp::launch_dag_factor<double>(L->P, L->W, L->S, D, L->G64, L->S.fronts, L->W.active, 1, L->st);
         mark(L, 4);   // the FP64 factorisation includes the forward solve
         mark(L, 5);
-        gp::launch_solve_bwd<double>(L->P, L->W, L->S, B, L->S.fronts, L->st);
+        gp::launch_solve_bwd(L->P, L->W, L->S, B, D, L->SG, fs, L->st);
+        facs = nfac;
+        launches += nfac + nsolve;
     } else {
-        if (refresh) gp::launch_dag_factor<float>(L->P, L->W, L->S, D, L->G32, L->Mx.fronts, L->Mx.refac, L->st);
+        const gp::FrontSel fs{L->Mx.fronts, L->S.fronts, L->Mx.refac, 1};
+        if (variant & 1) {
+            gp::launch_dag_factor<float>(L->P, L->W, L->S, D, L->G32, L->Mx.fronts, L->Mx.refac, gp::MX_FP32, L->st);
+            facs += nfac;
+        }
+        if (variant & 2) {
+            // the two factorisations share the claim counters and done
+            // flags: re-arm them (new epoch) for the second one
+            if (variant & 1) {
+                gp::launch_dag_begin(D, L->st);
+                launches += 1;
+            }
+            gp::launch_dag_factor<double>(L->P, L->W, L->S, D, L->G64, L->S.fronts, L->Mx.refac, gp::MX_EXACT, L->st);
+            facs += nfac;
+        }
         mark(L, 4);
-        gp::launch_solve_fwd<float>(L->P, L->W, L->S, B, L->Mx.fronts, L->st);
+        gp::launch_solve_fwd(L->P, L->W, L->S, B, D, L->SG, fs, L->st);
         mark(L, 5);
-        gp::launch_solve_bwd<float>(L->P, L->W, L->S, B, L->Mx.fronts, L->st);
+        gp::launch_solve_bwd(L->P, L->W, L->S, B, D, L->SG, fs, L->st);
+        launches += facs + 2 * nsolve;
     }
     mark(L, 6);
     gp::launch_update(L->P, L->W, L->S, L->d_state_maps, L->st);
     mark(L, 7);
-    return 1 + (mixed ? (refresh ? nfac : 0) + 2 * nsolve : nfac + nsolve) + 1;
+    *nfac_out = facs;
+    return launches;
 }
 
 void enqueue_eval(gp_layout *L, double tol, int itermax) {
@@ -1079,7 +1114,7 @@ void enqueue_eval(gp_layout *L, double tol, int itermax) {
     gp::launch_network(L->P, L->W, 0, L->st);
     mark(L, 2);
     gp::launch_check(L->P, L->W, L->Mx, tol, itermax, L->st);
-    ck(cudaMemcpyAsync(L->h_flag, L->W.flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, L->st), "flag copy");
+    ck(cudaMemcpyAsync(L->h_flag, L->W.flag, 3 * sizeof(int), cudaMemcpyDeviceToHost, L->st), "flag copy");
 }
 
 template <class F>
@@ -1092,14 +1127,6 @@ cudaGraphExec_t capture(gp_layout *L, F enqueue) {
     ck(cudaGraphInstantiate(&ex, g, 0), "graph instantiate");
     cudaGraphDestroy(g);
     return ex;
-}
-
-void drop_graphs(gp_layout *L) {
-    for (cudaGraphExec_t *g : {&L->g_eval, &L->g_solve, &L->g_solve_keep})
-        if (*g) {
-            cudaGraphExecDestroy(*g);
-            *g = nullptr;
-        }
 }
 
 // Kept FP32 factors of the mixed solver, allocated on its first use.
@@ -1116,6 +1143,7 @@ void ensure_mixed(gp_layout *L) {
     X.rho_max = L->mx_rho_max;
     X.refac = A.alloc<uint8_t>(M);
     X.refac_next = A.alloc<uint8_t>(M);
+    X.prev_mode = A.alloc<uint8_t>(M);
     X.age = A.alloc<int>(M);
     X.prev_norm = A.alloc<double>(M);
     X.lu = A.alloc<float>(M * std::max(1, L->C.n_tasks) * n_lu * 32);
@@ -1123,6 +1151,7 @@ void ensure_mixed(gp_layout *L) {
     X.fronts = A.alloc<float>(M * L->S.front_total);
     ck(cudaMemset(X.refac, 0, M), "memset");
     ck(cudaMemset(X.refac_next, 0, M), "memset");
+    ck(cudaMemset(X.prev_mode, 0, M), "memset");
     ck(cudaMemset(X.age, 0, M * sizeof(int)), "memset");
     // kept factors start at zero (zero pivot reciprocals give a zero step,
     // which the contraction test turns into a refresh)
@@ -1144,9 +1173,18 @@ void ensure_graphs(gp_layout *L, double tol, int itermax, int solver) {
         L->graph_itermax = itermax;
         L->solver = solver;
     }
-    if (!L->g_solve) L->g_solve = capture(L, [&] { L->solve_graph_launches = enqueue_solve(L, mixed, true); });
-    if (mixed && !L->g_solve_keep)
-        L->g_solve_keep = capture(L, [&] { L->keep_graph_launches = enqueue_solve(L, true, false); });
+    if (!mixed && !L->g_solve) {
+        int nf = 0;
+        L->g_solve = capture(L, [&] { L->solve_graph_launches = enqueue_solve(L, -1, &nf); });
+    }
+}
+
+// Solve graph of the mixed solver for the modes present (captured on first use).
+cudaGraphExec_t mixed_graph(gp_layout *L, int variant) {
+    if (!L->g_mix[variant])
+        L->g_mix[variant] = capture(
+            L, [&] { L->mix_launches[variant] = enqueue_solve(L, variant, &L->mix_factor_launches[variant]); });
+    return L->g_mix[variant];
 }
 
 // One Newton solve for the scenarios marked active; returns after every
@@ -1181,12 +1219,19 @@ void newton(gp_layout *L, double dt, double tol, int itermax, bool force_refresh
             solve_pending = false;
         }
         if (L->h_flag[0] == 0) return;
-        const bool refresh = !mixed || L->h_flag[1] > 0;
-        ck(cudaGraphLaunch(refresh ? L->g_solve : L->g_solve_keep, L->st), "graph launch");
+        if (mixed) {
+            const int v = (L->h_flag[1] > 0 ? 1 : 0) | (L->h_flag[2] > 0 ? 2 : 0);
+            ck(cudaGraphLaunch(mixed_graph(L, v), L->st), "graph launch");
+            L->launches += L->mix_launches[v];
+            L->factor_launches += L->mix_factor_launches[v];
+            L->refreshes += L->h_flag[1];
+            L->exact_iters += L->h_flag[2];
+        } else {
+            ck(cudaGraphLaunch(L->g_solve, L->st), "graph launch");
+            L->launches += L->solve_graph_launches;
+            L->factor_launches += (L->D.n_small > 0) + (L->D.nsup > L->D.n_small);
+        }
         solve_pending = true;
-        L->launches += refresh ? L->solve_graph_launches : L->keep_graph_launches;
-        if (refresh) L->factor_launches += (L->D.n_small > 0) + (L->D.nsup > L->D.n_small);
-        if (mixed) L->refreshes += L->h_flag[1];
         L->solves += 1;
     }
     fail(GP_E_NUMERIC, "Newton loop did not terminate");
@@ -1254,9 +1299,7 @@ int32_t gp_layout_create(const gp_problem *prob, int32_t M, const double *z0, co
 int32_t gp_layout_destroy(gp_layout *L) {
     API_BEGIN
     if (!L) return GP_OK;
-    if (L->g_eval) cudaGraphExecDestroy(L->g_eval);
-    if (L->g_solve) cudaGraphExecDestroy(L->g_solve);
-    if (L->g_solve_keep) cudaGraphExecDestroy(L->g_solve_keep);
+    drop_graphs(L);
     if (L->st) cudaStreamSynchronize(L->st);
     L->call.release();
     L->arena.release();
@@ -1371,6 +1414,7 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
     L->factor_launches = 0;
     L->solves = 0;
     L->refreshes = 0;
+    L->exact_iters = 0;
     for (int i = 0; i < 8; i++) L->ph_ms[i] = 0.0;
     ck(cudaMemsetAsync(L->D.err, 0, sizeof(int), L->st), "memset");
     // the mixed solver refreshes its kept factors at the first solve and
@@ -1556,6 +1600,7 @@ int32_t gp_last_timing(const gp_layout *L, double out[16]) {
     out[8] = L->factor_launches;
     out[9] = L->solves;
     out[10] = L->refreshes;
+    out[11] = L->exact_iters;
     API_END
 }
 
@@ -1628,7 +1673,7 @@ extern "C" int32_t gp_residual_static(gp_layout *L, const double *zold, double d
     W.xperm = cv.take<double>(M * std::max(1, P.n_red));
     W.norm = cv.take<unsigned long long>(M);
     W.active = cv.take<uint8_t>(M);
-    W.flag = cv.take<int>(2);
+    W.flag = cv.take<int>(3);
     W.dt = cv.take<double>(1);
     int *fl_ptr = cv.take<int>(M + 1);
     // no fault applied: every scenario's fault range is empty

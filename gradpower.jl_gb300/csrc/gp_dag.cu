@@ -1,4 +1,4 @@
-// Dataflow multifrontal factorisation and triangular solves of the reduced
+// Dataflow multifrontal factorisation of the reduced
 // network matrix S, batched over scenarios.
 //
 // This replaces cuDSS's factorization/solve of S
@@ -21,13 +21,12 @@
 // (column-major, leading dimension = front rows) keeps L, U and the update
 // matrix that the parent's extend-add reads.
 //
-// Solves, one launch each, one warp per task over all supernodes:
-//  - fwd_dag_kernel: extend-add of the children's update vectors, row
-//    swaps, unit-lower solve, update vector of this supernode;
-//  - bwd_dag_kernel: gather of the ancestors' solution, upper solve.
-//
 // The factor type T is double (exact Newton) or float (factors kept and
-// reused across Newton iterations); vectors are always double.
+// reused across Newton iterations).  The FP64 factorisation also does the
+// forward solve (the right-hand side rides along as an extra column); the
+// triangular solves are in gp_solve.cu.  Row interchanges are stored as one
+// composed permutation per supernode (ipiv[start + i] = assembled row that
+// became pivot row i), which the solves apply as a single gather.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -40,42 +39,14 @@ namespace gp {
 
 namespace {
 
-constexpr unsigned FULL = 0xffffffffu;
-constexpr int kWaitLimit = 1 << 20;
+constexpr unsigned FULL = kFullMask;
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kSmallFront = 32;
 
-__device__ __forceinline__ int ld_relaxed(const int *p) {
-    int v;
-    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ void fence_acquire() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
-
-__device__ __forceinline__ void st_release(int *p, int v) {
-    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
 template <class T>
 __device__ __forceinline__ T ldcg(const T *p) {
     return __ldcg(p);
-}
-
-// Waits until *flag == epoch; false when it gave up (error flag raised here
-// or by another task).
-__device__ bool wait_epoch(const int *flag, int epoch, int *err) {
-    for (int it = 0; it < kWaitLimit; ++it) {
-        if (ld_relaxed(flag) == epoch) {
-            fence_acquire();
-            return true;
-        }
-        if (*(volatile int *)err) return false;
-        __nanosleep(64);
-    }
-    atomicExch(err, 1);
-    return false;
 }
 
 // One warp waits for the children of supernode s (scenario m) whose
@@ -92,11 +63,6 @@ __device__ bool warp_wait_children(const DevSym &S, const DevDag &D, const int *
     ok = __all_sync(FULL, ok);
     __syncwarp();
     return ok;
-}
-
-__device__ __forceinline__ void signal_done(int *flag, int epoch) {
-    __threadfence();
-    st_release(flag, epoch);
 }
 
 // Magnitude of a factor entry as an unsigned key that orders like |v|
@@ -157,7 +123,7 @@ struct BlockGroup {
 //    and this supernode's update vector in uvec.
 template <class T, bool RHS, class G>
 __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym &S, T *fronts, int s, int m, T *F,
-                             G g) {
+                             int *piv, G g) {
     const int start = S.sup_start[s];
     const int ns = S.sup_start[s + 1] - start;
     const int mm = ns + S.row_ptr[s + 1] - S.row_ptr[s];
@@ -194,14 +160,13 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
         g.sync();
     }
     // ---- elimination ----
-    int *ipiv = S.ipiv + (size_t)m * S.n + start;
     for (int k = 0; k < ns; k++) {
         if (g.lead_warp()) {
             const int lane = threadIdx.x & 31;
             bool zero;
             const int pv = warp_pivot(F, mm, k, ns, zero);
             if (lane == 0) {
-                ipiv[k] = pv;
+                piv[k] = pv;
                 if (zero) atomicOr(W.status + m, 4);
             }
             if (pv != k)
@@ -234,8 +199,22 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
         g.sync();
     }
     // ---- store ----
+    // the row interchanges, composed: pivot row i of the factored front is
+    // row perm[i] of the assembled one
+    if (idx == 0) {
+        int *perm = piv + ns;
+        for (int i = 0; i < ns; i++) perm[i] = i;
+        for (int k = 0; k < ns; k++) {
+            const int p = piv[k], t = perm[k];
+            perm[k] = perm[p];
+            perm[p] = t;
+        }
+    }
     T *out = fr + S.front_off[s];
     for (int i = idx; i < mm * mm; i += step) out[i] = F[i];
+    g.sync();
+    int *ipiv = S.ipiv + (size_t)m * S.n + start;
+    for (int i = idx; i < ns; i += step) ipiv[i] = piv[ns + i];
     if (RHS) {
         for (int i = idx; i < ns; i += step) x[start + i] = (double)F[mm * mm + i];
         double *us = uv + S.uvec_off[s];
@@ -244,12 +223,30 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
     g.sync();
 }
 
+// Shared memory of the factorisation kernels: the front (with the
+// right-hand-side column) and 2 * front rows ints for the pivot indices and
+// their composed permutation, each part 16-byte aligned.
+template <class T>
+__host__ __device__ constexpr int small_front_bytes() {
+    return (kSmallFront * (kSmallFront + 1) * (int)sizeof(T) + 15) & ~15;
+}
+template <class T>
+__host__ __device__ constexpr int small_warp_bytes() {
+    return small_front_bytes<T>() + 2 * kSmallFront * 4;
+}
+template <class T>
+__host__ __device__ inline int big_front_bytes(int max_front) {
+    return (max_front * (max_front + 1) * (int)sizeof(T) + 15) & ~15;
+}
+
 template <class T, bool RHS>
 __global__ void __launch_bounds__(kThreads) factor_small_kernel(DevProblem P, DevWork W, DevSym S, DevDag D,
-                                                                T *fronts, const uint8_t *mask) {
+                                                                T *fronts, const uint8_t *mask, int want) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    T *F = reinterpret_cast<T *>(smem_raw) + warp * kSmallFront * (kSmallFront + 1);
+    unsigned char *wbase = smem_raw + (size_t)warp * small_warp_bytes<T>();
+    T *F = reinterpret_cast<T *>(wbase);
+    int *piv = reinterpret_cast<int *>(wbase + small_front_bytes<T>());
     const int M = P.M;
     const int epoch = *D.epoch;
     const int n_tasks = D.n_small * M;
@@ -259,18 +256,19 @@ __global__ void __launch_bounds__(kThreads) factor_small_kernel(DevProblem P, De
         t = __shfl_sync(FULL, t, 0);
         if (t >= n_tasks) break;
         const int s = D.order[t / M], m = t % M;
-        if (!mask[m]) continue;
+        if (mask[m] != want) continue;
         if (!warp_wait_children(S, D, D.fdone, s, m, M, epoch, 0) && lane == 0) atomicOr(W.status + m, 8);
-        factor_front<T, RHS>(P, W, S, fronts, s, m, F, WarpGroup{});
+        factor_front<T, RHS>(P, W, S, fronts, s, m, F, piv, WarpGroup{});
         if (lane == 0) signal_done(D.fdone + (size_t)s * M + m, epoch);
     }
 }
 
 template <class T, bool RHS>
 __global__ void __launch_bounds__(kThreads) factor_big_kernel(DevProblem P, DevWork W, DevSym S, DevDag D,
-                                                              T *fronts, const uint8_t *mask) {
+                                                              T *fronts, const uint8_t *mask, int want) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *F = reinterpret_cast<T *>(smem_raw);
+    int *piv = reinterpret_cast<int *>(smem_raw + big_front_bytes<T>(D.max_big_front));
     __shared__ int s_task, s_ok;
     const int tid = threadIdx.x, lane = tid & 31;
     const int M = P.M;
@@ -283,115 +281,15 @@ __global__ void __launch_bounds__(kThreads) factor_big_kernel(DevProblem P, DevW
         const int t = s_task;
         if (t >= n_tasks) break;
         const int s = D.order[D.n_small + t / M], m = t % M;
-        if (!mask[m]) continue;
+        if (mask[m] != want) continue;
         if (tid < 32) {
             const bool ok = warp_wait_children(S, D, D.fdone, s, m, M, epoch, D.n_small);
             if (lane == 0) s_ok = ok;
         }
         __syncthreads();
         if (!s_ok && tid == 0) atomicOr(W.status + m, 8);
-        factor_front<T, RHS>(P, W, S, fronts, s, m, F, BlockGroup{});
+        factor_front<T, RHS>(P, W, S, fronts, s, m, F, piv, BlockGroup{});
         if (tid == 0) signal_done(D.fdone + (size_t)s * M + m, epoch);
-    }
-}
-
-template <class T>
-__global__ void __launch_bounds__(kThreads) fwd_dag_kernel(DevProblem P, DevWork W, DevSym S, DevDag D,
-                                                           const T *fronts) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double *tv = reinterpret_cast<double *>(smem_raw) + warp * D.max_front;
-    const int M = P.M;
-    const int epoch = *D.epoch;
-    const int n_tasks = D.nsup * M;
-    for (;;) {
-        int t = 0;
-        if (lane == 0) t = atomicAdd(D.ctr + 2, 1);
-        t = __shfl_sync(FULL, t, 0);
-        if (t >= n_tasks) break;
-        const int s = D.order[t / M], m = t % M;
-        if (!W.active[m]) continue;
-        if (!warp_wait_children(S, D, D.xdone, s, m, M, epoch, 0) && lane == 0) atomicOr(W.status + m, 8);
-        const int start = S.sup_start[s];
-        const int ns = S.sup_start[s + 1] - start;
-        const int r = S.row_ptr[s + 1] - S.row_ptr[s];
-        const int mm = ns + r;
-        double *x = W.xperm + (size_t)m * P.n_red;
-        double *uv = S.uvec + (size_t)m * S.uvec_total;
-        for (int i = lane; i < ns; i += 32) tv[i] = x[start + i];
-        for (int i = lane; i < r; i += 32) tv[ns + i] = 0.0;
-        __syncwarp();
-        for (int q = S.child_ptr[s]; q < S.child_ptr[s + 1]; q++) {
-            const int c = S.children[q];
-            const int rc = S.row_ptr[c + 1] - S.row_ptr[c];
-            const int *rel = S.relmap + S.relmap_ptr[c];
-            const double *uc = uv + S.uvec_off[c];
-            for (int a = lane; a < rc; a += 32) tv[rel[a]] += ldcg(uc + a);
-            __syncwarp();
-        }
-        const T *F = fronts + (size_t)m * S.front_total + S.front_off[s];
-        const int *ipiv = S.ipiv + (size_t)m * S.n + start;
-        if (lane == 0)
-            for (int k = 0; k < ns; k++) {
-                const int pv = ipiv[k];
-                if (pv != k) { const double a = tv[k]; tv[k] = tv[pv]; tv[pv] = a; }
-            }
-        __syncwarp();
-        for (int k = 0; k < ns; k++) {
-            const double tk = tv[k];
-            for (int i = k + 1 + lane; i < ns; i += 32) tv[i] -= (double)F[i + k * mm] * tk;
-            __syncwarp();
-        }
-        double *us = uv + S.uvec_off[s];
-        warp_row_dots<double>(F + ns, 1, mm, r, ns, [&](int k) { return tv[k]; },
-                      [&](int a, double acc) { us[a] = tv[ns + a] - acc; });
-        for (int i = lane; i < ns; i += 32) x[start + i] = tv[i];
-        __syncwarp();
-        if (lane == 0) signal_done(D.xdone + (size_t)s * M + m, epoch);
-    }
-}
-
-template <class T>
-__global__ void __launch_bounds__(kThreads) bwd_dag_kernel(DevProblem P, DevWork W, DevSym S, DevDag D,
-                                                           const T *fronts) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double *tv = reinterpret_cast<double *>(smem_raw) + warp * D.max_front;
-    const int M = P.M;
-    const int epoch = *D.epoch;
-    const int n_tasks = D.nsup * M;
-    for (;;) {
-        int t = 0;
-        if (lane == 0) t = atomicAdd(D.ctr + 3, 1);
-        t = __shfl_sync(FULL, t, 0);
-        if (t >= n_tasks) break;
-        const int s = D.order[D.nsup - 1 - t / M], m = t % M;
-        if (!W.active[m]) continue;
-        const int par = D.parent[s];
-        if (par >= 0) {
-            bool ok = true;
-            if (lane == 0) ok = wait_epoch(D.bdone + (size_t)par * M + m, epoch, D.err);
-            ok = __shfl_sync(FULL, ok, 0);
-            __syncwarp();
-            if (!ok && lane == 0) atomicOr(W.status + m, 8);
-        }
-        const int start = S.sup_start[s];
-        const int ns = S.sup_start[s + 1] - start;
-        const int r = S.row_ptr[s + 1] - S.row_ptr[s];
-        const int mm = ns + r;
-        double *x = W.xperm + (size_t)m * P.n_red;
-        const T *F = fronts + (size_t)m * S.front_total + S.front_off[s];
-        const int *rows = S.rows + S.row_ptr[s];
-        warp_row_dots<double>(F + (size_t)ns * mm, 1, mm, ns, r, [&](int a) { return ldcg(x + rows[a]); },
-                      [&](int i, double acc) { tv[i] = x[start + i] - acc; });
-        __syncwarp();
-        for (int k = ns - 1; k >= 0; k--) {
-            const double tk = tv[k] * (double)F[k + k * mm];   // reciprocal of the pivot
-            if (lane == 0) x[start + k] = tk;
-            for (int i = lane; i < k; i += 32) tv[i] -= (double)F[i + k * mm] * tk;
-            __syncwarp();
-        }
-        if (lane == 0) signal_done(D.bdone + (size_t)s * M + m, epoch);
     }
 }
 
@@ -404,7 +302,7 @@ __global__ void dag_begin_kernel(DevDag D) {
 }
 
 // The FP64 factorisation carries the right-hand side (fused forward solve);
-// the FP32 one is reused across iterations and solved by fwd_dag_kernel.
+// the FP32 one is reused across iterations and solved in gp_solve.cu.
 template <class T>
 struct FusedRhs {
     static constexpr bool value = false;
@@ -415,7 +313,7 @@ struct FusedRhs<double> {
 };
 
 template <class T>
-int configure_one(DagGrid &g, int nsm, int small_bytes, int big_bytes, int vec_bytes) {
+int configure_one(DagGrid &g, int nsm, int small_bytes, int big_bytes) {
     constexpr bool R = FusedRhs<T>::value;
     int occ = 0;
     if (cudaFuncSetAttribute(factor_small_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, small_bytes) !=
@@ -430,18 +328,6 @@ int configure_one(DagGrid &g, int nsm, int small_bytes, int big_bytes, int vec_b
             cudaSuccess || occ < 1)
         return -1;
     g.big = nsm * occ;
-    if (cudaFuncSetAttribute(fwd_dag_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, vec_bytes) !=
-            cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fwd_dag_kernel<T>, kThreads, vec_bytes) != cudaSuccess ||
-        occ < 1)
-        return -1;
-    g.fwd = nsm * occ;
-    if (cudaFuncSetAttribute(bwd_dag_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, vec_bytes) !=
-            cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bwd_dag_kernel<T>, kThreads, vec_bytes) != cudaSuccess ||
-        occ < 1)
-        return -1;
-    g.bwd = nsm * occ;
     return 0;
 }
 
@@ -456,19 +342,17 @@ int dag_configure(const DevDag &D, int fp32, DagGrid &g) {
     int dev = 0, nsm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return -1;
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -1;
-    const int es = fp32 ? 4 : 8;
-    const int small_bytes = kWarps * kSmallFront * (kSmallFront + 1) * es;
-    const int big_bytes = std::max(1, D.max_big_front * (D.max_big_front + 1)) * es;
-    const int vec_bytes = kWarps * D.max_front * 8;
-    const int rc = fp32 ? configure_one<float>(g, nsm, small_bytes, big_bytes, vec_bytes)
-                        : configure_one<double>(g, nsm, small_bytes, big_bytes, vec_bytes);
+    const int mb = std::max(1, D.max_big_front);
+    const int small_bytes = kWarps * (fp32 ? small_warp_bytes<float>() : small_warp_bytes<double>());
+    const int big_bytes = (fp32 ? big_front_bytes<float>(mb) : big_front_bytes<double>(mb)) + 2 * mb * 4;
+    const int rc = fp32 ? configure_one<float>(g, nsm, small_bytes, big_bytes)
+                        : configure_one<double>(g, nsm, small_bytes, big_bytes);
     if (rc != 0) {
         cudaGetLastError();
         return -1;
     }
     g.small_bytes = small_bytes;
     g.big_bytes = big_bytes;
-    g.vec_bytes = vec_bytes;
     return 0;
 }
 
@@ -478,41 +362,19 @@ void launch_dag_begin(const DevDag &D, cudaStream_t st) { dag_begin_kernel<<<1, 
 
 template <class T>
 void launch_dag_factor(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, const DagGrid &g,
-                       T *fronts, const uint8_t *mask, cudaStream_t st) {
+                       T *fronts, const uint8_t *mask, int want, cudaStream_t st) {
     constexpr bool R = FusedRhs<T>::value;
     const long long ts = (long long)D.n_small * P.M, tb = (long long)(D.nsup - D.n_small) * P.M;
     if (ts > 0)
         factor_small_kernel<T, R><<<blocks_for(g.small, ts, kWarps), kThreads, g.small_bytes, st>>>(P, W, S, D,
-                                                                                                   fronts, mask);
+                                                                                                   fronts, mask, want);
     if (tb > 0)
-        factor_big_kernel<T, R><<<blocks_for(g.big, tb, 1), kThreads, g.big_bytes, st>>>(P, W, S, D, fronts, mask);
-}
-
-template <class T>
-void launch_dag_fwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, const DagGrid &g,
-                    const T *fronts, cudaStream_t st) {
-    const long long tasks = (long long)D.nsup * P.M;
-    fwd_dag_kernel<T><<<blocks_for(g.fwd, tasks, kWarps), kThreads, g.vec_bytes, st>>>(P, W, S, D, fronts);
-}
-
-template <class T>
-void launch_dag_bwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, const DagGrid &g,
-                    const T *fronts, cudaStream_t st) {
-    const long long tasks = (long long)D.nsup * P.M;
-    bwd_dag_kernel<T><<<blocks_for(g.bwd, tasks, kWarps), kThreads, g.vec_bytes, st>>>(P, W, S, D, fronts);
+        factor_big_kernel<T, R><<<blocks_for(g.big, tb, 1), kThreads, g.big_bytes, st>>>(P, W, S, D, fronts, mask, want);
 }
 
 template void launch_dag_factor<double>(const DevProblem &, const DevWork &, const DevSym &, const DevDag &,
-                                        const DagGrid &, double *, const uint8_t *, cudaStream_t);
+                                        const DagGrid &, double *, const uint8_t *, int, cudaStream_t);
 template void launch_dag_factor<float>(const DevProblem &, const DevWork &, const DevSym &, const DevDag &,
-                                       const DagGrid &, float *, const uint8_t *, cudaStream_t);
-template void launch_dag_fwd<double>(const DevProblem &, const DevWork &, const DevSym &, const DevDag &,
-                                     const DagGrid &, const double *, cudaStream_t);
-template void launch_dag_fwd<float>(const DevProblem &, const DevWork &, const DevSym &, const DevDag &,
-                                    const DagGrid &, const float *, cudaStream_t);
-template void launch_dag_bwd<double>(const DevProblem &, const DevWork &, const DevSym &, const DevDag &,
-                                     const DagGrid &, const double *, cudaStream_t);
-template void launch_dag_bwd<float>(const DevProblem &, const DevWork &, const DevSym &, const DevDag &,
-                                    const DagGrid &, const float *, cudaStream_t);
+                                       const DagGrid &, float *, const uint8_t *, int, cudaStream_t);
 
 }  // namespace gp

@@ -54,7 +54,7 @@ struct DevWork {
     uint8_t *active;                // [M] scenario takes part in this iteration
     int *iters;                     // [M] Newton updates in the current solve
     int *status;                    // [M] 0 ok, 1 itermax reached, 2 non-finite, 4 zero pivot
-    int *flag;                      // [2] scenarios still iterating; of those, refreshing factors
+    int *flag;                      // [3] scenarios still iterating; of those, MX_FP32 and MX_EXACT ones
     double *dt;                     // [1] time step of the current solve
 };
 
@@ -93,17 +93,25 @@ struct DevClu {
 // Factor reuse of the mixed-precision solver (GP_SOLVER_SCHUR_MIXED).  The
 // cluster blocks' LU values and the reduced-system factors are kept in FP32
 // and reused across Newton iterations; every iteration evaluates the
-// residual in FP64 and applies the kept factors to it.  A scenario refreshes
-// its factors (FP64 Jacobian at the current iterate, stored in FP32) when
-// refac[m] is set.
+// residual in FP64 and applies the kept factors to it.  Per scenario and
+// iteration, refac[m] selects the linear solve:
+//   0 (MX_KEEP)    the kept FP32 factors;
+//   1 (MX_FP32)    fresh factors (FP64 Jacobian at the current iterate),
+//                  stored in FP32 and kept;
+//   2 (MX_EXACT)   fresh FP64 factors, used once (exact Newton); a scenario
+//                  still iterating after exact_after iterations of one
+//                  solve uses these until the solve ends, and refreshes its
+//                  kept factors at the next solve.
+enum { MX_KEEP = 0, MX_FP32 = 1, MX_EXACT = 2 };
 struct DevMixed {
     int on;                // 0: exact Newton with fresh FP64 factors every iteration
     int n_lu;              // LU slots kept per cluster (maximum over classes)
     int max_age;           // Newton solves a factor set may serve before a refresh
-    int exact_after;       // iterations of one solve after which every iteration refreshes
+    int exact_after;       // iterations of one solve after which a scenario uses FP64 factors
     double rho_max;        // residual contraction above which the factors are refreshed
-    uint8_t *refac;        // [M] this iteration refreshes the scenario's factors
-    uint8_t *refac_next;   // [M] set for the next iteration
+    uint8_t *refac;        // [M] mode of this iteration (MX_*)
+    uint8_t *refac_next;   // [M] mode of the next iteration
+    uint8_t *prev_mode;    // [M] mode of the previous iteration (the step just taken)
     int *age;              // [M] Newton solves since the last refresh
     double *prev_norm;     // [M] residual norm of the previous iteration
     float *lu;             // [M][n_tasks][n_lu][32] cluster LU values and pivot reciprocals
@@ -121,15 +129,15 @@ struct DevDag {
     const int *order;       // [nsup]
     const int *rank;        // [nsup] position in order
     const int *parent;      // [nsup] parent supernode or -1
-    int *ctr;               // [4] claim counters: small factor, big factor, forward, backward
+    int *ctr;               // [4] claim counters: small factor, big factor, forward solve, backward solve
     int *epoch;             // [1] current solve
     int *err;               // [1] a wait gave up (sticky until the host clears it)
     int *fdone, *xdone, *bdone;   // [nsup][M] epoch at which the task finished
 };
 
 struct DagGrid {
-    int small = 0, big = 0, fwd = 0, bwd = 0;          // resident blocks
-    int small_bytes = 0, big_bytes = 0, vec_bytes = 0; // dynamic shared memory
+    int small = 0, big = 0;                  // resident blocks
+    int small_bytes = 0, big_bytes = 0;      // dynamic shared memory
 };
 
 int dag_configure(const DevDag &D, int fp32, DagGrid &g);
@@ -137,26 +145,22 @@ int dag_configure(const DevDag &D, int fp32, DagGrid &g);
 // rides along as an extra front column); launch_dag_factor<float> does not.
 int dag_small_front();
 void launch_dag_begin(const DevDag &D, cudaStream_t st);
+// Factors the scenarios m with mask[m] == want.
 template <class T>
 void launch_dag_factor(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, const DagGrid &g,
-                       T *fronts, const uint8_t *mask, cudaStream_t st);
-template <class T>
-void launch_dag_fwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, const DagGrid &g,
-                    const T *fronts, cudaStream_t st);
-template <class T>
-void launch_dag_bwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, const DagGrid &g,
-                    const T *fronts, cudaStream_t st);
-
+                       T *fronts, const uint8_t *mask, int want, cudaStream_t st);
 // Split of the assembly tree for the triangular solves (gp_solve.cu).
-// Entries are the supernodes of all blocks, block by block, children before
-// parents; the last entry of a block is its root.
+// Blocks are subtrees solved by one warp each from shared memory; their
+// entries are the block's supernodes, children before parents, the last
+// entry of a block being its root:
 //   ent0 = {supernode, first column, pivots ns, update rows r}
-//   ent1 = {factor-slice offset, vector offset, map offset, pivot offset}
+//   ent1 = {-, vector offset, map offset, pivot offset}
 // (offsets within the block's shared-memory staging area; map offsets
-// relative to the block's first map entry).
+// relative to the block's first map entry).  The supernodes above the blocks
+// form the top region, solved by a dataflow kernel.
 struct DevBlk {
     int nblk;
-    int max_n, max_l, max_v, max_p, max_map, max_ext;   // per-block maxima
+    int max_n, max_v, max_p, max_map;   // per-block maxima
     const int *blk_ptr;          // [nblk+1]
     const int4 *ent0, *ent1;
     const int *map_ptr;          // [nblk+1]
@@ -164,19 +168,33 @@ struct DevBlk {
     const int *map_bwd;          // per update row: vector position of that row's solution
     const int *ext_ptr;          // [nblk+1]
     const int *ext_pos, *ext_row;   // solution entries above the block: vector position, xperm row
-    int n_top_levels, top_max_front;
-    const int *top_ptr;          // [n_top_levels+1]
-    const int *top_sups;
+    int n_top, top_max_front;
+    const int *top_order;        // [n_top] top supernodes, children before parents
+    const int *top_rank;         // [nsup] position in top_order, -1 inside a block
 };
 
-int solve_configure(const DevBlk &B);
-int solve_block_bytes(const DevBlk &B, int fp32);
-template <class T>
-void launch_solve_fwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B, const T *fronts,
-                      cudaStream_t st);
-template <class T>
-void launch_solve_bwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B, const T *fronts,
-                      cudaStream_t st);
+// Factors of the triangular solves, per scenario: FP64 when f32 is null or
+// the scenario's mode is MX_EXACT, else FP32.  With fused64 set, the forward
+// solve skips the FP64 scenarios (their factorisation did it).
+struct FrontSel {
+    const float *f32;
+    const double *f64;
+    const uint8_t *mode;
+    int fused64;
+};
+
+struct SolveGrid {
+    int blk_bytes = 0, top_bytes = 0;   // dynamic shared memory per CTA
+    int top_fwd = 0, top_bwd = 0;       // resident CTAs of the dataflow kernels
+};
+
+int solve_configure(const DevBlk &B, SolveGrid &g);
+void launch_solve_fwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B, const DevDag &D,
+                      const SolveGrid &g, FrontSel fs, cudaStream_t st);
+void launch_solve_bwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B, const DevDag &D,
+                      const SolveGrid &g, FrontSel fs, cudaStream_t st);
+// Largest front the solves' register path handles in a block (rows).
+int solve_block_front_limit();
 
 // launches (gp_kernels.cu)
 void launch_cluster(const DevProblem &P, const DevWork &W, const DevClu &C, const DevMixed &Mx, int want_f,

@@ -96,15 +96,17 @@ __device__ __forceinline__ void eval_cluster(const DevProblem &P, int c, const d
     if (P.cl_pss[c] >= 0) ieeest_eval(devref(P.dev[5], P.cl_pss[c]), z, p, sink);
 }
 
-// Modes per scenario: 0 exact Newton (Jacobian block, FP64 LU, three solves);
-// 1 the same, and the LU values and coupling rows are kept in FP32 for the
-// following iterations; 2 residual only, solved with the kept FP32 LU (the
-// kept A^-1 B columns and C A^-1 B terms stay as they are).
+// Modes per scenario: 0 exact Newton (Jacobian block, FP64 LU, three solves;
+// also the mixed solver's MX_EXACT); 1 the same, and the LU values and
+// coupling rows are kept in FP32 for the following iterations (MX_FP32);
+// 2 residual only, solved with the kept FP32 LU (MX_KEEP: the kept A^-1 B
+// columns and C A^-1 B terms stay as they are).
 __global__ void __launch_bounds__(32) cluster_kernel(DevProblem P, DevWork W, DevClu Cl, DevMixed Mx, int want_f) {
     extern __shared__ double vals[];
     const int task = blockIdx.x, m = blockIdx.y, lane = threadIdx.x;
     if (!W.active[m]) return;
-    const int mode = Mx.on ? (Mx.refac[m] ? 1 : 2) : 0;
+    const int r = Mx.on ? Mx.refac[m] : MX_EXACT;
+    const int mode = r == MX_KEEP ? 2 : (r == MX_FP32 ? 1 : 0);
     const int cls = Cl.task_class[task];
     const int cnt = Cl.task_count[task];
     const bool act = lane < cnt;
@@ -427,7 +429,7 @@ void launch_network(const DevProblem &P, const DevWork &W, int want_f, cudaStrea
 // ---------------------------------------------------------------------------
 
 // Start of a Newton iteration: clears the residual norms and the counters;
-// the mixed solver takes the refresh decisions made at the previous check.
+// the mixed solver takes the modes decided at the previous check.
 __global__ void reset_norm_kernel(DevWork W, DevMixed Mx, int M) {
     int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m < M) {
@@ -435,13 +437,14 @@ __global__ void reset_norm_kernel(DevWork W, DevMixed Mx, int M) {
         if (Mx.on) {
             const uint8_t r = Mx.refac_next[m];
             Mx.refac[m] = r;
-            Mx.refac_next[m] = 0;
-            if (r) Mx.age[m] = 0;
+            Mx.refac_next[m] = MX_KEEP;
+            if (r == MX_FP32) Mx.age[m] = 0;
         }
     }
     if (m == 0) {
         W.flag[0] = 0;
         W.flag[1] = 0;
+        W.flag[2] = 0;
     }
 }
 
@@ -455,7 +458,7 @@ void launch_reset_norm(const DevProblem &P, const DevWork &W, const DevMixed &Mx
 __global__ void mixed_start_kernel(DevWork W, DevMixed Mx, int M, int force) {
     int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M || !W.active[m]) return;
-    if (force || Mx.age[m] >= Mx.max_age) Mx.refac_next[m] = 1;
+    if (force || Mx.age[m] >= Mx.max_age) Mx.refac_next[m] = MX_FP32;
     Mx.age[m] += 1;
 }
 
@@ -464,10 +467,16 @@ void launch_mixed_start(const DevProblem &P, const DevWork &W, const DevMixed &M
 }
 
 // Convergence test (infinity norm of the FP64 residual), the itermax and
-// non-finite checks, and for the mixed solver the refresh decision: a
-// residual that fell by less than rho_max in the last iteration with kept
-// factors refreshes them at the next one, and after exact_after iterations
-// of one solve every iteration refreshes them.
+// non-finite checks, and for the mixed solver the mode of the next
+// iteration, from the contraction of the step just taken (prev_mode: the
+// factors it used):
+//  - a step with kept factors that reduced the residual by less than the
+//    factor rho_max refreshes them;
+//  - a step with freshly refreshed FP32 factors that did not halve the
+//    residual means FP32 factors are too coarse for this scenario now: it
+//    takes exact Newton steps (fresh FP64 factors) until the solve ends;
+//  - so does every scenario still iterating after exact_after iterations.
+// A scenario that went exact refreshes its kept factors at the next solve.
 __global__ void check_kernel(DevWork W, DevMixed Mx, int M, double tol, int itermax) {
     int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M || !W.active[m]) return;
@@ -483,11 +492,20 @@ __global__ void check_kernel(DevWork W, DevMixed Mx, int M, double tol, int iter
         W.status[m] |= 1;
     } else {
         if (Mx.on) {
-            if (W.iters[m] >= Mx.exact_after ||
-                (W.iters[m] > 0 && !Mx.refac[m] && nrm > Mx.rho_max * Mx.prev_norm[m]))
-                Mx.refac_next[m] = 1;
+            const int cur = Mx.refac[m], used = Mx.prev_mode[m];
+            const bool stepped = W.iters[m] > 0;
+            int next = MX_KEEP;
+            if (cur == MX_EXACT || W.iters[m] + 1 >= Mx.exact_after ||
+                (stepped && used == MX_FP32 && nrm > 0.5 * Mx.prev_norm[m]))
+                next = MX_EXACT;
+            else if (stepped && used == MX_KEEP && nrm > Mx.rho_max * Mx.prev_norm[m])
+                next = MX_FP32;
+            if (next == MX_EXACT) Mx.age[m] = Mx.max_age;
+            Mx.refac_next[m] = (uint8_t)next;
+            Mx.prev_mode[m] = (uint8_t)cur;
             Mx.prev_norm[m] = nrm;
-            if (Mx.refac[m]) atomicAdd(W.flag + 1, 1);
+            if (cur == MX_FP32) atomicAdd(W.flag + 1, 1);
+            else if (cur == MX_EXACT) atomicAdd(W.flag + 2, 1);
         }
         W.iters[m] += 1;
         atomicAdd(W.flag, 1);

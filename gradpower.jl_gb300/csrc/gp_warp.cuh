@@ -4,6 +4,48 @@
 
 namespace gp {
 
+constexpr unsigned kFullMask = 0xffffffffu;
+
+// ---- flags between tasks of one persistent kernel ----------------------
+// A task signals completion by storing the current epoch (release); a
+// waiting task polls with relaxed loads and acquires on success.  Every wait
+// is bounded: after kWaitLimit polls it raises the error flag and gives up,
+// and every other wait then returns at once, so the kernel always ends.
+
+constexpr int kWaitLimit = 1 << 20;
+
+__device__ __forceinline__ int ld_relaxed(const int *p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void fence_acquire() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
+__device__ __forceinline__ void st_release(int *p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Waits until *flag == epoch; false when it gave up (error flag raised here
+// or by another task).
+__device__ inline bool wait_epoch(const int *flag, int epoch, int *err) {
+    for (int it = 0; it < kWaitLimit; ++it) {
+        if (ld_relaxed(flag) == epoch) {
+            fence_acquire();
+            return true;
+        }
+        if (*(volatile int *)err) return false;
+        __nanosleep(64);
+    }
+    atomicExch(err, 1);
+    return false;
+}
+
+__device__ __forceinline__ void signal_done(int *flag, int epoch) {
+    __threadfence();
+    st_release(flag, epoch);
+}
+
 // Next power of two >= n, for 1 <= n <= 32.
 __device__ __forceinline__ int np2(int n) { return n <= 1 ? 1 : 1 << (32 - __clz(n - 1)); }
 

@@ -206,16 +206,20 @@ int32_t gp_residual(gp_layout *L, const double *zold, double dt, int32_t n_fault
  * factorisation (all levels), out[4] triangular solves, out[5] Newton
  * iterations summed over steps (max over scenarios), out[6] kernel launches,
  * out[7] update kernel, out[8] factorisation launches, out[9] linear
- * solves (batched over scenarios), out[10] mixed solver: scenario factor
- * refreshes; out[11..15] zero. */
+ * solves (batched over scenarios), out[10] mixed solver: scenario FP32
+ * factor refreshes, out[11] mixed solver: scenario iterations solved with
+ * fresh FP64 factors; out[12..15] zero. */
 int32_t gp_last_timing(const gp_layout *L, double out[16]);
 
 /* Refresh policy of GP_SOLVER_SCHUR_MIXED (no counterpart in the reference,
  * whose solvers refactor every iteration): a scenario refreshes its kept
- * factors at the start of a solve once they have served max_age solves,
- * after an iteration that reduced the residual by less than the factor
- * rho_max, and at every iteration once a solve has taken exact_after
- * iterations.  Defaults: max_age 1, rho_max 0.1, exact_after 8. */
+ * FP32 factors at the start of a solve once they have served max_age
+ * solves, and after an iteration that reduced the residual by less than the
+ * factor rho_max.  A scenario still iterating after exact_after iterations
+ * of one solve takes exact Newton steps with fresh FP64 factors until that
+ * solve ends (its kept factors are refreshed at the next solve), so that a
+ * system too ill-conditioned for FP32 factors converges as in
+ * GP_SOLVER_SCHUR_FP64.  Defaults: max_age 1, rho_max 0.1, exact_after 8. */
 int32_t gp_set_mixed_policy(gp_layout *L, int32_t max_age, double rho_max, int32_t exact_after);
 
 /* gp_residual with no fault applied, computed without allocating anything:
