@@ -137,6 +137,7 @@ struct gp_layout {
     int solve_graph_launches = 0, mix_launches[4] = {}, mix_factor_launches[4] = {};
     double refreshes = 0.0;                   // mixed: scenario FP32 factor refreshes in the last call
     double exact_iters = 0.0;                 // mixed: scenario iterations with FP64 factors
+    double retries = 0.0;                     // mixed: scenario solves redone exactly
     int mx_max_age = 1, mx_exact_after = 8;   // mixed solver policy (gp_set_mixed_policy)
     double mx_rho_max = 0.1;
 };
@@ -797,7 +798,9 @@ void build_blocks(gp_layout *L, const gp::Symbolic &sym) {
     B.top_order = A.upload(H.top_order);
     B.top_rank = A.upload(H.top_rank);
     L->n_top_levels = H.n_top_levels;
-    if (gp::solve_configure(B, L->SG) != 0) fail(GP_E_CUDA, "could not configure the solve kernels");
+    const int sc = gp::solve_configure(B, L->SG);
+    if (sc == -2) fail(GP_E_INVALID, "front of %d rows exceeds the solve kernels' staging area", B.top_max_front);
+    if (sc != 0) fail(GP_E_CUDA, "could not configure the solve kernels");
 }
 
 void build_problem(gp_layout *L, const gp_problem *pr) {
@@ -927,7 +930,7 @@ void build_work(gp_layout *L, const double *z0, const double *u0, const double *
     W.active = A.alloc<uint8_t>(M);
     W.iters = A.alloc<int>(M);
     W.status = A.alloc<int>(M);
-    W.flag = A.alloc<int>(3);
+    W.flag = A.alloc<int>(4);
     W.dt = A.alloc<double>(1);
     DevSym &S = L->S;
     S.fronts = A.alloc<double>(M * S.front_total);
@@ -957,7 +960,7 @@ void build_work(gp_layout *L, const double *z0, const double *u0, const double *
     ck(cudaMemset(D.xdone, 0, M * D.nsup * sizeof(int)), "memset");
     ck(cudaMemset(D.bdone, 0, M * D.nsup * sizeof(int)), "memset");
     ck(cudaMemset(W.status, 0, M * sizeof(int)), "memset");
-    ck(cudaMallocHost(&L->h_flag, 3 * sizeof(int)), "cudaMallocHost");
+    ck(cudaMallocHost(&L->h_flag, 4 * sizeof(int)), "cudaMallocHost");
     ck(cudaMallocHost(&L->h_dt, sizeof(double)), "cudaMallocHost");
     ck(cudaStreamCreateWithFlags(&L->st, cudaStreamNonBlocking), "stream");
     for (int i = 0; i < 8; i++) ck(cudaEventCreate(&L->pev[i]), "event");
@@ -1114,7 +1117,7 @@ void enqueue_eval(gp_layout *L, double tol, int itermax) {
     gp::launch_network(L->P, L->W, 0, L->st);
     mark(L, 2);
     gp::launch_check(L->P, L->W, L->Mx, tol, itermax, L->st);
-    ck(cudaMemcpyAsync(L->h_flag, L->W.flag, 3 * sizeof(int), cudaMemcpyDeviceToHost, L->st), "flag copy");
+    ck(cudaMemcpyAsync(L->h_flag, L->W.flag, 4 * sizeof(int), cudaMemcpyDeviceToHost, L->st), "flag copy");
 }
 
 template <class F>
@@ -1145,6 +1148,8 @@ void ensure_mixed(gp_layout *L) {
     X.refac_next = A.alloc<uint8_t>(M);
     X.prev_mode = A.alloc<uint8_t>(M);
     X.age = A.alloc<int>(M);
+    X.all_exact = A.alloc<uint8_t>(M);
+    X.retry = A.alloc<uint8_t>(M);
     X.prev_norm = A.alloc<double>(M);
     X.lu = A.alloc<float>(M * std::max(1, L->C.n_tasks) * n_lu * 32);
     X.cc = A.alloc<float>(M * std::max(1, L->P.n_cl) * 6);
@@ -1153,6 +1158,8 @@ void ensure_mixed(gp_layout *L) {
     ck(cudaMemset(X.refac_next, 0, M), "memset");
     ck(cudaMemset(X.prev_mode, 0, M), "memset");
     ck(cudaMemset(X.age, 0, M * sizeof(int)), "memset");
+    ck(cudaMemset(X.all_exact, 0, M), "memset");
+    ck(cudaMemset(X.retry, 0, M), "memset");
     // kept factors start at zero (zero pivot reciprocals give a zero step,
     // which the contraction test turns into a refresh)
     ck(cudaMemset(X.lu, 0, M * std::max(1, L->C.n_tasks) * n_lu * 32 * sizeof(float)), "memset");
@@ -1195,10 +1202,10 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
     return ms;
 }
 
-void newton(gp_layout *L, double dt, double tol, int itermax, bool force_refresh) {
+void newton(gp_layout *L, double dt, double tol, int itermax, bool force_refresh, bool reset_iters) {
     *L->h_dt = dt;
     ck(cudaMemcpyAsync(L->W.dt, L->h_dt, sizeof(double), cudaMemcpyHostToDevice, L->st), "dt");
-    ck(cudaMemsetAsync(L->W.iters, 0, L->M * sizeof(int), L->st), "memset");
+    if (reset_iters) ck(cudaMemsetAsync(L->W.iters, 0, L->M * sizeof(int), L->st), "memset");
     const bool mixed = L->Mx.on != 0;
     if (mixed) {
         gp::launch_mixed_start(L->P, L->W, L->Mx, force_refresh ? 1 : 0, L->st);
@@ -1235,6 +1242,23 @@ void newton(gp_layout *L, double dt, double tol, int itermax, bool force_refresh
         L->solves += 1;
     }
     fail(GP_E_NUMERIC, "Newton loop did not terminate");
+}
+
+// One Newton solve of every scenario.  With the mixed solver, scenarios
+// whose solve failed with inexact steps redo it from the step's starting
+// point with exact Newton steps (retry_start_kernel), so that the mixed
+// solver converges wherever the FP64 one does.
+void solve_step(gp_layout *L, double dt, double tol, int itermax, bool force_refresh) {
+    ck(cudaMemsetAsync(L->W.flag + 3, 0, sizeof(int), L->st), "memset");
+    newton(L, dt, tol, itermax, force_refresh, true);
+    if (L->Mx.on && L->h_flag[3] > 0) {
+        L->retries += L->h_flag[3];
+        gp::launch_retry_start(L->P, L->W, L->Mx, L->st);
+        L->launches += 1;
+        newton(L, dt, tol, itermax, false, false);
+        ck(cudaMemsetAsync(L->Mx.retry, 0, L->M, L->st), "memset");
+        ck(cudaMemsetAsync(L->Mx.all_exact, 0, L->M, L->st), "memset");
+    }
 }
 
 }  // namespace
@@ -1415,6 +1439,7 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
     L->solves = 0;
     L->refreshes = 0;
     L->exact_iters = 0;
+    L->retries = 0;
     for (int i = 0; i < 8; i++) L->ph_ms[i] = 0.0;
     ck(cudaMemsetAsync(L->D.err, 0, sizeof(int), L->st), "memset");
     // the mixed solver refreshes its kept factors at the first solve and
@@ -1424,7 +1449,7 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
         ck(cudaMemcpyAsync(L->W.zold, L->W.z, (size_t)M * nsys * sizeof(double), cudaMemcpyDeviceToDevice, L->st),
            "zold");
         ck(cudaMemsetAsync(L->W.active, 1, M, L->st), "memset");
-        newton(L, opt->dt, opt->newton_tol, opt->itermax, force);
+        solve_step(L, opt->dt, opt->newton_tol, opt->itermax, force);
         force = false;
         ck(cudaMemcpyAsync(d_iters + (size_t)(2 * (k - 1)) * M, L->W.iters, M * sizeof(int),
                            cudaMemcpyDeviceToDevice, L->st),
@@ -1440,7 +1465,7 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
             ck(cudaMemcpyAsync(L->W.zold, L->W.z, (size_t)M * nsys * sizeof(double), cudaMemcpyDeviceToDevice,
                                L->st),
                "zold");
-            newton(L, 0.0, opt->newton_tol, opt->itermax, true);
+            solve_step(L, 0.0, opt->newton_tol, opt->itermax, true);
             force = true;
             ck(cudaMemcpyAsync(d_iters + (size_t)(2 * (k - 1) + 1) * M, L->W.iters, M * sizeof(int),
                                cudaMemcpyDeviceToDevice, L->st),
@@ -1601,6 +1626,7 @@ int32_t gp_last_timing(const gp_layout *L, double out[16]) {
     out[9] = L->solves;
     out[10] = L->refreshes;
     out[11] = L->exact_iters;
+    out[12] = L->retries;
     API_END
 }
 
@@ -1673,7 +1699,7 @@ extern "C" int32_t gp_residual_static(gp_layout *L, const double *zold, double d
     W.xperm = cv.take<double>(M * std::max(1, P.n_red));
     W.norm = cv.take<unsigned long long>(M);
     W.active = cv.take<uint8_t>(M);
-    W.flag = cv.take<int>(3);
+    W.flag = cv.take<int>(4);
     W.dt = cv.take<double>(1);
     int *fl_ptr = cv.take<int>(M + 1);
     // no fault applied: every scenario's fault range is empty

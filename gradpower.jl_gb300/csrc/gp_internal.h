@@ -54,7 +54,8 @@ struct DevWork {
     uint8_t *active;                // [M] scenario takes part in this iteration
     int *iters;                     // [M] Newton updates in the current solve
     int *status;                    // [M] 0 ok, 1 itermax reached, 2 non-finite, 4 zero pivot
-    int *flag;                      // [3] scenarios still iterating; of those, MX_FP32 and MX_EXACT ones
+    int *flag;                      // [4] scenarios still iterating; of those, MX_FP32 and MX_EXACT ones;
+                                    //     [3] mixed solver: solves to retry (kept across iterations)
     double *dt;                     // [1] time step of the current solve
 };
 
@@ -113,6 +114,8 @@ struct DevMixed {
     uint8_t *refac_next;   // [M] mode of the next iteration
     uint8_t *prev_mode;    // [M] mode of the previous iteration (the step just taken)
     int *age;              // [M] Newton solves since the last refresh
+    uint8_t *all_exact;    // [M] every iteration of this solve is exact (a retry)
+    uint8_t *retry;        // [M] this solve failed with inexact steps: redo it exactly
     double *prev_norm;     // [M] residual norm of the previous iteration
     float *lu;             // [M][n_tasks][n_lu][32] cluster LU values and pivot reciprocals
     float *cc;             // [M][n_cl][6] coupling rows of the network equations
@@ -204,6 +207,7 @@ void launch_check(const DevProblem &P, const DevWork &W, const DevMixed &Mx, dou
                   cudaStream_t st);
 void launch_reset_norm(const DevProblem &P, const DevWork &W, const DevMixed &Mx, cudaStream_t st);
 void launch_mixed_start(const DevProblem &P, const DevWork &W, const DevMixed &Mx, int force, cudaStream_t st);
+void launch_retry_start(const DevProblem &P, const DevWork &W, const DevMixed &Mx, cudaStream_t st);
 void launch_update(const DevProblem &P, const DevWork &W, const DevSym &S, const int *perm, cudaStream_t st);
 void launch_events(const DevProblem &P, const DevWork &W, const int *fl_on_step, const int *fl_off_step,
                    const int *fl_scen, uint8_t *fl_on, int n_fl, int step, cudaStream_t st);

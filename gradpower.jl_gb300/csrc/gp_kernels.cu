@@ -454,12 +454,35 @@ void launch_reset_norm(const DevProblem &P, const DevWork &W, const DevMixed &Mx
 
 // Start of a Newton solve of the mixed solver: scenarios whose factors have
 // served max_age solves, or every scenario when `force` (first solve, event
-// re-solves and the solve after them), refresh them at the first iteration.
+// re-solves and the solve after them), refresh them at the first iteration;
+// a retried solve is exact from its first iteration.
 __global__ void mixed_start_kernel(DevWork W, DevMixed Mx, int M, int force) {
     int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M || !W.active[m]) return;
-    if (force || Mx.age[m] >= Mx.max_age) Mx.refac_next[m] = MX_FP32;
+    if (Mx.all_exact[m]) Mx.refac_next[m] = MX_EXACT;
+    else if (force || Mx.age[m] >= Mx.max_age) Mx.refac_next[m] = MX_FP32;
     Mx.age[m] += 1;
+}
+
+// Restart of the solves marked for a retry: the state goes back to the
+// step's starting point (zold), the scenario iterates again from zero
+// updates, exactly.  The retry marks are cleared by the host afterwards.
+__global__ void retry_start_kernel(DevProblem P, DevWork W, DevMixed Mx) {
+    const long long task = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (task >= (long long)P.M * P.n_sys) return;
+    const int m = (int)(task / P.n_sys), i = (int)(task % P.n_sys);
+    if (!Mx.retry[m]) return;
+    W.z[(size_t)m * P.n_sys + i] = W.zold[(size_t)m * P.n_sys + i];
+    if (i == 0) {
+        W.active[m] = 1;
+        W.iters[m] = 0;
+        Mx.all_exact[m] = 1;
+    }
+}
+
+void launch_retry_start(const DevProblem &P, const DevWork &W, const DevMixed &Mx, cudaStream_t st) {
+    const long long tasks = (long long)P.M * P.n_sys;
+    retry_start_kernel<<<(int)((tasks + 255) / 256), 256, 0, st>>>(P, W, Mx);
 }
 
 void launch_mixed_start(const DevProblem &P, const DevWork &W, const DevMixed &Mx, int force, cudaStream_t st) {
@@ -477,19 +500,25 @@ void launch_mixed_start(const DevProblem &P, const DevWork &W, const DevMixed &M
 //    takes exact Newton steps (fresh FP64 factors) until the solve ends;
 //  - so does every scenario still iterating after exact_after iterations.
 // A scenario that went exact refreshes its kept factors at the next solve.
+// A mixed solve that ends at itermax or on a non-finite residual with
+// inexact steps is not reported: it is marked for a retry from the step's
+// starting point with exact Newton steps, whose outcome is reported.
 __global__ void check_kernel(DevWork W, DevMixed Mx, int M, double tol, int itermax) {
     int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M || !W.active[m]) return;
     const unsigned long long bits = W.norm[m];
     const double nrm = __longlong_as_double((long long)bits);
+    const bool can_retry = Mx.on && !Mx.all_exact[m];
     if (nrm < tol) {
         W.active[m] = 0;
-    } else if (bits >= 0x7ff0000000000000ull) {
+    } else if (bits >= 0x7ff0000000000000ull || W.iters[m] >= itermax) {
         W.active[m] = 0;
-        W.status[m] |= 2;
-    } else if (W.iters[m] >= itermax) {
-        W.active[m] = 0;
-        W.status[m] |= 1;
+        if (can_retry) {
+            Mx.retry[m] = 1;
+            atomicAdd(W.flag + 3, 1);
+        } else {
+            W.status[m] |= bits >= 0x7ff0000000000000ull ? 2 : 1;
+        }
     } else {
         if (Mx.on) {
             const int cur = Mx.refac[m], used = Mx.prev_mode[m];

@@ -9,18 +9,20 @@
 //    before parents forward, parents before children backward.  Blocks are
 //    independent: no flags, no waits.  One launch per direction.
 //  - top: the supernodes above the blocks.  A persistent dataflow kernel
-//    whose warps claim (supernode, scenario) tasks in a topological order
-//    (children first forward, parents first backward) and wait, bounded, on
-//    the done flags of the tasks they depend on.  One launch per direction.
+//    whose CTAs claim (supernode, scenario) tasks in a topological order
+//    (children first forward, parents first backward).  A task copies the
+//    part of the front it needs into shared memory (cp.async, all threads)
+//    and loads its own right-hand-side entries before it waits, bounded, on
+//    the done flags of the tasks it depends on; one warp then sweeps the
+//    front from shared memory.  One launch per direction.
 // Forward: blocks, then top.  Backward: top, then blocks.
 //
 // Within a front, one warp holds up to kMaxJ rows per lane in registers
 // (row i in lane i % 32, register i / 32).  The unit-lower and upper
 // triangular parts are swept column by column, the pivot value broadcast by
-// a shuffle; the factor columns are loaded chunk by chunk ahead of the
-// arithmetic, so that the sweep waits on memory once per chunk rather than
-// once per column.  The U12 product of the backward solve is a row-dot
-// product spread over all lanes.
+// a shuffle; the factor columns are read chunk by chunk ahead of the
+// arithmetic.  The U12 product of the backward solve is a row-dot product
+// spread over all lanes.
 //
 // Front layout (column-major, leading dimension mm = ns + r): columns
 // 0..ns-1 hold L (unit lower, below the diagonal), U11 above it and the
@@ -43,10 +45,24 @@ namespace {
 
 constexpr unsigned FULL = kFullMask;
 constexpr int kBlkWarps = 4;   // block tasks per CTA
-constexpr int kTopWarps = 4;   // dataflow warps per CTA
+constexpr int kTopThreads = 128;             // threads of a top-region task
+constexpr int kTopStage = 64 * 1024;         // shared memory for a task's factor columns
 constexpr int kMaxJ = 8;       // register rows per lane: fronts up to 256 rows
+constexpr int kBlkFront = 64;  // largest front inside a block (two rows per lane)
 
 __host__ __device__ constexpr int align16(int b) { return (b + 15) & ~15; }
+
+// Shared memory of one top-region CTA: two vectors sized for double and one
+// int vector (top_max_front entries each), then the factor staging area.
+__host__ __device__ constexpr int top_vec_bytes(int tmf) { return align16(tmf * (8 + 8 + 4)); }
+
+__device__ __forceinline__ void cp_async(void *dst, const void *src, int bytes) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if (bytes == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 __device__ __forceinline__ bool use64(const FrontSel &fs, int m) {
     return fs.f32 == nullptr || (fs.mode != nullptr && fs.mode[m] == MX_EXACT);
@@ -79,18 +95,20 @@ __device__ __forceinline__ void place(T (&r)[J], int j, T v) {
         if (j == q) r[q] = v;
 }
 
-// Columns loaded per chunk: the chunk's loads stay in registers.
+// Columns read per chunk of a sweep.
 template <int J>
 struct Chunk {
-    static constexpr int value = J <= 1 ? 16 : (J <= 2 ? 8 : (J <= 4 ? 4 : 2));
+    static constexpr int value = J <= 2 ? 8 : (J <= 4 ? 4 : 2);
 };
 
-// ---- forward elimination of one front ------------------------------------
-// v[0..mm) (shared memory): the assembled right-hand side of the front.
-// On return v[0..ns) holds the forward-solved pivot entries and v[ns..mm)
-// the update vector for the parent.
+// ---- forward elimination -------------------------------------------------
+// Sweeps columns k in [k0, k1) of the unit-lower factor over rows (k, mm):
+// v[i] -= L(i, k) v[k], with L(i, k) = F[i + (k - kbase) * ld].  v[0..mm)
+// is in shared memory; rows below ns are first gathered through the pivot
+// permutation perm (identity after the first chunk).
 template <class T, int J, class Perm>
-__device__ void fwd_front_j(const T *__restrict__ F, Perm perm, int ns, int mm, T *v) {
+__device__ void fwd_cols_j(const T *__restrict__ F, int ld, int kbase, int k0, int k1, int ns, int mm, T *v,
+                           Perm perm) {
     const int lane = threadIdx.x & 31;
     T r[J];
 #pragma unroll
@@ -99,21 +117,21 @@ __device__ void fwd_front_j(const T *__restrict__ F, Perm perm, int ns, int mm, 
         r[j] = i < ns ? v[perm(i)] : (i < mm ? v[i] : T(0));
     }
     constexpr int CH = Chunk<J>::value;
-    for (int k0 = 0; k0 < ns; k0 += CH) {
+    for (int kc = k0; kc < k1; kc += CH) {
         T c[CH][J];
 #pragma unroll
         for (int kk = 0; kk < CH; kk++) {
-            const int k = k0 + kk;
+            const int k = kc + kk;
 #pragma unroll
             for (int j = 0; j < J; j++) {
                 const int i = lane + 32 * j;
-                c[kk][j] = (k < ns && i > k && i < mm) ? F[i + k * mm] : T(0);
+                c[kk][j] = (k < k1 && i > k && i < mm) ? F[i + (k - kbase) * ld] : T(0);
             }
         }
 #pragma unroll
         for (int kk = 0; kk < CH; kk++) {
-            const int k = k0 + kk;
-            if (k < ns) {
+            const int k = kc + kk;
+            if (k < k1) {
                 const T vk = __shfl_sync(FULL, pick(r, k >> 5), k & 31);
 #pragma unroll
                 for (int j = 0; j < J; j++) r[j] -= c[kk][j] * vk;
@@ -129,51 +147,73 @@ __device__ void fwd_front_j(const T *__restrict__ F, Perm perm, int ns, int mm, 
     __syncwarp();
 }
 
-// Fronts beyond the register path: the same steps on shared memory (sc: a
-// scratch vector of ns entries).
+// Fronts beyond the register path: the same sweep on shared memory, the
+// permutation gathered through sc.
 template <class T, class Perm>
-__device__ void fwd_front_smem(const T *__restrict__ F, Perm perm, int ns, int mm, T *v, T *sc) {
+__device__ void fwd_cols_smem(const T *__restrict__ F, int ld, int kbase, int k0, int k1, int ns, int mm, T *v,
+                              T *sc, Perm perm, bool gather) {
     const int lane = threadIdx.x & 31;
-    for (int i = lane; i < ns; i += 32) sc[i] = v[perm(i)];
-    __syncwarp();
-    for (int i = lane; i < ns; i += 32) v[i] = sc[i];
-    __syncwarp();
-    for (int k = 0; k < ns; k++) {
+    if (gather) {
+        for (int i = lane; i < ns; i += 32) sc[i] = v[perm(i)];
+        __syncwarp();
+        for (int i = lane; i < ns; i += 32) v[i] = sc[i];
+        __syncwarp();
+    }
+    for (int k = k0; k < k1; k++) {
         const T vk = v[k];
-        for (int i = k + 1 + lane; i < mm; i += 32) v[i] -= F[i + k * mm] * vk;
+        for (int i = k + 1 + lane; i < mm; i += 32) v[i] -= F[i + (k - kbase) * ld] * vk;
         __syncwarp();
     }
 }
 
+struct Ident {
+    __device__ int operator()(int i) const { return i; }
+};
+
 template <class T, class Perm>
-__device__ void fwd_front(const T *F, Perm perm, int ns, int mm, T *v, T *sc) {
+__device__ void fwd_cols(const T *F, int ld, int kbase, int k0, int k1, int ns, int mm, T *v, T *sc, Perm perm,
+                         bool gather) {
+    if (!gather) {
+        switch ((mm + 31) >> 5) {
+        case 1: fwd_cols_j<T, 1>(F, ld, kbase, k0, k1, ns, mm, v, Ident{}); return;
+        case 2: fwd_cols_j<T, 2>(F, ld, kbase, k0, k1, ns, mm, v, Ident{}); return;
+        case 3: fwd_cols_j<T, 3>(F, ld, kbase, k0, k1, ns, mm, v, Ident{}); return;
+        case 4: fwd_cols_j<T, 4>(F, ld, kbase, k0, k1, ns, mm, v, Ident{}); return;
+        case 5: fwd_cols_j<T, 5>(F, ld, kbase, k0, k1, ns, mm, v, Ident{}); return;
+        case 6: fwd_cols_j<T, 6>(F, ld, kbase, k0, k1, ns, mm, v, Ident{}); return;
+        case 7: fwd_cols_j<T, 7>(F, ld, kbase, k0, k1, ns, mm, v, Ident{}); return;
+        case 8: fwd_cols_j<T, 8>(F, ld, kbase, k0, k1, ns, mm, v, Ident{}); return;
+        default: fwd_cols_smem<T>(F, ld, kbase, k0, k1, ns, mm, v, sc, Ident{}, false); return;
+        }
+    }
     switch ((mm + 31) >> 5) {
-    case 1: fwd_front_j<T, 1>(F, perm, ns, mm, v); break;
-    case 2: fwd_front_j<T, 2>(F, perm, ns, mm, v); break;
-    case 3: fwd_front_j<T, 3>(F, perm, ns, mm, v); break;
-    case 4: fwd_front_j<T, 4>(F, perm, ns, mm, v); break;
-    case 5: fwd_front_j<T, 5>(F, perm, ns, mm, v); break;
-    case 6: fwd_front_j<T, 6>(F, perm, ns, mm, v); break;
-    case 7: fwd_front_j<T, 7>(F, perm, ns, mm, v); break;
-    case 8: fwd_front_j<T, 8>(F, perm, ns, mm, v); break;
-    default: fwd_front_smem<T>(F, perm, ns, mm, v, sc); break;
+    case 1: fwd_cols_j<T, 1>(F, ld, kbase, k0, k1, ns, mm, v, perm); return;
+    case 2: fwd_cols_j<T, 2>(F, ld, kbase, k0, k1, ns, mm, v, perm); return;
+    case 3: fwd_cols_j<T, 3>(F, ld, kbase, k0, k1, ns, mm, v, perm); return;
+    case 4: fwd_cols_j<T, 4>(F, ld, kbase, k0, k1, ns, mm, v, perm); return;
+    case 5: fwd_cols_j<T, 5>(F, ld, kbase, k0, k1, ns, mm, v, perm); return;
+    case 6: fwd_cols_j<T, 6>(F, ld, kbase, k0, k1, ns, mm, v, perm); return;
+    case 7: fwd_cols_j<T, 7>(F, ld, kbase, k0, k1, ns, mm, v, perm); return;
+    case 8: fwd_cols_j<T, 8>(F, ld, kbase, k0, k1, ns, mm, v, perm); return;
+    default: fwd_cols_smem<T>(F, ld, kbase, k0, k1, ns, mm, v, sc, perm, true); return;
     }
 }
 
-// ---- backward substitution of one front ----------------------------------
-// v[0..ns): forward-solved pivot entries; v[ns..mm): the solution entries of
-// the update rows.  On return v[0..ns) holds the solution of the pivot rows.
+// ---- backward substitution -----------------------------------------------
+// U12 columns c in [c0, c1) (front columns, ns <= c < mm):
+// v[i] -= U(i, c) v[c] for i < ns, U(i, c) = F[i + (c - cbase) * ld].
 template <class T>
-__device__ __forceinline__ void bwd_u12(const T *__restrict__ F, int ns, int mm, T *v) {
-    warp_row_dots<T>(F + ns * mm, 1, mm, ns, mm - ns, [&](int a) { return v[ns + a]; },
+__device__ __forceinline__ void bwd_u12(const T *__restrict__ F, int ld, int cbase, int c0, int c1, int ns, T *v) {
+    warp_row_dots<T>(F + (c0 - cbase) * ld, 1, ld, ns, c1 - c0, [&](int a) { return v[c0 + a]; },
                      [&](int i, T acc) { v[i] -= acc; });
     __syncwarp();
 }
 
+// U11 columns k from k1 - 1 down to k0: v[k] *= U(k, k) (the stored
+// reciprocal pivot), then v[i] -= U(i, k) v[k] for i < k.
 template <class T, int J>
-__device__ void bwd_front_j(const T *__restrict__ F, int ns, int mm, T *v) {
+__device__ void bwd_cols_j(const T *__restrict__ F, int ld, int kbase, int k0, int k1, int ns, T *v) {
     const int lane = threadIdx.x & 31;
-    bwd_u12<T>(F, ns, mm, v);
     T r[J];
 #pragma unroll
     for (int j = 0; j < J; j++) {
@@ -181,23 +221,23 @@ __device__ void bwd_front_j(const T *__restrict__ F, int ns, int mm, T *v) {
         r[j] = i < ns ? v[i] : T(0);
     }
     constexpr int CH = Chunk<J>::value;
-    for (int k1 = ns - 1; k1 >= 0; k1 -= CH) {
+    for (int kc = k1 - 1; kc >= k0; kc -= CH) {
         T c[CH][J], d[CH];
 #pragma unroll
         for (int kk = 0; kk < CH; kk++) {
-            const int k = k1 - kk;
-            d[kk] = k >= 0 ? F[k + k * mm] : T(0);
+            const int k = kc - kk;
+            d[kk] = k >= k0 ? F[k + (k - kbase) * ld] : T(0);
 #pragma unroll
             for (int j = 0; j < J; j++) {
                 const int i = lane + 32 * j;
-                c[kk][j] = (k >= 0 && i < k) ? F[i + k * mm] : T(0);
+                c[kk][j] = (k >= k0 && i < k) ? F[i + (k - kbase) * ld] : T(0);
             }
         }
 #pragma unroll
         for (int kk = 0; kk < CH; kk++) {
-            const int k = k1 - kk;
-            if (k >= 0) {
-                const T tk = __shfl_sync(FULL, pick(r, k >> 5), k & 31) * d[kk];   // reciprocal pivot
+            const int k = kc - kk;
+            if (k >= k0) {
+                const T tk = __shfl_sync(FULL, pick(r, k >> 5), k & 31) * d[kk];
                 if (lane == (k & 31)) place(r, k >> 5, tk);
 #pragma unroll
                 for (int j = 0; j < J; j++) r[j] -= c[kk][j] * tk;
@@ -213,31 +253,44 @@ __device__ void bwd_front_j(const T *__restrict__ F, int ns, int mm, T *v) {
 }
 
 template <class T>
-__device__ void bwd_front_smem(const T *__restrict__ F, int ns, int mm, T *v) {
+__device__ void bwd_cols_smem(const T *__restrict__ F, int ld, int kbase, int k0, int k1, T *v) {
     const int lane = threadIdx.x & 31;
-    bwd_u12<T>(F, ns, mm, v);
-    for (int k = ns - 1; k >= 0; k--) {
-        const T tk = v[k] * F[k + k * mm];
+    for (int k = k1 - 1; k >= k0; k--) {
+        const T tk = v[k] * F[k + (k - kbase) * ld];
         __syncwarp();
         if (lane == 0) v[k] = tk;
-        for (int i = lane; i < k; i += 32) v[i] -= F[i + k * mm] * tk;
+        for (int i = lane; i < k; i += 32) v[i] -= F[i + (k - kbase) * ld] * tk;
         __syncwarp();
     }
 }
 
 template <class T>
-__device__ void bwd_front(const T *F, int ns, int mm, T *v) {
-    switch ((mm + 31) >> 5) {
-    case 1: bwd_front_j<T, 1>(F, ns, mm, v); break;
-    case 2: bwd_front_j<T, 2>(F, ns, mm, v); break;
-    case 3: bwd_front_j<T, 3>(F, ns, mm, v); break;
-    case 4: bwd_front_j<T, 4>(F, ns, mm, v); break;
-    case 5: bwd_front_j<T, 5>(F, ns, mm, v); break;
-    case 6: bwd_front_j<T, 6>(F, ns, mm, v); break;
-    case 7: bwd_front_j<T, 7>(F, ns, mm, v); break;
-    case 8: bwd_front_j<T, 8>(F, ns, mm, v); break;
-    default: bwd_front_smem<T>(F, ns, mm, v); break;
+__device__ void bwd_cols(const T *F, int ld, int kbase, int k0, int k1, int ns, T *v) {
+    switch ((ns + 31) >> 5) {
+    case 1: bwd_cols_j<T, 1>(F, ld, kbase, k0, k1, ns, v); return;
+    case 2: bwd_cols_j<T, 2>(F, ld, kbase, k0, k1, ns, v); return;
+    case 3: bwd_cols_j<T, 3>(F, ld, kbase, k0, k1, ns, v); return;
+    case 4: bwd_cols_j<T, 4>(F, ld, kbase, k0, k1, ns, v); return;
+    case 5: bwd_cols_j<T, 5>(F, ld, kbase, k0, k1, ns, v); return;
+    case 6: bwd_cols_j<T, 6>(F, ld, kbase, k0, k1, ns, v); return;
+    case 7: bwd_cols_j<T, 7>(F, ld, kbase, k0, k1, ns, v); return;
+    case 8: bwd_cols_j<T, 8>(F, ld, kbase, k0, k1, ns, v); return;
+    default: bwd_cols_smem<T>(F, ld, kbase, k0, k1, v); return;
     }
+}
+
+// Block fronts (at most kBlkFront rows): the whole front from global memory.
+template <class T, class Perm>
+__device__ void fwd_front_blk(const T *F, Perm perm, int ns, int mm, T *v) {
+    if (mm <= 32) fwd_cols_j<T, 1>(F, mm, 0, 0, ns, ns, mm, v, perm);
+    else fwd_cols_j<T, 2>(F, mm, 0, 0, ns, ns, mm, v, perm);
+}
+
+template <class T>
+__device__ void bwd_front_blk(const T *F, int ns, int mm, T *v) {
+    bwd_u12<T>(F, mm, 0, ns, mm, ns, v);
+    if (ns <= 32) bwd_cols_j<T, 1>(F, mm, 0, 0, ns, ns, v);
+    else bwd_cols_j<T, 2>(F, mm, 0, 0, ns, ns, v);
 }
 
 // ---- blocks ----------------------------------------------------------------
@@ -317,7 +370,7 @@ __device__ void fwd_block(const DevProblem &P, const DevWork &W, const DevSym &S
         const int ns = a.z, r = a.w;
         T *v = vs + b.y;
         const int *pv = t.pv + b.w;
-        fwd_front<T>(fr + t.FO[q], [&](int i) { return pv[i]; }, ns, ns + r, v, v);
+        fwd_front_blk<T>(fr + t.FO[q], [&](int i) { return pv[i]; }, ns, ns + r, v);
         for (int i = lane; i < ns; i += 32) xo[a.y + i] = (double)v[i];
         if (q < t.n - 1) {
             const int *pm = t.mp + b.z;
@@ -368,7 +421,7 @@ __device__ void bwd_block(const DevProblem &P, const DevWork &W, const DevSym &S
         const int *gm = t.mp + b.z;
         for (int c = lane; c < r; c += 32) v[ns + c] = vs[gm[c]];
         __syncwarp();
-        bwd_front<T>(fr + t.FO[q], ns, ns + r, v);
+        bwd_front_blk<T>(fr + t.FO[q], ns, ns + r, v);
         for (int i = lane; i < ns; i += 32) x[a.y + i] = (double)v[i];
     }
 }
@@ -389,142 +442,210 @@ __global__ void __launch_bounds__(32 * kBlkWarps) bwd_blocks_kernel(DevProblem P
     else bwd_block<float>(P, W, S, B, fs, t, blk, m, reinterpret_cast<float *>(base + lay.v));
 }
 
-// ---- top region: dataflow ---------------------------------------------------
+// ---- top region: dataflow of CTA tasks ------------------------------------
+
+// All threads of the CTA copy columns [c0, c1) of rows [0, nrow) of the
+// front F (leading dimension mm) into Fs (leading dimension nrow).
+template <class T>
+__device__ void stage_cols(T *Fs, const T *F, int mm, int nrow, int c0, int c1) {
+    const int n = nrow * (c1 - c0);
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const int c = e / nrow, i = e - c * nrow;
+        cp_async(Fs + e, F + i + (size_t)(c0 + c) * mm, (int)sizeof(T));
+    }
+}
+
+struct TopCtx {
+    int s, m, start, ns, r, mm;
+};
+
+__device__ __forceinline__ TopCtx top_ctx(const DevSym &S, int s, int m) {
+    TopCtx c;
+    c.s = s;
+    c.m = m;
+    c.start = S.sup_start[s];
+    c.ns = S.sup_start[s + 1] - c.start;
+    c.r = S.row_ptr[s + 1] - S.row_ptr[s];
+    c.mm = c.ns + c.r;
+    return c;
+}
+
+// Waits (warp 0) on the done flags of the top-region children; false when
+// a wait gave up.  Ends with a CTA barrier.
+__device__ bool wait_top_children(const DevSym &S, const DevBlk &B, const DevDag &D, int s, int m, int M, int epoch,
+                                  int *s_ok) {
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        const int c0 = S.child_ptr[s], nc = S.child_ptr[s + 1] - c0;
+        bool ok = true;
+        for (int q = lane; q < nc; q += 32) {
+            const int c = S.children[c0 + q];
+            if (B.top_rank[c] >= 0) ok = wait_epoch(D.xdone + (size_t)c * M + m, epoch, D.err) && ok;
+        }
+        ok = __all_sync(FULL, ok);
+        if (lane == 0) *s_ok = ok;
+    }
+    __syncthreads();
+    return *s_ok != 0;
+}
+
+__device__ bool wait_top_parent(const DevDag &D, int s, int m, int M, int epoch, int *s_ok) {
+    const int par = D.parent[s];
+    if (threadIdx.x == 0) *s_ok = par < 0 ? 1 : (int)wait_epoch(D.bdone + (size_t)par * M + m, epoch, D.err);
+    __syncthreads();
+    return *s_ok != 0;
+}
 
 template <class T>
-__device__ void fwd_top_one(const DevProblem &P, const DevWork &W, const DevSym &S, const FrontSel &fs, int s,
-                            int m, T *v, T *sc) {
-    const int lane = threadIdx.x & 31;
-    const int start = S.sup_start[s];
-    const int ns = S.sup_start[s + 1] - start;
-    const int r = S.row_ptr[s + 1] - S.row_ptr[s];
-    const int mm = ns + r;
-    double *x = W.xperm + (size_t)m * P.n_red;
-    double *uv = S.uvec + (size_t)m * S.uvec_total;
-    for (int i = lane; i < mm; i += 32) v[i] = i < ns ? (T)x[start + i] : T(0);
-    __syncwarp();
-    for (int q = S.child_ptr[s]; q < S.child_ptr[s + 1]; q++) {
+__device__ void fwd_top_task(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B,
+                             const DevDag &D, const FrontSel &fs, const TopCtx &t, int epoch, unsigned char *smem,
+                             int *s_ok) {
+    const int tmf = B.top_max_front;
+    T *v = reinterpret_cast<T *>(smem);
+    T *sc = reinterpret_cast<T *>(smem + tmf * 8);
+    int *pi = reinterpret_cast<int *>(smem + tmf * 16);
+    T *Fs = reinterpret_cast<T *>(smem + top_vec_bytes(tmf));
+    const T *F = front_base<T>(fs) + (size_t)t.m * S.front_total + S.front_off[t.s];
+    const int cap = kTopStage / ((int)sizeof(T) * t.mm);   // columns per staged chunk
+    double *x = W.xperm + (size_t)t.m * P.n_red;
+    double *uv = S.uvec + (size_t)t.m * S.uvec_total;
+    const int *ip = S.ipiv + (size_t)t.m * S.n + t.start;
+    // independent of other tasks: own entries, pivot permutation, factor columns
+    for (int i = threadIdx.x; i < t.mm; i += blockDim.x) v[i] = i < t.ns ? (T)x[t.start + i] : T(0);
+    for (int i = threadIdx.x; i < t.ns; i += blockDim.x) pi[i] = ip[i];
+    int k1 = min(t.ns, cap);
+    stage_cols<T>(Fs, F, t.mm, t.mm, 0, k1);
+    if (!wait_top_children(S, B, D, t.s, t.m, P.M, epoch, s_ok) && threadIdx.x == 0) atomicOr(W.status + t.m, 8);
+    for (int q = S.child_ptr[t.s]; q < S.child_ptr[t.s + 1]; q++) {
         const int c = S.children[q];
         const int rc = S.row_ptr[c + 1] - S.row_ptr[c];
         const int *rel = S.relmap + S.relmap_ptr[c];
         const double *uc = uv + S.uvec_off[c];
-        for (int a = lane; a < rc; a += 32) v[rel[a]] += (T)__ldcg(uc + a);
-        __syncwarp();
+        for (int a = threadIdx.x; a < rc; a += blockDim.x) v[rel[a]] += (T)__ldcg(uc + a);
+        __syncthreads();
     }
-    const T *F = front_base<T>(fs) + (size_t)m * S.front_total + S.front_off[s];
-    const int *ip = S.ipiv + (size_t)m * S.n + start;
-    fwd_front<T>(F, [&](int i) { return ip[i]; }, ns, mm, v, sc);
-    for (int i = lane; i < ns; i += 32) x[start + i] = (double)v[i];
-    double *us = uv + S.uvec_off[s];
-    for (int i = lane; i < r; i += 32) us[i] = (double)v[ns + i];
-    __syncwarp();
+    int k0 = 0;
+    bool gather = true;
+    for (;;) {
+        cp_async_wait_all();
+        __syncthreads();
+        if (threadIdx.x < 32)
+            fwd_cols<T>(Fs, t.mm, k0, k0, k1, t.ns, t.mm, v, sc, [&](int i) { return pi[i]; }, gather);
+        __syncthreads();
+        gather = false;
+        if (k1 >= t.ns) break;
+        k0 = k1;
+        k1 = min(t.ns, k0 + cap);
+        stage_cols<T>(Fs, F, t.mm, t.mm, k0, k1);
+    }
+    for (int i = threadIdx.x; i < t.ns; i += blockDim.x) x[t.start + i] = (double)v[i];
+    double *us = uv + S.uvec_off[t.s];
+    for (int i = threadIdx.x; i < t.r; i += blockDim.x) us[i] = (double)v[t.ns + i];
 }
 
 template <class T>
-__device__ void bwd_top_one(const DevProblem &P, const DevWork &W, const DevSym &S, const FrontSel &fs, int s,
-                            int m, T *v) {
-    const int lane = threadIdx.x & 31;
-    const int start = S.sup_start[s];
-    const int ns = S.sup_start[s + 1] - start;
-    const int r = S.row_ptr[s + 1] - S.row_ptr[s];
-    const int mm = ns + r;
-    double *x = W.xperm + (size_t)m * P.n_red;
-    const int *rows = S.rows + S.row_ptr[s];
-    for (int i = lane; i < mm; i += 32) v[i] = (T)__ldcg(x + (i < ns ? start + i : rows[i - ns]));
-    __syncwarp();
-    const T *F = front_base<T>(fs) + (size_t)m * S.front_total + S.front_off[s];
-    bwd_front<T>(F, ns, mm, v);
-    for (int i = lane; i < ns; i += 32) x[start + i] = (double)v[i];
-    __syncwarp();
-}
-
-// One warp waits for the top-region children of supernode s (scenario m).
-__device__ bool wait_top_children(const DevSym &S, const DevBlk &B, const DevDag &D, int s, int m, int M,
-                                  int epoch) {
-    const int lane = threadIdx.x & 31;
-    const int c0 = S.child_ptr[s], nc = S.child_ptr[s + 1] - c0;
-    bool ok = true;
-    for (int q = lane; q < nc; q += 32) {
-        const int c = S.children[c0 + q];
-        if (B.top_rank[c] >= 0) ok = wait_epoch(D.xdone + (size_t)c * M + m, epoch, D.err) && ok;
+__device__ void bwd_top_task(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B,
+                             const DevDag &D, const FrontSel &fs, const TopCtx &t, int epoch, unsigned char *smem,
+                             int *s_ok) {
+    const int tmf = B.top_max_front;
+    T *v = reinterpret_cast<T *>(smem);
+    int *pi = reinterpret_cast<int *>(smem + tmf * 16);
+    T *Fs = reinterpret_cast<T *>(smem + top_vec_bytes(tmf));
+    const T *F = front_base<T>(fs) + (size_t)t.m * S.front_total + S.front_off[t.s];
+    const int cap = kTopStage / ((int)sizeof(T) * max(1, t.ns));   // columns per staged chunk
+    double *x = W.xperm + (size_t)t.m * P.n_red;
+    const int *rows = S.rows + S.row_ptr[t.s];
+    for (int i = threadIdx.x; i < t.ns; i += blockDim.x) v[i] = (T)x[t.start + i];
+    for (int a = threadIdx.x; a < t.r; a += blockDim.x) pi[a] = rows[a];
+    // chunks run over the front's columns from mm - 1 down to 0: U12 first,
+    // then U11 from the last pivot column
+    int c1 = t.mm, c0 = max(0, t.mm - cap);
+    stage_cols<T>(Fs, F, t.mm, t.ns, c0, c1);
+    if (!wait_top_parent(D, t.s, t.m, P.M, epoch, s_ok) && threadIdx.x == 0) atomicOr(W.status + t.m, 8);
+    for (int a = threadIdx.x; a < t.r; a += blockDim.x) v[t.ns + a] = (T)__ldcg(x + pi[a]);
+    for (;;) {
+        cp_async_wait_all();
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            const int u0 = max(c0, t.ns);
+            if (u0 < c1) bwd_u12<T>(Fs, t.ns, c0, u0, c1, t.ns, v);
+            if (c0 < t.ns) bwd_cols<T>(Fs, t.ns, c0, c0, min(c1, t.ns), t.ns, v);
+        }
+        __syncthreads();
+        if (c0 == 0) break;
+        c1 = c0;
+        c0 = max(0, c1 - cap);
+        stage_cols<T>(Fs, F, t.mm, t.ns, c0, c1);
     }
-    ok = __all_sync(FULL, ok);
-    __syncwarp();
-    return ok;
+    for (int i = threadIdx.x; i < t.ns; i += blockDim.x) x[t.start + i] = (double)v[i];
 }
 
-__global__ void __launch_bounds__(32 * kTopWarps) fwd_top_kernel(DevProblem P, DevWork W, DevSym S, DevBlk B,
-                                                                 DevDag D, FrontSel fs) {
+__global__ void __launch_bounds__(kTopThreads) fwd_top_kernel(DevProblem P, DevWork W, DevSym S, DevBlk B, DevDag D,
+                                                              FrontSel fs) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double *vb = reinterpret_cast<double *>(smem) + (size_t)warp * 2 * B.top_max_front;
+    __shared__ int s_task, s_ok;
     const int M = P.M;
     const int epoch = *D.epoch;
     const int n_tasks = B.n_top * M;
     for (;;) {
-        int t = 0;
-        if (lane == 0) t = atomicAdd(D.ctr + 2, 1);
-        t = __shfl_sync(FULL, t, 0);
+        __syncthreads();
+        if (threadIdx.x == 0) s_task = atomicAdd(D.ctr + 2, 1);
+        __syncthreads();
+        const int t = s_task;
         if (t >= n_tasks) break;
         const int s = B.top_order[t / M], m = t % M;
         if (!W.active[m]) continue;
         const bool d = use64(fs, m);
         if (d && fs.fused64) continue;
-        if (!wait_top_children(S, B, D, s, m, M, epoch) && lane == 0) atomicOr(W.status + m, 8);
-        if (d) fwd_top_one<double>(P, W, S, fs, s, m, vb, vb + B.top_max_front);
-        else {
-            float *vf = reinterpret_cast<float *>(vb);
-            fwd_top_one<float>(P, W, S, fs, s, m, vf, vf + B.top_max_front);
-        }
-        if (lane == 0) signal_done(D.xdone + (size_t)s * M + m, epoch);
+        const TopCtx c = top_ctx(S, s, m);
+        if (d) fwd_top_task<double>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
+        else fwd_top_task<float>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
+        __syncthreads();
+        if (threadIdx.x == 0) signal_done(D.xdone + (size_t)s * M + m, epoch);
     }
 }
 
-__global__ void __launch_bounds__(32 * kTopWarps) bwd_top_kernel(DevProblem P, DevWork W, DevSym S, DevBlk B,
-                                                                 DevDag D, FrontSel fs) {
+__global__ void __launch_bounds__(kTopThreads) bwd_top_kernel(DevProblem P, DevWork W, DevSym S, DevBlk B, DevDag D,
+                                                              FrontSel fs) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double *vb = reinterpret_cast<double *>(smem) + (size_t)warp * 2 * B.top_max_front;
+    __shared__ int s_task, s_ok;
     const int M = P.M;
     const int epoch = *D.epoch;
     const int n_tasks = B.n_top * M;
     for (;;) {
-        int t = 0;
-        if (lane == 0) t = atomicAdd(D.ctr + 3, 1);
-        t = __shfl_sync(FULL, t, 0);
+        __syncthreads();
+        if (threadIdx.x == 0) s_task = atomicAdd(D.ctr + 3, 1);
+        __syncthreads();
+        const int t = s_task;
         if (t >= n_tasks) break;
         const int s = B.top_order[B.n_top - 1 - t / M], m = t % M;
         if (!W.active[m]) continue;
-        const int par = D.parent[s];
-        if (par >= 0) {
-            bool ok = true;
-            if (lane == 0) ok = wait_epoch(D.bdone + (size_t)par * M + m, epoch, D.err);
-            ok = __shfl_sync(FULL, ok, 0);
-            __syncwarp();
-            if (!ok && lane == 0) atomicOr(W.status + m, 8);
-        }
-        if (use64(fs, m)) bwd_top_one<double>(P, W, S, fs, s, m, vb);
-        else bwd_top_one<float>(P, W, S, fs, s, m, reinterpret_cast<float *>(vb));
-        if (lane == 0) signal_done(D.bdone + (size_t)s * M + m, epoch);
+        const TopCtx c = top_ctx(S, s, m);
+        if (use64(fs, m)) bwd_top_task<double>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
+        else bwd_top_task<float>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
+        __syncthreads();
+        if (threadIdx.x == 0) signal_done(D.bdone + (size_t)s * M + m, epoch);
     }
 }
 
-int grid_for(int resident, long long warp_tasks, int per_block) {
-    const long long need = (warp_tasks + per_block - 1) / per_block;
+int grid_for(int resident, long long tasks, int per_block) {
+    const long long need = (tasks + per_block - 1) / per_block;
     return (int)std::max<long long>(1, std::min<long long>(need, resident));
 }
 
 }  // namespace
 
-int solve_block_front_limit() { return 32 * kMaxJ; }
+int solve_block_front_limit() { return kBlkFront; }
 
 int solve_configure(const DevBlk &B, SolveGrid &g) {
     int dev = 0, nsm = 0, occ = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return -1;
+    // a staged chunk holds at least one whole front column in FP64
+    if ((long)B.top_max_front * 8 > kTopStage) return -2;
     g.blk_bytes = kBlkWarps * blk_layout(B).total;
-    g.top_bytes = kTopWarps * 2 * std::max(1, B.top_max_front) * (int)sizeof(double);
+    g.top_bytes = top_vec_bytes(std::max(1, B.top_max_front)) + kTopStage;
     if (cudaFuncSetAttribute(fwd_blocks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, g.blk_bytes) !=
             cudaSuccess ||
         cudaFuncSetAttribute(bwd_blocks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, g.blk_bytes) !=
@@ -536,11 +657,11 @@ int solve_configure(const DevBlk &B, SolveGrid &g) {
         cudaGetLastError();
         return -1;
     }
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fwd_top_kernel, 32 * kTopWarps, g.top_bytes) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fwd_top_kernel, kTopThreads, g.top_bytes) !=
             cudaSuccess || occ < 1)
         return -1;
     g.top_fwd = nsm * occ;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bwd_top_kernel, 32 * kTopWarps, g.top_bytes) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bwd_top_kernel, kTopThreads, g.top_bytes) !=
             cudaSuccess || occ < 1)
         return -1;
     g.top_bwd = nsm * occ;
@@ -554,15 +675,13 @@ void launch_solve_fwd(const DevProblem &P, const DevWork &W, const DevSym &S, co
         fwd_blocks_kernel<<<(int)((tasks + kBlkWarps - 1) / kBlkWarps), 32 * kBlkWarps, g.blk_bytes, st>>>(P, W, S,
                                                                                                           B, fs);
     const long long top = (long long)B.n_top * P.M;
-    if (top > 0)
-        fwd_top_kernel<<<grid_for(g.top_fwd, top, kTopWarps), 32 * kTopWarps, g.top_bytes, st>>>(P, W, S, B, D, fs);
+    if (top > 0) fwd_top_kernel<<<grid_for(g.top_fwd, top, 1), kTopThreads, g.top_bytes, st>>>(P, W, S, B, D, fs);
 }
 
 void launch_solve_bwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B, const DevDag &D,
                       const SolveGrid &g, FrontSel fs, cudaStream_t st) {
     const long long top = (long long)B.n_top * P.M;
-    if (top > 0)
-        bwd_top_kernel<<<grid_for(g.top_bwd, top, kTopWarps), 32 * kTopWarps, g.top_bytes, st>>>(P, W, S, B, D, fs);
+    if (top > 0) bwd_top_kernel<<<grid_for(g.top_bwd, top, 1), kTopThreads, g.top_bytes, st>>>(P, W, S, B, D, fs);
     const long long tasks = (long long)B.nblk * P.M;
     if (tasks > 0)
         bwd_blocks_kernel<<<(int)((tasks + kBlkWarps - 1) / kBlkWarps), 32 * kBlkWarps, g.blk_bytes, st>>>(P, W, S,

@@ -138,7 +138,8 @@ class GpuBatchedLayout:
                     factor_ms=float(out[3]), solve_ms=float(out[4]), update_ms=float(out[7]),
                     newton_iters=float(out[5]), launches=float(out[6]),
                     factor_launches=float(out[8]), linear_solves=float(out[9]),
-                    refreshes=float(out[10]), exact_iters=float(out[11]))
+                    refreshes=float(out[10]), exact_iters=float(out[11]),
+                    retries=float(out[12]))
 
     def restore_initial_state(self):
         _check(library().gp_restore_initial_state(self._h))

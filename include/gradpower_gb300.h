@@ -208,7 +208,8 @@ int32_t gp_residual(gp_layout *L, const double *zold, double dt, int32_t n_fault
  * out[7] update kernel, out[8] factorisation launches, out[9] linear
  * solves (batched over scenarios), out[10] mixed solver: scenario FP32
  * factor refreshes, out[11] mixed solver: scenario iterations solved with
- * fresh FP64 factors; out[12..15] zero. */
+ * fresh FP64 factors, out[12] mixed solver: scenario solves redone with
+ * exact Newton steps after failing with inexact ones; out[13..15] zero. */
 int32_t gp_last_timing(const gp_layout *L, double out[16]);
 
 /* Refresh policy of GP_SOLVER_SCHUR_MIXED (no counterpart in the reference,
@@ -219,7 +220,10 @@ int32_t gp_last_timing(const gp_layout *L, double out[16]);
  * of one solve takes exact Newton steps with fresh FP64 factors until that
  * solve ends (its kept factors are refreshed at the next solve), so that a
  * system too ill-conditioned for FP32 factors converges as in
- * GP_SOLVER_SCHUR_FP64.  Defaults: max_age 1, rho_max 0.1, exact_after 8. */
+ * GP_SOLVER_SCHUR_FP64.  A solve that still ends at itermax (or on a
+ * non-finite residual) after inexact steps is redone from the step's
+ * starting point with exact Newton steps only, and that outcome is the one
+ * reported.  Defaults: max_age 1, rho_max 0.1, exact_after 8. */
 int32_t gp_set_mixed_policy(gp_layout *L, int32_t max_age, double rho_max, int32_t exact_after);
 
 /* gp_residual with no fault applied, computed without allocating anything:
