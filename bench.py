@@ -12,15 +12,20 @@ steps, their Newton iterations and the two dt = 0 event re-solves, i.e.
   python bench.py --profile TF [--steps K] [--warmup W]
 
 `--profile TF` is the short run used under ncu: the same workload and
-layout over a TF-second horizon, no end-to-end leg and no CPU baseline;
-it prints the library's phase timing (not a benchmark line).
+layout over a TF-second horizon, mixed solver then FP64 solver, no
+end-to-end leg and no CPU baseline; it prints the library's phase timing
+(not a benchmark line).
 
-The GPU arm prints one JSON line with `value` measured with inputs resident
-on the device (device-clock CUDA events recorded by the library), `e2e`
-measured through the public API with the state uploaded from pinned host
-memory and the full trajectory read back every step, the roofline of the
-dominant kernel phase, the CPU oracle baseline and the SM clocks sampled
-during the timed region.  `--impl reference` times the CPU restatement of
+The GPU arm prints one JSON line.  `value` is the mixed-precision Schur
+path (FP32 kept factors, FP64 residuals and updates) measured with inputs
+resident on the device (device-clock CUDA events recorded by the library);
+`fp64` is the plain FP64 Schur path timed the same way, and
+`max_state_err_vs_fp64` the largest rotor-angle, rotor-speed and bus |V|
+difference between the two.  `e2e` is the mixed path through the public
+API with the state uploaded from pinned host memory and the full trajectory
+read back every step.  The line also carries the roofline of the dominant
+kernel phase, the CPU oracle baseline and the SM clocks sampled during the
+timed region.  `--impl reference` times the CPU restatement of
 the reference's integrate! path (the oracle, OpenMP over scenarios) on the
 same workload.
 """
@@ -142,6 +147,43 @@ def cpu_baseline(gp, orc, w):
                       % (ns, WORKLOAD)}
 
 
+def timed_runs(gbl, faults, steps, solver, flush, torch):
+    """`steps` integrations with inputs resident on the device, an L2 flush
+    before each; device time from the library's CUDA events."""
+    acc = dict(total_ms=0.0, cluster_ms=0.0, network_ms=0.0, factor_ms=0.0, solve_ms=0.0, update_ms=0.0,
+               launches=0.0, factor_launches=0.0, linear_solves=0.0, newton_iters=0.0, refreshes=0.0,
+               exact_iters=0.0, retries=0.0)
+    status = 0
+    for _ in range(steps):
+        flush.fill_(1.0)                      # L2 flush between steps (buffer > 129 MB L2)
+        torch.cuda.synchronize()
+        gbl.restore_initial_state()
+        r = gbl.integrate(TF, DT, scenario_faults=faults, want_traj=False, solver=solver)
+        status = max(status, int(r["status"].max()))
+        t = gbl.timing()
+        for k in acc:
+            acc[k] += t[k]
+    acc["status_max"] = status
+    return acc
+
+
+def state_errors(w, traj, ref):
+    """Max |difference| of rotor angle, rotor speed (every GENROU/GENSAL) and
+    bus voltage magnitude over all scenarios and time points."""
+    import numpy as np
+    dyn = w.ps.dynamic
+    gens = [d for d in dyn.devices if d.dtype.kind == "genrou"]
+    ang = np.array([d.diff_ptr + 5 for d in gens])
+    spd = np.array([d.diff_ptr + 4 for d in gens])
+    net = dyn.diff_dim + dyn.alg_dim
+    vr = net + 2 * np.arange(w.ps.nbus)
+    vm = np.hypot(traj[..., vr], traj[..., vr + 1])
+    vm_ref = np.hypot(ref[..., vr], ref[..., vr + 1])
+    return {"rotor_angle": float(np.max(np.abs(traj[..., ang] - ref[..., ang]))),
+            "rotor_speed": float(np.max(np.abs(traj[..., spd] - ref[..., spd]))),
+            "bus_vm": float(np.max(np.abs(vm - vm_ref)))}
+
+
 def gpu_arm(args):
     import numpy as np
     import torch
@@ -151,7 +193,7 @@ def gpu_arm(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
     gp = load_package()
-    from gradpower_gb300 import build, gpu, synthetic
+    from gradpower_gb300 import build, gpu, layout as LY, synthetic
     if rank == 0 or world > 1:
         build.build()
     M_total = SCEN_PER_GPU * world
@@ -163,13 +205,12 @@ def gpu_arm(args):
     stats = gbl.stats()
     nsteps = int(round(TF / DT))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-
-    def one(want_traj=False):
-        gbl.restore_initial_state()
-        return gbl.integrate(TF, DT, scenario_faults=faults, want_traj=want_traj)
+    MIXED, FP64 = LY.SOLVER_SCHUR_MIXED, LY.SOLVER_SCHUR_FP64
 
     for _ in range(args.warmup):
-        one()
+        for solver in (MIXED, FP64):
+            gbl.restore_initial_state()
+            gbl.integrate(TF, DT, scenario_faults=faults, want_traj=False, solver=solver)
 
     def barrier():
         if world > 1:
@@ -177,50 +218,53 @@ def gpu_arm(args):
             dist.barrier()
         torch.cuda.synchronize()
 
-    # ---- device-resident timed region ----
+    def max_over_ranks(x):
+        if world > 1:
+            import torch.distributed as dist
+            tt = torch.tensor([x], dtype=torch.float64, device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            return float(tt.item())
+        return x
+
+    # ---- device-resident timed region: the mixed-precision Schur path ----
     clk = ClockSampler(local)
     barrier()
     clk.start()
-    acc = dict(total_ms=0.0, cluster_ms=0.0, network_ms=0.0, factor_ms=0.0, solve_ms=0.0, update_ms=0.0,
-               launches=0.0, factor_launches=0.0, linear_solves=0.0, newton_iters=0.0)
-    statuses = []
-    for _ in range(args.steps):
-        flush.fill_(1.0)                      # L2 flush between steps (buffer > 129 MB L2)
-        torch.cuda.synchronize()
-        r = one()
-        statuses.append(int(r["status"].max()))
-        t = gbl.timing()
-        for k in acc:
-            acc[k] += t[k]
+    acc = timed_runs(gbl, faults, args.steps, MIXED, flush, torch)
     barrier()
     clocks = clk.stop()
-    dev_ms = acc["total_ms"]
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([dev_ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        dev_ms = float(tt.item())
+    dev_ms = max_over_ranks(acc["total_ms"])
     units = M_total * nsteps * args.steps
     value = units / (dev_ms / 1e3)
 
-    # ---- end to end through the public API (host buffers) ----
+    # ---- the plain FP64 Schur path, timed the same way ----
+    barrier()
+    acc64 = timed_runs(gbl, faults, args.steps, FP64, flush, torch)
+    barrier()
+    dev64_ms = max_over_ranks(acc64["total_ms"])
+    value64 = units / (dev64_ms / 1e3)
+
+    # ---- state error of the mixed path against the FP64 path ----
+    gbl.restore_initial_state()
+    t_mix = gbl.integrate(TF, DT, scenario_faults=faults, solver=MIXED)["traj"]
+    gbl.restore_initial_state()
+    t_64 = gbl.integrate(TF, DT, scenario_faults=faults, solver=FP64)["traj"]
+    errs = state_errors(w, t_mix, t_64)
+    del t_mix, t_64
+
+    # ---- end to end through the public API (host buffers), mixed path ----
     z_host = torch.empty((Mloc, gbl.n_sys), dtype=torch.float64, pin_memory=True).numpy()
     z_host[:] = w.dp.zvec[None, :]
     traj_host = torch.empty((Mloc, nsteps + 1, gbl.n_sys), dtype=torch.float64, pin_memory=True).numpy()
     gbl.z = z_host
-    gbl.integrate(TF, DT, scenario_faults=faults, traj_out=traj_host)      # warm the trajectory buffer
+    gbl.integrate(TF, DT, scenario_faults=faults, traj_out=traj_host, solver=MIXED)   # warm the buffer
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         gbl.z = z_host                                                     # H2D of the inputs
-        gbl.integrate(TF, DT, scenario_faults=faults, traj_out=traj_host)  # D2H of the trajectories
+        gbl.integrate(TF, DT, scenario_faults=faults, traj_out=traj_host, solver=MIXED)   # D2H of the trajectories
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e = {"value": units / e2e_s, "unit": "scenario-steps/s",
            "h2d_bytes_per_step": int(z_host.nbytes * world),
            "d2h_bytes_per_step": int(traj_host.nbytes * world)}
@@ -229,30 +273,30 @@ def gpu_arm(args):
         gbl.close()
         return
 
-    # ---- roofline of the dominant phase ----
+    # ---- roofline of the dominant kernel phase of the mixed path ----
     peak, peak_kind = peaks()
     n_red = stats["n_red"]
     nnz_lu = stats["nnz_LU"]
-    # algorithmic bytes (FP64) per scenario, documented in the design doc:
-    #   factorisation: read S (4 per 2x2 block entry ~ nnz of the reduced
-    #   pattern) + write L and U;  solves: read L and U twice + vectors;
-    #   cluster kernel: read 2w+4 state/voltage values + 50 parameters,
-    #   write 3w solution columns + 8 Schur terms
+    # algorithmic bytes per scenario and pass (the figures of the design
+    # notes): the triangular solves read L and U once each in the factor
+    # type (4 bytes on kept FP32 factors) and read/write the vectors in FP64;
+    # the factorisation reads S and writes L and U; the cluster kernel reads
+    # 2w+4 state/voltage values and 50 parameters per cluster and writes 3w
+    # solution entries and 8 Schur terms; the network kernel reads V, Ybus
+    # and the cluster terms and writes the diagonal blocks and the rhs
     nnz_s = 4 * (w.ps.nbus + 2 * len(w.ps.branches))
     sum_w = int(w.ps.dynamic.diff_dim + w.ps.dynamic.alg_dim)
     n_cl = len(w.ps.dynamic.clusters)
     phases = {
-        "factor": (acc["factor_ms"], 8.0 * (nnz_s + nnz_lu)),
-        "solve": (acc["solve_ms"], 8.0 * (2 * nnz_lu + 4 * n_red)),
+        "solve": (acc["solve_ms"], 4.0 * 2 * nnz_lu + 8.0 * 4 * n_red),
+        "factor": (acc["factor_ms"], 4.0 * (nnz_s + nnz_lu)),
         "cluster": (acc["cluster_ms"], 8.0 * (5 * sum_w + n_cl * (4 + 50 + 8))),
-        "network": (acc["network_ms"], 8.0 * (4 * w.ps.nbus + 2 * len(ps_branches(w)) * 2 + 8 * w.ps.nbus)),
+        "network": (acc["network_ms"], 8.0 * (4 * w.ps.nbus + 4 * len(w.ps.branches) + 8 * w.ps.nbus)),
     }
     dom = max(phases, key=lambda k: phases[k][0])
     ms, bytes_per_scen = phases[dom]
-    # scenario-passes of the dominant phase in the timed region: every
-    # linear solve covers all scenarios still iterating; count Mloc per solve
-    # for the solve phases, per evaluation for the evaluation phases
-    passes = acc["linear_solves"] * Mloc if dom in ("factor", "solve") else acc["newton_iters"] * Mloc
+    passes = acc["linear_solves"] * Mloc if dom == "solve" else (
+        acc["refreshes"] if dom == "factor" else acc["newton_iters"] * Mloc)
     achieved = bytes_per_scen * passes / (ms / 1e3) / 1e9 if ms > 0 else 0.0
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": None, "kernel": dom,
@@ -262,7 +306,7 @@ def gpu_arm(args):
     oracle = load_oracle()
     base = cpu_baseline(gp, oracle, w)
     line = {
-        "metric": "scenario-steps/s at 70k-bus (FP64 Schur path)",
+        "metric": "scenario-steps/s at 70k-bus (mixed vs FP64 Schur, <=1e-6 err)",
         "value": value,
         "unit": "scenario-steps/s",
         "n_gpus": world,
@@ -272,16 +316,24 @@ def gpu_arm(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64",
+        "dtype": "f64 residuals and updates, f32 kept factors",
         "data": "synthetic (seeded 70,000-bus planar grid, random-parameter machine mix)",
         "config": {"workload": "%s: %d buses, %d unknowns, %d clusters, %d scenarios/GPU, tf=%gs, dt=1/120s"
                                % (WORKLOAD, w.ps.nbus, gbl.n_sys, n_cl, SCEN_PER_GPU, TF),
-                   "scenarios": M_total, "time_steps": nsteps, "solver": "schur_fp64",
+                   "scenarios": M_total, "time_steps": nsteps, "solver": "schur_mixed",
                    "l2": "flushed between steps (256 MB write); working set > 129 MB L2",
                    "parallelism": "scenario shards, %d GPU(s)" % world,
                    "nnz_LU": nnz_lu, "levels": stats["levels"], "supernodes": stats["supernodes"],
                    "sum_w2": stats["sum_w2"], "newton_iters_per_run": acc["newton_iters"] / args.steps,
-                   "status_max": max(statuses) if statuses else None},
+                   "refreshes_per_run": acc["refreshes"] / args.steps,
+                   "exact_iters_per_run": acc["exact_iters"] / args.steps,
+                   "retries_per_run": acc["retries"] / args.steps,
+                   "status_max": acc["status_max"]},
+        "fp64": {"value": value64, "ms_per_step": dev64_ms / args.steps,
+                 "newton_iters_per_run": acc64["newton_iters"] / args.steps, "status_max": acc64["status_max"],
+                 "phase_ms": {k: round(acc64[k + "_ms"], 3) for k in ("factor", "solve", "cluster", "network")}},
+        "mixed_over_fp64": value / value64,
+        "max_state_err_vs_fp64": errs,
         "e2e": e2e,
         "gpu_launches": int(acc["launches"]),
         "roofline": roofline,
@@ -290,10 +342,6 @@ def gpu_arm(args):
     }
     print(json.dumps(line), flush=True)
     gbl.close()
-
-
-def ps_branches(w):
-    return w.ps.branches
 
 
 def reference_arm(args):
@@ -322,7 +370,7 @@ def reference_arm(args):
     v = Ms * ns * args.steps / t
     line = {
         "impl": "reference",
-        "metric": "scenario-steps/s at 70k-bus (FP64 Schur path)",
+        "metric": "scenario-steps/s at 70k-bus (mixed vs FP64 Schur, <=1e-6 err)",
         "value": v, "unit": "scenario-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded 70,000-bus planar grid)",
@@ -344,13 +392,15 @@ def profile_arm(args):
     from gradpower_gb300 import build, gpu, synthetic
     build.build()
     w = synthetic.planar70k(n_scenarios=SCEN_PER_GPU)
+    from gradpower_gb300 import layout as LY
     gbl = gpu.GpuBatchedLayout(w.dp, w.ps, SCEN_PER_GPU)
-    for k in range(args.warmup + args.steps):
-        gbl.restore_initial_state()
-        r = gbl.integrate(args.profile, DT, scenario_faults=w.faults, want_traj=False)
-        if k >= args.warmup:
-            print(json.dumps({"profile_tf": args.profile, "status_max": int(r["status"].max()), **gbl.timing()}),
-                  flush=True)
+    for solver in (LY.SOLVER_SCHUR_MIXED, LY.SOLVER_SCHUR_FP64):
+        for k in range(args.warmup + args.steps):
+            gbl.restore_initial_state()
+            r = gbl.integrate(args.profile, DT, scenario_faults=w.faults, want_traj=False, solver=solver)
+            if k >= args.warmup:
+                print(json.dumps({"profile_tf": args.profile, "solver": solver,
+                                  "status_max": int(r["status"].max()), **gbl.timing()}), flush=True)
     gbl.close()
 
 
