@@ -1,6 +1,6 @@
 """Build libgradpower_gb300.so for sm_103a, in-tree (gradpower.jl_gb300/_build/).
 
-Six translation units compiled in parallel with nvcc, then linked; no
+Seven translation units compiled in parallel with nvcc, then linked; no
 cmake, no torch extension machinery.  Safe to call repeatedly: sources newer
 than the library trigger a rebuild.
 """
@@ -17,7 +17,8 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgradpower_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["gp_api.cu", "gp_kernels.cu", "gp_dag.cu", "gp_solve.cu", "gp_symbolic.cpp", "gp_cluster_plan.cpp"]
+SOURCES = ["gp_api.cu", "gp_kernels.cu", "gp_dag.cu", "gp_solve.cu", "gp_adjoint.cu", "gp_symbolic.cpp",
+           "gp_cluster_plan.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 

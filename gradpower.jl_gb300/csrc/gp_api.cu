@@ -92,11 +92,14 @@ struct gp_layout {
     gp::DevProblem P{};
     gp::DevWork W{};
     gp::DevSym S{};
+    gp::DevSym ST{};   // S^T: the same structure and buffers, transposed assembly lists (adjoint)
     gp::Symbolic sym;
     DeviceArena arena;     // lifetime of the layout
     DeviceArena call;      // lifetime of one gp_integrate call
     cudaStream_t st = nullptr;
     int *d_state_maps = nullptr;   // state_bus then red_of
+    int *d_gen_w = nullptr;        // z index of every machine's speed deviation
+    int n_gen = 0;
     int *h_flag = nullptr;         // pinned
     double *h_dt = nullptr;        // pinned
     // faults of the current call
@@ -156,6 +159,8 @@ struct Plan {
     gp::Symbolic sym;
     std::vector<int> acp, acpos, avp, avpos, avidx;
     std::vector<double> acval;
+    std::vector<int> t_acp, t_acpos, t_avp, t_avpos, t_avidx;   // the same for S^T
+    std::vector<double> t_acval;
     int64_t sum_w2 = 0;
 };
 
@@ -343,36 +348,47 @@ void make_plan(const gp_problem *pr, Plan &pl) {
         if (it == e || *it != k) fail(GP_E_INVALID, "entry outside the symbolic structure");
         return (en - st0) + (int)(it - b);
     };
-    std::vector<std::vector<std::pair<int, double>>> ac(sym.nsup);
-    std::vector<std::vector<std::pair<int, int>>> av(sym.nsup);
-    for (const Ent &e : ents) {
-        if (e.kind == 0 && e.val == 0.0) continue;
-        const int pi = sym.iperm[e.r], pj = sym.iperm[e.c];
-        const int s = sym.sup_of[std::min(pi, pj)];
-        const int m = sym.front_m(s);
-        const int lin = fpos(s, pi) + fpos(s, pj) * m;
-        if (lin < 0 || lin >= m * m) fail(GP_E_INVALID, "assembly position outside its front");
-        if (e.kind == 0) ac[s].push_back({lin, e.val});
-        else av[s].push_back({lin, e.idx});
-    }
-    // merge duplicate constant positions (parallel branches share a Ybus entry)
-    pl.acp.assign(sym.nsup + 1, 0);
-    pl.avp.assign(sym.nsup + 1, 0);
-    for (int s = 0; s < sym.nsup; s++) {
-        std::sort(ac[s].begin(), ac[s].end());
-        for (size_t q = 0; q < ac[s].size(); q++) {
-            if (q > 0 && ac[s][q].first == ac[s][q - 1].first) pl.acval.back() += ac[s][q].second;
-            else { pl.acpos.push_back(ac[s][q].first); pl.acval.push_back(ac[s][q].second); }
+    // the lists for S, and for S^T (same pattern, entry (r, c) at front
+    // position (c, r)): the adjoint factors S^T with the same kernels
+    auto build_lists = [&](bool tr, std::vector<int> &acp, std::vector<int> &acpos, std::vector<double> &acval,
+                           std::vector<int> &avp, std::vector<int> &avpos, std::vector<int> &avidx) {
+        std::vector<std::vector<std::pair<int, double>>> ac(sym.nsup);
+        std::vector<std::vector<std::pair<int, int>>> av(sym.nsup);
+        for (const Ent &e : ents) {
+            if (e.kind == 0 && e.val == 0.0) continue;
+            const int pi = sym.iperm[tr ? e.c : e.r], pj = sym.iperm[tr ? e.r : e.c];
+            const int s = sym.sup_of[std::min(pi, pj)];
+            const int m = sym.front_m(s);
+            const int lin = fpos(s, pi) + fpos(s, pj) * m;
+            if (lin < 0 || lin >= m * m) fail(GP_E_INVALID, "assembly position outside its front");
+            if (e.kind == 0) ac[s].push_back({lin, e.val});
+            else av[s].push_back({lin, e.idx});
         }
-        pl.acp[s + 1] = (int)pl.acpos.size();
-        std::sort(av[s].begin(), av[s].end());
-        for (size_t q = 0; q < av[s].size(); q++) {
-            if (q > 0 && av[s][q].first == av[s][q - 1].first) fail(GP_E_INVALID, "duplicate variable entry of S");
-            pl.avpos.push_back(av[s][q].first);
-            pl.avidx.push_back(av[s][q].second);
+        // merge duplicate constant positions (parallel branches share a Ybus entry)
+        acp.assign(sym.nsup + 1, 0);
+        avp.assign(sym.nsup + 1, 0);
+        acpos.clear();
+        acval.clear();
+        avpos.clear();
+        avidx.clear();
+        for (int s = 0; s < sym.nsup; s++) {
+            std::sort(ac[s].begin(), ac[s].end());
+            for (size_t q = 0; q < ac[s].size(); q++) {
+                if (q > 0 && ac[s][q].first == ac[s][q - 1].first) acval.back() += ac[s][q].second;
+                else { acpos.push_back(ac[s][q].first); acval.push_back(ac[s][q].second); }
+            }
+            acp[s + 1] = (int)acpos.size();
+            std::sort(av[s].begin(), av[s].end());
+            for (size_t q = 0; q < av[s].size(); q++) {
+                if (q > 0 && av[s][q].first == av[s][q - 1].first) fail(GP_E_INVALID, "duplicate variable entry of S");
+                avpos.push_back(av[s][q].first);
+                avidx.push_back(av[s][q].second);
+            }
+            avp[s + 1] = (int)avpos.size();
         }
-        pl.avp[s + 1] = (int)pl.avpos.size();
-    }
+    };
+    build_lists(false, pl.acp, pl.acpos, pl.acval, pl.avp, pl.avpos, pl.avidx);
+    build_lists(true, pl.t_acp, pl.t_acpos, pl.t_acval, pl.t_avp, pl.t_avpos, pl.t_avidx);
 }
 
 // Split of the assembly tree for the triangular solves (gp_solve.cu), on
@@ -502,7 +518,12 @@ void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
 // keeps the reciprocal of each pivot and ipiv the composed row permutation
 // of each supernode (pivot row i = assembled row ipiv[start + i]), as on the
 // device.  Returns the number of zero pivots.
-int host_factor(const Plan &pl, const std::vector<double> &svar, std::vector<double> &fronts, std::vector<int> &ipiv) {
+int host_factor(const Plan &pl, const std::vector<double> &svar, std::vector<double> &fronts, std::vector<int> &ipiv,
+                bool transpose = false) {
+    const std::vector<int> &acp = transpose ? pl.t_acp : pl.acp, &acpos = transpose ? pl.t_acpos : pl.acpos;
+    const std::vector<double> &acval = transpose ? pl.t_acval : pl.acval;
+    const std::vector<int> &avp = transpose ? pl.t_avp : pl.avp, &avpos = transpose ? pl.t_avpos : pl.avpos;
+    const std::vector<int> &avidx = transpose ? pl.t_avidx : pl.avidx;
     const gp::Symbolic &S = pl.sym;
     fronts.assign(S.front_off[S.nsup], 0.0);
     ipiv.assign(S.n, 0);
@@ -512,8 +533,8 @@ int host_factor(const Plan &pl, const std::vector<double> &svar, std::vector<dou
             const int s = S.level_sups[q];
             const int ns = S.front_n(s), mm = S.front_m(s), start = S.sup_start[s];
             double *F = fronts.data() + S.front_off[s];
-            for (int e = pl.acp[s]; e < pl.acp[s + 1]; e++) F[pl.acpos[e]] += pl.acval[e];
-            for (int e = pl.avp[s]; e < pl.avp[s + 1]; e++) F[pl.avpos[e]] += svar[pl.avidx[e]];
+            for (int e = acp[s]; e < acp[s + 1]; e++) F[acpos[e]] += acval[e];
+            for (int e = avp[s]; e < avp[s + 1]; e++) F[avpos[e]] += svar[avidx[e]];
             for (int cq = S.child_ptr[s]; cq < S.child_ptr[s + 1]; cq++) {
                 const int c = S.children[cq];
                 const int nc = S.front_n(c), rc = S.front_r(c), mc = S.front_m(c);
@@ -849,6 +870,14 @@ void build_problem(gp_layout *L, const gp_problem *pr) {
         D.link1 = up(T.link1);
     }
     P.is_diff = A.upload(pr->is_diff, P.net);
+    {
+        // z index of every machine's speed deviation (objective of the adjoint)
+        const gp_device_table &G = pr->dev[GP_GENROU];
+        std::vector<int> gw;
+        for (int k = 0; k < G.n; k++) gw.push_back(G.diff_ptr[k] + 4);
+        L->n_gen = (int)gw.size();
+        L->d_gen_w = A.upload(gw);
+    }
     L->sum_w2 = pl.sum_w2;
     P.n_cl = (int)pl.ws.size();
     P.cl_w_start = A.upload(pl.ws);
@@ -906,6 +935,13 @@ void build_problem(gp_layout *L, const gp_problem *pr) {
     S.asmv_ptr = A.upload(pl.avp);
     S.asmv_pos = A.upload(pl.avpos);
     S.asmv_idx = A.upload(pl.avidx);
+    L->ST = S;
+    L->ST.asmc_ptr = A.upload(pl.t_acp);
+    L->ST.asmc_pos = A.upload(pl.t_acpos);
+    L->ST.asmc_val = A.upload(pl.t_acval);
+    L->ST.asmv_ptr = A.upload(pl.t_avp);
+    L->ST.asmv_pos = A.upload(pl.t_avpos);
+    L->ST.asmv_idx = A.upload(pl.t_avidx);
     L->sym = pl.sym;
     build_dag(L, sym);
     build_blocks(L, sym);
@@ -936,6 +972,10 @@ void build_work(gp_layout *L, const double *z0, const double *u0, const double *
     S.fronts = A.alloc<double>(M * S.front_total);
     S.uvec = A.alloc<double>(M * std::max<int64_t>(1, S.uvec_total));
     S.ipiv = A.alloc<int>(M * S.n);
+    // S^T (the adjoint) factors into the same buffers
+    L->ST.fronts = S.fronts;
+    L->ST.uvec = S.uvec;
+    L->ST.ipiv = S.ipiv;
     {
         // no row swaps until a factorisation has run: the solves of a
         // scenario whose factors were never computed stay in bounds
@@ -995,9 +1035,23 @@ void build_clusters(gp_layout *L, const gp_problem *pr, const double *z0, const 
     C.nslot = A.upload(cp.nslot);
     C.perm_col = A.upload(cp.perm_col);
     C.pos3 = A.upload(cp.pos3);
+    {
+        // position of each local row in the class program (the residual
+        // placement ops name it): the transposed solves of the adjoint
+        // return the row of each position
+        std::vector<int> row_pos((size_t)cp.n_class * 32, 0);
+        for (int cls = 0; cls < cp.n_class; cls++) {
+            const int W = cp.cls_W[cls], rb = cp.rhs_base[cls];
+            for (int q = cp.prog_ptr[cls]; q < cp.prog_mid[cls]; q++) {
+                const gp::CluOp &o = cp.ops[q];
+                if (o.code == gp::OP_BEF || o.code == gp::OP_ROW) row_pos[(size_t)cls * 32 + o.a] = o.d - rb - 2 * W;
+            }
+        }
+        C.row_pos = A.upload(row_pos);
+    }
     C.max_slots = cp.max_slots;
     const int bytes = cp.max_slots * 32 * (int)sizeof(double);
-    if (bytes > 48 * 1024 && gp::cluster_smem_optin(bytes) < 0)
+    if (bytes > 48 * 1024 && (gp::cluster_smem_optin(bytes) < 0 || gp::adj_smem_optin(bytes) < 0))
         fail(GP_E_CUDA, "cluster kernel needs %d bytes of shared memory", bytes);
 }
 
@@ -1259,6 +1313,39 @@ void solve_step(gp_layout *L, double dt, double tol, int itermax, bool force_ref
         ck(cudaMemsetAsync(L->Mx.retry, 0, L->M, L->st), "memset");
         ck(cudaMemsetAsync(L->Mx.all_exact, 0, L->M, L->st), "memset");
     }
+}
+
+// Event steps of the current fault table, and per step the scenarios whose
+// faults toggle there (they take a dt = 0 re-solve after that step).
+std::map<int, std::vector<uint8_t>> event_masks(const gp_layout *L) {
+    std::map<int, std::vector<uint8_t>> ev;
+    for (int e = 0; e < L->n_fl; e++)
+        for (int k : {L->h_fl_on_step[e], L->h_fl_off_step[e]}) {
+            auto &mk = ev[k];
+            if (mk.empty()) mk.assign(L->M, 0);
+            mk[L->h_fl_scen[e]] = 1;
+        }
+    return ev;
+}
+
+// One transposed Newton-Jacobian solve of the adjoint for the active
+// scenarios at the current state W.z (time step dt, current fault status):
+// g holds the right-hand side on entry and E lambda on exit; lambda and the
+// parameter partials go to A.
+void adj_solve(gp_layout *L, const gp::DevAdj &A, const gp::DevClu &Csave, double dt) {
+    using namespace gp;
+    const size_t M = L->M, nsys = L->n_sys;
+    launch_set_double(L->W.dt, dt, L->st);
+    ck(cudaMemcpyAsync(L->W.zold, L->W.z, M * nsys * sizeof(double), cudaMemcpyDeviceToDevice, L->st), "zold");
+    const DevMixed exact{};
+    launch_cluster(L->P, L->W, Csave, exact, 0, L->st);
+    launch_network(L->P, L->W, 0, L->st);
+    launch_adj_rhs(L->P, L->W, Csave, A, L->st);
+    launch_dag_begin(L->D, L->st);
+    launch_dag_factor<double>(L->P, L->W, L->ST, L->D, L->G64, L->ST.fronts, L->W.active, 1, L->st);
+    launch_solve_bwd(L->P, L->W, L->ST, L->B, L->D, L->SG, FrontSel{nullptr, L->ST.fronts, nullptr, 1}, L->st);
+    launch_adj_back(L->P, L->W, Csave, A, L->d_state_maps, L->st);
+    ck(cudaGetLastError(), "adjoint launch");
 }
 
 }  // namespace
@@ -1538,7 +1625,7 @@ int32_t gp_cluster_selftest(const gp_problem *prob, const double *z, const doubl
 }
 
 int32_t gp_reduced_selftest(const gp_problem *prob, const int32_t *s_rowptr, const int32_t *s_colidx,
-                            const double *s_val, const double *rhs, double *x, double out[8]) {
+                            const double *s_val, const double *rhs, double *x, double out[12]) {
     API_BEGIN
     if (!prob || !s_rowptr || !s_colidx || !s_val || !rhs || !x || !out) fail(GP_E_INVALID, "null argument");
     Plan pl;
@@ -1593,6 +1680,160 @@ int32_t gp_reduced_selftest(const gp_problem *prob, const int32_t *s_rowptr, con
     out[5] = hb.nblk;
     out[6] = hb.n_top_levels;
     out[7] = hb.max_n;
+    // S^T from the transposed assembly lists (the adjoint's system):
+    // relative residual of S^T y = rhs
+    {
+        std::vector<double> ft;
+        std::vector<int> pt;
+        host_factor(pl, svar, ft, pt, true);
+        std::vector<double> yp(n);
+        for (int k = 0; k < n; k++) yp[k] = rhs[pl.sym.perm[k]];
+        host_level_solve(pl.sym, ft, pt, yp);
+        std::vector<double> y(n), res(n);
+        for (int k = 0; k < n; k++) y[pl.sym.perm[k]] = yp[k];
+        for (int i = 0; i < n; i++) res[i] = -rhs[i];
+        double ymax = 0.0, rmax = 0.0;
+        for (int i = 0; i < n; i++)
+            for (int q = s_rowptr[i]; q < s_rowptr[i + 1]; q++) res[s_colidx[q]] += s_val[q] * y[i];
+        for (int i = 0; i < n; i++) {
+            ymax = std::max(ymax, std::fabs(y[i]));
+            rmax = std::max(rmax, std::fabs(res[i]));
+        }
+        out[8] = ymax > 0.0 ? rmax / ymax : rmax;
+    }
+    API_END
+}
+
+int32_t gp_adjoint(gp_layout *L, const gp_options *opt, int32_t n_faults, const gp_fault *faults,
+                   const gp_objective *obj, int32_t checkpoint_every, double *J, double *grad_p, double *grad_z0,
+                   int32_t *status) {
+    API_BEGIN
+    using namespace gp;
+    if (!L || !opt || !obj) fail(GP_E_INVALID, "null argument");
+    if (opt->n_steps < 1 || !(opt->dt > 0.0) || opt->itermax <= 0 || checkpoint_every < 1)
+        fail(GP_E_INVALID, "bad options");
+    if (opt->solver != GP_SOLVER_SCHUR_FP64) fail(GP_E_INVALID, "the adjoint runs on the FP64 Schur path");
+    const int M = L->M, ns = opt->n_steps, K = checkpoint_every;
+    const size_t nsys = L->n_sys, blk = (size_t)M * nsys;
+    set_faults(L, n_faults, faults);
+    ensure_graphs(L, opt->newton_tol, opt->itermax, GP_SOLVER_SCHUR_FP64);
+    ck(cudaMemsetAsync(L->W.status, 0, M * sizeof(int), L->st), "memset");
+    ck(cudaMemsetAsync(L->D.err, 0, sizeof(int), L->st), "memset");
+    const auto ev = event_masks(L);
+    // device copies of the re-solve masks
+    std::map<int, uint8_t *> d_mask;
+    for (const auto &kv : ev) d_mask[kv.first] = L->call.upload(kv.second);
+    DeviceArena &CA = L->call;
+    const int nck = (ns + K - 1) / K;                       // checkpoints at steps 0, K, 2K, ...
+    double *ckp = CA.alloc<double>(blk * nck);
+    double *seg = CA.alloc<double>(blk * 2 * K);           // per step: regular and re-solve states
+    double *zfin = CA.alloc<double>(blk);
+    L->launches = L->factor_launches = L->solves = 0;
+    L->refreshes = L->exact_iters = L->retries = 0;
+    for (int i = 0; i < 8; i++) L->ph_ms[i] = 0.0;
+    cudaEvent_t e0, e1;
+    ck(cudaEventCreate(&e0), "event");
+    ck(cudaEventCreate(&e1), "event");
+    ck(cudaEventRecord(e0, L->st), "event");
+    // one forward step k; after(0) runs after the regular solve, after(1)
+    // after the re-solve of the scenarios whose faults toggle at k
+    auto step = [&](int k, auto after) {
+        ck(cudaMemcpyAsync(L->W.zold, L->W.z, blk * sizeof(double), cudaMemcpyDeviceToDevice, L->st), "zold");
+        ck(cudaMemsetAsync(L->W.active, 1, M, L->st), "memset");
+        solve_step(L, opt->dt, opt->newton_tol, opt->itermax, false);
+        after(0);
+        if (ev.count(k)) {
+            ck(cudaMemsetAsync(L->W.active, 0, M, L->st), "memset");
+            launch_events(L->P, L->W, L->d_fl_on_step, L->d_fl_off_step, L->d_fl_scen, L->d_fl_on, L->n_fl, k,
+                          L->st);
+            ck(cudaMemcpyAsync(L->W.zold, L->W.z, blk * sizeof(double), cudaMemcpyDeviceToDevice, L->st), "zold");
+            solve_step(L, 0.0, opt->newton_tol, opt->itermax, false);
+            after(1);
+        }
+    };
+    // ---- forward, keeping the checkpoints ----
+    ck(cudaMemcpyAsync(ckp, L->W.z, blk * sizeof(double), cudaMemcpyDeviceToDevice, L->st), "checkpoint");
+    for (int k = 1; k <= ns; k++) {
+        step(k, [](int) {});
+        if (k % K == 0 && k / K < nck)
+            ck(cudaMemcpyAsync(ckp + blk * (k / K), L->W.z, blk * sizeof(double), cudaMemcpyDeviceToDevice, L->st),
+               "checkpoint");
+    }
+    ck(cudaMemcpyAsync(zfin, L->W.z, blk * sizeof(double), cudaMemcpyDeviceToDevice, L->st), "final state");
+    if (status) {
+        ck(cudaStreamSynchronize(L->st), "forward");
+        ck(cudaMemcpy(status, L->W.status, M * sizeof(int), cudaMemcpyDeviceToHost), "status copy");
+    }
+    // ---- backward sweep ----
+    DevAdj A{};
+    A.g = CA.alloc<double>(blk);
+    A.lam = CA.alloc<double>(blk);
+    A.cadj = CA.alloc<double>((size_t)M * std::max(1, L->P.n_cl) * 2);
+    A.grad = CA.alloc<double>((size_t)M * std::max(1, L->n_par));
+    A.J = CA.alloc<double>(M);
+    A.gen_w = L->d_gen_w;
+    A.n_gen = L->n_gen;
+    A.w_speed = obj->w_speed;
+    A.w_volt = obj->w_volt;
+    A.v_min = obj->v_min;
+    ck(cudaMemsetAsync(A.g, 0, blk * sizeof(double), L->st), "memset");
+    ck(cudaMemsetAsync(A.lam, 0, blk * sizeof(double), L->st), "memset");
+    ck(cudaMemsetAsync(A.grad, 0, (size_t)M * std::max(1, L->n_par) * sizeof(double), L->st), "memset");
+    ck(cudaMemsetAsync(A.J, 0, M * sizeof(double), L->st), "memset");
+    DevClu Cs = L->C;
+    Cs.n_save = 1;
+    for (int v : L->cplan.rhs_base) Cs.n_save = std::max(Cs.n_save, v);
+    Cs.save_lu = CA.alloc<double>((size_t)M * std::max(1, Cs.n_tasks) * Cs.n_save * 32);
+    Cs.save_cc = CA.alloc<double>((size_t)M * std::max(1, L->P.n_cl) * 6);
+    for (int c = nck - 1; c >= 0; c--) {
+        const int ka = c * K, kb = std::min(ns, ka + K);
+        // recompute the segment from its checkpoint, keeping every solve's state
+        ck(cudaMemcpyAsync(L->W.z, ckp + blk * c, blk * sizeof(double), cudaMemcpyDeviceToDevice, L->st), "restore");
+        launch_fault_status(L->P, L->d_fl_on_step, L->d_fl_off_step, L->d_fl_on, L->n_fl, ka, L->st);
+        for (int k = ka + 1; k <= kb; k++)
+            step(k, [&](int kind) {
+                ck(cudaMemcpyAsync(seg + blk * (2 * (k - ka - 1) + kind), L->W.z, blk * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, L->st),
+                   "segment state");
+            });
+        for (int k = kb; k > ka; k--) {
+            if (ev.count(k)) {
+                // the dt = 0 re-solve after step k, for the scenarios that took it
+                ck(cudaMemcpyAsync(L->W.z, seg + blk * (2 * (k - ka - 1) + 1), blk * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, L->st),
+                   "state");
+                ck(cudaMemcpyAsync(L->W.active, d_mask[k], M, cudaMemcpyDeviceToDevice, L->st), "mask");
+                launch_fault_status(L->P, L->d_fl_on_step, L->d_fl_off_step, L->d_fl_on, L->n_fl, k, L->st);
+                adj_solve(L, A, Cs, 0.0);
+            }
+            // the regular solve of step k: its state is trajectory point k
+            ck(cudaMemcpyAsync(L->W.z, seg + blk * (2 * (k - ka - 1)), blk * sizeof(double),
+                               cudaMemcpyDeviceToDevice, L->st),
+               "state");
+            ck(cudaMemsetAsync(L->W.active, 1, M, L->st), "memset");
+            launch_fault_status(L->P, L->d_fl_on_step, L->d_fl_off_step, L->d_fl_on, L->n_fl, k - 1, L->st);
+            launch_adj_objective(L->P, L->W, A, opt->dt, L->st);
+            adj_solve(L, A, Cs, opt->dt);
+        }
+    }
+    ck(cudaMemcpyAsync(L->W.z, zfin, blk * sizeof(double), cudaMemcpyDeviceToDevice, L->st), "final state");
+    launch_fault_status(L->P, L->d_fl_on_step, L->d_fl_off_step, L->d_fl_on, L->n_fl, ns, L->st);
+    ck(cudaEventRecord(e1, L->st), "event");
+    ck(cudaStreamSynchronize(L->st), "adjoint");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    L->t_total_ms = ms;
+    {
+        int err = 0;
+        ck(cudaMemcpy(&err, L->D.err, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
+        if (err) fail(GP_E_TIMEOUT, "a dataflow wait of the reduced-system solve ran out its iteration limit");
+    }
+    if (J) ck(cudaMemcpy(J, A.J, M * sizeof(double), cudaMemcpyDeviceToHost), "J copy");
+    if (grad_p && L->n_par > 0)
+        ck(cudaMemcpy(grad_p, A.grad, (size_t)M * L->n_par * sizeof(double), cudaMemcpyDeviceToHost), "grad copy");
+    if (grad_z0) ck(cudaMemcpy(grad_z0, A.g, blk * sizeof(double), cudaMemcpyDeviceToHost), "grad z0 copy");
     API_END
 }
 

@@ -88,7 +88,12 @@ struct DevClu {
     const int *nslot;           // [n_class] slots used (values + pivots + 3 W)
     const int *perm_col;        // [class][32] state (local) of solution position j
     const int *pos3;            // [class][3] solution positions of delta, i_q, i_d
+    const int *row_pos;         // [class][32] position of local row r in the program
     int max_slots;
+    // adjoint: when set, the cluster kernel also saves its FP64 LU values
+    // ([M][n_tasks][n_save][32]) and the coupling rows C ([M][n_cl][6])
+    double *save_lu, *save_cc;
+    int n_save;
 };
 
 // Factor reuse of the mixed-precision solver (GP_SOLVER_SCHUR_MIXED).  The
@@ -213,5 +218,25 @@ void launch_events(const DevProblem &P, const DevWork &W, const int *fl_on_step,
                    const int *fl_scen, uint8_t *fl_on, int n_fl, int step, cudaStream_t st);
 void launch_snapshot(const double *z, double *traj, int M, int n_sys, int n_steps, int k, cudaStream_t st);
 int cluster_smem_optin(int bytes);
+
+// Discrete adjoint of the backward-Euler step (gp_adjoint.cu).
+struct DevAdj {
+    double *g;            // [M][n_sys] right-hand side of J^T lambda = g; after a step, E lambda
+    double *lam;          // [M][n_sys] lambda of the last backward solve
+    double *cadj;         // [M][n_cl][2] (A^-1 B)^T g_w per cluster
+    double *grad;         // [M][n_par] dJ/dp
+    double *J;            // [M] objective
+    const int *gen_w;     // [n_gen] z index of every machine's speed
+    int n_gen;
+    double w_speed, w_volt, v_min;   // objective weights and the voltage floor
+};
+void launch_adj_objective(const DevProblem &P, const DevWork &W, const DevAdj &A, double dt, cudaStream_t st);
+void launch_adj_rhs(const DevProblem &P, const DevWork &W, const DevClu &C, const DevAdj &A, cudaStream_t st);
+void launch_adj_back(const DevProblem &P, const DevWork &W, const DevClu &C, const DevAdj &A, const int *state_maps,
+                     cudaStream_t st);
+int adj_smem_optin(int bytes);
+void launch_set_double(double *dst, double v, cudaStream_t st);
+void launch_fault_status(const DevProblem &P, const int *fl_on_step, const int *fl_off_step, uint8_t *fl_on,
+                         int n_fl, int upto, cudaStream_t st);
 
 }  // namespace gp

@@ -209,6 +209,10 @@ __global__ void __launch_bounds__(32) cluster_kernel(DevProblem P, DevWork W, De
         }
         if (mode == 1)
             for (int s = 0; s < rb; s++) keep[s * 32] = (float)vals[s * 32 + lane];
+        if (Cl.save_lu) {
+            double *sv = Cl.save_lu + (((size_t)m * Cl.n_tasks + task) * Cl.n_save) * 32 + lane;
+            for (int s = 0; s < rb; s++) sv[s * 32] = vals[s * 32 + lane];
+        }
     }
     if (!act) return;
     const int n_da = P.n_diff + P.n_alg;
@@ -250,6 +254,10 @@ __global__ void __launch_bounds__(32) cluster_kernel(DevProblem P, DevWork W, De
     if (mode == 1) {
         float *cc = Mx.cc + ((size_t)m * P.n_cl + c) * 6;
         for (int t = 0; t < 6; t++) cc[t] = (float)Cc[t];
+    }
+    if (Cl.save_cc) {
+        double *cc = Cl.save_cc + ((size_t)m * P.n_cl + c) * 6;
+        for (int t = 0; t < 6; t++) cc[t] = Cc[t];
     }
 }
 

@@ -54,10 +54,11 @@ def library():
         L.gp_cluster_selftest.argtypes = [vp] * 5 + [C.c_double] + [vp] * 4
         L.gp_residual_static.argtypes = [vp, vp, C.c_double, vp]
         L.gp_set_mixed_policy.argtypes = [vp, C.c_int32, C.c_double, C.c_int32]
+        L.gp_adjoint.argtypes = [vp, vp, C.c_int32, vp, vp, C.c_int32, vp, vp, vp, vp]
         for f in ("gp_layout_create", "gp_layout_destroy", "gp_layout_stats", "gp_set_state",
                   "gp_get_state", "gp_integrate", "gp_residual", "gp_last_timing",
                   "gp_restore_initial_state", "gp_reduced_selftest", "gp_cluster_selftest",
-                  "gp_residual_static", "gp_set_mixed_policy"):
+                  "gp_residual_static", "gp_set_mixed_policy", "gp_adjoint"):
             getattr(L, f).restype = C.c_int32
         _lib = L
     return _lib
@@ -90,6 +91,7 @@ class GpuBatchedLayout:
         if p is not None:
             pp = np.ascontiguousarray(p, dtype=np.float64).reshape(self.M, -1)
         self.n_sys = self.arrays.n_sys
+        self.n_par = self.arrays.n_par
         self._keep = (z, u, pp)
         h = C.c_void_p()
         P = self.arrays.as_ctypes()
@@ -179,6 +181,28 @@ class GpuBatchedLayout:
                                       _p(status)))
         tvec = np.arange(nsteps + 1) * dt
         return dict(tvec=tvec, traj=traj, iters=iters[:, :2 * nsteps], status=status)
+
+    def adjoint(self, tf: float, dt: float = 1.0 / 120.0, newton_tol: float = 1e-10, itermax: int = 30,
+                events: Sequence[Mdl.ContingencyEvent] = (),
+                scenario_faults: Optional[Sequence[Sequence[Mdl.ContingencyEvent]]] = None,
+                w_speed: float = 1.0, w_volt: float = 0.0, v_min: float = 0.9, checkpoint_every: int = 60):
+        """Objective and its gradients for every scenario, by the discrete
+        adjoint of the FP64 Schur integration from the current state
+        (gp_adjoint in include/gradpower_gb300.h).  Returns J [M], grad_p
+        [M, n_par] (H, D, exciter gain, governor droop; zero elsewhere),
+        grad_z0 [M, n_sys] and the forward run's status [M]."""
+        nsteps = LY.jl_round(tf / dt)
+        per = scenario_faults if scenario_faults is not None else [[] for _ in range(self.M)]
+        fa, nf = LY.fault_array(per, dt, events)
+        opt = LY.GpOptions(dt, nsteps, newton_tol, itermax, LY.SOLVER_SCHUR_FP64)
+        obj = LY.GpObjective(w_speed, w_volt, v_min)
+        J = np.zeros(self.M)
+        gp_ = np.zeros((self.M, max(self.n_par, 1)))
+        gz = np.zeros((self.M, self.n_sys))
+        status = np.zeros(self.M, dtype=np.int32)
+        _check(library().gp_adjoint(self._h, C.byref(opt), nf, C.addressof(fa), C.byref(obj), int(checkpoint_every),
+                                    _p(J), _p(gp_), _p(gz), _p(status)))
+        return dict(J=J, grad_p=gp_[:, :self.n_par], grad_z0=gz, status=status)
 
 
 def scenario_shard(M: int, rank: int, world: int):

@@ -57,6 +57,12 @@ class GpFault(C.Structure):
                 ("on_step", C.c_int32), ("off_step", C.c_int32)]
 
 
+class GpObjective(C.Structure):
+    """gp_objective: J = sum_t dt * (w_speed * sum_gen w^2
+    + w_volt * sum_bus max(0, v_min - |V|)^2)."""
+    _fields_ = [("w_speed", C.c_double), ("w_volt", C.c_double), ("v_min", C.c_double)]
+
+
 class GpOptions(C.Structure):
     _fields_ = [("dt", C.c_double), ("n_steps", C.c_int32), ("newton_tol", C.c_double),
                 ("itermax", C.c_int32), ("solver", C.c_int32)]

@@ -212,6 +212,42 @@ int32_t gp_residual(gp_layout *L, const double *zold, double dt, int32_t n_fault
  * exact Newton steps after failing with inexact ones; out[13..15] zero. */
 int32_t gp_last_timing(const gp_layout *L, double out[16]);
 
+/* Objective of the adjoint:
+ *   J = sum over the stored trajectory points t = 1..n_steps of
+ *       dt * ( w_speed * sum over machines of w^2
+ *            + w_volt * sum over buses of max(0, v_min - |V|)^2 )
+ * where w is the machine speed deviation.  w_speed = 1, w_volt = 0 is the
+ * reference's functional (src/dynamics.jl:330-337 with the time weighting of
+ * src/nlp.jl:30-46). */
+typedef struct gp_objective {
+    double w_speed;
+    double w_volt;
+    double v_min;
+} gp_objective;
+
+/* Discrete adjoint of gp_integrate (FP64 Schur path), for every scenario:
+ * integrates opt->n_steps steps forward from the current state, keeping the
+ * state every checkpoint_every steps, then sweeps backwards, recomputing the
+ * steps between checkpoints, with one transposed Newton-Jacobian solve per
+ * forward solve (regular steps and dt = 0 event re-solves) at its converged
+ * state and fault status.
+ *   J        [M] objective value
+ *   grad_p   [M][n_par] dJ/dp at the fixed initial state: filled for the
+ *            machine inertia H and damping D (GENROU/GENSAL), the exciter
+ *            gain (SEXS K, ESDC1A KA) and the governor droop (TGOV1 R,
+ *            IEESGO K1); zero for the other parameters.  May be NULL.
+ *   grad_z0  [M][n_sys] dJ/dz0 (differential states; the algebraic ones are
+ *            determined by the first solve and get zero).  May be NULL.
+ *   status   [M] as gp_integrate, for the forward run.  May be NULL.
+ * opt->solver must be GP_SOLVER_SCHUR_FP64.  On return the layout holds the
+ * final state.  Replaces the reference's GradPower.adjoint(lambda0, dprob,
+ * sys, traj, tvec; functional=true) (examples/adjoint.jl:105,
+ * test/test_adjoint_event_offset.jl:50-53), whose source is no longer in the
+ * reference (src/nlp.jl:50-53). */
+int32_t gp_adjoint(gp_layout *L, const gp_options *opt, int32_t n_faults, const gp_fault *faults,
+                   const gp_objective *obj, int32_t checkpoint_every, double *J, double *grad_p, double *grad_z0,
+                   int32_t *status);
+
 /* Refresh policy of GP_SOLVER_SCHUR_MIXED (no counterpart in the reference,
  * whose solvers refactor every iteration): a scenario refreshes its kept
  * FP32 factors at the start of a solve once they have served max_age
@@ -249,11 +285,13 @@ int32_t gp_residual_static(gp_layout *L, const double *zold, double dt, double *
  * off-diagonal blocks, out[1] zero pivots, out[2] nnz(L+U), out[3]
  * elimination-tree levels, out[4] max |x_blocked - x_levels| / max |x|,
  * out[5] solve blocks, out[6] levels of the top region, out[7] most
- * supernodes in one block.
+ * supernodes in one block, out[8] max |S^T y - rhs| / max |y| for S^T
+ * factored from the transposed assembly lists of the adjoint, out[9..11]
+ * zero.
  * No counterpart in the reference: a test hook for the analysis that
  * replaces cuDSS's. */
 int32_t gp_reduced_selftest(const gp_problem *prob, const int32_t *s_rowptr, const int32_t *s_colidx,
-                            const double *s_val, const double *rhs, double *x, double out[8]);
+                            const double *s_val, const double *rhs, double *x, double out[12]);
 
 /* Host-only check of the cluster factorisation, needs no GPU: builds the
  * class plans of gp_layout_create from (z, u0, p) of one scenario and runs

@@ -74,7 +74,7 @@ def test_reduced_factorisation_matches_scipy(lib, name):
     S = _reduced_S(w.ps, rng)
     rhs = rng.normal(size=S.shape[0])
     x = np.zeros_like(rhs)
-    out = np.zeros(8)
+    out = np.zeros(12)
     rp, ci, sv = S.indptr.astype(np.int32), S.indices.astype(np.int32), S.data.astype(np.float64)
     lib.gp_reduced_selftest.argtypes = [C.c_void_p] * 7
     rc = lib.gp_reduced_selftest(C.addressof(P), rp.ctypes.data, ci.ctypes.data, sv.ctypes.data,
@@ -84,6 +84,8 @@ def test_reduced_factorisation_matches_scipy(lib, name):
     # blocked triangular solves (staging indices checked) agree with the
     # level-order solves
     assert out[4] <= 1e-13 and out[5] >= 1
+    # S^T from the transposed assembly lists (the adjoint's system)
+    assert out[8] <= 1e-10
     xr = spla.spsolve(S.tocsc(), rhs)
     assert np.max(np.abs(x - xr)) <= 1e-12 * np.max(np.abs(xr))
 
@@ -115,13 +117,15 @@ def test_reduced_factorisation_with_static_generators(lib, golden_cases, orc):
     Ssp.sort_indices()
     rhs = np.random.default_rng(2).normal(size=len(red_global))
     x = np.zeros_like(rhs)
-    out = np.zeros(8)
+    out = np.zeros(12)
     P = PA.as_ctypes()
     rp, ci, sv = Ssp.indptr.astype(np.int32), Ssp.indices.astype(np.int32), Ssp.data.astype(np.float64)
     lib.gp_reduced_selftest.argtypes = [C.c_void_p] * 7
     assert lib.gp_reduced_selftest(C.addressof(P), rp.ctypes.data, ci.ctypes.data, sv.ctypes.data,
                                    rhs.ctypes.data, x.ctypes.data, out.ctypes.data) == 0
     assert out[0] < 1e-12
+    # S^T, whose static-generator couplings are not symmetric
+    assert out[8] <= 1e-10
     xr = np.linalg.solve(S, rhs)
     assert np.max(np.abs(x - xr)) <= 1e-10 * np.max(np.abs(xr))
 
