@@ -43,6 +43,9 @@ WORKLOAD = "planar70k"
 SCEN_PER_GPU = 8
 TF = 1.0
 DT = 1.0 / 120.0
+ADJ_SCEN_PER_GPU = 128
+ADJ_TF = 3.0
+ADJ_STEPS = 2
 
 
 def load_package():
@@ -184,6 +187,38 @@ def state_errors(w, traj, ref):
             "bus_vm": float(np.max(np.abs(vm - vm_ref)))}
 
 
+def adjoint_bench(args, world, rank, torch, max_over_ranks):
+    """Gradients per second of the discrete adjoint on the differentiation
+    workload: the 2,000-bus grid, 128 fault scenarios per GPU, 3 s at
+    dt = 1/120 (360 steps), checkpoints every 60 steps, objective
+    sum_t dt (sum_gen w^2 + 10 sum_bus max(0, 0.9 - |V|)^2).  One gradient
+    is one scenario's reverse sweep (forward run, recomputation and the
+    transposed solves included)."""
+    from gradpower_gb300 import gpu, synthetic
+    M = ADJ_SCEN_PER_GPU
+    w = synthetic.planar2k(n_scenarios=M * world)
+    lo, hi = gpu.scenario_shard(M * world, rank, world)
+    faults = w.faults[lo:hi]
+    gbl = gpu.GpuBatchedLayout(w.dp, w.ps, hi - lo)
+    kw = dict(scenario_faults=faults, w_speed=1.0, w_volt=10.0, v_min=0.9, checkpoint_every=60)
+    gbl.adjoint(0.5, DT, **kw)                      # warm-up (graphs, buffers)
+    ms, status = 0.0, 0
+    for _ in range(ADJ_STEPS):
+        gbl.restore_initial_state()
+        r = gbl.adjoint(ADJ_TF, DT, **kw)
+        ms += gbl.timing()["total_ms"]
+        status = max(status, int(r["status"].max()))
+    gbl.close()
+    ms = max_over_ranks(ms)
+    grads = M * world * ADJ_STEPS
+    return {"metric": "adjoint grads/s (2,000-bus, 360 steps)", "value": grads / (ms / 1e3), "unit": "grads/s",
+            "ms_per_run": ms / ADJ_STEPS, "runs": ADJ_STEPS,
+            "config": {"workload": "planar2k: %d buses, %d unknowns, %d scenarios/GPU, tf=%gs, dt=1/120s"
+                                   % (w.ps.nbus, len(w.dp.zvec), M, ADJ_TF),
+                       "checkpoint_every": 60, "parameters": "H, D, exciter gain, governor droop of every machine",
+                       "objective": "sum_t dt (sum w^2 + 10 sum max(0, 0.9 - |V|)^2)", "status_max": status}}
+
+
 def gpu_arm(args):
     import numpy as np
     import torch
@@ -269,8 +304,9 @@ def gpu_arm(args):
            "h2d_bytes_per_step": int(z_host.nbytes * world),
            "d2h_bytes_per_step": int(traj_host.nbytes * world)}
 
+    gbl.close()
+    adj = adjoint_bench(args, world, rank, torch, max_over_ranks)
     if rank != 0:
-        gbl.close()
         return
 
     # ---- roofline of the dominant kernel phase of the mixed path ----
@@ -339,9 +375,9 @@ def gpu_arm(args):
         "roofline": roofline,
         "cpu_baseline": base,
         "clocks": clocks,
+        "adjoint": adj,
     }
     print(json.dumps(line), flush=True)
-    gbl.close()
 
 
 def reference_arm(args):
