@@ -403,6 +403,7 @@ struct HostBlk {
     std::vector<int4> ent0, ent1;
     int n_top_levels = 0, top_max_front = 1;
     std::vector<int> top_order, top_rank;
+    std::vector<int> top_xptr, top_xrow, top_xent;   // extend-add lists of the top region
 };
 
 void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
@@ -511,6 +512,26 @@ void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
                 B.top_order.push_back(s);
             }
     B.n_top_levels = ntl;
+    // extend-add lists: for every front row of a top supernode, the
+    // children's update-vector entries that add into it, in child order
+    B.top_xptr.assign(1, 0);
+    B.top_xrow.clear();
+    B.top_xent.clear();
+    for (int s : B.top_order) {
+        const int mm = sym.front_m(s);
+        std::vector<std::vector<int>> per(mm);
+        for (int q = sym.child_ptr[s]; q < sym.child_ptr[s + 1]; q++) {
+            const int c = sym.children[q];
+            for (int a = 0; a < sym.front_r(c); a++)
+                per[sym.relmap[sym.relmap_ptr[c] + a]].push_back((int)sym.uvec_off[c] + a);
+        }
+        for (int i = 0; i < mm; i++) {
+            B.top_xrow.push_back((int)B.top_xent.size());
+            B.top_xent.insert(B.top_xent.end(), per[i].begin(), per[i].end());
+        }
+        B.top_xrow.push_back((int)B.top_xent.size());
+        B.top_xptr.push_back((int)B.top_xrow.size());
+    }
 }
 
 // Host emulation of the device factorisation (gp_dag.cu): the same front
@@ -708,11 +729,12 @@ void host_block_solve(const gp::Symbolic &S, const HostBlk &B, const std::vector
         }
         const int start = S.sup_start[s], ns = S.front_n(s), r = S.front_r(s), mm = ns + r;
         Staged tv(B.top_max_front, "top vector");
-        for (int i = 0; i < mm; i++) tv[i] = i < ns ? x[start + i] : 0.0;
-        for (int cq = S.child_ptr[s]; cq < S.child_ptr[s + 1]; cq++) {
-            const int c = S.children[cq];
-            const int *rel = S.relmap.data() + S.relmap_ptr[c];
-            for (int a = 0; a < S.front_r(c); a++) tv[rel[a]] += uvec[S.uvec_off[c] + a];
+        const int *xr = B.top_xrow.data() + B.top_xptr[t];
+        if (B.top_xptr[t + 1] - B.top_xptr[t] != mm + 1) fail(GP_E_INTERNAL, "top extend-add rows of %d", s);
+        for (int i = 0; i < mm; i++) {
+            double acc = i < ns ? x[start + i] : 0.0;
+            for (int e = xr[i]; e < xr[i + 1]; e++) acc += uvec[B.top_xent[e]];
+            tv[i] = acc;
         }
         host_fwd_front(fronts.data() + S.front_off[s], ipiv.data() + start, ns, mm, tv, 0);
         for (int i = 0; i < ns; i++) x[start + i] = tv[i];
@@ -818,6 +840,9 @@ void build_blocks(gp_layout *L, const gp::Symbolic &sym) {
     B.top_max_front = H.top_max_front;
     B.top_order = A.upload(H.top_order);
     B.top_rank = A.upload(H.top_rank);
+    B.top_xptr = A.upload(H.top_xptr);
+    B.top_xrow = A.upload(H.top_xrow);
+    B.top_xent = A.upload(H.top_xent);
     L->n_top_levels = H.n_top_levels;
     const int sc = gp::solve_configure(B, L->SG);
     if (sc == -2) fail(GP_E_INVALID, "front of %d rows exceeds the solve kernels' staging area", B.top_max_front);
@@ -1168,7 +1193,7 @@ void enqueue_eval(gp_layout *L, double tol, int itermax) {
     mark(L, 0);
     gp::launch_cluster(L->P, L->W, L->C, L->Mx, 0, L->st);
     mark(L, 1);
-    gp::launch_network(L->P, L->W, 0, L->st);
+    gp::launch_network(L->P, L->W, L->Mx, 0, L->st);
     mark(L, 2);
     gp::launch_check(L->P, L->W, L->Mx, tol, itermax, L->st);
     ck(cudaMemcpyAsync(L->h_flag, L->W.flag, 4 * sizeof(int), cudaMemcpyDeviceToHost, L->st), "flag copy");
@@ -1339,7 +1364,7 @@ void adj_solve(gp_layout *L, const gp::DevAdj &A, const gp::DevClu &Csave, doubl
     ck(cudaMemcpyAsync(L->W.zold, L->W.z, M * nsys * sizeof(double), cudaMemcpyDeviceToDevice, L->st), "zold");
     const DevMixed exact{};
     launch_cluster(L->P, L->W, Csave, exact, 0, L->st);
-    launch_network(L->P, L->W, 0, L->st);
+    launch_network(L->P, L->W, exact, 0, L->st);
     launch_adj_rhs(L->P, L->W, Csave, A, L->st);
     launch_dag_begin(L->D, L->st);
     launch_dag_factor<double>(L->P, L->W, L->ST, L->D, L->G64, L->ST.fronts, L->W.active, 1, L->st);
@@ -1484,7 +1509,7 @@ int32_t gp_residual(gp_layout *L, const double *zold, double dt, int32_t n_fault
     const gp::DevMixed exact{};
     gp::launch_reset_norm(L->P, L->W, exact, L->st);
     gp::launch_cluster(L->P, L->W, L->C, exact, 1, L->st);
-    gp::launch_network(L->P, L->W, 1, L->st);
+    gp::launch_network(L->P, L->W, exact, 1, L->st);
     ck(cudaGetLastError(), "residual launch");
     ck(cudaStreamSynchronize(L->st), "residual");
     ck(cudaMemcpy(f, L->W.f, n * sizeof(double), cudaMemcpyDeviceToHost), "residual copy");
@@ -1956,7 +1981,7 @@ extern "C" int32_t gp_residual_static(gp_layout *L, const double *zold, double d
     const gp::DevMixed exact{};
     gp::launch_reset_norm(P, W, exact, st);
     gp::launch_cluster(P, W, L->C, exact, 1, st);
-    gp::launch_network(P, W, 1, st);
+    gp::launch_network(P, W, exact, 1, st);
     ck(cudaGetLastError(), "residual launch");
     ck(cudaMemcpyAsync(f, W.f, M * P.n_sys * sizeof(double), cudaMemcpyDeviceToHost, st), "residual copy");
     ck(cudaStreamSynchronize(st), "residual");

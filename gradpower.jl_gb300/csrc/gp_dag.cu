@@ -17,7 +17,10 @@
 //  - factor_small_kernel: supernodes whose whole subtree has fronts of at
 //    most 32 rows, one warp per task, the front in shared memory;
 //  - factor_big_kernel: the rest, one CTA per task.
-// Partial pivoting is restricted to a supernode's pivot rows.  The front
+// Partial pivoting is restricted to a supernode's pivot rows.  The FP32
+// elimination is blocked (the pivot panel column by column, then one
+// triangular solve and one update of the rest of the front); the FP64 one
+// is right-looking.  The front
 // (column-major, leading dimension = front rows) keeps L, U and the update
 // matrix that the parent's extend-add reads.
 //
@@ -160,6 +163,14 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
         g.sync();
     }
     // ---- elimination ----
+    // FP64: right-looking, column by column over the whole front (every
+    // update of a column is an independent FMA, which keeps GB300's long
+    // FP64 pipeline busy).  FP32: blocked; the pivot panel (columns
+    // 0..ns-1) column by column, then the right part (columns ns..nc-1) once:
+    // U12 = L11^-1 A12 by forward substitution, one column per thread, and
+    // A22 -= L21 U12, four entries per thread with the sums in registers.
+    // Both give every entry the same operations in the same order.
+    constexpr bool kBlocked = sizeof(T) == 4;
     for (int k = 0; k < ns; k++) {
         if (g.lead_warp()) {
             const int lane = threadIdx.x & 31;
@@ -182,8 +193,9 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
             if (lane == 0) F[k + k * mm] = inv;
         }
         g.sync();
-        // rank-1 update of rows k+1.., columns k+1.. (the right-hand side too)
-        const int lr = mm - k - 1, lc = nc - k - 1;
+        // rank-1 update: rows k+1.., columns k+1.. of the whole front
+        // (right-looking) or of the panel only (blocked)
+        const int lr = mm - k - 1, lc = (kBlocked ? ns : nc) - k - 1;
         if (lr > 0 && lc > 0) {
             int i = idx % lr, j = idx / lr;
             const int di = step % lr, dj = step / lr;
@@ -195,6 +207,38 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
                 j += dj;
                 if (i >= lr) { i -= lr; j++; }
             }
+        }
+        g.sync();
+    }
+    if (kBlocked) {
+        for (int j = ns + idx; j < nc; j += step) {
+            T *cj = F + j * mm;
+            for (int k = 0; k < ns; k++) {
+                const T u = cj[k];
+                const T *lk = F + k * mm;
+                for (int i = k + 1; i < ns; i++) cj[i] -= lk[i] * u;
+            }
+        }
+        g.sync();
+        const int r = mm - ns, n = r * (nc - ns);
+        for (int t0 = idx; t0 < n; t0 += 4 * step) {
+            int ri[4], cj[4];
+            T acc[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int t = min(t0 + q * step, n - 1);
+                ri[q] = ns + t % r;
+                cj[q] = (ns + t / r) * mm;
+                acc[q] = F[ri[q] + cj[q]];
+            }
+            for (int k = 0; k < ns; k++) {
+                const T *lk = F + k * mm;
+#pragma unroll
+                for (int q = 0; q < 4; q++) acc[q] -= lk[ri[q]] * F[k + cj[q]];
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (t0 + q * step < n) F[ri[q] + cj[q]] = acc[q];
         }
         g.sync();
     }
@@ -240,7 +284,7 @@ __host__ __device__ inline int big_front_bytes(int max_front) {
 }
 
 template <class T, bool RHS>
-__global__ void __launch_bounds__(kThreads) factor_small_kernel(DevProblem P, DevWork W, DevSym S, DevDag D,
+__global__ void __launch_bounds__(kThreads, 6) factor_small_kernel(DevProblem P, DevWork W, DevSym S, DevDag D,
                                                                 T *fronts, const uint8_t *mask, int want) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -264,7 +308,7 @@ __global__ void __launch_bounds__(kThreads) factor_small_kernel(DevProblem P, De
 }
 
 template <class T, bool RHS>
-__global__ void __launch_bounds__(kThreads) factor_big_kernel(DevProblem P, DevWork W, DevSym S, DevDag D,
+__global__ void __launch_bounds__(kThreads, 3) factor_big_kernel(DevProblem P, DevWork W, DevSym S, DevDag D,
                                                               T *fronts, const uint8_t *mask, int want) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *F = reinterpret_cast<T *>(smem_raw);

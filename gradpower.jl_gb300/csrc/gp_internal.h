@@ -179,6 +179,12 @@ struct DevBlk {
     int n_top, top_max_front;
     const int *top_order;        // [n_top] top supernodes, children before parents
     const int *top_rank;         // [nsup] position in top_order, -1 inside a block
+    // forward extend-add of the top region, per top supernode (by rank) and
+    // front row: the children's update-vector entries (offsets within a
+    // scenario's uvec) that add into the row, in child order
+    const int *top_xptr;         // [n_top+1] first row pointer of each top supernode
+    const int *top_xrow;         // row pointers into top_xent
+    const int *top_xent;
 };
 
 // Factors of the triangular solves, per scenario: FP64 when f32 is null or
@@ -207,7 +213,7 @@ int solve_block_front_limit();
 // launches (gp_kernels.cu)
 void launch_cluster(const DevProblem &P, const DevWork &W, const DevClu &C, const DevMixed &Mx, int want_f,
                     cudaStream_t st);
-void launch_network(const DevProblem &P, const DevWork &W, int want_f, cudaStream_t st);
+void launch_network(const DevProblem &P, const DevWork &W, const DevMixed &Mx, int want_f, cudaStream_t st);
 void launch_check(const DevProblem &P, const DevWork &W, const DevMixed &Mx, double tol, int itermax,
                   cudaStream_t st);
 void launch_reset_norm(const DevProblem &P, const DevWork &W, const DevMixed &Mx, cudaStream_t st);

@@ -280,7 +280,10 @@ int cluster_smem_optin(int bytes) {
 // network kernel
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, int want_f) {
+// With the mixed solver, a scenario iterating on kept factors needs only the
+// residual and the right-hand side: the entries of S (diagonal blocks,
+// static-generator couplings) are skipped for it.
+__global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, DevMixed Mx, int want_f) {
     const long long task = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = task < (long long)P.M * P.n_bus;
     const int m = valid ? (int)(task / P.n_bus) : P.M;
@@ -288,6 +291,7 @@ __global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, i
     const bool act = valid && W.active[m];
     unsigned long long nb = 0ull;
     if (act) {
+        const bool need_s = !(Mx.on && Mx.refac[m] == MX_KEEP);
         const double *z = W.z + (size_t)m * P.n_sys;
         const double *p = W.p + (size_t)m * P.n_par;
         const int net = P.net;
@@ -299,11 +303,11 @@ __global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, i
             const double vrj = z[net + 2 * j], vij = z[net + 2 * j + 1];
             fr -= g * vrj - bb * vij;
             fi -= bb * vrj + g * vij;
-            if (j == b) { d00 -= g; d01 += bb; d10 -= bb; d11 -= g; }
+            if (need_s && j == b) { d00 -= g; d01 += bb; d10 -= bb; d11 -= g; }
         }
         for (int q = P.bus_cl_ptr[b]; q < P.bus_cl_ptr[b + 1]; q++) {
             const double *o = W.clout + ((size_t)m * P.n_cl + P.bus_cl[q]) * 8;
-            d00 -= o[0]; d01 -= o[1]; d10 -= o[2]; d11 -= o[3];
+            if (need_s) { d00 -= o[0]; d01 -= o[1]; d10 -= o[2]; d11 -= o[3]; }
             rr += o[4]; ri += o[5];
             fr += o[6]; fi += o[7];
         }
@@ -319,6 +323,7 @@ __global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, i
             const double den = vm2 > vm2_tld ? vm2 : vm2_tld;
             fr -= (1.0 - al) * (pl * vr - ql * vi) / den;
             fi -= (1.0 - al) * (ql * vr + pl * vi) / den;
+            if (!need_s) continue;
             double p11, p12, p21, p22;
             if (vm2 > vm2_tld) {
                 const double iv4 = 1.0 / (vm2 * vm2);
@@ -350,6 +355,32 @@ __global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, i
             const double irn = Pg * vr + Qg * vi, iin = Pg * vi - Qg * vr;
             fr += irn / vm2;
             fi += iin / vm2;
+            if (!need_s) {
+                double *xp = W.xperm + (size_t)m * P.n_red;
+                const int r0 = P.sg_red[k];
+                if (bt == 2) {
+                    const double vset = p[pp + 2];
+                    const double fa = vr * vr + vi * vi - vset * vset;
+                    xp[P.iperm[r0]] = -fa;
+                    if (want_f) W.f[(size_t)m * P.n_sys + ap] = fa;
+                    const unsigned long long t = norm_bits(fa);
+                    nb = t > nb ? t : nb;
+                } else if (bt == 3) {
+                    const double vset = p[pp + 2], aset = p[pp + 3];
+                    const double fa0 = vr - vset * cos(aset), fa1 = vi - vset * sin(aset);
+                    xp[P.iperm[r0]] = -fa0;
+                    xp[P.iperm[r0 + 1]] = -fa1;
+                    if (want_f) {
+                        W.f[(size_t)m * P.n_sys + ap] = fa0;
+                        W.f[(size_t)m * P.n_sys + ap + 1] = fa1;
+                    }
+                    unsigned long long t = norm_bits(fa0);
+                    nb = t > nb ? t : nb;
+                    t = norm_bits(fa1);
+                    nb = t > nb ? t : nb;
+                }
+                continue;
+            }
             if (vm2r > 0.2) {
                 const double vm4 = vm2 * vm2;
                 d00 += Pg / vm2 - 2.0 * vr * irn / vm4;
@@ -404,8 +435,10 @@ __global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, i
             W.f[(size_t)m * P.n_sys + net + 2 * b] = fr;
             W.f[(size_t)m * P.n_sys + net + 2 * b + 1] = fi;
         }
-        double *sv = W.svar + (size_t)m * P.n_var + 4 * b;
-        sv[0] = d00; sv[1] = d01; sv[2] = d10; sv[3] = d11;
+        if (need_s) {
+            double *sv = W.svar + (size_t)m * P.n_var + 4 * b;
+            sv[0] = d00; sv[1] = d01; sv[2] = d10; sv[3] = d11;
+        }
         double *xp = W.xperm + (size_t)m * P.n_red;
         xp[P.iperm[2 * b]] = -(fr - rr);
         xp[P.iperm[2 * b + 1]] = -(fi - ri);
@@ -426,10 +459,10 @@ __global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, i
     if (act && (lane == 0 || mprev != m)) atomicMax(W.norm + m, nb);
 }
 
-void launch_network(const DevProblem &P, const DevWork &W, int want_f, cudaStream_t st) {
+void launch_network(const DevProblem &P, const DevWork &W, const DevMixed &Mx, int want_f, cudaStream_t st) {
     long long tasks = (long long)P.M * P.n_bus;
     int blocks = (int)((tasks + 255) / 256);
-    network_kernel<<<blocks, 256, 0, st>>>(P, W, want_f);
+    network_kernel<<<blocks, 256, 0, st>>>(P, W, Mx, want_f);
 }
 
 // ---------------------------------------------------------------------------

@@ -456,13 +456,14 @@ __device__ void stage_cols(T *Fs, const T *F, int mm, int nrow, int c0, int c1) 
 }
 
 struct TopCtx {
-    int s, m, start, ns, r, mm;
+    int s, m, rank, start, ns, r, mm;
 };
 
-__device__ __forceinline__ TopCtx top_ctx(const DevSym &S, int s, int m) {
+__device__ __forceinline__ TopCtx top_ctx(const DevSym &S, int s, int m, int rank) {
     TopCtx c;
     c.s = s;
     c.m = m;
+    c.rank = rank;
     c.start = S.sup_start[s];
     c.ns = S.sup_start[s + 1] - c.start;
     c.r = S.row_ptr[s + 1] - S.row_ptr[s];
@@ -516,13 +517,16 @@ __device__ void fwd_top_task(const DevProblem &P, const DevWork &W, const DevSym
     int k1 = min(t.ns, cap);
     stage_cols<T>(Fs, F, t.mm, t.mm, 0, k1);
     if (!wait_top_children(S, B, D, t.s, t.m, P.M, epoch, s_ok) && threadIdx.x == 0) atomicOr(W.status + t.m, 8);
-    for (int q = S.child_ptr[t.s]; q < S.child_ptr[t.s + 1]; q++) {
-        const int c = S.children[q];
-        const int rc = S.row_ptr[c + 1] - S.row_ptr[c];
-        const int *rel = S.relmap + S.relmap_ptr[c];
-        const double *uc = uv + S.uvec_off[c];
-        for (int a = threadIdx.x; a < rc; a += blockDim.x) v[rel[a]] += (T)__ldcg(uc + a);
-        __syncthreads();
+    // extend-add: one thread per front row sums the children's entries in
+    // child order (the update vectors of the children were written by other
+    // CTAs: read through L2)
+    {
+        const int *xr = B.top_xrow + B.top_xptr[t.rank];
+        for (int i = threadIdx.x; i < t.mm; i += blockDim.x) {
+            T acc = v[i];
+            for (int e = xr[i]; e < xr[i + 1]; e++) acc += (T)__ldcg(uv + B.top_xent[e]);
+            v[i] = acc;
+        }
     }
     int k0 = 0;
     bool gather = true;
@@ -597,7 +601,7 @@ __global__ void __launch_bounds__(kTopThreads) fwd_top_kernel(DevProblem P, DevW
         if (!W.active[m]) continue;
         const bool d = use64(fs, m);
         if (d && fs.fused64) continue;
-        const TopCtx c = top_ctx(S, s, m);
+        const TopCtx c = top_ctx(S, s, m, t / M);
         if (d) fwd_top_task<double>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
         else fwd_top_task<float>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
         __syncthreads();
@@ -620,7 +624,7 @@ __global__ void __launch_bounds__(kTopThreads) bwd_top_kernel(DevProblem P, DevW
         if (t >= n_tasks) break;
         const int s = B.top_order[B.n_top - 1 - t / M], m = t % M;
         if (!W.active[m]) continue;
-        const TopCtx c = top_ctx(S, s, m);
+        const TopCtx c = top_ctx(S, s, m, B.n_top - 1 - t / M);
         if (use64(fs, m)) bwd_top_task<double>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
         else bwd_top_task<float>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
         __syncthreads();
