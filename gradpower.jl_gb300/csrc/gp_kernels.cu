@@ -521,6 +521,18 @@ __global__ void retry_start_kernel(DevProblem P, DevWork W, DevMixed Mx) {
     }
 }
 
+__global__ void predict_kernel(double *z, const double *zold, double *zprev, size_t n, int extrapolate) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double a = zold[i];
+    if (extrapolate) z[i] = 2.0 * a - zprev[i];
+    zprev[i] = a;
+}
+
+void launch_predict(double *z, const double *zold, double *zprev, size_t n, bool extrapolate, cudaStream_t st) {
+    predict_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(z, zold, zprev, n, extrapolate ? 1 : 0);
+}
+
 void launch_retry_start(const DevProblem &P, const DevWork &W, const DevMixed &Mx, cudaStream_t st) {
     const long long tasks = (long long)P.M * P.n_sys;
     retry_start_kernel<<<(int)((tasks + 255) / 256), 256, 0, st>>>(P, W, Mx);

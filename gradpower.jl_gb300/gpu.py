@@ -53,7 +53,7 @@ def library():
         L.gp_reduced_selftest.argtypes = [vp] * 7
         L.gp_cluster_selftest.argtypes = [vp] * 5 + [C.c_double] + [vp] * 4
         L.gp_residual_static.argtypes = [vp, vp, C.c_double, vp]
-        L.gp_set_mixed_policy.argtypes = [vp, C.c_int32, C.c_double, C.c_int32]
+        L.gp_set_mixed_policy.argtypes = [vp, C.c_int32, C.c_double, C.c_int32, C.c_int32]
         L.gp_adjoint.argtypes = [vp, vp, C.c_int32, vp, vp, C.c_int32, vp, vp, vp, vp]
         for f in ("gp_layout_create", "gp_layout_destroy", "gp_layout_stats", "gp_set_state",
                   "gp_get_state", "gp_integrate", "gp_residual", "gp_last_timing",
@@ -126,10 +126,11 @@ class GpuBatchedLayout:
         keys = ("n_red", "nnz_S", "nnz_LU", "supernodes", "levels", "factor_flops", "sum_w2", "max_front")
         return dict(zip(keys, (int(v) for v in out)))
 
-    def set_mixed_policy(self, max_age: int = 1, rho_max: float = 0.1, exact_after: int = 8):
-        """Refresh policy of the mixed-precision solver (see
-        gp_set_mixed_policy in include/gradpower_gb300.h)."""
-        _check(library().gp_set_mixed_policy(self._h, int(max_age), float(rho_max), int(exact_after)))
+    def set_mixed_policy(self, max_age: int = 1, rho_max: float = 0.1, exact_after: int = 8, predict: bool = True):
+        """Policy of the mixed-precision solver (see gp_set_mixed_policy in
+        include/gradpower_gb300.h)."""
+        _check(library().gp_set_mixed_policy(self._h, int(max_age), float(rho_max), int(exact_after),
+                                             1 if predict else 0))
 
     def timing(self) -> dict:
         """Device time of the last integrate call by phase (CUDA events on

@@ -248,19 +248,25 @@ int32_t gp_adjoint(gp_layout *L, const gp_options *opt, int32_t n_faults, const 
                    const gp_objective *obj, int32_t checkpoint_every, double *J, double *grad_p, double *grad_z0,
                    int32_t *status);
 
-/* Refresh policy of GP_SOLVER_SCHUR_MIXED (no counterpart in the reference,
- * whose solvers refactor every iteration): a scenario refreshes its kept
- * FP32 factors at the start of a solve once they have served max_age
- * solves, and after an iteration that reduced the residual by less than the
- * factor rho_max.  A scenario still iterating after exact_after iterations
- * of one solve takes exact Newton steps with fresh FP64 factors until that
- * solve ends (its kept factors are refreshed at the next solve), so that a
- * system too ill-conditioned for FP32 factors converges as in
- * GP_SOLVER_SCHUR_FP64.  A solve that still ends at itermax (or on a
- * non-finite residual) after inexact steps is redone from the step's
- * starting point with exact Newton steps only, and that outcome is the one
- * reported.  Defaults: max_age 1, rho_max 0.1, exact_after 8. */
-int32_t gp_set_mixed_policy(gp_layout *L, int32_t max_age, double rho_max, int32_t exact_after);
+/* Policy of GP_SOLVER_SCHUR_MIXED (no counterpart in the reference, whose
+ * solvers refactor every iteration):
+ *  - a scenario refreshes its kept FP32 factors at the start of a solve once
+ *    they have served max_age solves, and after an iteration that reduced
+ *    the residual by less than the factor rho_max;
+ *  - a scenario still iterating after exact_after iterations of one solve
+ *    takes exact Newton steps with fresh FP64 factors until that solve ends
+ *    (its kept factors are refreshed at the next solve), so that a system
+ *    too ill-conditioned for FP32 factors converges as in
+ *    GP_SOLVER_SCHUR_FP64; a solve that still ends at itermax (or on a
+ *    non-finite residual) after inexact steps is redone from the step's
+ *    starting point with exact Newton steps only, and that outcome is the
+ *    one reported;
+ *  - predict = 1 starts every step whose two previous states lie on one
+ *    smooth stretch (no event re-solve in between) from their linear
+ *    extrapolation instead of the previous state: the same backward-Euler
+ *    equations and convergence test, a closer initial iterate.
+ * Defaults: max_age 1, rho_max 0.1, exact_after 8, predict 1. */
+int32_t gp_set_mixed_policy(gp_layout *L, int32_t max_age, double rho_max, int32_t exact_after, int32_t predict);
 
 /* gp_residual with no fault applied, computed without allocating anything:
  * its scratch (zold, residual, cluster and network intermediates) lives in
