@@ -106,7 +106,7 @@ struct Chunk {
 // v[i] -= L(i, k) v[k], with L(i, k) = F[i + (k - kbase) * ld].  v[0..mm)
 // is in shared memory; rows below ns are first gathered through the pivot
 // permutation perm (identity after the first chunk).
-template <class T, int J, class Perm>
+template <class T, int J, class Perm, int CH = Chunk<J>::value>
 __device__ void fwd_cols_j(const T *__restrict__ F, int ld, int kbase, int k0, int k1, int ns, int mm, T *v,
                            Perm perm) {
     const int lane = threadIdx.x & 31;
@@ -116,7 +116,6 @@ __device__ void fwd_cols_j(const T *__restrict__ F, int ld, int kbase, int k0, i
         const int i = lane + 32 * j;
         r[j] = i < ns ? v[perm(i)] : (i < mm ? v[i] : T(0));
     }
-    constexpr int CH = Chunk<J>::value;
     for (int kc = k0; kc < k1; kc += CH) {
         T c[CH][J];
 #pragma unroll
@@ -211,7 +210,7 @@ __device__ __forceinline__ void bwd_u12(const T *__restrict__ F, int ld, int cba
 
 // U11 columns k from k1 - 1 down to k0: v[k] *= U(k, k) (the stored
 // reciprocal pivot), then v[i] -= U(i, k) v[k] for i < k.
-template <class T, int J>
+template <class T, int J, int CH = Chunk<J>::value>
 __device__ void bwd_cols_j(const T *__restrict__ F, int ld, int kbase, int k0, int k1, int ns, T *v) {
     const int lane = threadIdx.x & 31;
     T r[J];
@@ -220,7 +219,6 @@ __device__ void bwd_cols_j(const T *__restrict__ F, int ld, int kbase, int k0, i
         const int i = lane + 32 * j;
         r[j] = i < ns ? v[i] : T(0);
     }
-    constexpr int CH = Chunk<J>::value;
     for (int kc = k1 - 1; kc >= k0; kc -= CH) {
         T c[CH][J], d[CH];
 #pragma unroll
@@ -280,17 +278,18 @@ __device__ void bwd_cols(const T *F, int ld, int kbase, int k0, int k1, int ns, 
 }
 
 // Block fronts (at most kBlkFront rows): the whole front from global memory.
+// (block fronts are small: four columns per chunk)
 template <class T, class Perm>
 __device__ void fwd_front_blk(const T *F, Perm perm, int ns, int mm, T *v) {
-    if (mm <= 32) fwd_cols_j<T, 1>(F, mm, 0, 0, ns, ns, mm, v, perm);
-    else fwd_cols_j<T, 2>(F, mm, 0, 0, ns, ns, mm, v, perm);
+    if (mm <= 32) fwd_cols_j<T, 1, Perm, 4>(F, mm, 0, 0, ns, ns, mm, v, perm);
+    else fwd_cols_j<T, 2, Perm, 4>(F, mm, 0, 0, ns, ns, mm, v, perm);
 }
 
 template <class T>
 __device__ void bwd_front_blk(const T *F, int ns, int mm, T *v) {
     bwd_u12<T>(F, mm, 0, ns, mm, ns, v);
-    if (ns <= 32) bwd_cols_j<T, 1>(F, mm, 0, 0, ns, ns, v);
-    else bwd_cols_j<T, 2>(F, mm, 0, 0, ns, ns, v);
+    if (ns <= 32) bwd_cols_j<T, 1, 4>(F, mm, 0, 0, ns, ns, v);
+    else bwd_cols_j<T, 2, 4>(F, mm, 0, 0, ns, ns, v);
 }
 
 // ---- blocks ----------------------------------------------------------------
@@ -383,7 +382,7 @@ __device__ void fwd_block(const DevProblem &P, const DevWork &W, const DevSym &S
     }
 }
 
-__global__ void __launch_bounds__(32 * kBlkWarps) fwd_blocks_kernel(DevProblem P, DevWork W, DevSym S, DevBlk B,
+__global__ void __launch_bounds__(32 * kBlkWarps, 8) fwd_blocks_kernel(DevProblem P, DevWork W, DevSym S, DevBlk B,
                                                                      FrontSel fs) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5;
@@ -426,7 +425,7 @@ __device__ void bwd_block(const DevProblem &P, const DevWork &W, const DevSym &S
     }
 }
 
-__global__ void __launch_bounds__(32 * kBlkWarps) bwd_blocks_kernel(DevProblem P, DevWork W, DevSym S, DevBlk B,
+__global__ void __launch_bounds__(32 * kBlkWarps, 8) bwd_blocks_kernel(DevProblem P, DevWork W, DevSym S, DevBlk B,
                                                                      FrontSel fs) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5;
