@@ -142,9 +142,9 @@ struct gp_layout {
     double exact_iters = 0.0;                 // mixed: scenario iterations with FP64 factors
     double retries = 0.0;                     // mixed: scenario solves redone exactly
     int mx_max_age = 1, mx_exact_after = 8;   // mixed solver policy (gp_set_mixed_policy)
-    double mx_rho_max = 0.1;
-    int mx_predict = 1;                       // mixed: start steps from the extrapolated state
-    double *zprev = nullptr;                  // mixed: state at the start of the previous step
+    double mx_rho_max = 0.9;
+    int mx_predict = 2;                       // mixed: extrapolation order of the step's first iterate
+    double *zprev = nullptr, *zprev2 = nullptr;   // mixed: states at the start of the last two steps
 };
 
 namespace {
@@ -1236,6 +1236,7 @@ void ensure_mixed(gp_layout *L) {
     X.cc = A.alloc<float>(M * std::max(1, L->P.n_cl) * 6);
     X.fronts = A.alloc<float>(M * L->S.front_total);
     L->zprev = A.alloc<double>(M * L->n_sys);
+    L->zprev2 = A.alloc<double>(M * L->n_sys);
     ck(cudaMemset(X.refac, 0, M), "memset");
     ck(cudaMemset(X.refac_next, 0, M), "memset");
     ck(cudaMemset(X.prev_mode, 0, M), "memset");
@@ -1563,14 +1564,15 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
     // one smooth stretch (no event in between) from their linear
     // extrapolation
     bool force = true;
-    const bool predict = opt->solver == GP_SOLVER_SCHUR_MIXED && L->mx_predict;
-    bool smooth = false;
+    const int predict = opt->solver == GP_SOLVER_SCHUR_MIXED ? L->mx_predict : 0;
+    int smooth = 0;   // earlier states on the current smooth stretch
     for (int k = 1; k <= ns; k++) {
         ck(cudaMemcpyAsync(L->W.zold, L->W.z, (size_t)M * nsys * sizeof(double), cudaMemcpyDeviceToDevice, L->st),
            "zold");
         if (predict) {
-            gp::launch_predict(L->W.z, L->W.zold, L->zprev, (size_t)M * nsys, smooth, L->st);
-            smooth = true;
+            gp::launch_predict(L->W.z, L->W.zold, L->zprev, L->zprev2, (size_t)M * nsys, std::min(predict, smooth),
+                               L->st);
+            smooth += 1;
         }
         ck(cudaMemsetAsync(L->W.active, 1, M, L->st), "memset");
         solve_step(L, opt->dt, opt->newton_tol, opt->itermax, force);
@@ -1591,7 +1593,7 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
                "zold");
             solve_step(L, 0.0, opt->newton_tol, opt->itermax, true);
             force = true;
-            smooth = false;
+            smooth = 0;
             ck(cudaMemcpyAsync(d_iters + (size_t)(2 * (k - 1) + 1) * M, L->W.iters, M * sizeof(int),
                                cudaMemcpyDeviceToDevice, L->st),
                "iters");
@@ -1878,7 +1880,7 @@ int32_t gp_adjoint(gp_layout *L, const gp_options *opt, int32_t n_faults, const 
 int32_t gp_set_mixed_policy(gp_layout *L, int32_t max_age, double rho_max, int32_t exact_after, int32_t predict) {
     API_BEGIN
     if (!L) fail(GP_E_INVALID, "null argument");
-    if (max_age < 1 || !(rho_max > 0.0) || exact_after < 1 || (predict != 0 && predict != 1))
+    if (max_age < 1 || !(rho_max > 0.0) || exact_after < 1 || predict < 0 || predict > 2)
         fail(GP_E_INVALID, "bad mixed-solver policy");
     L->mx_predict = predict;
     L->mx_max_age = max_age;

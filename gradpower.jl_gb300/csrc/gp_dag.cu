@@ -82,17 +82,27 @@ __device__ __forceinline__ unsigned long long mag_key(float v) {
 // magnitude, the smallest index on ties.  Called by a whole warp; every lane
 // returns the same result.  zero is set when the column is zero there.
 template <class T>
+struct KeyOf {
+    using type = unsigned long long;
+};
+template <>
+struct KeyOf<float> {
+    using type = unsigned;
+};
+
+template <class T>
 __device__ __forceinline__ int warp_pivot(const T *F, int mm, int k, int ns, bool &zero) {
+    using K = typename KeyOf<T>::type;
     const int lane = threadIdx.x & 31;
-    unsigned long long bk = 0;
+    K bk = 0;
     int bi = k;
     for (int i = k + lane; i < ns; i += 32) {
-        const unsigned long long v = mag_key(F[i + k * mm]);
+        const K v = (K)mag_key(F[i + k * mm]);
         if (v > bk) { bk = v; bi = i; }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-        const unsigned long long ok = __shfl_xor_sync(FULL, bk, off);
+        const K ok = __shfl_xor_sync(FULL, bk, off);
         const int oi = __shfl_xor_sync(FULL, bi, off);
         if (ok > bk || (ok == bk && oi < bi)) { bk = ok; bi = oi; }
     }

@@ -521,16 +521,19 @@ __global__ void retry_start_kernel(DevProblem P, DevWork W, DevMixed Mx) {
     }
 }
 
-__global__ void predict_kernel(double *z, const double *zold, double *zprev, size_t n, int extrapolate) {
+__global__ void predict_kernel(double *z, const double *zold, double *zprev, double *zprev2, size_t n, int order) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double a = zold[i];
-    if (extrapolate) z[i] = 2.0 * a - zprev[i];
+    const double a = zold[i], b = zprev[i];
+    if (order == 1) z[i] = 2.0 * a - b;
+    else if (order == 2) z[i] = 3.0 * (a - b) + zprev2[i];
+    zprev2[i] = b;
     zprev[i] = a;
 }
 
-void launch_predict(double *z, const double *zold, double *zprev, size_t n, bool extrapolate, cudaStream_t st) {
-    predict_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(z, zold, zprev, n, extrapolate ? 1 : 0);
+void launch_predict(double *z, const double *zold, double *zprev, double *zprev2, size_t n, int order,
+                    cudaStream_t st) {
+    predict_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(z, zold, zprev, zprev2, n, order);
 }
 
 void launch_retry_start(const DevProblem &P, const DevWork &W, const DevMixed &Mx, cudaStream_t st) {

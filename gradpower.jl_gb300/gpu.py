@@ -126,11 +126,10 @@ class GpuBatchedLayout:
         keys = ("n_red", "nnz_S", "nnz_LU", "supernodes", "levels", "factor_flops", "sum_w2", "max_front")
         return dict(zip(keys, (int(v) for v in out)))
 
-    def set_mixed_policy(self, max_age: int = 1, rho_max: float = 0.1, exact_after: int = 8, predict: bool = True):
+    def set_mixed_policy(self, max_age: int = 1, rho_max: float = 0.9, exact_after: int = 8, predict: int = 2):
         """Policy of the mixed-precision solver (see gp_set_mixed_policy in
-        include/gradpower_gb300.h)."""
-        _check(library().gp_set_mixed_policy(self._h, int(max_age), float(rho_max), int(exact_after),
-                                             1 if predict else 0))
+        include/gradpower_gb300.h); predict: 0 none, 1 linear, 2 quadratic."""
+        _check(library().gp_set_mixed_policy(self._h, int(max_age), float(rho_max), int(exact_after), int(predict)))
 
     def timing(self) -> dict:
         """Device time of the last integrate call by phase (CUDA events on

@@ -263,9 +263,11 @@ int32_t gp_adjoint(gp_layout *L, const gp_options *opt, int32_t n_faults, const 
  *    one reported;
  *  - predict = 1 starts every step whose two previous states lie on one
  *    smooth stretch (no event re-solve in between) from their linear
- *    extrapolation instead of the previous state: the same backward-Euler
- *    equations and convergence test, a closer initial iterate.
- * Defaults: max_age 1, rho_max 0.1, exact_after 8, predict 1. */
+ *    extrapolation instead of the previous state, predict = 2 from the
+ *    quadratic one through three states when there are three (linear with
+ *    two): the same backward-Euler equations and convergence test, a closer
+ *    initial iterate; predict = 0 starts from the previous state.
+ * Defaults: max_age 1, rho_max 0.9, exact_after 8, predict 2. */
 int32_t gp_set_mixed_policy(gp_layout *L, int32_t max_age, double rho_max, int32_t exact_after, int32_t predict);
 
 /* gp_residual with no fault applied, computed without allocating anything:
