@@ -143,8 +143,8 @@ struct gp_layout {
     double retries = 0.0;                     // mixed: scenario solves redone exactly
     int mx_max_age = 1, mx_exact_after = 8;   // mixed solver policy (gp_set_mixed_policy)
     double mx_rho_max = 0.9;
-    int mx_predict = 2;                       // mixed: extrapolation order of the step's first iterate
-    double *zprev = nullptr, *zprev2 = nullptr;   // mixed: states at the start of the last two steps
+    int mx_predict = 3;                       // mixed: extrapolation order of the step's first iterate
+    double *zprev = nullptr, *zprev2 = nullptr, *zprev3 = nullptr;   // mixed: states at the start of the last steps
 };
 
 namespace {
@@ -1237,6 +1237,7 @@ void ensure_mixed(gp_layout *L) {
     X.fronts = A.alloc<float>(M * L->S.front_total);
     L->zprev = A.alloc<double>(M * L->n_sys);
     L->zprev2 = A.alloc<double>(M * L->n_sys);
+    L->zprev3 = A.alloc<double>(M * L->n_sys);
     ck(cudaMemset(X.refac, 0, M), "memset");
     ck(cudaMemset(X.refac_next, 0, M), "memset");
     ck(cudaMemset(X.prev_mode, 0, M), "memset");
@@ -1560,9 +1561,9 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
     ck(cudaMemsetAsync(L->D.err, 0, sizeof(int), L->st), "memset");
     // the mixed solver refreshes its kept factors at the first solve and
     // around every event (the dt = 0 re-solve and the step after it); with
-    // prediction on, it starts every step whose two previous states lie on
-    // one smooth stretch (no event in between) from their linear
-    // extrapolation
+    // prediction on, it starts every step from the polynomial extrapolation
+    // of the previous states on the current smooth stretch (no event in
+    // between), of order at most mx_predict
     bool force = true;
     const int predict = opt->solver == GP_SOLVER_SCHUR_MIXED ? L->mx_predict : 0;
     int smooth = 0;   // earlier states on the current smooth stretch
@@ -1570,8 +1571,8 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
         ck(cudaMemcpyAsync(L->W.zold, L->W.z, (size_t)M * nsys * sizeof(double), cudaMemcpyDeviceToDevice, L->st),
            "zold");
         if (predict) {
-            gp::launch_predict(L->W.z, L->W.zold, L->zprev, L->zprev2, (size_t)M * nsys, std::min(predict, smooth),
-                               L->st);
+            gp::launch_predict(L->W.z, L->W.zold, L->zprev, L->zprev2, L->zprev3, (size_t)M * nsys,
+                               std::min(predict, smooth), L->st);
             smooth += 1;
         }
         ck(cudaMemsetAsync(L->W.active, 1, M, L->st), "memset");
@@ -1880,7 +1881,7 @@ int32_t gp_adjoint(gp_layout *L, const gp_options *opt, int32_t n_faults, const 
 int32_t gp_set_mixed_policy(gp_layout *L, int32_t max_age, double rho_max, int32_t exact_after, int32_t predict) {
     API_BEGIN
     if (!L) fail(GP_E_INVALID, "null argument");
-    if (max_age < 1 || !(rho_max > 0.0) || exact_after < 1 || predict < 0 || predict > 2)
+    if (max_age < 1 || !(rho_max > 0.0) || exact_after < 1 || predict < 0 || predict > 3)
         fail(GP_E_INVALID, "bad mixed-solver policy");
     L->mx_predict = predict;
     L->mx_max_age = max_age;

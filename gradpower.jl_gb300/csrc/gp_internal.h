@@ -220,10 +220,11 @@ void launch_reset_norm(const DevProblem &P, const DevWork &W, const DevMixed &Mx
 void launch_mixed_start(const DevProblem &P, const DevWork &W, const DevMixed &Mx, int force, cudaStream_t st);
 void launch_retry_start(const DevProblem &P, const DevWork &W, const DevMixed &Mx, cudaStream_t st);
 // Start of a step of the mixed solver: the first iterate z from the
-// extrapolation of order `order` (0 none, 1 linear 2 zold - zprev, 2
-// quadratic 3 zold - 3 zprev + zprev2), then zprev2 <- zprev <- zold.
-void launch_predict(double *z, const double *zold, double *zprev, double *zprev2, size_t n, int order,
-                    cudaStream_t st);
+// polynomial extrapolation of order `order` through zold, zprev, zprev2,
+// zprev3 (0 none, 1 linear, 2 quadratic, 3 cubic), then the history shifts:
+// zprev3 <- zprev2 <- zprev <- zold.
+void launch_predict(double *z, const double *zold, double *zprev, double *zprev2, double *zprev3, size_t n,
+                    int order, cudaStream_t st);
 void launch_update(const DevProblem &P, const DevWork &W, const DevSym &S, const int *perm, cudaStream_t st);
 void launch_events(const DevProblem &P, const DevWork &W, const int *fl_on_step, const int *fl_off_step,
                    const int *fl_scen, uint8_t *fl_on, int n_fl, int step, cudaStream_t st);

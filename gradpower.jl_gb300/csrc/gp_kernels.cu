@@ -24,6 +24,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "gp_devices.cuh"
 #include "gp_internal.h"
 
@@ -496,13 +498,28 @@ void launch_reset_norm(const DevProblem &P, const DevWork &W, const DevMixed &Mx
 // Start of a Newton solve of the mixed solver: scenarios whose factors have
 // served max_age solves, or every scenario when `force` (first solve, event
 // re-solves and the solve after them), refresh them at the first iteration;
-// a retried solve is exact from its first iteration.
-__global__ void mixed_start_kernel(DevWork W, DevMixed Mx, int M, int force) {
-    int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= M || !W.active[m]) return;
-    if (Mx.all_exact[m]) Mx.refac_next[m] = MX_EXACT;
-    else if (force || Mx.age[m] >= Mx.max_age) Mx.refac_next[m] = MX_FP32;
-    Mx.age[m] += 1;
+// a retried solve is exact from its first iteration.  Refreshes are taken
+// together: a refresh costs one factorisation launch whatever the number of
+// scenarios in it, so when one scenario refreshes, every scenario does.
+// One CTA, so that the decision can be shared.
+__global__ void __launch_bounds__(1024) mixed_start_kernel(DevWork W, DevMixed Mx, int M, int force) {
+    bool any = false;
+    for (int m = threadIdx.x; m < M; m += blockDim.x) {
+        if (!W.active[m]) continue;
+        if (Mx.all_exact[m]) Mx.refac_next[m] = MX_EXACT;
+        else if (force || Mx.age[m] >= Mx.max_age) {
+            Mx.refac_next[m] = MX_FP32;
+            any = true;
+        }
+        Mx.age[m] += 1;
+    }
+    if (__syncthreads_or(any))
+        for (int m = threadIdx.x; m < M; m += blockDim.x)
+            if (W.active[m] && Mx.refac_next[m] == MX_KEEP) Mx.refac_next[m] = MX_FP32;
+}
+
+void launch_mixed_start(const DevProblem &P, const DevWork &W, const DevMixed &Mx, int force, cudaStream_t st) {
+    mixed_start_kernel<<<1, std::min(1024, (P.M + 31) / 32 * 32), 0, st>>>(W, Mx, P.M, force);
 }
 
 // Restart of the solves marked for a retry: the state goes back to the
@@ -521,19 +538,22 @@ __global__ void retry_start_kernel(DevProblem P, DevWork W, DevMixed Mx) {
     }
 }
 
-__global__ void predict_kernel(double *z, const double *zold, double *zprev, double *zprev2, size_t n, int order) {
+__global__ void predict_kernel(double *z, const double *zold, double *zprev, double *zprev2, double *zprev3, size_t n,
+                               int order) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double a = zold[i], b = zprev[i];
+    const double a = zold[i], b = zprev[i], c = zprev2[i];
     if (order == 1) z[i] = 2.0 * a - b;
-    else if (order == 2) z[i] = 3.0 * (a - b) + zprev2[i];
+    else if (order == 2) z[i] = 3.0 * (a - b) + c;
+    else if (order == 3) z[i] = 4.0 * (a + c) - 6.0 * b - zprev3[i];
+    zprev3[i] = c;
     zprev2[i] = b;
     zprev[i] = a;
 }
 
-void launch_predict(double *z, const double *zold, double *zprev, double *zprev2, size_t n, int order,
-                    cudaStream_t st) {
-    predict_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(z, zold, zprev, zprev2, n, order);
+void launch_predict(double *z, const double *zold, double *zprev, double *zprev2, double *zprev3, size_t n,
+                    int order, cudaStream_t st) {
+    predict_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(z, zold, zprev, zprev2, zprev3, n, order);
 }
 
 void launch_retry_start(const DevProblem &P, const DevWork &W, const DevMixed &Mx, cudaStream_t st) {
@@ -541,9 +561,6 @@ void launch_retry_start(const DevProblem &P, const DevWork &W, const DevMixed &M
     retry_start_kernel<<<(int)((tasks + 255) / 256), 256, 0, st>>>(P, W, Mx);
 }
 
-void launch_mixed_start(const DevProblem &P, const DevWork &W, const DevMixed &Mx, int force, cudaStream_t st) {
-    mixed_start_kernel<<<(P.M + 255) / 256, 256, 0, st>>>(W, Mx, P.M, force);
-}
 
 // Convergence test (infinity norm of the FP64 residual), the itermax and
 // non-finite checks, and for the mixed solver the mode of the next
@@ -556,50 +573,58 @@ void launch_mixed_start(const DevProblem &P, const DevWork &W, const DevMixed &M
 //    takes exact Newton steps (fresh FP64 factors) until the solve ends;
 //  - so does every scenario still iterating after exact_after iterations.
 // A scenario that went exact refreshes its kept factors at the next solve.
+// When one scenario refreshes, every scenario on kept factors does.
 // A mixed solve that ends at itermax or on a non-finite residual with
 // inexact steps is not reported: it is marked for a retry from the step's
 // starting point with exact Newton steps, whose outcome is reported.
-__global__ void check_kernel(DevWork W, DevMixed Mx, int M, double tol, int itermax) {
-    int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= M || !W.active[m]) return;
-    const unsigned long long bits = W.norm[m];
-    const double nrm = __longlong_as_double((long long)bits);
-    const bool can_retry = Mx.on && !Mx.all_exact[m];
-    if (nrm < tol) {
-        W.active[m] = 0;
-    } else if (bits >= 0x7ff0000000000000ull || W.iters[m] >= itermax) {
-        W.active[m] = 0;
-        if (can_retry) {
-            Mx.retry[m] = 1;
-            atomicAdd(W.flag + 3, 1);
+__global__ void __launch_bounds__(1024) check_kernel(DevWork W, DevMixed Mx, int M, double tol, int itermax) {
+    bool any = false;
+    for (int m = threadIdx.x; m < M; m += blockDim.x) {
+        if (!W.active[m]) continue;
+        const unsigned long long bits = W.norm[m];
+        const double nrm = __longlong_as_double((long long)bits);
+        const bool can_retry = Mx.on && !Mx.all_exact[m];
+        if (nrm < tol) {
+            W.active[m] = 0;
+        } else if (bits >= 0x7ff0000000000000ull || W.iters[m] >= itermax) {
+            W.active[m] = 0;
+            if (can_retry) {
+                Mx.retry[m] = 1;
+                atomicAdd(W.flag + 3, 1);
+            } else {
+                W.status[m] |= bits >= 0x7ff0000000000000ull ? 2 : 1;
+            }
         } else {
-            W.status[m] |= bits >= 0x7ff0000000000000ull ? 2 : 1;
+            if (Mx.on) {
+                const int cur = Mx.refac[m], used = Mx.prev_mode[m];
+                const bool stepped = W.iters[m] > 0;
+                int next = MX_KEEP;
+                if (cur == MX_EXACT || W.iters[m] + 1 >= Mx.exact_after ||
+                    (stepped && used == MX_FP32 && nrm > 0.5 * Mx.prev_norm[m]))
+                    next = MX_EXACT;
+                else if (stepped && used == MX_KEEP && nrm > Mx.rho_max * Mx.prev_norm[m])
+                    next = MX_FP32;
+                if (next == MX_EXACT) Mx.age[m] = Mx.max_age;
+                if (next == MX_FP32) any = true;
+                Mx.refac_next[m] = (uint8_t)next;
+                Mx.prev_mode[m] = (uint8_t)cur;
+                Mx.prev_norm[m] = nrm;
+                if (cur == MX_FP32) atomicAdd(W.flag + 1, 1);
+                else if (cur == MX_EXACT) atomicAdd(W.flag + 2, 1);
+            }
+            W.iters[m] += 1;
+            atomicAdd(W.flag, 1);
         }
-    } else {
-        if (Mx.on) {
-            const int cur = Mx.refac[m], used = Mx.prev_mode[m];
-            const bool stepped = W.iters[m] > 0;
-            int next = MX_KEEP;
-            if (cur == MX_EXACT || W.iters[m] + 1 >= Mx.exact_after ||
-                (stepped && used == MX_FP32 && nrm > 0.5 * Mx.prev_norm[m]))
-                next = MX_EXACT;
-            else if (stepped && used == MX_KEEP && nrm > Mx.rho_max * Mx.prev_norm[m])
-                next = MX_FP32;
-            if (next == MX_EXACT) Mx.age[m] = Mx.max_age;
-            Mx.refac_next[m] = (uint8_t)next;
-            Mx.prev_mode[m] = (uint8_t)cur;
-            Mx.prev_norm[m] = nrm;
-            if (cur == MX_FP32) atomicAdd(W.flag + 1, 1);
-            else if (cur == MX_EXACT) atomicAdd(W.flag + 2, 1);
-        }
-        W.iters[m] += 1;
-        atomicAdd(W.flag, 1);
     }
+    // refreshes are taken together (see mixed_start_kernel)
+    if (Mx.on && __syncthreads_or(any))
+        for (int m = threadIdx.x; m < M; m += blockDim.x)
+            if (W.active[m] && Mx.refac_next[m] == MX_KEEP) Mx.refac_next[m] = MX_FP32;
 }
 
 void launch_check(const DevProblem &P, const DevWork &W, const DevMixed &Mx, double tol, int itermax,
                   cudaStream_t st) {
-    check_kernel<<<(P.M + 255) / 256, 256, 0, st>>>(W, Mx, P.M, tol, itermax);
+    check_kernel<<<1, std::min(1024, (P.M + 31) / 32 * 32), 0, st>>>(W, Mx, P.M, tol, itermax);
 }
 
 // ---------------------------------------------------------------------------

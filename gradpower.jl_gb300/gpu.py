@@ -126,9 +126,10 @@ class GpuBatchedLayout:
         keys = ("n_red", "nnz_S", "nnz_LU", "supernodes", "levels", "factor_flops", "sum_w2", "max_front")
         return dict(zip(keys, (int(v) for v in out)))
 
-    def set_mixed_policy(self, max_age: int = 1, rho_max: float = 0.9, exact_after: int = 8, predict: int = 2):
+    def set_mixed_policy(self, max_age: int = 1, rho_max: float = 0.9, exact_after: int = 8, predict: int = 3):
         """Policy of the mixed-precision solver (see gp_set_mixed_policy in
-        include/gradpower_gb300.h); predict: 0 none, 1 linear, 2 quadratic."""
+        include/gradpower_gb300.h); predict: degree of the extrapolated first
+        iterate of a step, 0 (none) to 3 (cubic)."""
         _check(library().gp_set_mixed_policy(self._h, int(max_age), float(rho_max), int(exact_after), int(predict)))
 
     def timing(self) -> dict:

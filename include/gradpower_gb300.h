@@ -252,7 +252,9 @@ int32_t gp_adjoint(gp_layout *L, const gp_options *opt, int32_t n_faults, const 
  * solvers refactor every iteration):
  *  - a scenario refreshes its kept FP32 factors at the start of a solve once
  *    they have served max_age solves, and after an iteration that reduced
- *    the residual by less than the factor rho_max;
+ *    the residual by less than the factor rho_max; refreshes are taken
+ *    together (when one scenario refreshes, every scenario on kept factors
+ *    does: the factorisation launch costs the same);
  *  - a scenario still iterating after exact_after iterations of one solve
  *    takes exact Newton steps with fresh FP64 factors until that solve ends
  *    (its kept factors are refreshed at the next solve), so that a system
@@ -261,13 +263,13 @@ int32_t gp_adjoint(gp_layout *L, const gp_options *opt, int32_t n_faults, const 
  *    non-finite residual) after inexact steps is redone from the step's
  *    starting point with exact Newton steps only, and that outcome is the
  *    one reported;
- *  - predict = 1 starts every step whose two previous states lie on one
- *    smooth stretch (no event re-solve in between) from their linear
- *    extrapolation instead of the previous state, predict = 2 from the
- *    quadratic one through three states when there are three (linear with
- *    two): the same backward-Euler equations and convergence test, a closer
- *    initial iterate; predict = 0 starts from the previous state.
- * Defaults: max_age 1, rho_max 0.9, exact_after 8, predict 2. */
+ *  - predict = p > 0 starts every step from the polynomial extrapolation,
+ *    of degree at most p (1 linear, 2 quadratic, 3 cubic), through the
+ *    previous states that lie on the current smooth stretch (no event
+ *    re-solve in between) instead of from the previous state: the same
+ *    backward-Euler equations and convergence test, a closer initial
+ *    iterate; predict = 0 starts from the previous state.
+ * Defaults: max_age 1, rho_max 0.9, exact_after 8, predict 3. */
 int32_t gp_set_mixed_policy(gp_layout *L, int32_t max_age, double rho_max, int32_t exact_after, int32_t predict);
 
 /* gp_residual with no fault applied, computed without allocating anything:
