@@ -138,6 +138,7 @@ struct gp_layout {
     // scenario refreshes its FP32 factors, bit 1: some scenario uses FP64)
     cudaGraphExec_t g_mix[4] = {};
     int solve_graph_launches = 0, mix_launches[4] = {}, mix_factor_launches[4] = {};
+    int eval_launches = 4;        // kernels of the evaluation graph
     double refreshes = 0.0;                   // mixed: scenario FP32 factor refreshes in the last call
     double exact_iters = 0.0;                 // mixed: scenario iterations with FP64 factors
     double retries = 0.0;                     // mixed: scenario solves redone exactly
@@ -1014,13 +1015,13 @@ void build_work(gp_layout *L, const double *z0, const double *u0, const double *
         ck(cudaMemcpy(S.ipiv, ident.data(), ident.size() * sizeof(int), cudaMemcpyHostToDevice), "ipiv");
     }
     gp::DevDag &D = L->D;
-    D.ctr = A.alloc<int>(4);
+    D.ctr = A.alloc<int>(8);
     D.epoch = A.alloc<int>(1);
     D.err = A.alloc<int>(1);
     D.fdone = A.alloc<int>(M * D.nsup);
     D.xdone = A.alloc<int>(M * D.nsup);
     D.bdone = A.alloc<int>(M * D.nsup);
-    ck(cudaMemset(D.ctr, 0, 4 * sizeof(int)), "memset");
+    ck(cudaMemset(D.ctr, 0, 8 * sizeof(int)), "memset");
     ck(cudaMemset(D.epoch, 0, sizeof(int)), "memset");
     ck(cudaMemset(D.err, 0, sizeof(int)), "memset");
     ck(cudaMemset(D.fdone, 0, M * D.nsup * sizeof(int)), "memset");
@@ -1057,6 +1058,7 @@ void build_clusters(gp_layout *L, const gp_problem *pr, const double *z0, const 
     C.slot_of = A.upload(cp.slot_of);
     C.prog_ptr = A.upload(cp.prog_ptr);
     C.prog_mid = A.upload(cp.prog_mid);
+    C.prog_sol = A.upload(cp.prog_sol);
     C.ops = A.upload(cp.ops);
     C.rhs_base = A.upload(cp.rhs_base);
     C.nslot = A.upload(cp.nslot);
@@ -1077,6 +1079,8 @@ void build_clusters(gp_layout *L, const gp_problem *pr, const double *z0, const 
         C.row_pos = A.upload(row_pos);
     }
     C.max_slots = cp.max_slots;
+    C.max_w = 1;
+    for (int w : cp.cls_W) C.max_w = std::max(C.max_w, w);
     const int bytes = cp.max_slots * 32 * (int)sizeof(double);
     if (bytes > 48 * 1024 && (gp::cluster_smem_optin(bytes) < 0 || gp::adj_smem_optin(bytes) < 0))
         fail(GP_E_CUDA, "cluster kernel needs %d bytes of shared memory", bytes);
@@ -1149,7 +1153,7 @@ int enqueue_solve(gp_layout *L, int variant, int *nfac_out) {
     const gp::DevDag &D = L->D;
     const int nfac = (D.n_small > 0) + (D.nsup > D.n_small);
     const gp::DevBlk &B = L->B;
-    const int nsolve = (B.nblk > 0) + (B.n_top > 0);
+    const int nsolve = (B.nblk + B.n_top) > 0;   // one fused kernel per direction
     int launches = 2, facs = 0;   // dag_begin, update
     mark(L, 3);
     gp::launch_dag_begin(D, L->st);
@@ -1193,7 +1197,7 @@ int enqueue_solve(gp_layout *L, int variant, int *nfac_out) {
 void enqueue_eval(gp_layout *L, double tol, int itermax) {
     gp::launch_reset_norm(L->P, L->W, L->Mx, L->st);
     mark(L, 0);
-    gp::launch_cluster(L->P, L->W, L->C, L->Mx, 0, L->st);
+    L->eval_launches = 3 + gp::launch_cluster(L->P, L->W, L->C, L->Mx, 0, L->st);
     mark(L, 1);
     gp::launch_network(L->P, L->W, L->Mx, 0, L->st);
     mark(L, 2);
@@ -1299,7 +1303,7 @@ void newton(gp_layout *L, double dt, double tol, int itermax, bool force_refresh
     for (int guard = 0; guard <= itermax + 1; guard++) {
         ck(cudaGraphLaunch(L->g_eval, L->st), "graph launch");
         ck(cudaStreamSynchronize(L->st), "newton sync");
-        L->launches += 4;
+        L->launches += L->eval_launches;
         L->ph_ms[0] += elapsed(L->pev[0], L->pev[1]);
         L->ph_ms[1] += elapsed(L->pev[1], L->pev[2]);
         if (solve_pending) {
@@ -1721,6 +1725,8 @@ int32_t gp_reduced_selftest(const gp_problem *prob, const int32_t *s_rowptr, con
     out[5] = hb.nblk;
     out[6] = hb.n_top_levels;
     out[7] = hb.max_n;
+    out[9] = hb.top_order.empty() ? 0 : hb.top_max_front;
+    out[10] = hb.max_v;
     // S^T from the transposed assembly lists (the adjoint's system):
     // relative residual of S^T y = rhs
     {

@@ -154,6 +154,7 @@ void make_cluster_plan(const gp_problem *pr, const double *z0, const double *u0,
     pl.pos3.assign((size_t)pl.n_class * 3, 0);
     pl.prog_ptr.assign(1, 0);
     pl.prog_mid.clear();
+    pl.prog_sol.clear();
     pl.rhs_base.clear();
     pl.nslot.clear();
     pl.ops.clear();
@@ -294,6 +295,7 @@ void make_cluster_plan(const gp_problem *pr, const double *z0, const double *u0,
                     for (int j = k + 1; j < W; j++)
                         if (Q[k][j]) { op(OP_FMS, slot[i][j], slot[i][k], slot[k][j]); fl++; }
         }
+        pl.prog_sol.push_back((int)pl.ops.size());
         for (int k = 0; k < W; k++)
             for (int i = k + 1; i < W; i++)
                 if (Q[i][k]) { op(OP_FMS3, i, slot[i][k], k); fl += 3; }

@@ -24,7 +24,7 @@ struct ClusterPlan {
     std::vector<int> cluster_class;                  // per problem cluster (-1 trivial)
     std::vector<int> task_class, task_first, task_count, order;   // order: problem cluster ids
     std::vector<short> slot_of;                      // [class][1024]
-    std::vector<int> prog_ptr, prog_mid, rhs_base, nslot, perm_col, pos3;
+    std::vector<int> prog_ptr, prog_mid, prog_sol, rhs_base, nslot, perm_col, pos3;
     std::vector<CluOp> ops;
     int64_t lu_flops = 0;                            // per scenario, all clusters (FMA count)
 };

@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(kThreads, 3) factor_big_kernel(DevProblem P, D
 // previous solve no longer match.  The error flag stays raised until the
 // host clears it.
 __global__ void dag_begin_kernel(DevDag D) {
-    if (threadIdx.x < 4) D.ctr[threadIdx.x] = 0;
+    if (threadIdx.x < 8) D.ctr[threadIdx.x] = 0;
     if (threadIdx.x == 0) *D.epoch += 1;
 }
 

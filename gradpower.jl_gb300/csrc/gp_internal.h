@@ -83,6 +83,7 @@ struct DevClu {
     const short *slot_of;       // [class][32*32] slot of local entry (r, c); c = 29/30 B, 31 f
     const int *prog_ptr;        // [n_class+1]
     const int *prog_mid;        // [n_class] first op of the factorisation part
+    const int *prog_sol;        // [n_class] first op of the solve part (after the factorisation)
     const CluOp *ops;
     const int *rhs_base;        // [n_class] first right-hand-side slot
     const int *nslot;           // [n_class] slots used (values + pivots + 3 W)
@@ -90,6 +91,7 @@ struct DevClu {
     const int *pos3;            // [class][3] solution positions of delta, i_q, i_d
     const int *row_pos;         // [class][32] position of local row r in the program
     int max_slots;
+    int max_w;                  // widest class
     // adjoint: when set, the cluster kernel also saves its FP64 LU values
     // ([M][n_tasks][n_save][32]) and the coupling rows C ([M][n_cl][6])
     double *save_lu, *save_cc;
@@ -137,7 +139,8 @@ struct DevDag {
     const int *order;       // [nsup]
     const int *rank;        // [nsup] position in order
     const int *parent;      // [nsup] parent supernode or -1
-    int *ctr;               // [4] claim counters: small factor, big factor, forward solve, backward solve
+    int *ctr;               // [8] claim counters: small factor, big factor, forward top, backward top,
+                            //     forward blocks, backward blocks
     int *epoch;             // [1] current solve
     int *err;               // [1] a wait gave up (sticky until the host clears it)
     int *fdone, *xdone, *bdone;   // [nsup][M] epoch at which the task finished
@@ -211,7 +214,7 @@ void launch_solve_bwd(const DevProblem &P, const DevWork &W, const DevSym &S, co
 int solve_block_front_limit();
 
 // launches (gp_kernels.cu)
-void launch_cluster(const DevProblem &P, const DevWork &W, const DevClu &C, const DevMixed &Mx, int want_f,
+int launch_cluster(const DevProblem &P, const DevWork &W, const DevClu &C, const DevMixed &Mx, int want_f,
                     cudaStream_t st);
 void launch_network(const DevProblem &P, const DevWork &W, const DevMixed &Mx, int want_f, cudaStream_t st);
 void launch_check(const DevProblem &P, const DevWork &W, const DevMixed &Mx, double tol, int itermax,

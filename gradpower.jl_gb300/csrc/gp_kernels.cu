@@ -74,17 +74,6 @@ __device__ __forceinline__ DevRef devref(const DTab &T, int k) {
     return d;
 }
 
-// Sink of a residual-only evaluation: Jacobian entries are dropped (the
-// compiler removes their arithmetic), residuals go to their slots.
-struct ResidualSink {
-    double *v;
-    const short *slot_of;
-    int ws, lane;
-    __device__ __forceinline__ void put(int, int, double) {}
-    __device__ __forceinline__ void putv(int, int, double) {}
-    __device__ __forceinline__ void putf(int r, double x) { v[(int)slot_of[(r - ws) * 32 + 31] * 32 + lane] = x; }
-};
-
 template <class Sink>
 __device__ __forceinline__ void eval_cluster(const DevProblem &P, int c, const double *z, const double *u0,
                                              const double *p, Sink &sink, double Cc[6], double Ic[2]) {
@@ -100,15 +89,16 @@ __device__ __forceinline__ void eval_cluster(const DevProblem &P, int c, const d
 
 // Modes per scenario: 0 exact Newton (Jacobian block, FP64 LU, three solves;
 // also the mixed solver's MX_EXACT); 1 the same, and the LU values and
-// coupling rows are kept in FP32 for the following iterations (MX_FP32);
-// 2 residual only, solved with the kept FP32 LU (MX_KEEP: the kept A^-1 B
-// columns and C A^-1 B terms stay as they are).
+// coupling rows are kept in FP32 for the following iterations (MX_FP32).
+// The mixed solver's MX_KEEP scenarios (residual only, solved with the kept
+// FP32 LU) run cluster_keep_kernel instead.
 __global__ void __launch_bounds__(32) cluster_kernel(DevProblem P, DevWork W, DevClu Cl, DevMixed Mx, int want_f) {
     extern __shared__ double vals[];
     const int task = blockIdx.x, m = blockIdx.y, lane = threadIdx.x;
     if (!W.active[m]) return;
     const int r = Mx.on ? Mx.refac[m] : MX_EXACT;
-    const int mode = r == MX_KEEP ? 2 : (r == MX_FP32 ? 1 : 0);
+    if (r == MX_KEEP) return;
+    const int mode = r == MX_FP32 ? 1 : 0;
     const int cls = Cl.task_class[task];
     const int cnt = Cl.task_count[task];
     const bool act = lane < cnt;
@@ -124,14 +114,9 @@ __global__ void __launch_bounds__(32) cluster_kernel(DevProblem P, DevWork W, De
     const CluOp *ops = Cl.ops;
     const int q0 = Cl.prog_ptr[cls], qm = Cl.prog_mid[cls], q1 = Cl.prog_ptr[cls + 1];
     if (act) {
-        if (mode == 2) {
-            ResidualSink sink{vals, Cl.slot_of + (size_t)cls * 1024, ws, lane};
-            eval_cluster(P, c, z, u0, p, sink, Cc, Ic);
-        } else {
-            LaneSink sink{vals, Cl.slot_of + (size_t)cls * 1024, ws, lane};
-            eval_cluster(P, c, z, u0, p, sink, Cc, Ic);
-        }
-    } else if (mode != 2) {
+        LaneSink sink{vals, Cl.slot_of + (size_t)cls * 1024, ws, lane};
+        eval_cluster(P, c, z, u0, p, sink, Cc, Ic);
+    } else {
         // idle lanes factor an identity so that no lane divides by zero
         for (int q = qm; q < q1; q++)
             if (ops[q].code == OP_RCP) vals[ops[q].a * 32 + lane] = 1.0;
@@ -169,15 +154,7 @@ __global__ void __launch_bounds__(32) cluster_kernel(DevProblem P, DevWork W, De
     }
     if (lane == 0) atomicMax(W.norm + m, nb);
     float *keep = Mx.on ? Mx.lu + (((size_t)m * Cl.n_tasks + task) * Mx.n_lu) * 32 + lane : nullptr;
-    if (mode == 2) {
-        // kept LU values; the solve of the residual column alone
-        for (int s = 0; s < rb; s++) vals[s * 32 + lane] = (double)keep[s * 32];
-        for (int q = qm; q < q1; q++) {
-            const CluOp o = ops[q];
-            if (o.code == OP_FMS3) R2[o.d * 32 + lane] -= vals[o.a * 32 + lane] * R2[o.b * 32 + lane];
-            else if (o.code == OP_MUL3) R2[o.d * 32 + lane] *= vals[o.a * 32 + lane];
-        }
-    } else {
+    {
         // factorisation and solves
         for (int q = qm; q < q1; q++) {
             const CluOp o = ops[q];
@@ -224,15 +201,6 @@ __global__ void __launch_bounds__(32) cluster_kernel(DevProblem P, DevWork W, De
     double Y[3];
 #pragma unroll
     for (int t = 0; t < 3; t++) Y[t] = R2[p3[t] * 32 + lane];
-    if (mode == 2) {
-        for (int j = 0; j < Wn; j++) yx[pc[j]] = R2[j * 32 + lane];
-        const float *cc = Mx.cc + ((size_t)m * P.n_cl + c) * 6;
-        o[4] = (double)cc[0] * Y[0] + (double)cc[1] * Y[1] + (double)cc[2] * Y[2];
-        o[5] = (double)cc[3] * Y[0] + (double)cc[4] * Y[1] + (double)cc[5] * Y[2];
-        o[6] = Ic[0];
-        o[7] = Ic[1];
-        return;
-    }
     for (int j = 0; j < Wn; j++) {
         const int st = pc[j];
         yx[st] = R2[j * 32 + lane];
@@ -263,11 +231,115 @@ __global__ void __launch_bounds__(32) cluster_kernel(DevProblem P, DevWork W, De
     }
 }
 
-void launch_cluster(const DevProblem &P, const DevWork &W, const DevClu &C, const DevMixed &Mx, int want_f,
-                    cudaStream_t st) {
-    if (C.n_tasks == 0) return;
+// MX_KEEP scenarios of the mixed solver: the residual and its solve with the
+// kept FP32 LU, nothing else.  The same operations in the same order as
+// cluster_kernel's mode 2 (so the same results), but only the residual
+// column is staged in shared memory (W doubles per lane instead of the whole
+// program's slots), the LU values are read straight from the kept copy, and
+// the op list is the solve part of the program alone: many more warps fit
+// on an SM.
+// Sink of a residual-only evaluation: Jacobian entries are dropped (the
+// compiler removes their arithmetic), residuals go to their positions in the
+// staged residual column.
+struct KeepSink {
+    double *v;
+    const short *slot_of;
+    int ws, lane, base;
+    __device__ __forceinline__ void put(int, int, double) {}
+    __device__ __forceinline__ void putv(int, int, double) {}
+    __device__ __forceinline__ void putf(int r, double x) {
+        v[((int)slot_of[(r - ws) * 32 + 31] - base) * 32 + lane] = x;
+    }
+};
+
+__global__ void __launch_bounds__(32, 16) cluster_keep_kernel(DevProblem P, DevWork W, DevClu Cl, DevMixed Mx,
+                                                             int want_f) {
+    extern __shared__ double R2[];   // [W][32] residual, by pivot position
+    const int task = blockIdx.x, m = blockIdx.y, lane = threadIdx.x;
+    if (!W.active[m] || Mx.refac[m] != MX_KEEP) return;
+    const int cls = Cl.task_class[task];
+    const int cnt = Cl.task_count[task];
+    const bool act = lane < cnt;
+    const int c = act ? Cl.order[Cl.task_first[task] + lane] : Cl.order[Cl.task_first[task]];
+    const int ws = P.cl_w_start[c], Wn = P.cl_w_size[c];
+    const int rb = Cl.rhs_base[cls], base = rb + 2 * Wn;
+    for (int j = 0; j < Wn; j++) R2[j * 32 + lane] = 0.0;
+    const double *z = W.z + (size_t)m * P.n_sys;
+    const double *zold = W.zold + (size_t)m * P.n_sys;
+    double Cc[6] = {0, 0, 0, 0, 0, 0}, Ic[2] = {0, 0};
+    if (act) {
+        KeepSink sink{R2, Cl.slot_of + (size_t)cls * 1024, ws, lane, base};
+        eval_cluster(P, c, z, W.u0 + (size_t)m * P.n_ctrl, W.p + (size_t)m * P.n_par, sink, Cc, Ic);
+    }
+    const double dt = *W.dt;
+    const CluOp *ops = Cl.ops;
+    const int q0 = Cl.prog_ptr[cls], qm = Cl.prog_mid[cls], qs = Cl.prog_sol[cls], q1 = Cl.prog_ptr[cls + 1];
+    for (int q = q0; q < qm; q++) {
+        const CluOp o = ops[q];
+        if (o.code == OP_BEF) {
+            double *vd = R2 + (o.d - base) * 32 + lane;
+            *vd = act ? z[ws + o.a] - zold[ws + o.a] - dt * *vd : 0.0;
+        }
+    }
+    unsigned long long nb = 0ull;
+    for (int j = 0; j < Wn; j++) {
+        const unsigned long long t = norm_bits(R2[j * 32 + lane]);
+        nb = t > nb ? t : nb;
+    }
+    if (!act) nb = 0ull;
+    if (want_f && act) {
+        for (int q = q0; q < qm; q++)
+            if (ops[q].code == OP_BEF || ops[q].code == OP_ROW)
+                W.f[(size_t)m * P.n_sys + ws + ops[q].a] = R2[(ops[q].d - base) * 32 + lane];
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(FULL_MASK, nb, off);
+        nb = o > nb ? o : nb;
+    }
+    if (lane == 0) atomicMax(W.norm + m, nb);
+    // the solves (OP_FMS3 / OP_MUL3 on the residual column), eight ops and
+    // their LU values loaded ahead of the arithmetic
+    const float *kl = Mx.lu + (((size_t)m * Cl.n_tasks + task) * Mx.n_lu) * 32 + lane;
+    constexpr int kAhead = 8;
+    for (int q = qs; q < q1; q += kAhead) {
+        CluOp o[kAhead];
+        double l[kAhead];
+#pragma unroll
+        for (int u = 0; u < kAhead; u++) {
+            o[u] = ops[min(q + u, q1 - 1)];
+            l[u] = (double)kl[o[u].a * 32];
+        }
+#pragma unroll
+        for (int u = 0; u < kAhead; u++) {
+            if (q + u >= q1) break;
+            if (o[u].code == OP_FMS3) R2[o[u].d * 32 + lane] -= l[u] * R2[o[u].b * 32 + lane];
+            else R2[o[u].d * 32 + lane] *= l[u];
+        }
+    }
+    if (!act) return;
+    const int n_da = P.n_diff + P.n_alg;
+    double *yx = W.yx + (size_t)m * 3 * n_da + ws;
+    const int *pc = Cl.perm_col + cls * 32;
+    const int *p3 = Cl.pos3 + cls * 3;
+    for (int j = 0; j < Wn; j++) yx[pc[j]] = R2[j * 32 + lane];
+    const double Y0 = R2[p3[0] * 32 + lane], Y1 = R2[p3[1] * 32 + lane], Y2 = R2[p3[2] * 32 + lane];
+    const float *cc = Mx.cc + ((size_t)m * P.n_cl + c) * 6;
+    double *o = W.clout + ((size_t)m * P.n_cl + c) * 8;
+    o[4] = (double)cc[0] * Y0 + (double)cc[1] * Y1 + (double)cc[2] * Y2;
+    o[5] = (double)cc[3] * Y0 + (double)cc[4] * Y1 + (double)cc[5] * Y2;
+    o[6] = Ic[0];
+    o[7] = Ic[1];
+}
+
+int launch_cluster(const DevProblem &P, const DevWork &W, const DevClu &C, const DevMixed &Mx, int want_f,
+                   cudaStream_t st) {
+    if (C.n_tasks == 0) return 0;
     dim3 grid(C.n_tasks, P.M);
     cluster_kernel<<<grid, 32, (size_t)C.max_slots * 32 * sizeof(double), st>>>(P, W, C, Mx, want_f);
+    if (!Mx.on) return 1;
+    cluster_keep_kernel<<<grid, 32, (size_t)C.max_w * 32 * sizeof(double), st>>>(P, W, C, Mx, want_f);
+    return 2;
 }
 
 int cluster_smem_optin(int bytes) {

@@ -46,7 +46,7 @@ namespace {
 constexpr unsigned FULL = kFullMask;
 constexpr int kBlkWarps = 4;   // block tasks per CTA
 constexpr int kTopThreads = 128;             // threads of a top-region task
-constexpr int kTopStage = 64 * 1024;         // shared memory for a task's factor columns
+constexpr int kTopStage = 20 * 1024;         // shared memory for a task's factor columns
 constexpr int kMaxJ = 8;       // register rows per lane: fronts up to 256 rows
 constexpr int kBlkFront = 64;  // largest front inside a block (two rows per lane)
 
@@ -382,24 +382,6 @@ __device__ void fwd_block(const DevProblem &P, const DevWork &W, const DevSym &S
     }
 }
 
-__global__ void __launch_bounds__(32 * kBlkWarps, 8) fwd_blocks_kernel(DevProblem P, DevWork W, DevSym S, DevBlk B,
-                                                                     FrontSel fs) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const int warp = threadIdx.x >> 5;
-    const long long task = (long long)blockIdx.x * kBlkWarps + warp;
-    if (task >= (long long)B.nblk * P.M) return;
-    const int blk = (int)(task / P.M), m = (int)(task % P.M);
-    if (!W.active[m]) return;
-    const bool d = use64(fs, m);
-    if (d && fs.fused64) return;
-    const BlkLayout lay = blk_layout(B);
-    unsigned char *base = smem + (size_t)warp * lay.total;
-    const BlkTask t = stage_block(S, B, blk, m, base, lay, B.map_fwd, true);
-    __syncwarp();
-    if (d) fwd_block<double>(P, W, S, fs, t, m, reinterpret_cast<double *>(base + lay.v));
-    else fwd_block<float>(P, W, S, fs, t, m, reinterpret_cast<float *>(base + lay.v));
-}
-
 template <class T>
 __device__ void bwd_block(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B,
                           const FrontSel &fs, const BlkTask &t, int blk, int m, T *vs) {
@@ -423,22 +405,6 @@ __device__ void bwd_block(const DevProblem &P, const DevWork &W, const DevSym &S
         bwd_front_blk<T>(fr + t.FO[q], ns, ns + r, v);
         for (int i = lane; i < ns; i += 32) x[a.y + i] = (double)v[i];
     }
-}
-
-__global__ void __launch_bounds__(32 * kBlkWarps, 8) bwd_blocks_kernel(DevProblem P, DevWork W, DevSym S, DevBlk B,
-                                                                     FrontSel fs) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const int warp = threadIdx.x >> 5;
-    const long long task = (long long)blockIdx.x * kBlkWarps + warp;
-    if (task >= (long long)B.nblk * P.M) return;
-    const int blk = (int)(task / P.M), m = (int)(task % P.M);
-    if (!W.active[m]) return;
-    const BlkLayout lay = blk_layout(B);
-    unsigned char *base = smem + (size_t)warp * lay.total;
-    const BlkTask t = stage_block(S, B, blk, m, base, lay, B.map_bwd, false);
-    __syncwarp();
-    if (use64(fs, m)) bwd_block<double>(P, W, S, B, fs, t, blk, m, reinterpret_cast<double *>(base + lay.v));
-    else bwd_block<float>(P, W, S, B, fs, t, blk, m, reinterpret_cast<float *>(base + lay.v));
 }
 
 // ---- top region: dataflow of CTA tasks ------------------------------------
@@ -470,8 +436,8 @@ __device__ __forceinline__ TopCtx top_ctx(const DevSym &S, int s, int m, int ran
     return c;
 }
 
-// Waits (warp 0) on the done flags of the top-region children; false when
-// a wait gave up.  Ends with a CTA barrier.
+// Waits (warp 0) on the done flags of the children (block roots and top
+// supernodes); false when a wait gave up.  Ends with a CTA barrier.
 __device__ bool wait_top_children(const DevSym &S, const DevBlk &B, const DevDag &D, int s, int m, int M, int epoch,
                                   int *s_ok) {
     if (threadIdx.x < 32) {
@@ -480,7 +446,7 @@ __device__ bool wait_top_children(const DevSym &S, const DevBlk &B, const DevDag
         bool ok = true;
         for (int q = lane; q < nc; q += 32) {
             const int c = S.children[c0 + q];
-            if (B.top_rank[c] >= 0) ok = wait_epoch(D.xdone + (size_t)c * M + m, epoch, D.err) && ok;
+            ok = wait_epoch(D.xdone + (size_t)c * M + m, epoch, D.err) && ok;
         }
         ok = __all_sync(FULL, ok);
         if (lane == 0) *s_ok = ok;
@@ -583,12 +549,49 @@ __device__ void bwd_top_task(const DevProblem &P, const DevWork &W, const DevSym
     for (int i = threadIdx.x; i < t.ns; i += blockDim.x) x[t.start + i] = (double)v[i];
 }
 
-__global__ void __launch_bounds__(kTopThreads) fwd_top_kernel(DevProblem P, DevWork W, DevSym S, DevBlk B, DevDag D,
-                                                              FrontSel fs) {
+// ---- the solves: one persistent kernel per direction ------------------------
+// Forward: the warps first claim block tasks (no waits); each block signals
+// its root's done flag.  Once every block task is claimed, the CTAs claim the
+// top-region tasks, which wait only on their own children (block roots or
+// top supernodes), so the top region starts as soon as the blocks below it
+// are done.  Backward: the CTAs first claim the top-region tasks (parents
+// first), then the warps claim block tasks, each waiting only on the top
+// supernode above its root.  A task only ever waits on tasks claimed before
+// it by running warps or CTAs, so the kernels cannot deadlock; every wait is
+// bounded.
+
+__device__ __forceinline__ unsigned char *warp_area(unsigned char *smem, const BlkLayout &lay) {
+    return smem + (size_t)(threadIdx.x >> 5) * lay.total;
+}
+
+__global__ void __launch_bounds__(kTopThreads, 8) fwd_solve_kernel(DevProblem P, DevWork W, DevSym S, DevBlk B,
+                                                                   DevDag D, FrontSel fs) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_task, s_ok;
+    const int lane = threadIdx.x & 31;
     const int M = P.M;
     const int epoch = *D.epoch;
+    {
+        const long long n_blk = (long long)B.nblk * M;
+        const BlkLayout lay = blk_layout(B);
+        unsigned char *base = warp_area(smem, lay);
+        for (;;) {
+            long long t = 0;
+            if (lane == 0) t = atomicAdd(D.ctr + 4, 1);
+            t = __shfl_sync(FULL, t, 0);
+            if (t >= n_blk) break;
+            const int blk = (int)(t / M), m = (int)(t % M);
+            if (!W.active[m]) continue;
+            const bool d = use64(fs, m);
+            if (d && fs.fused64) continue;
+            const BlkTask bt = stage_block(S, B, blk, m, base, lay, B.map_fwd, true);
+            __syncwarp();
+            if (d) fwd_block<double>(P, W, S, fs, bt, m, reinterpret_cast<double *>(base + lay.v));
+            else fwd_block<float>(P, W, S, fs, bt, m, reinterpret_cast<float *>(base + lay.v));
+            __syncwarp();
+            if (lane == 0) signal_done(D.xdone + (size_t)B.ent0[B.blk_ptr[blk + 1] - 1].x * M + m, epoch);
+        }
+    }
     const int n_tasks = B.n_top * M;
     for (;;) {
         __syncthreads();
@@ -608,10 +611,11 @@ __global__ void __launch_bounds__(kTopThreads) fwd_top_kernel(DevProblem P, DevW
     }
 }
 
-__global__ void __launch_bounds__(kTopThreads) bwd_top_kernel(DevProblem P, DevWork W, DevSym S, DevBlk B, DevDag D,
-                                                              FrontSel fs) {
+__global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P, DevWork W, DevSym S, DevBlk B,
+                                                                   DevDag D, FrontSel fs) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_task, s_ok;
+    const int lane = threadIdx.x & 31;
     const int M = P.M;
     const int epoch = *D.epoch;
     const int n_tasks = B.n_top * M;
@@ -628,6 +632,28 @@ __global__ void __launch_bounds__(kTopThreads) bwd_top_kernel(DevProblem P, DevW
         else bwd_top_task<float>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
         __syncthreads();
         if (threadIdx.x == 0) signal_done(D.bdone + (size_t)s * M + m, epoch);
+    }
+    const long long n_blk = (long long)B.nblk * M;
+    const BlkLayout lay = blk_layout(B);
+    unsigned char *base = warp_area(smem, lay);
+    for (;;) {
+        long long t = 0;
+        if (lane == 0) t = atomicAdd(D.ctr + 5, 1);
+        t = __shfl_sync(FULL, t, 0);
+        if (t >= n_blk) break;
+        const int blk = (int)(t / M), m = (int)(t % M);
+        if (!W.active[m]) continue;
+        const BlkTask bt = stage_block(S, B, blk, m, base, lay, B.map_bwd, false);
+        const int par = D.parent[B.ent0[B.blk_ptr[blk + 1] - 1].x];
+        if (par >= 0) {
+            bool ok = true;
+            if (lane == 0) ok = wait_epoch(D.bdone + (size_t)par * M + m, epoch, D.err);
+            ok = __shfl_sync(FULL, ok, 0);
+            if (!ok && lane == 0) atomicOr(W.status + m, 8);
+        }
+        __syncwarp();
+        if (use64(fs, m)) bwd_block<double>(P, W, S, B, fs, bt, blk, m, reinterpret_cast<double *>(base + lay.v));
+        else bwd_block<float>(P, W, S, B, fs, bt, blk, m, reinterpret_cast<float *>(base + lay.v));
     }
 }
 
@@ -647,24 +673,21 @@ int solve_configure(const DevBlk &B, SolveGrid &g) {
         return -1;
     // a staged chunk holds at least one whole front column in FP64
     if ((long)B.top_max_front * 8 > kTopStage) return -2;
+    static_assert(kBlkWarps * 32 == kTopThreads, "one CTA runs block tasks per warp and top tasks together");
     g.blk_bytes = kBlkWarps * blk_layout(B).total;
-    g.top_bytes = top_vec_bytes(std::max(1, B.top_max_front)) + kTopStage;
-    if (cudaFuncSetAttribute(fwd_blocks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, g.blk_bytes) !=
+    g.top_bytes = std::max(g.blk_bytes, top_vec_bytes(std::max(1, B.top_max_front)) + kTopStage);
+    if (cudaFuncSetAttribute(fwd_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, g.top_bytes) !=
             cudaSuccess ||
-        cudaFuncSetAttribute(bwd_blocks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, g.blk_bytes) !=
-            cudaSuccess ||
-        cudaFuncSetAttribute(fwd_top_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, g.top_bytes) !=
-            cudaSuccess ||
-        cudaFuncSetAttribute(bwd_top_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, g.top_bytes) !=
+        cudaFuncSetAttribute(bwd_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, g.top_bytes) !=
             cudaSuccess) {
         cudaGetLastError();
         return -1;
     }
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fwd_top_kernel, kTopThreads, g.top_bytes) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fwd_solve_kernel, kTopThreads, g.top_bytes) !=
             cudaSuccess || occ < 1)
         return -1;
     g.top_fwd = nsm * occ;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bwd_top_kernel, kTopThreads, g.top_bytes) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bwd_solve_kernel, kTopThreads, g.top_bytes) !=
             cudaSuccess || occ < 1)
         return -1;
     g.top_bwd = nsm * occ;
@@ -673,22 +696,16 @@ int solve_configure(const DevBlk &B, SolveGrid &g) {
 
 void launch_solve_fwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B, const DevDag &D,
                       const SolveGrid &g, FrontSel fs, cudaStream_t st) {
-    const long long tasks = (long long)B.nblk * P.M;
-    if (tasks > 0)
-        fwd_blocks_kernel<<<(int)((tasks + kBlkWarps - 1) / kBlkWarps), 32 * kBlkWarps, g.blk_bytes, st>>>(P, W, S,
-                                                                                                          B, fs);
-    const long long top = (long long)B.n_top * P.M;
-    if (top > 0) fwd_top_kernel<<<grid_for(g.top_fwd, top, 1), kTopThreads, g.top_bytes, st>>>(P, W, S, B, D, fs);
+    const long long work = std::max((long long)B.nblk * P.M / kBlkWarps + 1, (long long)B.n_top * P.M);
+    if (B.nblk + B.n_top > 0)
+        fwd_solve_kernel<<<grid_for(g.top_fwd, work, 1), kTopThreads, g.top_bytes, st>>>(P, W, S, B, D, fs);
 }
 
 void launch_solve_bwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B, const DevDag &D,
                       const SolveGrid &g, FrontSel fs, cudaStream_t st) {
-    const long long top = (long long)B.n_top * P.M;
-    if (top > 0) bwd_top_kernel<<<grid_for(g.top_bwd, top, 1), kTopThreads, g.top_bytes, st>>>(P, W, S, B, D, fs);
-    const long long tasks = (long long)B.nblk * P.M;
-    if (tasks > 0)
-        bwd_blocks_kernel<<<(int)((tasks + kBlkWarps - 1) / kBlkWarps), 32 * kBlkWarps, g.blk_bytes, st>>>(P, W, S,
-                                                                                                          B, fs);
+    const long long work = std::max((long long)B.nblk * P.M / kBlkWarps + 1, (long long)B.n_top * P.M);
+    if (B.nblk + B.n_top > 0)
+        bwd_solve_kernel<<<grid_for(g.top_bwd, work, 1), kTopThreads, g.top_bytes, st>>>(P, W, S, B, D, fs);
 }
 
 }  // namespace gp
