@@ -404,7 +404,7 @@ struct HostBlk {
     int max_n = 1, max_v = 1, max_p = 1, max_map = 1, max_ext = 1;
     std::vector<int> blk_ptr{0}, map_ptr{0}, ext_ptr{0}, map_fwd, map_bwd, ext_pos, ext_row;
     std::vector<int4> ent0, ent1;
-    int n_top_levels = 0, top_max_front = 1;
+    int n_top_levels = 0, top_max_front = 1, top_max_xent = 1;
     std::vector<int> top_order, top_rank;
     std::vector<int> top_xptr, top_xrow, top_xent;   // extend-add lists of the top region
 };
@@ -534,6 +534,7 @@ void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
         }
         B.top_xrow.push_back((int)B.top_xent.size());
         B.top_xptr.push_back((int)B.top_xrow.size());
+        B.top_max_xent = std::max(B.top_max_xent, B.top_xrow.back() - B.top_xrow[B.top_xptr[B.top_xptr.size() - 2]]);
     }
 }
 
@@ -841,6 +842,7 @@ void build_blocks(gp_layout *L, const gp::Symbolic &sym) {
     B.ext_row = A.upload(H.ext_row);
     B.n_top = (int)H.top_order.size();
     B.top_max_front = H.top_max_front;
+    B.top_max_xent = H.top_max_xent;
     B.top_order = A.upload(H.top_order);
     B.top_rank = A.upload(H.top_rank);
     B.top_xptr = A.upload(H.top_xptr);

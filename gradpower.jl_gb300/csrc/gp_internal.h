@@ -180,6 +180,7 @@ struct DevBlk {
     const int *ext_ptr;          // [nblk+1]
     const int *ext_pos, *ext_row;   // solution entries above the block: vector position, xperm row
     int n_top, top_max_front;
+    int top_max_xent;            // most extend-add entries of one top supernode
     const int *top_order;        // [n_top] top supernodes, children before parents
     const int *top_rank;         // [nsup] position in top_order, -1 inside a block
     // forward extend-add of the top region, per top supernode (by rank) and

@@ -231,13 +231,15 @@ __global__ void __launch_bounds__(32) cluster_kernel(DevProblem P, DevWork W, De
     }
 }
 
-// MX_KEEP scenarios of the mixed solver: the residual and its solve with the
-// kept FP32 LU, nothing else.  The same operations in the same order as
-// cluster_kernel's mode 2 (so the same results), but only the residual
-// column is staged in shared memory (W doubles per lane instead of the whole
-// program's slots), the LU values are read straight from the kept copy, and
-// the op list is the solve part of the program alone: many more warps fit
-// on an SM.
+// MX_KEEP scenarios of the mixed solver: the FP64 residual and its solve
+// with the kept FP32 LU, nothing else.  Only the residual column is staged in
+// shared memory (W values per lane instead of the whole program's slots), the
+// LU values are read straight from the kept copy, and the op list is the
+// solve part of the program alone, so many more warps fit on an SM.  The
+// solve runs in FP32, like the kept LU it applies: FP64 arithmetic and
+// FP32<->FP64 conversions are scarce on this GPU, and the correction of an
+// iteration on kept factors is inexact at the FP32 level anyway (the residual
+// that drives it stays FP64).
 // Sink of a residual-only evaluation: Jacobian entries are dropped (the
 // compiler removes their arithmetic), residuals go to their positions in the
 // staged residual column.
@@ -254,7 +256,8 @@ struct KeepSink {
 
 __global__ void __launch_bounds__(32, 16) cluster_keep_kernel(DevProblem P, DevWork W, DevClu Cl, DevMixed Mx,
                                                              int want_f) {
-    extern __shared__ double R2[];   // [W][32] residual, by pivot position
+    extern __shared__ double R2[];   // [max_w][32] FP64 residual by pivot position, then [max_w][32] FP32
+    float *Rf = reinterpret_cast<float *>(R2 + (size_t)Cl.max_w * 32);
     const int task = blockIdx.x, m = blockIdx.y, lane = threadIdx.x;
     if (!W.active[m] || Mx.refac[m] != MX_KEEP) return;
     const int cls = Cl.task_class[task];
@@ -298,23 +301,24 @@ __global__ void __launch_bounds__(32, 16) cluster_keep_kernel(DevProblem P, DevW
         nb = o > nb ? o : nb;
     }
     if (lane == 0) atomicMax(W.norm + m, nb);
+    for (int j = 0; j < Wn; j++) Rf[j * 32 + lane] = (float)R2[j * 32 + lane];
     // the solves (OP_FMS3 / OP_MUL3 on the residual column), eight ops and
     // their LU values loaded ahead of the arithmetic
     const float *kl = Mx.lu + (((size_t)m * Cl.n_tasks + task) * Mx.n_lu) * 32 + lane;
     constexpr int kAhead = 8;
     for (int q = qs; q < q1; q += kAhead) {
         CluOp o[kAhead];
-        double l[kAhead];
+        float l[kAhead];
 #pragma unroll
         for (int u = 0; u < kAhead; u++) {
             o[u] = ops[min(q + u, q1 - 1)];
-            l[u] = (double)kl[o[u].a * 32];
+            l[u] = kl[o[u].a * 32];
         }
 #pragma unroll
         for (int u = 0; u < kAhead; u++) {
             if (q + u >= q1) break;
-            if (o[u].code == OP_FMS3) R2[o[u].d * 32 + lane] -= l[u] * R2[o[u].b * 32 + lane];
-            else R2[o[u].d * 32 + lane] *= l[u];
+            if (o[u].code == OP_FMS3) Rf[o[u].d * 32 + lane] = fmaf(-l[u], Rf[o[u].b * 32 + lane], Rf[o[u].d * 32 + lane]);
+            else Rf[o[u].d * 32 + lane] *= l[u];
         }
     }
     if (!act) return;
@@ -322,12 +326,12 @@ __global__ void __launch_bounds__(32, 16) cluster_keep_kernel(DevProblem P, DevW
     double *yx = W.yx + (size_t)m * 3 * n_da + ws;
     const int *pc = Cl.perm_col + cls * 32;
     const int *p3 = Cl.pos3 + cls * 3;
-    for (int j = 0; j < Wn; j++) yx[pc[j]] = R2[j * 32 + lane];
-    const double Y0 = R2[p3[0] * 32 + lane], Y1 = R2[p3[1] * 32 + lane], Y2 = R2[p3[2] * 32 + lane];
+    for (int j = 0; j < Wn; j++) yx[pc[j]] = (double)Rf[j * 32 + lane];
+    const float Y0 = Rf[p3[0] * 32 + lane], Y1 = Rf[p3[1] * 32 + lane], Y2 = Rf[p3[2] * 32 + lane];
     const float *cc = Mx.cc + ((size_t)m * P.n_cl + c) * 6;
     double *o = W.clout + ((size_t)m * P.n_cl + c) * 8;
-    o[4] = (double)cc[0] * Y0 + (double)cc[1] * Y1 + (double)cc[2] * Y2;
-    o[5] = (double)cc[3] * Y0 + (double)cc[4] * Y1 + (double)cc[5] * Y2;
+    o[4] = (double)fmaf(cc[2], Y2, fmaf(cc[1], Y1, cc[0] * Y0));
+    o[5] = (double)fmaf(cc[5], Y2, fmaf(cc[4], Y1, cc[3] * Y0));
     o[6] = Ic[0];
     o[7] = Ic[1];
 }
@@ -338,7 +342,8 @@ int launch_cluster(const DevProblem &P, const DevWork &W, const DevClu &C, const
     dim3 grid(C.n_tasks, P.M);
     cluster_kernel<<<grid, 32, (size_t)C.max_slots * 32 * sizeof(double), st>>>(P, W, C, Mx, want_f);
     if (!Mx.on) return 1;
-    cluster_keep_kernel<<<grid, 32, (size_t)C.max_w * 32 * sizeof(double), st>>>(P, W, C, Mx, want_f);
+    cluster_keep_kernel<<<grid, 32, (size_t)C.max_w * 32 * (sizeof(double) + sizeof(float)), st>>>(P, W, C, Mx,
+                                                                                                  want_f);
     return 2;
 }
 
@@ -375,8 +380,9 @@ __global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, D
             const int j = P.y_colidx[q];
             const double g = P.y_re[q], bb = P.y_im[q];
             const double vrj = z[net + 2 * j], vij = z[net + 2 * j + 1];
-            fr -= g * vrj - bb * vij;
-            fi -= bb * vrj + g * vij;
+            // -(g + j bb)(vrj + j vij), two FMAs per part
+            fr = fma(-g, vrj, fma(bb, vij, fr));
+            fi = fma(-bb, vrj, fma(-g, vij, fi));
             if (need_s && j == b) { d00 -= g; d01 += bb; d10 -= bb; d11 -= g; }
         }
         for (int q = P.bus_cl_ptr[b]; q < P.bus_cl_ptr[b + 1]; q++) {
@@ -390,27 +396,30 @@ __global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, D
             const int k = P.bus_zl[q];
             const int pp = ZL.par_ptr[k];
             const double pl = p[pp], ql = p[pp + 1], al = p[pp + 2], yre0 = p[pp + 7], yim0 = p[pp + 8];
-            const double yre = al * yre0, yim = al * yim0;
             const double vm2 = vr * vr + vi * vi, vm2_tld = 0.2;
-            fr -= vr * yre - vi * yim;
-            fi -= vr * yim + vi * yre;
-            const double den = vm2 > vm2_tld ? vm2 : vm2_tld;
-            fr -= (1.0 - al) * (pl * vr - ql * vi) / den;
-            fi -= (1.0 - al) * (ql * vr + pl * vi) / den;
+            const bool above = vm2 > vm2_tld;
+            // one division per load (FP64 division is dear here)
+            const double inv = 1.0 / (above ? vm2 : vm2_tld);
+            const double sp = (1.0 - al) * inv;
+            // the constant-impedance part al*y0 and the constant-power part
+            // (1 - al)(P - jQ)/max(|V|^2, 0.2) multiply the same V: one
+            // complex admittance a + jc
+            const double a = fma(sp, pl, al * yre0), c = fma(sp, ql, al * yim0);
+            fr -= vr * a - vi * c;
+            fi -= vr * c + vi * a;
             if (!need_s) continue;
             double p11, p12, p21, p22;
-            if (vm2 > vm2_tld) {
-                const double iv4 = 1.0 / (vm2 * vm2);
+            if (above) {
+                const double iv4 = inv * inv;
                 p11 = (1.0 - al) * ((pl * vr - ql * vi) * 2.0 * vr - pl * vm2) * iv4;
                 p12 = (1.0 - al) * ((pl * vr - ql * vi) * 2.0 * vi + ql * vm2) * iv4;
                 p21 = (1.0 - al) * ((ql * vr + pl * vi) * 2.0 * vr - ql * vm2) * iv4;
                 p22 = (1.0 - al) * ((ql * vr + pl * vi) * 2.0 * vi - pl * vm2) * iv4;
             } else {
-                const double ith = 1.0 / vm2_tld;
-                p11 = (1.0 - al) * (-pl) * ith;
-                p12 = (1.0 - al) * (ql)*ith;
-                p21 = (1.0 - al) * (-ql) * ith;
-                p22 = (1.0 - al) * (-pl) * ith;
+                p11 = -pl * sp;
+                p12 = ql * sp;
+                p21 = -ql * sp;
+                p22 = -pl * sp;
             }
             d00 += -al * yre0 + p11;
             d01 += al * yim0 + p12;
@@ -427,8 +436,9 @@ __global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, D
             else if (bt == 3) { Pg = z[ap]; Qg = z[ap + 1]; }
             else { Pg = p[pp]; Qg = p[pp + 1]; }
             const double irn = Pg * vr + Qg * vi, iin = Pg * vi - Qg * vr;
-            fr += irn / vm2;
-            fi += iin / vm2;
+            const double inv = 1.0 / vm2;
+            fr += irn * inv;
+            fi += iin * inv;
             if (!need_s) {
                 double *xp = W.xperm + (size_t)m * P.n_red;
                 const int r0 = P.sg_red[k];
@@ -456,16 +466,16 @@ __global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, D
                 continue;
             }
             if (vm2r > 0.2) {
-                const double vm4 = vm2 * vm2;
-                d00 += Pg / vm2 - 2.0 * vr * irn / vm4;
-                d01 += Qg / vm2 - 2.0 * vi * irn / vm4;
-                d10 += -Qg / vm2 - 2.0 * vr * iin / vm4;
-                d11 += Pg / vm2 - 2.0 * vi * iin / vm4;
+                const double iv4 = inv * inv;
+                d00 += Pg * inv - 2.0 * vr * irn * iv4;
+                d01 += Qg * inv - 2.0 * vi * irn * iv4;
+                d10 += -Qg * inv - 2.0 * vr * iin * iv4;
+                d11 += Pg * inv - 2.0 * vi * iin * iv4;
             } else {
-                d00 += Pg / vm2;
-                d01 += Qg / vm2;
-                d10 += -Qg / vm2;
-                d11 += Pg / vm2;
+                d00 += Pg * inv;
+                d01 += Qg * inv;
+                d10 += -Qg * inv;
+                d11 += Pg * inv;
             }
             double *sv = W.svar + (size_t)m * P.n_var + P.sg_var[k];
             double *xp = W.xperm + (size_t)m * P.n_red;
@@ -474,7 +484,7 @@ __global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, D
                 const double vset = p[pp + 2];
                 const double fa = vr * vr + vi * vi - vset * vset;
                 // (ap,vr) (ap,vi) (vr,ap) (vi,ap)
-                sv[0] = 2.0 * vr; sv[1] = 2.0 * vi; sv[2] = vi / vm2; sv[3] = -vr / vm2;
+                sv[0] = 2.0 * vr; sv[1] = 2.0 * vi; sv[2] = vi * inv; sv[3] = -vr * inv;
                 xp[P.iperm[r0]] = -fa;
                 if (want_f) W.f[(size_t)m * P.n_sys + ap] = fa;
                 const unsigned long long t = norm_bits(fa);
@@ -483,7 +493,7 @@ __global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, D
                 const double vset = p[pp + 2], aset = p[pp + 3];
                 const double fa0 = vr - vset * cos(aset), fa1 = vi - vset * sin(aset);
                 // (ap,vr) (ap+1,vi) (vr,ap) (vi,ap) (vr,ap+1) (vi,ap+1)
-                sv[0] = 1.0; sv[1] = 1.0; sv[2] = vr / vm2; sv[3] = vi / vm2; sv[4] = vi / vm2; sv[5] = -vr / vm2;
+                sv[0] = 1.0; sv[1] = 1.0; sv[2] = vr * inv; sv[3] = vi * inv; sv[4] = vi * inv; sv[5] = -vr * inv;
                 xp[P.iperm[r0]] = -fa0;
                 xp[P.iperm[r0 + 1]] = -fa1;
                 if (want_f) {

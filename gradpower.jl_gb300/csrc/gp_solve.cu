@@ -55,6 +55,8 @@ __host__ __device__ constexpr int align16(int b) { return (b + 15) & ~15; }
 // Shared memory of one top-region CTA: two vectors sized for double and one
 // int vector (top_max_front entries each), then the factor staging area.
 __host__ __device__ constexpr int top_vec_bytes(int tmf) { return align16(tmf * (8 + 8 + 4)); }
+// the forward tasks' extend-add lists (row pointers, then entries)
+__host__ __device__ constexpr int top_idx_bytes(int tmf, int mx) { return align16((tmf + 1) * 4) + align16(mx * 4); }
 
 __device__ __forceinline__ void cp_async(void *dst, const void *src, int bytes) {
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
@@ -470,26 +472,37 @@ __device__ void fwd_top_task(const DevProblem &P, const DevWork &W, const DevSym
     T *v = reinterpret_cast<T *>(smem);
     T *sc = reinterpret_cast<T *>(smem + tmf * 8);
     int *pi = reinterpret_cast<int *>(smem + tmf * 16);
-    T *Fs = reinterpret_cast<T *>(smem + top_vec_bytes(tmf));
+    int *sxr = reinterpret_cast<int *>(smem + top_vec_bytes(tmf));
+    int *sxe = sxr + align16((tmf + 1) * 4) / 4;
+    T *Fs = reinterpret_cast<T *>(smem + top_vec_bytes(tmf) + top_idx_bytes(tmf, B.top_max_xent));
     const T *F = front_base<T>(fs) + (size_t)t.m * S.front_total + S.front_off[t.s];
     const int cap = kTopStage / ((int)sizeof(T) * t.mm);   // columns per staged chunk
     double *x = W.xperm + (size_t)t.m * P.n_red;
     double *uv = S.uvec + (size_t)t.m * S.uvec_total;
     const int *ip = S.ipiv + (size_t)t.m * S.n + t.start;
-    // independent of other tasks: own entries, pivot permutation, factor columns
+    // independent of other tasks: own entries, pivot permutation, factor
+    // columns and the extend-add lists, all fetched before the wait so that
+    // only the children's update entries remain on the path after it
+    const int *xr = B.top_xrow + B.top_xptr[t.rank];
+    for (int i = threadIdx.x; i <= t.mm; i += blockDim.x) sxr[i] = xr[i];
     for (int i = threadIdx.x; i < t.mm; i += blockDim.x) v[i] = i < t.ns ? (T)x[t.start + i] : T(0);
     for (int i = threadIdx.x; i < t.ns; i += blockDim.x) pi[i] = ip[i];
     int k1 = min(t.ns, cap);
     stage_cols<T>(Fs, F, t.mm, t.mm, 0, k1);
+    __syncthreads();
+    {
+        const int e0 = sxr[0], ne = sxr[t.mm] - e0;
+        for (int e = threadIdx.x; e < ne; e += blockDim.x) sxe[e] = B.top_xent[e0 + e];
+    }
     if (!wait_top_children(S, B, D, t.s, t.m, P.M, epoch, s_ok) && threadIdx.x == 0) atomicOr(W.status + t.m, 8);
     // extend-add: one thread per front row sums the children's entries in
     // child order (the update vectors of the children were written by other
     // CTAs: read through L2)
     {
-        const int *xr = B.top_xrow + B.top_xptr[t.rank];
+        const int e0 = sxr[0];
         for (int i = threadIdx.x; i < t.mm; i += blockDim.x) {
             T acc = v[i];
-            for (int e = xr[i]; e < xr[i + 1]; e++) acc += (T)__ldcg(uv + B.top_xent[e]);
+            for (int e = sxr[i] - e0; e < sxr[i + 1] - e0; e++) acc += (T)__ldcg(uv + sxe[e]);
             v[i] = acc;
         }
     }
@@ -675,7 +688,8 @@ int solve_configure(const DevBlk &B, SolveGrid &g) {
     if ((long)B.top_max_front * 8 > kTopStage) return -2;
     static_assert(kBlkWarps * 32 == kTopThreads, "one CTA runs block tasks per warp and top tasks together");
     g.blk_bytes = kBlkWarps * blk_layout(B).total;
-    g.top_bytes = std::max(g.blk_bytes, top_vec_bytes(std::max(1, B.top_max_front)) + kTopStage);
+    g.top_bytes = std::max(g.blk_bytes, top_vec_bytes(std::max(1, B.top_max_front)) +
+                                            top_idx_bytes(std::max(1, B.top_max_front), B.top_max_xent) + kTopStage);
     if (cudaFuncSetAttribute(fwd_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, g.top_bytes) !=
             cudaSuccess ||
         cudaFuncSetAttribute(bwd_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, g.top_bytes) !=

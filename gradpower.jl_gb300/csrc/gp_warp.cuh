@@ -27,24 +27,24 @@ __device__ __forceinline__ void st_release(int *p, int v) {
 }
 
 // Waits until *flag == epoch; false when it gave up (error flag raised here
-// or by another task).
+// or by another task).  The error flag is read every 32nd poll only, so that
+// a poll is one load on the path between a signal and its waiter.
 __device__ inline bool wait_epoch(const int *flag, int epoch, int *err) {
     for (int it = 0; it < kWaitLimit; ++it) {
         if (ld_relaxed(flag) == epoch) {
             fence_acquire();
             return true;
         }
-        if (*(volatile int *)err) return false;
-        __nanosleep(64);
+        if ((it & 31) == 31 && ld_relaxed(err)) return false;
+        __nanosleep(32);
     }
     atomicExch(err, 1);
     return false;
 }
 
-__device__ __forceinline__ void signal_done(int *flag, int epoch) {
-    __threadfence();
-    st_release(flag, epoch);
-}
+// Called by one thread after a CTA or warp barrier that orders the task's
+// writes before it; the release store makes them visible with the flag.
+__device__ __forceinline__ void signal_done(int *flag, int epoch) { st_release(flag, epoch); }
 
 // Next power of two >= n, for 1 <= n <= 32.
 __device__ __forceinline__ int np2(int n) { return n <= 1 ? 1 : 1 << (32 - __clz(n - 1)); }
