@@ -109,6 +109,14 @@ struct gp_layout {
     std::vector<int> h_fl_on_step, h_fl_off_step, h_fl_scen;
     // graphs
     cudaGraphExec_t g_eval = nullptr, g_solve = nullptr;
+    // device-driven Newton loop (profiling off): eval, then WHILE(some
+    // scenario iterates) { solve; eval }, the solve picked by a SWITCH node
+    // for the mixed solver; counts into d_cnt (gp::LoopCtl)
+    cudaGraphExec_t g_loop = nullptr;
+    cudaGraphConditionalHandle h_loop = 0, h_var = 0;
+    int *d_cnt = nullptr;
+    bool profiling = false;      // host-driven loop with phase events (gp_set_profiling)
+    bool no_marks = false;       // capturing into a conditional body: no event nodes
     double graph_tol = -1.0;
     int graph_itermax = -1;
     // timing of the last integrate call
@@ -1031,6 +1039,8 @@ void build_work(gp_layout *L, const double *z0, const double *u0, const double *
     ck(cudaMemset(D.bdone, 0, M * D.nsup * sizeof(int)), "memset");
     ck(cudaMemset(W.status, 0, M * sizeof(int)), "memset");
     ck(cudaMallocHost(&L->h_flag, 4 * sizeof(int)), "cudaMallocHost");
+    L->d_cnt = A.alloc<int>(8);
+    ck(cudaMemset(L->d_cnt, 0, 8 * sizeof(int)), "memset");
     ck(cudaMallocHost(&L->h_dt, sizeof(double)), "cudaMallocHost");
     ck(cudaStreamCreateWithFlags(&L->st, cudaStreamNonBlocking), "stream");
     for (int i = 0; i < 8; i++) ck(cudaEventCreate(&L->pev[i]), "event");
@@ -1089,7 +1099,8 @@ void build_clusters(gp_layout *L, const gp_problem *pr, const double *z0, const 
 }
 
 void drop_graphs(gp_layout *L) {
-    for (cudaGraphExec_t *g : {&L->g_eval, &L->g_solve, &L->g_mix[0], &L->g_mix[1], &L->g_mix[2], &L->g_mix[3]})
+    for (cudaGraphExec_t *g :
+         {&L->g_eval, &L->g_solve, &L->g_mix[0], &L->g_mix[1], &L->g_mix[2], &L->g_mix[3], &L->g_loop})
         if (*g) {
             cudaGraphExecDestroy(*g);
             *g = nullptr;
@@ -1141,6 +1152,7 @@ void set_faults(gp_layout *L, int n_faults, const gp_fault *faults) {
 }
 
 void mark(gp_layout *L, int i) {
+    if (L->no_marks) return;
     ck(cudaEventRecordWithFlags(L->pev[i], L->st, cudaEventRecordExternal), "event record");
 }
 
@@ -1196,15 +1208,19 @@ int enqueue_solve(gp_layout *L, int variant, int *nfac_out) {
     return launches;
 }
 
-void enqueue_eval(gp_layout *L, double tol, int itermax) {
+// Evaluation: residuals, cluster solves, reduced right-hand side, check.
+// The host-driven loop copies the flags to the host; the device-driven loop
+// (ctl.on) leaves the decision to the check kernel.
+void enqueue_eval(gp_layout *L, double tol, int itermax, const gp::LoopCtl &ctl) {
     gp::launch_reset_norm(L->P, L->W, L->Mx, L->st);
     mark(L, 0);
     L->eval_launches = 3 + gp::launch_cluster(L->P, L->W, L->C, L->Mx, 0, L->st);
     mark(L, 1);
     gp::launch_network(L->P, L->W, L->Mx, 0, L->st);
     mark(L, 2);
-    gp::launch_check(L->P, L->W, L->Mx, tol, itermax, L->st);
-    ck(cudaMemcpyAsync(L->h_flag, L->W.flag, 4 * sizeof(int), cudaMemcpyDeviceToHost, L->st), "flag copy");
+    gp::launch_check(L->P, L->W, L->Mx, tol, itermax, ctl, L->st);
+    if (!ctl.on)
+        ck(cudaMemcpyAsync(L->h_flag, L->W.flag, 4 * sizeof(int), cudaMemcpyDeviceToHost, L->st), "flag copy");
 }
 
 template <class F>
@@ -1217,6 +1233,92 @@ cudaGraphExec_t capture(gp_layout *L, F enqueue) {
     ck(cudaGraphInstantiate(&ex, g, 0), "graph instantiate");
     cudaGraphDestroy(g);
     return ex;
+}
+
+// Captures the work of enqueue into the existing graph g after the nodes
+// deps; returns the last node captured.
+template <class F>
+cudaGraphNode_t capture_into(gp_layout *L, cudaGraph_t g, const cudaGraphNode_t *deps, size_t n_deps, F enqueue) {
+    ck(cudaStreamBeginCaptureToGraph(L->st, g, deps, nullptr, n_deps, cudaStreamCaptureModeThreadLocal),
+       "begin capture");
+    enqueue();
+    cudaStreamCaptureStatus status;
+    const cudaGraphNode_t *tail = nullptr;
+    size_t n_tail = 0;
+    ck(cudaStreamGetCaptureInfo(L->st, &status, nullptr, nullptr, &tail, nullptr, &n_tail), "capture info");
+    const cudaGraphNode_t last = n_tail == 1 ? tail[0] : nullptr;
+    cudaGraph_t out;
+    ck(cudaStreamEndCapture(L->st, &out), "end capture");
+    if (!last) fail(GP_E_INTERNAL, "captured work does not end in one node");
+    return last;
+}
+
+cudaGraphNode_t add_conditional(cudaGraph_t g, const cudaGraphNode_t *deps, size_t n_deps,
+                                cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type, unsigned size,
+                                cudaGraph_t *bodies) {
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = type;
+    np.conditional.size = size;
+    cudaGraphNode_t node;
+    ck(cudaGraphAddNode(&node, g, deps, nullptr, n_deps, &np), "conditional node");
+    for (unsigned b = 0; b < size; b++) bodies[b] = np.conditional.phGraph_out[b];
+    return node;
+}
+
+int enqueue_solve(gp_layout *L, int variant, int *nfac_out);
+
+// The whole Newton solve as one graph: the first evaluation, then
+// WHILE(some scenario iterates) { solve; evaluation }.  The mixed solver's
+// solve is a SWITCH over the four factorisation variants, chosen by the
+// check kernel; the FP64 solve is always the same.  No event nodes: the
+// phase timing needs the host-driven loop.
+cudaGraphExec_t build_loop(gp_layout *L, double tol, int itermax, bool mixed) {
+    cudaGraph_t g;
+    ck(cudaGraphCreate(&g, 0), "graph create");
+    ck(cudaGraphConditionalHandleCreate(&L->h_loop, g, 0, cudaGraphCondAssignDefault), "conditional handle");
+    L->h_var = 0;
+    if (mixed) ck(cudaGraphConditionalHandleCreate(&L->h_var, g, 0, cudaGraphCondAssignDefault), "conditional handle");
+    const gp::LoopCtl ctl{L->h_loop, L->h_var, L->d_cnt, 1, mixed ? 1 : 0};
+    L->no_marks = true;
+    const cudaGraphNode_t first = capture_into(L, g, nullptr, 0, [&] { enqueue_eval(L, tol, itermax, ctl); });
+    cudaGraph_t body;
+    add_conditional(g, &first, 1, L->h_loop, cudaGraphCondTypeWhile, 1, &body);
+    cudaGraphNode_t solved;
+    if (mixed) {
+        cudaGraph_t var[4];
+        solved = add_conditional(body, nullptr, 0, L->h_var, cudaGraphCondTypeSwitch, 4, var);
+        for (int v = 0; v < 4; v++)
+            capture_into(L, var[v], nullptr, 0,
+                         [&] { L->mix_launches[v] = enqueue_solve(L, v, &L->mix_factor_launches[v]); });
+    } else {
+        int nf = 0;
+        solved = capture_into(L, body, nullptr, 0, [&] { L->solve_graph_launches = enqueue_solve(L, -1, &nf); });
+    }
+    capture_into(L, body, &solved, 1, [&] { enqueue_eval(L, tol, itermax, ctl); });
+    L->no_marks = false;
+    cudaGraphExec_t ex;
+    ck(cudaGraphInstantiate(&ex, g, 0), "graph instantiate");
+    cudaGraphDestroy(g);
+    return ex;
+}
+
+// Folds the device-driven loop's counts into the call's totals.
+void harvest_counts(gp_layout *L) {
+    int c[8];
+    ck(cudaMemcpy(c, L->d_cnt, sizeof(c), cudaMemcpyDeviceToHost), "count copy");
+    ck(cudaMemset(L->d_cnt, 0, sizeof(c)), "memset");
+    const bool mixed = L->Mx.on != 0;
+    const int nfac = (L->D.n_small > 0) + (L->D.nsup > L->D.n_small);
+    L->launches += (double)c[0] * L->eval_launches;
+    L->solves += c[1];
+    L->refreshes += c[2];
+    L->exact_iters += c[3];
+    for (int v = 0; v < 4; v++) {
+        L->launches += (double)c[4 + v] * (mixed ? L->mix_launches[v] : L->solve_graph_launches);
+        L->factor_launches += (double)c[4 + v] * (mixed ? L->mix_factor_launches[v] : nfac);
+    }
 }
 
 // Kept FP32 factors of the mixed solver, allocated on its first use.
@@ -1264,12 +1366,14 @@ void ensure_graphs(gp_layout *L, double tol, int itermax, int solver) {
     const bool mixed = solver == GP_SOLVER_SCHUR_MIXED;
     if (mixed) ensure_mixed(L);
     L->Mx.on = mixed ? 1 : 0;
-    if (!L->g_eval) {
-        L->g_eval = capture(L, [&] { enqueue_eval(L, tol, itermax); });
-        L->graph_tol = tol;
-        L->graph_itermax = itermax;
-        L->solver = solver;
+    L->graph_tol = tol;
+    L->graph_itermax = itermax;
+    L->solver = solver;
+    if (!L->profiling) {
+        if (!L->g_loop) L->g_loop = build_loop(L, tol, itermax, mixed);
+        return;
     }
+    if (!L->g_eval) L->g_eval = capture(L, [&] { enqueue_eval(L, tol, itermax, gp::LoopCtl{0, 0, nullptr, 0, 0}); });
     if (!mixed && !L->g_solve) {
         int nf = 0;
         L->g_solve = capture(L, [&] { L->solve_graph_launches = enqueue_solve(L, -1, &nf); });
@@ -1293,13 +1397,24 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
 }
 
 void newton(gp_layout *L, double dt, double tol, int itermax, bool force_refresh, bool reset_iters) {
-    *L->h_dt = dt;
-    ck(cudaMemcpyAsync(L->W.dt, L->h_dt, sizeof(double), cudaMemcpyHostToDevice, L->st), "dt");
+    // dt by value (a kernel argument): the host may run steps ahead of the GPU
+    gp::launch_set_double(L->W.dt, dt, L->st);
+    L->launches += 1;
     if (reset_iters) ck(cudaMemsetAsync(L->W.iters, 0, L->M * sizeof(int), L->st), "memset");
     const bool mixed = L->Mx.on != 0;
     if (mixed) {
         gp::launch_mixed_start(L->P, L->W, L->Mx, force_refresh ? 1 : 0, L->st);
         L->launches += 1;
+    }
+    if (!L->profiling) {
+        // the whole loop on the device; the mixed solver's retry test reads
+        // the flags afterwards
+        ck(cudaGraphLaunch(L->g_loop, L->st), "graph launch");
+        if (mixed) {
+            ck(cudaMemcpyAsync(L->h_flag, L->W.flag, 4 * sizeof(int), cudaMemcpyDeviceToHost, L->st), "flag copy");
+            ck(cudaStreamSynchronize(L->st), "newton sync");
+        }
+        return;
     }
     bool solve_pending = false;
     for (int guard = 0; guard <= itermax + 1; guard++) {
@@ -1613,6 +1728,7 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     L->t_total_ms = ms;
+    if (!L->profiling) harvest_counts(L);
     {
         int err = 0;
         ck(cudaMemcpy(&err, L->D.err, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
@@ -1874,6 +1990,7 @@ int32_t gp_adjoint(gp_layout *L, const gp_options *opt, int32_t n_faults, const 
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     L->t_total_ms = ms;
+    if (!L->profiling) harvest_counts(L);
     {
         int err = 0;
         ck(cudaMemcpy(&err, L->D.err, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
@@ -1899,6 +2016,16 @@ int32_t gp_set_mixed_policy(gp_layout *L, int32_t max_age, double rho_max, int32
     L->Mx.rho_max = rho_max;
     L->Mx.exact_after = exact_after;
     drop_graphs(L);   // the graphs hold the policy by value
+    API_END
+}
+
+int32_t gp_set_profiling(gp_layout *L, int32_t on) {
+    API_BEGIN
+    if (!L) fail(GP_E_INVALID, "null argument");
+    if ((on != 0) != L->profiling) {
+        L->profiling = on != 0;
+        drop_graphs(L);
+    }
     API_END
 }
 

@@ -218,8 +218,21 @@ int solve_block_front_limit();
 int launch_cluster(const DevProblem &P, const DevWork &W, const DevClu &C, const DevMixed &Mx, int want_f,
                     cudaStream_t st);
 void launch_network(const DevProblem &P, const DevWork &W, const DevMixed &Mx, int want_f, cudaStream_t st);
+// Control of a Newton loop run on the device (a CUDA graph whose WHILE node
+// repeats solve + evaluation): the check kernel sets the loop condition
+// (some scenario still iterating) and, for the mixed solver, the SWITCH
+// value that picks the next solve's factorisations (bit 0 FP32 refresh,
+// bit 1 FP64), and counts into cnt: [0] evaluations, [1] solves, [2]
+// scenario FP32 refreshes, [3] scenario FP64 iterations, [4 + v] solves of
+// variant v.  on == 0 for the host-driven loop.
+struct LoopCtl {
+    cudaGraphConditionalHandle loop, var;
+    int *cnt;
+    int on, mixed;
+};
+
 void launch_check(const DevProblem &P, const DevWork &W, const DevMixed &Mx, double tol, int itermax,
-                  cudaStream_t st);
+                  const LoopCtl &ctl, cudaStream_t st);
 void launch_reset_norm(const DevProblem &P, const DevWork &W, const DevMixed &Mx, cudaStream_t st);
 void launch_mixed_start(const DevProblem &P, const DevWork &W, const DevMixed &Mx, int force, cudaStream_t st);
 void launch_retry_start(const DevProblem &P, const DevWork &W, const DevMixed &Mx, cudaStream_t st);

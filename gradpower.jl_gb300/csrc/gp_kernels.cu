@@ -87,6 +87,43 @@ __device__ __forceinline__ void eval_cluster(const DevProblem &P, int c, const d
     if (P.cl_pss[c] >= 0) ieeest_eval(devref(P.dev[5], P.cl_pss[c]), z, p, sink);
 }
 
+// The factorisation part of a class program and the solves of the three
+// right-hand-side columns R0, R1 (B) and R2 (f), on one lane's slots.
+template <class T>
+__device__ __forceinline__ void clu_program(T *vals, T *R0, T *R1, T *R2, const CluOp *ops, int qm, int q1,
+                                            int lane) {
+    for (int q = qm; q < q1; q++) {
+        const CluOp o = ops[q];
+        switch (o.code) {
+        case OP_RCP:
+            vals[o.d * 32 + lane] = T(1) / vals[o.a * 32 + lane];
+            break;
+        case OP_MUL:
+            vals[o.d * 32 + lane] *= vals[o.a * 32 + lane];
+            break;
+        case OP_FMS:
+            vals[o.d * 32 + lane] -= vals[o.a * 32 + lane] * vals[o.b * 32 + lane];
+            break;
+        case OP_FMS3: {
+            const T l = vals[o.a * 32 + lane];
+            R0[o.d * 32 + lane] -= l * R0[o.b * 32 + lane];
+            R1[o.d * 32 + lane] -= l * R1[o.b * 32 + lane];
+            R2[o.d * 32 + lane] -= l * R2[o.b * 32 + lane];
+            break;
+        }
+        case OP_MUL3: {
+            const T l = vals[o.a * 32 + lane];
+            R0[o.d * 32 + lane] *= l;
+            R1[o.d * 32 + lane] *= l;
+            R2[o.d * 32 + lane] *= l;
+            break;
+        }
+        default:
+            break;
+        }
+    }
+}
+
 // Modes per scenario: 0 exact Newton (Jacobian block, FP64 LU, three solves;
 // also the mixed solver's MX_EXACT); 1 the same, and the LU values and
 // coupling rows are kept in FP32 for the following iterations (MX_FP32).
@@ -154,71 +191,67 @@ __global__ void __launch_bounds__(32) cluster_kernel(DevProblem P, DevWork W, De
     }
     if (lane == 0) atomicMax(W.norm + m, nb);
     float *keep = Mx.on ? Mx.lu + (((size_t)m * Cl.n_tasks + task) * Mx.n_lu) * 32 + lane : nullptr;
-    {
-        // factorisation and solves
-        for (int q = qm; q < q1; q++) {
-            const CluOp o = ops[q];
-            switch (o.code) {
-            case OP_RCP:
-                vals[o.d * 32 + lane] = 1.0 / vals[o.a * 32 + lane];
-                break;
-            case OP_MUL:
-                vals[o.d * 32 + lane] *= vals[o.a * 32 + lane];
-                break;
-            case OP_FMS:
-                vals[o.d * 32 + lane] -= vals[o.a * 32 + lane] * vals[o.b * 32 + lane];
-                break;
-            case OP_FMS3: {
-                const double l = vals[o.a * 32 + lane];
-                R0[o.d * 32 + lane] -= l * R0[o.b * 32 + lane];
-                R1[o.d * 32 + lane] -= l * R1[o.b * 32 + lane];
-                R2[o.d * 32 + lane] -= l * R2[o.b * 32 + lane];
-                break;
-            }
-            case OP_MUL3: {
-                const double l = vals[o.a * 32 + lane];
-                R0[o.d * 32 + lane] *= l;
-                R1[o.d * 32 + lane] *= l;
-                R2[o.d * 32 + lane] *= l;
-                break;
-            }
-            default:
-                break;
-            }
+    const int n_da = P.n_diff + P.n_alg;
+    double *yx = W.yx + (size_t)m * 3 * n_da + ws;
+    const int *p3 = Cl.pos3 + cls * 3;
+    double X0[3], X1[3], X2[3];
+    if (mode == 1) {
+        // MX_FP32: the factors are kept in FP32, so the factorisation and
+        // the three solves run in FP32 too.  The slots are converted in place:
+        // float slot s lies in the first half of double slot s / 2, which was
+        // read before (each slot is read into registers before the warp
+        // writes over it).
+        float *fv = reinterpret_cast<float *>(vals);
+        for (int s = 0; s < nslot; s++) {
+            const float x = (float)vals[s * 32 + lane];
+            __syncwarp();
+            fv[s * 32 + lane] = x;
+            __syncwarp();
         }
-        if (mode == 1)
-            for (int s = 0; s < rb; s++) keep[s * 32] = (float)vals[s * 32 + lane];
+        float *F0 = fv + (size_t)rb * 32, *F1 = F0 + (size_t)Wn * 32, *F2 = F1 + (size_t)Wn * 32;
+        clu_program<float>(fv, F0, F1, F2, ops, qm, q1, lane);
+        for (int s = 0; s < rb; s++) keep[s * 32] = fv[s * 32 + lane];
+        if (!act) return;
+        for (int j = 0; j < Wn; j++) {
+            const int st = pc[j];
+            yx[st] = (double)F2[j * 32 + lane];
+            yx[n_da + st] = (double)F0[j * 32 + lane];
+            yx[2 * n_da + st] = (double)F1[j * 32 + lane];
+        }
+#pragma unroll
+        for (int t = 0; t < 3; t++) {
+            X0[t] = (double)F2[p3[t] * 32 + lane];
+            X1[t] = (double)F0[p3[t] * 32 + lane];
+            X2[t] = (double)F1[p3[t] * 32 + lane];
+        }
+    } else {
+        // factorisation and solves in FP64
+        clu_program<double>(vals, R0, R1, R2, ops, qm, q1, lane);
         if (Cl.save_lu) {
             double *sv = Cl.save_lu + (((size_t)m * Cl.n_tasks + task) * Cl.n_save) * 32 + lane;
             for (int s = 0; s < rb; s++) sv[s * 32] = vals[s * 32 + lane];
         }
+        if (!act) return;
+        for (int j = 0; j < Wn; j++) {
+            const int st = pc[j];
+            yx[st] = R2[j * 32 + lane];
+            yx[n_da + st] = R0[j * 32 + lane];
+            yx[2 * n_da + st] = R1[j * 32 + lane];
+        }
+#pragma unroll
+        for (int t = 0; t < 3; t++) {
+            X0[t] = R2[p3[t] * 32 + lane];
+            X1[t] = R0[p3[t] * 32 + lane];
+            X2[t] = R1[p3[t] * 32 + lane];
+        }
     }
-    if (!act) return;
-    const int n_da = P.n_diff + P.n_alg;
-    double *yx = W.yx + (size_t)m * 3 * n_da + ws;
-    const int *p3 = Cl.pos3 + cls * 3;
     double *o = W.clout + ((size_t)m * P.n_cl + c) * 8;
-    double Y[3];
-#pragma unroll
-    for (int t = 0; t < 3; t++) Y[t] = R2[p3[t] * 32 + lane];
-    for (int j = 0; j < Wn; j++) {
-        const int st = pc[j];
-        yx[st] = R2[j * 32 + lane];
-        yx[n_da + st] = R0[j * 32 + lane];
-        yx[2 * n_da + st] = R1[j * 32 + lane];
-    }
-    double X1[3], X2[3];
-#pragma unroll
-    for (int t = 0; t < 3; t++) {
-        X1[t] = R0[p3[t] * 32 + lane];
-        X2[t] = R1[p3[t] * 32 + lane];
-    }
     o[0] = Cc[0] * X1[0] + Cc[1] * X1[1] + Cc[2] * X1[2];
     o[1] = Cc[0] * X2[0] + Cc[1] * X2[1] + Cc[2] * X2[2];
     o[2] = Cc[3] * X1[0] + Cc[4] * X1[1] + Cc[5] * X1[2];
     o[3] = Cc[3] * X2[0] + Cc[4] * X2[1] + Cc[5] * X2[2];
-    o[4] = Cc[0] * Y[0] + Cc[1] * Y[1] + Cc[2] * Y[2];
-    o[5] = Cc[3] * Y[0] + Cc[4] * Y[1] + Cc[5] * Y[2];
+    o[4] = Cc[0] * X0[0] + Cc[1] * X0[1] + Cc[2] * X0[2];
+    o[5] = Cc[3] * X0[0] + Cc[4] * X0[1] + Cc[5] * X0[2];
     o[6] = Ic[0];
     o[7] = Ic[1];
     if (mode == 1) {
@@ -231,15 +264,6 @@ __global__ void __launch_bounds__(32) cluster_kernel(DevProblem P, DevWork W, De
     }
 }
 
-// MX_KEEP scenarios of the mixed solver: the FP64 residual and its solve
-// with the kept FP32 LU, nothing else.  Only the residual column is staged in
-// shared memory (W values per lane instead of the whole program's slots), the
-// LU values are read straight from the kept copy, and the op list is the
-// solve part of the program alone, so many more warps fit on an SM.  The
-// solve runs in FP32, like the kept LU it applies: FP64 arithmetic and
-// FP32<->FP64 conversions are scarce on this GPU, and the correction of an
-// iteration on kept factors is inexact at the FP32 level anyway (the residual
-// that drives it stays FP64).
 // Sink of a residual-only evaluation: Jacobian entries are dropped (the
 // compiler removes their arithmetic), residuals go to their positions in the
 // staged residual column.
@@ -254,6 +278,15 @@ struct KeepSink {
     }
 };
 
+// MX_KEEP scenarios of the mixed solver: the FP64 residual and its solve
+// with the kept FP32 LU, nothing else.  Only the residual column is staged in
+// shared memory (W values per lane instead of the whole program's slots), the
+// LU values are read straight from the kept copy, and the op list is the
+// solve part of the program alone, so many more warps fit on an SM.  The
+// solve runs in FP32, like the kept LU it applies: FP64 arithmetic and
+// FP32<->FP64 conversions are scarce on this GPU, and the correction of an
+// iteration on kept factors is inexact at the FP32 level anyway (the residual
+// that drives it stays FP64).
 __global__ void __launch_bounds__(32, 16) cluster_keep_kernel(DevProblem P, DevWork W, DevClu Cl, DevMixed Mx,
                                                              int want_f) {
     extern __shared__ double R2[];   // [max_w][32] FP64 residual by pivot position, then [max_w][32] FP32
@@ -659,7 +692,8 @@ void launch_retry_start(const DevProblem &P, const DevWork &W, const DevMixed &M
 // A mixed solve that ends at itermax or on a non-finite residual with
 // inexact steps is not reported: it is marked for a retry from the step's
 // starting point with exact Newton steps, whose outcome is reported.
-__global__ void __launch_bounds__(1024) check_kernel(DevWork W, DevMixed Mx, int M, double tol, int itermax) {
+__global__ void __launch_bounds__(1024) check_kernel(DevWork W, DevMixed Mx, int M, double tol, int itermax,
+                                                    LoopCtl ctl) {
     bool any = false;
     for (int m = threadIdx.x; m < M; m += blockDim.x) {
         if (!W.active[m]) continue;
@@ -702,11 +736,27 @@ __global__ void __launch_bounds__(1024) check_kernel(DevWork W, DevMixed Mx, int
     if (Mx.on && __syncthreads_or(any))
         for (int m = threadIdx.x; m < M; m += blockDim.x)
             if (W.active[m] && Mx.refac_next[m] == MX_KEEP) Mx.refac_next[m] = MX_FP32;
+    if (!ctl.on) return;
+    // device-driven loop: the next solve, if any, and its factorisations
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int act = atomicAdd(W.flag, 0), n32 = atomicAdd(W.flag + 1, 0), n64 = atomicAdd(W.flag + 2, 0);
+        const int v = ctl.mixed ? (n32 > 0 ? 1 : 0) | (n64 > 0 ? 2 : 0) : 0;
+        cudaGraphSetConditional(ctl.loop, act > 0 ? 1u : 0u);
+        if (ctl.mixed) cudaGraphSetConditional(ctl.var, (unsigned)v);
+        ctl.cnt[0] += 1;
+        if (act > 0) {
+            ctl.cnt[1] += 1;
+            ctl.cnt[2] += n32;
+            ctl.cnt[3] += n64;
+            ctl.cnt[4 + v] += 1;
+        }
+    }
 }
 
 void launch_check(const DevProblem &P, const DevWork &W, const DevMixed &Mx, double tol, int itermax,
-                  cudaStream_t st) {
-    check_kernel<<<1, std::min(1024, (P.M + 31) / 32 * 32), 0, st>>>(W, Mx, P.M, tol, itermax);
+                  const LoopCtl &ctl, cudaStream_t st) {
+    check_kernel<<<1, std::min(1024, (P.M + 31) / 32 * 32), 0, st>>>(W, Mx, P.M, tol, itermax, ctl);
 }
 
 // ---------------------------------------------------------------------------

@@ -353,6 +353,35 @@ __device__ BlkTask stage_block(const DevSym &S, const DevBlk &B, int blk, int m,
     return BlkTask{e0, n, E0, E1, FO, mp, pv};
 }
 
+__device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
+// Pulls the factor entries a block task's sweep will read into L1 before
+// the sweep (and, backward, before the wait on the parent), so that the
+// sweep's column chunks do not each wait on L2.  Forward: columns [0, ns) of
+// every front, one contiguous range; backward: rows [0, ns) of every column.
+// Every address lies inside the front.
+template <class T>
+__device__ void prefetch_block(const DevSym &S, const FrontSel &fs, const BlkTask &t, int m, bool fwd) {
+    const int lane = threadIdx.x & 31;
+    const T *fr = front_base<T>(fs) + (size_t)m * S.front_total;
+    for (int q = 0; q < t.n; q++) {
+        const int4 a = t.E0[q];
+        const int ns = a.z, mm = a.z + a.w;
+        const T *f = fr + t.FO[q];
+        if (fwd) {
+            const uintptr_t l0 = (uintptr_t)f & ~(uintptr_t)127, l1 = (uintptr_t)(f + (size_t)mm * ns - 1);
+            for (uintptr_t ad = l0 + (uintptr_t)lane * 128; ad <= l1; ad += 32 * 128)
+                prefetch_l1(reinterpret_cast<const void *>(ad));
+        } else {
+            for (int c = lane; c < mm; c += 32) {
+                const T *col = f + (size_t)c * mm;
+                prefetch_l1(col);
+                if ((((uintptr_t)col) >> 7) != (((uintptr_t)(col + ns - 1)) >> 7)) prefetch_l1(col + ns - 1);
+            }
+        }
+    }
+}
+
 template <class T>
 __device__ void fwd_block(const DevProblem &P, const DevWork &W, const DevSym &S, const FrontSel &fs,
                           const BlkTask &t, int m, T *vs) {
@@ -599,6 +628,8 @@ __global__ void __launch_bounds__(kTopThreads, 8) fwd_solve_kernel(DevProblem P,
             if (d && fs.fused64) continue;
             const BlkTask bt = stage_block(S, B, blk, m, base, lay, B.map_fwd, true);
             __syncwarp();
+            if (d) prefetch_block<double>(S, fs, bt, m, true);
+            else prefetch_block<float>(S, fs, bt, m, true);
             if (d) fwd_block<double>(P, W, S, fs, bt, m, reinterpret_cast<double *>(base + lay.v));
             else fwd_block<float>(P, W, S, fs, bt, m, reinterpret_cast<float *>(base + lay.v));
             __syncwarp();
@@ -657,6 +688,9 @@ __global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P,
         const int blk = (int)(t / M), m = (int)(t % M);
         if (!W.active[m]) continue;
         const BlkTask bt = stage_block(S, B, blk, m, base, lay, B.map_bwd, false);
+        __syncwarp();
+        if (use64(fs, m)) prefetch_block<double>(S, fs, bt, m, false);
+        else prefetch_block<float>(S, fs, bt, m, false);
         const int par = D.parent[B.ent0[B.blk_ptr[blk + 1] - 1].x];
         if (par >= 0) {
             bool ok = true;

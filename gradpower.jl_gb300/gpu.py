@@ -54,11 +54,12 @@ def library():
         L.gp_cluster_selftest.argtypes = [vp] * 5 + [C.c_double] + [vp] * 4
         L.gp_residual_static.argtypes = [vp, vp, C.c_double, vp]
         L.gp_set_mixed_policy.argtypes = [vp, C.c_int32, C.c_double, C.c_int32, C.c_int32]
+        L.gp_set_profiling.argtypes = [vp, C.c_int32]
         L.gp_adjoint.argtypes = [vp, vp, C.c_int32, vp, vp, C.c_int32, vp, vp, vp, vp]
         for f in ("gp_layout_create", "gp_layout_destroy", "gp_layout_stats", "gp_set_state",
                   "gp_get_state", "gp_integrate", "gp_residual", "gp_last_timing",
                   "gp_restore_initial_state", "gp_reduced_selftest", "gp_cluster_selftest",
-                  "gp_residual_static", "gp_set_mixed_policy", "gp_adjoint"):
+                  "gp_residual_static", "gp_set_mixed_policy", "gp_set_profiling", "gp_adjoint"):
             getattr(L, f).restype = C.c_int32
         _lib = L
     return _lib
@@ -132,9 +133,15 @@ class GpuBatchedLayout:
         iterate of a step, 0 (none) to 3 (cubic)."""
         _check(library().gp_set_mixed_policy(self._h, int(max_age), float(rho_max), int(exact_after), int(predict)))
 
+    def set_profiling(self, on: bool = True):
+        """Host-driven Newton loop with CUDA events around every phase (for
+        timing()); off by default: the loop runs on the device (see
+        gp_set_profiling in include/gradpower_gb300.h).  Same results."""
+        _check(library().gp_set_profiling(self._h, 1 if on else 0))
+
     def timing(self) -> dict:
-        """Device time of the last integrate call by phase (CUDA events on
-        the library's stream, recorded inside its graphs)."""
+        """Device time of the last integrate call (CUDA events on the
+        library's stream); by phase only with set_profiling(True)."""
         out = np.zeros(16)
         _check(library().gp_last_timing(self._h, _p(out)))
         return dict(total_ms=float(out[0]), cluster_ms=float(out[1]), network_ms=float(out[2]),

@@ -200,8 +200,20 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults,
 int32_t gp_residual(gp_layout *L, const double *zold, double dt, int32_t n_faults,
                     const gp_fault *faults, const uint8_t *fault_on, double *f);
 
+/* Newton loop driver.  Off (the default): each Newton solve is one CUDA
+ * graph that runs the whole loop on the device (a WHILE node over solve +
+ * evaluation, conditions set by the convergence-check kernel; the mixed
+ * solver's factorisation variant is a SWITCH node), so the host does not
+ * wait on the GPU between iterations.  On: the host drives the loop, one
+ * evaluation graph and one solve graph per iteration, with CUDA events
+ * around every phase for gp_last_timing.  Both give the same results.
+ * No counterpart in the reference: its Newton loop is host code
+ * (src/schur.jl:285, `for iter = 1:itermax`). */
+int32_t gp_set_profiling(gp_layout *L, int32_t on);
+
 /* Time of the last gp_integrate call split by phase, milliseconds between
- * CUDA events recorded on the library's stream inside the captured graphs:
+ * CUDA events recorded on the library's stream inside the captured graphs
+ * (the phases only with profiling on, gp_set_profiling; zero otherwise):
  * out[0] total, out[1] cluster kernel, out[2] network kernel, out[3]
  * factorisation (all levels), out[4] triangular solves, out[5] Newton
  * iterations summed over steps (max over scenarios), out[6] kernel launches,

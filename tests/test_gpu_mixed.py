@@ -104,3 +104,28 @@ def test_mixed_then_fp64_on_one_layout(G, orc):
     o = run_oracle(orc, c, 20, itermax=30)
     assert np.array_equal(r["iters"], o["iters"])
     assert np.max(np.abs(r["traj"] - o["traj"]) / np.maximum(1.0, np.abs(o["traj"]))) <= 1e-9
+
+
+@pytest.mark.parametrize("solver", [LY.SOLVER_SCHUR_FP64, LY.SOLVER_SCHUR_MIXED])
+def test_device_loop_matches_host_loop(G, solver):
+    """The Newton loop run on the device (conditional graph nodes, the
+    default) and the host-driven loop with phase events take the same
+    iterations and give bit-identical trajectories; the counters agree."""
+    c, w = synthetic_case("planar2k", 4)
+    gbl = G.GpuBatchedLayout(c.dp, c.ps, c.M)
+    try:
+        out = []
+        for prof in (False, True):
+            gbl.set_profiling(prof)
+            gbl.restore_initial_state()
+            r = gbl.integrate(40 * DT, DT, scenario_faults=c.faults, solver=solver)
+            out.append((r, gbl.timing()))
+    finally:
+        gbl.close()
+    (rd, td), (rh, th) = out
+    assert np.all(rd["status"] == 0)
+    assert np.array_equal(rd["status"], rh["status"]) and np.array_equal(rd["iters"], rh["iters"])
+    assert np.array_equal(rd["traj"], rh["traj"])
+    for k in ("newton_iters", "linear_solves", "launches", "factor_launches", "refreshes", "exact_iters"):
+        assert td[k] == th[k], k
+    assert th["solve_ms"] > 0.0 and td["solve_ms"] == 0.0
