@@ -43,7 +43,7 @@ WORKLOAD = "planar70k"
 SCEN_PER_GPU = 8
 TF = 1.0
 DT = 1.0 / 120.0
-SOLVE_TRAFFIC_BYTES = 236e6
+SOLVE_TRAFFIC_BYTES = 197e6
 ADJ_SCEN_PER_GPU = 128
 ADJ_TF = 3.0
 ADJ_STEPS = 2
@@ -348,10 +348,10 @@ def gpu_arm(args):
     passes = accp["linear_solves"] * Mloc if dom == "solve" else (
         accp["refreshes"] if dom == "factor" else accp["newton_iters"] * Mloc)
     achieved = bytes_per_scen * passes / (ms / 1e3) / 1e9 if ms > 0 else 0.0
-    # DRAM bytes per pass of the solve phase (fwd_blocks + fwd_top + bwd_top +
-    # bwd_blocks, 8 scenarios) from one ncu capture of `bench.py --profile
-    # 0.1` (profiles/planar70k_kernels.md); the algorithmic figure above is
-    # 8 x 24.2 MB = 194 MB per pass
+    # DRAM bytes per pass of the solve phase (fwd_solve_kernel +
+    # bwd_solve_kernel, 8 scenarios, FP32 factors) from one ncu capture of
+    # `bench.py --profile 0.15` (profiles/planar70k_kernels.md); the
+    # algorithmic figure above is 8 x 24.2 MB = 194 MB per pass
     traffic = SOLVE_TRAFFIC_BYTES if dom == "solve" else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per pass", "kernel": dom,
