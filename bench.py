@@ -285,6 +285,15 @@ def gpu_arm(args):
     dev64_ms = max_over_ranks(acc64["total_ms"])
     value64 = units / (dev64_ms / 1e3)
 
+    # ---- the shared-factor Woodbury path (the reference's
+    # integrate_gpu_shared_multi!), timed the same way ----
+    WB = LY.SOLVER_SHARED_WOODBURY
+    barrier()
+    accw = timed_runs(gbl, faults, args.steps, WB, flush, torch)
+    barrier()
+    devw_ms = max_over_ranks(accw["total_ms"])
+    valuew = units / (devw_ms / 1e3)
+
     # ---- phase times: one pass of each path with the host-driven loop and
     # CUDA events around every phase (the same kernels; the roofline of the
     # dominant phase and the breakdowns come from here) ----
@@ -299,7 +308,11 @@ def gpu_arm(args):
     gbl.restore_initial_state()
     t_64 = gbl.integrate(TF, DT, scenario_faults=faults, solver=FP64)["traj"]
     errs = state_errors(w, t_mix, t_64)
-    del t_mix, t_64
+    del t_mix
+    gbl.restore_initial_state()
+    t_wb = gbl.integrate(TF, DT, scenario_faults=faults, solver=WB)["traj"]
+    errs_wb = state_errors(w, t_wb, t_64)
+    del t_wb, t_64
 
     # ---- end to end through the public API (host buffers), mixed path ----
     z_host = torch.empty((Mloc, gbl.n_sys), dtype=torch.float64, pin_memory=True).numpy()
@@ -391,6 +404,12 @@ def gpu_arm(args):
         "fp64": {"value": value64, "ms_per_step": dev64_ms / args.steps,
                  "newton_iters_per_run": acc64["newton_iters"] / args.steps, "status_max": acc64["status_max"],
                  "phase_ms": {k: round(accp64[k + "_ms"], 3) for k in ("factor", "solve", "cluster", "network")}},
+        "shared_woodbury": {"value": valuew, "ms_per_step": devw_ms / args.steps,
+                            "newton_iters_per_run": accw["newton_iters"] / args.steps,
+                            "status_max": accw["status_max"], "max_state_err_vs_fp64": errs_wb,
+                            "algorithm": "reduced matrix of scenario 0 at the initial state factored once "
+                                         "per run (FP64), per-scenario fault by a rank-2 Woodbury correction, "
+                                         "exact cluster blocks and residual"},
         "mixed_over_fp64": value / value64,
         "max_state_err_vs_fp64": errs,
         "e2e": e2e,

@@ -116,6 +116,12 @@ struct gp_layout {
     cudaGraphConditionalHandle h_loop = 0, h_var = 0;
     int *d_cnt = nullptr;
     bool profiling = false;      // host-driven loop with phase events (gp_set_profiling)
+    // shared-factor Woodbury path (allocated on first use): W = P^-1 U per
+    // scenario (two columns), H^-1 (2x2), the correction's coefficients, and
+    // the mask that selects scenario 0 for the factorisation of P
+    double *wb_W1 = nullptr, *wb_W2 = nullptr, *wb_Hinv = nullptr, *wb_s = nullptr;
+    uint8_t *d_only0 = nullptr;
+    int solve_graph_factors = 0;   // factorisation launches of the non-mixed solve graph
     bool no_marks = false;       // capturing into a conditional body: no event nodes
     double graph_tol = -1.0;
     int graph_itermax = -1;
@@ -1171,7 +1177,17 @@ int enqueue_solve(gp_layout *L, int variant, int *nfac_out) {
     int launches = 2, facs = 0;   // dag_begin, update
     mark(L, 3);
     gp::launch_dag_begin(D, L->st);
-    if (variant < 0) {
+    if (variant == -2) {
+        // shared-factor Woodbury: the factors of P (scenario 0's slot), the
+        // fault's rank-2 correction, no factorisation
+        const gp::FrontSel fs{nullptr, L->S.fronts, nullptr, 0, 1};
+        mark(L, 4);
+        gp::launch_solve_fwd(L->P, L->W, L->S, B, D, L->SG, fs, L->st);
+        mark(L, 5);
+        gp::launch_solve_bwd(L->P, L->W, L->S, B, D, L->SG, fs, L->st);
+        gp::launch_wb_correct(L->P, L->W, L->wb_W1, L->wb_W2, L->wb_Hinv, L->wb_s, L->st);
+        launches += 2 * nsolve + 2;
+    } else if (variant < 0) {
         const gp::FrontSel fs{nullptr, L->S.fronts, nullptr, 1};
         gp::launch_dag_factor<double>(L->P, L->W, L->S, D, L->G64, L->S.fronts, L->W.active, 1, L->st);
         mark(L, 4);   // the FP64 factorisation includes the forward solve
@@ -1216,7 +1232,7 @@ void enqueue_eval(gp_layout *L, double tol, int itermax, const gp::LoopCtl &ctl)
     mark(L, 0);
     L->eval_launches = 3 + gp::launch_cluster(L->P, L->W, L->C, L->Mx, 0, L->st);
     mark(L, 1);
-    gp::launch_network(L->P, L->W, L->Mx, 0, L->st);
+    gp::launch_network(L->P, L->W, L->Mx, 0, L->st, L->solver == GP_SOLVER_SHARED_WOODBURY ? 1 : 0);
     mark(L, 2);
     gp::launch_check(L->P, L->W, L->Mx, tol, itermax, ctl, L->st);
     if (!ctl.on)
@@ -1274,7 +1290,7 @@ int enqueue_solve(gp_layout *L, int variant, int *nfac_out);
 // solve is a SWITCH over the four factorisation variants, chosen by the
 // check kernel; the FP64 solve is always the same.  No event nodes: the
 // phase timing needs the host-driven loop.
-cudaGraphExec_t build_loop(gp_layout *L, double tol, int itermax, bool mixed) {
+cudaGraphExec_t build_loop(gp_layout *L, double tol, int itermax, bool mixed, int plain_variant) {
     cudaGraph_t g;
     ck(cudaGraphCreate(&g, 0), "graph create");
     ck(cudaGraphConditionalHandleCreate(&L->h_loop, g, 0, cudaGraphCondAssignDefault), "conditional handle");
@@ -1293,8 +1309,9 @@ cudaGraphExec_t build_loop(gp_layout *L, double tol, int itermax, bool mixed) {
             capture_into(L, var[v], nullptr, 0,
                          [&] { L->mix_launches[v] = enqueue_solve(L, v, &L->mix_factor_launches[v]); });
     } else {
-        int nf = 0;
-        solved = capture_into(L, body, nullptr, 0, [&] { L->solve_graph_launches = enqueue_solve(L, -1, &nf); });
+        solved = capture_into(L, body, nullptr, 0, [&] {
+            L->solve_graph_launches = enqueue_solve(L, plain_variant, &L->solve_graph_factors);
+        });
     }
     capture_into(L, body, &solved, 1, [&] { enqueue_eval(L, tol, itermax, ctl); });
     L->no_marks = false;
@@ -1310,7 +1327,7 @@ void harvest_counts(gp_layout *L) {
     ck(cudaMemcpy(c, L->d_cnt, sizeof(c), cudaMemcpyDeviceToHost), "count copy");
     ck(cudaMemset(L->d_cnt, 0, sizeof(c)), "memset");
     const bool mixed = L->Mx.on != 0;
-    const int nfac = (L->D.n_small > 0) + (L->D.nsup > L->D.n_small);
+    const int nfac = L->solve_graph_factors;
     L->launches += (double)c[0] * L->eval_launches;
     L->solves += c[1];
     L->refreshes += c[2];
@@ -1361,6 +1378,53 @@ void ensure_mixed(gp_layout *L) {
     L->mixed_ready = true;
 }
 
+// Buffers of the shared-factor Woodbury path, allocated on its first use.
+void ensure_woodbury(gp_layout *L) {
+    if (L->wb_W1) return;
+    DeviceArena &A = L->arena;
+    const size_t M = L->M, nr = std::max(1, L->P.n_red);
+    L->wb_W1 = A.alloc<double>(M * nr);
+    L->wb_W2 = A.alloc<double>(M * nr);
+    L->wb_Hinv = A.alloc<double>(M * 4);
+    L->wb_s = A.alloc<double>(M * 2);
+    std::vector<uint8_t> only0(M, 0);
+    only0[0] = 1;
+    L->d_only0 = A.upload(only0);
+}
+
+// Start of a shared-factor Woodbury integration: P, the reduced matrix of
+// scenario 0 at the initial state with the call's dt and no fault, is
+// factored once into scenario 0's front slot (_factor_shared_P_gpu!,
+// ext/GradPowerCUDAExt/GradPowerCUDAExt.jl:2149-2172); then per scenario
+// W = P^-1 [e_vr e_vi] at its fault bus and H^-1
+// (_precompute_woodbury_multi_gpu!, :2441-2489).
+void wb_prepare(gp_layout *L, double dt) {
+    const int M = L->M;
+    gp::launch_set_double(L->W.dt, dt, L->st);
+    ck(cudaMemcpyAsync(L->W.zold, L->W.z, (size_t)M * L->n_sys * sizeof(double), cudaMemcpyDeviceToDevice, L->st),
+       "zold");
+    ck(cudaMemsetAsync(L->W.active, 1, M, L->st), "memset");
+    gp::launch_reset_norm(L->P, L->W, L->Mx, L->st);
+    gp::launch_cluster(L->P, L->W, L->C, L->Mx, 0, L->st);
+    gp::launch_network(L->P, L->W, L->Mx, 0, L->st);
+    gp::launch_dag_begin(L->D, L->st);
+    gp::launch_dag_factor<double>(L->P, L->W, L->S, L->D, L->G64, L->S.fronts, L->d_only0, 1, L->st);
+    const gp::FrontSel fs{nullptr, L->S.fronts, nullptr, 0, 1};
+    double *cols[2] = {L->wb_W1, L->wb_W2};
+    for (int c = 0; c < 2; c++) {
+        gp::launch_wb_unit(L->P, L->W, c, L->st);
+        gp::launch_dag_begin(L->D, L->st);
+        gp::launch_solve_fwd(L->P, L->W, L->S, L->B, L->D, L->SG, fs, L->st);
+        gp::launch_solve_bwd(L->P, L->W, L->S, L->B, L->D, L->SG, fs, L->st);
+        ck(cudaMemcpyAsync(cols[c], L->W.xperm, (size_t)M * L->P.n_red * sizeof(double), cudaMemcpyDeviceToDevice,
+                           L->st),
+           "woodbury column");
+    }
+    gp::launch_wb_setup(L->P, L->wb_W1, L->wb_W2, L->wb_Hinv, L->st);
+    L->launches += 14 + (L->D.n_small > 0) + (L->D.nsup > L->D.n_small);
+    L->factor_launches += (L->D.n_small > 0) + (L->D.nsup > L->D.n_small);
+}
+
 void ensure_graphs(gp_layout *L, double tol, int itermax, int solver) {
     if (L->solver != solver || L->graph_tol != tol || L->graph_itermax != itermax) drop_graphs(L);
     const bool mixed = solver == GP_SOLVER_SCHUR_MIXED;
@@ -1369,15 +1433,15 @@ void ensure_graphs(gp_layout *L, double tol, int itermax, int solver) {
     L->graph_tol = tol;
     L->graph_itermax = itermax;
     L->solver = solver;
+    const int plain = solver == GP_SOLVER_SHARED_WOODBURY ? -2 : -1;
+    if (solver == GP_SOLVER_SHARED_WOODBURY) ensure_woodbury(L);
     if (!L->profiling) {
-        if (!L->g_loop) L->g_loop = build_loop(L, tol, itermax, mixed);
+        if (!L->g_loop) L->g_loop = build_loop(L, tol, itermax, mixed, plain);
         return;
     }
     if (!L->g_eval) L->g_eval = capture(L, [&] { enqueue_eval(L, tol, itermax, gp::LoopCtl{0, 0, nullptr, 0, 0}); });
-    if (!mixed && !L->g_solve) {
-        int nf = 0;
-        L->g_solve = capture(L, [&] { L->solve_graph_launches = enqueue_solve(L, -1, &nf); });
-    }
+    if (!mixed && !L->g_solve)
+        L->g_solve = capture(L, [&] { L->solve_graph_launches = enqueue_solve(L, plain, &L->solve_graph_factors); });
 }
 
 // Solve graph of the mixed solver for the modes present (captured on first use).
@@ -1441,7 +1505,7 @@ void newton(gp_layout *L, double dt, double tol, int itermax, bool force_refresh
         } else {
             ck(cudaGraphLaunch(L->g_solve, L->st), "graph launch");
             L->launches += L->solve_graph_launches;
-            L->factor_launches += (L->D.n_small > 0) + (L->D.nsup > L->D.n_small);
+            L->factor_launches += L->solve_graph_factors;
         }
         solve_pending = true;
         L->solves += 1;
@@ -1647,8 +1711,22 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
     API_BEGIN
     if (!L || !opt) fail(GP_E_INVALID, "null argument");
     if (opt->n_steps < 0 || !(opt->dt > 0.0) || opt->itermax <= 0) fail(GP_E_INVALID, "bad options");
-    if (opt->solver != GP_SOLVER_SCHUR_FP64 && opt->solver != GP_SOLVER_SCHUR_MIXED)
+    if (opt->solver != GP_SOLVER_SCHUR_FP64 && opt->solver != GP_SOLVER_SCHUR_MIXED &&
+        opt->solver != GP_SOLVER_SHARED_WOODBURY)
         fail(GP_E_INVALID, "solver %d is not available", opt->solver);
+    if (opt->solver == GP_SOLVER_SHARED_WOODBURY) {
+        // one fault (bus, rfault) per scenario: its rank-2 correction of P
+        std::vector<int> fb(L->M, -1);
+        std::vector<double> fr(L->M, 0.0);
+        for (int e = 0; e < n_faults; e++)
+            for (int m = 0; m < L->M; m++) {
+                if (faults[e].scenario >= 0 && faults[e].scenario != m) continue;
+                if (fb[m] >= 0 && (fb[m] != faults[e].bus || fr[m] != faults[e].rfault))
+                    fail(GP_E_INVALID, "shared-factor Woodbury solver: scenario %d has more than one fault bus", m);
+                fb[m] = faults[e].bus;
+                fr[m] = faults[e].rfault;
+            }
+    }
     const int M = L->M, ns = opt->n_steps, nsys = L->n_sys;
     set_faults(L, n_faults, faults);
     ensure_graphs(L, opt->newton_tol, opt->itermax, opt->solver);
@@ -1680,6 +1758,7 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
     L->retries = 0;
     for (int i = 0; i < 8; i++) L->ph_ms[i] = 0.0;
     ck(cudaMemsetAsync(L->D.err, 0, sizeof(int), L->st), "memset");
+    if (opt->solver == GP_SOLVER_SHARED_WOODBURY) wb_prepare(L, opt->dt);
     // the mixed solver refreshes its kept factors at the first solve and
     // around every event (the dt = 0 re-solve and the step after it); with
     // prediction on, it starts every step from the polynomial extrapolation

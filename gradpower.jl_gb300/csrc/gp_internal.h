@@ -199,6 +199,7 @@ struct FrontSel {
     const double *f64;
     const uint8_t *mode;
     int fused64;
+    int shared;    // every scenario solves with scenario 0's factors (shared-factor Woodbury path)
 };
 
 struct SolveGrid {
@@ -217,7 +218,21 @@ int solve_block_front_limit();
 // launches (gp_kernels.cu)
 int launch_cluster(const DevProblem &P, const DevWork &W, const DevClu &C, const DevMixed &Mx, int want_f,
                     cudaStream_t st);
-void launch_network(const DevProblem &P, const DevWork &W, const DevMixed &Mx, int want_f, cudaStream_t st);
+// skip_s: the entries of S are not needed (shared-factor Woodbury path)
+void launch_network(const DevProblem &P, const DevWork &W, const DevMixed &Mx, int want_f, cudaStream_t st,
+                    int skip_s = 0);
+
+// Shared-factor Woodbury path: per scenario, its fault (one bus and
+// admittance, possibly several on/off windows) is a rank-2 change of the
+// shared reduced matrix P.  wb_unit: xperm[m] = the unit vector at the
+// fault bus's vr (col 0) or vi (col 1) row, zero without a fault.
+// wb_setup: H = U^T W - I/yf and its inverse per scenario.  wb_correct: the
+// Woodbury correction of the solution x = P^-1 rhs of the scenarios whose
+// fault is on, x -= W H^-1 U^T x.
+void launch_wb_unit(const DevProblem &P, const DevWork &W, int col, cudaStream_t st);
+void launch_wb_setup(const DevProblem &P, const double *W1, const double *W2, double *Hinv, cudaStream_t st);
+void launch_wb_correct(const DevProblem &P, const DevWork &W, const double *W1, const double *W2,
+                       const double *Hinv, double *s, cudaStream_t st);
 // Control of a Newton loop run on the device (a CUDA graph whose WHILE node
 // repeats solve + evaluation): the check kernel sets the loop condition
 // (some scenario still iterating) and, for the mixed solver, the SWITCH

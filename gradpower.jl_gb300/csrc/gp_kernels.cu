@@ -395,7 +395,8 @@ int cluster_smem_optin(int bytes) {
 // With the mixed solver, a scenario iterating on kept factors needs only the
 // residual and the right-hand side: the entries of S (diagonal blocks,
 // static-generator couplings) are skipped for it.
-__global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, DevMixed Mx, int want_f) {
+__global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, DevMixed Mx, int want_f,
+                                                      int skip_s) {
     const long long task = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = task < (long long)P.M * P.n_bus;
     const int m = valid ? (int)(task / P.n_bus) : P.M;
@@ -403,7 +404,7 @@ __global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, D
     const bool act = valid && W.active[m];
     unsigned long long nb = 0ull;
     if (act) {
-        const bool need_s = !(Mx.on && Mx.refac[m] == MX_KEEP);
+        const bool need_s = !skip_s && !(Mx.on && Mx.refac[m] == MX_KEEP);
         const double *z = W.z + (size_t)m * P.n_sys;
         const double *p = W.p + (size_t)m * P.n_par;
         const int net = P.net;
@@ -576,10 +577,105 @@ __global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, D
     if (act && (lane == 0 || mprev != m)) atomicMax(W.norm + m, nb);
 }
 
-void launch_network(const DevProblem &P, const DevWork &W, const DevMixed &Mx, int want_f, cudaStream_t st) {
+void launch_network(const DevProblem &P, const DevWork &W, const DevMixed &Mx, int want_f, cudaStream_t st,
+                    int skip_s) {
     long long tasks = (long long)P.M * P.n_bus;
     int blocks = (int)((tasks + 255) / 256);
-    network_kernel<<<blocks, 256, 0, st>>>(P, W, Mx, want_f);
+    network_kernel<<<blocks, 256, 0, st>>>(P, W, Mx, want_f, skip_s);
+}
+
+// ---------------------------------------------------------------------------
+// shared-factor Woodbury path
+// ---------------------------------------------------------------------------
+// The reduced matrix P (scenario 0 at the call's initial state, no fault) is
+// factored once per call and shared by every scenario and iteration.  A
+// scenario's fault (bus b, admittance yf) subtracts yf from the two
+// diagonal entries of its bus: S_m = P - yf U U^T with U = [e_vr e_vi], and
+// by the Woodbury identity S_m^-1 r = x - W H^-1 U^T x, x = P^-1 r,
+// W = P^-1 U, H = U^T W - I / yf (integrate_gpu_shared_multi!,
+// ext/GradPowerCUDAExt/GradPowerCUDAExt.jl:2441-2489, 2560-2574; every
+// scenario of the table has one fault bus and admittance, checked by the
+// host).
+
+// The scenario's fault: its first table entry (-1: none); *on when one of
+// its windows is on.
+__device__ __forceinline__ int wb_fault(const DevProblem &P, int m, bool *on) {
+    const int e0 = P.fl_ptr[m], e1 = P.fl_ptr[m + 1];
+    bool any = false;
+    for (int e = e0; e < e1; e++) any = any || P.fl_on[e];
+    *on = any;
+    return e0 < e1 ? e0 : -1;
+}
+
+__global__ void wb_unit_kernel(DevProblem P, DevWork W, int col) {
+    const long long task = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (task >= (long long)P.M * P.n_red) return;
+    const int m = (int)(task / P.n_red), i = (int)(task % P.n_red);
+    bool on;
+    const int e = wb_fault(P, m, &on);
+    W.xperm[task] = e >= 0 && i == P.iperm[2 * P.fl_bus[e] + col] ? 1.0 : 0.0;
+}
+
+__global__ void wb_setup_kernel(DevProblem P, const double *W1, const double *W2, double *Hinv) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= P.M) return;
+    bool on;
+    const int e = wb_fault(P, m, &on);
+    double *h = Hinv + 4 * (size_t)m;
+    if (e < 0) {
+        h[0] = h[1] = h[2] = h[3] = 0.0;
+        return;
+    }
+    const size_t o = (size_t)m * P.n_red;
+    const int r0 = P.iperm[2 * P.fl_bus[e]], r1 = P.iperm[2 * P.fl_bus[e] + 1];
+    const double rf = 1.0 / P.fl_yf[e];
+    const double a = W1[o + r0] - rf, b = W2[o + r0], c = W1[o + r1], d = W2[o + r1] - rf;
+    const double det = a * d - b * c;
+    h[0] = d / det;
+    h[1] = -b / det;
+    h[2] = -c / det;
+    h[3] = a / det;
+}
+
+__global__ void wb_dots_kernel(DevProblem P, DevWork W, const double *Hinv, double *sv) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= P.M) return;
+    bool on;
+    const int e = wb_fault(P, m, &on);
+    double s0 = 0.0, s1 = 0.0;
+    if (e >= 0 && on && W.active[m]) {
+        const double *x = W.xperm + (size_t)m * P.n_red;
+        const double t0 = x[P.iperm[2 * P.fl_bus[e]]], t1 = x[P.iperm[2 * P.fl_bus[e] + 1]];
+        const double *h = Hinv + 4 * (size_t)m;
+        s0 = h[0] * t0 + h[1] * t1;
+        s1 = h[2] * t0 + h[3] * t1;
+    }
+    sv[2 * m] = s0;
+    sv[2 * m + 1] = s1;
+}
+
+__global__ void wb_apply_kernel(DevProblem P, DevWork W, const double *W1, const double *W2, const double *sv) {
+    const long long task = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (task >= (long long)P.M * P.n_red) return;
+    const int m = (int)(task / P.n_red);
+    const double s0 = sv[2 * m], s1 = sv[2 * m + 1];
+    if (s0 != 0.0 || s1 != 0.0) W.xperm[task] -= W1[task] * s0 + W2[task] * s1;
+}
+
+void launch_wb_unit(const DevProblem &P, const DevWork &W, int col, cudaStream_t st) {
+    const long long tasks = (long long)P.M * P.n_red;
+    wb_unit_kernel<<<(unsigned)((tasks + 255) / 256), 256, 0, st>>>(P, W, col);
+}
+
+void launch_wb_setup(const DevProblem &P, const double *W1, const double *W2, double *Hinv, cudaStream_t st) {
+    wb_setup_kernel<<<(P.M + 127) / 128, 128, 0, st>>>(P, W1, W2, Hinv);
+}
+
+void launch_wb_correct(const DevProblem &P, const DevWork &W, const double *W1, const double *W2,
+                       const double *Hinv, double *s, cudaStream_t st) {
+    wb_dots_kernel<<<(P.M + 127) / 128, 128, 0, st>>>(P, W, Hinv, s);
+    const long long tasks = (long long)P.M * P.n_red;
+    wb_apply_kernel<<<(unsigned)((tasks + 255) / 256), 256, 0, st>>>(P, W, W1, W2, s);
 }
 
 // ---------------------------------------------------------------------------

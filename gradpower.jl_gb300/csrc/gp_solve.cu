@@ -324,8 +324,8 @@ struct BlkTask {
 };
 
 // Stages the block's entries, front offsets, index maps and (forward) the
-// pivot permutations; the caller syncs.
-__device__ BlkTask stage_block(const DevSym &S, const DevBlk &B, int blk, int m, unsigned char *base,
+// pivot permutations of the factors of scenario mf; the caller syncs.
+__device__ BlkTask stage_block(const DevSym &S, const DevBlk &B, int blk, int mf, unsigned char *base,
                                const BlkLayout &lay, const int *map, bool with_piv) {
     const int lane = threadIdx.x & 31;
     int4 *E0 = reinterpret_cast<int4 *>(base + lay.e0);
@@ -344,7 +344,7 @@ __device__ BlkTask stage_block(const DevSym &S, const DevBlk &B, int blk, int m,
     for (int i = lane; i < nmap; i += 32) mp[i] = map[mb + i];
     __syncwarp();
     if (with_piv) {
-        const int *ip = S.ipiv + (size_t)m * S.n;
+        const int *ip = S.ipiv + (size_t)mf * S.n;
         for (int q = 0; q < n; q++) {
             const int4 a = E0[q], b = E1[q];
             for (int i = lane; i < a.z; i += 32) pv[b.w + i] = ip[a.y + i];
@@ -363,7 +363,7 @@ __device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefe
 template <class T>
 __device__ void prefetch_block(const DevSym &S, const FrontSel &fs, const BlkTask &t, int m, bool fwd) {
     const int lane = threadIdx.x & 31;
-    const T *fr = front_base<T>(fs) + (size_t)m * S.front_total;
+    const T *fr = front_base<T>(fs) + (size_t)(fs.shared ? 0 : m) * S.front_total;
     for (int q = 0; q < t.n; q++) {
         const int4 a = t.E0[q];
         const int ns = a.z, mm = a.z + a.w;
@@ -392,7 +392,7 @@ __device__ void fwd_block(const DevProblem &P, const DevWork &W, const DevSym &S
         for (int i = lane; i < a.z + a.w; i += 32) vs[b.y + i] = i < a.z ? (T)x[a.y + i] : T(0);
     }
     __syncwarp();
-    const T *fr = front_base<T>(fs) + (size_t)m * S.front_total;
+    const T *fr = front_base<T>(fs) + (size_t)(fs.shared ? 0 : m) * S.front_total;
     double *xo = W.xperm + (size_t)m * P.n_red;
     double *uv = S.uvec + (size_t)m * S.uvec_total;
     for (int q = 0; q < t.n; q++) {
@@ -425,7 +425,7 @@ __device__ void bwd_block(const DevProblem &P, const DevWork &W, const DevSym &S
     const int xb = B.ext_ptr[blk], next = B.ext_ptr[blk + 1] - xb;
     for (int k = lane; k < next; k += 32) vs[B.ext_pos[xb + k]] = (T)x[B.ext_row[xb + k]];
     __syncwarp();
-    const T *fr = front_base<T>(fs) + (size_t)m * S.front_total;
+    const T *fr = front_base<T>(fs) + (size_t)(fs.shared ? 0 : m) * S.front_total;
     for (int q = t.n - 1; q >= 0; q--) {
         const int4 a = t.E0[q], b = t.E1[q];
         const int ns = a.z, r = a.w;
@@ -504,11 +504,11 @@ __device__ void fwd_top_task(const DevProblem &P, const DevWork &W, const DevSym
     int *sxr = reinterpret_cast<int *>(smem + top_vec_bytes(tmf));
     int *sxe = sxr + align16((tmf + 1) * 4) / 4;
     T *Fs = reinterpret_cast<T *>(smem + top_vec_bytes(tmf) + top_idx_bytes(tmf, B.top_max_xent));
-    const T *F = front_base<T>(fs) + (size_t)t.m * S.front_total + S.front_off[t.s];
+    const T *F = front_base<T>(fs) + (size_t)(fs.shared ? 0 : t.m) * S.front_total + S.front_off[t.s];
     const int cap = kTopStage / ((int)sizeof(T) * t.mm);   // columns per staged chunk
     double *x = W.xperm + (size_t)t.m * P.n_red;
     double *uv = S.uvec + (size_t)t.m * S.uvec_total;
-    const int *ip = S.ipiv + (size_t)t.m * S.n + t.start;
+    const int *ip = S.ipiv + (size_t)(fs.shared ? 0 : t.m) * S.n + t.start;
     // independent of other tasks: own entries, pivot permutation, factor
     // columns and the extend-add lists, all fetched before the wait so that
     // only the children's update entries remain on the path after it
@@ -562,7 +562,7 @@ __device__ void bwd_top_task(const DevProblem &P, const DevWork &W, const DevSym
     T *v = reinterpret_cast<T *>(smem);
     int *pi = reinterpret_cast<int *>(smem + tmf * 16);
     T *Fs = reinterpret_cast<T *>(smem + top_vec_bytes(tmf));
-    const T *F = front_base<T>(fs) + (size_t)t.m * S.front_total + S.front_off[t.s];
+    const T *F = front_base<T>(fs) + (size_t)(fs.shared ? 0 : t.m) * S.front_total + S.front_off[t.s];
     const int cap = kTopStage / ((int)sizeof(T) * max(1, t.ns));   // columns per staged chunk
     double *x = W.xperm + (size_t)t.m * P.n_red;
     const int *rows = S.rows + S.row_ptr[t.s];
@@ -626,7 +626,7 @@ __global__ void __launch_bounds__(kTopThreads, 8) fwd_solve_kernel(DevProblem P,
             if (!W.active[m]) continue;
             const bool d = use64(fs, m);
             if (d && fs.fused64) continue;
-            const BlkTask bt = stage_block(S, B, blk, m, base, lay, B.map_fwd, true);
+            const BlkTask bt = stage_block(S, B, blk, fs.shared ? 0 : m, base, lay, B.map_fwd, true);
             __syncwarp();
             if (d) prefetch_block<double>(S, fs, bt, m, true);
             else prefetch_block<float>(S, fs, bt, m, true);
@@ -687,7 +687,7 @@ __global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P,
         if (t >= n_blk) break;
         const int blk = (int)(t / M), m = (int)(t % M);
         if (!W.active[m]) continue;
-        const BlkTask bt = stage_block(S, B, blk, m, base, lay, B.map_bwd, false);
+        const BlkTask bt = stage_block(S, B, blk, fs.shared ? 0 : m, base, lay, B.map_bwd, false);
         __syncwarp();
         if (use64(fs, m)) prefetch_block<double>(S, fs, bt, m, false);
         else prefetch_block<float>(S, fs, bt, m, false);

@@ -240,6 +240,22 @@ def integrate_gpu_cudss(gbl: GpuBatchedLayout, ps: Mdl.PowerSystem, tf: float,
     return integrate_gpu_schur_cudss(gbl, ps, tf, dt, newton_tol, scenario_faults)
 
 
+def integrate_gpu_shared_multi(gbl: GpuBatchedLayout, ps: Mdl.PowerSystem, tf: float, fault_buses, rfaults,
+                               ton: float, toff: float, dt: float = 1.0 / 120.0, newton_tol: float = 1e-10):
+    """(tvec, trajs): the reference's shared-factor integrator with a
+    per-scenario Woodbury correction
+    (ext/GradPowerCUDAExt/GradPowerCUDAExt.jl:2640-2708): scenario m faults
+    bus fault_buses[m] (0-based here) through rfaults[m] from ton to toff;
+    the reduced matrix of scenario 0 at the initial state is factored once
+    and shared (GP_SOLVER_SHARED_WOODBURY)."""
+    if len(fault_buses) != gbl.M or len(rfaults) != gbl.M:
+        raise ValueError("one fault bus and rfault per scenario")
+    faults = [[Mdl.ContingencyEvent(int(b), float(r), float(ton), float(toff))]
+              for b, r in zip(fault_buses, rfaults)]
+    r = gbl.integrate(tf, dt, newton_tol, 30, (), faults, solver=LY.SOLVER_SHARED_WOODBURY)
+    return r["tvec"], [r["traj"][m].T for m in range(gbl.M)]
+
+
 class BatchedLayout(GpuBatchedLayout):
     """The reference's CPU batch container (src/batched.jl:16-72), same
     constructor `BatchedLayout(dp, ps, M)`; here the batch lives on the GPU

@@ -26,6 +26,7 @@ NTYPES = 8
 
 SOLVER_SCHUR_FP64 = 0
 SOLVER_SCHUR_MIXED = 1
+SOLVER_SHARED_WOODBURY = 2
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)

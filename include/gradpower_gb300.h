@@ -136,6 +136,19 @@ typedef struct gp_fault {
 /* GP_SOLVER_SCHUR_FP64: exact Newton, the reference's batched schedule: the
  *   cluster blocks and the reduced network matrix are factored in FP64 at
  *   every iteration.
+ * GP_SOLVER_SHARED_WOODBURY: integrate_gpu_shared_multi!
+ *   (ext/GradPowerCUDAExt/GradPowerCUDAExt.jl:2640-2708, Newton step
+ *   :2523-2627): the reduced network matrix P of scenario 0 at the initial
+ *   state (no fault, the call's dt) is factored once per call and shared by
+ *   every scenario, iteration and step; a scenario's fault enters as the
+ *   rank-2 Woodbury correction of P at its bus.  The cluster blocks, the
+ *   residual and the convergence test are exact at every iteration, so the
+ *   result is the same root to the same tolerance, reached by a chord
+ *   iteration (linear convergence).  Each scenario may have one fault bus
+ *   and rfault (several on/off windows allowed; they must not overlap).
+ *   The reference shares ton/toff over the scenarios and stops on the L2
+ *   norm over all of them; here every scenario has its own windows and its
+ *   own infinity-norm test, as the other solvers.
  * GP_SOLVER_SCHUR_MIXED: the cluster blocks' LU and the reduced-system
  *   factors are kept in FP32 and reused across Newton iterations and steps;
  *   every iteration evaluates the residual in FP64 and corrects with the
@@ -146,6 +159,7 @@ typedef struct gp_fault {
  *   policy of gp_set_mixed_policy. */
 #define GP_SOLVER_SCHUR_FP64   0
 #define GP_SOLVER_SCHUR_MIXED  1
+#define GP_SOLVER_SHARED_WOODBURY 2
 
 typedef struct gp_options {
     double dt;

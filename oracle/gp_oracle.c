@@ -1204,103 +1204,151 @@ static int newton_mono(newton_ws *W, double *z, const double *zold, const double
     return it;
 }
 
+/* One Schur reduction at the iterate zb (src/schur.jl:285-360): the BE
+ * residual into W->f, J, the reduced matrix S = J_red - sum_k C_k A_k^-1 B_k
+ * into S->S.val and the reduced right-hand side -(f_red - sum_k C_k A_k^-1
+ * f_wk) into W->rhs.  Returns the residual's infinity norm. */
+static double schur_reduce(newton_ws *W, const double *zold, const double *u0, const double *p, const faults_t *F,
+                           double dt) {
+    sym_t *S = W->S;
+    const gp_problem *P = S->P;
+    int n = S->nsys, nr = S->n_red;
+    residual_be(P, W->zb, zold, u0, p, F, dt, W->f);
+    double nf = inf_norm(W->f, n);
+    assemble_J(S, W->zb, u0, p, F, dt, &W->t);
+    /* S := J restricted to the reduced set */
+    memset(S->S.val, 0, sizeof(double) * S->S.nnz);
+    for (int lj = 0; lj < nr; lj++) {
+        int gj = S->red_idx[lj];
+        for (int q = S->J.colptr[gj]; q < S->J.colptr[gj + 1]; q++) {
+            int li = S->g2r[S->J.rowind[q]];
+            if (li >= 0) S->S.val[csc_find(&S->S, li, lj)] = S->J.val[q];
+        }
+    }
+    for (int i = 0; i < nr; i++) W->rhs[i] = W->f[S->red_idx[i]];
+    /* per non-trivial cluster */
+    for (int ci = 0; ci < S->nt; ci++) {
+        int c = S->nt_cl[ci];
+        int ws = P->cl_w_start[c], wk = P->cl_w_size[c], bus = P->cl_bus[c];
+        int vr_g = S->net + 2 * bus, vr_l = S->g2r[vr_g], vi_l = S->g2r[vr_g + 1];
+        double *A = W->Ak, *B = W->Bk, *C = W->Ck;
+        memset(A, 0, sizeof(double) * wk * wk);
+        memset(B, 0, sizeof(double) * wk * 2);
+        memset(C, 0, sizeof(double) * wk * 2);
+        for (int j = 0; j < wk; j++)
+            for (int q = S->J.colptr[ws + j]; q < S->J.colptr[ws + j + 1]; q++) {
+                int r = S->J.rowind[q];
+                if (r >= ws && r < ws + wk) A[(r - ws) + j * wk] = S->J.val[q];
+                else if (r == vr_g) C[0 + 2 * j] = S->J.val[q];
+                else if (r == vr_g + 1) C[1 + 2 * j] = S->J.val[q];
+            }
+        for (int b2 = 0; b2 < 2; b2++)
+            for (int q = S->J.colptr[vr_g + b2]; q < S->J.colptr[vr_g + b2 + 1]; q++) {
+                int r = S->J.rowind[q];
+                if (r >= ws && r < ws + wk) B[(r - ws) + b2 * wk] = S->J.val[q];
+            }
+        dense_lu(A, W->ipiv, wk);
+        double D[4];
+        for (int b2 = 0; b2 < 2; b2++) {
+            for (int i = 0; i < wk; i++) W->tmp[i] = B[i + b2 * wk];
+            dense_solve(A, W->ipiv, W->tmp, wk);
+            double d1 = 0, d2 = 0;
+            for (int i = 0; i < wk; i++) { d1 += C[0 + 2 * i] * W->tmp[i]; d2 += C[1 + 2 * i] * W->tmp[i]; }
+            D[0 + 2 * b2] = d1;
+            D[1 + 2 * b2] = d2;
+        }
+        S->S.val[csc_find(&S->S, vr_l, vr_l)] -= D[0];
+        S->S.val[csc_find(&S->S, vi_l, vr_l)] -= D[1];
+        S->S.val[csc_find(&S->S, vr_l, vi_l)] -= D[2];
+        S->S.val[csc_find(&S->S, vi_l, vi_l)] -= D[3];
+        for (int i = 0; i < wk; i++) W->tmp[i] = W->f[ws + i];
+        dense_solve(A, W->ipiv, W->tmp, wk);
+        for (int i = 0; i < wk; i++) {
+            W->rhs[vr_l] -= C[0 + 2 * i] * W->tmp[i];
+            W->rhs[vi_l] -= C[1 + 2 * i] * W->tmp[i];
+        }
+    }
+    for (int i = 0; i < nr; i++) W->rhs[i] = -W->rhs[i];
+    return nf;
+}
+
+/* Back-substitution of the cluster rows from the reduced solution in
+ * W->rhs, then zb += dz (src/schur.jl:380-420). */
+static void schur_backsub(newton_ws *W) {
+    sym_t *S = W->S;
+    const gp_problem *P = S->P;
+    int n = S->nsys, nr = S->n_red;
+    for (int i = 0; i < nr; i++) W->dz[S->red_idx[i]] = W->rhs[i];
+    /* recompute each cluster's factor (values are kept only for the
+     * current cluster in this restatement) */
+    for (int ci = 0; ci < S->nt; ci++) {
+        int c = S->nt_cl[ci];
+        int ws = P->cl_w_start[c], wk = P->cl_w_size[c], bus = P->cl_bus[c];
+        int vr_g = S->net + 2 * bus;
+        double *A = W->Ak, *B = W->Bk;
+        memset(A, 0, sizeof(double) * wk * wk);
+        memset(B, 0, sizeof(double) * wk * 2);
+        for (int j = 0; j < wk; j++)
+            for (int q = S->J.colptr[ws + j]; q < S->J.colptr[ws + j + 1]; q++) {
+                int r = S->J.rowind[q];
+                if (r >= ws && r < ws + wk) A[(r - ws) + j * wk] = S->J.val[q];
+            }
+        for (int b2 = 0; b2 < 2; b2++)
+            for (int q = S->J.colptr[vr_g + b2]; q < S->J.colptr[vr_g + b2 + 1]; q++) {
+                int r = S->J.rowind[q];
+                if (r >= ws && r < ws + wk) B[(r - ws) + b2 * wk] = S->J.val[q];
+            }
+        dense_lu(A, W->ipiv, wk);
+        double dv1 = W->dz[vr_g], dv2 = W->dz[vr_g + 1];
+        for (int i = 0; i < wk; i++) W->tmp[i] = W->f[ws + i] + B[i] * dv1 + B[i + wk] * dv2;
+        dense_solve(A, W->ipiv, W->tmp, wk);
+        for (int i = 0; i < wk; i++) W->dz[ws + i] = -W->tmp[i];
+    }
+    for (int i = 0; i < n; i++) W->zb[i] += W->dz[i];
+}
+
 /* newton_step_schur! (src/schur.jl:253-426). */
 static int newton_schur(newton_ws *W, double *z, const double *zold, const double *u0, const double *p,
                         const faults_t *F, double dt, double tol, int itermax, int *ok) {
     sym_t *S = W->S;
-    const gp_problem *P = S->P;
-    int n = S->nsys, nr = S->n_red;
+    int n = S->nsys;
     memcpy(W->zb, z, sizeof(double) * n);
     *ok = 0;
     int it;
     for (it = 0; it < itermax; it++) {
-        residual_be(P, W->zb, zold, u0, p, F, dt, W->f);
-        double nf = inf_norm(W->f, n);
+        double nf = schur_reduce(W, zold, u0, p, F, dt);
         if (nf < tol) { *ok = 1; break; }
         if (!isfinite(nf)) break;
-        assemble_J(S, W->zb, u0, p, F, dt, &W->t);
-        /* S := J restricted to the reduced set */
-        memset(S->S.val, 0, sizeof(double) * S->S.nnz);
-        for (int lj = 0; lj < nr; lj++) {
-            int gj = S->red_idx[lj];
-            for (int q = S->J.colptr[gj]; q < S->J.colptr[gj + 1]; q++) {
-                int li = S->g2r[S->J.rowind[q]];
-                if (li >= 0) S->S.val[csc_find(&S->S, li, lj)] = S->J.val[q];
-            }
-        }
-        for (int i = 0; i < nr; i++) W->rhs[i] = W->f[S->red_idx[i]];
-        /* per non-trivial cluster */
-        for (int ci = 0; ci < S->nt; ci++) {
-            int c = S->nt_cl[ci];
-            int ws = P->cl_w_start[c], wk = P->cl_w_size[c], bus = P->cl_bus[c];
-            int vr_g = S->net + 2 * bus, vr_l = S->g2r[vr_g], vi_l = S->g2r[vr_g + 1];
-            double *A = W->Ak, *B = W->Bk, *C = W->Ck;
-            memset(A, 0, sizeof(double) * wk * wk);
-            memset(B, 0, sizeof(double) * wk * 2);
-            memset(C, 0, sizeof(double) * wk * 2);
-            for (int j = 0; j < wk; j++)
-                for (int q = S->J.colptr[ws + j]; q < S->J.colptr[ws + j + 1]; q++) {
-                    int r = S->J.rowind[q];
-                    if (r >= ws && r < ws + wk) A[(r - ws) + j * wk] = S->J.val[q];
-                    else if (r == vr_g) C[0 + 2 * j] = S->J.val[q];
-                    else if (r == vr_g + 1) C[1 + 2 * j] = S->J.val[q];
-                }
-            for (int b2 = 0; b2 < 2; b2++)
-                for (int q = S->J.colptr[vr_g + b2]; q < S->J.colptr[vr_g + b2 + 1]; q++) {
-                    int r = S->J.rowind[q];
-                    if (r >= ws && r < ws + wk) B[(r - ws) + b2 * wk] = S->J.val[q];
-                }
-            dense_lu(A, W->ipiv, wk);
-            double D[4];
-            for (int b2 = 0; b2 < 2; b2++) {
-                for (int i = 0; i < wk; i++) W->tmp[i] = B[i + b2 * wk];
-                dense_solve(A, W->ipiv, W->tmp, wk);
-                double d1 = 0, d2 = 0;
-                for (int i = 0; i < wk; i++) { d1 += C[0 + 2 * i] * W->tmp[i]; d2 += C[1 + 2 * i] * W->tmp[i]; }
-                D[0 + 2 * b2] = d1;
-                D[1 + 2 * b2] = d2;
-            }
-            S->S.val[csc_find(&S->S, vr_l, vr_l)] -= D[0];
-            S->S.val[csc_find(&S->S, vi_l, vr_l)] -= D[1];
-            S->S.val[csc_find(&S->S, vr_l, vi_l)] -= D[2];
-            S->S.val[csc_find(&S->S, vi_l, vi_l)] -= D[3];
-            for (int i = 0; i < wk; i++) W->tmp[i] = W->f[ws + i];
-            dense_solve(A, W->ipiv, W->tmp, wk);
-            for (int i = 0; i < wk; i++) {
-                W->rhs[vr_l] -= C[0 + 2 * i] * W->tmp[i];
-                W->rhs[vi_l] -= C[1 + 2 * i] * W->tmp[i];
-            }
-        }
-        for (int i = 0; i < nr; i++) W->rhs[i] = -W->rhs[i];
         if (factor_or_refactor(W, &S->S, it == 0) != 0) break;
         splu_solve(&W->LU, W->rhs, W->work);
-        for (int i = 0; i < nr; i++) W->dz[S->red_idx[i]] = W->rhs[i];
-        /* back-substitution: recompute each cluster's factor (values are kept
-         * only for the current cluster in this restatement) */
-        for (int ci = 0; ci < S->nt; ci++) {
-            int c = S->nt_cl[ci];
-            int ws = P->cl_w_start[c], wk = P->cl_w_size[c], bus = P->cl_bus[c];
-            int vr_g = S->net + 2 * bus;
-            double *A = W->Ak, *B = W->Bk;
-            memset(A, 0, sizeof(double) * wk * wk);
-            memset(B, 0, sizeof(double) * wk * 2);
-            for (int j = 0; j < wk; j++)
-                for (int q = S->J.colptr[ws + j]; q < S->J.colptr[ws + j + 1]; q++) {
-                    int r = S->J.rowind[q];
-                    if (r >= ws && r < ws + wk) A[(r - ws) + j * wk] = S->J.val[q];
-                }
-            for (int b2 = 0; b2 < 2; b2++)
-                for (int q = S->J.colptr[vr_g + b2]; q < S->J.colptr[vr_g + b2 + 1]; q++) {
-                    int r = S->J.rowind[q];
-                    if (r >= ws && r < ws + wk) B[(r - ws) + b2 * wk] = S->J.val[q];
-                }
-            dense_lu(A, W->ipiv, wk);
-            double dv1 = W->dz[vr_g], dv2 = W->dz[vr_g + 1];
-            for (int i = 0; i < wk; i++) W->tmp[i] = W->f[ws + i] + B[i] * dv1 + B[i + wk] * dv2;
-            dense_solve(A, W->ipiv, W->tmp, wk);
-            for (int i = 0; i < wk; i++) W->dz[ws + i] = -W->tmp[i];
-        }
-        for (int i = 0; i < n; i++) W->zb[i] += W->dz[i];
+        schur_backsub(W);
+    }
+    memcpy(z, W->zb, sizeof(double) * n);
+    return it;
+}
+
+/* Shared-factor Newton step (_newton_step_shared_multi_gpu!,
+ * ext/GradPowerCUDAExt/GradPowerCUDAExt.jl:2523-2627): the cluster blocks,
+ * the residual and the reduced right-hand side at the current iterate, the
+ * reduced solve with the frozen matrix P of scenario 0 at the initial
+ * state, or with P plus the scenario's fault shunt while the fault is on
+ * (the matrix the reference's Woodbury correction inverts, factored here
+ * directly: Pf). */
+static int newton_frozen(newton_ws *W, double *z, const double *zold, const double *u0, const double *p,
+                         const faults_t *F, double dt, double tol, int itermax, int *ok, splu_t *LP, splu_t *LPf) {
+    sym_t *S = W->S;
+    int n = S->nsys;
+    int fault_on = 0;
+    for (int e = 0; e < F->n; e++) fault_on |= F->on[e];
+    memcpy(W->zb, z, sizeof(double) * n);
+    *ok = 0;
+    int it;
+    for (it = 0; it < itermax; it++) {
+        double nf = schur_reduce(W, zold, u0, p, F, dt);
+        if (nf < tol) { *ok = 1; break; }
+        if (!isfinite(nf)) break;
+        splu_solve(fault_on ? LPf : LP, W->rhs, W->work);
+        schur_backsub(W);
     }
     memcpy(z, W->zb, sizeof(double) * n);
     return it;
@@ -1340,6 +1388,7 @@ static void ws_free(newton_ws *W) {
 
 static int integrate_one(const gp_problem *P, const double *z0, const double *u0, const double *p, int nf,
                          const gp_fault *faults, double dt, int nsteps, double tol, int itermax, int solver,
+                         const double *z0_s0, const double *u0_s0, const double *p_s0,
                          double *traj, double *zfinal, int *iters, long long *stats) {
     int n = n_sys_of(P);
     sym_t S;
@@ -1358,11 +1407,36 @@ static int integrate_one(const gp_problem *P, const double *z0, const double *u0
         assemble_J(&S, z, u0, p, &F, dt, &W.t);
         if (factor_or_refactor(&W, &S.J, 1) != 0) status = 2;
     }
+    /* shared-factor path: P = S of scenario 0 at its initial state, no
+     * fault, this call's dt (_factor_shared_P_gpu!, ext/...:2149-2172); Pf =
+     * P with the scenario's fault shunt on its bus diagonal */
+    splu_t LP, LPf;
+    int have_p = 0;
+    if (solver == 3) {
+        uint8_t none = 0;
+        faults_t F0 = {0, faults, &none};
+        memcpy(W.zb, z0_s0, sizeof(double) * n);
+        schur_reduce(&W, z0_s0, u0_s0, p_s0, &F0, dt);
+        int *q = min_degree_order(S.S.n, S.S.colptr, S.S.rowind);
+        int *q2 = (int *)malloc(sizeof(int) * (S.S.n > 0 ? S.S.n : 1));
+        memcpy(q2, q, sizeof(int) * S.S.n);
+        splu_init(&LP, S.S.n, q);
+        splu_init(&LPf, S.S.n, q2);
+        have_p = 1;
+        if (splu_factor(&LP, &S.S, 1e-3) != 0) status = 2;
+        if (nf > 0) {
+            const int vr_l = S.g2r[S.net + 2 * faults[0].bus], vi_l = S.g2r[S.net + 2 * faults[0].bus + 1];
+            S.S.val[csc_find(&S.S, vr_l, vr_l)] -= 1.0 / faults[0].rfault;
+            S.S.val[csc_find(&S.S, vi_l, vi_l)] -= 1.0 / faults[0].rfault;
+        }
+        if (splu_factor(&LPf, &S.S, 1e-3) != 0) status = 2;
+    }
     for (int k = 1; k <= nsteps && status != 2; k++) {
         int ok;
         memcpy(zold, z, sizeof(double) * n);
-        int it = solver != 1 ? newton_mono(&W, z, zold, u0, p, &F, dt, tol, itermax, &ok, solver == 0)
-                             : newton_schur(&W, z, zold, u0, p, &F, dt, tol, itermax, &ok);
+        int it = solver == 3   ? newton_frozen(&W, z, zold, u0, p, &F, dt, tol, itermax, &ok, &LP, &LPf)
+                 : solver != 1 ? newton_mono(&W, z, zold, u0, p, &F, dt, tol, itermax, &ok, solver == 0)
+                               : newton_schur(&W, z, zold, u0, p, &F, dt, tol, itermax, &ok);
         if (!ok) status = isfinite(inf_norm(z, n)) ? 1 : 2;
         if (iters) { iters[2 * (k - 1)] = it; iters[2 * (k - 1) + 1] = 0; }
         if (traj) memcpy(traj + (size_t)k * n, z, sizeof(double) * n);
@@ -1373,8 +1447,9 @@ static int integrate_one(const gp_problem *P, const double *z0, const double *u0
         }
         if (any) {
             memcpy(zold, z, sizeof(double) * n);
-            it = solver != 1 ? newton_mono(&W, z, zold, u0, p, &F, 0.0, tol, itermax, &ok, solver == 0)
-                             : newton_schur(&W, z, zold, u0, p, &F, 0.0, tol, itermax, &ok);
+            it = solver == 3   ? newton_frozen(&W, z, zold, u0, p, &F, 0.0, tol, itermax, &ok, &LP, &LPf)
+                 : solver != 1 ? newton_mono(&W, z, zold, u0, p, &F, 0.0, tol, itermax, &ok, solver == 0)
+                               : newton_schur(&W, z, zold, u0, p, &F, 0.0, tol, itermax, &ok);
             if (!ok) status = isfinite(inf_norm(z, n)) ? 1 : 2;
             if (iters) iters[2 * (k - 1) + 1] = it;
         }
@@ -1387,6 +1462,10 @@ static int integrate_one(const gp_problem *P, const double *z0, const double *u0
         stats[3] = S.J.nnz;
         stats[4] = S.S.nnz;
         stats[5] = S.n_red;
+    }
+    if (have_p) {
+        splu_free(&LP);
+        splu_free(&LPf);
     }
     free(on);
     free(z);
@@ -1404,7 +1483,10 @@ static int integrate_one(const gp_problem *P, const double *z0, const double *u0
  * scenario == -1 apply to every scenario.  solver: 0 monolithic sparse LU
  * with the batched path's factorisation schedule (integrate_batched!),
  * 1 Schur path (newton_step_schur!), 2 monolithic with integrate!'s
- * schedule (one pivoting factorisation at z0, refactorisations after).  traj [M][nsteps+1][n_sys] or NULL; zfinal [M][n_sys]
+ * schedule (one pivoting factorisation at z0, refactorisations after),
+ * 3 shared-factor path (integrate_gpu_shared_multi!: the reduced matrix of
+ * scenario 0 at its initial state, factored once, with each scenario's
+ * fault shunt; every scenario has at most one fault bus and rfault).  traj [M][nsteps+1][n_sys] or NULL; zfinal [M][n_sys]
  * or NULL; iters [M][2*nsteps] or NULL; status [M]; stats [M][6] or NULL. */
 int gpo_integrate(const gp_problem *P, int M, const double *z0, const double *u0, const double *p, int nf,
                   const gp_fault *faults, double dt, int nsteps, double tol, int itermax, int solver,
@@ -1423,7 +1505,7 @@ int gpo_integrate(const gp_problem *P, int M, const double *z0, const double *u0
         for (int e = 0; e < nf; e++)
             if (faults[e].scenario < 0 || faults[e].scenario == m) fm[cnt++] = faults[e];
         status[m] = integrate_one(P, z0 + (size_t)m * n, u0 + (size_t)m * P->n_ctrl, p + (size_t)m * P->n_par, cnt,
-                                  fm, dt, nsteps, tol, itermax, solver,
+                                  fm, dt, nsteps, tol, itermax, solver, z0, u0, p,
                                   traj ? traj + (size_t)m * (nsteps + 1) * n : NULL,
                                   zfinal ? zfinal + (size_t)m * n : NULL,
                                   iters ? iters + (size_t)m * 2 * nsteps : NULL,

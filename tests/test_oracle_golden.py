@@ -6,7 +6,7 @@ only and gate every GPU parity test (which compares against this oracle).
 import numpy as np
 import pytest
 
-from helpers import DT, Case, M, case9_system, psse_case, run_oracle
+from helpers import DT, Case, M, case9_system, psse_case, run_oracle, synthetic_case
 
 
 def test_case9_powerflow_vs_matpower(golden_known):
@@ -182,3 +182,16 @@ def test_monolithic_equals_schur(orc):
     b = run_oracle(orc, c, 40, solver=1)
     assert np.array_equal(a["iters"], b["iters"])
     assert np.max(np.abs(a["traj"] - b["traj"])) < 1e-9
+
+
+def test_oracle_shared_factor_path(orc):
+    """The oracle's shared-factor iteration (solver 3: the reduced matrix of
+    scenario 0 at the initial state, frozen, plus each scenario's fault
+    shunt) reaches the exact Schur Newton trajectory on the 2,000-bus grid
+    within 1e-8, in more iterations."""
+    c, w = synthetic_case("planar2k", 2)
+    o3 = run_oracle(orc, c, 30, solver=3, nthreads=2)
+    o1 = run_oracle(orc, c, 30, solver=1, nthreads=2)
+    assert np.all(o3["status"] == 0) and np.all(o1["status"] == 0)
+    assert o3["iters"].sum() > o1["iters"].sum()
+    assert np.max(np.abs(o3["traj"] - o1["traj"]) / np.maximum(1.0, np.abs(o1["traj"]))) <= 1e-8
