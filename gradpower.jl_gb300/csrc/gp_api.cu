@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -116,6 +117,14 @@ struct gp_layout {
     cudaGraphConditionalHandle h_loop = 0, h_var = 0;
     int *d_cnt = nullptr;
     bool profiling = false;      // host-driven loop with phase events (gp_set_profiling)
+    // line trips (gp_set_line_trips): expanded per scenario, with their
+    // off-diagonal assembly entries; statuses reset at every call
+    DeviceArena trip_arena;
+    int n_tr = 0;
+    uint8_t *d_tr_on = nullptr;
+    int *d_tr_on_step = nullptr, *d_tr_off_step = nullptr, *d_tr_scen = nullptr;
+    std::vector<int> h_tr_on_step, h_tr_off_step;
+    std::vector<int> h_adj_ptr, h_adj;   // bus adjacency (line trips are checked against it)
     // shared-factor Woodbury path (allocated on first use): W = P^-1 U per
     // scenario (two columns), H^-1 (2x2), the correction's coefficients, and
     // the mask that selects scenario 0 for the factorisation of P
@@ -1605,18 +1614,21 @@ int32_t gp_layout_create(const gp_problem *prob, int32_t M, const double *z0, co
     build_problem(L, prob);
     build_work(L, z0, u0, p);
     build_clusters(L, prob, z0, u0, p);
+    L->h_adj_ptr.assign(prob->adj_rowptr, prob->adj_rowptr + prob->n_bus + 1);
+    L->h_adj.assign(prob->adj_colidx, prob->adj_colidx + prob->adj_rowptr[prob->n_bus]);
+    if (gp_set_line_trips(L, 0, nullptr) != GP_OK) fail(GP_E_CUDA, "%s", g_last_error.c_str());
     ck(cudaDeviceSynchronize(), "layout create");
     *out = L;
     L = nullptr;
     }
     catch (const gp_error &e) {
         g_last_error = e.what();
-        if (L) { L->arena.release(); delete L; }
+        if (L) { L->trip_arena.release(); L->arena.release(); delete L; }
         return e.code;
     }
     catch (const std::exception &e) {
         g_last_error = e.what();
-        if (L) { L->arena.release(); delete L; }
+        if (L) { L->trip_arena.release(); L->arena.release(); delete L; }
         return GP_E_INVALID;
     }
     return GP_OK;
@@ -1628,6 +1640,7 @@ int32_t gp_layout_destroy(gp_layout *L) {
     drop_graphs(L);
     if (L->st) cudaStreamSynchronize(L->st);
     L->call.release();
+    L->trip_arena.release();
     L->arena.release();
     if (L->h_flag) cudaFreeHost(L->h_flag);
     if (L->h_dt) cudaFreeHost(L->h_dt);
@@ -1714,6 +1727,8 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
     if (opt->solver != GP_SOLVER_SCHUR_FP64 && opt->solver != GP_SOLVER_SCHUR_MIXED &&
         opt->solver != GP_SOLVER_SHARED_WOODBURY)
         fail(GP_E_INVALID, "solver %d is not available", opt->solver);
+    if (opt->solver == GP_SOLVER_SHARED_WOODBURY && L->n_tr > 0)
+        fail(GP_E_INVALID, "the shared-factor Woodbury solver does not take line trips");
     if (opt->solver == GP_SOLVER_SHARED_WOODBURY) {
         // one fault (bus, rfault) per scenario: its rank-2 correction of P
         std::vector<int> fb(L->M, -1);
@@ -1737,6 +1752,11 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
         ev_steps[L->h_fl_on_step[e]] = 1;
         ev_steps[L->h_fl_off_step[e]] = 1;
     }
+    for (int e = 0; e < L->n_tr; e++) {
+        ev_steps[L->h_tr_on_step[e]] = 1;
+        if (L->h_tr_off_step[e] >= 0) ev_steps[L->h_tr_off_step[e]] = 1;
+    }
+    if (L->n_tr > 0) ck(cudaMemsetAsync(L->d_tr_on, 0, L->n_tr, L->st), "memset");
     double *d_traj = nullptr;
     int *d_iters = L->call.alloc<int>((size_t)2 * std::max(ns, 1) * M);
     ck(cudaMemsetAsync(d_iters, 0, (size_t)2 * std::max(ns, 1) * M * sizeof(int), L->st), "memset");
@@ -1788,6 +1808,8 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
         if (ev_steps.count(k)) {
             ck(cudaMemsetAsync(L->W.active, 0, M, L->st), "memset");
             gp::launch_events(L->P, L->W, L->d_fl_on_step, L->d_fl_off_step, L->d_fl_scen, L->d_fl_on, L->n_fl, k,
+                              L->st);
+            gp::launch_events(L->P, L->W, L->d_tr_on_step, L->d_tr_off_step, L->d_tr_scen, L->d_tr_on, L->n_tr, k,
                               L->st);
             ck(cudaMemcpyAsync(L->W.zold, L->W.z, (size_t)M * nsys * sizeof(double), cudaMemcpyDeviceToDevice,
                                L->st),
@@ -1957,6 +1979,7 @@ int32_t gp_adjoint(gp_layout *L, const gp_options *opt, int32_t n_faults, const 
     if (opt->n_steps < 1 || !(opt->dt > 0.0) || opt->itermax <= 0 || checkpoint_every < 1)
         fail(GP_E_INVALID, "bad options");
     if (opt->solver != GP_SOLVER_SCHUR_FP64) fail(GP_E_INVALID, "the adjoint runs on the FP64 Schur path");
+    if (L->n_tr > 0) fail(GP_E_INVALID, "the adjoint does not take line trips");
     const int M = L->M, ns = opt->n_steps, K = checkpoint_every;
     const size_t nsys = L->n_sys, blk = (size_t)M * nsys;
     set_faults(L, n_faults, faults);
@@ -2095,6 +2118,114 @@ int32_t gp_set_mixed_policy(gp_layout *L, int32_t max_age, double rho_max, int32
     L->Mx.rho_max = rho_max;
     L->Mx.exact_after = exact_after;
     drop_graphs(L);   // the graphs hold the policy by value
+    API_END
+}
+
+// Front position (supernode s, column-major offset) of the reduced entry
+// (r, c), both in the original reduced numbering.
+std::pair<int, int> front_entry(const gp::Symbolic &sym, int r, int c) {
+    const int pi = sym.iperm[r], pj = sym.iperm[c];
+    const int s = sym.sup_of[std::min(pi, pj)];
+    auto pos = [&](int k) -> int {
+        const int st0 = sym.sup_start[s], en = sym.sup_start[s + 1];
+        if (k >= st0 && k < en) return k - st0;
+        auto b = sym.rows.begin() + sym.row_ptr[s], e = sym.rows.begin() + sym.row_ptr[s + 1];
+        auto it = std::lower_bound(b, e, k);
+        if (it == e || *it != k) fail(GP_E_INVALID, "entry outside the symbolic structure");
+        return (en - st0) + (int)(it - b);
+    };
+    return {s, pos(pi) + pos(pj) * sym.front_m(s)};
+}
+
+int32_t gp_set_line_trips(gp_layout *L, int32_t n, const gp_line_trip *trips) {
+    API_BEGIN
+    if (!L || (n > 0 && !trips) || n < 0) fail(GP_E_INVALID, "bad arguments");
+    if (n == 0 && L->n_tr == 0 && L->P.tr_ptr) return GP_OK;
+    const int M = L->M;
+    std::vector<std::vector<int>> per(M);
+    for (int e = 0; e < n; e++) {
+        const gp_line_trip &t = trips[e];
+        if (t.from_bus < 0 || t.from_bus >= L->n_bus || t.to_bus < 0 || t.to_bus >= L->n_bus ||
+            t.from_bus == t.to_bus)
+            fail(GP_E_INVALID, "line trip %d: buses %d-%d", e, t.from_bus, t.to_bus);
+        if (t.scenario >= M) fail(GP_E_INVALID, "line trip %d: scenario %d out of range", e, t.scenario);
+        bool adjacent = false;
+        for (int q = L->h_adj_ptr[t.from_bus]; q < L->h_adj_ptr[t.from_bus + 1]; q++)
+            adjacent = adjacent || L->h_adj[q] == t.to_bus;
+        if (!adjacent) fail(GP_E_INVALID, "line trip %d: no branch between buses %d and %d", e, t.from_bus, t.to_bus);
+        if (t.scenario < 0)
+            for (int m = 0; m < M; m++) per[m].push_back(e);
+        else
+            per[t.scenario].push_back(e);
+    }
+    std::vector<int> ptr(M + 1, 0), fb, tb, on, off, scen;
+    std::vector<double> y;
+    for (int m = 0; m < M; m++) {
+        for (int e : per[m]) {
+            const gp_line_trip &t = trips[e];
+            fb.push_back(t.from_bus);
+            tb.push_back(t.to_bus);
+            for (const double *v : {t.yff, t.yft, t.ytf, t.ytt}) {
+                y.push_back(v[0]);
+                y.push_back(v[1]);
+            }
+            on.push_back(t.on_step);
+            off.push_back(t.off_step);
+            scen.push_back(m);
+        }
+        ptr[m + 1] = (int)fb.size();
+    }
+    // assembly entries of the off-diagonal blocks: + realified y_ft at
+    // (from, to), + realified y_tf at (to, from)
+    const gp::Symbolic &sym = L->sym;
+    std::vector<std::vector<std::array<double, 3>>> per_s(sym.nsup);   // (position, entry, value)
+    for (int e = 0; e < (int)fb.size(); e++)
+        for (int side = 0; side < 2; side++) {
+            const int rb = side == 0 ? fb[e] : tb[e], cb = side == 0 ? tb[e] : fb[e];
+            const double g = y[8 * e + (side == 0 ? 2 : 4)], b = y[8 * e + (side == 0 ? 3 : 5)];
+            const double blk[4] = {g, -b, b, g};   // (vr,vr) (vr,vi) (vi,vr) (vi,vi)
+            for (int q = 0; q < 4; q++) {
+                const auto fe = front_entry(sym, 2 * rb + q / 2, 2 * cb + q % 2);
+                per_s[fe.first].push_back({(double)fe.second, (double)e, blk[q]});
+            }
+        }
+    std::vector<int> ap(sym.nsup + 1, 0), apos, atr;
+    std::vector<double> aval;
+    for (int s = 0; s < sym.nsup; s++) {
+        for (const auto &t : per_s[s]) {
+            apos.push_back((int)t[0]);
+            atr.push_back((int)t[1]);
+            aval.push_back(t[2]);
+        }
+        ap[s + 1] = (int)apos.size();
+    }
+    L->trip_arena.release();
+    DeviceArena &A = L->trip_arena;
+    auto up_i = [&](const std::vector<int> &v) { return A.upload(v.empty() ? std::vector<int>{0} : v); };
+    L->n_tr = (int)fb.size();
+    L->P.n_tr = L->n_tr;
+    L->P.tr_ptr = up_i(ptr);
+    L->P.tr_from = up_i(fb);
+    L->P.tr_to = up_i(tb);
+    L->P.tr_y = A.upload(y.empty() ? std::vector<double>{0.0} : y);
+    L->d_tr_on = A.alloc<uint8_t>(std::max(1, L->n_tr));
+    ck(cudaMemset(L->d_tr_on, 0, std::max(1, L->n_tr)), "memset");
+    L->P.tr_on = L->d_tr_on;
+    L->d_tr_on_step = up_i(on);
+    L->d_tr_off_step = up_i(off);
+    L->d_tr_scen = up_i(scen);
+    L->h_tr_on_step = on;
+    L->h_tr_off_step = off;
+    if (L->n_tr > 0) {
+        L->S.asmt_ptr = up_i(ap);
+        L->S.asmt_pos = up_i(apos);
+        L->S.asmt_tr = up_i(atr);
+        L->S.asmt_val = A.upload(aval.empty() ? std::vector<double>{0.0} : aval);
+    } else {
+        L->S.asmt_ptr = L->S.asmt_pos = L->S.asmt_tr = nullptr;
+        L->S.asmt_val = nullptr;
+    }
+    drop_graphs(L);   // the graphs hold the problem and structure by value
     API_END
 }
 

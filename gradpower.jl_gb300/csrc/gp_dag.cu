@@ -154,6 +154,11 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
     g.sync();
     const double *sv = W.svar + (size_t)m * P.n_var;
     for (int e = S.asmv_ptr[s] + idx; e < S.asmv_ptr[s + 1]; e += step) F[S.asmv_pos[e]] += (T)sv[S.asmv_idx[e]];
+    if (S.asmt_ptr)
+        for (int e = S.asmt_ptr[s] + idx; e < S.asmt_ptr[s + 1]; e += step) {
+            const int t = S.asmt_tr[e];
+            if (P.tr_on[t] && t >= P.tr_ptr[m] && t < P.tr_ptr[m + 1]) F[S.asmt_pos[e]] += (T)S.asmt_val[e];
+        }
     g.sync();
     for (int q = S.child_ptr[s]; q < S.child_ptr[s + 1]; q++) {
         const int c = S.children[q];

@@ -38,6 +38,12 @@ struct DevProblem {
     const int *fl_bus;
     const double *fl_yf;   // 1/rfault
     const uint8_t *fl_on;  // current status
+    // line trips expanded per scenario (gp_set_line_trips)
+    int n_tr;
+    const int *tr_ptr;     // [M+1]
+    const int *tr_from, *tr_to;
+    const double *tr_y;    // [n_tr][8]: yff, yft, ytf, ytt (re, im)
+    const uint8_t *tr_on;  // current status (tripped)
     // symbolic permutation of the reduced system
     const int *iperm;      // reduced index -> permuted position
 };
@@ -68,6 +74,11 @@ struct DevSym {
     const int *asmc_ptr, *asmc_pos;   // constant entries: front position, value
     const double *asmc_val;
     const int *asmv_ptr, *asmv_pos, *asmv_idx;   // variable entries: front position, svar index
+    // line-trip entries of the off-diagonal bus blocks: front position,
+    // trip entry (its scenario and status in DevProblem), value added while
+    // the line is tripped; null without trips
+    const int *asmt_ptr, *asmt_pos, *asmt_tr;
+    const double *asmt_val;
     double *fronts;                   // [M][front_total]
     double *uvec;                     // [M][uvec_total]
     int *ipiv;                        // [M][n] pivot row within the supernode, per column

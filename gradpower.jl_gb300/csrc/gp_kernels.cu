@@ -540,6 +540,21 @@ __global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, D
                 nb = t > nb ? t : nb;
             }
         }
+        // tripped lines: their Ybus terms removed (f = -Y V gains
+        // +y_line V; the S diagonal block gains the realified y_line)
+        for (int e = P.tr_ptr[m]; e < P.tr_ptr[m + 1]; e++) {
+            if (!P.tr_on[e]) continue;
+            const int fb = P.tr_from[e], tb = P.tr_to[e];
+            if (fb != b && tb != b) continue;
+            const double *y = P.tr_y + 8 * (size_t)e + (fb == b ? 0 : 4);   // (yff, yft) or (ytf, ytt)
+            const double ybr = fb == b ? y[0] : y[2], ybi = fb == b ? y[1] : y[3];
+            const double yor = fb == b ? y[2] : y[0], yoi = fb == b ? y[3] : y[1];
+            const int o = fb == b ? tb : fb;
+            const double vro = z[net + 2 * o], vio = z[net + 2 * o + 1];
+            fr += ybr * vr - ybi * vi + yor * vro - yoi * vio;
+            fi += ybi * vr + ybr * vi + yoi * vro + yor * vio;
+            if (need_s) { d00 += ybr; d01 -= ybi; d10 += ybi; d11 += ybr; }
+        }
         for (int e = P.fl_ptr[m]; e < P.fl_ptr[m + 1]; e++) {
             if (P.fl_on[e] && P.fl_bus[e] == b) {
                 const double yf = P.fl_yf[e];

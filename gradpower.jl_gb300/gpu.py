@@ -55,11 +55,13 @@ def library():
         L.gp_residual_static.argtypes = [vp, vp, C.c_double, vp]
         L.gp_set_mixed_policy.argtypes = [vp, C.c_int32, C.c_double, C.c_int32, C.c_int32]
         L.gp_set_profiling.argtypes = [vp, C.c_int32]
+        L.gp_set_line_trips.argtypes = [vp, C.c_int32, vp]
         L.gp_adjoint.argtypes = [vp, vp, C.c_int32, vp, vp, C.c_int32, vp, vp, vp, vp]
         for f in ("gp_layout_create", "gp_layout_destroy", "gp_layout_stats", "gp_set_state",
                   "gp_get_state", "gp_integrate", "gp_residual", "gp_last_timing",
                   "gp_restore_initial_state", "gp_reduced_selftest", "gp_cluster_selftest",
-                  "gp_residual_static", "gp_set_mixed_policy", "gp_set_profiling", "gp_adjoint"):
+                  "gp_residual_static", "gp_set_mixed_policy", "gp_set_profiling", "gp_set_line_trips",
+                  "gp_adjoint"):
             getattr(L, f).restype = C.c_int32
         _lib = L
     return _lib
@@ -98,6 +100,7 @@ class GpuBatchedLayout:
         P = self.arrays.as_ctypes()
         _check(library().gp_layout_create(C.addressof(P), self.M, _p(z), _p(u), _p(pp), C.byref(h)))
         self._h = h
+        self._trips_set = False
 
     def close(self):
         if getattr(self, "_h", None):
@@ -167,13 +170,20 @@ class GpuBatchedLayout:
                   itermax: int = 30, events: Sequence[Mdl.ContingencyEvent] = (),
                   scenario_faults: Optional[Sequence[Sequence[Mdl.ContingencyEvent]]] = None,
                   want_traj: bool = True, solver: int = LY.SOLVER_SCHUR_FP64,
-                  traj_out: Optional[np.ndarray] = None):
+                  traj_out: Optional[np.ndarray] = None, trip_events: Sequence[Mdl.TripLineEvent] = (),
+                  scenario_trips: Optional[Sequence[Sequence[Mdl.TripLineEvent]]] = None):
         """Integrate every scenario from the current state.  `traj_out`, if
         given, is a C-contiguous float64 array [M, n_steps+1, n_sys] (for
-        example a pinned buffer) that receives the trajectories."""
+        example a pinned buffer) that receives the trajectories.
+        `trip_events` (every scenario, the reference's ps.dynamic.trip_events)
+        and `scenario_trips` (per scenario) trip lines (gp_set_line_trips)."""
         nsteps = LY.jl_round(tf / dt)
         per = scenario_faults if scenario_faults is not None else [[] for _ in range(self.M)]
         fa, nf = LY.fault_array(per, dt, events)
+        if trip_events or scenario_trips or self._trips_set:
+            ta, nt = LY.trip_array(scenario_trips, dt, trip_events)
+            _check(library().gp_set_line_trips(self._h, nt, C.addressof(ta)))
+            self._trips_set = nt > 0
         opt = LY.GpOptions(dt, nsteps, newton_tol, itermax, solver)
         if traj_out is not None:
             if (traj_out.shape != (self.M, nsteps + 1, self.n_sys) or traj_out.dtype != np.float64

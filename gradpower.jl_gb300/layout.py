@@ -10,6 +10,7 @@ call that receives the struct.
 from __future__ import annotations
 
 import ctypes as C
+import math
 from dataclasses import dataclass
 from typing import Dict, List, Sequence
 
@@ -56,6 +57,31 @@ class GpProblem(C.Structure):
 class GpFault(C.Structure):
     _fields_ = [("scenario", C.c_int32), ("bus", C.c_int32), ("rfault", C.c_double),
                 ("on_step", C.c_int32), ("off_step", C.c_int32)]
+
+
+class GpLineTrip(C.Structure):
+    _fields_ = [("scenario", C.c_int32), ("from_bus", C.c_int32), ("to_bus", C.c_int32),
+                ("yff", C.c_double * 2), ("yft", C.c_double * 2), ("ytf", C.c_double * 2),
+                ("ytt", C.c_double * 2), ("on_step", C.c_int32), ("off_step", C.c_int32)]
+
+
+def trip_array(trips_per_scenario, dt: float, global_trips=()):
+    """The gp_line_trip array: one entry per (scenario, trip), plus
+    scenario = -1 entries for trips of every scenario; steps as the
+    reference schedules them (Int(round(t/dt)); no reclose: -1)."""
+    rows = [(-1, t) for t in global_trips]
+    for m, ts in enumerate(trips_per_scenario or ()):
+        rows.extend((m, t) for t in ts)
+    arr = (GpLineTrip * max(1, len(rows)))()
+    for k, (m, t) in enumerate(rows):
+        a = arr[k]
+        a.scenario, a.from_bus, a.to_bus = m, t.from_bus, t.to_bus
+        for name in ("yff", "yft", "ytf", "ytt"):
+            v = complex(getattr(t, name))
+            getattr(a, name)[0], getattr(a, name)[1] = v.real, v.imag
+        a.on_step = jl_round(t.ton / dt)
+        a.off_step = jl_round(t.toff / dt) if math.isfinite(t.toff) else -1
+    return arr, len(rows)
 
 
 class GpObjective(C.Structure):

@@ -97,6 +97,49 @@ class ContingencyEvent:
     status: bool = False
 
 
+@dataclass
+class TripLineEvent:
+    """Line trip (src/GradPower.jl:148-167): the line's admittance terms
+    leave Ybus at ton and come back at toff (inf: permanent).  Buses are
+    internal 0-based indices; the y terms are complex."""
+    from_bus: int
+    to_bus: int
+    ton: float
+    toff: float
+    yff: complex
+    yft: complex
+    ytf: complex
+    ytt: complex
+
+
+def create_trip_line_event(ps: "PowerSystem", from_bus_ext: int, to_bus_ext: int, ton: float,
+                           toff: float = math.inf) -> TripLineEvent:
+    """The branch between two buses given by their external (PSS/E) numbers
+    and its admittance terms, as Ybus holds them (create_trip_line_event,
+    src/GradPower.jl:500-543)."""
+    fr_i = ps.busmap[from_bus_ext] if ps.busmap else from_bus_ext
+    to_i = ps.busmap[to_bus_ext] if ps.busmap else to_bus_ext
+    for br in ps.branches:
+        if (br.fr, br.to) in ((fr_i, to_i), (to_i, fr_i)):
+            return trip_branch_event(br, ton, toff)
+    raise ValueError("no branch between buses %d and %d" % (from_bus_ext, to_bus_ext))
+
+
+def trip_branch_event(br: "Branch", ton: float, toff: float = math.inf) -> TripLineEvent:
+    """TripLineEvent of one branch (its Ybus terms, as build_network adds
+    them)."""
+    tap, shift = br.tap, br.shift
+    if tap > 0.0:
+        tpsh = tap * np.exp(1j * math.pi / 180.0 * shift)
+    else:
+        tpsh = 1.0 + 0.0j
+        tap = 1.0
+    y = 1.0 / complex(br.r, br.x)
+    return TripLineEvent(br.fr, br.to, ton, toff,
+                         y / (tap * tap) + 1j * 0.5 * br.sh, -y / np.conj(tpsh), -y / tpsh,
+                         y + (1j * 0.5 * br.sh) / (tap * tap))
+
+
 # ---------------------------------------------------------------------------
 # Device models.  Sizes follow the reference constructors; parameter
 # vectors follow each type's `fill_pvec!`.

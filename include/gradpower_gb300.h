@@ -133,6 +133,23 @@ typedef struct gp_fault {
     int32_t off_step;
 } gp_fault;
 
+/* A line trip (TripLineEvent, src/GradPower.jl:148-167; its admittance
+ * terms as create_trip_line_event computes them, :500-543): at the end of
+ * step on_step the line's admittance contributions are removed from Ybus
+ * (_apply_trip_line!, :551-564), and at the end of step off_step they are
+ * added back (_apply_reclose_line!, :566-574; off_step < 0: never), each
+ * followed by the dt = 0 re-solve (src/dynamics.jl:612-646).  Buses are
+ * 0-based internal indices.  Every gp_integrate call starts with all lines
+ * in service (the reference leaves a permanent trip in ps.network.ybus_real
+ * after integrate!). */
+typedef struct gp_line_trip {
+    int32_t scenario;            /* -1: every scenario */
+    int32_t from_bus, to_bus;
+    double yff[2], yft[2], ytf[2], ytt[2];   /* (real, imag) */
+    int32_t on_step;
+    int32_t off_step;
+} gp_line_trip;
+
 /* GP_SOLVER_SCHUR_FP64: exact Newton, the reference's batched schedule: the
  *   cluster blocks and the reduced network matrix are factored in FP64 at
  *   every iteration.
@@ -195,6 +212,13 @@ int32_t gp_get_state(const gp_layout *L, double *z);
 /* Reset the state to the z0 given to gp_layout_create (device-side copy;
  * reruns a batch without host traffic). */
 int32_t gp_restore_initial_state(gp_layout *L);
+
+/* Line trips for the following gp_integrate calls (replaces the previous
+ * set; n = 0 clears them).  GP_SOLVER_SCHUR_FP64 and GP_SOLVER_SCHUR_MIXED
+ * only: GP_SOLVER_SHARED_WOODBURY and gp_adjoint return GP_E_INVALID while
+ * trips are set.  The batched GPU path of the reference has no line trips:
+ * this carries integrate!'s to it (per scenario). */
+int32_t gp_set_line_trips(gp_layout *L, int32_t n, const gp_line_trip *trips);
 
 /* Integrate every scenario for opt->n_steps backward-Euler steps from the
  * current state.  Replaces integrate_gpu_schur_cudss! / integrate_gpu_cudss!.

@@ -97,12 +97,24 @@ static double genrou_sat_se(double psi, double sa, double sb) {
     return sb * (psi - sa) * (psi - sa) / psi;
 }
 
-/* fault flags: which faults of this scenario are active */
+/* fault flags: which faults of this scenario are active; line trips and
+ * which of them are tripped */
 typedef struct {
     int n;
     const gp_fault *f;
     const uint8_t *on;
+    int ntr;
+    const gp_line_trip *tr;
+    const uint8_t *tr_on;
 } faults_t;
+
+/* The tripped line's admittance terms of bus b: diagonal yb, to the other
+ * end yo; 0 when the trip does not touch b. */
+static int trip_terms(const gp_line_trip *t, int b, const double **yb, const double **yo, int *other) {
+    if (t->from_bus == b) { *yb = t->yff; *yo = t->yft; *other = t->to_bus; return 1; }
+    if (t->to_bus == b) { *yb = t->ytt; *yo = t->ytf; *other = t->from_bus; return 1; }
+    return 0;
+}
 
 /* ------------------------------------------------------------------ */
 /* residual (src/dynamics.jl:265-327 and the kernel leaves)            */
@@ -303,6 +315,23 @@ static void residual_rhs(const gp_problem *P, const double *z, const double *u0,
         double yf = 1.0 / F->f[e].rfault;
         f[vr_idx] -= yf * z[vr_idx];
         f[vr_idx + 1] -= yf * z[vr_idx + 1];
+    }
+    /* tripped lines: their Ybus terms removed, f = -Y V gains +y_line V
+     * (_apply_trip_line!, src/GradPower.jl:551-564) */
+    for (int e = 0; e < F->ntr; e++) {
+        if (!F->tr_on[e]) continue;
+        const gp_line_trip *t = &F->tr[e];
+        const int ends[2] = {t->from_bus, t->to_bus};
+        for (int q = 0; q < 2; q++) {
+            const double *yb, *yo;
+            int o;
+            if (q == 1 && t->to_bus == t->from_bus) break;
+            trip_terms(t, ends[q], &yb, &yo, &o);
+            int r = net + 2 * ends[q], c = net + 2 * o;
+            double vr = z[r], vi = z[r + 1], vro = z[c], vio = z[c + 1];
+            f[r] += yb[0] * vr - yb[1] * vi + yo[0] * vro - yo[1] * vio;
+            f[r + 1] += yb[1] * vr + yb[0] * vi + yo[1] * vro + yo[0] * vio;
+        }
     }
 }
 
@@ -613,6 +642,28 @@ static void jacobian_rhs(const gp_problem *P, const double *z, const double *u0,
         double yf = 1.0 / F->f[e].rfault;
         trip_push(t, r, r, -yf);
         trip_push(t, r + 1, r + 1, -yf);
+    }
+    /* tripped lines: + the realified line terms (the inverse of the
+     * network's -Ybus blocks) */
+    for (int e = 0; e < F->ntr; e++) {
+        if (!F->tr_on[e]) continue;
+        const gp_line_trip *tr = &F->tr[e];
+        const int ends[2] = {tr->from_bus, tr->to_bus};
+        for (int q = 0; q < 2; q++) {
+            const double *yb, *yo;
+            int o;
+            if (q == 1 && tr->to_bus == tr->from_bus) break;
+            trip_terms(tr, ends[q], &yb, &yo, &o);
+            int r = net + 2 * ends[q], c = net + 2 * o;
+            trip_push(t, r, r, yb[0]);
+            trip_push(t, r + 1, r + 1, yb[0]);
+            trip_push(t, r, r + 1, -yb[1]);
+            trip_push(t, r + 1, r, yb[1]);
+            trip_push(t, r, c, yo[0]);
+            trip_push(t, r + 1, c + 1, yo[0]);
+            trip_push(t, r, c + 1, -yo[1]);
+            trip_push(t, r + 1, c, yo[1]);
+        }
     }
 }
 
@@ -1387,9 +1438,9 @@ static void ws_free(newton_ws *W) {
 /* ------------------------------------------------------------------ */
 
 static int integrate_one(const gp_problem *P, const double *z0, const double *u0, const double *p, int nf,
-                         const gp_fault *faults, double dt, int nsteps, double tol, int itermax, int solver,
-                         const double *z0_s0, const double *u0_s0, const double *p_s0,
-                         double *traj, double *zfinal, int *iters, long long *stats) {
+                         const gp_fault *faults, int ntr, const gp_line_trip *trips, double dt, int nsteps,
+                         double tol, int itermax, int solver, const double *z0_s0, const double *u0_s0,
+                         const double *p_s0, double *traj, double *zfinal, int *iters, long long *stats) {
     int n = n_sys_of(P);
     sym_t S;
     sym_build(&S, P, z0, u0, p, nf, faults);
@@ -1400,7 +1451,8 @@ static int integrate_one(const gp_problem *P, const double *z0, const double *u0
     memcpy(z, z0, sizeof(double) * n);
     if (traj) memcpy(traj, z, sizeof(double) * n);
     uint8_t *on = (uint8_t *)calloc(nf > 0 ? nf : 1, 1);
-    faults_t F = {nf, faults, on};
+    uint8_t *tr_on = (uint8_t *)calloc(ntr > 0 ? ntr : 1, 1);
+    faults_t F = {nf, faults, on, ntr, trips, tr_on};
     int status = 0;
     if (solver == 2) {
         /* integrate! factors J at z0 once before the loop (src/dynamics.jl:572-580) */
@@ -1445,6 +1497,10 @@ static int integrate_one(const gp_problem *P, const double *z0, const double *u0
             if (faults[e].on_step == k) { on[e] = 1; any = 1; }
             if (faults[e].off_step == k) { on[e] = 0; any = 1; }
         }
+        for (int e = 0; e < ntr; e++) {
+            if (trips[e].on_step == k) { tr_on[e] = 1; any = 1; }
+            if (trips[e].off_step == k) { tr_on[e] = 0; any = 1; }
+        }
         if (any) {
             memcpy(zold, z, sizeof(double) * n);
             it = solver == 3   ? newton_frozen(&W, z, zold, u0, p, &F, 0.0, tol, itermax, &ok, &LP, &LPf)
@@ -1468,6 +1524,7 @@ static int integrate_one(const gp_problem *P, const double *z0, const double *u0
         splu_free(&LPf);
     }
     free(on);
+    free(tr_on);
     free(z);
     free(zold);
     ws_free(&W);
@@ -1488,9 +1545,10 @@ static int integrate_one(const gp_problem *P, const double *z0, const double *u0
  * scenario 0 at its initial state, factored once, with each scenario's
  * fault shunt; every scenario has at most one fault bus and rfault).  traj [M][nsteps+1][n_sys] or NULL; zfinal [M][n_sys]
  * or NULL; iters [M][2*nsteps] or NULL; status [M]; stats [M][6] or NULL. */
-int gpo_integrate(const gp_problem *P, int M, const double *z0, const double *u0, const double *p, int nf,
-                  const gp_fault *faults, double dt, int nsteps, double tol, int itermax, int solver,
-                  int nthreads, double *traj, double *zfinal, int *iters, int *status, long long *stats) {
+int gpo_integrate_trips(const gp_problem *P, int M, const double *z0, const double *u0, const double *p, int nf,
+                        const gp_fault *faults, int ntr_all, const gp_line_trip *trips_all, double dt, int nsteps,
+                        double tol, int itermax, int solver, int nthreads, double *traj, double *zfinal,
+                        int *iters, int *status, long long *stats) {
     int n = n_sys_of(P);
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -1504,16 +1562,31 @@ int gpo_integrate(const gp_problem *P, int M, const double *z0, const double *u0
         cnt = 0;
         for (int e = 0; e < nf; e++)
             if (faults[e].scenario < 0 || faults[e].scenario == m) fm[cnt++] = faults[e];
+        int ct = 0;
+        for (int e = 0; e < ntr_all; e++)
+            if (trips_all[e].scenario < 0 || trips_all[e].scenario == m) ct++;
+        gp_line_trip *tm = (gp_line_trip *)malloc(sizeof(gp_line_trip) * (ct > 0 ? ct : 1));
+        ct = 0;
+        for (int e = 0; e < ntr_all; e++)
+            if (trips_all[e].scenario < 0 || trips_all[e].scenario == m) tm[ct++] = trips_all[e];
         status[m] = integrate_one(P, z0 + (size_t)m * n, u0 + (size_t)m * P->n_ctrl, p + (size_t)m * P->n_par, cnt,
-                                  fm, dt, nsteps, tol, itermax, solver, z0, u0, p,
+                                  fm, ct, tm, dt, nsteps, tol, itermax, solver, z0, u0, p,
                                   traj ? traj + (size_t)m * (nsteps + 1) * n : NULL,
                                   zfinal ? zfinal + (size_t)m * n : NULL,
                                   iters ? iters + (size_t)m * 2 * nsteps : NULL,
                                   stats ? stats + (size_t)m * 6 : NULL);
         free(fm);
+        free(tm);
     }
     (void)nthreads;
     return 0;
+}
+
+int gpo_integrate(const gp_problem *P, int M, const double *z0, const double *u0, const double *p, int nf,
+                  const gp_fault *faults, double dt, int nsteps, double tol, int itermax, int solver,
+                  int nthreads, double *traj, double *zfinal, int *iters, int *status, long long *stats) {
+    return gpo_integrate_trips(P, M, z0, u0, p, nf, faults, 0, NULL, dt, nsteps, tol, itermax, solver, nthreads,
+                               traj, zfinal, iters, status, stats);
 }
 
 /* Backward-Euler residual of one scenario with the flagged faults on. */
@@ -1530,6 +1603,32 @@ int gpo_jacobian_dense(const gp_problem *P, const double *z, const double *u0, c
                        const gp_fault *faults, const uint8_t *fault_on, double dt, double *Jd) {
     int n = n_sys_of(P), nda = P->n_diff + P->n_alg;
     faults_t F = {nf, faults, fault_on};
+    trip_t t = {0};
+    jacobian_rhs(P, z, u0, p, &F, &t);
+    memset(Jd, 0, sizeof(double) * (size_t)n * n);
+    for (int k = 0; k < t.n; k++) Jd[(size_t)t.r[k] * n + t.c[k]] += t.v[k];
+    for (int i = 0; i < nda; i++)
+        if (P->is_diff[i]) {
+            for (int j = 0; j < n; j++) Jd[(size_t)i * n + j] *= -dt;
+            Jd[(size_t)i * n + i] += 1.0;
+        }
+    trip_free(&t);
+    return 0;
+}
+
+/* The residual and the dense Jacobian with line trips: trips [ntr] of this
+ * scenario, trip_on [ntr] which of them are tripped. */
+int gpo_residual_trips(const gp_problem *P, const double *z, const double *zold, const double *u0, const double *p,
+                       int ntr, const gp_line_trip *trips, const uint8_t *trip_on, double dt, double *f) {
+    faults_t F = {0, NULL, NULL, ntr, trips, trip_on};
+    residual_be(P, z, zold, u0, p, &F, dt, f);
+    return 0;
+}
+
+int gpo_jacobian_dense_trips(const gp_problem *P, const double *z, const double *u0, const double *p, int ntr,
+                             const gp_line_trip *trips, const uint8_t *trip_on, double dt, double *Jd) {
+    int n = n_sys_of(P), nda = P->n_diff + P->n_alg;
+    faults_t F = {0, NULL, NULL, ntr, trips, trip_on};
     trip_t t = {0};
     jacobian_rhs(P, z, u0, p, &F, &t);
     memset(Jd, 0, sizeof(double) * (size_t)n * n);
