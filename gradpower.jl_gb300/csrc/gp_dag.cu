@@ -167,9 +167,16 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
         const int mc = ncc + rc;
         const int *rel = S.relmap + S.relmap_ptr[c];
         const T *Fc = fr + S.front_off[c];
+        // (a, b) = (t % rc, t / rc), advanced by the stride without a
+        // division per entry
+        const int rcs = rc > 0 ? rc : 1;   // (a child always has update rows)
+        int a = idx % rcs, b = idx / rcs;
+        const int da = step % rcs, db = step / rcs;
         for (int t = idx; t < rc * rc; t += step) {
-            const int a = t % rc, b = t / rc;
             F[rel[a] + rel[b] * mm] += ldcg(Fc + (ncc + a) + (size_t)(ncc + b) * mc);
+            a += da;
+            b += db;
+            if (a >= rc) { a -= rc; b++; }
         }
         if (RHS) {
             const double *uc = uv + S.uvec_off[c];
@@ -236,15 +243,28 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
         }
         g.sync();
         const int r = mm - ns, n = r * (nc - ns);
+        // entry t0 + q * step is (ns + t % r, ns + t / r); the four row and
+        // column indices advance by 4 * step without a division per entry
+        const int rr = r > 0 ? r : 1;   // (no entries when r == 0)
+        int rq[4], cq[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            rq[q] = (idx + q * step) % rr;
+            cq[q] = (idx + q * step) / rr;
+        }
+        const int dr = (4 * step) % rr, dc = (4 * step) / rr;
         for (int t0 = idx; t0 < n; t0 += 4 * step) {
             int ri[4], cj[4];
             T acc[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
-                const int t = min(t0 + q * step, n - 1);
-                ri[q] = ns + t % r;
-                cj[q] = (ns + t / r) * mm;
+                const bool in = t0 + q * step < n;
+                ri[q] = ns + (in ? rq[q] : r - 1);
+                cj[q] = (ns + (in ? cq[q] : nc - ns - 1)) * mm;
                 acc[q] = F[ri[q] + cj[q]];
+                rq[q] += dr;
+                cq[q] += dc;
+                if (rq[q] >= r) { rq[q] -= r; cq[q]++; }
             }
             for (int k = 0; k < ns; k++) {
                 const T *lk = F + k * mm;
