@@ -56,70 +56,82 @@ GP_HD void genrou_eval(const DevRef &d, int net, const double *z, const double *
     const int pm_idx = d.link0, efd_idx = d.link1;
     const double e_fd = efd_idx >= 0 ? z[efd_idx] : u0[cp];
     const double p_m = pm_idx >= 0 ? z[pm_idx] : u0[cp + 1];
+    // every division by a parameter is taken once, as a reciprocal
+    // (FP64 division is dear on this GPU; the equations are unchanged)
     const double dpl = x_dp - xl, qpl = x_qp - xl;
-    const double psi_de = (x_ddp - xl) / dpl * e_qp + (x_dp - x_ddp) / dpl * phi_1d;
-    const double psi_qe = -(x_ddp - xl) / qpl * e_dp + (x_qp - x_ddp) / qpl * phi_2q;
+    const double idpl = 1.0 / dpl, iqpl = 1.0 / qpl;
+    const double iTd = 1.0 / T_d0p, iTq = 1.0 / T_q0p, iTdd = 1.0 / T_d0dp, iTqd = 1.0 / T_q0dp;
+    const double i2H = 0.5 / H, ixd = 1.0 / x_ddp;   // x_qdp = x_ddp
+    const double a_eqp = (x_ddp - xl) * idpl, a_phi1d = (x_dp - x_ddp) * idpl;
+    const double b_edp = -(x_ddp - xl) * iqpl, b_phi2q = (x_qp - x_ddp) * iqpl;
+    const double kd = (x_dp - x_ddp) * idpl * idpl, kq = (x_qp - x_qdp) * iqpl * iqpl;
+    const double psi_de = a_eqp * e_qp + a_phi1d * phi_1d;
+    const double psi_qe = b_edp * e_dp + b_phi2q * phi_2q;
     double sa, sb;
     sat_coef(S1, S2, sa, sb);
     const double psi2 = sqrt(psi_de * psi_de + psi_qe * psi_qe);
     const bool sat_on = !(sb == 0.0 || psi2 <= sa || psi2 == 0.0);
-    const double Se = sat_on ? sb * (psi2 - sa) * (psi2 - sa) / psi2 : 0.0;
-    const double sd = sin(delta), cd = cos(delta);
-    M.putf(dp, (-e_qp + e_fd - (i_d - (-x_ddp + x_dp) * (-e_qp + i_d * dpl + phi_1d) / (dpl * dpl)) * (x_d - x_dp) -
-                Se * psi_de) / T_d0p);
-    M.putf(dp + 1, (-e_dp + (i_q - (-x_qdp + x_qp) * (e_dp + i_q * qpl + phi_2q) / (qpl * qpl)) * (x_q - x_qp)) / T_q0p);
-    M.putf(dp + 2, (e_qp - i_d * dpl - phi_1d) / T_d0dp);
-    M.putf(dp + 3, (-e_dp - i_q * qpl - phi_2q) / T_q0dp);
-    M.putf(dp + 4, (p_m - D * w - psi_de * i_q + psi_qe * i_d) / (2.0 * H));
+    const double ipsi2 = psi2 == 0.0 ? 0.0 : 1.0 / psi2;
+    const double Se = sat_on ? sb * (psi2 - sa) * (psi2 - sa) * ipsi2 : 0.0;
+    double sd, cd;
+#ifdef __CUDA_ARCH__
+    sincos(delta, &sd, &cd);
+#else
+    sd = sin(delta);
+    cd = cos(delta);
+#endif
+    M.putf(dp, (-e_qp + e_fd - (i_d - kd * (-e_qp + i_d * dpl + phi_1d)) * (x_d - x_dp) - Se * psi_de) * iTd);
+    M.putf(dp + 1, (-e_dp + (i_q - kq * (e_dp + i_q * qpl + phi_2q)) * (x_q - x_qp)) * iTq);
+    M.putf(dp + 2, (e_qp - i_d * dpl - phi_1d) * iTdd);
+    M.putf(dp + 3, (-e_dp - i_q * qpl - phi_2q) * iTqd);
+    M.putf(dp + 4, (p_m - D * w - psi_de * i_q + psi_qe * i_d) * i2H);
     M.putf(dp + 5, kTwoPi60 * w);
-    M.putf(ap, i_d - ((x_ddp - xl) / dpl * e_qp + (x_dp - x_ddp) / dpl * phi_1d - v_q) / x_ddp);
-    M.putf(ap + 1, i_q - (-(x_qdp - xl) / qpl * e_dp + (x_qp - x_qdp) / qpl * phi_2q + v_d) / x_qdp);
+    M.putf(ap, i_d - (psi_de - v_q) * ixd);
+    M.putf(ap + 1, i_q - (psi_qe + v_d) * ixd);
     M.putf(ap + 2, v_d - (vr * sd - vi * cd));
     M.putf(ap + 3, v_q - (vr * cd + vi * sd));
     double dSe = 0.0;
     if (sat_on) {
         double g = psi2 - sa;
-        dSe = sb * (2.0 * g * psi2 - g * g) / (psi2 * psi2);
+        dSe = sb * (2.0 * g * psi2 - g * g) * ipsi2 * ipsi2;
     }
-    const double dpd = psi2 == 0.0 ? 0.0 : psi_de / psi2;
-    const double dpq = psi2 == 0.0 ? 0.0 : psi_qe / psi2;
-    const double a_eqp = (x_ddp - xl) / dpl, a_phi1d = (x_dp - x_ddp) / dpl;
-    const double b_edp = -(x_ddp - xl) / qpl, b_phi2q = (x_qp - x_ddp) / qpl;
+    const double dpd = psi_de * ipsi2;
+    const double dpq = psi_qe * ipsi2;
     const double dT_dde = -(dSe * dpd * psi_de + Se);
     const double dT_dqe = -(dSe * dpq * psi_de);
     const int c_eqp = dp, c_edp = dp + 1, c_phi1d = dp + 2, c_phi2q = dp + 3, c_w = dp + 4, c_delta = dp + 5;
     const int c_vq = ap, c_vd = ap + 1, c_iq = ap + 2, c_id = ap + 3;
-    M.put(dp, c_eqp, (-(x_d - x_dp) * (-x_ddp + x_dp) / (dpl * dpl) - 1) / T_d0p + dT_dde * a_eqp / T_d0p);
-    M.put(dp, c_phi1d, (x_d - x_dp) * (-x_ddp + x_dp) / (dpl * dpl) / T_d0p + dT_dde * a_phi1d / T_d0p);
-    M.put(dp, c_id, -(x_d - x_dp) * (-(-x_ddp + x_dp) / dpl + 1) / T_d0p);
-    M.put(dp, c_edp, dT_dqe * b_edp / T_d0p);
-    M.put(dp, c_phi2q, dT_dqe * b_phi2q / T_d0p);
-    if (efd_idx >= 0) M.put(dp, efd_idx, 1.0 / T_d0p);
-    M.put(dp + 1, c_edp, (-(x_q - x_qp) * (-x_qdp + x_qp) / (qpl * qpl) - 1) / T_q0p);
-    M.put(dp + 1, c_phi2q, -(x_q - x_qp) * (-x_qdp + x_qp) / (qpl * qpl) / T_q0p);
-    M.put(dp + 1, c_iq, (x_q - x_qp) * (-(-x_qdp + x_qp) / qpl + 1) / T_q0p);
-    M.put(dp + 2, c_eqp, 1.0 / T_d0dp);
-    M.put(dp + 2, c_phi1d, -1.0 / T_d0dp);
-    M.put(dp + 2, c_id, (-x_dp + xl) / T_d0dp);
-    M.put(dp + 3, c_edp, -1.0 / T_q0dp);
-    M.put(dp + 3, c_phi2q, -1.0 / T_q0dp);
-    M.put(dp + 3, c_iq, (-x_qp + xl) / T_q0dp);
-    M.put(dp + 4, c_eqp, -0.5 * i_q * (x_ddp - xl) / (H * dpl));
-    M.put(dp + 4, c_edp, 0.5 * i_d * (-x_ddp + xl) / (H * qpl));
-    M.put(dp + 4, c_phi1d, -0.5 * i_q * (-x_ddp + x_dp) / (H * dpl));
-    M.put(dp + 4, c_phi2q, 0.5 * i_d * (-x_ddp + x_qp) / (H * qpl));
-    M.put(dp + 4, c_w, -0.5 * D / H);
-    if (pm_idx >= 0) M.put(dp + 4, pm_idx, 0.5 / H);
-    M.put(dp + 4, c_iq, 0.5 * (-e_qp * (x_ddp - xl) / dpl - phi_1d * (-x_ddp + x_dp) / dpl) / H);
-    M.put(dp + 4, c_id, 0.5 * (e_dp * (-x_ddp + xl) / qpl + phi_2q * (-x_ddp + x_qp) / qpl) / H);
+    M.put(dp, c_eqp, (-(x_d - x_dp) * kd - 1) * iTd + dT_dde * a_eqp * iTd);
+    M.put(dp, c_phi1d, (x_d - x_dp) * kd * iTd + dT_dde * a_phi1d * iTd);
+    M.put(dp, c_id, -(x_d - x_dp) * (-(x_dp - x_ddp) * idpl + 1) * iTd);
+    M.put(dp, c_edp, dT_dqe * b_edp * iTd);
+    M.put(dp, c_phi2q, dT_dqe * b_phi2q * iTd);
+    if (efd_idx >= 0) M.put(dp, efd_idx, iTd);
+    M.put(dp + 1, c_edp, (-(x_q - x_qp) * kq - 1) * iTq);
+    M.put(dp + 1, c_phi2q, -(x_q - x_qp) * kq * iTq);
+    M.put(dp + 1, c_iq, (x_q - x_qp) * (-(x_qp - x_qdp) * iqpl + 1) * iTq);
+    M.put(dp + 2, c_eqp, iTdd);
+    M.put(dp + 2, c_phi1d, -iTdd);
+    M.put(dp + 2, c_id, (-x_dp + xl) * iTdd);
+    M.put(dp + 3, c_edp, -iTqd);
+    M.put(dp + 3, c_phi2q, -iTqd);
+    M.put(dp + 3, c_iq, (-x_qp + xl) * iTqd);
+    M.put(dp + 4, c_eqp, -i_q * a_eqp * i2H);
+    M.put(dp + 4, c_edp, i_d * b_edp * i2H);
+    M.put(dp + 4, c_phi1d, -i_q * a_phi1d * i2H);
+    M.put(dp + 4, c_phi2q, i_d * b_phi2q * i2H);
+    M.put(dp + 4, c_w, -D * i2H);
+    if (pm_idx >= 0) M.put(dp + 4, pm_idx, i2H);
+    M.put(dp + 4, c_iq, -psi_de * i2H);
+    M.put(dp + 4, c_id, psi_qe * i2H);
     M.put(dp + 5, c_w, kTwoPi60);
-    M.put(ap, c_eqp, -(x_ddp - xl) / (x_ddp * dpl));
-    M.put(ap, c_phi1d, -(-x_ddp + x_dp) / (x_ddp * dpl));
-    M.put(ap, c_vq, 1.0 / x_ddp);
+    M.put(ap, c_eqp, -a_eqp * ixd);
+    M.put(ap, c_phi1d, -a_phi1d * ixd);
+    M.put(ap, c_vq, ixd);
     M.put(ap, c_id, 1.0);
-    M.put(ap + 1, c_edp, -(-x_qdp + xl) / (x_qdp * qpl));
-    M.put(ap + 1, c_phi2q, -(-x_qdp + x_qp) / (x_qdp * qpl));
-    M.put(ap + 1, c_vd, -1.0 / x_qdp);
+    M.put(ap + 1, c_edp, -b_edp * ixd);
+    M.put(ap + 1, c_phi2q, -b_phi2q * ixd);
+    M.put(ap + 1, c_vd, -ixd);
     M.put(ap + 1, c_iq, 1.0);
     M.put(ap + 2, c_delta, -vr * cd - vi * sd);
     M.put(ap + 2, c_vd, 1.0);
@@ -146,24 +158,25 @@ GP_HD void ieesgo_eval(const DevRef &d, const double *z, const double *p, Sink &
     const double K1 = p[pp + 6], K2 = p[pp + 7], K3 = p[pp + 8], pref = p[pp + 11];
     const double PF0 = z[dp], PLL = z[dp + 1], TP1 = z[dp + 2], TP2 = z[dp + 3], TP3 = z[dp + 4], p_m = z[ap];
     const double w = wi < 0 ? 0.0 : z[wi];
-    M.putf(dp, (1.0 / T1) * (K1 * w - PF0));
-    M.putf(dp + 1, (1.0 / T3) * ((1.0 - (T2 / T3)) * PF0 - PLL));
-    const double SatP = pref - (T2 / T3) * PF0 - PLL;
-    M.putf(dp + 2, (1.0 / T4) * (SatP - TP1));
-    M.putf(dp + 3, (1.0 / T5) * (K2 * TP1 - TP2));
-    M.putf(dp + 4, (1.0 / T6) * (K3 * TP2 - TP3));
+    const double i1 = 1.0 / T1, i3 = 1.0 / T3, i4 = 1.0 / T4, i5 = 1.0 / T5, i6 = 1.0 / T6, r23 = T2 * i3;
+    M.putf(dp, i1 * (K1 * w - PF0));
+    M.putf(dp + 1, i3 * ((1.0 - r23) * PF0 - PLL));
+    const double SatP = pref - r23 * PF0 - PLL;
+    M.putf(dp + 2, i4 * (SatP - TP1));
+    M.putf(dp + 3, i5 * (K2 * TP1 - TP2));
+    M.putf(dp + 4, i6 * (K3 * TP2 - TP3));
     M.putf(ap, TP1 * (1.0 - K2) + TP2 * (1.0 - K3) + TP3 - p_m);
-    M.put(dp, dp, -1.0 / T1);
-    if (wi >= 0) M.put(dp, wi, K1 / T1);
-    M.put(dp + 1, dp, (1.0 - T2 / T3) / T3);
-    M.put(dp + 1, dp + 1, -1.0 / T3);
-    M.put(dp + 2, dp, -T2 / (T3 * T4));
-    M.put(dp + 2, dp + 1, -1.0 / T4);
-    M.put(dp + 2, dp + 2, -1.0 / T4);
-    M.put(dp + 3, dp + 2, K2 / T5);
-    M.put(dp + 3, dp + 3, -1.0 / T5);
-    M.put(dp + 4, dp + 3, K3 / T6);
-    M.put(dp + 4, dp + 4, -1.0 / T6);
+    M.put(dp, dp, -i1);
+    if (wi >= 0) M.put(dp, wi, K1 * i1);
+    M.put(dp + 1, dp, (1.0 - r23) * i3);
+    M.put(dp + 1, dp + 1, -i3);
+    M.put(dp + 2, dp, -r23 * i4);
+    M.put(dp + 2, dp + 1, -i4);
+    M.put(dp + 2, dp + 2, -i4);
+    M.put(dp + 3, dp + 2, K2 * i5);
+    M.put(dp + 3, dp + 3, -i5);
+    M.put(dp + 4, dp + 3, K3 * i6);
+    M.put(dp + 4, dp + 4, -i6);
     M.put(ap, dp + 2, 1.0 - K2);
     M.put(ap, dp + 3, 1.0 - K3);
     M.put(ap, dp + 4, 1.0);
@@ -176,14 +189,14 @@ GP_HD void tgov1_eval(const DevRef &d, const double *z, const double *p, Sink &M
     const double R = p[pp], T1 = p[pp + 1], T2 = p[pp + 4], T3 = p[pp + 5], DT = p[pp + 6], pref = p[pp + 7];
     const double x1 = z[dp], x2 = z[dp + 1], p_m = z[ap];
     const double w = wi < 0 ? 0.0 : z[wi];
-    const double r23 = T2 / T3;
-    M.putf(dp, (-x1 + (1.0 - r23) * x2) / T3);
-    M.putf(dp + 1, ((pref - w) / R - x2) / T1);
+    const double i1 = 1.0 / T1, i3 = 1.0 / T3, iR = 1.0 / R, r23 = T2 * i3;
+    M.putf(dp, (-x1 + (1.0 - r23) * x2) * i3);
+    M.putf(dp + 1, ((pref - w) * iR - x2) * i1);
     M.putf(ap, x1 + r23 * x2 - DT * w - p_m);
-    M.put(dp, dp, -1.0 / T3);
-    M.put(dp, dp + 1, (1.0 - r23) / T3);
-    M.put(dp + 1, dp + 1, -1.0 / T1);
-    if (wi >= 0) M.put(dp + 1, wi, -1.0 / (R * T1));
+    M.put(dp, dp, -i3);
+    M.put(dp, dp + 1, (1.0 - r23) * i3);
+    M.put(dp + 1, dp + 1, -i1);
+    if (wi >= 0) M.put(dp + 1, wi, -iR * i1);
     M.put(ap, dp, 1.0);
     M.put(ap, dp + 1, r23);
     if (wi >= 0) M.put(ap, wi, -DT);
@@ -200,18 +213,19 @@ GP_HD void sexs_eval(const DevRef &d, int net, const double *z, const double *p,
     vm = vm == 0.0 ? 1e-12 : vm;
     const double vs = vsi >= 0 ? z[vsi] : 0.0;
     const double err = vref - vm + vs;
-    M.putf(dp, (-x1 + (1.0 - TA_TB) * err) / TB);
-    M.putf(dp + 1, (-e_fd + K * (x1 + TA_TB * err)) / TE);
-    const double dvr = vr / vm, dvi = vi / vm;
-    M.put(dp, dp, -1.0 / TB);
-    M.putv(dp, 0, -(1.0 - TA_TB) * dvr / TB);
-    M.putv(dp, 1, -(1.0 - TA_TB) * dvi / TB);
-    if (vsi >= 0) M.put(dp, vsi, (1.0 - TA_TB) / TB);
-    M.put(dp + 1, dp, K / TE);
-    M.put(dp + 1, dp + 1, -1.0 / TE);
-    M.putv(dp + 1, 0, -K * TA_TB * dvr / TE);
-    M.putv(dp + 1, 1, -K * TA_TB * dvi / TE);
-    if (vsi >= 0) M.put(dp + 1, vsi, K * TA_TB / TE);
+    const double iTB = 1.0 / TB, iTE = 1.0 / TE;
+    M.putf(dp, (-x1 + (1.0 - TA_TB) * err) * iTB);
+    M.putf(dp + 1, (-e_fd + K * (x1 + TA_TB * err)) * iTE);
+    const double ivm = 1.0 / vm, dvr = vr * ivm, dvi = vi * ivm;
+    M.put(dp, dp, -iTB);
+    M.putv(dp, 0, -(1.0 - TA_TB) * dvr * iTB);
+    M.putv(dp, 1, -(1.0 - TA_TB) * dvi * iTB);
+    if (vsi >= 0) M.put(dp, vsi, (1.0 - TA_TB) * iTB);
+    M.put(dp + 1, dp, K * iTE);
+    M.put(dp + 1, dp + 1, -iTE);
+    M.putv(dp + 1, 0, -K * TA_TB * dvr * iTE);
+    M.putv(dp + 1, 1, -K * TA_TB * dvi * iTE);
+    if (vsi >= 0) M.put(dp + 1, vsi, K * TA_TB * iTE);
 }
 
 template <class Sink>
@@ -226,21 +240,22 @@ GP_HD void esdc1a_eval(const DevRef &d, int net, const double *z, const double *
     const double vs = vsi >= 0 ? z[vsi] : 0.0;
     const bool son = !(sat_b == 0.0 || e_fd <= sat_a);
     const double sat = son ? sat_b * (e_fd - sat_a) * (e_fd - sat_a) : 0.0;
-    M.putf(dp, (Ka * (vref - vm + vs - vr2 - (Kf / Tf) * e_fd) - vr1) / Ta);
-    M.putf(dp + 1, -((Kf / Tf) * e_fd + vr2) / Tf);
-    M.putf(dp + 2, (vr1 - Ke * e_fd - sat) / Te);
-    const double dvr = vr / vm, dvi = vi / vm;
+    const double iTa = 1.0 / Ta, iTf = 1.0 / Tf, iTe = 1.0 / Te, kft = Kf * iTf;
+    M.putf(dp, (Ka * (vref - vm + vs - vr2 - kft * e_fd) - vr1) * iTa);
+    M.putf(dp + 1, -(kft * e_fd + vr2) * iTf);
+    M.putf(dp + 2, (vr1 - Ke * e_fd - sat) * iTe);
+    const double ivm = 1.0 / vm, dvr = vr * ivm, dvi = vi * ivm;
     const double dsat = son ? 2.0 * sat_b * (e_fd - sat_a) : 0.0;
-    M.put(dp, dp, -1.0 / Ta);
-    M.put(dp, dp + 1, -Ka / Ta);
-    M.put(dp, dp + 2, -Ka * Kf / (Ta * Tf));
-    M.putv(dp, 0, -Ka * dvr / Ta);
-    M.putv(dp, 1, -Ka * dvi / Ta);
-    if (vsi >= 0) M.put(dp, vsi, Ka / Ta);
-    M.put(dp + 1, dp + 1, -1.0 / Tf);
-    M.put(dp + 1, dp + 2, -Kf / (Tf * Tf));
-    M.put(dp + 2, dp, 1.0 / Te);
-    M.put(dp + 2, dp + 2, -(Ke + dsat) / Te);
+    M.put(dp, dp, -iTa);
+    M.put(dp, dp + 1, -Ka * iTa);
+    M.put(dp, dp + 2, -Ka * kft * iTa);
+    M.putv(dp, 0, -Ka * dvr * iTa);
+    M.putv(dp, 1, -Ka * dvi * iTa);
+    if (vsi >= 0) M.put(dp, vsi, Ka * iTa);
+    M.put(dp + 1, dp + 1, -iTf);
+    M.put(dp + 1, dp + 2, -kft * iTf);
+    M.put(dp + 2, dp, iTe);
+    M.put(dp + 2, dp + 2, -(Ke + dsat) * iTe);
 }
 
 template <class Sink>
@@ -252,48 +267,46 @@ GP_HD void ieeest_eval(const DevRef &d, const double *z, const double *p, Sink &
     const double s0 = z[dp], s1 = z[dp + 1], s2 = z[dp + 2], s3 = z[dp + 3], s4 = z[dp + 4], s5 = z[dp + 5],
                  s6 = z[dp + 6], vs = z[ap];
     const double sig = wi >= 0 ? z[wi] : 0.0;
+    const double iA2 = 1.0 / A2, iA4 = 1.0 / A4, iT2 = 1.0 / T2, iT4 = 1.0 / T4, iT6 = 1.0 / T6;
+    const double rA = A6 * iA4, r12 = T1 * iT2, r34 = T3 * iT4, r56 = T5 * iT6;
     const double q = s1 - s3 - A3 * s2;
-    const double y2 = s3 + A5 * s2 + (A6 / A4) * q;
-    const double y3 = s4 + (T1 / T2) * (y2 - s4);
-    const double y4 = s5 + (T3 / T4) * (y3 - s5);
-    M.putf(dp, (sig - s1 - A1 * s0) / A2);
+    const double y2 = s3 + A5 * s2 + rA * q;
+    const double y3 = s4 + r12 * (y2 - s4);
+    const double y4 = s5 + r34 * (y3 - s5);
+    M.putf(dp, (sig - s1 - A1 * s0) * iA2);
     M.putf(dp + 1, s0);
-    M.putf(dp + 2, (s1 - s3 - A3 * s2) / A4);
+    M.putf(dp + 2, (s1 - s3 - A3 * s2) * iA4);
     M.putf(dp + 3, s2);
-    M.putf(dp + 4, (y2 - s4) / T2);
-    M.putf(dp + 5, (y3 - s5) / T4);
-    M.putf(dp + 6, (KS * y4 - s6) / T6);
-    M.putf(ap, vs - (T5 / T6) * (KS * y4 - s6));
-    const double rA = A6 / A4;
+    M.putf(dp + 4, (y2 - s4) * iT2);
+    M.putf(dp + 5, (y3 - s5) * iT4);
+    M.putf(dp + 6, (KS * y4 - s6) * iT6);
+    M.putf(ap, vs - r56 * (KS * y4 - s6));
     const double d20 = rA, d21 = A5 - A3 * rA, d22 = 1.0 - rA;
-    const double r12 = T1 / T2;
     const double d30 = r12 * d20, d31 = r12 * d21, d32 = r12 * d22, d33 = 1.0 - r12;
-    const double r34 = T3 / T4;
     const double d40 = r34 * d30, d41 = r34 * d31, d42 = r34 * d32, d43 = r34 * d33, d44 = 1.0 - r34;
-    M.put(dp, dp, -A1 / A2);
-    M.put(dp, dp + 1, -1.0 / A2);
-    if (wi >= 0) M.put(dp, wi, 1.0 / A2);
+    M.put(dp, dp, -A1 * iA2);
+    M.put(dp, dp + 1, -iA2);
+    if (wi >= 0) M.put(dp, wi, iA2);
     M.put(dp + 1, dp, 1.0);
-    M.put(dp + 2, dp + 1, 1.0 / A4);
-    M.put(dp + 2, dp + 2, -A3 / A4);
-    M.put(dp + 2, dp + 3, -1.0 / A4);
+    M.put(dp + 2, dp + 1, iA4);
+    M.put(dp + 2, dp + 2, -A3 * iA4);
+    M.put(dp + 2, dp + 3, -iA4);
     M.put(dp + 3, dp + 2, 1.0);
-    M.put(dp + 4, dp + 1, d20 / T2);
-    M.put(dp + 4, dp + 2, d21 / T2);
-    M.put(dp + 4, dp + 3, d22 / T2);
-    M.put(dp + 4, dp + 4, -1.0 / T2);
-    M.put(dp + 5, dp + 1, d30 / T4);
-    M.put(dp + 5, dp + 2, d31 / T4);
-    M.put(dp + 5, dp + 3, d32 / T4);
-    M.put(dp + 5, dp + 4, d33 / T4);
-    M.put(dp + 5, dp + 5, -1.0 / T4);
-    M.put(dp + 6, dp + 1, KS * d40 / T6);
-    M.put(dp + 6, dp + 2, KS * d41 / T6);
-    M.put(dp + 6, dp + 3, KS * d42 / T6);
-    M.put(dp + 6, dp + 4, KS * d43 / T6);
-    M.put(dp + 6, dp + 5, KS * d44 / T6);
-    M.put(dp + 6, dp + 6, -1.0 / T6);
-    const double r56 = T5 / T6;
+    M.put(dp + 4, dp + 1, d20 * iT2);
+    M.put(dp + 4, dp + 2, d21 * iT2);
+    M.put(dp + 4, dp + 3, d22 * iT2);
+    M.put(dp + 4, dp + 4, -iT2);
+    M.put(dp + 5, dp + 1, d30 * iT4);
+    M.put(dp + 5, dp + 2, d31 * iT4);
+    M.put(dp + 5, dp + 3, d32 * iT4);
+    M.put(dp + 5, dp + 4, d33 * iT4);
+    M.put(dp + 5, dp + 5, -iT4);
+    M.put(dp + 6, dp + 1, KS * d40 * iT6);
+    M.put(dp + 6, dp + 2, KS * d41 * iT6);
+    M.put(dp + 6, dp + 3, KS * d42 * iT6);
+    M.put(dp + 6, dp + 4, KS * d43 * iT6);
+    M.put(dp + 6, dp + 5, KS * d44 * iT6);
+    M.put(dp + 6, dp + 6, -iT6);
     M.put(ap, dp + 1, -r56 * KS * d40);
     M.put(ap, dp + 2, -r56 * KS * d41);
     M.put(ap, dp + 3, -r56 * KS * d42);

@@ -265,7 +265,9 @@ def test_cluster_factorisation_matches_dense_solves(lib, golden_cases, orc, case
         A = J[s, s]
         B = J[s][:, rows]
         Cm = J[rows][:, s]
-        assert np.max(np.abs(fc[s] - f[s])) <= 1e-15 * max(1.0, np.max(np.abs(f[s])))
+        # the device equations take each division by a parameter once, as a
+        # reciprocal: the same residual to rounding (terms up to ~1/x''_d)
+        assert np.max(np.abs(fc[s] - f[s])) <= 1e-12 * max(1.0, np.max(np.abs(f[s])))
         fmax = max(fmax, np.max(np.abs(f[s])))
         y = np.linalg.solve(A, f[s])
         X = np.linalg.solve(A, B)
