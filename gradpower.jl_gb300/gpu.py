@@ -84,7 +84,8 @@ class GpuBatchedLayout:
     garbage collection releases it."""
 
     def __init__(self, dp: Mdl.DynamicProblem, ps: Mdl.PowerSystem, M: int,
-                 z0: Optional[np.ndarray] = None, p: Optional[np.ndarray] = None):
+                 z0: Optional[np.ndarray] = None, p: Optional[np.ndarray] = None,
+                 u0: Optional[np.ndarray] = None):
         self.ps = ps
         self.M = int(M)
         self.arrays = LY.ProblemArrays(ps)
@@ -93,6 +94,8 @@ class GpuBatchedLayout:
             z = np.ascontiguousarray(z0, dtype=np.float64).reshape(self.M, -1)
         if p is not None:
             pp = np.ascontiguousarray(p, dtype=np.float64).reshape(self.M, -1)
+        if u0 is not None:
+            u = np.ascontiguousarray(u0, dtype=np.float64).reshape(self.M, -1)
         self.n_sys = self.arrays.n_sys
         self.n_par = self.arrays.n_par
         self._keep = (z, u, pp)
@@ -264,6 +267,86 @@ def integrate_gpu_shared_multi(gbl: GpuBatchedLayout, ps: Mdl.PowerSystem, tf: f
               for b, r in zip(fault_buses, rfaults)]
     r = gbl.integrate(tf, dt, newton_tol, 30, (), faults, solver=LY.SOLVER_SHARED_WOODBURY)
     return r["tvec"], [r["traj"][m].T for m in range(gbl.M)]
+
+
+def batched_power_flow(ps: Mdl.PowerSystem, load_scale, gen_scale=None, tol: float = 1e-10,
+                       itermax: int = 30, v_start=None):
+    """Power flows of len(load_scale) scenarios at once on the GPU: scenario
+    m scales every load (P and Q) by load_scale[m] and the scheduled output
+    of the non-slack generators by gen_scale[m] (default load_scale[m]).
+    The library's Newton step runs on Mdl.power_flow_problem(ps) (the
+    reference's power flow, src/pflow.jl, in current-injection form), one
+    scenario per batch member; the start is ps's bus voltages (or v_start
+    [M, n_bus] complex).  Returns dict(vm, va [M, n_bus], v [M, n_bus]
+    complex, iters [M], status [M], p_slack [M] the slack bus's output)."""
+    load_scale = np.asarray(load_scale, dtype=np.float64).reshape(-1)
+    gen_scale = load_scale if gen_scale is None else np.asarray(gen_scale, dtype=np.float64).reshape(-1)
+    M_ = load_scale.size
+    ps2, dp = Mdl.power_flow_problem(ps)
+    psd = ps2.dynamic
+    pvec = np.tile(dp.pvec, (M_, 1))
+    for rec in psd.devices:
+        d = rec.dtype
+        if d.kind == "zipload":
+            pvec[:, rec.par_ptr] *= load_scale
+            pvec[:, rec.par_ptr + 1] *= load_scale
+        elif d.kind == "static_gen" and d.bus_type != Mdl.SLACK:
+            pvec[:, rec.par_ptr] *= gen_scale
+    z0 = np.tile(dp.zvec, (M_, 1))
+    net = psd.diff_dim + psd.alg_dim
+    if v_start is not None:
+        v = np.asarray(v_start, dtype=np.complex128).reshape(M_, ps2.nbus)
+        z0[:, net::2] = v.real
+        z0[:, net + 1::2] = v.imag
+    gbl = GpuBatchedLayout(dp, ps2, M_, z0=z0, p=pvec)
+    try:
+        dt = 1.0 / 120.0      # no differential states: dt does not enter
+        r = gbl.integrate(dt, dt, newton_tol=tol, itermax=itermax)
+    finally:
+        gbl.close()
+    z = r["traj"][:, 1, :]
+    v = z[:, net::2] + 1j * z[:, net + 1::2]
+    out = dict(v=v, vm=np.abs(v), va=np.angle(v), iters=r["iters"][:, 0].copy(), status=r["status"])
+    for rec in psd.devices:
+        d = rec.dtype
+        if d.kind == "static_gen" and d.bus_type == Mdl.SLACK:
+            out["p_slack"] = z[:, rec.alg_ptr].copy()
+    return out
+
+
+def scenario_initial_states(ps: Mdl.PowerSystem, load_scale, gen_scale=None, tol: float = 1e-10):
+    """Per-scenario initial conditions for a parameter sweep over load
+    levels: the power flows of every scenario on the GPU
+    (batched_power_flow), then each scenario's device initialisation
+    (model.initialize_dynamics, the reference's initialize_dynamics!,
+    src/dynamics.jl:123-250) on its solution, on the host.  Returns
+    (z0 [M, n_sys], u0 [M, n_ctrl], p [M, n_par]) for GpuBatchedLayout."""
+    import copy
+    load_scale = np.asarray(load_scale, dtype=np.float64).reshape(-1)
+    gen_scale = load_scale if gen_scale is None else np.asarray(gen_scale, dtype=np.float64).reshape(-1)
+    r = batched_power_flow(ps, load_scale, gen_scale, tol=tol)
+    if np.any(r["status"] != 0):
+        raise GradPowerError("power flow of scenario(s) %s did not converge" % np.nonzero(r["status"])[0].tolist())
+    slack = {i for i, b in enumerate(ps.buses) if b.type == Mdl.SLACK}
+    zs, us, ps_ = [], [], []
+    for m in range(load_scale.size):
+        s = copy.deepcopy(ps)
+        for l in s.loads:
+            l.pd *= load_scale[m]
+            l.qd *= load_scale[m]
+        for g in s.gens:
+            if g.bus not in slack:
+                g.psch *= gen_scale[m]
+        for rec in s.dynamic.devices:
+            if rec.dtype.kind == "zipload":
+                rec.dtype.pinj *= load_scale[m]
+                rec.dtype.qinj *= load_scale[m]
+        Mdl.apply_pf_solution(s, r["vm"][m], r["va"][m])
+        dp = Mdl.initialize_dynamics(s)
+        zs.append(dp.zvec)
+        us.append(dp.uvec)
+        ps_.append(dp.pvec)
+    return np.array(zs), np.array(us), np.array(ps_)
 
 
 class BatchedLayout(GpuBatchedLayout):

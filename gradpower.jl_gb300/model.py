@@ -497,6 +497,22 @@ def runpf(ps: PowerSystem, tol: float = 1e-13, maxiter: int = 50):
     return vm, va, P, Q
 
 
+def power_flow_problem(ps: PowerSystem):
+    """The power flow of ps as a problem of the library's Newton step: every
+    generator as a StaticGenerator stand-in (PV: q unknown and |V| = vset;
+    slack: p and q unknown and V fixed; PQ: fixed injection) and every load
+    as a constant-power ZIPLoad (alpha = 0).  These are the mismatch
+    equations of `resfun!` (src/pflow.jl:3-53) in current-injection form, so
+    the root is the power-flow solution.  Returns (ps_pf, dp_pf): ps_pf
+    shares ps's network; dp_pf starts at ps's bus voltages."""
+    ps2 = PowerSystem(ps.baseMVA, ps.buses, ps.gens, ps.loads, ps.branches, ps.shunts, dict(ps.busmap),
+                      ps.ybus, ps.adjacency)
+    psd = PowerSystemDynamics([])
+    set_dynamics(ps2, psd, add_loads=True, add_static_gen_stubs=True, load_alpha=0.0)
+    ps2.dynamic = psd
+    return ps2, initialize_dynamics(ps2)
+
+
 def runpf_inplace(ps: PowerSystem, **kw) -> None:
     """Write the power-flow solution back into the buses and generators,
     restating `runpf!` (src/pflow.jl:375-418): PV buses split the computed
@@ -504,6 +520,17 @@ def runpf_inplace(ps: PowerSystem, **kw) -> None:
     generator output is the computed injection minus the stored load terms,
     exactly as the reference computes it."""
     vm, va, P, Q = runpf(ps, **kw)
+    apply_pf_solution(ps, vm, va, P, Q)
+
+
+def apply_pf_solution(ps: PowerSystem, vm, va, P=None, Q=None) -> None:
+    """The write-back half of runpf_inplace for a solution found elsewhere
+    (the GPU power flow): bus voltages, then the generator outputs from the
+    bus injections (computed from V when P, Q are not given)."""
+    vm = np.asarray(vm, dtype=np.float64)
+    va = np.asarray(va, dtype=np.float64)
+    if P is None or Q is None:
+        P, Q = _pf_injections(ps.ybus.tocsr(), vm, va)
     for i, b in enumerate(ps.buses):
         b.v0m = float(vm[i])
         b.v0a = float(va[i])
