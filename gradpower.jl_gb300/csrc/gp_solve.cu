@@ -108,14 +108,16 @@ struct Chunk {
 // v[i] -= L(i, k) v[k], with L(i, k) = F[i + (k - kbase) * ld].  v[0..mm)
 // is in shared memory; rows below ns are first gathered through the pivot
 // permutation perm (identity after the first chunk).
-template <class T, int J, class Perm, int CH = Chunk<J>::value>
+// LW < 32: the warp works as 32 / LW segments of LW lanes, each segment on
+// its own vector v and front F (same shape), rows i = lane + LW * j.
+template <class T, int J, class Perm, int CH = Chunk<J>::value, int LW = 32>
 __device__ void fwd_cols_j(const T *__restrict__ F, int ld, int kbase, int k0, int k1, int ns, int mm, T *v,
                            Perm perm) {
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & (LW - 1);
     T r[J];
 #pragma unroll
     for (int j = 0; j < J; j++) {
-        const int i = lane + 32 * j;
+        const int i = lane + LW * j;
         r[j] = i < ns ? v[perm(i)] : (i < mm ? v[i] : T(0));
     }
     for (int kc = k0; kc < k1; kc += CH) {
@@ -125,7 +127,7 @@ __device__ void fwd_cols_j(const T *__restrict__ F, int ld, int kbase, int k0, i
             const int k = kc + kk;
 #pragma unroll
             for (int j = 0; j < J; j++) {
-                const int i = lane + 32 * j;
+                const int i = lane + LW * j;
                 c[kk][j] = (k < k1 && i > k && i < mm) ? F[i + (k - kbase) * ld] : T(0);
             }
         }
@@ -133,7 +135,7 @@ __device__ void fwd_cols_j(const T *__restrict__ F, int ld, int kbase, int k0, i
         for (int kk = 0; kk < CH; kk++) {
             const int k = kc + kk;
             if (k < k1) {
-                const T vk = __shfl_sync(FULL, pick(r, k >> 5), k & 31);
+                const T vk = __shfl_sync(FULL, pick(r, k / LW), k % LW, LW);
 #pragma unroll
                 for (int j = 0; j < J; j++) r[j] -= c[kk][j] * vk;
             }
@@ -142,7 +144,7 @@ __device__ void fwd_cols_j(const T *__restrict__ F, int ld, int kbase, int k0, i
     __syncwarp();
 #pragma unroll
     for (int j = 0; j < J; j++) {
-        const int i = lane + 32 * j;
+        const int i = lane + LW * j;
         if (i < mm) v[i] = r[j];
     }
     __syncwarp();
@@ -203,22 +205,22 @@ __device__ void fwd_cols(const T *F, int ld, int kbase, int k0, int k1, int ns, 
 // ---- backward substitution -----------------------------------------------
 // U12 columns c in [c0, c1) (front columns, ns <= c < mm):
 // v[i] -= U(i, c) v[c] for i < ns, U(i, c) = F[i + (c - cbase) * ld].
-template <class T>
+template <class T, int LW = 32>
 __device__ __forceinline__ void bwd_u12(const T *__restrict__ F, int ld, int cbase, int c0, int c1, int ns, T *v) {
-    warp_row_dots<T>(F + (c0 - cbase) * ld, 1, ld, ns, c1 - c0, [&](int a) { return v[c0 + a]; },
-                     [&](int i, T acc) { v[i] -= acc; });
+    warp_row_dots<T, LW>(F + (c0 - cbase) * ld, 1, ld, ns, c1 - c0, [&](int a) { return v[c0 + a]; },
+                         [&](int i, T acc) { v[i] -= acc; });
     __syncwarp();
 }
 
 // U11 columns k from k1 - 1 down to k0: v[k] *= U(k, k) (the stored
 // reciprocal pivot), then v[i] -= U(i, k) v[k] for i < k.
-template <class T, int J, int CH = Chunk<J>::value>
+template <class T, int J, int CH = Chunk<J>::value, int LW = 32>
 __device__ void bwd_cols_j(const T *__restrict__ F, int ld, int kbase, int k0, int k1, int ns, T *v) {
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & (LW - 1);
     T r[J];
 #pragma unroll
     for (int j = 0; j < J; j++) {
-        const int i = lane + 32 * j;
+        const int i = lane + LW * j;
         r[j] = i < ns ? v[i] : T(0);
     }
     for (int kc = k1 - 1; kc >= k0; kc -= CH) {
@@ -229,7 +231,7 @@ __device__ void bwd_cols_j(const T *__restrict__ F, int ld, int kbase, int k0, i
             d[kk] = k >= k0 ? F[k + (k - kbase) * ld] : T(0);
 #pragma unroll
             for (int j = 0; j < J; j++) {
-                const int i = lane + 32 * j;
+                const int i = lane + LW * j;
                 c[kk][j] = (k >= k0 && i < k) ? F[i + (k - kbase) * ld] : T(0);
             }
         }
@@ -237,8 +239,8 @@ __device__ void bwd_cols_j(const T *__restrict__ F, int ld, int kbase, int k0, i
         for (int kk = 0; kk < CH; kk++) {
             const int k = kc - kk;
             if (k >= k0) {
-                const T tk = __shfl_sync(FULL, pick(r, k >> 5), k & 31) * d[kk];
-                if (lane == (k & 31)) place(r, k >> 5, tk);
+                const T tk = __shfl_sync(FULL, pick(r, k / LW), k % LW, LW) * d[kk];
+                if (lane == k % LW) place(r, k / LW, tk);
 #pragma unroll
                 for (int j = 0; j < J; j++) r[j] -= c[kk][j] * tk;
             }
@@ -246,7 +248,7 @@ __device__ void bwd_cols_j(const T *__restrict__ F, int ld, int kbase, int k0, i
     }
 #pragma unroll
     for (int j = 0; j < J; j++) {
-        const int i = lane + 32 * j;
+        const int i = lane + LW * j;
         if (i < ns) v[i] = r[j];
     }
     __syncwarp();
@@ -281,17 +283,26 @@ __device__ void bwd_cols(const T *F, int ld, int kbase, int k0, int k1, int ns, 
 
 // Block fronts (at most kBlkFront rows): the whole front from global memory.
 // (block fronts are small: four columns per chunk)
-template <class T, class Perm>
+template <class T, class Perm, int LW = 32>
 __device__ void fwd_front_blk(const T *F, Perm perm, int ns, int mm, T *v) {
-    if (mm <= 32) fwd_cols_j<T, 1, Perm, 4>(F, mm, 0, 0, ns, ns, mm, v, perm);
-    else fwd_cols_j<T, 2, Perm, 4>(F, mm, 0, 0, ns, ns, mm, v, perm);
+    static_assert(kBlkFront <= 4 * LW, "rows per lane");
+    if (mm <= LW) fwd_cols_j<T, 1, Perm, 4, LW>(F, mm, 0, 0, ns, ns, mm, v, perm);
+    else if (mm <= 2 * LW) fwd_cols_j<T, 2, Perm, 4, LW>(F, mm, 0, 0, ns, ns, mm, v, perm);
+    else if constexpr (LW < 32) {
+        if (mm <= 3 * LW) fwd_cols_j<T, 3, Perm, 2, LW>(F, mm, 0, 0, ns, ns, mm, v, perm);
+        else fwd_cols_j<T, 4, Perm, 2, LW>(F, mm, 0, 0, ns, ns, mm, v, perm);
+    }
 }
 
-template <class T>
+template <class T, int LW = 32>
 __device__ void bwd_front_blk(const T *F, int ns, int mm, T *v) {
-    bwd_u12<T>(F, mm, 0, ns, mm, ns, v);
-    if (ns <= 32) bwd_cols_j<T, 1, 4>(F, mm, 0, 0, ns, ns, v);
-    else bwd_cols_j<T, 2, 4>(F, mm, 0, 0, ns, ns, v);
+    bwd_u12<T, LW>(F, mm, 0, ns, mm, ns, v);
+    if (ns <= LW) bwd_cols_j<T, 1, 4, LW>(F, mm, 0, 0, ns, ns, v);
+    else if (ns <= 2 * LW) bwd_cols_j<T, 2, 4, LW>(F, mm, 0, 0, ns, ns, v);
+    else if constexpr (LW < 32) {
+        if (ns <= 3 * LW) bwd_cols_j<T, 3, 2, LW>(F, mm, 0, 0, ns, ns, v);
+        else bwd_cols_j<T, 4, 2, LW>(F, mm, 0, 0, ns, ns, v);
+    }
 }
 
 // ---- blocks ----------------------------------------------------------------
@@ -360,9 +371,9 @@ __device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefe
 // sweep's column chunks do not each wait on L2.  Forward: columns [0, ns) of
 // every front, one contiguous range; backward: rows [0, ns) of every column.
 // Every address lies inside the front.
-template <class T>
+template <class T, int LW = 32>
 __device__ void prefetch_block(const DevSym &S, const FrontSel &fs, const BlkTask &t, int m, bool fwd) {
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & (LW - 1);
     const T *fr = front_base<T>(fs) + (size_t)(fs.shared ? 0 : m) * S.front_total;
     for (int q = 0; q < t.n; q++) {
         const int4 a = t.E0[q];
@@ -370,10 +381,10 @@ __device__ void prefetch_block(const DevSym &S, const FrontSel &fs, const BlkTas
         const T *f = fr + t.FO[q];
         if (fwd) {
             const uintptr_t l0 = (uintptr_t)f & ~(uintptr_t)127, l1 = (uintptr_t)(f + (size_t)mm * ns - 1);
-            for (uintptr_t ad = l0 + (uintptr_t)lane * 128; ad <= l1; ad += 32 * 128)
+            for (uintptr_t ad = l0 + (uintptr_t)lane * 128; ad <= l1; ad += LW * 128)
                 prefetch_l1(reinterpret_cast<const void *>(ad));
         } else {
-            for (int c = lane; c < mm; c += 32) {
+            for (int c = lane; c < mm; c += LW) {
                 const T *col = f + (size_t)c * mm;
                 prefetch_l1(col);
                 if ((((uintptr_t)col) >> 7) != (((uintptr_t)(col + ns - 1)) >> 7)) prefetch_l1(col + ns - 1);
@@ -382,14 +393,35 @@ __device__ void prefetch_block(const DevSym &S, const FrontSel &fs, const BlkTas
     }
 }
 
-template <class T>
+// Pivot rows of one segment in the interleaved byte table.
+struct PermBytes {
+    const unsigned char *p;
+    __device__ int operator()(int i) const { return p[2 * i]; }
+};
+
+// Two scenarios per warp (LW = 16, segment seg = 0, 1 of the warp): the
+// pivots of both, one byte each (pivot rows are within the supernode's
+// pivot block, fewer than kBlkFront), interleaved in the pivot area.
+__device__ void stage_piv_pair(const DevSym &S, const BlkTask &t, int m0, int m1, unsigned char *pvb) {
+    const int lane = threadIdx.x & 15, seg = (threadIdx.x >> 4) & 1;
+    const int *ip = S.ipiv + (size_t)(seg ? m1 : m0) * S.n;
+    for (int q = 0; q < t.n; q++) {
+        const int4 a = t.E0[q], b = t.E1[q];
+        for (int i = lane; i < a.z; i += 16) pvb[2 * (b.w + i) + seg] = (unsigned char)ip[a.y + i];
+    }
+}
+
+// The forward sweep of one block for scenario m.  LW = 32: the warp on one
+// scenario, pivots in t.pv; LW = 16: each half-warp on its own scenario
+// (same block, so the same control flow), pivots in pvb.
+template <class T, int LW = 32>
 __device__ void fwd_block(const DevProblem &P, const DevWork &W, const DevSym &S, const FrontSel &fs,
-                          const BlkTask &t, int m, T *vs) {
-    const int lane = threadIdx.x & 31;
+                          const BlkTask &t, int m, T *vs, const unsigned char *pvb = nullptr) {
+    const int lane = threadIdx.x & (LW - 1), seg = (threadIdx.x >> 4) & 1;
     const double *x = W.xperm + (size_t)m * P.n_red;
     for (int q = 0; q < t.n; q++) {
         const int4 a = t.E0[q], b = t.E1[q];
-        for (int i = lane; i < a.z + a.w; i += 32) vs[b.y + i] = i < a.z ? (T)x[a.y + i] : T(0);
+        for (int i = lane; i < a.z + a.w; i += LW) vs[b.y + i] = i < a.z ? (T)x[a.y + i] : T(0);
     }
     __syncwarp();
     const T *fr = front_base<T>(fs) + (size_t)(fs.shared ? 0 : m) * S.front_total;
@@ -399,31 +431,36 @@ __device__ void fwd_block(const DevProblem &P, const DevWork &W, const DevSym &S
         const int4 a = t.E0[q], b = t.E1[q];
         const int ns = a.z, r = a.w;
         T *v = vs + b.y;
-        const int *pv = t.pv + b.w;
-        fwd_front_blk<T>(fr + t.FO[q], [&](int i) { return pv[i]; }, ns, ns + r, v);
-        for (int i = lane; i < ns; i += 32) xo[a.y + i] = (double)v[i];
+        if constexpr (LW == 32) {
+            const int *pv = t.pv + b.w;
+            fwd_front_blk<T>(fr + t.FO[q], [&](int i) { return pv[i]; }, ns, ns + r, v);
+        } else {
+            const unsigned char *pb = pvb + 2 * b.w + seg;
+            fwd_front_blk<T, PermBytes, LW>(fr + t.FO[q], PermBytes{pb}, ns, ns + r, v);
+        }
+        for (int i = lane; i < ns; i += LW) xo[a.y + i] = (double)v[i];
         if (q < t.n - 1) {
             const int *pm = t.mp + b.z;
-            for (int i = lane; i < r; i += 32) vs[pm[i]] += v[ns + i];
+            for (int i = lane; i < r; i += LW) vs[pm[i]] += v[ns + i];
         } else {
             double *us = uv + S.uvec_off[a.x];
-            for (int i = lane; i < r; i += 32) us[i] = (double)v[ns + i];
+            for (int i = lane; i < r; i += LW) us[i] = (double)v[ns + i];
         }
         __syncwarp();
     }
 }
 
-template <class T>
+template <class T, int LW = 32>
 __device__ void bwd_block(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B,
                           const FrontSel &fs, const BlkTask &t, int blk, int m, T *vs) {
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & (LW - 1);
     double *x = W.xperm + (size_t)m * P.n_red;
     for (int q = 0; q < t.n; q++) {
         const int4 a = t.E0[q], b = t.E1[q];
-        for (int i = lane; i < a.z; i += 32) vs[b.y + i] = (T)x[a.y + i];
+        for (int i = lane; i < a.z; i += LW) vs[b.y + i] = (T)x[a.y + i];
     }
     const int xb = B.ext_ptr[blk], next = B.ext_ptr[blk + 1] - xb;
-    for (int k = lane; k < next; k += 32) vs[B.ext_pos[xb + k]] = (T)x[B.ext_row[xb + k]];
+    for (int k = lane; k < next; k += LW) vs[B.ext_pos[xb + k]] = (T)x[B.ext_row[xb + k]];
     __syncwarp();
     const T *fr = front_base<T>(fs) + (size_t)(fs.shared ? 0 : m) * S.front_total;
     for (int q = t.n - 1; q >= 0; q--) {
@@ -431,10 +468,10 @@ __device__ void bwd_block(const DevProblem &P, const DevWork &W, const DevSym &S
         const int ns = a.z, r = a.w;
         T *v = vs + b.y;
         const int *gm = t.mp + b.z;
-        for (int c = lane; c < r; c += 32) v[ns + c] = vs[gm[c]];
+        for (int c = lane; c < r; c += LW) v[ns + c] = vs[gm[c]];
         __syncwarp();
-        bwd_front_blk<T>(fr + t.FO[q], ns, ns + r, v);
-        for (int i = lane; i < ns; i += 32) x[a.y + i] = (double)v[i];
+        bwd_front_blk<T, LW>(fr + t.FO[q], ns, ns + r, v);
+        for (int i = lane; i < ns; i += LW) x[a.y + i] = (double)v[i];
     }
 }
 
@@ -602,6 +639,14 @@ __device__ void bwd_top_task(const DevProblem &P, const DevWork &W, const DevSym
 // it by running warps or CTAs, so the kernels cannot deadlock; every wait is
 // bounded.
 
+// Mixed solves pair the scenarios in the block phase (two per warp); a pair
+// runs in the two half-warps when both scenarios are active and on FP32
+// factors (the FP32 vector of each fits half of the area sized for FP64).
+__device__ __forceinline__ bool pair_mode(const FrontSel &fs) { return fs.f32 != nullptr && !fs.shared; }
+__device__ __forceinline__ bool pair_ok(const DevWork &W, const FrontSel &fs, int m) {
+    return W.active[m] && !use64(fs, m);
+}
+
 __device__ __forceinline__ unsigned char *warp_area(unsigned char *smem, const BlkLayout &lay) {
     return smem + (size_t)(threadIdx.x >> 5) * lay.total;
 }
@@ -614,7 +659,11 @@ __global__ void __launch_bounds__(kTopThreads, 8) fwd_solve_kernel(DevProblem P,
     const int M = P.M;
     const int epoch = *D.epoch;
     {
-        const long long n_blk = (long long)B.nblk * M;
+        // mixed solves: a warp task is a block for a pair of scenarios, both
+        // on FP32 factors in the two half-warps when it can (else each
+        // scenario of the pair in turn with the whole warp)
+        const int MP = pair_mode(fs) ? (M + 1) / 2 : M;
+        const long long n_blk = (long long)B.nblk * MP;
         const BlkLayout lay = blk_layout(B);
         unsigned char *base = warp_area(smem, lay);
         for (;;) {
@@ -622,18 +671,40 @@ __global__ void __launch_bounds__(kTopThreads, 8) fwd_solve_kernel(DevProblem P,
             if (lane == 0) t = atomicAdd(D.ctr + 4, 1);
             t = __shfl_sync(FULL, t, 0);
             if (t >= n_blk) break;
-            const int blk = (int)(t / M), m = (int)(t % M);
-            if (!W.active[m]) continue;
-            const bool d = use64(fs, m);
-            if (d && fs.fused64) continue;
-            const BlkTask bt = stage_block(S, B, blk, fs.shared ? 0 : m, base, lay, B.map_fwd, true);
-            __syncwarp();
-            if (d) prefetch_block<double>(S, fs, bt, m, true);
-            else prefetch_block<float>(S, fs, bt, m, true);
-            if (d) fwd_block<double>(P, W, S, fs, bt, m, reinterpret_cast<double *>(base + lay.v));
-            else fwd_block<float>(P, W, S, fs, bt, m, reinterpret_cast<float *>(base + lay.v));
-            __syncwarp();
-            if (lane == 0) signal_done(D.xdone + (size_t)B.ent0[B.blk_ptr[blk + 1] - 1].x * M + m, epoch);
+            const int blk = (int)(t / MP), u = (int)(t % MP);
+            const int root = B.ent0[B.blk_ptr[blk + 1] - 1].x;
+            if (MP != M) {
+                const int m0 = 2 * u, m1 = 2 * u + 1;
+                if (m1 < M && pair_ok(W, fs, m0) && pair_ok(W, fs, m1)) {
+                    const int seg = (threadIdx.x >> 4) & 1, m = seg ? m1 : m0;
+                    const BlkTask bt = stage_block(S, B, blk, 0, base, lay, B.map_fwd, false);
+                    __syncwarp();
+                    unsigned char *pvb = base + lay.piv;
+                    stage_piv_pair(S, bt, m0, m1, pvb);
+                    prefetch_block<float, 16>(S, fs, bt, m, true);
+                    __syncwarp();
+                    fwd_block<float, 16>(P, W, S, fs, bt, m, reinterpret_cast<float *>(base + lay.v) + seg * B.max_v,
+                                         pvb);
+                    __syncwarp();
+                    if ((threadIdx.x & 15) == 0) signal_done(D.xdone + (size_t)root * M + m, epoch);
+                    continue;
+                }
+            }
+            for (int h = 0; h < (MP != M ? 2 : 1); h++) {
+                const int m = MP != M ? 2 * u + h : u;
+                if (m >= M || !W.active[m]) continue;
+                const bool d = use64(fs, m);
+                if (d && fs.fused64) continue;
+                const BlkTask bt = stage_block(S, B, blk, fs.shared ? 0 : m, base, lay, B.map_fwd, true);
+                __syncwarp();
+                if (d) prefetch_block<double>(S, fs, bt, m, true);
+                else prefetch_block<float>(S, fs, bt, m, true);
+                if (d) fwd_block<double>(P, W, S, fs, bt, m, reinterpret_cast<double *>(base + lay.v));
+                else fwd_block<float>(P, W, S, fs, bt, m, reinterpret_cast<float *>(base + lay.v));
+                __syncwarp();
+                if (lane == 0) signal_done(D.xdone + (size_t)root * M + m, epoch);
+                __syncwarp();
+            }
         }
     }
     const int n_tasks = B.n_top * M;
@@ -677,7 +748,8 @@ __global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P,
         __syncthreads();
         if (threadIdx.x == 0) signal_done(D.bdone + (size_t)s * M + m, epoch);
     }
-    const long long n_blk = (long long)B.nblk * M;
+    const int MP = pair_mode(fs) ? (M + 1) / 2 : M;
+    const long long n_blk = (long long)B.nblk * MP;
     const BlkLayout lay = blk_layout(B);
     unsigned char *base = warp_area(smem, lay);
     for (;;) {
@@ -685,22 +757,46 @@ __global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P,
         if (lane == 0) t = atomicAdd(D.ctr + 5, 1);
         t = __shfl_sync(FULL, t, 0);
         if (t >= n_blk) break;
-        const int blk = (int)(t / M), m = (int)(t % M);
-        if (!W.active[m]) continue;
-        const BlkTask bt = stage_block(S, B, blk, fs.shared ? 0 : m, base, lay, B.map_bwd, false);
-        __syncwarp();
-        if (use64(fs, m)) prefetch_block<double>(S, fs, bt, m, false);
-        else prefetch_block<float>(S, fs, bt, m, false);
+        const int blk = (int)(t / MP), u = (int)(t % MP);
         const int par = D.parent[B.ent0[B.blk_ptr[blk + 1] - 1].x];
-        if (par >= 0) {
-            bool ok = true;
-            if (lane == 0) ok = wait_epoch(D.bdone + (size_t)par * M + m, epoch, D.err);
-            ok = __shfl_sync(FULL, ok, 0);
-            if (!ok && lane == 0) atomicOr(W.status + m, 8);
+        if (MP != M) {
+            const int m0 = 2 * u, m1 = 2 * u + 1;
+            if (m1 < M && pair_ok(W, fs, m0) && pair_ok(W, fs, m1)) {
+                const int seg = (threadIdx.x >> 4) & 1, m = seg ? m1 : m0;
+                const BlkTask bt = stage_block(S, B, blk, 0, base, lay, B.map_bwd, false);
+                __syncwarp();
+                prefetch_block<float, 16>(S, fs, bt, m, false);
+                if (par >= 0) {
+                    bool ok = true;
+                    if ((threadIdx.x & 15) == 0) ok = wait_epoch(D.bdone + (size_t)par * M + m, epoch, D.err);
+                    ok = __shfl_sync(FULL, ok, threadIdx.x & 16);
+                    if (!ok && (threadIdx.x & 15) == 0) atomicOr(W.status + m, 8);
+                }
+                __syncwarp();
+                bwd_block<float, 16>(P, W, S, B, fs, bt, blk, m,
+                                     reinterpret_cast<float *>(base + lay.v) + seg * B.max_v);
+                __syncwarp();
+                continue;
+            }
         }
-        __syncwarp();
-        if (use64(fs, m)) bwd_block<double>(P, W, S, B, fs, bt, blk, m, reinterpret_cast<double *>(base + lay.v));
-        else bwd_block<float>(P, W, S, B, fs, bt, blk, m, reinterpret_cast<float *>(base + lay.v));
+        for (int h = 0; h < (MP != M ? 2 : 1); h++) {
+            const int m = MP != M ? 2 * u + h : u;
+            if (m >= M || !W.active[m]) continue;
+            const BlkTask bt = stage_block(S, B, blk, fs.shared ? 0 : m, base, lay, B.map_bwd, false);
+            __syncwarp();
+            if (use64(fs, m)) prefetch_block<double>(S, fs, bt, m, false);
+            else prefetch_block<float>(S, fs, bt, m, false);
+            if (par >= 0) {
+                bool ok = true;
+                if (lane == 0) ok = wait_epoch(D.bdone + (size_t)par * M + m, epoch, D.err);
+                ok = __shfl_sync(FULL, ok, 0);
+                if (!ok && lane == 0) atomicOr(W.status + m, 8);
+            }
+            __syncwarp();
+            if (use64(fs, m)) bwd_block<double>(P, W, S, B, fs, bt, blk, m, reinterpret_cast<double *>(base + lay.v));
+            else bwd_block<float>(P, W, S, B, fs, bt, blk, m, reinterpret_cast<float *>(base + lay.v));
+            __syncwarp();
+        }
     }
 }
 

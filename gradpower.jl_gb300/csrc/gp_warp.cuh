@@ -54,18 +54,20 @@ __device__ __forceinline__ int np2(int n) { return n <= 1 ? 1 : 1 << (32 - __clz
 // (G = 32 / np2(nrow), 1 when nrow >= 32) that split the j range and combine
 // by shuffles in a fixed order, so that short rows still fill the warp.
 // emit(i, acc) runs on the first lane of each group.
-template <class Acc, class T, class V, class E>
+// LW < 32: the warp is LW-lane segments, each on its own data (same nrow
+// and ncol in every segment).
+template <class Acc, int LW = 32, class T, class V, class E>
 __device__ __forceinline__ void warp_row_dots(const T *A, int si, int sj, int nrow, int ncol, V v, E emit) {
-    const int lane = threadIdx.x & 31;
-    const int G = nrow >= 32 ? 1 : 32 / np2(nrow);
-    const int rows_per_pass = 32 / G;
+    const int lane = threadIdx.x & (LW - 1);
+    const int G = nrow >= LW ? 1 : LW / np2(nrow);
+    const int rows_per_pass = LW / G;
     const int g = lane & (G - 1);
     for (int i0 = 0; i0 < nrow; i0 += rows_per_pass) {
         const int i = i0 + lane / G;
         Acc acc = Acc(0);
         if (i < nrow)
             for (int j = g; j < ncol; j += G) acc += (Acc)A[i * si + j * sj] * (Acc)v(j);
-        for (int off = G >> 1; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+        for (int off = G >> 1; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off, LW);
         if (g == 0 && i < nrow) emit(i, acc);
     }
 }
