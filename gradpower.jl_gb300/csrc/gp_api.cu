@@ -1369,6 +1369,7 @@ void ensure_mixed(gp_layout *L) {
     X.lu = A.alloc<float>(M * std::max(1, L->C.n_tasks) * n_lu * 32);
     X.cc = A.alloc<float>(M * std::max(1, L->P.n_cl) * 6);
     X.fronts = A.alloc<float>(M * L->S.front_total);
+    X.kc = A.alloc<double>(M * std::max(1, L->C.n_tasks) * gp::kConstSlots * 32);
     L->zprev = A.alloc<double>(M * L->n_sys);
     L->zprev2 = A.alloc<double>(M * L->n_sys);
     L->zprev3 = A.alloc<double>(M * L->n_sys);
@@ -1745,6 +1746,11 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
     const int M = L->M, ns = opt->n_steps, nsys = L->n_sys;
     set_faults(L, n_faults, faults);
     ensure_graphs(L, opt->newton_tol, opt->itermax, opt->solver);
+    if (L->Mx.on) {
+        // the parameters may have changed since the last integration
+        gp::launch_cluster_const(L->P, L->W, L->C, L->Mx, L->st);
+        L->launches += L->C.n_tasks > 0;
+    }
     ck(cudaMemsetAsync(L->W.status, 0, M * sizeof(int), L->st), "memset");
     // event steps
     std::map<int, int> ev_steps;

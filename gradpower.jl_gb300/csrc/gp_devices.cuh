@@ -22,6 +22,43 @@ namespace gp {
 
 constexpr double kTwoPi60 = 2.0 * 3.14159265358979323846 * 60.0;
 
+// Constants of a device that depend on its parameters only (reciprocals of
+// time constants, reactance ratios, saturation coefficients).  K(slot, f)
+// returns the constant in that slot: ComputeK evaluates f; RecordK
+// evaluates it and stores it (slot-major, stride apart); LoadK reads the
+// stored value and never evaluates f.  Slots: machine 0-15, governor
+// 16-21, exciter 22-25, stabiliser 26-34.
+constexpr int kConstSlots = 36;
+struct ComputeK {
+    static constexpr bool kLoad = false;
+    template <class F>
+    GP_HD double operator()(int, F f) const { return f(); }
+    GP_HD void rec(int, double) const {}
+    GP_HD double at(int) const { return 0.0; }
+};
+struct RecordK {
+    double *k;
+    int stride;
+    static constexpr bool kLoad = false;
+    template <class F>
+    GP_HD double operator()(int i, F f) const {
+        const double v = f();
+        k[i * stride] = v;
+        return v;
+    }
+    GP_HD void rec(int i, double v) const { k[i * stride] = v; }
+    GP_HD double at(int) const { return 0.0; }
+};
+struct LoadK {
+    const double *k;
+    int stride;
+    static constexpr bool kLoad = true;
+    template <class F>
+    GP_HD double operator()(int i, F) const { return k[i * stride]; }
+    GP_HD void rec(int, double) const {}
+    GP_HD double at(int i) const { return k[i * stride]; }
+};
+
 // Pointers of one device row of a struct-of-arrays table.
 struct DevRef {
     int dp, ap, cp, pp, bus, link0, link1;
@@ -40,9 +77,9 @@ GP_HD void sat_coef(double s1, double s2, double &sa, double &sb) {
 
 // GENROU.  C receives the network-row couplings d f_vr/d{delta,i_q,i_d},
 // d f_vi/d{delta,i_q,i_d}; I the injected current (vr, vi rows).
-template <class Sink>
+template <class Sink, class KP = ComputeK>
 GP_HD void genrou_eval(const DevRef &d, int net, const double *z, const double *u0, const double *p, Sink &M,
-                       double *C, double *I) {
+                       double *C, double *I, const KP &kc = KP()) {
     const int dp = d.dp, ap = d.ap, cp = d.cp, pp = d.pp;
     const double x_d = p[pp], x_q = p[pp + 1], x_dp = p[pp + 2], x_qp = p[pp + 3], x_ddp = p[pp + 4],
                  xl = p[pp + 5], H = p[pp + 6], D = p[pp + 7], T_d0p = p[pp + 8], T_q0p = p[pp + 9],
@@ -59,16 +96,27 @@ GP_HD void genrou_eval(const DevRef &d, int net, const double *z, const double *
     // every division by a parameter is taken once, as a reciprocal
     // (FP64 division is dear on this GPU; the equations are unchanged)
     const double dpl = x_dp - xl, qpl = x_qp - xl;
-    const double idpl = 1.0 / dpl, iqpl = 1.0 / qpl;
-    const double iTd = 1.0 / T_d0p, iTq = 1.0 / T_q0p, iTdd = 1.0 / T_d0dp, iTqd = 1.0 / T_q0dp;
-    const double i2H = 0.5 / H, ixd = 1.0 / x_ddp;   // x_qdp = x_ddp
-    const double a_eqp = (x_ddp - xl) * idpl, a_phi1d = (x_dp - x_ddp) * idpl;
-    const double b_edp = -(x_ddp - xl) * iqpl, b_phi2q = (x_qp - x_ddp) * iqpl;
-    const double kd = (x_dp - x_ddp) * idpl * idpl, kq = (x_qp - x_qdp) * iqpl * iqpl;
+    const double idpl = kc(0, [&] { return 1.0 / dpl; }), iqpl = kc(1, [&] { return 1.0 / qpl; });
+    const double iTd = kc(2, [&] { return 1.0 / T_d0p; }), iTq = kc(3, [&] { return 1.0 / T_q0p; });
+    const double iTdd = kc(4, [&] { return 1.0 / T_d0dp; }), iTqd = kc(5, [&] { return 1.0 / T_q0dp; });
+    const double i2H = kc(6, [&] { return 0.5 / H; }), ixd = kc(7, [&] { return 1.0 / x_ddp; });   // x_qdp = x_ddp
+    const double a_eqp = kc(8, [&] { return (x_ddp - xl) * idpl; });
+    const double a_phi1d = kc(9, [&] { return (x_dp - x_ddp) * idpl; });
+    const double b_edp = kc(10, [&] { return -(x_ddp - xl) * iqpl; });
+    const double b_phi2q = kc(11, [&] { return (x_qp - x_ddp) * iqpl; });
+    const double kd = kc(12, [&] { return (x_dp - x_ddp) * idpl * idpl; });
+    const double kq = kc(13, [&] { return (x_qp - x_qdp) * iqpl * iqpl; });
     const double psi_de = a_eqp * e_qp + a_phi1d * phi_1d;
     const double psi_qe = b_edp * e_dp + b_phi2q * phi_2q;
     double sa, sb;
-    sat_coef(S1, S2, sa, sb);
+    if constexpr (KP::kLoad) {
+        sa = kc.at(14);
+        sb = kc.at(15);
+    } else {
+        sat_coef(S1, S2, sa, sb);
+        kc.rec(14, sa);
+        kc.rec(15, sb);
+    }
     const double psi2 = sqrt(psi_de * psi_de + psi_qe * psi_qe);
     const bool sat_on = !(sb == 0.0 || psi2 <= sa || psi2 == 0.0);
     const double ipsi2 = psi2 == 0.0 ? 0.0 : 1.0 / psi2;
@@ -151,14 +199,16 @@ GP_HD void genrou_eval(const DevRef &d, int net, const double *z, const double *
     I[1] = -cd * i_d + sd * i_q;
 }
 
-template <class Sink>
-GP_HD void ieesgo_eval(const DevRef &d, const double *z, const double *p, Sink &M) {
+template <class Sink, class KP = ComputeK>
+GP_HD void ieesgo_eval(const DevRef &d, const double *z, const double *p, Sink &M, const KP &kc = KP()) {
     const int dp = d.dp, ap = d.ap, pp = d.pp, wi = d.link0;
     const double T1 = p[pp], T2 = p[pp + 1], T3 = p[pp + 2], T4 = p[pp + 3], T5 = p[pp + 4], T6 = p[pp + 5];
     const double K1 = p[pp + 6], K2 = p[pp + 7], K3 = p[pp + 8], pref = p[pp + 11];
     const double PF0 = z[dp], PLL = z[dp + 1], TP1 = z[dp + 2], TP2 = z[dp + 3], TP3 = z[dp + 4], p_m = z[ap];
     const double w = wi < 0 ? 0.0 : z[wi];
-    const double i1 = 1.0 / T1, i3 = 1.0 / T3, i4 = 1.0 / T4, i5 = 1.0 / T5, i6 = 1.0 / T6, r23 = T2 * i3;
+    const double i1 = kc(16, [&] { return 1.0 / T1; }), i3 = kc(17, [&] { return 1.0 / T3; });
+    const double i4 = kc(18, [&] { return 1.0 / T4; }), i5 = kc(19, [&] { return 1.0 / T5; });
+    const double i6 = kc(20, [&] { return 1.0 / T6; }), r23 = kc(21, [&] { return T2 * i3; });
     M.putf(dp, i1 * (K1 * w - PF0));
     M.putf(dp + 1, i3 * ((1.0 - r23) * PF0 - PLL));
     const double SatP = pref - r23 * PF0 - PLL;
@@ -183,13 +233,14 @@ GP_HD void ieesgo_eval(const DevRef &d, const double *z, const double *p, Sink &
     M.put(ap, ap, -1.0);
 }
 
-template <class Sink>
-GP_HD void tgov1_eval(const DevRef &d, const double *z, const double *p, Sink &M) {
+template <class Sink, class KP = ComputeK>
+GP_HD void tgov1_eval(const DevRef &d, const double *z, const double *p, Sink &M, const KP &kc = KP()) {
     const int dp = d.dp, ap = d.ap, pp = d.pp, wi = d.link0;
     const double R = p[pp], T1 = p[pp + 1], T2 = p[pp + 4], T3 = p[pp + 5], DT = p[pp + 6], pref = p[pp + 7];
     const double x1 = z[dp], x2 = z[dp + 1], p_m = z[ap];
     const double w = wi < 0 ? 0.0 : z[wi];
-    const double i1 = 1.0 / T1, i3 = 1.0 / T3, iR = 1.0 / R, r23 = T2 * i3;
+    const double i1 = kc(16, [&] { return 1.0 / T1; }), i3 = kc(17, [&] { return 1.0 / T3; });
+    const double iR = kc(18, [&] { return 1.0 / R; }), r23 = kc(19, [&] { return T2 * i3; });
     M.putf(dp, (-x1 + (1.0 - r23) * x2) * i3);
     M.putf(dp + 1, ((pref - w) * iR - x2) * i1);
     M.putf(ap, x1 + r23 * x2 - DT * w - p_m);
@@ -203,8 +254,8 @@ GP_HD void tgov1_eval(const DevRef &d, const double *z, const double *p, Sink &M
     M.put(ap, ap, -1.0);
 }
 
-template <class Sink>
-GP_HD void sexs_eval(const DevRef &d, int net, const double *z, const double *p, Sink &M) {
+template <class Sink, class KP = ComputeK>
+GP_HD void sexs_eval(const DevRef &d, int net, const double *z, const double *p, Sink &M, const KP &kc = KP()) {
     const int dp = d.dp, pp = d.pp, vsi = d.link0;
     const int vr_idx = net + 2 * d.bus;
     const double TA_TB = p[pp], TB = p[pp + 1], K = p[pp + 2], TE = p[pp + 3], vref = p[pp + 6];
@@ -213,7 +264,7 @@ GP_HD void sexs_eval(const DevRef &d, int net, const double *z, const double *p,
     vm = vm == 0.0 ? 1e-12 : vm;
     const double vs = vsi >= 0 ? z[vsi] : 0.0;
     const double err = vref - vm + vs;
-    const double iTB = 1.0 / TB, iTE = 1.0 / TE;
+    const double iTB = kc(22, [&] { return 1.0 / TB; }), iTE = kc(23, [&] { return 1.0 / TE; });
     M.putf(dp, (-x1 + (1.0 - TA_TB) * err) * iTB);
     M.putf(dp + 1, (-e_fd + K * (x1 + TA_TB * err)) * iTE);
     const double ivm = 1.0 / vm, dvr = vr * ivm, dvi = vi * ivm;
@@ -228,8 +279,8 @@ GP_HD void sexs_eval(const DevRef &d, int net, const double *z, const double *p,
     if (vsi >= 0) M.put(dp + 1, vsi, K * TA_TB * iTE);
 }
 
-template <class Sink>
-GP_HD void esdc1a_eval(const DevRef &d, int net, const double *z, const double *p, Sink &M) {
+template <class Sink, class KP = ComputeK>
+GP_HD void esdc1a_eval(const DevRef &d, int net, const double *z, const double *p, Sink &M, const KP &kc = KP()) {
     const int dp = d.dp, pp = d.pp, vsi = d.link0;
     const int vr_idx = net + 2 * d.bus;
     const double Ka = p[pp], Ta = p[pp + 1], Kf = p[pp + 2], Tf = p[pp + 3], Ke = p[pp + 4], Te = p[pp + 5];
@@ -240,7 +291,8 @@ GP_HD void esdc1a_eval(const DevRef &d, int net, const double *z, const double *
     const double vs = vsi >= 0 ? z[vsi] : 0.0;
     const bool son = !(sat_b == 0.0 || e_fd <= sat_a);
     const double sat = son ? sat_b * (e_fd - sat_a) * (e_fd - sat_a) : 0.0;
-    const double iTa = 1.0 / Ta, iTf = 1.0 / Tf, iTe = 1.0 / Te, kft = Kf * iTf;
+    const double iTa = kc(22, [&] { return 1.0 / Ta; }), iTf = kc(23, [&] { return 1.0 / Tf; });
+    const double iTe = kc(24, [&] { return 1.0 / Te; }), kft = kc(25, [&] { return Kf * iTf; });
     M.putf(dp, (Ka * (vref - vm + vs - vr2 - kft * e_fd) - vr1) * iTa);
     M.putf(dp + 1, -(kft * e_fd + vr2) * iTf);
     M.putf(dp + 2, (vr1 - Ke * e_fd - sat) * iTe);
@@ -258,8 +310,8 @@ GP_HD void esdc1a_eval(const DevRef &d, int net, const double *z, const double *
     M.put(dp + 2, dp + 2, -(Ke + dsat) * iTe);
 }
 
-template <class Sink>
-GP_HD void ieeest_eval(const DevRef &d, const double *z, const double *p, Sink &M) {
+template <class Sink, class KP = ComputeK>
+GP_HD void ieeest_eval(const DevRef &d, const double *z, const double *p, Sink &M, const KP &kc = KP()) {
     const int dp = d.dp, ap = d.ap, pp = d.pp, wi = d.link0;
     const double A1 = p[pp], A2 = p[pp + 1], A3 = p[pp + 2], A4 = p[pp + 3], A5 = p[pp + 4], A6 = p[pp + 5];
     const double T1 = p[pp + 6], T2 = p[pp + 7], T3 = p[pp + 8], T4 = p[pp + 9], T5 = p[pp + 10], T6 = p[pp + 11],
@@ -267,8 +319,11 @@ GP_HD void ieeest_eval(const DevRef &d, const double *z, const double *p, Sink &
     const double s0 = z[dp], s1 = z[dp + 1], s2 = z[dp + 2], s3 = z[dp + 3], s4 = z[dp + 4], s5 = z[dp + 5],
                  s6 = z[dp + 6], vs = z[ap];
     const double sig = wi >= 0 ? z[wi] : 0.0;
-    const double iA2 = 1.0 / A2, iA4 = 1.0 / A4, iT2 = 1.0 / T2, iT4 = 1.0 / T4, iT6 = 1.0 / T6;
-    const double rA = A6 * iA4, r12 = T1 * iT2, r34 = T3 * iT4, r56 = T5 * iT6;
+    const double iA2 = kc(26, [&] { return 1.0 / A2; }), iA4 = kc(27, [&] { return 1.0 / A4; });
+    const double iT2 = kc(28, [&] { return 1.0 / T2; }), iT4 = kc(29, [&] { return 1.0 / T4; });
+    const double iT6 = kc(30, [&] { return 1.0 / T6; }), rA = kc(31, [&] { return A6 * iA4; });
+    const double r12 = kc(32, [&] { return T1 * iT2; }), r34 = kc(33, [&] { return T3 * iT4; });
+    const double r56 = kc(34, [&] { return T5 * iT6; });
     const double q = s1 - s3 - A3 * s2;
     const double y2 = s3 + A5 * s2 + rA * q;
     const double y3 = s4 + r12 * (y2 - s4);

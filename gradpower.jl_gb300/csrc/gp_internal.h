@@ -138,6 +138,7 @@ struct DevMixed {
     float *lu;             // [M][n_tasks][n_lu][32] cluster LU values and pivot reciprocals
     float *cc;             // [M][n_cl][6] coupling rows of the network equations
     float *fronts;         // [M][front_total] reduced-system factors
+    double *kc;            // [M][n_tasks][kConstSlots][32] parameter constants of the cluster devices
 };
 
 // Dataflow schedule of the multifrontal factorisation and solves
@@ -227,6 +228,9 @@ void launch_solve_bwd(const DevProblem &P, const DevWork &W, const DevSym &S, co
 int solve_block_front_limit();
 
 // launches (gp_kernels.cu)
+// Parameter constants of the cluster devices for cluster_keep_kernel.
+void launch_cluster_const(const DevProblem &P, const DevWork &W, const DevClu &C, const DevMixed &Mx,
+                          cudaStream_t st);
 int launch_cluster(const DevProblem &P, const DevWork &W, const DevClu &C, const DevMixed &Mx, int want_f,
                     cudaStream_t st);
 // skip_s: the entries of S are not needed (shared-factor Woodbury path)

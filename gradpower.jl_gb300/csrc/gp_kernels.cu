@@ -74,17 +74,39 @@ __device__ __forceinline__ DevRef devref(const DTab &T, int k) {
     return d;
 }
 
-template <class Sink>
+template <class Sink, class KP = ComputeK>
 __device__ __forceinline__ void eval_cluster(const DevProblem &P, int c, const double *z, const double *u0,
-                                             const double *p, Sink &sink, double Cc[6], double Ic[2]) {
-    genrou_eval(devref(P.dev[0], P.cl_gen[c]), P.net, z, u0, p, sink, Cc, Ic);
+                                             const double *p, Sink &sink, double Cc[6], double Ic[2],
+                                             const KP &kc = KP()) {
+    genrou_eval(devref(P.dev[0], P.cl_gen[c]), P.net, z, u0, p, sink, Cc, Ic, kc);
     const int gt = P.cl_gov_type[c];
-    if (gt == 1) ieesgo_eval(devref(P.dev[1], P.cl_gov[c]), z, p, sink);
-    else if (gt == 2) tgov1_eval(devref(P.dev[2], P.cl_gov[c]), z, p, sink);
+    if (gt == 1) ieesgo_eval(devref(P.dev[1], P.cl_gov[c]), z, p, sink, kc);
+    else if (gt == 2) tgov1_eval(devref(P.dev[2], P.cl_gov[c]), z, p, sink, kc);
     const int et = P.cl_exc_type[c];
-    if (et == 3) sexs_eval(devref(P.dev[3], P.cl_exc[c]), P.net, z, p, sink);
-    else if (et == 4) esdc1a_eval(devref(P.dev[4], P.cl_exc[c]), P.net, z, p, sink);
-    if (P.cl_pss[c] >= 0) ieeest_eval(devref(P.dev[5], P.cl_pss[c]), z, p, sink);
+    if (et == 3) sexs_eval(devref(P.dev[3], P.cl_exc[c]), P.net, z, p, sink, kc);
+    else if (et == 4) esdc1a_eval(devref(P.dev[4], P.cl_exc[c]), P.net, z, p, sink, kc);
+    if (P.cl_pss[c] >= 0) ieeest_eval(devref(P.dev[5], P.cl_pss[c]), z, p, sink, kc);
+}
+
+// Sink that drops every entry (the evaluation of the parameter constants).
+struct NullSink {
+    __device__ __forceinline__ void put(int, int, double) {}
+    __device__ __forceinline__ void putv(int, int, double) {}
+    __device__ __forceinline__ void putf(int, double) {}
+};
+
+// Parameter constants of every cluster's devices for every scenario, stored
+// for cluster_keep_kernel (they depend on the parameters alone; run once per
+// integration, after the parameters are set).
+__global__ void __launch_bounds__(32) cluster_const_kernel(DevProblem P, DevWork W, DevClu Cl, DevMixed Mx) {
+    const int task = blockIdx.x, m = blockIdx.y, lane = threadIdx.x;
+    if (lane >= Cl.task_count[task]) return;
+    const int c = Cl.order[Cl.task_first[task] + lane];
+    const double *z = W.z + (size_t)m * P.n_sys;
+    double Cc[6], Ic[2];
+    NullSink sink;
+    RecordK rk{Mx.kc + (((size_t)m * Cl.n_tasks + task) * kConstSlots) * 32 + lane, 32};
+    eval_cluster(P, c, z, W.u0 + (size_t)m * P.n_ctrl, W.p + (size_t)m * P.n_par, sink, Cc, Ic, rk);
 }
 
 // The factorisation part of a class program and the solves of the three
@@ -305,7 +327,8 @@ __global__ void __launch_bounds__(32, 16) cluster_keep_kernel(DevProblem P, DevW
     double Cc[6] = {0, 0, 0, 0, 0, 0}, Ic[2] = {0, 0};
     if (act) {
         KeepSink sink{R2, Cl.slot_of + (size_t)cls * 1024, ws, lane, base};
-        eval_cluster(P, c, z, W.u0 + (size_t)m * P.n_ctrl, W.p + (size_t)m * P.n_par, sink, Cc, Ic);
+        LoadK lk{Mx.kc + (((size_t)m * Cl.n_tasks + task) * kConstSlots) * 32 + lane, 32};
+        eval_cluster(P, c, z, W.u0 + (size_t)m * P.n_ctrl, W.p + (size_t)m * P.n_par, sink, Cc, Ic, lk);
     }
     const double dt = *W.dt;
     const CluOp *ops = Cl.ops;
@@ -378,6 +401,12 @@ int launch_cluster(const DevProblem &P, const DevWork &W, const DevClu &C, const
     cluster_keep_kernel<<<grid, 32, (size_t)C.max_w * 32 * (sizeof(double) + sizeof(float)), st>>>(P, W, C, Mx,
                                                                                                   want_f);
     return 2;
+}
+
+void launch_cluster_const(const DevProblem &P, const DevWork &W, const DevClu &C, const DevMixed &Mx,
+                          cudaStream_t st) {
+    if (C.n_tasks == 0) return;
+    cluster_const_kernel<<<dim3(C.n_tasks, P.M), 32, 0, st>>>(P, W, C, Mx);
 }
 
 int cluster_smem_optin(int bytes) {
