@@ -44,6 +44,11 @@ struct DevProblem {
     const int *tr_from, *tr_to;
     const double *tr_y;    // [n_tr][8]: yff, yft, ytf, ytt (re, im)
     const uint8_t *tr_on;  // current status (tripped)
+    // device disconnections (gp_set_device_disconnects): 1 = offline; null
+    // when none are set
+    const uint8_t *zl_off;   // [M][n ZIP loads]
+    const uint8_t *sg_off;   // [M][n static generators]
+    const uint8_t *exc_off;  // [M][n_cl] the exciter of cluster c
     // symbolic permutation of the reduced system
     const int *iperm;      // reduced index -> permuted position
 };
@@ -228,6 +233,10 @@ void launch_solve_bwd(const DevProblem &P, const DevWork &W, const DevSym &S, co
 int solve_block_front_limit();
 
 // launches (gp_kernels.cu)
+// Device disconnections taking effect at `step`: flags[idx[e]] = 1 and the
+// scenario marked active for the dt = 0 re-solve.
+void launch_disconnects(const int *on_step, const int *scen, const int *idx, uint8_t *flags, uint8_t *active,
+                        int n, int step, cudaStream_t st);
 // Parameter constants of the cluster devices for cluster_keep_kernel.
 void launch_cluster_const(const DevProblem &P, const DevWork &W, const DevClu &C, const DevMixed &Mx,
                           cudaStream_t st);

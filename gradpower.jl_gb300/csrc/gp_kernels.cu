@@ -77,12 +77,12 @@ __device__ __forceinline__ DevRef devref(const DTab &T, int k) {
 template <class Sink, class KP = ComputeK>
 __device__ __forceinline__ void eval_cluster(const DevProblem &P, int c, const double *z, const double *u0,
                                              const double *p, Sink &sink, double Cc[6], double Ic[2],
-                                             const KP &kc = KP()) {
+                                             const KP &kc = KP(), bool exc_on = true) {
     genrou_eval(devref(P.dev[0], P.cl_gen[c]), P.net, z, u0, p, sink, Cc, Ic, kc);
     const int gt = P.cl_gov_type[c];
     if (gt == 1) ieesgo_eval(devref(P.dev[1], P.cl_gov[c]), z, p, sink, kc);
     else if (gt == 2) tgov1_eval(devref(P.dev[2], P.cl_gov[c]), z, p, sink, kc);
-    const int et = P.cl_exc_type[c];
+    const int et = exc_on ? P.cl_exc_type[c] : -1;   // an offline exciter's states hold
     if (et == 3) sexs_eval(devref(P.dev[3], P.cl_exc[c]), P.net, z, p, sink, kc);
     else if (et == 4) esdc1a_eval(devref(P.dev[4], P.cl_exc[c]), P.net, z, p, sink, kc);
     if (P.cl_pss[c] >= 0) ieeest_eval(devref(P.dev[5], P.cl_pss[c]), z, p, sink, kc);
@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(32) cluster_kernel(DevProblem P, DevWork W, De
     const int q0 = Cl.prog_ptr[cls], qm = Cl.prog_mid[cls], q1 = Cl.prog_ptr[cls + 1];
     if (act) {
         LaneSink sink{vals, Cl.slot_of + (size_t)cls * 1024, ws, lane};
-        eval_cluster(P, c, z, u0, p, sink, Cc, Ic);
+        eval_cluster(P, c, z, u0, p, sink, Cc, Ic, ComputeK(), !P.exc_off || !P.exc_off[(size_t)m * P.n_cl + c]);
     } else {
         // idle lanes factor an identity so that no lane divides by zero
         for (int q = qm; q < q1; q++)
@@ -328,7 +328,8 @@ __global__ void __launch_bounds__(32, 16) cluster_keep_kernel(DevProblem P, DevW
     if (act) {
         KeepSink sink{R2, Cl.slot_of + (size_t)cls * 1024, ws, lane, base};
         LoadK lk{Mx.kc + (((size_t)m * Cl.n_tasks + task) * kConstSlots) * 32 + lane, 32};
-        eval_cluster(P, c, z, W.u0 + (size_t)m * P.n_ctrl, W.p + (size_t)m * P.n_par, sink, Cc, Ic, lk);
+        eval_cluster(P, c, z, W.u0 + (size_t)m * P.n_ctrl, W.p + (size_t)m * P.n_par, sink, Cc, Ic, lk,
+                     !P.exc_off || !P.exc_off[(size_t)m * P.n_cl + c]);
     }
     const double dt = *W.dt;
     const CluOp *ops = Cl.ops;
@@ -457,6 +458,7 @@ __global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, D
         const DTab &ZL = P.dev[6];
         for (int q = P.bus_zl_ptr[b]; q < P.bus_zl_ptr[b + 1]; q++) {
             const int k = P.bus_zl[q];
+            if (P.zl_off && P.zl_off[(size_t)m * ZL.n + k]) continue;
             const int pp = ZL.par_ptr[k];
             const double pl = p[pp], ql = p[pp + 1], al = p[pp + 2], yre0 = p[pp + 7], yim0 = p[pp + 8];
             const double vm2 = vr * vr + vi * vi, vm2_tld = 0.2;
@@ -492,6 +494,7 @@ __global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, D
         const DTab &SG = P.dev[7];
         for (int q = P.bus_sg_ptr[b]; q < P.bus_sg_ptr[b + 1]; q++) {
             const int k = P.bus_sg[q];
+            if (P.sg_off && P.sg_off[(size_t)m * SG.n + k]) continue;   // constant-power ones only
             const int pp = SG.par_ptr[k], ap = SG.alg_ptr[k], bt = SG.link0[k];
             const double vm2r = vr * vr + vi * vi, vm2 = vm2r > 0.2 ? vm2r : 0.2;
             double Pg, Qg;
@@ -957,6 +960,20 @@ void launch_events(const DevProblem &P, const DevWork &W, const int *fl_on_step,
     (void)P;
     if (n_fl == 0) return;
     events_kernel<<<(n_fl + 255) / 256, 256, 0, st>>>(fl_on_step, fl_off_step, fl_scen, fl_on, W.active, n_fl, step);
+}
+
+__global__ void disconnect_kernel(const int *on_step, const int *scen, const int *idx, uint8_t *flags,
+                                  uint8_t *active, int n, int step) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n || on_step[e] != step) return;
+    flags[idx[e]] = 1;
+    active[scen[e]] = 1;
+}
+
+void launch_disconnects(const int *on_step, const int *scen, const int *idx, uint8_t *flags, uint8_t *active,
+                        int n, int step, cudaStream_t st) {
+    if (n == 0) return;
+    disconnect_kernel<<<(n + 255) / 256, 256, 0, st>>>(on_step, scen, idx, flags, active, n, step);
 }
 
 }  // namespace gp

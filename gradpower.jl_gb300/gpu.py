@@ -56,12 +56,13 @@ def library():
         L.gp_set_mixed_policy.argtypes = [vp, C.c_int32, C.c_double, C.c_int32, C.c_int32]
         L.gp_set_profiling.argtypes = [vp, C.c_int32]
         L.gp_set_line_trips.argtypes = [vp, C.c_int32, vp]
+        L.gp_set_device_disconnects.argtypes = [vp, C.c_int32, vp]
         L.gp_adjoint.argtypes = [vp, vp, C.c_int32, vp, vp, C.c_int32, vp, vp, vp, vp]
         for f in ("gp_layout_create", "gp_layout_destroy", "gp_layout_stats", "gp_set_state",
                   "gp_get_state", "gp_integrate", "gp_residual", "gp_last_timing",
                   "gp_restore_initial_state", "gp_reduced_selftest", "gp_cluster_selftest",
                   "gp_residual_static", "gp_set_mixed_policy", "gp_set_profiling", "gp_set_line_trips",
-                  "gp_adjoint"):
+                  "gp_set_device_disconnects", "gp_adjoint"):
             getattr(L, f).restype = C.c_int32
         _lib = L
     return _lib
@@ -104,6 +105,7 @@ class GpuBatchedLayout:
         _check(library().gp_layout_create(C.addressof(P), self.M, _p(z), _p(u), _p(pp), C.byref(h)))
         self._h = h
         self._trips_set = False
+        self._disconnects_set = False
 
     def close(self):
         if getattr(self, "_h", None):
@@ -174,12 +176,17 @@ class GpuBatchedLayout:
                   scenario_faults: Optional[Sequence[Sequence[Mdl.ContingencyEvent]]] = None,
                   want_traj: bool = True, solver: int = LY.SOLVER_SCHUR_FP64,
                   traj_out: Optional[np.ndarray] = None, trip_events: Sequence[Mdl.TripLineEvent] = (),
-                  scenario_trips: Optional[Sequence[Sequence[Mdl.TripLineEvent]]] = None):
+                  scenario_trips: Optional[Sequence[Sequence[Mdl.TripLineEvent]]] = None,
+                  disconnect_events: Sequence[Mdl.DisconnectDeviceEvent] = (),
+                  scenario_disconnects: Optional[Sequence[Sequence[Mdl.DisconnectDeviceEvent]]] = None):
         """Integrate every scenario from the current state.  `traj_out`, if
         given, is a C-contiguous float64 array [M, n_steps+1, n_sys] (for
         example a pinned buffer) that receives the trajectories.
         `trip_events` (every scenario, the reference's ps.dynamic.trip_events)
-        and `scenario_trips` (per scenario) trip lines (gp_set_line_trips)."""
+        and `scenario_trips` (per scenario) trip lines (gp_set_line_trips);
+        `disconnect_events` (every scenario, ps.dynamic.disconnect_events) and
+        `scenario_disconnects` take devices offline
+        (gp_set_device_disconnects)."""
         nsteps = LY.jl_round(tf / dt)
         per = scenario_faults if scenario_faults is not None else [[] for _ in range(self.M)]
         fa, nf = LY.fault_array(per, dt, events)
@@ -187,6 +194,10 @@ class GpuBatchedLayout:
             ta, nt = LY.trip_array(scenario_trips, dt, trip_events)
             _check(library().gp_set_line_trips(self._h, nt, C.addressof(ta)))
             self._trips_set = nt > 0
+        if disconnect_events or scenario_disconnects or self._disconnects_set:
+            da, nd = LY.disconnect_array(self.arrays, scenario_disconnects, dt, disconnect_events)
+            _check(library().gp_set_device_disconnects(self._h, nd, C.addressof(da)))
+            self._disconnects_set = nd > 0
         opt = LY.GpOptions(dt, nsteps, newton_tol, itermax, solver)
         if traj_out is not None:
             if (traj_out.shape != (self.M, nsteps + 1, self.n_sys) or traj_out.dtype != np.float64

@@ -84,6 +84,30 @@ def trip_array(trips_per_scenario, dt: float, global_trips=()):
     return arr, len(rows)
 
 
+class GpDeviceDisconnect(C.Structure):
+    _fields_ = [("scenario", C.c_int32), ("type", C.c_int32), ("index", C.c_int32), ("on_step", C.c_int32)]
+
+
+def disconnect_array(PA: "ProblemArrays", per_scenario, dt: float, global_events=()):
+    """The gp_device_disconnect array: one entry per (scenario, event), plus
+    scenario = -1 entries for events of every scenario; a device is named by
+    its table and row (the device's rank among the devices of its type, as
+    _set_device_offline! finds it, src/GradPower.jl:684-697); steps as the
+    reference schedules them (Int(round(ton/dt)))."""
+    rows = [(-1, e) for e in global_events]
+    for m, es in enumerate(per_scenario or ()):
+        rows.extend((m, e) for e in es)
+    arr = (GpDeviceDisconnect * max(1, len(rows)))()
+    for k, (m, e) in enumerate(rows):
+        t = next((t for t, T in enumerate(PA.tables) if e.device_idx in set(T.device_index.tolist())), None)
+        if t is None:
+            raise ValueError("no device %d" % e.device_idx)
+        a = arr[k]
+        a.scenario, a.type, a.index = m, t, PA.table_pos[e.device_idx]
+        a.on_step = jl_round(e.ton / dt)
+    return arr, len(rows)
+
+
 class GpObjective(C.Structure):
     """gp_objective: J = sum_t dt * (w_speed * sum_gen w^2
     + w_volt * sum_bus max(0, v_min - |V|)^2)."""

@@ -112,6 +112,15 @@ class TripLineEvent:
     ytt: complex
 
 
+@dataclass
+class DisconnectDeviceEvent:
+    """Device disconnection (src/GradPower.jl:131-146): the device's online
+    flag is cleared at ton for the rest of the run.  device_idx is the
+    0-based index into PowerSystemDynamics.devices."""
+    device_idx: int
+    ton: float
+
+
 def create_trip_line_event(ps: "PowerSystem", from_bus_ext: int, to_bus_ext: int, ton: float,
                            toff: float = math.inf) -> TripLineEvent:
     """The branch between two buses given by their external (PSS/E) numbers

@@ -150,6 +150,24 @@ typedef struct gp_line_trip {
     int32_t off_step;
 } gp_line_trip;
 
+/* A device disconnection (DisconnectDeviceEvent, src/GradPower.jl:131-146):
+ * at the end of step on_step the device's online flag is cleared
+ * (_set_device_offline!, :672-698) for the rest of the call, followed by the
+ * dt = 0 re-solve (src/dynamics.jl:612-646).  The batch kernels skip an
+ * offline device (`table.online[k] || continue` in src/kernels/*.jl): its
+ * differential states hold (their backward-Euler rows become z - zold) and
+ * it injects nothing into the network.  A device that owns algebraic rows
+ * (GENROU, IEESGO, TGOV1, IEEEST, a PV or slack static generator) would
+ * leave those rows without equations, a singular Jacobian: such events are
+ * refused with GP_E_INVALID.  Every gp_integrate call starts with all
+ * devices online. */
+typedef struct gp_device_disconnect {
+    int32_t scenario;            /* -1: every scenario */
+    int32_t type;                /* GP_SEXS, GP_ESDC1A, GP_ZIPLOAD or GP_STATIC_GEN (PQ) */
+    int32_t index;               /* row in that device table */
+    int32_t on_step;
+} gp_device_disconnect;
+
 /* GP_SOLVER_SCHUR_FP64: exact Newton, the reference's batched schedule: the
  *   cluster blocks and the reduced network matrix are factored in FP64 at
  *   every iteration.
@@ -219,6 +237,14 @@ int32_t gp_restore_initial_state(gp_layout *L);
  * trips are set.  The batched GPU path of the reference has no line trips:
  * this carries integrate!'s to it (per scenario). */
 int32_t gp_set_line_trips(gp_layout *L, int32_t n, const gp_line_trip *trips);
+
+/* Device disconnections for the following gp_integrate calls (replaces the
+ * previous set; n = 0 clears them).  GP_SOLVER_SCHUR_FP64 and
+ * GP_SOLVER_SCHUR_MIXED only, like line trips: GP_SOLVER_SHARED_WOODBURY
+ * and gp_adjoint return GP_E_INVALID while disconnections are set.  The
+ * reference's batched GPU path has none: this carries integrate!'s to it
+ * (per scenario). */
+int32_t gp_set_device_disconnects(gp_layout *L, int32_t n, const gp_device_disconnect *events);
 
 /* Integrate every scenario for opt->n_steps backward-Euler steps from the
  * current state.  Replaces integrate_gpu_schur_cudss! / integrate_gpu_cudss!.

@@ -1437,10 +1437,25 @@ static void ws_free(newton_ws *W) {
 /* integrate! for one scenario (src/dynamics.jl:502-655)               */
 /* ------------------------------------------------------------------ */
 
-static int integrate_one(const gp_problem *P, const double *z0, const double *u0, const double *p, int nf,
-                         const gp_fault *faults, int ntr, const gp_line_trip *trips, double dt, int nsteps,
-                         double tol, int itermax, int solver, const double *z0_s0, const double *u0_s0,
-                         const double *p_s0, double *traj, double *zfinal, int *iters, long long *stats) {
+static int integrate_one(const gp_problem *P0, const double *z0, const double *u0, const double *p, int nf,
+                         const gp_fault *faults, int ntr, const gp_line_trip *trips, int ndc,
+                         const gp_device_disconnect *dcs, double dt, int nsteps, double tol, int itermax, int solver,
+                         const double *z0_s0, const double *u0_s0, const double *p_s0, double *traj, double *zfinal,
+                         int *iters, long long *stats) {
+    /* device disconnections: a private copy of the problem whose online
+     * flags this scenario's events clear, for the rest of the run
+     * (_set_device_offline!, src/GradPower.jl:672-698; every kernel skips an
+     * offline device, src/kernels/*.jl) */
+    gp_problem Pm = *P0;
+    uint8_t *onl[GP_NTYPES] = {0};
+    for (int e = 0; e < ndc; e++) {
+        const int t = dcs[e].type, nt = P0->dev[t].n;
+        if (onl[t]) continue;
+        onl[t] = (uint8_t *)malloc(nt > 0 ? nt : 1);
+        for (int k = 0; k < nt; k++) onl[t][k] = P0->dev[t].online ? P0->dev[t].online[k] : 1;
+        Pm.dev[t].online = onl[t];
+    }
+    const gp_problem *P = &Pm;
     int n = n_sys_of(P);
     sym_t S;
     sym_build(&S, P, z0, u0, p, nf, faults);
@@ -1501,6 +1516,8 @@ static int integrate_one(const gp_problem *P, const double *z0, const double *u0
             if (trips[e].on_step == k) { tr_on[e] = 1; any = 1; }
             if (trips[e].off_step == k) { tr_on[e] = 0; any = 1; }
         }
+        for (int e = 0; e < ndc; e++)
+            if (dcs[e].on_step == k) { onl[dcs[e].type][dcs[e].index] = 0; any = 1; }
         if (any) {
             memcpy(zold, z, sizeof(double) * n);
             it = solver == 3   ? newton_frozen(&W, z, zold, u0, p, &F, 0.0, tol, itermax, &ok, &LP, &LPf)
@@ -1525,6 +1542,7 @@ static int integrate_one(const gp_problem *P, const double *z0, const double *u0
     }
     free(on);
     free(tr_on);
+    for (int t = 0; t < GP_NTYPES; t++) free(onl[t]);
     free(z);
     free(zold);
     ws_free(&W);
@@ -1545,10 +1563,11 @@ static int integrate_one(const gp_problem *P, const double *z0, const double *u0
  * scenario 0 at its initial state, factored once, with each scenario's
  * fault shunt; every scenario has at most one fault bus and rfault).  traj [M][nsteps+1][n_sys] or NULL; zfinal [M][n_sys]
  * or NULL; iters [M][2*nsteps] or NULL; status [M]; stats [M][6] or NULL. */
-int gpo_integrate_trips(const gp_problem *P, int M, const double *z0, const double *u0, const double *p, int nf,
-                        const gp_fault *faults, int ntr_all, const gp_line_trip *trips_all, double dt, int nsteps,
-                        double tol, int itermax, int solver, int nthreads, double *traj, double *zfinal,
-                        int *iters, int *status, long long *stats) {
+int gpo_integrate_events(const gp_problem *P, int M, const double *z0, const double *u0, const double *p, int nf,
+                         const gp_fault *faults, int ntr_all, const gp_line_trip *trips_all, int ndc_all,
+                         const gp_device_disconnect *dcs_all, double dt, int nsteps, double tol, int itermax,
+                         int solver, int nthreads, double *traj, double *zfinal, int *iters, int *status,
+                         long long *stats) {
     int n = n_sys_of(P);
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -1569,17 +1588,33 @@ int gpo_integrate_trips(const gp_problem *P, int M, const double *z0, const doub
         ct = 0;
         for (int e = 0; e < ntr_all; e++)
             if (trips_all[e].scenario < 0 || trips_all[e].scenario == m) tm[ct++] = trips_all[e];
+        int cd = 0;
+        for (int e = 0; e < ndc_all; e++)
+            if (dcs_all[e].scenario < 0 || dcs_all[e].scenario == m) cd++;
+        gp_device_disconnect *dm = (gp_device_disconnect *)malloc(sizeof(gp_device_disconnect) * (cd > 0 ? cd : 1));
+        cd = 0;
+        for (int e = 0; e < ndc_all; e++)
+            if (dcs_all[e].scenario < 0 || dcs_all[e].scenario == m) dm[cd++] = dcs_all[e];
         status[m] = integrate_one(P, z0 + (size_t)m * n, u0 + (size_t)m * P->n_ctrl, p + (size_t)m * P->n_par, cnt,
-                                  fm, ct, tm, dt, nsteps, tol, itermax, solver, z0, u0, p,
+                                  fm, ct, tm, cd, dm, dt, nsteps, tol, itermax, solver, z0, u0, p,
                                   traj ? traj + (size_t)m * (nsteps + 1) * n : NULL,
                                   zfinal ? zfinal + (size_t)m * n : NULL,
                                   iters ? iters + (size_t)m * 2 * nsteps : NULL,
                                   stats ? stats + (size_t)m * 6 : NULL);
         free(fm);
         free(tm);
+        free(dm);
     }
     (void)nthreads;
     return 0;
+}
+
+int gpo_integrate_trips(const gp_problem *P, int M, const double *z0, const double *u0, const double *p, int nf,
+                        const gp_fault *faults, int ntr_all, const gp_line_trip *trips_all, double dt, int nsteps,
+                        double tol, int itermax, int solver, int nthreads, double *traj, double *zfinal,
+                        int *iters, int *status, long long *stats) {
+    return gpo_integrate_events(P, M, z0, u0, p, nf, faults, ntr_all, trips_all, 0, NULL, dt, nsteps, tol, itermax,
+                                solver, nthreads, traj, zfinal, iters, status, stats);
 }
 
 int gpo_integrate(const gp_problem *P, int M, const double *z0, const double *u0, const double *p, int nf,

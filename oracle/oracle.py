@@ -30,6 +30,10 @@ def lib():
         L.gpo_integrate_trips.argtypes = [vp, C.c_int, vp, vp, vp, C.c_int, vp, C.c_int, vp, C.c_double, C.c_int,
                                           C.c_double, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp]
         L.gpo_integrate_trips.restype = C.c_int
+        L.gpo_integrate_events.argtypes = [vp, C.c_int, vp, vp, vp, C.c_int, vp, C.c_int, vp, C.c_int, vp,
+                                           C.c_double, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, vp, vp, vp,
+                                           vp, vp]
+        L.gpo_integrate_events.restype = C.c_int
         L.gpo_residual.argtypes = [vp, vp, vp, vp, vp, C.c_int, vp, vp, C.c_double, vp]
         L.gpo_residual_trips.argtypes = [vp, vp, vp, vp, vp, C.c_int, vp, vp, C.c_double, vp]
         L.gpo_jacobian_dense_trips.argtypes = [vp, vp, vp, vp, C.c_int, vp, vp, C.c_double, vp]
@@ -45,7 +49,7 @@ def _p(a):
 
 
 def integrate(PA, z0, u0, p, faults, n_faults, dt, nsteps, tol=1e-10, itermax=50, solver=0,
-              nthreads=1, want_traj=True, trips=None, n_trips=0):
+              nthreads=1, want_traj=True, trips=None, n_trips=0, disconnects=None, n_disc=0):
     """Run M independent integrate! restatements (one per row of z0).
     Returns dict(traj [M, nsteps+1, n_sys] or None, z [M, n_sys],
     iters [M, 2*nsteps], status [M], stats [M, 6])."""
@@ -60,7 +64,12 @@ def integrate(PA, z0, u0, p, faults, n_faults, dt, nsteps, tol=1e-10, itermax=50
     status = np.zeros(M, dtype=np.int32)
     stats = np.zeros((M, 6), dtype=np.int64)
     P = PA.as_ctypes()
-    if n_trips:
+    if n_disc:
+        lib().gpo_integrate_events(C.addressof(P), M, _p(z0), _p(u0), _p(p), n_faults, C.addressof(faults),
+                                   n_trips, C.addressof(trips) if n_trips else None, n_disc,
+                                   C.addressof(disconnects), dt, nsteps, tol, itermax, solver, nthreads,
+                                   _p(traj), _p(zf), _p(iters), _p(status), _p(stats))
+    elif n_trips:
         lib().gpo_integrate_trips(C.addressof(P), M, _p(z0), _p(u0), _p(p), n_faults, C.addressof(faults),
                                   n_trips, C.addressof(trips), dt, nsteps, tol, itermax, solver, nthreads,
                                   _p(traj), _p(zf), _p(iters), _p(status), _p(stats))
