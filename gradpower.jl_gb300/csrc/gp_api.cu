@@ -98,6 +98,14 @@ struct gp_layout {
     DeviceArena arena;     // lifetime of the layout
     DeviceArena call;      // lifetime of one gp_integrate call
     cudaStream_t st = nullptr;
+    // trajectory snapshots of gp_integrate (kept between calls, grown on
+    // demand) and the stream that copies them to a pinned host buffer while
+    // the following steps run
+    DeviceArena traj_arena;
+    double *d_traj = nullptr;
+    size_t traj_cap = 0;
+    cudaStream_t st_copy = nullptr;
+    cudaEvent_t ev_snap = nullptr;
     int *d_state_maps = nullptr;   // state_bus then red_of
     int *d_gen_w = nullptr;        // z index of every machine's speed deviation
     int n_gen = 0;
@@ -125,6 +133,17 @@ struct gp_layout {
     int *d_tr_on_step = nullptr, *d_tr_off_step = nullptr, *d_tr_scen = nullptr;
     std::vector<int> h_tr_on_step, h_tr_off_step;
     std::vector<int> h_adj_ptr, h_adj;   // bus adjacency (line trips are checked against it)
+    // device disconnections (gp_set_device_disconnects): offline flags of
+    // ZIP loads, static generators and cluster exciters per scenario (zeroed
+    // at every call), and the events as (flag index, scenario, step)
+    DeviceArena dc_arena;
+    int n_dc = 0;
+    size_t dc_bytes = 0;
+    uint8_t *d_dc_flags = nullptr;
+    int *d_dc_on_step = nullptr, *d_dc_scen = nullptr, *d_dc_idx = nullptr;
+    std::vector<int> h_dc_on_step;
+    std::vector<int> h_cl_ext, h_cl_ex, h_sg_type;   // cluster exciters; static generator bus types
+    int h_ntab[GP_NTYPES] = {};
     // shared-factor Woodbury path (allocated on first use): W = P^-1 U per
     // scenario (two columns), H^-1 (2x2), the correction's coefficients, and
     // the mask that selects scenario 0 for the factorisation of P
@@ -940,6 +959,13 @@ void build_problem(gp_layout *L, const gp_problem *pr) {
     P.cl_gov = A.upload(pl.gv);
     P.cl_exc_type = A.upload(pl.ext);
     P.cl_exc = A.upload(pl.ex);
+    L->h_cl_ext = pl.ext;
+    L->h_cl_ex = pl.ex;
+    for (int t = 0; t < GP_NTYPES; t++) L->h_ntab[t] = pr->dev[t].n;
+    {
+        const gp_device_table &SG = pr->dev[GP_STATIC_GEN];
+        L->h_sg_type.assign(SG.link0, SG.link0 + SG.n);
+    }
     P.cl_pss = A.upload(pl.pss);
     P.n_red = pl.n_red;
     P.n_var = pl.n_var;
@@ -1058,6 +1084,8 @@ void build_work(gp_layout *L, const double *z0, const double *u0, const double *
     ck(cudaMemset(L->d_cnt, 0, 8 * sizeof(int)), "memset");
     ck(cudaMallocHost(&L->h_dt, sizeof(double)), "cudaMallocHost");
     ck(cudaStreamCreateWithFlags(&L->st, cudaStreamNonBlocking), "stream");
+    ck(cudaStreamCreateWithFlags(&L->st_copy, cudaStreamNonBlocking), "stream");
+    ck(cudaEventCreateWithFlags(&L->ev_snap, cudaEventDisableTiming), "event");
     for (int i = 0; i < 8; i++) ck(cudaEventCreate(&L->pev[i]), "event");
     // keep the initial state for gp_restore_initial_state
     L->z_init = A.alloc<double>(M * P.n_sys);
@@ -1624,12 +1652,24 @@ int32_t gp_layout_create(const gp_problem *prob, int32_t M, const double *z0, co
     }
     catch (const gp_error &e) {
         g_last_error = e.what();
-        if (L) { L->trip_arena.release(); L->arena.release(); delete L; }
+        if (L) {
+            L->traj_arena.release();
+            L->dc_arena.release();
+            L->trip_arena.release();
+            L->arena.release();
+            delete L;
+        }
         return e.code;
     }
     catch (const std::exception &e) {
         g_last_error = e.what();
-        if (L) { L->trip_arena.release(); L->arena.release(); delete L; }
+        if (L) {
+            L->traj_arena.release();
+            L->dc_arena.release();
+            L->trip_arena.release();
+            L->arena.release();
+            delete L;
+        }
         return GP_E_INVALID;
     }
     return GP_OK;
@@ -1641,6 +1681,9 @@ int32_t gp_layout_destroy(gp_layout *L) {
     drop_graphs(L);
     if (L->st) cudaStreamSynchronize(L->st);
     L->call.release();
+    if (L->st_copy) cudaStreamSynchronize(L->st_copy);
+    L->traj_arena.release();
+    L->dc_arena.release();
     L->trip_arena.release();
     L->arena.release();
     if (L->h_flag) cudaFreeHost(L->h_flag);
@@ -1648,6 +1691,8 @@ int32_t gp_layout_destroy(gp_layout *L) {
     for (int i = 0; i < 8; i++)
         if (L->pev[i]) cudaEventDestroy(L->pev[i]);
     if (L->st) cudaStreamDestroy(L->st);
+    if (L->st_copy) cudaStreamDestroy(L->st_copy);
+    if (L->ev_snap) cudaEventDestroy(L->ev_snap);
     delete L;
     API_END
 }
@@ -1730,6 +1775,8 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
         fail(GP_E_INVALID, "solver %d is not available", opt->solver);
     if (opt->solver == GP_SOLVER_SHARED_WOODBURY && L->n_tr > 0)
         fail(GP_E_INVALID, "the shared-factor Woodbury solver does not take line trips");
+    if (opt->solver == GP_SOLVER_SHARED_WOODBURY && L->n_dc > 0)
+        fail(GP_E_INVALID, "the shared-factor Woodbury solver does not take device disconnections");
     if (opt->solver == GP_SOLVER_SHARED_WOODBURY) {
         // one fault (bus, rfault) per scenario: its rank-2 correction of P
         std::vector<int> fb(L->M, -1);
@@ -1763,15 +1810,47 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
         if (L->h_tr_off_step[e] >= 0) ev_steps[L->h_tr_off_step[e]] = 1;
     }
     if (L->n_tr > 0) ck(cudaMemsetAsync(L->d_tr_on, 0, L->n_tr, L->st), "memset");
+    for (int e = 0; e < L->n_dc; e++) ev_steps[L->h_dc_on_step[e]] = 1;
+    if (L->n_dc > 0) ck(cudaMemsetAsync(L->d_dc_flags, 0, L->dc_bytes, L->st), "memset");
     double *d_traj = nullptr;
     int *d_iters = L->call.alloc<int>((size_t)2 * std::max(ns, 1) * M);
     ck(cudaMemsetAsync(d_iters, 0, (size_t)2 * std::max(ns, 1) * M * sizeof(int), L->st), "memset");
+    // a page-locked host trajectory receives each step's snapshot as soon as
+    // it is taken (copy stream); any other host buffer, all of them at the end
+    bool stream_traj = false;
+    const size_t tpitch = (size_t)(ns + 1) * nsys * sizeof(double);
     if (traj) {
-        d_traj = L->call.alloc<double>((size_t)M * (ns + 1) * nsys);
-        ck(cudaMemcpy2DAsync(d_traj, (size_t)(ns + 1) * nsys * sizeof(double), L->W.z, nsys * sizeof(double),
-                             nsys * sizeof(double), M, cudaMemcpyDeviceToDevice, L->st),
+        const size_t need = (size_t)M * (ns + 1) * nsys;
+        if (need > L->traj_cap) {
+            L->traj_arena.release();
+            L->d_traj = L->traj_arena.alloc<double>(need);
+            L->traj_cap = need;
+        }
+        d_traj = L->d_traj;
+        cudaPointerAttributes pa{};
+        stream_traj = cudaPointerGetAttributes(&pa, traj) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+        cudaGetLastError();
+        ck(cudaMemcpy2DAsync(d_traj, tpitch, L->W.z, nsys * sizeof(double), nsys * sizeof(double), M,
+                             cudaMemcpyDeviceToDevice, L->st),
            "snapshot");
     }
+    auto send_slice = [&](int k) {
+        if (!stream_traj) return;
+        ck(cudaEventRecord(L->ev_snap, L->st), "event");
+        ck(cudaStreamWaitEvent(L->st_copy, L->ev_snap, 0), "event wait");
+        ck(cudaMemcpy2DAsync(traj + (size_t)k * nsys, tpitch, d_traj + (size_t)k * nsys, tpitch,
+                             nsys * sizeof(double), M, cudaMemcpyDeviceToHost, L->st_copy),
+           "trajectory copy");
+    };
+    // the copy stream ends before the call returns, on every path
+    struct CopyJoin {
+        cudaStream_t s;
+        bool on;
+        ~CopyJoin() {
+            if (on) cudaStreamSynchronize(s);
+        }
+    } join{L->st_copy, stream_traj};
+    send_slice(0);
     cudaEvent_t e0, e1;
     ck(cudaEventCreate(&e0), "event");
     ck(cudaEventCreate(&e1), "event");
@@ -1807,16 +1886,20 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
         ck(cudaMemcpyAsync(d_iters + (size_t)(2 * (k - 1)) * M, L->W.iters, M * sizeof(int),
                            cudaMemcpyDeviceToDevice, L->st),
            "iters");
-        if (d_traj)
-            ck(cudaMemcpy2DAsync(d_traj + (size_t)k * nsys, (size_t)(ns + 1) * nsys * sizeof(double), L->W.z,
-                                 nsys * sizeof(double), nsys * sizeof(double), M, cudaMemcpyDeviceToDevice, L->st),
+        if (d_traj) {
+            ck(cudaMemcpy2DAsync(d_traj + (size_t)k * nsys, tpitch, L->W.z, nsys * sizeof(double),
+                                 nsys * sizeof(double), M, cudaMemcpyDeviceToDevice, L->st),
                "snapshot");
+            send_slice(k);
+        }
         if (ev_steps.count(k)) {
             ck(cudaMemsetAsync(L->W.active, 0, M, L->st), "memset");
             gp::launch_events(L->P, L->W, L->d_fl_on_step, L->d_fl_off_step, L->d_fl_scen, L->d_fl_on, L->n_fl, k,
                               L->st);
             gp::launch_events(L->P, L->W, L->d_tr_on_step, L->d_tr_off_step, L->d_tr_scen, L->d_tr_on, L->n_tr, k,
                               L->st);
+            gp::launch_disconnects(L->d_dc_on_step, L->d_dc_scen, L->d_dc_idx, L->d_dc_flags, L->W.active, L->n_dc,
+                                   k, L->st);
             ck(cudaMemcpyAsync(L->W.zold, L->W.z, (size_t)M * nsys * sizeof(double), cudaMemcpyDeviceToDevice,
                                L->st),
                "zold");
@@ -1841,7 +1924,10 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
         ck(cudaMemcpy(&err, L->D.err, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
         if (err) fail(GP_E_TIMEOUT, "a dataflow wait of the reduced-system solve ran out its iteration limit");
     }
-    if (traj)
+    if (stream_traj) {
+        join.on = false;
+        ck(cudaStreamSynchronize(L->st_copy), "trajectory copy");
+    } else if (traj)
         ck(cudaMemcpy(traj, d_traj, (size_t)M * (ns + 1) * nsys * sizeof(double), cudaMemcpyDeviceToHost),
            "trajectory copy");
     std::vector<int> hi((size_t)2 * std::max(ns, 1) * M);
@@ -1986,6 +2072,7 @@ int32_t gp_adjoint(gp_layout *L, const gp_options *opt, int32_t n_faults, const 
         fail(GP_E_INVALID, "bad options");
     if (opt->solver != GP_SOLVER_SCHUR_FP64) fail(GP_E_INVALID, "the adjoint runs on the FP64 Schur path");
     if (L->n_tr > 0) fail(GP_E_INVALID, "the adjoint does not take line trips");
+    if (L->n_dc > 0) fail(GP_E_INVALID, "the adjoint does not take device disconnections");
     const int M = L->M, ns = opt->n_steps, K = checkpoint_every;
     const size_t nsys = L->n_sys, blk = (size_t)M * nsys;
     set_faults(L, n_faults, faults);
@@ -2232,6 +2319,74 @@ int32_t gp_set_line_trips(gp_layout *L, int32_t n, const gp_line_trip *trips) {
         L->S.asmt_val = nullptr;
     }
     drop_graphs(L);   // the graphs hold the problem and structure by value
+    API_END
+}
+
+int32_t gp_set_device_disconnects(gp_layout *L, int32_t n, const gp_device_disconnect *events) {
+    API_BEGIN
+    if (!L || (n > 0 && !events) || n < 0) fail(GP_E_INVALID, "bad arguments");
+    if (n == 0 && L->n_dc == 0) return GP_OK;
+    const int M = L->M, nzl = L->h_ntab[GP_ZIPLOAD], nsg = L->h_ntab[GP_STATIC_GEN], ncl = L->P.n_cl;
+    // flag areas: ZIP loads, static generators, cluster exciters
+    const size_t o_zl = 0, o_sg = o_zl + (size_t)M * nzl, o_cl = o_sg + (size_t)M * nsg;
+    const size_t bytes = o_cl + (size_t)M * ncl;
+    std::vector<int> on, scen, idx;
+    for (int e = 0; e < n; e++) {
+        const gp_device_disconnect &d = events[e];
+        if (d.scenario >= M) fail(GP_E_INVALID, "disconnection %d: scenario %d out of range", e, d.scenario);
+        if (d.type < 0 || d.type >= GP_NTYPES || d.index < 0 || d.index >= L->h_ntab[d.type])
+            fail(GP_E_INVALID, "disconnection %d: no device %d of type %d", e, d.index, d.type);
+        size_t base = 0;
+        int row = d.index, stride = 0;
+        if (d.type == GP_ZIPLOAD) {
+            base = o_zl;
+            stride = nzl;
+        } else if (d.type == GP_STATIC_GEN) {
+            if (L->h_sg_type[d.index] == 2 || L->h_sg_type[d.index] == 3)
+                fail(GP_E_INVALID, "disconnection %d: a PV or slack static generator owns algebraic rows "
+                                   "(offline, its Jacobian is singular)", e);
+            base = o_sg;
+            stride = nsg;
+        } else if (d.type == GP_SEXS || d.type == GP_ESDC1A) {
+            row = -1;
+            for (int c = 0; c < ncl && row < 0; c++)
+                if (L->h_cl_ext[c] == d.type && L->h_cl_ex[c] == d.index) row = c;
+            if (row < 0) fail(GP_E_INVALID, "disconnection %d: exciter %d belongs to no machine cluster", e, d.index);
+            base = o_cl;
+            stride = ncl;
+        } else {
+            fail(GP_E_INVALID, "disconnection %d: device type %d owns algebraic rows (offline, its Jacobian is "
+                               "singular)", e, d.type);
+        }
+        for (int m = 0; m < M; m++) {
+            if (d.scenario >= 0 && d.scenario != m) continue;
+            on.push_back(d.on_step);
+            scen.push_back(m);
+            idx.push_back((int)(base + (size_t)m * stride + row));
+        }
+    }
+    L->dc_arena.release();
+    DeviceArena &A = L->dc_arena;
+    L->n_dc = (int)on.size();
+    L->h_dc_on_step = on;
+    if (L->n_dc > 0) {
+        auto up_i = [&](const std::vector<int> &v) { return A.upload(v); };
+        L->dc_bytes = bytes;
+        L->d_dc_flags = A.alloc<uint8_t>(std::max<size_t>(1, bytes));
+        ck(cudaMemset(L->d_dc_flags, 0, std::max<size_t>(1, bytes)), "memset");
+        L->d_dc_on_step = up_i(on);
+        L->d_dc_scen = up_i(scen);
+        L->d_dc_idx = up_i(idx);
+        L->P.zl_off = L->d_dc_flags + o_zl;
+        L->P.sg_off = L->d_dc_flags + o_sg;
+        L->P.exc_off = L->d_dc_flags + o_cl;
+    } else {
+        L->dc_bytes = 0;
+        L->d_dc_flags = nullptr;
+        L->d_dc_on_step = L->d_dc_scen = L->d_dc_idx = nullptr;
+        L->P.zl_off = L->P.sg_off = L->P.exc_off = nullptr;
+    }
+    drop_graphs(L);   // the graphs hold the problem by value
     API_END
 }
 

@@ -129,3 +129,27 @@ def test_device_loop_matches_host_loop(G, solver):
     for k in ("newton_iters", "linear_solves", "launches", "factor_launches", "refreshes", "exact_iters"):
         assert td[k] == th[k], k
     assert th["solve_ms"] > 0.0 and td["solve_ms"] == 0.0
+
+
+def test_pinned_trajectory_matches_pageable(G):
+    """A page-locked trajectory buffer is filled step by step on the copy
+    stream while the run goes on; it equals the trajectory returned through
+    a pageable buffer (copied at the end), for a longer and then a shorter
+    run on the same layout (the device snapshot buffer is kept and reused)."""
+    torch = pytest.importorskip("torch")
+    c, w = synthetic_case("planar2k", 4)
+    gbl = G.GpuBatchedLayout(c.dp, c.ps, c.M)
+    try:
+        for nsteps in (40, 25):
+            gbl.restore_initial_state()
+            r = gbl.integrate(nsteps * DT, DT, scenario_faults=c.faults, solver=LY.SOLVER_SCHUR_MIXED)
+            buf = torch.empty((c.M, nsteps + 1, gbl.n_sys), dtype=torch.float64, pin_memory=True).numpy()
+            buf[:] = np.nan
+            gbl.restore_initial_state()
+            rp = gbl.integrate(nsteps * DT, DT, scenario_faults=c.faults, solver=LY.SOLVER_SCHUR_MIXED,
+                               traj_out=buf)
+            assert np.all(r["status"] == 0)
+            assert np.array_equal(rp["iters"], r["iters"])
+            assert np.array_equal(buf, r["traj"])
+    finally:
+        gbl.close()
