@@ -17,8 +17,8 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgradpower_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["gp_api.cu", "gp_kernels.cu", "gp_dag.cu", "gp_solve.cu", "gp_adjoint.cu", "gp_symbolic.cpp",
-           "gp_cluster_plan.cpp"]
+SOURCES = ["gp_api.cu", "gp_kernels.cu", "gp_dag.cu", "gp_solve.cu", "gp_adjoint.cu", "gp_init.cu",
+           "gp_symbolic.cpp", "gp_cluster_plan.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 

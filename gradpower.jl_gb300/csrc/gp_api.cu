@@ -227,7 +227,10 @@ void make_plan(const gp_problem *pr, Plan &pl) {
         for (int k = 0; k < T.n; k++) {
             if (T.online && !T.online[k]) fail(GP_E_INVALID, "offline devices are not supported (type %d, row %d)", t, k);
             if (T.bus[k] < 0 || T.bus[k] >= nb) fail(GP_E_INVALID, "type %d row %d: bus out of range", t, k);
-            if (T.par_ptr[k] < 0 || T.par_ptr[k] >= pr->n_par) fail(GP_E_INVALID, "type %d row %d: par_ptr out of range", t, k);
+            // every parameter a kernel reads lies inside the parameter vector
+            static const int par_size[GP_NTYPES] = {14, 12, 8, 7, 10, 19, 9, 4};
+            if (T.par_ptr[k] < 0 || T.par_ptr[k] + par_size[t] > pr->n_par)
+                fail(GP_E_INVALID, "type %d row %d: par_ptr out of range", t, k);
         }
     }
     for (int q = 0; q < pr->y_nnz; q++)
@@ -2319,6 +2322,36 @@ int32_t gp_set_line_trips(gp_layout *L, int32_t n, const gp_line_trip *trips) {
         L->S.asmt_val = nullptr;
     }
     drop_graphs(L);   // the graphs hold the problem and structure by value
+    API_END
+}
+
+int32_t gp_initialize(gp_layout *L, const double *v_polar, const double *gen_pq, const double *sg_pq, double *z0,
+                      double *u0, double *p) {
+    API_BEGIN
+    if (!L || !v_polar || (!gen_pq && L->h_ntab[GP_GENROU] > 0) || (!sg_pq && L->h_ntab[GP_STATIC_GEN] > 0))
+        fail(GP_E_INVALID, "null argument");
+    const size_t M = L->M;
+    DeviceArena A;
+    struct Release {
+        DeviceArena &a;
+        ~Release() { a.release(); }
+    } rel{A};
+    const double *d_v = A.upload(v_polar, M * L->n_bus * 2);
+    const double *d_g = A.upload(gen_pq ? gen_pq : v_polar, gen_pq ? M * L->h_ntab[GP_GENROU] * 2 : 1);
+    const double *d_s = A.upload(sg_pq ? sg_pq : v_polar, sg_pq ? M * L->h_ntab[GP_STATIC_GEN] * 2 : 1);
+    int *d_bad = A.alloc<int>(1);
+    ck(cudaMemsetAsync(d_bad, 0, sizeof(int), L->st), "memset");
+    gp::launch_initialize(L->P, L->W, d_v, d_g, d_s, d_bad, L->st);
+    ck(cudaGetLastError(), "initialise");
+    ck(cudaMemcpyAsync(L->z_init, L->W.z, M * L->n_sys * sizeof(double), cudaMemcpyDeviceToDevice, L->st),
+       "initial state");
+    int bad = 0;
+    ck(cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, L->st), "status copy");
+    ck(cudaStreamSynchronize(L->st), "initialise");
+    if (z0) ck(cudaMemcpy(z0, L->W.z, M * L->n_sys * sizeof(double), cudaMemcpyDeviceToHost), "state copy");
+    if (u0) ck(cudaMemcpy(u0, L->W.u0, M * L->n_ctrl * sizeof(double), cudaMemcpyDeviceToHost), "control copy");
+    if (p) ck(cudaMemcpy(p, L->W.p, M * L->n_par * sizeof(double), cudaMemcpyDeviceToHost), "parameter copy");
+    if (bad) fail(GP_E_NUMERIC, "%d machine initialisation(s) left a residual of 1e-9 or more", bad);
     API_END
 }
 

@@ -233,6 +233,11 @@ void launch_solve_bwd(const DevProblem &P, const DevWork &W, const DevSym &S, co
 int solve_block_front_limit();
 
 // launches (gp_kernels.cu)
+// Device initialisation of every scenario from solved power flows
+// (gp_init.cu): writes W.z, W.u0 and the derived entries of W.p; *bad
+// counts machines whose initialisation residual stayed at or above 1e-9.
+void launch_initialize(const DevProblem &P, const DevWork &W, const double *vpol, const double *gen_pq,
+                       const double *sg_pq, int *bad, cudaStream_t st);
 // Device disconnections taking effect at `step`: flags[idx[e]] = 1 and the
 // scenario marked active for the dt = 0 re-solve.
 void launch_disconnects(const int *on_step, const int *scen, const int *idx, uint8_t *flags, uint8_t *active,

@@ -57,12 +57,13 @@ def library():
         L.gp_set_profiling.argtypes = [vp, C.c_int32]
         L.gp_set_line_trips.argtypes = [vp, C.c_int32, vp]
         L.gp_set_device_disconnects.argtypes = [vp, C.c_int32, vp]
+        L.gp_initialize.argtypes = [vp] * 7
         L.gp_adjoint.argtypes = [vp, vp, C.c_int32, vp, vp, C.c_int32, vp, vp, vp, vp]
         for f in ("gp_layout_create", "gp_layout_destroy", "gp_layout_stats", "gp_set_state",
                   "gp_get_state", "gp_integrate", "gp_residual", "gp_last_timing",
                   "gp_restore_initial_state", "gp_reduced_selftest", "gp_cluster_selftest",
                   "gp_residual_static", "gp_set_mixed_policy", "gp_set_profiling", "gp_set_line_trips",
-                  "gp_set_device_disconnects", "gp_adjoint"):
+                  "gp_set_device_disconnects", "gp_initialize", "gp_adjoint"):
             getattr(L, f).restype = C.c_int32
         _lib = L
     return _lib
@@ -117,6 +118,26 @@ class GpuBatchedLayout:
             self.close()
         except Exception:
             pass
+
+    def initialize(self, vm, va, gen_pq, sg_pq=None):
+        """Device initialisation of every scenario on the GPU from solved
+        power flows (gp_initialize; initialize_dynamics!,
+        src/dynamics.jl:123-250): vm, va [M, n_bus]; gen_pq [M, n GENROU, 2]
+        each machine's output; sg_pq [M, n static generators, 2] their
+        totals.  The layout's parameter vectors give every parameter (each
+        scenario's load powers in the ZIP rows).  The result becomes the
+        layout's state and initial state; returns (z0, u0, p) copies."""
+        M, nb = self.M, self.arrays.n_bus
+        v = np.ascontiguousarray(np.stack([np.asarray(vm, dtype=np.float64).reshape(M, nb),
+                                           np.asarray(va, dtype=np.float64).reshape(M, nb)], axis=2))
+        g = np.ascontiguousarray(gen_pq, dtype=np.float64).reshape(M, -1, 2)
+        sg = None if sg_pq is None else np.ascontiguousarray(sg_pq, dtype=np.float64).reshape(M, -1, 2)
+        z0 = np.empty((M, self.n_sys))
+        u0 = np.empty((M, max(1, self.arrays.n_ctrl)))
+        p = np.empty((M, self.n_par))
+        _check(library().gp_initialize(self._h, _p(v), _p(g) if g.size else None,
+                                       _p(sg) if sg is not None and sg.size else None, _p(z0), _p(u0), _p(p)))
+        return z0, u0[:, :self.arrays.n_ctrl], p
 
     @property
     def z(self) -> np.ndarray:
@@ -325,12 +346,44 @@ def batched_power_flow(ps: Mdl.PowerSystem, load_scale, gen_scale=None, tol: flo
     return out
 
 
-def scenario_initial_states(ps: Mdl.PowerSystem, load_scale, gen_scale=None, tol: float = 1e-10):
+def generator_outputs(ps: Mdl.PowerSystem, vm, va, load_scale, gen_scale):
+    """Each generator's output in every scenario after its power flow (the
+    write-back of apply_pf_solution / runpf_inplace, vectorised over
+    scenarios): PV-bus generators share their bus's reactive injection,
+    slack-bus generators its active and reactive injection, the others keep
+    their scheduled output (active part scaled by gen_scale).  Returns
+    psch, qsch [M, n_gens]."""
+    vm = np.asarray(vm, dtype=np.float64)
+    va = np.asarray(va, dtype=np.float64)
+    M_ = vm.shape[0]
+    V = vm * np.exp(1j * va)
+    S = V * np.conj((ps.ybus.tocsr() @ V.T).T)
+    P, Q = S.real.copy(), S.imag.copy()
+    for l in ps.loads:
+        P[:, l.bus] -= l.pd * load_scale
+        Q[:, l.bus] -= l.qd * load_scale
+    ng = np.zeros(ps.nbus, dtype=np.int64)
+    for g in ps.gens:
+        ng[g.bus] += 1
+    psch = np.empty((M_, len(ps.gens)))
+    qsch = np.empty((M_, len(ps.gens)))
+    for k, g in enumerate(ps.gens):
+        bt = ps.buses[g.bus].type
+        psch[:, k] = P[:, g.bus] / ng[g.bus] if bt == Mdl.SLACK else g.psch * gen_scale
+        qsch[:, k] = Q[:, g.bus] / ng[g.bus] if bt in (Mdl.PV, Mdl.SLACK) else g.qsch
+    return psch, qsch
+
+
+def scenario_initial_states(ps: Mdl.PowerSystem, load_scale, gen_scale=None, tol: float = 1e-10,
+                            on_gpu: bool = True, dp: Optional[Mdl.DynamicProblem] = None):
     """Per-scenario initial conditions for a parameter sweep over load
     levels: the power flows of every scenario on the GPU
-    (batched_power_flow), then each scenario's device initialisation
-    (model.initialize_dynamics, the reference's initialize_dynamics!,
-    src/dynamics.jl:123-250) on its solution, on the host.  Returns
+    (batched_power_flow), then each scenario's device initialisation (the
+    reference's initialize_dynamics!, src/dynamics.jl:123-250) on its
+    solution: on the GPU (gp_initialize; `dp`, the initialised base case,
+    gives the layout its representative state and static parameters,
+    computed on the host once if not given), or with on_gpu=False on the
+    host per scenario (model.initialize_dynamics).  Returns
     (z0 [M, n_sys], u0 [M, n_ctrl], p [M, n_par]) for GpuBatchedLayout."""
     import copy
     load_scale = np.asarray(load_scale, dtype=np.float64).reshape(-1)
@@ -338,6 +391,32 @@ def scenario_initial_states(ps: Mdl.PowerSystem, load_scale, gen_scale=None, tol
     r = batched_power_flow(ps, load_scale, gen_scale, tol=tol)
     if np.any(r["status"] != 0):
         raise GradPowerError("power flow of scenario(s) %s did not converge" % np.nonzero(r["status"])[0].tolist())
+    if on_gpu:
+        M_ = load_scale.size
+        base = dp if dp is not None else Mdl.initialize_dynamics(copy.deepcopy(ps))
+        psch, qsch = generator_outputs(ps, r["vm"], r["va"], load_scale, gen_scale)
+        arrays = LY.ProblemArrays(ps)
+        devs = ps.dynamic.devices
+        G = arrays.tables[LY.GP_GENROU]
+        SG = arrays.tables[LY.GP_STATIC_GEN]
+        gen_pq = np.zeros((M_, G.n, 2))
+        for k, i in enumerate(G.device_index):
+            gen_pq[:, k, 0] = psch[:, devs[i].gen]
+            gen_pq[:, k, 1] = qsch[:, devs[i].gen]
+        sg_pq = np.zeros((M_, SG.n, 2))
+        for k, i in enumerate(SG.device_index):
+            for gi in devs[i].dtype.gen_idxs:
+                sg_pq[:, k, 0] += psch[:, gi]
+                sg_pq[:, k, 1] += qsch[:, gi]
+        p = np.tile(base.pvec, (M_, 1))
+        ZL = arrays.tables[LY.GP_ZIPLOAD]
+        p[:, ZL.par_ptr] *= load_scale[:, None]
+        p[:, ZL.par_ptr + 1] *= load_scale[:, None]
+        gbl = GpuBatchedLayout(base, ps, M_, p=p)
+        try:
+            return gbl.initialize(r["vm"], r["va"], gen_pq, sg_pq if SG.n else None)
+        finally:
+            gbl.close()
     slack = {i for i, b in enumerate(ps.buses) if b.type == Mdl.SLACK}
     zs, us, ps_ = [], [], []
     for m in range(load_scale.size):

@@ -238,6 +238,26 @@ int32_t gp_restore_initial_state(gp_layout *L);
  * this carries integrate!'s to it (per scenario). */
 int32_t gp_set_line_trips(gp_layout *L, int32_t n, const gp_line_trip *trips);
 
+/* Device initialisation of every scenario on the GPU from solved power
+ * flows: initialize_dynamics! (src/dynamics.jl:123-250), with the GENROU
+ * initialisation of src/generators.jl:159-285 (a Newton solve of each
+ * machine's steady state) and the controllers' steady states.
+ *   v_polar [M][n_bus][2]       bus voltage magnitude and angle (rad)
+ *   gen_pq  [M][n GENROU][2]    each machine's active and reactive output
+ *   sg_pq   [M][n STATIC_GEN][2] each static generator's totals p0, q0
+ *                               (NULL when the problem has none)
+ * Every parameter comes from the layout's parameter vectors (as given to
+ * gp_layout_create, with each scenario's load powers in the ZIP rows); the
+ * derived ones are written back: ZIP v0mag and admittance, static-generator
+ * p0/q0, governor pref, exciter vref.  The result becomes the layout's
+ * state, initial state (gp_restore_initial_state), controls and
+ * parameters; z0 [M*n_sys], u0 [M*n_ctrl] and p [M*n_par] receive copies
+ * (each may be NULL).  GP_E_NUMERIC when a machine's initialisation
+ * residual stays at or above 1e-9 (the reference's bound,
+ * src/dynamics.jl:58); the layout then holds the failed state. */
+int32_t gp_initialize(gp_layout *L, const double *v_polar, const double *gen_pq, const double *sg_pq,
+                      double *z0, double *u0, double *p);
+
 /* Device disconnections for the following gp_integrate calls (replaces the
  * previous set; n = 0 clears them).  GP_SOLVER_SCHUR_FP64 and
  * GP_SOLVER_SCHUR_MIXED only, like line trips: GP_SOLVER_SHARED_WOODBURY

@@ -95,3 +95,49 @@ def test_scenario_initial_states_are_equilibria(G, orc):
         gbl.close()
     assert np.all(r["status"] == 0) and np.all(r["iters"] == 0)
     assert not np.allclose(z0[0], z0[1])
+
+
+def _close(a, b, tol):
+    return np.max(np.abs(a - b)) <= tol * max(1.0, np.max(np.abs(b)))
+
+
+@pytest.mark.parametrize("case", ["ring39", "planar2k", "ieee9_v33.raw/2bus_SEXS.dyr",
+                                  "ieee9_v33.raw/ieee9bus_gov.dyr"])
+def test_gpu_device_init_matches_host_init(G, golden_cases, case):
+    """Device initialisation on the GPU (gp_initialize) against the host
+    restatement of initialize_dynamics! (model.initialize_dynamics) on the
+    same GPU power flows: states, controls and parameters within 1e-11.
+    The cases cover GENROU with IEESGO, TGOV1, SEXS, ESDC1A and IEEEST, and
+    PV and slack static generators."""
+    from helpers import psse_case
+    if "/" in case:
+        ps, dp = psse_case(golden_cases, *case.split("/"))
+    else:
+        w = synthetic.WORKLOADS[case]()
+        ps, dp = w.ps, w.dp
+    scales = np.array([0.92, 1.0, 1.06])
+    zg, ug, pg = G.scenario_initial_states(ps, scales, dp=dp)
+    zh, uh, ph = G.scenario_initial_states(ps, scales, on_gpu=False)
+    assert _close(zg, zh, 1e-11) and _close(ug, uh, 1e-11) and _close(pg, ph, 1e-11)
+    assert not np.allclose(zg[0], zg[2])
+
+
+def test_gpu_device_init_reports_failure(G):
+    """A machine asked for an output it cannot give at its terminal voltage
+    leaves a residual above 1e-9: gp_initialize fails with GP_E_NUMERIC and
+    says how many machines."""
+    from gradpower_gb300 import layout as LY
+    w = synthetic.ring39()
+    gbl = G.GpuBatchedLayout(w.dp, w.ps, 1)
+    try:
+        A = gbl.arrays
+        nb, ng = A.n_bus, A.tables[LY.GP_GENROU].n
+        vm = np.ones((1, nb))
+        va = np.zeros((1, nb))
+        pq = np.zeros((1, ng, 2))
+        pq[0, :, 0] = 0.5
+        pq[0, 0, 0] = np.inf
+        with pytest.raises(Exception, match="1 machine initialisation"):
+            gbl.initialize(vm, va, pq)
+    finally:
+        gbl.close()
