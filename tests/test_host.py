@@ -281,3 +281,48 @@ def test_cluster_factorisation_matches_dense_solves(lib, golden_cases, orc, case
         k += 1
     assert k == nt
     assert abs(out[0] - fmax) <= 1e-15 * max(1.0, fmax)
+
+
+def test_generator_outputs_match_apply_pf_solution():
+    """gpu.generator_outputs (the power-flow write-back vectorised over
+    scenarios) equals model.apply_pf_solution run on each scenario's scaled
+    copy of the system."""
+    import copy
+    from gradpower_gb300 import gpu
+    w = synthetic.planar2k()
+    ps = w.ps
+    rng = np.random.default_rng(5)
+    scales = np.array([0.95, 1.0, 1.04])
+    vm = np.array([[b.v0m for b in ps.buses]] * 3) * (1.0 + 1e-3 * rng.standard_normal((3, ps.nbus)))
+    va = np.array([[b.v0a for b in ps.buses]] * 3) + 1e-3 * rng.standard_normal((3, ps.nbus))
+    psch, qsch = gpu.generator_outputs(ps, vm, va, scales, scales)
+    slack = {i for i, b in enumerate(ps.buses) if b.type == M.SLACK}
+    assert any(ps.buses[g.bus].type == M.PV for g in ps.gens) and any(g.bus in slack for g in ps.gens)
+    for m, s in enumerate(scales):
+        ps2 = copy.deepcopy(ps)
+        for l in ps2.loads:
+            l.pd *= s
+            l.qd *= s
+        for g in ps2.gens:
+            if g.bus not in slack:
+                g.psch *= s
+        M.apply_pf_solution(ps2, vm[m], va[m])
+        assert np.allclose(psch[m], [g.psch for g in ps2.gens], rtol=0, atol=1e-12)
+        assert np.allclose(qsch[m], [g.qsch for g in ps2.gens], rtol=0, atol=1e-12)
+
+
+def test_disconnect_array_names_table_rows():
+    """layout.disconnect_array finds each device's table and row as
+    _set_device_offline! does (its rank among the devices of its type),
+    expands per-scenario and global events, and rounds steps like the
+    reference's schedule."""
+    w = synthetic.ring39()
+    PA = LY.ProblemArrays(w.ps)
+    ZL, SX = PA.tables[LY.GP_ZIPLOAD], PA.tables[LY.GP_SEXS]
+    dz, dx = int(ZL.device_index[3]), int(SX.device_index[1])
+    arr, n = LY.disconnect_array(PA, [[M.DisconnectDeviceEvent(dz, 0.05)], [], [M.DisconnectDeviceEvent(dx, 0.1)]],
+                                 1.0 / 120.0, [M.DisconnectDeviceEvent(dx, 0.2)])
+    rows = [(arr[k].scenario, arr[k].type, arr[k].index, arr[k].on_step) for k in range(n)]
+    assert rows == [(-1, LY.GP_SEXS, 1, 24), (0, LY.GP_ZIPLOAD, 3, 6), (2, LY.GP_SEXS, 1, 12)]
+    with pytest.raises(ValueError):
+        LY.disconnect_array(PA, [[M.DisconnectDeviceEvent(10 ** 6, 0.05)]], 1.0 / 120.0)
