@@ -994,6 +994,19 @@ void build_problem(gp_layout *L, const gp_problem *pr) {
     bus_csr(pl.cbus, &P.bus_cl_ptr, &P.bus_cl);
     bus_csr(vec(pr->dev[GP_ZIPLOAD].bus, pr->dev[GP_ZIPLOAD].n), &P.bus_zl_ptr, &P.bus_zl);
     bus_csr(vec(pr->dev[GP_STATIC_GEN].bus, pr->dev[GP_STATIC_GEN].n), &P.bus_sg_ptr, &P.bus_sg);
+    {
+        // the network kernel's bus order: buses with the same device counts
+        // and Ybus row length side by side (same loop trip counts per warp)
+        std::vector<std::array<int, 5>> key(nb);
+        for (int b = 0; b < nb; b++) key[b] = {0, 0, 0, pr->y_rowptr[b + 1] - pr->y_rowptr[b], b};
+        for (int k = 0; k < pr->dev[GP_STATIC_GEN].n; k++) key[pr->dev[GP_STATIC_GEN].bus[k]][0]++;
+        for (int k = 0; k < pr->dev[GP_ZIPLOAD].n; k++) key[pr->dev[GP_ZIPLOAD].bus[k]][1]++;
+        for (int b : pl.cbus) key[b][2]++;
+        std::sort(key.begin(), key.end());
+        std::vector<int> order(nb);
+        for (int i = 0; i < nb; i++) order[i] = key[i][4];
+        P.bus_order = A.upload(order);
+    }
     const gp::Symbolic &sym = pl.sym;
     P.iperm = A.upload(sym.iperm);
     DevSym &S = L->S;

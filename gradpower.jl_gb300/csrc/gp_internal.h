@@ -29,6 +29,7 @@ struct DevProblem {
     const int *cl_w_start, *cl_w_size, *cl_gen, *cl_gov_type, *cl_gov, *cl_exc_type, *cl_exc, *cl_pss;
     // per bus: non-trivial clusters, ZIP loads, static generators
     const int *bus_cl_ptr, *bus_cl, *bus_zl_ptr, *bus_zl, *bus_sg_ptr, *bus_sg;
+    const int *bus_order;  // [n_bus] buses sorted by (static generators, loads, clusters, Ybus row length)
     // static generators in the reduced system
     const int *sg_red;     // [n_sg] reduced index of the first alg state (or -1)
     const int *sg_var;     // [n_sg] first index of its coupling entries in the var block

@@ -38,9 +38,11 @@ namespace gp {
 // ---------------------------------------------------------------------------
 
 __device__ __forceinline__ unsigned long long norm_bits(double v) {
-    // non-negative doubles order like their bit patterns; NaN counts as +inf
-    if (!(v == v)) return 0x7ff0000000000000ull;
-    return (unsigned long long)__double_as_longlong(fabs(v));
+    // the bit pattern of |v| (non-negative doubles order like their bit
+    // patterns); NaN counts as +inf.  Integer operations only: the FP64
+    // pipe is the scarce one on this GPU.
+    const unsigned long long a = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+    return a > 0x7ff0000000000000ull ? 0x7ff0000000000000ull : a;
 }
 
 // ---------------------------------------------------------------------------
@@ -430,7 +432,9 @@ __global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, D
     const long long task = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = task < (long long)P.M * P.n_bus;
     const int m = valid ? (int)(task / P.n_bus) : P.M;
-    const int b = valid ? (int)(task % P.n_bus) : 0;
+    // buses in the order of their work (devices, then Ybus row length), so
+    // that the lanes of a warp run the same loop trip counts
+    const int b = valid ? P.bus_order[(int)(task % P.n_bus)] : 0;
     const bool act = valid && W.active[m];
     unsigned long long nb = 0ull;
     if (act) {
