@@ -106,6 +106,7 @@ struct gp_layout {
     size_t traj_cap = 0;
     cudaStream_t st_copy = nullptr;
     cudaEvent_t ev_snap = nullptr;
+    double *d_zl_k = nullptr;   // DevProblem::zl_k
     int *d_state_maps = nullptr;   // state_bus then red_of
     int *d_gen_w = nullptr;        // z index of every machine's speed deviation
     int n_gen = 0;
@@ -1052,6 +1053,8 @@ void build_work(gp_layout *L, const double *z0, const double *u0, const double *
     W.zold = A.alloc<double>(M * P.n_sys);
     W.u0 = A.upload(u0, M * std::max(1, P.n_ctrl));
     W.p = A.upload(p, M * std::max(1, P.n_par));
+    L->d_zl_k = A.alloc<double>(M * 4 * std::max(1, P.dev[6].n));
+    P.zl_k = L->d_zl_k;
     W.yx = A.alloc<double>(M * 3 * std::max(1, P.net));
     W.clout = A.alloc<double>(M * 8 * std::max(1, P.n_cl));
     W.svar = A.alloc<double>(M * P.n_var);
@@ -1103,6 +1106,8 @@ void build_work(gp_layout *L, const double *z0, const double *u0, const double *
     ck(cudaStreamCreateWithFlags(&L->st_copy, cudaStreamNonBlocking), "stream");
     ck(cudaEventCreateWithFlags(&L->ev_snap, cudaEventDisableTiming), "event");
     for (int i = 0; i < 8; i++) ck(cudaEventCreate(&L->pev[i]), "event");
+    gp::launch_zip_const(P, W, L->d_zl_k, L->st);
+    ck(cudaStreamSynchronize(L->st), "load constants");
     // keep the initial state for gp_restore_initial_state
     L->z_init = A.alloc<double>(M * P.n_sys);
     ck(cudaMemcpy(L->z_init, W.z, M * P.n_sys * sizeof(double), cudaMemcpyDeviceToDevice), "z0 copy");
@@ -2355,6 +2360,7 @@ int32_t gp_initialize(gp_layout *L, const double *v_polar, const double *gen_pq,
     int *d_bad = A.alloc<int>(1);
     ck(cudaMemsetAsync(d_bad, 0, sizeof(int), L->st), "memset");
     gp::launch_initialize(L->P, L->W, d_v, d_g, d_s, d_bad, L->st);
+    gp::launch_zip_const(L->P, L->W, L->d_zl_k, L->st);   // the loads' admittances changed
     ck(cudaGetLastError(), "initialise");
     ck(cudaMemcpyAsync(L->z_init, L->W.z, M * L->n_sys * sizeof(double), cudaMemcpyDeviceToDevice, L->st),
        "initial state");

@@ -50,6 +50,7 @@ struct DevProblem {
     const uint8_t *zl_off;   // [M][n ZIP loads]
     const uint8_t *sg_off;   // [M][n static generators]
     const uint8_t *exc_off;  // [M][n_cl] the exciter of cluster c
+    const double *zl_k;      // [M][n ZIP loads][4] (1 - al) P, (1 - al) Q, al g0, al b0 (launch_zip_const)
     // symbolic permutation of the reduced system
     const int *iperm;      // reduced index -> permuted position
 };
@@ -243,6 +244,9 @@ void launch_initialize(const DevProblem &P, const DevWork &W, const double *vpol
 // scenario marked active for the dt = 0 re-solve.
 void launch_disconnects(const int *on_step, const int *scen, const int *idx, uint8_t *flags, uint8_t *active,
                         int n, int step, cudaStream_t st);
+// Parameter products of the ZIP loads for network_kernel; rerun whenever
+// the parameter vectors change.
+void launch_zip_const(const DevProblem &P, const DevWork &W, double *out, cudaStream_t st);
 // Parameter constants of the cluster devices for cluster_keep_kernel.
 void launch_cluster_const(const DevProblem &P, const DevWork &W, const DevClu &C, const DevMixed &Mx,
                           cudaStream_t st);

@@ -406,6 +406,27 @@ int launch_cluster(const DevProblem &P, const DevWork &W, const DevClu &C, const
     return 2;
 }
 
+// Parameter products of every ZIP load per scenario for network_kernel:
+// (1 - al) P, (1 - al) Q, al g0, al b0.
+__global__ void zip_const_kernel(DevProblem P, DevWork W, double *out) {
+    const DTab &ZL = P.dev[6];
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)P.M * ZL.n) return;
+    const int m = (int)(t / ZL.n), k = (int)(t % ZL.n);
+    const double *p = W.p + (size_t)m * P.n_par + ZL.par_ptr[k];
+    const double al = p[2];
+    double *o = out + (size_t)t * 4;
+    o[0] = (1.0 - al) * p[0];
+    o[1] = (1.0 - al) * p[1];
+    o[2] = al * p[7];
+    o[3] = al * p[8];
+}
+
+void launch_zip_const(const DevProblem &P, const DevWork &W, double *out, cudaStream_t st) {
+    const long long n = (long long)P.M * P.dev[6].n;
+    if (n > 0) zip_const_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(P, W, out);
+}
+
 void launch_cluster_const(const DevProblem &P, const DevWork &W, const DevClu &C, const DevMixed &Mx,
                           cudaStream_t st) {
     if (C.n_tasks == 0) return;
@@ -463,37 +484,38 @@ __global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, D
         for (int q = P.bus_zl_ptr[b]; q < P.bus_zl_ptr[b + 1]; q++) {
             const int k = P.bus_zl[q];
             if (P.zl_off && P.zl_off[(size_t)m * ZL.n + k]) continue;
-            const int pp = ZL.par_ptr[k];
-            const double pl = p[pp], ql = p[pp + 1], al = p[pp + 2], yre0 = p[pp + 7], yim0 = p[pp + 8];
+            // the load's parameter products ((1 - al) P, (1 - al) Q, al y0),
+            // from the table zip_const_kernel fills once per call
+            const double *kz = P.zl_k + ((size_t)m * ZL.n + k) * 4;
+            const double A1 = kz[0], A2 = kz[1], B1 = kz[2], B2 = kz[3];
             const double vm2 = vr * vr + vi * vi, vm2_tld = 0.2;
             const bool above = vm2 > vm2_tld;
             // one division per load (FP64 division is dear here)
             const double inv = 1.0 / (above ? vm2 : vm2_tld);
-            const double sp = (1.0 - al) * inv;
             // the constant-impedance part al*y0 and the constant-power part
             // (1 - al)(P - jQ)/max(|V|^2, 0.2) multiply the same V: one
-            // complex admittance a + jc
-            const double a = fma(sp, pl, al * yre0), c = fma(sp, ql, al * yim0);
-            fr -= vr * a - vi * c;
-            fi -= vr * c + vi * a;
+            // complex admittance a + jc; f -= (a + jc) V in FMA form
+            const double a = fma(inv, A1, B1), c = fma(inv, A2, B2);
+            fr = fma(vi, c, fma(-vr, a, fr));
+            fi = fma(-vi, a, fma(-vr, c, fi));
             if (!need_s) continue;
             double p11, p12, p21, p22;
             if (above) {
                 const double iv4 = inv * inv;
-                p11 = (1.0 - al) * ((pl * vr - ql * vi) * 2.0 * vr - pl * vm2) * iv4;
-                p12 = (1.0 - al) * ((pl * vr - ql * vi) * 2.0 * vi + ql * vm2) * iv4;
-                p21 = (1.0 - al) * ((ql * vr + pl * vi) * 2.0 * vr - ql * vm2) * iv4;
-                p22 = (1.0 - al) * ((ql * vr + pl * vi) * 2.0 * vi - pl * vm2) * iv4;
+                p11 = ((A1 * vr - A2 * vi) * 2.0 * vr - A1 * vm2) * iv4;
+                p12 = ((A1 * vr - A2 * vi) * 2.0 * vi + A2 * vm2) * iv4;
+                p21 = ((A2 * vr + A1 * vi) * 2.0 * vr - A2 * vm2) * iv4;
+                p22 = ((A2 * vr + A1 * vi) * 2.0 * vi - A1 * vm2) * iv4;
             } else {
-                p11 = -pl * sp;
-                p12 = ql * sp;
-                p21 = -ql * sp;
-                p22 = -pl * sp;
+                p11 = -A1 * inv;
+                p12 = A2 * inv;
+                p21 = -A2 * inv;
+                p22 = -A1 * inv;
             }
-            d00 += -al * yre0 + p11;
-            d01 += al * yim0 + p12;
-            d10 += -al * yim0 + p21;
-            d11 += -al * yre0 + p22;
+            d00 += -B1 + p11;
+            d01 += B2 + p12;
+            d10 += -B2 + p21;
+            d11 += -B1 + p22;
         }
         const DTab &SG = P.dev[7];
         for (int q = P.bus_sg_ptr[b]; q < P.bus_sg_ptr[b + 1]; q++) {
