@@ -134,6 +134,15 @@ struct gp_layout {
     int *d_tr_on_step = nullptr, *d_tr_off_step = nullptr, *d_tr_scen = nullptr;
     std::vector<int> h_tr_on_step, h_tr_off_step;
     std::vector<int> h_adj_ptr, h_adj;   // bus adjacency (line trips are checked against it)
+    // fault table (set_faults; grow-only, see there) and the per-step
+    // iteration counts of gp_integrate (grow-only)
+    DeviceArena fault_arena;
+    int fl_cap = 0;
+    int *d_fl_ptr = nullptr, *d_fl_bus = nullptr;
+    double *d_fl_yf = nullptr;
+    DeviceArena iters_arena;
+    int *d_iters_buf = nullptr;
+    size_t iters_cap = 0;
     // device disconnections (gp_set_device_disconnects): offline flags of
     // ZIP loads, static generators and cluster exciters per scenario (zeroed
     // at every call), and the events as (flag index, scenario, step)
@@ -1199,20 +1208,39 @@ void set_faults(gp_layout *L, int n_faults, const gp_fault *faults) {
         ptr[m + 1] = (int)bus.size();
     }
     L->n_fl = (int)bus.size();
-    L->P.fl_ptr = L->call.upload(ptr);
-    L->P.fl_bus = L->call.upload(bus);
-    L->P.fl_yf = L->call.upload(yf);
-    L->d_fl_on = L->call.alloc<uint8_t>(std::max(1, L->n_fl));
-    ck(cudaMemset(L->d_fl_on, 0, std::max(1, L->n_fl)), "memset");
-    L->P.fl_on = L->d_fl_on;
-    L->d_fl_on_step = L->call.upload(on);
-    L->d_fl_off_step = L->call.upload(off);
-    L->d_fl_scen = L->call.upload(scen);
+    // the fault table keeps its device addresses while it fits (grow-only):
+    // the captured graphs hold those addresses, and stay valid across calls
+    const int cap = std::max(1, L->n_fl);
+    if (!L->d_fl_ptr || cap > L->fl_cap) {
+        L->fault_arena.release();
+        DeviceArena &A = L->fault_arena;
+        L->d_fl_ptr = A.alloc<int>(M + 1);
+        L->d_fl_bus = A.alloc<int>(cap);
+        L->d_fl_yf = A.alloc<double>(cap);
+        L->d_fl_on = A.alloc<uint8_t>(cap);
+        L->d_fl_on_step = A.alloc<int>(cap);
+        L->d_fl_off_step = A.alloc<int>(cap);
+        L->d_fl_scen = A.alloc<int>(cap);
+        L->fl_cap = cap;
+        L->P.fl_ptr = L->d_fl_ptr;
+        L->P.fl_bus = L->d_fl_bus;
+        L->P.fl_yf = L->d_fl_yf;
+        L->P.fl_on = L->d_fl_on;
+        drop_graphs(L);
+    }
+    auto put = [&](void *d, const void *h, size_t bytes) {
+        if (bytes) ck(cudaMemcpy(d, h, bytes, cudaMemcpyHostToDevice), "fault table");
+    };
+    put(L->d_fl_ptr, ptr.data(), ptr.size() * sizeof(int));
+    put(L->d_fl_bus, bus.data(), bus.size() * sizeof(int));
+    put(L->d_fl_yf, yf.data(), yf.size() * sizeof(double));
+    put(L->d_fl_on_step, on.data(), on.size() * sizeof(int));
+    put(L->d_fl_off_step, off.data(), off.size() * sizeof(int));
+    put(L->d_fl_scen, scen.data(), scen.size() * sizeof(int));
+    ck(cudaMemset(L->d_fl_on, 0, cap), "memset");
     L->h_fl_on_step = on;
     L->h_fl_off_step = off;
     L->h_fl_scen = scen;
-    // graphs capture the fault pointers: rebuild them
-    drop_graphs(L);
 }
 
 void mark(gp_layout *L, int i) {
@@ -1674,6 +1702,8 @@ int32_t gp_layout_create(const gp_problem *prob, int32_t M, const double *z0, co
     catch (const gp_error &e) {
         g_last_error = e.what();
         if (L) {
+            L->fault_arena.release();
+            L->iters_arena.release();
             L->traj_arena.release();
             L->dc_arena.release();
             L->trip_arena.release();
@@ -1685,6 +1715,8 @@ int32_t gp_layout_create(const gp_problem *prob, int32_t M, const double *z0, co
     catch (const std::exception &e) {
         g_last_error = e.what();
         if (L) {
+            L->fault_arena.release();
+            L->iters_arena.release();
             L->traj_arena.release();
             L->dc_arena.release();
             L->trip_arena.release();
@@ -1704,6 +1736,8 @@ int32_t gp_layout_destroy(gp_layout *L) {
     L->call.release();
     if (L->st_copy) cudaStreamSynchronize(L->st_copy);
     L->traj_arena.release();
+    L->fault_arena.release();
+    L->iters_arena.release();
     L->dc_arena.release();
     L->trip_arena.release();
     L->arena.release();
@@ -1834,7 +1868,13 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
     for (int e = 0; e < L->n_dc; e++) ev_steps[L->h_dc_on_step[e]] = 1;
     if (L->n_dc > 0) ck(cudaMemsetAsync(L->d_dc_flags, 0, L->dc_bytes, L->st), "memset");
     double *d_traj = nullptr;
-    int *d_iters = L->call.alloc<int>((size_t)2 * std::max(ns, 1) * M);
+    const size_t n_it = (size_t)2 * std::max(ns, 1) * M;
+    if (n_it > L->iters_cap) {
+        L->iters_arena.release();
+        L->d_iters_buf = L->iters_arena.alloc<int>(n_it);
+        L->iters_cap = n_it;
+    }
+    int *d_iters = L->d_iters_buf;
     ck(cudaMemsetAsync(d_iters, 0, (size_t)2 * std::max(ns, 1) * M * sizeof(int), L->st), "memset");
     // a page-locked host trajectory receives each step's snapshot as soon as
     // it is taken (copy stream); any other host buffer, all of them at the end
