@@ -1973,6 +1973,10 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
         }
     }
     ck(cudaEventRecord(e1, L->st), "event");
+    // the call's events end with it: lines back in service, devices online
+    // (gp_residual and the next call see the intact system)
+    if (L->n_tr > 0) ck(cudaMemsetAsync(L->d_tr_on, 0, L->n_tr, L->st), "memset");
+    if (L->n_dc > 0) ck(cudaMemsetAsync(L->d_dc_flags, 0, L->dc_bytes, L->st), "memset");
     ck(cudaStreamSynchronize(L->st), "integrate");
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);

@@ -139,9 +139,9 @@ typedef struct gp_fault {
  * (_apply_trip_line!, :551-564), and at the end of step off_step they are
  * added back (_apply_reclose_line!, :566-574; off_step < 0: never), each
  * followed by the dt = 0 re-solve (src/dynamics.jl:612-646).  Buses are
- * 0-based internal indices.  Every gp_integrate call starts with all lines
- * in service (the reference leaves a permanent trip in ps.network.ybus_real
- * after integrate!). */
+ * 0-based internal indices.  Every gp_integrate call starts and ends with
+ * all lines in service (the reference leaves a permanent trip in
+ * ps.network.ybus_real after integrate!). */
 typedef struct gp_line_trip {
     int32_t scenario;            /* -1: every scenario */
     int32_t from_bus, to_bus;
@@ -159,8 +159,8 @@ typedef struct gp_line_trip {
  * it injects nothing into the network.  A device that owns algebraic rows
  * (GENROU, IEESGO, TGOV1, IEEEST, a PV or slack static generator) would
  * leave those rows without equations, a singular Jacobian: such events are
- * refused with GP_E_INVALID.  Every gp_integrate call starts with all
- * devices online. */
+ * refused with GP_E_INVALID.  Every gp_integrate call starts and ends
+ * with all devices online. */
 typedef struct gp_device_disconnect {
     int32_t scenario;            /* -1: every scenario */
     int32_t type;                /* GP_SEXS, GP_ESDC1A, GP_ZIPLOAD or GP_STATIC_GEN (PQ) */
