@@ -118,3 +118,23 @@ def test_disconnects_cleared_and_rejected(G):
     finally:
         gbl.close()
     assert np.array_equal(r0["traj"], r1["traj"]) and np.array_equal(r0["iters"], r1["iters"])
+
+
+def test_events_end_with_the_call(G):
+    """After a run with line trips and device disconnections the layout holds
+    the intact system again: its residual at the final state equals that of
+    a layout that never had the events, set to the same state."""
+    c, per, glob = _case("ring39", 3)
+    trips = [[M.trip_branch_event(c.ps.branches[2], 0.05)]] * 3
+    a = G.GpuBatchedLayout(c.dp, c.ps, c.M)
+    b = G.GpuBatchedLayout(c.dp, c.ps, c.M)
+    try:
+        a.integrate(20 * DT, DT, scenario_faults=c.faults, scenario_disconnects=per, disconnect_events=glob,
+                    scenario_trips=trips, want_traj=False)
+        z = a.z
+        b.z = z
+        zold = z * (1.0 + 1e-6)
+        assert np.array_equal(a.residual(zold, DT), b.residual(zold, DT))
+    finally:
+        a.close()
+        b.close()
