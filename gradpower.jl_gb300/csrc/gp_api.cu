@@ -50,8 +50,13 @@ void ck(cudaError_t e, const char *what) {
     if (e != cudaSuccess) fail(GP_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
+// Device allocations of one lifetime.  Uploads go through the layout's
+// stream `st` and are complete on return: that stream does not wait for the
+// legacy default stream (cudaStreamNonBlocking), so a plain cudaMemcpy would
+// not be ordered before the kernels launched on it.
 struct DeviceArena {
     std::vector<void *> ptrs;
+    cudaStream_t st = nullptr;
     template <class T>
     T *alloc(size_t n) {
         void *p = nullptr;
@@ -63,14 +68,15 @@ struct DeviceArena {
     }
     template <class T>
     T *upload(const std::vector<T> &v) {
-        T *p = alloc<T>(v.size());
-        if (!v.empty()) ck(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "upload");
-        return p;
+        return upload(v.data(), v.size());
     }
     template <class T>
     T *upload(const T *v, size_t n) {
         T *p = alloc<T>(n);
-        if (n && v) ck(cudaMemcpy(p, v, n * sizeof(T), cudaMemcpyHostToDevice), "upload");
+        if (n && v) {
+            ck(cudaMemcpyAsync(p, v, n * sizeof(T), cudaMemcpyHostToDevice, st), "upload");
+            ck(cudaStreamSynchronize(st), "upload");
+        }
         return p;
     }
     void release() {
@@ -89,6 +95,7 @@ std::vector<int> vec(const int32_t *p, int n) {
 
 struct gp_layout {
     int M = 0;
+    int device = 0;        // CUDA device the layout lives on (current at gp_layout_create)
     int n_sys = 0, n_da = 0, n_red = 0, n_bus = 0, n_ctrl = 0, n_par = 0;
     gp::DevProblem P{};
     gp::DevWork W{};
@@ -173,6 +180,7 @@ struct gp_layout {
     double factor_launches = 0.0, solves = 0.0;
     double *z_init = nullptr;    // z0 as given to gp_layout_create
     int64_t sum_w2 = 0;
+    int64_t nnz_s = 0;           // structural nonzeros of the reduced matrix S
     // sparse cluster factorisation
     gp::ClusterPlan cplan;
     gp::DevClu C{};
@@ -202,6 +210,40 @@ struct gp_layout {
 
 namespace {
 
+// Copies and fills issued by the entry points, all on the layout's stream
+// (ordered with its kernels and graphs).  to_device and to_host return with
+// the copy complete, so the caller's host buffer is free again; fill is
+// asynchronous.
+void to_device(const gp_layout *L, void *d, const void *h, size_t bytes, const char *what) {
+    if (!bytes) return;
+    ck(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, L->st), what);
+    ck(cudaStreamSynchronize(L->st), what);
+}
+void to_host(const gp_layout *L, void *h, const void *d, size_t bytes, const char *what) {
+    if (!bytes) return;
+    ck(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, L->st), what);
+    ck(cudaStreamSynchronize(L->st), what);
+}
+void fill(const gp_layout *L, void *d, int value, size_t bytes) {
+    if (bytes) ck(cudaMemsetAsync(d, value, bytes, L->st), "memset");
+}
+
+// Makes the layout's device current for the duration of an entry point.
+struct DeviceScope {
+    int prev = -1;
+    explicit DeviceScope(const gp_layout *L) {
+        int cur = 0;
+        ck(cudaGetDevice(&cur), "cudaGetDevice");
+        if (cur != L->device) {
+            ck(cudaSetDevice(L->device), "cudaSetDevice");
+            prev = cur;
+        }
+    }
+    ~DeviceScope() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
 // Host-side plan of a layout: everything derived from the problem before
 // any device allocation (validated cluster tables, reduced-system maps,
 // symbolic analysis, front assembly lists).  Also used, without a GPU, by
@@ -217,6 +259,7 @@ struct Plan {
     std::vector<int> t_acp, t_acpos, t_avp, t_avpos, t_avidx;   // the same for S^T
     std::vector<double> t_acval;
     int64_t sum_w2 = 0;
+    int64_t nnz_s = 0;       // structural nonzeros of S
 };
 
 void check_in_cluster(int c, int w0, int w, int idx, const char *what) {
@@ -395,6 +438,7 @@ void make_plan(const gp_problem *pr, Plan &pl) {
         const int na = SG.link0[k] == 2 ? 1 : 2;
         for (int j = 0; j < na; j++) group[a0 + j] = SG.bus[k];
     }
+    pl.nnz_s = (int64_t)ci.size();
     gp::Symbolic &sym = pl.sym;
     gp::analyse(n_red, rp, ci, group, nb, sym);
     // ---- assembly lists ----
@@ -964,6 +1008,7 @@ void build_problem(gp_layout *L, const gp_problem *pr) {
         L->d_gen_w = A.upload(gw);
     }
     L->sum_w2 = pl.sum_w2;
+    L->nnz_s = pl.nnz_s;
     P.n_cl = (int)pl.ws.size();
     P.cl_w_start = A.upload(pl.ws);
     P.cl_w_size = A.upload(pl.wsz);
@@ -1091,7 +1136,7 @@ void build_work(gp_layout *L, const double *z0, const double *u0, const double *
             for (int s = 0; s < L->sym.nsup; s++)
                 for (int c = L->sym.sup_start[s]; c < L->sym.sup_start[s + 1]; c++)
                     ident[m * S.n + c] = c - L->sym.sup_start[s];
-        ck(cudaMemcpy(S.ipiv, ident.data(), ident.size() * sizeof(int), cudaMemcpyHostToDevice), "ipiv");
+        to_device(L, S.ipiv, ident.data(), ident.size() * sizeof(int), "ipiv");
     }
     gp::DevDag &D = L->D;
     D.ctr = A.alloc<int>(8);
@@ -1100,26 +1145,24 @@ void build_work(gp_layout *L, const double *z0, const double *u0, const double *
     D.fdone = A.alloc<int>(M * D.nsup);
     D.xdone = A.alloc<int>(M * D.nsup);
     D.bdone = A.alloc<int>(M * D.nsup);
-    ck(cudaMemset(D.ctr, 0, 8 * sizeof(int)), "memset");
-    ck(cudaMemset(D.epoch, 0, sizeof(int)), "memset");
-    ck(cudaMemset(D.err, 0, sizeof(int)), "memset");
-    ck(cudaMemset(D.fdone, 0, M * D.nsup * sizeof(int)), "memset");
-    ck(cudaMemset(D.xdone, 0, M * D.nsup * sizeof(int)), "memset");
-    ck(cudaMemset(D.bdone, 0, M * D.nsup * sizeof(int)), "memset");
-    ck(cudaMemset(W.status, 0, M * sizeof(int)), "memset");
+    fill(L, D.ctr, 0, 8 * sizeof(int));
+    fill(L, D.epoch, 0, sizeof(int));
+    fill(L, D.err, 0, sizeof(int));
+    fill(L, D.fdone, 0, M * D.nsup * sizeof(int));
+    fill(L, D.xdone, 0, M * D.nsup * sizeof(int));
+    fill(L, D.bdone, 0, M * D.nsup * sizeof(int));
+    fill(L, W.status, 0, M * sizeof(int));
     ck(cudaMallocHost(&L->h_flag, 4 * sizeof(int)), "cudaMallocHost");
     L->d_cnt = A.alloc<int>(8);
-    ck(cudaMemset(L->d_cnt, 0, 8 * sizeof(int)), "memset");
+    fill(L, L->d_cnt, 0, 8 * sizeof(int));
     ck(cudaMallocHost(&L->h_dt, sizeof(double)), "cudaMallocHost");
-    ck(cudaStreamCreateWithFlags(&L->st, cudaStreamNonBlocking), "stream");
-    ck(cudaStreamCreateWithFlags(&L->st_copy, cudaStreamNonBlocking), "stream");
     ck(cudaEventCreateWithFlags(&L->ev_snap, cudaEventDisableTiming), "event");
     for (int i = 0; i < 8; i++) ck(cudaEventCreate(&L->pev[i]), "event");
     gp::launch_zip_const(P, W, L->d_zl_k, L->st);
     ck(cudaStreamSynchronize(L->st), "load constants");
     // keep the initial state for gp_restore_initial_state
     L->z_init = A.alloc<double>(M * P.n_sys);
-    ck(cudaMemcpy(L->z_init, W.z, M * P.n_sys * sizeof(double), cudaMemcpyDeviceToDevice), "z0 copy");
+    ck(cudaMemcpyAsync(L->z_init, W.z, M * P.n_sys * sizeof(double), cudaMemcpyDeviceToDevice, L->st), "z0 copy");
 }
 
 // Sparse cluster programs (gp_cluster_plan.cpp), uploaded with the cluster
@@ -1229,7 +1272,7 @@ void set_faults(gp_layout *L, int n_faults, const gp_fault *faults) {
         drop_graphs(L);
     }
     auto put = [&](void *d, const void *h, size_t bytes) {
-        if (bytes) ck(cudaMemcpy(d, h, bytes, cudaMemcpyHostToDevice), "fault table");
+        if (bytes) to_device(L, d, h, bytes, "fault table");
     };
     put(L->d_fl_ptr, ptr.data(), ptr.size() * sizeof(int));
     put(L->d_fl_bus, bus.data(), bus.size() * sizeof(int));
@@ -1237,7 +1280,7 @@ void set_faults(gp_layout *L, int n_faults, const gp_fault *faults) {
     put(L->d_fl_on_step, on.data(), on.size() * sizeof(int));
     put(L->d_fl_off_step, off.data(), off.size() * sizeof(int));
     put(L->d_fl_scen, scen.data(), scen.size() * sizeof(int));
-    ck(cudaMemset(L->d_fl_on, 0, cap), "memset");
+    fill(L, L->d_fl_on, 0, cap);
     L->h_fl_on_step = on;
     L->h_fl_off_step = off;
     L->h_fl_scen = scen;
@@ -1410,8 +1453,8 @@ cudaGraphExec_t build_loop(gp_layout *L, double tol, int itermax, bool mixed, in
 // Folds the device-driven loop's counts into the call's totals.
 void harvest_counts(gp_layout *L) {
     int c[8];
-    ck(cudaMemcpy(c, L->d_cnt, sizeof(c), cudaMemcpyDeviceToHost), "count copy");
-    ck(cudaMemset(L->d_cnt, 0, sizeof(c)), "memset");
+    to_host(L, c, L->d_cnt, sizeof(c), "count copy");
+    fill(L, L->d_cnt, 0, sizeof(c));
     const bool mixed = L->Mx.on != 0;
     const int nfac = L->solve_graph_factors;
     L->launches += (double)c[0] * L->eval_launches;
@@ -1450,17 +1493,17 @@ void ensure_mixed(gp_layout *L) {
     L->zprev = A.alloc<double>(M * L->n_sys);
     L->zprev2 = A.alloc<double>(M * L->n_sys);
     L->zprev3 = A.alloc<double>(M * L->n_sys);
-    ck(cudaMemset(X.refac, 0, M), "memset");
-    ck(cudaMemset(X.refac_next, 0, M), "memset");
-    ck(cudaMemset(X.prev_mode, 0, M), "memset");
-    ck(cudaMemset(X.age, 0, M * sizeof(int)), "memset");
-    ck(cudaMemset(X.all_exact, 0, M), "memset");
-    ck(cudaMemset(X.retry, 0, M), "memset");
+    fill(L, X.refac, 0, M);
+    fill(L, X.refac_next, 0, M);
+    fill(L, X.prev_mode, 0, M);
+    fill(L, X.age, 0, M * sizeof(int));
+    fill(L, X.all_exact, 0, M);
+    fill(L, X.retry, 0, M);
     // kept factors start at zero (zero pivot reciprocals give a zero step,
     // which the contraction test turns into a refresh)
-    ck(cudaMemset(X.lu, 0, M * std::max(1, L->C.n_tasks) * n_lu * 32 * sizeof(float)), "memset");
-    ck(cudaMemset(X.cc, 0, M * std::max(1, L->P.n_cl) * 6 * sizeof(float)), "memset");
-    ck(cudaMemset(X.fronts, 0, M * L->S.front_total * sizeof(float)), "memset");
+    fill(L, X.lu, 0, M * std::max(1, L->C.n_tasks) * n_lu * 32 * sizeof(float));
+    fill(L, X.cc, 0, M * std::max(1, L->P.n_cl) * 6 * sizeof(float));
+    fill(L, X.fronts, 0, M * L->S.front_total * sizeof(float));
     if (gp::dag_configure(L->D, 1, L->G32) != 0) fail(GP_E_CUDA, "could not configure the FP32 dataflow kernels");
     L->mixed_ready = true;
 }
@@ -1656,6 +1699,33 @@ void adj_solve(gp_layout *L, const gp::DevAdj &A, const gp::DevClu &Csave, doubl
 // exported API
 // ---------------------------------------------------------------------------
 
+namespace {
+
+// Frees everything a layout holds (also a partly built one).
+void free_layout(gp_layout *L) {
+    if (!L) return;
+    drop_graphs(L);
+    if (L->st) cudaStreamSynchronize(L->st);
+    if (L->st_copy) cudaStreamSynchronize(L->st_copy);
+    L->call.release();
+    L->traj_arena.release();
+    L->fault_arena.release();
+    L->iters_arena.release();
+    L->dc_arena.release();
+    L->trip_arena.release();
+    L->arena.release();
+    if (L->h_flag) cudaFreeHost(L->h_flag);
+    if (L->h_dt) cudaFreeHost(L->h_dt);
+    for (int i = 0; i < 8; i++)
+        if (L->pev[i]) cudaEventDestroy(L->pev[i]);
+    if (L->st) cudaStreamDestroy(L->st);
+    if (L->st_copy) cudaStreamDestroy(L->st_copy);
+    if (L->ev_snap) cudaEventDestroy(L->ev_snap);
+    delete L;
+}
+
+}  // namespace
+
 #define API_BEGIN try {
 #define API_END                                  \
     }                                            \
@@ -1689,6 +1759,12 @@ int32_t gp_layout_create(const gp_problem *prob, int32_t M, const double *z0, co
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) fail(GP_E_CUDA, "no CUDA device available");
     L = new gp_layout();
     L->M = M;
+    ck(cudaGetDevice(&L->device), "cudaGetDevice");
+    ck(cudaStreamCreateWithFlags(&L->st, cudaStreamNonBlocking), "stream");
+    ck(cudaStreamCreateWithFlags(&L->st_copy, cudaStreamNonBlocking), "stream");
+    for (DeviceArena *a : {&L->arena, &L->call, &L->traj_arena, &L->trip_arena, &L->fault_arena, &L->iters_arena,
+                           &L->dc_arena})
+        a->st = L->st;
     build_problem(L, prob);
     build_work(L, z0, u0, p);
     build_clusters(L, prob, z0, u0, p);
@@ -1701,28 +1777,12 @@ int32_t gp_layout_create(const gp_problem *prob, int32_t M, const double *z0, co
     }
     catch (const gp_error &e) {
         g_last_error = e.what();
-        if (L) {
-            L->fault_arena.release();
-            L->iters_arena.release();
-            L->traj_arena.release();
-            L->dc_arena.release();
-            L->trip_arena.release();
-            L->arena.release();
-            delete L;
-        }
+        free_layout(L);
         return e.code;
     }
     catch (const std::exception &e) {
         g_last_error = e.what();
-        if (L) {
-            L->fault_arena.release();
-            L->iters_arena.release();
-            L->traj_arena.release();
-            L->dc_arena.release();
-            L->trip_arena.release();
-            L->arena.release();
-            delete L;
-        }
+        free_layout(L);
         return GP_E_INVALID;
     }
     return GP_OK;
@@ -1731,24 +1791,8 @@ int32_t gp_layout_create(const gp_problem *prob, int32_t M, const double *z0, co
 int32_t gp_layout_destroy(gp_layout *L) {
     API_BEGIN
     if (!L) return GP_OK;
-    drop_graphs(L);
-    if (L->st) cudaStreamSynchronize(L->st);
-    L->call.release();
-    if (L->st_copy) cudaStreamSynchronize(L->st_copy);
-    L->traj_arena.release();
-    L->fault_arena.release();
-    L->iters_arena.release();
-    L->dc_arena.release();
-    L->trip_arena.release();
-    L->arena.release();
-    if (L->h_flag) cudaFreeHost(L->h_flag);
-    if (L->h_dt) cudaFreeHost(L->h_dt);
-    for (int i = 0; i < 8; i++)
-        if (L->pev[i]) cudaEventDestroy(L->pev[i]);
-    if (L->st) cudaStreamDestroy(L->st);
-    if (L->st_copy) cudaStreamDestroy(L->st_copy);
-    if (L->ev_snap) cudaEventDestroy(L->ev_snap);
-    delete L;
+    DeviceScope dev(L);
+    free_layout(L);
     API_END
 }
 
@@ -1756,9 +1800,8 @@ int32_t gp_layout_stats(const gp_layout *L, int64_t out[8]) {
     API_BEGIN
     if (!L || !out) fail(GP_E_INVALID, "null argument");
     const gp::Symbolic &s = L->sym;
-    int64_t nnz_s = 0;
     out[0] = L->n_red;
-    out[1] = nnz_s;
+    out[1] = L->nnz_s;
     out[2] = s.nnz_lu;
     out[3] = s.nsup;
     out[4] = s.nlevels;
@@ -1771,13 +1814,15 @@ int32_t gp_layout_stats(const gp_layout *L, int64_t out[8]) {
 int32_t gp_set_state(gp_layout *L, const double *z) {
     API_BEGIN
     if (!L || !z) fail(GP_E_INVALID, "null argument");
-    ck(cudaMemcpy(L->W.z, z, (size_t)L->M * L->n_sys * sizeof(double), cudaMemcpyHostToDevice), "set state");
+    DeviceScope dev(L);
+    to_device(L, L->W.z, z, (size_t)L->M * L->n_sys * sizeof(double), "set state");
     API_END
 }
 
 int32_t gp_restore_initial_state(gp_layout *L) {
     API_BEGIN
     if (!L) fail(GP_E_INVALID, "null argument");
+    DeviceScope dev(L);
     ck(cudaMemcpyAsync(L->W.z, L->z_init, (size_t)L->M * L->n_sys * sizeof(double), cudaMemcpyDeviceToDevice,
                        L->st),
        "restore state");
@@ -1788,7 +1833,8 @@ int32_t gp_restore_initial_state(gp_layout *L) {
 int32_t gp_get_state(const gp_layout *L, double *z) {
     API_BEGIN
     if (!L || !z) fail(GP_E_INVALID, "null argument");
-    ck(cudaMemcpy(z, L->W.z, (size_t)L->M * L->n_sys * sizeof(double), cudaMemcpyDeviceToHost), "get state");
+    DeviceScope dev(L);
+    to_host(L, z, L->W.z, (size_t)L->M * L->n_sys * sizeof(double), "get state");
     API_END
 }
 
@@ -1796,6 +1842,7 @@ int32_t gp_residual(gp_layout *L, const double *zold, double dt, int32_t n_fault
                     const uint8_t *fault_on, double *f) {
     API_BEGIN
     if (!L || !zold || !f) fail(GP_E_INVALID, "null argument");
+    DeviceScope dev(L);
     set_faults(L, n_faults, faults);
     // expanded fault status from the per-input flags
     {
@@ -1803,20 +1850,20 @@ int32_t gp_residual(gp_layout *L, const double *zold, double dt, int32_t n_fault
         for (int m = 0; m < L->M; m++)
             for (int e = 0; e < n_faults; e++)
                 if (faults[e].scenario < 0 || faults[e].scenario == m) on.push_back(fault_on ? fault_on[e] : 0);
-        if (!on.empty()) ck(cudaMemcpy(L->d_fl_on, on.data(), on.size(), cudaMemcpyHostToDevice), "fault flags");
+        if (!on.empty()) to_device(L, L->d_fl_on, on.data(), on.size(), "fault flags");
     }
     const size_t n = (size_t)L->M * L->n_sys;
-    ck(cudaMemcpy(L->W.zold, zold, n * sizeof(double), cudaMemcpyHostToDevice), "zold");
+    to_device(L, L->W.zold, zold, n * sizeof(double), "zold");
     *L->h_dt = dt;
-    ck(cudaMemcpy(L->W.dt, L->h_dt, sizeof(double), cudaMemcpyHostToDevice), "dt");
-    ck(cudaMemset(L->W.active, 1, L->M), "memset");
+    to_device(L, L->W.dt, L->h_dt, sizeof(double), "dt");
+    fill(L, L->W.active, 1, L->M);
     const gp::DevMixed exact{};
     gp::launch_reset_norm(L->P, L->W, exact, L->st);
     gp::launch_cluster(L->P, L->W, L->C, exact, 1, L->st);
     gp::launch_network(L->P, L->W, exact, 1, L->st);
     ck(cudaGetLastError(), "residual launch");
     ck(cudaStreamSynchronize(L->st), "residual");
-    ck(cudaMemcpy(f, L->W.f, n * sizeof(double), cudaMemcpyDeviceToHost), "residual copy");
+    to_host(L, f, L->W.f, n * sizeof(double), "residual copy");
     API_END
 }
 
@@ -1824,6 +1871,7 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
                      int32_t *iters, int32_t *status) {
     API_BEGIN
     if (!L || !opt) fail(GP_E_INVALID, "null argument");
+    DeviceScope dev(L);
     if (opt->n_steps < 0 || !(opt->dt > 0.0) || opt->itermax <= 0) fail(GP_E_INVALID, "bad options");
     if (opt->solver != GP_SOLVER_SCHUR_FP64 && opt->solver != GP_SOLVER_SCHUR_MIXED &&
         opt->solver != GP_SOLVER_SHARED_WOODBURY)
@@ -1903,6 +1951,18 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
                              nsys * sizeof(double), M, cudaMemcpyDeviceToHost, L->st_copy),
            "trajectory copy");
     };
+    // line trips and device disconnections end with the call, also when it
+    // fails part way (the success path resets them before its last sync)
+    struct EventReset {
+        gp_layout *L;
+        bool armed = true;
+        ~EventReset() {
+            if (!armed) return;
+            if (L->n_tr > 0) cudaMemsetAsync(L->d_tr_on, 0, L->n_tr, L->st);
+            if (L->n_dc > 0) cudaMemsetAsync(L->d_dc_flags, 0, L->dc_bytes, L->st);
+            cudaStreamSynchronize(L->st);
+        }
+    } reset{L};
     // the copy stream ends before the call returns, on every path
     struct CopyJoin {
         cudaStream_t s;
@@ -1977,6 +2037,7 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
     // (gp_residual and the next call see the intact system)
     if (L->n_tr > 0) ck(cudaMemsetAsync(L->d_tr_on, 0, L->n_tr, L->st), "memset");
     if (L->n_dc > 0) ck(cudaMemsetAsync(L->d_dc_flags, 0, L->dc_bytes, L->st), "memset");
+    reset.armed = false;
     ck(cudaStreamSynchronize(L->st), "integrate");
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
@@ -1986,17 +2047,16 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
     if (!L->profiling) harvest_counts(L);
     {
         int err = 0;
-        ck(cudaMemcpy(&err, L->D.err, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
+        to_host(L, &err, L->D.err, sizeof(int), "error flag");
         if (err) fail(GP_E_TIMEOUT, "a dataflow wait of the reduced-system solve ran out its iteration limit");
     }
     if (stream_traj) {
         join.on = false;
         ck(cudaStreamSynchronize(L->st_copy), "trajectory copy");
     } else if (traj)
-        ck(cudaMemcpy(traj, d_traj, (size_t)M * (ns + 1) * nsys * sizeof(double), cudaMemcpyDeviceToHost),
-           "trajectory copy");
+        to_host(L, traj, d_traj, (size_t)M * (ns + 1) * nsys * sizeof(double), "trajectory copy");
     std::vector<int> hi((size_t)2 * std::max(ns, 1) * M);
-    ck(cudaMemcpy(hi.data(), d_iters, hi.size() * sizeof(int), cudaMemcpyDeviceToHost), "iters copy");
+    to_host(L, hi.data(), d_iters, hi.size() * sizeof(int), "iters copy");
     double tot = 0.0;
     for (int m = 0; m < M; m++) {
         double s = 0.0;
@@ -2008,7 +2068,7 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
         tot = std::max(tot, s);
     }
     L->iters_total = tot;
-    if (status) ck(cudaMemcpy(status, L->W.status, M * sizeof(int), cudaMemcpyDeviceToHost), "status copy");
+    if (status) to_host(L, status, L->W.status, M * sizeof(int), "status copy");
     ck(cudaGetLastError(), "integrate");
     API_END
 }
@@ -2131,8 +2191,9 @@ int32_t gp_adjoint(gp_layout *L, const gp_options *opt, int32_t n_faults, const 
                    const gp_objective *obj, int32_t checkpoint_every, double *J, double *grad_p, double *grad_z0,
                    int32_t *status) {
     API_BEGIN
-    using namespace gp;
     if (!L || !opt || !obj) fail(GP_E_INVALID, "null argument");
+    DeviceScope dev(L);
+    using namespace gp;
     if (opt->n_steps < 1 || !(opt->dt > 0.0) || opt->itermax <= 0 || checkpoint_every < 1)
         fail(GP_E_INVALID, "bad options");
     if (opt->solver != GP_SOLVER_SCHUR_FP64) fail(GP_E_INVALID, "the adjoint runs on the FP64 Schur path");
@@ -2187,7 +2248,7 @@ int32_t gp_adjoint(gp_layout *L, const gp_options *opt, int32_t n_faults, const 
     ck(cudaMemcpyAsync(zfin, L->W.z, blk * sizeof(double), cudaMemcpyDeviceToDevice, L->st), "final state");
     if (status) {
         ck(cudaStreamSynchronize(L->st), "forward");
-        ck(cudaMemcpy(status, L->W.status, M * sizeof(int), cudaMemcpyDeviceToHost), "status copy");
+        to_host(L, status, L->W.status, M * sizeof(int), "status copy");
     }
     // ---- backward sweep ----
     DevAdj A{};
@@ -2253,19 +2314,20 @@ int32_t gp_adjoint(gp_layout *L, const gp_options *opt, int32_t n_faults, const 
     if (!L->profiling) harvest_counts(L);
     {
         int err = 0;
-        ck(cudaMemcpy(&err, L->D.err, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
+        to_host(L, &err, L->D.err, sizeof(int), "error flag");
         if (err) fail(GP_E_TIMEOUT, "a dataflow wait of the reduced-system solve ran out its iteration limit");
     }
-    if (J) ck(cudaMemcpy(J, A.J, M * sizeof(double), cudaMemcpyDeviceToHost), "J copy");
+    if (J) to_host(L, J, A.J, M * sizeof(double), "J copy");
     if (grad_p && L->n_par > 0)
-        ck(cudaMemcpy(grad_p, A.grad, (size_t)M * L->n_par * sizeof(double), cudaMemcpyDeviceToHost), "grad copy");
-    if (grad_z0) ck(cudaMemcpy(grad_z0, A.g, blk * sizeof(double), cudaMemcpyDeviceToHost), "grad z0 copy");
+        to_host(L, grad_p, A.grad, (size_t)M * L->n_par * sizeof(double), "grad copy");
+    if (grad_z0) to_host(L, grad_z0, A.g, blk * sizeof(double), "grad z0 copy");
     API_END
 }
 
 int32_t gp_set_mixed_policy(gp_layout *L, int32_t max_age, double rho_max, int32_t exact_after, int32_t predict) {
     API_BEGIN
     if (!L) fail(GP_E_INVALID, "null argument");
+    DeviceScope dev(L);
     if (max_age < 1 || !(rho_max > 0.0) || exact_after < 1 || predict < 0 || predict > 3)
         fail(GP_E_INVALID, "bad mixed-solver policy");
     L->mx_predict = predict;
@@ -2298,6 +2360,7 @@ std::pair<int, int> front_entry(const gp::Symbolic &sym, int r, int c) {
 int32_t gp_set_line_trips(gp_layout *L, int32_t n, const gp_line_trip *trips) {
     API_BEGIN
     if (!L || (n > 0 && !trips) || n < 0) fail(GP_E_INVALID, "bad arguments");
+    DeviceScope dev(L);
     if (n == 0 && L->n_tr == 0 && L->P.tr_ptr) return GP_OK;
     const int M = L->M;
     std::vector<std::vector<int>> per(M);
@@ -2367,7 +2430,7 @@ int32_t gp_set_line_trips(gp_layout *L, int32_t n, const gp_line_trip *trips) {
     L->P.tr_to = up_i(tb);
     L->P.tr_y = A.upload(y.empty() ? std::vector<double>{0.0} : y);
     L->d_tr_on = A.alloc<uint8_t>(std::max(1, L->n_tr));
-    ck(cudaMemset(L->d_tr_on, 0, std::max(1, L->n_tr)), "memset");
+    fill(L, L->d_tr_on, 0, std::max(1, L->n_tr));
     L->P.tr_on = L->d_tr_on;
     L->d_tr_on_step = up_i(on);
     L->d_tr_off_step = up_i(off);
@@ -2392,8 +2455,10 @@ int32_t gp_initialize(gp_layout *L, const double *v_polar, const double *gen_pq,
     API_BEGIN
     if (!L || !v_polar || (!gen_pq && L->h_ntab[GP_GENROU] > 0) || (!sg_pq && L->h_ntab[GP_STATIC_GEN] > 0))
         fail(GP_E_INVALID, "null argument");
+    DeviceScope dev(L);
     const size_t M = L->M;
     DeviceArena A;
+    A.st = L->st;
     struct Release {
         DeviceArena &a;
         ~Release() { a.release(); }
@@ -2411,9 +2476,9 @@ int32_t gp_initialize(gp_layout *L, const double *v_polar, const double *gen_pq,
     int bad = 0;
     ck(cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, L->st), "status copy");
     ck(cudaStreamSynchronize(L->st), "initialise");
-    if (z0) ck(cudaMemcpy(z0, L->W.z, M * L->n_sys * sizeof(double), cudaMemcpyDeviceToHost), "state copy");
-    if (u0) ck(cudaMemcpy(u0, L->W.u0, M * L->n_ctrl * sizeof(double), cudaMemcpyDeviceToHost), "control copy");
-    if (p) ck(cudaMemcpy(p, L->W.p, M * L->n_par * sizeof(double), cudaMemcpyDeviceToHost), "parameter copy");
+    if (z0) to_host(L, z0, L->W.z, M * L->n_sys * sizeof(double), "state copy");
+    if (u0) to_host(L, u0, L->W.u0, M * L->n_ctrl * sizeof(double), "control copy");
+    if (p) to_host(L, p, L->W.p, M * L->n_par * sizeof(double), "parameter copy");
     if (bad) fail(GP_E_NUMERIC, "%d machine initialisation(s) left a residual of 1e-9 or more", bad);
     API_END
 }
@@ -2421,6 +2486,7 @@ int32_t gp_initialize(gp_layout *L, const double *v_polar, const double *gen_pq,
 int32_t gp_set_device_disconnects(gp_layout *L, int32_t n, const gp_device_disconnect *events) {
     API_BEGIN
     if (!L || (n > 0 && !events) || n < 0) fail(GP_E_INVALID, "bad arguments");
+    DeviceScope dev(L);
     if (n == 0 && L->n_dc == 0) return GP_OK;
     const int M = L->M, nzl = L->h_ntab[GP_ZIPLOAD], nsg = L->h_ntab[GP_STATIC_GEN], ncl = L->P.n_cl;
     // flag areas: ZIP loads, static generators, cluster exciters
@@ -2469,7 +2535,7 @@ int32_t gp_set_device_disconnects(gp_layout *L, int32_t n, const gp_device_disco
         auto up_i = [&](const std::vector<int> &v) { return A.upload(v); };
         L->dc_bytes = bytes;
         L->d_dc_flags = A.alloc<uint8_t>(std::max<size_t>(1, bytes));
-        ck(cudaMemset(L->d_dc_flags, 0, std::max<size_t>(1, bytes)), "memset");
+        fill(L, L->d_dc_flags, 0, std::max<size_t>(1, bytes));
         L->d_dc_on_step = up_i(on);
         L->d_dc_scen = up_i(scen);
         L->d_dc_idx = up_i(idx);
@@ -2486,9 +2552,21 @@ int32_t gp_set_device_disconnects(gp_layout *L, int32_t n, const gp_device_disco
     API_END
 }
 
+int32_t gp_set_wait_limit(gp_layout *L, int32_t polls) {
+    API_BEGIN
+    if (!L || polls < 1) fail(GP_E_INVALID, "gp_set_wait_limit: null layout or polls < 1");
+    DeviceScope dev(L);
+    if (L->D.wait_limit != polls) {
+        L->D.wait_limit = polls;
+        drop_graphs(L);   // the graphs hold the schedule by value
+    }
+    API_END
+}
+
 int32_t gp_set_profiling(gp_layout *L, int32_t on) {
     API_BEGIN
     if (!L) fail(GP_E_INVALID, "null argument");
+    DeviceScope dev(L);
     if ((on != 0) != L->profiling) {
         L->profiling = on != 0;
         drop_graphs(L);
@@ -2563,6 +2641,7 @@ struct Carver {
 extern "C" int32_t gp_residual_static(gp_layout *L, const double *zold, double dt, double *f) {
     API_BEGIN
     if (!L || !zold || !f) fail(GP_E_INVALID, "null argument");
+    DeviceScope dev(L);
     const size_t M = L->M;
     const gp::DevProblem &P0 = L->P;
     // bytes the residual needs, with the same 256-byte rounding as Carver

@@ -10,7 +10,7 @@
 // parent in the reversed order), which were claimed earlier by warps or
 // CTAs that are running, so the smallest unfinished claimed task can always
 // proceed and the kernel cannot deadlock.  Every wait is bounded: after
-// kWaitLimit polls it raises the error flag, every other wait then returns
+// D.wait_limit polls it raises the error flag, every other wait then returns
 // at once, and the kernel finishes with the scenario marked in `status`.
 //
 // Factorisation, in two launches:
@@ -61,7 +61,7 @@ __device__ bool warp_wait_children(const DevSym &S, const DevDag &D, const int *
     bool ok = true;
     for (int q = lane; q < nc; q += 32) {
         const int c = S.children[c0 + q];
-        if (D.rank[c] >= from_rank) ok = wait_epoch(done + (size_t)c * M + m, epoch, D.err) && ok;
+        if (D.rank[c] >= from_rank) ok = wait_epoch(done + (size_t)c * M + m, epoch, D.err, D.wait_limit) && ok;
     }
     ok = __all_sync(FULL, ok);
     __syncwarp();

@@ -163,6 +163,7 @@ struct DevDag {
     int *epoch;             // [1] current solve
     int *err;               // [1] a wait gave up (sticky until the host clears it)
     int *fdone, *xdone, *bdone;   // [nsup][M] epoch at which the task finished
+    int wait_limit = 1 << 20;     // polls before a wait gives up (gp_set_wait_limit)
 };
 
 struct DagGrid {

@@ -514,7 +514,7 @@ __device__ bool wait_top_children(const DevSym &S, const DevBlk &B, const DevDag
         bool ok = true;
         for (int q = lane; q < nc; q += 32) {
             const int c = S.children[c0 + q];
-            ok = wait_epoch(D.xdone + (size_t)c * M + m, epoch, D.err) && ok;
+            ok = wait_epoch(D.xdone + (size_t)c * M + m, epoch, D.err, D.wait_limit) && ok;
         }
         ok = __all_sync(FULL, ok);
         if (lane == 0) *s_ok = ok;
@@ -525,7 +525,7 @@ __device__ bool wait_top_children(const DevSym &S, const DevBlk &B, const DevDag
 
 __device__ bool wait_top_parent(const DevDag &D, int s, int m, int M, int epoch, int *s_ok) {
     const int par = D.parent[s];
-    if (threadIdx.x == 0) *s_ok = par < 0 ? 1 : (int)wait_epoch(D.bdone + (size_t)par * M + m, epoch, D.err);
+    if (threadIdx.x == 0) *s_ok = par < 0 ? 1 : (int)wait_epoch(D.bdone + (size_t)par * M + m, epoch, D.err, D.wait_limit);
     __syncthreads();
     return *s_ok != 0;
 }
@@ -768,7 +768,7 @@ __global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P,
                 prefetch_block<float, 16>(S, fs, bt, m, false);
                 if (par >= 0) {
                     bool ok = true;
-                    if ((threadIdx.x & 15) == 0) ok = wait_epoch(D.bdone + (size_t)par * M + m, epoch, D.err);
+                    if ((threadIdx.x & 15) == 0) ok = wait_epoch(D.bdone + (size_t)par * M + m, epoch, D.err, D.wait_limit);
                     ok = __shfl_sync(FULL, ok, threadIdx.x & 16);
                     if (!ok && (threadIdx.x & 15) == 0) atomicOr(W.status + m, 8);
                 }
@@ -788,7 +788,7 @@ __global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P,
             else prefetch_block<float>(S, fs, bt, m, false);
             if (par >= 0) {
                 bool ok = true;
-                if (lane == 0) ok = wait_epoch(D.bdone + (size_t)par * M + m, epoch, D.err);
+                if (lane == 0) ok = wait_epoch(D.bdone + (size_t)par * M + m, epoch, D.err, D.wait_limit);
                 ok = __shfl_sync(FULL, ok, 0);
                 if (!ok && lane == 0) atomicOr(W.status + m, 8);
             }

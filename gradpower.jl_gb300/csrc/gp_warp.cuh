@@ -9,10 +9,9 @@ constexpr unsigned kFullMask = 0xffffffffu;
 // ---- flags between tasks of one persistent kernel ----------------------
 // A task signals completion by storing the current epoch (release); a
 // waiting task polls with relaxed loads and acquires on success.  Every wait
-// is bounded: after kWaitLimit polls it raises the error flag and gives up,
-// and every other wait then returns at once, so the kernel always ends.
-
-constexpr int kWaitLimit = 1 << 20;
+// is bounded: after `limit` polls (DevDag::wait_limit, 2^20 unless the host
+// sets another) it raises the error flag and gives up, and every other wait
+// then returns at once, so the kernel always ends.
 
 __device__ __forceinline__ int ld_relaxed(const int *p) {
     int v;
@@ -29,8 +28,8 @@ __device__ __forceinline__ void st_release(int *p, int v) {
 // Waits until *flag == epoch; false when it gave up (error flag raised here
 // or by another task).  The error flag is read every 32nd poll only, so that
 // a poll is one load on the path between a signal and its waiter.
-__device__ inline bool wait_epoch(const int *flag, int epoch, int *err) {
-    for (int it = 0; it < kWaitLimit; ++it) {
+__device__ inline bool wait_epoch(const int *flag, int epoch, int *err, int limit) {
+    for (int it = 0; it < limit; ++it) {
         if (ld_relaxed(flag) == epoch) {
             fence_acquire();
             return true;

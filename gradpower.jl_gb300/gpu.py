@@ -55,6 +55,7 @@ def library():
         L.gp_residual_static.argtypes = [vp, vp, C.c_double, vp]
         L.gp_set_mixed_policy.argtypes = [vp, C.c_int32, C.c_double, C.c_int32, C.c_int32]
         L.gp_set_profiling.argtypes = [vp, C.c_int32]
+        L.gp_set_wait_limit.argtypes = [vp, C.c_int32]
         L.gp_set_line_trips.argtypes = [vp, C.c_int32, vp]
         L.gp_set_device_disconnects.argtypes = [vp, C.c_int32, vp]
         L.gp_initialize.argtypes = [vp] * 7
@@ -62,7 +63,8 @@ def library():
         for f in ("gp_layout_create", "gp_layout_destroy", "gp_layout_stats", "gp_set_state",
                   "gp_get_state", "gp_integrate", "gp_residual", "gp_last_timing",
                   "gp_restore_initial_state", "gp_reduced_selftest", "gp_cluster_selftest",
-                  "gp_residual_static", "gp_set_mixed_policy", "gp_set_profiling", "gp_set_line_trips",
+                  "gp_residual_static", "gp_set_mixed_policy", "gp_set_profiling", "gp_set_wait_limit",
+                  "gp_set_line_trips",
                   "gp_set_device_disconnects", "gp_initialize", "gp_adjoint"):
             getattr(L, f).restype = C.c_int32
         _lib = L
@@ -161,6 +163,12 @@ class GpuBatchedLayout:
         include/gradpower_gb300.h); predict: degree of the extrapolated first
         iterate of a step, 0 (none) to 3 (cubic)."""
         _check(library().gp_set_mixed_policy(self._h, int(max_age), float(rho_max), int(exact_after), int(predict)))
+
+    def set_wait_limit(self, polls: int = 1 << 20):
+        """Polls after which a dataflow wait gives up (see gp_set_wait_limit
+        in include/gradpower_gb300.h); the call then raises GradPowerError
+        with GP_E_TIMEOUT and the waiting scenarios get status bit 8."""
+        _check(library().gp_set_wait_limit(self._h, int(polls)))
 
     def set_profiling(self, on: bool = True):
         """Host-driven Newton loop with CUDA events around every phase (for

@@ -295,6 +295,16 @@ int32_t gp_residual(gp_layout *L, const double *zold, double dt, int32_t n_fault
  * (src/schur.jl:285, `for iter = 1:itermax`). */
 int32_t gp_set_profiling(gp_layout *L, int32_t on);
 
+/* Polls (at about 32 ns each) after which a wait of the dataflow kernels on
+ * another task's done flag gives up (default 2^20, about 30 ms): the kernel
+ * then raises an error flag, every other wait returns at once, the kernel
+ * finishes, the waiting scenario gets status bit 8 and the call returns
+ * GP_E_TIMEOUT.  The next call clears the flag and starts afresh.  polls >=
+ * 1; GP_E_INVALID otherwise.  No counterpart in the reference (cuDSS has no
+ * such wait); a failure-detection hook: a tiny limit makes the waits run
+ * out without anything on the GPU hanging. */
+int32_t gp_set_wait_limit(gp_layout *L, int32_t polls);
+
 /* Time of the last gp_integrate call split by phase, milliseconds between
  * CUDA events recorded on the library's stream inside the captured graphs
  * (the phases only with profiling on, gp_set_profiling; zero otherwise):
@@ -368,14 +378,21 @@ int32_t gp_adjoint(gp_layout *L, const gp_options *opt, int32_t n_faults, const 
  * Defaults: max_age 1, rho_max 0.9, exact_after 8, predict 3. */
 int32_t gp_set_mixed_policy(gp_layout *L, int32_t max_age, double rho_max, int32_t exact_after, int32_t predict);
 
-/* gp_residual with no fault applied, computed without allocating anything:
- * its scratch (zold, residual, cluster and network intermediates) lives in
- * one file-scope 16 MiB device array instead of the layout's buffers.
+/* gp_residual with no fault applied, computed without allocating anything,
+ * for callers that may not call cudaMalloc or cudaFree: a host whose device
+ * memory is all handed out by its own pool allocator, or a loop in which the
+ * implicit device synchronisation of those calls is not allowed.  Its
+ * scratch (zold, residual, cluster and network intermediates) lives in one
+ * file-scope 16 MiB device array instead of the layout's buffers.
  * f[M][n_sys] as gp_residual(L, zold, dt, 0, NULL, NULL, f).  Returns
- * GP_E_INVALID when M * (about 3 n_sys + 3 n_diff + 3 n_alg + 8 clusters +
- * n_var) doubles exceed the 16 MiB.  The first call on a device looks up the
- * array's address: make it before any stream capture.  The array is shared
- * by every layout on the device, so overlapping calls race.
+ * GP_E_INVALID when the scratch, 8 M (2 n_sys + 3 (n_diff + n_alg) +
+ * 8 machine clusters + n_var + n_red) bytes plus a few small arrays, each
+ * rounded up to 256 bytes, exceeds the 16 MiB (n_var: the scenario-varying
+ * entries of S, 4 per bus plus 4 or 6 per PV or slack static generator;
+ * n_red: 2 per bus plus the static generators' algebraic states).  The first
+ * call on a device looks up the array's address: make it before any stream
+ * capture.  The array is shared by every layout on the device and keeps
+ * the last call's contents, so overlapping calls race.
  * No counterpart in the reference. */
 int32_t gp_residual_static(gp_layout *L, const double *zold, double dt, double *f);
 

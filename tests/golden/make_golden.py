@@ -1,7 +1,7 @@
 """Generate the golden fixtures of this directory from the reference tree.
 
-Run in a container that has the reference checked out (default path
-/root/reference, override with GRADPOWER_REFERENCE).  Outputs, all JSON:
+Run where the reference is checked out, with its root given as the first
+argument or in GRADPOWER_REFERENCE.  Outputs, all JSON:
 
   cases.json      the reference's example cases (examples/2bus*.raw|dyr,
                   ieee9_v33.raw + ieee9bus*.dyr, IEEE39.raw + IEEE39*.dyr,
@@ -23,7 +23,7 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("GRADPOWER_REFERENCE", "/root/reference")
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GRADPOWER_REFERENCE", "")
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 
@@ -103,6 +103,8 @@ def known():
 
 
 if __name__ == "__main__":
+    if not REF or not os.path.isdir(REF):
+        sys.exit("usage: make_golden.py REFERENCE_ROOT (or set GRADPOWER_REFERENCE)")
     psse = _load_psse()
     with open(os.path.join(HERE, "cases.json"), "w") as f:
         json.dump(cases(psse), f)

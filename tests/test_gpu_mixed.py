@@ -61,14 +61,18 @@ def test_mixed_psse_cases_against_oracle(G, orc, golden_cases, raw, dyr):
 
 
 def test_mixed_ring39_against_oracle(G, orc):
-    c, w = synthetic_case("ring39", 16)
+    """All 64 ring39 scenarios; 2 and 12 have no backward-Euler solution at
+    one step of their fault (tests/test_ring39_no_solution.py): the mixed
+    solver retries those solves with exact steps and reports them as the
+    FP64 path does (status 1)."""
+    c, w = synthetic_case("ring39", 64)
     g = _run(G, c, 120, LY.SOLVER_SCHUR_MIXED)
     o = run_oracle(orc, c, 120, itermax=30, nthreads=8)
     ok = o["status"] == 0
-    assert ok.sum() >= 12
-    assert np.all(g["status"][ok] == 0)
+    assert np.array_equal(np.where(~ok)[0], [2, 12])
+    assert np.array_equal(g["status"] != 0, ~ok) and np.all(g["status"][~ok] & 1)
     assert max(_errors(c.PA, g["traj"][ok], o["traj"][ok])) <= TOL
-    assert g["timing"]["refreshes"] > 0
+    assert g["timing"]["refreshes"] > 0 and g["timing"]["retries"] > 0
 
 
 def test_mixed_planar2k_against_oracle(G, orc):

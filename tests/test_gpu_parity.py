@@ -34,14 +34,23 @@ def _gpu_run(G, c, nsteps, itermax=30, dt=DT):
     return r
 
 
-def _parity(G, orc, c, nsteps, itermax=30):
+def _parity(G, orc, c, nsteps, itermax=30, nthreads=1):
+    """Same status per scenario; converged scenarios: identical Newton
+    iteration counts and trajectories within RTOL; unconverged ones: the
+    same up to the first solve that ran out of iterations (the iterate it
+    leaves behind is not a solution, and the two need not agree after it)."""
     g = _gpu_run(G, c, nsteps, itermax)
-    o = run_oracle(orc, c, nsteps, itermax=itermax)
+    o = run_oracle(orc, c, nsteps, itermax=itermax, nthreads=nthreads)
     assert np.array_equal(g["status"], o["status"])
     ok = o["status"] == 0
     assert np.array_equal(g["iters"][ok], o["iters"][ok])
     if ok.any():
         assert _close(g["traj"][ok], o["traj"][ok]) <= RTOL
+    for m in np.where(~ok)[0]:
+        q = int(np.argmax(o["iters"][m] >= itermax))     # first solve that ran out
+        assert o["iters"][m][q] >= itermax and np.array_equal(g["iters"][m][:q + 1], o["iters"][m][:q + 1])
+        k = q // 2                                       # states before that step's solve
+        assert _close(g["traj"][m][:k + 1], o["traj"][m][:k + 1]) <= RTOL
     return g, o
 
 
@@ -102,10 +111,13 @@ def test_uqgrid_golden_trajectory_on_gpu(G, golden_cases, golden_known):
 
 
 def test_ring39_all_scenarios(G, orc):
-    """39-bus batch, M=64, one seeded fault bus per scenario, 1 s."""
+    """39-bus batch, M=64, one seeded fault bus per scenario, 1 s.  Scenarios
+    2 and 12 have no backward-Euler solution at one step of their fault (the
+    voltage collapses: tests/test_ring39_no_solution.py shows it on the CPU);
+    both paths report status 1 there and agree up to that step."""
     c, w = synthetic_case("ring39", 64)
-    g, o = _parity(G, orc, c, 120)
-    assert (o["status"] == 0).mean() > 0.9
+    g, o = _parity(G, orc, c, 120, nthreads=8)
+    assert np.array_equal(np.where(o["status"] != 0)[0], [2, 12])
 
 
 def test_planar2k_batch(G, orc):
@@ -114,7 +126,8 @@ def test_planar2k_batch(G, orc):
 
 
 def test_planar70k_short(G, orc):
-    """The 70,000-bus grid, two scenarios, 15 steps around the fault onset."""
+    """The 70,000-bus grid, two scenarios, 15 steps around the fault onset
+    (the whole horizon is in test_gpu_configs.py)."""
     c, w = synthetic_case("planar70k", 2)
     _parity(G, orc, c, 15)
 
