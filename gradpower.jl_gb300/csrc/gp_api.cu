@@ -2048,7 +2048,11 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
     {
         int err = 0;
         to_host(L, &err, L->D.err, sizeof(int), "error flag");
-        if (err) fail(GP_E_TIMEOUT, "a dataflow wait of the reduced-system solve ran out its iteration limit");
+        if (err) {
+            // the status words still say which scenarios' waits gave up (bit 8)
+            if (status) to_host(L, status, L->W.status, M * sizeof(int), "status copy");
+            fail(GP_E_TIMEOUT, "a dataflow wait of the reduced-system solve ran out its iteration limit");
+        }
     }
     if (stream_traj) {
         join.on = false;
@@ -2315,7 +2319,11 @@ int32_t gp_adjoint(gp_layout *L, const gp_options *opt, int32_t n_faults, const 
     {
         int err = 0;
         to_host(L, &err, L->D.err, sizeof(int), "error flag");
-        if (err) fail(GP_E_TIMEOUT, "a dataflow wait of the reduced-system solve ran out its iteration limit");
+        if (err) {
+            // the status words still say which scenarios' waits gave up (bit 8)
+            if (status) to_host(L, status, L->W.status, M * sizeof(int), "status copy");
+            fail(GP_E_TIMEOUT, "a dataflow wait of the reduced-system solve ran out its iteration limit");
+        }
     }
     if (J) to_host(L, J, A.J, M * sizeof(double), "J copy");
     if (grad_p && L->n_par > 0)

@@ -303,7 +303,8 @@ def ring39(seed=1, n_scenarios=64):
                          "TGOV1 VMAX=1.2, VMIN=0, DT=0 (not enforced by the model)"])
 
 
-def _planar(name, seed, n_bus, n_gen, load_frac, n_scenarios, tf, fault_mode):
+def _planar(name, seed, n_bus, n_gen, load_frac, n_scenarios, tf, fault_mode, b_range=(0.0, 0.0),
+            load_range=(0.005, 0.03), extra_notes=()):
     rng = np.random.default_rng(seed)
     edges, pts = planar_graph(rng, n_bus)
     # Machines are spread evenly: one per cell of a square grid laid over the
@@ -327,7 +328,7 @@ def _planar(name, seed, n_bus, n_gen, load_frac, n_scenarios, tf, fault_mode):
     rest = [b for b in rest if b not in gset]
     n_load = int(round(load_frac * n_bus))
     load_buses = rest[:n_load]
-    load_p = rng.uniform(0.005, 0.03, size=n_load)
+    load_p = rng.uniform(*load_range, size=n_load)
     machines = []
     kinds = rng.random((n_gen, 4))
     for k, bus in enumerate(gen_buses):
@@ -348,7 +349,7 @@ def _planar(name, seed, n_bus, n_gen, load_frac, n_scenarios, tf, fault_mode):
     else:
         fault_buses = rng.choice(n_bus, size=n_scenarios, replace=n_scenarios > n_bus)
     return _build(name, rng, n_bus, edges, gen_buses, load_buses, load_p, machines,
-                  (0.0, 0.0), pv_v=(1.0, 1.0), M_scen=n_scenarios, tf=tf,
+                  b_range, pv_v=(1.0, 1.0), M_scen=n_scenarios, tf=tf,
                   fault_buses=fault_buses,
                   notes=["planar graph: Delaunay MST + shortest Delaunay edges to mean degree 2.7",
                          "load P ~ U[0.005, 0.03] pu with Q = 0.3 P (per-bus size not fixed by the benchmark; "

@@ -271,8 +271,10 @@ int32_t gp_set_device_disconnects(gp_layout *L, int32_t n, const gp_device_disco
  *   traj    [M][n_steps+1][n_sys] host output, or NULL
  *   iters   [M][2*n_steps] Newton iterations: slot 2k the step solve of
  *           step k+1, slot 2k+1 its event re-solve (0 if none); or NULL
- *   status  [M] 0 converged everywhere, 1 some solve hit itermax,
- *           2 non-finite values; or NULL
+ *   status  [M] bit flags, 0 = converged everywhere: 1 some solve hit
+ *           itermax, 2 non-finite values, 4 a zero pivot in the reduced
+ *           matrix, 8 a dataflow wait gave up (the call then returns
+ *           GP_E_TIMEOUT, with status still filled); or NULL
  * On return the layout holds the final state. */
 int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults,
                      const gp_fault *faults, double *traj, int32_t *iters,

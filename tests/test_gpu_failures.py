@@ -47,7 +47,7 @@ def test_wait_limit_runs_out_and_layout_recovers(G, orc, solver):
     gbl = G.GpuBatchedLayout(c.dp, c.ps, c.M)
     try:
         gbl.set_wait_limit(1)
-        rc, status = _integrate_raw(G, gbl, c, 4, solver)
+        rc, status = _integrate_raw(G, gbl, c, 16, solver)   # past the fault at step 12
         assert rc == GP_E_TIMEOUT
         assert np.any(status & 8)
         buf = C.create_string_buffer(512)

@@ -111,13 +111,16 @@ def test_uqgrid_golden_trajectory_on_gpu(G, golden_cases, golden_known):
 
 
 def test_ring39_all_scenarios(G, orc):
-    """39-bus batch, M=64, one seeded fault bus per scenario, 1 s.  Scenarios
-    2 and 12 have no backward-Euler solution at one step of their fault (the
-    voltage collapses: tests/test_ring39_no_solution.py shows it on the CPU);
-    both paths report status 1 there and agree up to that step."""
+    """39-bus batch, M=64, one seeded fault bus per scenario, 1 s, the
+    reference's itermax of 30.  Scenarios 2, 12 and 35 run out of Newton
+    iterations at one step of their fault (voltage collapse under the fault:
+    tests/test_ring39_no_solution.py shows on the CPU that 2 and 12 have no
+    solution near the previous state, and that 35 needs 31 to 50
+    iterations); both paths report status 1 there and agree up to that
+    step."""
     c, w = synthetic_case("ring39", 64)
     g, o = _parity(G, orc, c, 120, nthreads=8)
-    assert np.array_equal(np.where(o["status"] != 0)[0], [2, 12])
+    assert np.array_equal(np.where(o["status"] != 0)[0], [2, 12, 35])
 
 
 def test_planar2k_batch(G, orc):
