@@ -117,3 +117,65 @@ def test_adjoint_planar2k_against_fd_and_checkpoints(G):
         g = r["grad_p"][m, pick]
         err = np.abs(g - fd) / np.abs(fd)
         assert np.max(err) <= 1e-5, (m, list(zip(pick.tolist(), g.tolist(), fd.tolist(), err.tolist())))
+
+
+def test_adjoint_differentiation_workload_against_fd(G):
+    """The differentiation workload as stated: the 2,000-bus grid over 3 s
+    (360 steps), checkpoints every 60 steps, objective
+    sum dt (sum w^2 + 10 sum max(0, 0.9 - |V|)^2).  Twenty differentiated
+    parameters drawn with a fixed seed (not picked by sensitivity) against
+    central differences with step 1e-6 (relative to max(1, |p|)) of the
+    FP64 integration, two fault scenarios: relative error at most 1e-5,
+    measured against max(|fd|, 1e-4 max |gradient|) so that a parameter the
+    objective hardly depends on is held to the absolute accuracy of the
+    differences."""
+    c, w = synthetic_case("planar2k_adj", 2)
+    ns = 360
+    idx = np.array(AO.differentiated_params(c.PA))
+    pick = np.sort(np.random.default_rng(2026).choice(idx, size=20, replace=False))
+    gbl = G.GpuBatchedLayout(c.dp, c.ps, c.M)
+    try:
+        r = gbl.adjoint(ns * DT, DT, newton_tol=1e-12, scenario_faults=c.faults, w_volt=10.0, v_min=0.9,
+                        checkpoint_every=60)
+    finally:
+        gbl.close()
+    assert np.all(r["status"] == 0)
+    p0 = c.dp.pvec
+    for m in range(c.M):
+        P = np.tile(p0, (2 * len(pick), 1))
+        hs = 1e-6 * np.maximum(1.0, np.abs(p0[pick]))
+        for q, j in enumerate(pick):
+            P[2 * q, j] += hs[q]
+            P[2 * q + 1, j] -= hs[q]
+        fd_l = G.GpuBatchedLayout(c.dp, c.ps, len(P), p=P)
+        try:
+            t = fd_l.integrate(ns * DT, DT, newton_tol=1e-12, scenario_faults=[c.faults[m]] * len(P))["traj"]
+        finally:
+            fd_l.close()
+        Jv = AO.objective_of_traj(c.PA, t, DT, w_volt=10.0)
+        fd = (Jv[0::2] - Jv[1::2]) / (2 * hs)
+        g = r["grad_p"][m, pick]
+        floor = 1e-4 * np.max(np.abs(r["grad_p"][m, idx]))
+        err = np.abs(g - fd) / np.maximum(np.abs(fd), floor)
+        assert np.max(err) <= 1e-5, (m, list(zip(pick.tolist(), g.tolist(), fd.tolist(), err.tolist())))
+
+
+def test_adjoint_batch_of_128_equals_single_scenario_runs(G):
+    """One call over the 128 scenarios of the differentiation workload: the
+    gradients of three of them equal runs of those scenarios alone."""
+    c, w = synthetic_case("planar2k_adj", 128)
+    kw = dict(newton_tol=1e-10, w_volt=10.0, v_min=0.9, checkpoint_every=60)
+    gbl = G.GpuBatchedLayout(c.dp, c.ps, c.M)
+    try:
+        r = gbl.adjoint(3.0, DT, scenario_faults=c.faults, **kw)
+    finally:
+        gbl.close()
+    assert np.all(r["status"] == 0)
+    for m in (0, 57, 127):
+        one = G.GpuBatchedLayout(c.dp, c.ps, 1)
+        try:
+            r1 = one.adjoint(3.0, DT, scenario_faults=[c.faults[m]], **kw)
+        finally:
+            one.close()
+        assert abs(r1["J"][0] - r["J"][m]) <= 1e-12 * abs(r1["J"][0])
+        assert np.max(np.abs(r1["grad_p"][0] - r["grad_p"][m])) <= 1e-10 * np.max(np.abs(r1["grad_p"][0]))

@@ -6,8 +6,8 @@
   on the scenarios whose waits gave up, and the next call (default limit)
   on the same layout is exact again.
 - A non-finite parameter in one scenario: that scenario stops with status
-  bit 2 (non-finite residual), as the oracle's does; the other scenarios
-  are untouched and still match the oracle.
+  bit 2 (non-finite residual) where the oracle stops unconverged; the other
+  scenarios are untouched and still match the oracle.
 
 The reference is silent on both (src/batched.jl:459, src/numerics.jl:146-166).
 """
@@ -89,7 +89,9 @@ def test_nan_parameter_stops_only_its_scenario(G, orc, solver):
         gbl.close()
     fa, nf = c.fault_array()
     o = orc.integrate(c.PA, z, u, p, fa, nf, DT, 20, itermax=30, nthreads=4)
-    assert o["status"][1] == 2 and r["status"][1] & 2
+    # the oracle (as the reference) stops the solve unconverged; the GPU
+    # path also says why: a non-finite residual (bit 2)
+    assert o["status"][1] != 0 and r["status"][1] & 2
     good = [0, 2, 3]
     assert np.all(o["status"][good] == 0) and np.all(r["status"][good] == 0)
     err = np.max(np.abs(r["traj"][good] - o["traj"][good]) / np.maximum(1.0, np.abs(o["traj"][good])))
