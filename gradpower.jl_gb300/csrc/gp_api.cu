@@ -549,8 +549,22 @@ void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
             const int s = sym.level_sups[q];
             if (blk_of[s] >= 0) members[blk_of[s]].push_back(s);
         }
+    // blocks are emitted (and claimed by the solve kernels) longest first:
+    // one warp runs a block's supernodes one after the other, so the block
+    // phase ends with its slowest blocks, which should start first.  The
+    // estimate per supernode: a fixed cost, one step per pivot column, one
+    // per 32 factor entries
+    std::vector<double> cost(nblk, 0.0);
+    for (int b = 0; b < nblk; b++)
+        for (int s : members[b]) {
+            const double m = sym.front_m(s), n = sym.front_n(s);
+            cost[b] += 8.0 + n + m * n / 32.0;
+        }
+    std::vector<int> emit(nblk);
+    for (int b = 0; b < nblk; b++) emit[b] = b;
+    std::stable_sort(emit.begin(), emit.end(), [&](int a, int c) { return cost[a] > cost[c]; });
     std::vector<int> voff_of(ns, -1);
-    for (int b = 0; b < nblk; b++) {
+    for (int b : emit) {
         int vo = 0, mo = 0, po = 0;
         for (int s : members[b]) {
             const int m = sym.front_m(s), n = sym.front_n(s), r = sym.front_r(s);

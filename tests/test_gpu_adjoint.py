@@ -126,9 +126,11 @@ def test_adjoint_differentiation_workload_against_fd(G):
     parameters drawn with a fixed seed (not picked by sensitivity) against
     central differences with step 1e-6 (relative to max(1, |p|)) of the
     FP64 integration, two fault scenarios: relative error at most 1e-5,
-    measured against max(|fd|, 1e-4 max |gradient|) so that a parameter the
-    objective hardly depends on is held to the absolute accuracy of the
-    differences."""
+    measured against max(|fd|, 2e-2 max |gradient|).  The differences carry
+    an absolute error of about 1e-7 of the largest gradient (the 1e-12
+    Newton tolerance over a 1e-6 step), so a parameter the objective hardly
+    depends on is held to that absolute accuracy instead; at least five of
+    the twenty are above the floor."""
     c, w = synthetic_case("planar2k_adj", 2)
     ns = 360
     idx = np.array(AO.differentiated_params(c.PA))
@@ -155,9 +157,10 @@ def test_adjoint_differentiation_workload_against_fd(G):
         Jv = AO.objective_of_traj(c.PA, t, DT, w_volt=10.0)
         fd = (Jv[0::2] - Jv[1::2]) / (2 * hs)
         g = r["grad_p"][m, pick]
-        floor = 1e-4 * np.max(np.abs(r["grad_p"][m, idx]))
+        floor = 2e-2 * np.max(np.abs(r["grad_p"][m, idx]))
         err = np.abs(g - fd) / np.maximum(np.abs(fd), floor)
         assert np.max(err) <= 1e-5, (m, list(zip(pick.tolist(), g.tolist(), fd.tolist(), err.tolist())))
+        assert np.sum(np.abs(fd) >= floor) >= 5
 
 
 def test_adjoint_batch_of_128_equals_single_scenario_runs(G):
