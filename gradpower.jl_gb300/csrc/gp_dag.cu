@@ -124,6 +124,133 @@ struct BlockGroup {
     __device__ void sync() const { __syncthreads(); }
 };
 
+// Columns per panel of the blocked FP32 elimination of CTA-sized fronts.
+constexpr int kPanel = 8;
+
+// Elimination of an FP32 front by the whole CTA (fronts above the warp
+// size), blocked right-looking in panels of kPanel pivot columns:
+//  (a) the panel, column by column: warp 0 finds the pivot among the pivot
+//      rows (one max and one min reduction), swaps the two rows within the
+//      panel, stores the multipliers and the pivot's reciprocal; the CTA then
+//      updates the panel's later columns (a rank-1 update kPanel columns
+//      wide, not the whole front);
+//  (b) the panel's row interchanges applied to every other column;
+//  (c) U of the panel rows right of it, by a forward substitution per
+//      column with the panel's unit lower block (values in registers);
+//  (d) the trailing update A -= L U (rank kPanel): a warp takes four
+//      columns and its lanes the rows, each lane the same four columns of
+//      up to five rows, sums in registers; the U entries are broadcasts and
+//      the L and A entries consecutive across lanes (no bank conflicts).
+// The front is left in the layout of the other paths: multipliers below the
+// diagonal, U above it, the pivots' reciprocals on it, piv[k] the row
+// swapped with row k at step k.
+__device__ void eliminate_cta32(float *F, int mm, int ns, int nc, int *piv, int *status) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+    for (int kb = 0; kb < ns; kb += kPanel) {
+        const int ke = min(ns, kb + kPanel), nb = ke - kb;
+        // ---- (a) the panel ----
+        for (int k = kb; k < ke; k++) {
+            if (warp == 0) {
+                unsigned key = 0u;
+                int bi = k;
+                for (int i = k + lane; i < ns; i += 32) {
+                    const unsigned v = __float_as_uint(F[i + k * mm]) & 0x7fffffffu;
+                    if (v > key) { key = v; bi = i; }
+                }
+                const unsigned kmax = __reduce_max_sync(FULL, key);
+                const int pv = (int)__reduce_min_sync(FULL, key == kmax ? (unsigned)bi : 0xffffffffu);
+                if (lane == 0) {
+                    piv[k] = pv;
+                    if (kmax == 0u) atomicOr(status, 4);
+                }
+                if (pv != k && lane < nb) {
+                    const float a = F[k + (kb + lane) * mm];
+                    F[k + (kb + lane) * mm] = F[pv + (kb + lane) * mm];
+                    F[pv + (kb + lane) * mm] = a;
+                }
+                __syncwarp();
+                const float inv = 1.0f / F[k + k * mm];
+                for (int i = k + 1 + lane; i < mm; i += 32) F[i + k * mm] *= inv;
+                __syncwarp();
+                if (lane == 0) F[k + k * mm] = inv;
+            }
+            __syncthreads();
+            // rank-1 update of the panel's later columns, rows k+1..mm-1:
+            // threads over rows, the columns split between the CTA's halves
+            const int half = blockDim.x >> 1, h = tid >= half, rt = tid - h * half;
+            for (int j = k + 1 + h; j < ke; j += 2) {
+                const float u = F[k + j * mm];
+                for (int i = k + 1 + rt; i < mm; i += half) F[i + j * mm] -= F[i + k * mm] * u;
+            }
+            __syncthreads();
+        }
+        // ---- (b) the panel's interchanges on the other columns ----
+        for (int j = tid; j < nc; j += blockDim.x) {
+            if (j >= kb && j < ke) continue;
+            for (int k = kb; k < ke; k++) {
+                const int pv = piv[k];
+                if (pv != k) {
+                    const float a = F[k + j * mm];
+                    F[k + j * mm] = F[pv + j * mm];
+                    F[pv + j * mm] = a;
+                }
+            }
+        }
+        __syncthreads();
+        if (ke >= nc) break;
+        // ---- (c) U of the panel rows, columns ke..nc-1 ----
+        for (int j = ke + tid; j < nc; j += blockDim.x) {
+            float u[kPanel];
+#pragma unroll
+            for (int q = 0; q < kPanel; q++) u[q] = q < nb ? F[kb + q + j * mm] : 0.0f;
+#pragma unroll
+            for (int q = 0; q < kPanel; q++)
+#pragma unroll
+                for (int p = q + 1; p < kPanel; p++)
+                    if (p < nb) u[p] -= F[kb + p + (kb + q) * mm] * u[q];
+#pragma unroll
+            for (int q = 0; q < kPanel; q++)
+                if (q < nb) F[kb + q + j * mm] = u[q];
+        }
+        __syncthreads();
+        // ---- (d) trailing update, rows ke..mm-1, columns ke..nc-1 ----
+        // (rows in chunks of 160: five per lane)
+        const int nq = (nc - ke + 3) >> 2, nr = (mm - ke + 159) / 160;
+        for (int t = warp; t < nq * nr; t += nwarp) {
+            const int c0 = ke + 4 * (t % nq), r0 = ke + 160 * (t / nq);
+            float acc[5][4];
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                const int i = r0 + lane + 32 * q;
+#pragma unroll
+                for (int c = 0; c < 4; c++) acc[q][c] = (i < mm && c0 + c < nc) ? F[i + (c0 + c) * mm] : 0.0f;
+            }
+            for (int k = kb; k < ke; k++) {
+                float u[4], l[5];
+#pragma unroll
+                for (int c = 0; c < 4; c++) u[c] = c0 + c < nc ? F[k + (c0 + c) * mm] : 0.0f;
+#pragma unroll
+                for (int q = 0; q < 5; q++) {
+                    const int i = r0 + lane + 32 * q;
+                    l[q] = i < mm ? F[i + k * mm] : 0.0f;
+                }
+#pragma unroll
+                for (int q = 0; q < 5; q++)
+#pragma unroll
+                    for (int c = 0; c < 4; c++) acc[q][c] = fmaf(-l[q], u[c], acc[q][c]);
+            }
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                const int i = r0 + lane + 32 * q;
+#pragma unroll
+                for (int c = 0; c < 4; c++)
+                    if (i < mm && c0 + c < nc) F[i + (c0 + c) * mm] = acc[q][c];
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // Factors the front of supernode s for scenario m in shared memory F
 // (leading dimension mm = front rows) and stores it to global memory.
 //  - Assembly: constant entries of S, the scenario's entries from svar, and
@@ -193,6 +320,10 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
     // A22 -= L21 U12, four entries per thread with the sums in registers.
     // Both give every entry the same operations in the same order.
     constexpr bool kBlocked = sizeof(T) == 4;
+    if constexpr (kBlocked && G::size > 32) {
+        static_assert(!RHS, "the FP32 factorisation carries no right-hand side");
+        eliminate_cta32(F, mm, ns, nc, piv, W.status + m);
+    } else {
     for (int k = 0; k < ns; k++) {
         if (g.lead_warp()) {
             const int lane = threadIdx.x & 31;
@@ -276,6 +407,7 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
                 if (t0 + q * step < n) F[ri[q] + cj[q]] = acc[q];
         }
         g.sync();
+    }
     }
     // ---- store ----
     // the row interchanges, composed: pivot row i of the factored front is
