@@ -46,6 +46,12 @@ constexpr unsigned FULL = kFullMask;
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kSmallFront = 32;
+// update-matrix entries a thread loads ahead in the extend-add: none in the
+// warp kernel, which runs at 40 registers a thread and many warps a SM
+template <class G>
+__host__ __device__ constexpr int asm_batch() {
+    return G::size > 32 ? 8 : 1;
+}
 
 template <class T>
 __device__ __forceinline__ T ldcg(const T *p) {
@@ -295,15 +301,30 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
         const int *rel = S.relmap + S.relmap_ptr[c];
         const T *Fc = fr + S.front_off[c];
         // (a, b) = (t % rc, t / rc), advanced by the stride without a
-        // division per entry
+        // division per entry.  A thread loads asm_batch entries (and their
+        // positions) before it adds any of them, so that their round trips
+        // to L2 overlap instead of following one another
         const int rcs = rc > 0 ? rc : 1;   // (a child always has update rows)
         int a = idx % rcs, b = idx / rcs;
         const int da = step % rcs, db = step / rcs;
-        for (int t = idx; t < rc * rc; t += step) {
-            F[rel[a] + rel[b] * mm] += ldcg(Fc + (ncc + a) + (size_t)(ncc + b) * mc);
-            a += da;
-            b += db;
-            if (a >= rc) { a -= rc; b++; }
+        const int n = rc * rc;
+        constexpr int kAsmBatch = asm_batch<G>();
+        for (int t0 = idx; t0 < n; t0 += kAsmBatch * step) {
+            T val[kAsmBatch];
+            int pos[kAsmBatch];
+#pragma unroll
+            for (int u = 0; u < kAsmBatch; u++) {
+                if (t0 + u * step < n) {
+                    pos[u] = rel[a] + rel[b] * mm;
+                    val[u] = ldcg(Fc + (ncc + a) + (size_t)(ncc + b) * mc);
+                }
+                a += da;
+                b += db;
+                if (a >= rc) { a -= rc; b++; }
+            }
+#pragma unroll
+            for (int u = 0; u < kAsmBatch; u++)
+                if (t0 + u * step < n) F[pos[u]] += val[u];
         }
         if (RHS) {
             const double *uc = uv + S.uvec_off[c];
