@@ -508,8 +508,8 @@ struct HostBlk {
     std::vector<int> top_xptr, top_xrow, top_xent;   // extend-add lists of the top region
     // upper part of the top region (narrow levels near the root), solved by
     // one CTA per scenario (gp_solve.cu, upper_kernel): ranks from n_lower_top
-    int n_lower_top = 0, up_nlev = 0, n_xu = 0;
-    std::vector<int> up_lev_ptr{0}, up_xoff, up_xrow, up_rmap_ptr{0}, up_rmap;
+    int n_lower_top = 0, up_nlev = 0, n_xu = 0, up_stage = 0;
+    std::vector<int> up_lev_ptr{0}, up_xoff, up_soff, up_xrow, up_rmap_ptr{0}, up_rmap;
 };
 
 void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
@@ -665,20 +665,35 @@ void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
             U = d;
             break;
         }
+    // and as long as the shared memory of the upper kernel holds its rows
+    // and the factor entries of its widest level (staged a level at a time:
+    // pivot columns forward, pivot rows backward, ns * mm entries a front)
+    std::vector<long> lev_stage(ntl, 0);
+    for (int s : B.top_order) lev_stage[tlev[s]] += (long)sym.front_n(s) * sym.front_m(s);
     auto upper_rows = [&](int from) {
         long n = 0;
         for (int s : B.top_order)
             if (tlev[s] >= from) n += sym.front_n(s);
         return n;
     };
-    while (U < ntl && upper_rows(U) > gp::solve_upper_max_rows()) U++;
+    auto upper_stage = [&](int from) {
+        long n = 0;
+        for (int d = from; d < ntl; d++) n = std::max(n, lev_stage[d]);
+        return n;
+    };
+    while (U < ntl && (upper_rows(U) > gp::solve_upper_max_rows() ||
+                       gp::solve_upper_bytes((int)upper_rows(U), (int)upper_stage(U), B.top_max_front) >
+                           gp::solve_upper_smem()))
+        U++;
     B.n_lower_top = 0;
     for (int s : B.top_order)
         if (tlev[s] < U) B.n_lower_top++;
     B.up_nlev = ntl - U;
     B.up_lev_ptr.assign(1, 0);
     B.up_xoff.clear();
+    B.up_soff.clear();
     B.up_xrow.clear();
+    B.up_stage = U < ntl ? (int)upper_stage(U) : 0;
     B.up_rmap_ptr.assign(1, 0);
     B.up_rmap.clear();
     std::vector<int> slot_of_row(sym.n, -1);
@@ -691,9 +706,13 @@ void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
         }
     }
     for (int d = U; d < ntl; d++) {
-        int c = B.up_lev_ptr.back();
+        int c = B.up_lev_ptr.back(), so = 0;
         for (int s : B.top_order)
-            if (tlev[s] == d) c++;
+            if (tlev[s] == d) {
+                c++;
+                B.up_soff.push_back(so);   // staging offset within the level (upper order is by level)
+                so += sym.front_n(s) * sym.front_m(s);
+            }
         B.up_lev_ptr.push_back(c);
     }
     for (int q = B.n_lower_top; q < (int)B.top_order.size(); q++) {
@@ -840,16 +859,18 @@ void host_fwd_front(const double *F, const int *perm, int ns, int mm, Staged &v,
     }
 }
 
-void host_bwd_front(const double *F, int ns, int mm, Staged &v, long o) {
+// ld: leading dimension of F (mm for a front, ns for its pivot rows alone).
+void host_bwd_front(const double *F, int ns, int mm, Staged &v, long o, int ld = -1) {
+    if (ld < 0) ld = mm;
     for (int i = 0; i < ns; i++) {
         double acc = 0.0;
-        for (int a = 0; a < mm - ns; a++) acc += F[i + (size_t)(ns + a) * mm] * v[o + ns + a];
+        for (int a = 0; a < mm - ns; a++) acc += F[i + (size_t)(ns + a) * ld] * v[o + ns + a];
         v[o + i] -= acc;
     }
     for (int k = ns - 1; k >= 0; k--) {
-        const double tk = v[o + k] * F[k + (size_t)k * mm];
+        const double tk = v[o + k] * F[k + (size_t)k * ld];
         v[o + k] = tk;
-        for (int i = 0; i < k; i++) v[o + i] -= F[i + (size_t)k * mm] * tk;
+        for (int i = 0; i < k; i++) v[o + i] -= F[i + (size_t)k * ld] * tk;
     }
 }
 
@@ -866,6 +887,8 @@ void check_upper(const gp::Symbolic &S, const HostBlk &B) {
         const int s = B.top_order[B.n_lower_top + q];
         const int ns = S.front_n(s), r = S.front_r(s);
         if (B.up_xoff[q] < 0 || B.up_xoff[q] + ns > B.n_xu) fail(GP_E_INTERNAL, "upper part: slots of %d", s);
+        if ((int)B.up_soff.size() != nu || B.up_soff[q] < 0 || B.up_soff[q] + ns * (ns + r) > B.up_stage)
+            fail(GP_E_INTERNAL, "upper part: staging area of %d", s);
         for (int i = 0; i < ns; i++)
             if (B.up_xrow[B.up_xoff[q] + i] != S.sup_start[s] + i) fail(GP_E_INTERNAL, "upper part: row of %d", s);
         if (B.up_rmap_ptr[q + 1] - B.up_rmap_ptr[q] != r) fail(GP_E_INTERNAL, "upper part: update rows of %d", s);
@@ -966,7 +989,11 @@ void host_block_solve(const gp::Symbolic &S, const HostBlk &B, const std::vector
                     for (int e = xr[i]; e < xr[i + 1]; e++) acc += uvec[B.top_xent[e]];
                     tv[i] = acc;
                 }
-                host_fwd_front(fronts.data() + S.front_off[s], ipiv.data() + start, ns, mm, tv, 0);
+                // the pivot columns through the staging area, as the kernel copies them
+                Staged stg(std::max(1, B.up_stage), "upper staging");
+                const double *F = fronts.data() + S.front_off[s];
+                for (int e = 0; e < mm * ns; e++) stg[B.up_soff[q] + e] = F[e];
+                host_fwd_front(&stg[B.up_soff[q]], ipiv.data() + start, ns, mm, tv, 0);
                 for (int i = 0; i < ns; i++) xu[B.up_xoff[q] + i] = tv[i];
                 for (int a = 0; a < r; a++) uvec[S.uvec_off[s] + a] = tv[ns + a];
             }
@@ -977,7 +1004,12 @@ void host_block_solve(const gp::Symbolic &S, const HostBlk &B, const std::vector
                 Staged tv(B.top_max_front, "upper front vector");
                 for (int i = 0; i < mm; i++)
                     tv[i] = i < ns ? (double)xu[B.up_xoff[q] + i] : (double)xu[B.up_rmap[B.up_rmap_ptr[q] + i - ns]];
-                host_bwd_front(fronts.data() + S.front_off[s], ns, mm, tv, 0);
+                // the pivot rows through the staging area (leading dimension ns)
+                Staged stg(std::max(1, B.up_stage), "upper staging");
+                const double *F = fronts.data() + S.front_off[s];
+                for (int c = 0; c < mm; c++)
+                    for (int i = 0; i < ns; i++) stg[B.up_soff[q] + i + (long)c * ns] = F[i + (size_t)c * mm];
+                host_bwd_front(&stg[B.up_soff[q]], ns, mm, tv, 0, ns);
                 for (int i = 0; i < ns; i++) xu[B.up_xoff[q] + i] = tv[i];
             }
         for (int k = 0; k < B.n_xu; k++) x[B.up_xrow[k]] = xu[k];
@@ -1091,6 +1123,8 @@ void build_blocks(gp_layout *L, const gp::Symbolic &sym) {
     B.n_xu = H.n_xu;
     B.up_lev_ptr = A.upload(H.up_lev_ptr);
     B.up_xoff = A.upload(H.up_xoff);
+    B.up_soff = A.upload(H.up_soff);
+    B.up_stage = H.up_stage;
     B.up_xrow = A.upload(H.up_xrow);
     B.up_rmap_ptr = A.upload(H.up_rmap_ptr);
     B.up_rmap = A.upload(H.up_rmap);

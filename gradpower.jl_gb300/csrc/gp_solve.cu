@@ -60,6 +60,7 @@ constexpr int kBlkFront = 64;  // largest front inside a block (two rows per lan
 constexpr int kUpThreads = 512;           // threads of the upper kernel (one CTA per scenario)
 constexpr int kUpWidth = 48;              // a level of at most this many supernodes is upper
 constexpr int kUpMaxRows = 8192;          // most pivot rows of the upper part (shared vector)
+constexpr int kUpSmem = 200 * 1024;       // most shared memory of the upper kernel
 
 __host__ __device__ constexpr int align16(int b) { return (b + 15) & ~15; }
 
@@ -820,30 +821,48 @@ __global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P,
 
 // ---- upper part: one CTA per scenario ------------------------------------
 // Shared memory: the upper rows' vector (double slots, whatever the factor
-// type), then per warp a front vector, a gather scratch (both sized for
-// double) and the pivot permutation.
+// type), the staging area of one level's factor entries (up_stage entries,
+// sized for double), then per warp a front vector, a gather scratch (both
+// sized for double) and the pivot permutation.
 __host__ __device__ constexpr int up_warp_bytes(int tmf) { return align16(tmf * (8 + 8 + 4)); }
-__host__ __device__ constexpr int up_bytes(int n_xu, int tmf) {
-    return align16(n_xu * 8) + (kUpThreads / 32) * up_warp_bytes(tmf);
+__host__ __device__ constexpr int up_bytes(int n_xu, int stage, int tmf) {
+    return align16(n_xu * 8) + align16(stage * 8) + (kUpThreads / 32) * up_warp_bytes(tmf);
+}
+
+// The lanes of one warp copy columns [c0, c1) of rows [0, nrow) of the front F
+// (leading dimension mm) into Fs (leading dimension nrow).
+template <class T>
+__device__ void warp_stage_cols(T *Fs, const T *F, int mm, int nrow, int c0, int c1) {
+    const int lane = threadIdx.x & 31;
+    const int n = nrow * (c1 - c0);
+    int c = lane / nrow, i = lane - c * nrow;
+    const int dc = 32 / nrow, di = 32 - dc * nrow;
+    for (int e = lane; e < n; e += 32) {
+        cp_async(Fs + e, F + i + (size_t)(c0 + c) * mm, (int)sizeof(T));
+        i += di;
+        c += dc;
+        if (i >= nrow) { i -= nrow; c++; }
+    }
 }
 
 // Forward then backward solve of the upper supernodes of scenario m with
-// factors of type T.  Forward (skipped when the FP64 factorisation already
-// did it): level by level from the leaves, a warp per supernode: its front
-// vector from the upper rows and the children's update vectors (the lower
-// children's from the forward dataflow kernel, the upper ones' from earlier
-// levels, all through global memory), the unit-lower sweep, the pivot rows
-// back to the vector and the update rows to the supernode's update vector.
-// Backward: level by level from the root, the U12 dot products with the
-// ancestors' solution and the upper triangular sweep.  Ends with the upper
-// rows written to xperm.
+// factors of type T, a level per step and a warp per supernode.  The warp
+// first copies its front's factor entries into the level's staging area
+// (cp.async; forward: the pivot columns, backward: the pivot rows), builds
+// the front vector while the copies are in flight (forward: the upper rows
+// plus the children's update vectors from global memory; backward: the
+// upper rows and the ancestors' solution, all in shared memory), then
+// sweeps from shared memory.  One CTA barrier per level.  The forward part
+// is skipped when the FP64 factorisation already did it.  Ends with the
+// upper rows written to xperm.
 template <class T>
 __device__ void upper_solve(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B,
                             const FrontSel &fs, int m, bool do_fwd, unsigned char *smem) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     const int tmf = B.top_max_front;
     T *xu = reinterpret_cast<T *>(smem);
-    unsigned char *wb = smem + align16(B.n_xu * 8) + (size_t)warp * up_warp_bytes(tmf);
+    T *stg = reinterpret_cast<T *>(smem + align16(B.n_xu * 8));
+    unsigned char *wb = smem + align16(B.n_xu * 8) + align16(B.up_stage * 8) + (size_t)warp * up_warp_bytes(tmf);
     T *v = reinterpret_cast<T *>(wb);
     T *sc = reinterpret_cast<T *>(wb + tmf * 8);
     int *pi = reinterpret_cast<int *>(wb + tmf * 16);
@@ -853,43 +872,40 @@ __device__ void upper_solve(const DevProblem &P, const DevWork &W, const DevSym 
     const int *ip = S.ipiv + (size_t)(fs.shared ? 0 : m) * S.n;
     for (int k = threadIdx.x; k < B.n_xu; k += blockDim.x) xu[k] = (T)x[B.up_xrow[k]];
     __syncthreads();
-    if (do_fwd) {
-        for (int l = 0; l < B.up_nlev; l++) {
-            for (int q = B.up_lev_ptr[l] + warp; q < B.up_lev_ptr[l + 1]; q += nwarp) {
-                const int rank = B.n_lower_top + q, s = B.top_order[rank];
-                const int start = S.sup_start[s], ns = S.sup_start[s + 1] - start;
-                const int mm = ns + S.row_ptr[s + 1] - S.row_ptr[s];
-                const T *F = fr + S.front_off[s];
+    for (int step = do_fwd ? 0 : B.up_nlev; step < 2 * B.up_nlev; step++) {
+        const bool fwd = step < B.up_nlev;
+        const int l = fwd ? step : 2 * B.up_nlev - 1 - step;
+        for (int q = B.up_lev_ptr[l] + warp; q < B.up_lev_ptr[l + 1]; q += nwarp) {
+            const int rank = B.n_lower_top + q, s = B.top_order[rank];
+            const int start = S.sup_start[s], ns = S.sup_start[s + 1] - start;
+            const int mm = ns + S.row_ptr[s + 1] - S.row_ptr[s];
+            const int xo = B.up_xoff[q];
+            T *Fs = stg + B.up_soff[q];
+            if (fwd) {
+                warp_stage_cols<T>(Fs, fr + S.front_off[s], mm, mm, 0, ns);
                 const int *xr = B.top_xrow + B.top_xptr[rank];
-                const int xo = B.up_xoff[q];
                 for (int i = lane; i < mm; i += 32) {
                     T acc = i < ns ? xu[xo + i] : T(0);
                     for (int e = xr[i]; e < xr[i + 1]; e++) acc += (T)uv[B.top_xent[e]];
                     v[i] = acc;
                 }
                 for (int i = lane; i < ns; i += 32) pi[i] = ip[start + i];
+                cp_async_wait_all();
                 __syncwarp();
-                fwd_cols<T>(F, mm, 0, 0, ns, ns, mm, v, sc, [&](int i) { return pi[i]; }, true);
+                fwd_cols<T>(Fs, mm, 0, 0, ns, ns, mm, v, sc, [&](int i) { return pi[i]; }, true);
                 for (int i = lane; i < ns; i += 32) xu[xo + i] = v[i];
                 double *us = uv + S.uvec_off[s];
                 for (int a = lane; a < mm - ns; a += 32) us[a] = (double)v[ns + a];
+            } else {
+                warp_stage_cols<T>(Fs, fr + S.front_off[s], mm, ns, 0, mm);
+                const int *rm = B.up_rmap + B.up_rmap_ptr[q];
+                for (int i = lane; i < mm; i += 32) v[i] = i < ns ? xu[xo + i] : xu[rm[i - ns]];
+                cp_async_wait_all();
                 __syncwarp();
+                if (mm > ns) bwd_u12<T>(Fs, ns, 0, ns, mm, ns, v);
+                bwd_cols<T>(Fs, ns, 0, 0, ns, ns, v);
+                for (int i = lane; i < ns; i += 32) xu[xo + i] = v[i];
             }
-            __syncthreads();
-        }
-    }
-    for (int l = B.up_nlev - 1; l >= 0; l--) {
-        for (int q = B.up_lev_ptr[l] + warp; q < B.up_lev_ptr[l + 1]; q += nwarp) {
-            const int s = B.top_order[B.n_lower_top + q];
-            const int ns = S.sup_start[s + 1] - S.sup_start[s];
-            const int mm = ns + S.row_ptr[s + 1] - S.row_ptr[s];
-            const T *F = fr + S.front_off[s];
-            const int xo = B.up_xoff[q], *rm = B.up_rmap + B.up_rmap_ptr[q];
-            for (int i = lane; i < mm; i += 32) v[i] = i < ns ? xu[xo + i] : xu[rm[i - ns]];
-            __syncwarp();
-            if (mm > ns) bwd_u12<T>(F, mm, 0, ns, mm, ns, v);
-            bwd_cols<T>(F, mm, 0, 0, ns, ns, v);
-            for (int i = lane; i < ns; i += 32) xu[xo + i] = v[i];
             __syncwarp();
         }
         __syncthreads();
@@ -917,6 +933,8 @@ int grid_for(int resident, long long tasks, int per_block) {
 int solve_block_front_limit() { return kBlkFront; }
 int solve_upper_width() { return kUpWidth; }
 int solve_upper_max_rows() { return kUpMaxRows; }
+int solve_upper_bytes(int n_xu, int stage, int tmf) { return up_bytes(n_xu, stage, std::max(1, tmf)); }
+int solve_upper_smem() { return kUpSmem; }
 
 int solve_configure(const DevBlk &B, SolveGrid &g) {
     int dev = 0, nsm = 0, occ = 0;
@@ -944,7 +962,7 @@ int solve_configure(const DevBlk &B, SolveGrid &g) {
             cudaSuccess || occ < 1)
         return -1;
     g.top_bwd = nsm * occ;
-    g.up_bytes = up_bytes(B.n_xu, std::max(1, B.top_max_front));
+    g.up_bytes = up_bytes(B.n_xu, B.up_stage, std::max(1, B.top_max_front));
     if (B.up_nlev > 0 &&
         cudaFuncSetAttribute(upper_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, g.up_bytes) != cudaSuccess) {
         cudaGetLastError();
