@@ -265,14 +265,17 @@ def vs_oracle(w, g, o, subset=None):
 
 def config_legs(orc, nthreads):
     """The precision form at the other batched configurations: ring39 x 64
-    (1 s) and planar2k x 256 (2 s).  The FP64 and the mixed Schur paths run
+    (1 s) and planar2k x 256 (2 s), and on the two harder grids: planar2k
+    with four times the loads and line charging (x 256, 2 s) and planar70k
+    with line charging (x 8, 1 s).  The FP64 and the mixed Schur paths run
     on the GPU (device time of one integration each, after a warm-up, then
     once more with trajectories); both are compared with the oracle (all 64
-    ring39 scenarios, the first 32 planar2k scenarios) and with each other on
-    every scenario."""
+    ring39 scenarios, the first 32 or 16 planar2k ones, the first 2 planar70k
+    ones) and with each other on every scenario."""
     from gradpower_gb300 import gpu, layout as LY, synthetic
     out = {}
-    for name, M, n_or in (("ring39", 64, 64), ("planar2k", 256, 32)):
+    for name, M, n_or in (("ring39", 64, 64), ("planar2k", 256, 32), ("planar2k_stressed", 256, 16),
+                          ("planar70k_charged", 8, 2)):
         w = synthetic.WORKLOADS[name](n_scenarios=M)
         faults = w.faults[:M]
         ns = LY.jl_round(w.tf / DT)

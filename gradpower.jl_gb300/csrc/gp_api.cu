@@ -653,18 +653,14 @@ void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
         B.top_xptr.push_back((int)B.top_xrow.size());
         B.top_max_xent = std::max(B.top_max_xent, B.top_xrow.back() - B.top_xrow[B.top_xptr[B.top_xptr.size() - 2]]);
     }
-    // upper part: the levels from the first one with at most
-    // solve_upper_width() supernodes up to the root, as long as their pivot
+    // upper part: the levels near the root that have at most
+    // solve_upper_width() supernodes each, as long as their pivot
     // rows fit the upper kernel's shared vector; every ancestor of an upper
     // supernode is upper, so its update rows are upper rows
     std::vector<int> lev_cnt(ntl, 0);
     for (int s : B.top_order) lev_cnt[tlev[s]]++;
     int U = ntl;
-    for (int d = 0; d < ntl; d++)
-        if (lev_cnt[d] <= gp::solve_upper_width()) {
-            U = d;
-            break;
-        }
+    while (U > 0 && lev_cnt[U - 1] <= gp::solve_upper_width()) U--;
     // and as long as the shared memory of the upper kernel holds its rows
     // and the factor entries of its widest level (staged a level at a time:
     // pivot columns forward, pivot rows backward, ns * mm entries a front)
@@ -883,6 +879,9 @@ void check_upper(const gp::Symbolic &S, const HostBlk &B) {
         (int)B.up_lev_ptr.size() != B.up_nlev + 1 || B.up_lev_ptr.back() != nu || B.n_xu != (int)B.up_xrow.size())
         fail(GP_E_INTERNAL, "upper part: inconsistent sizes");
     if (B.n_xu > gp::solve_upper_max_rows()) fail(GP_E_INTERNAL, "upper part: %d rows above the limit", B.n_xu);
+    for (int l = 0; l < B.up_nlev; l++)
+        if (B.up_lev_ptr[l + 1] - B.up_lev_ptr[l] > gp::solve_upper_width())
+            fail(GP_E_INTERNAL, "upper part: level %d wider than %d", l, gp::solve_upper_width());
     for (int q = 0; q < nu; q++) {
         const int s = B.top_order[B.n_lower_top + q];
         const int ns = S.front_n(s), r = S.front_r(s);
@@ -1088,6 +1087,53 @@ void build_dag(gp_layout *L, const gp::Symbolic &sym) {
     D.order = A.upload(order);
     D.rank = A.upload(rank);
     D.parent = A.upload(sym.parent);
+    // extend-add lists of the fronts the CTA kernel factors: per front entry
+    // (and right-hand-side row) its children's contributions, in child order
+    {
+        if (sym.front_off[ns] > INT32_MAX || sym.uvec_off[ns] > INT32_MAX)
+            fail(GP_E_INVALID, "fronts too large for 32-bit assembly offsets");
+        std::vector<int> pa_base(ns, -1), pr_base(ns, -1), pa_ptr, pa_src, pr_ptr, pr_src;
+        for (int s = 0; s < ns; s++) {
+            if (submax[s] <= lim) continue;
+            const int mm = sym.front_m(s);
+            std::vector<std::vector<int>> per((size_t)mm * mm), perr(mm);
+            for (int q = sym.child_ptr[s]; q < sym.child_ptr[s + 1]; q++) {
+                const int c = sym.children[q];
+                const int ncc = sym.front_n(c), rc = sym.front_r(c), mc = ncc + rc;
+                const int *rel = sym.relmap.data() + sym.relmap_ptr[c];
+                for (int b = 0; b < rc; b++)
+                    for (int a = 0; a < rc; a++)
+                        per[(size_t)rel[a] + (size_t)rel[b] * mm].push_back(
+                            (int)(sym.front_off[c] + (ncc + a) + (int64_t)(ncc + b) * mc));
+                for (int a = 0; a < rc; a++) perr[rel[a]].push_back((int)sym.uvec_off[c] + a);
+            }
+            pa_base[s] = (int)pa_ptr.size();
+            for (size_t p = 0; p < per.size(); p++) {
+                pa_ptr.push_back((int)pa_src.size());
+                pa_src.insert(pa_src.end(), per[p].begin(), per[p].end());
+            }
+            pa_ptr.push_back((int)pa_src.size());
+            pr_base[s] = (int)pr_ptr.size();
+            for (int i = 0; i < mm; i++) {
+                pr_ptr.push_back((int)pr_src.size());
+                pr_src.insert(pr_src.end(), perr[i].begin(), perr[i].end());
+            }
+            pr_ptr.push_back((int)pr_src.size());
+        }
+        gp::DevSym &S = L->S;
+        S.pa_base = A.upload(pa_base);
+        S.pa_ptr = A.upload(pa_ptr);
+        S.pa_src = A.upload(pa_src);
+        S.pr_base = A.upload(pr_base);
+        S.pr_ptr = A.upload(pr_ptr);
+        S.pr_src = A.upload(pr_src);
+        L->ST.pa_base = S.pa_base;
+        L->ST.pa_ptr = S.pa_ptr;
+        L->ST.pa_src = S.pa_src;
+        L->ST.pr_base = S.pr_base;
+        L->ST.pr_ptr = S.pr_ptr;
+        L->ST.pr_src = S.pr_src;
+    }
     if (gp::dag_configure(D, 0, L->G64) != 0) fail(GP_E_CUDA, "could not configure the dataflow kernels");
 }
 
@@ -1157,8 +1203,11 @@ void build_problem(gp_layout *L, const gp_problem *pr) {
     L->n_par = pr->n_par;
     P.y_rowptr = A.upload(pr->y_rowptr, nb + 1);
     P.y_colidx = A.upload(pr->y_colidx, pr->y_nnz);
-    P.y_re = A.upload(pr->y_re, pr->y_nnz);
-    P.y_im = A.upload(pr->y_im, pr->y_nnz);
+    {
+        std::vector<double2> yv(std::max(1, pr->y_nnz));
+        for (int q = 0; q < pr->y_nnz; q++) yv[q] = make_double2(pr->y_re[q], pr->y_im[q]);
+        P.y_val = A.upload(yv);
+    }
     for (int t = 0; t < GP_NTYPES; t++) {
         const gp_device_table &T = pr->dev[t];
         DTab &D = P.dev[t];

@@ -293,6 +293,41 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
             if (P.tr_on[t] && t >= P.tr_ptr[m] && t < P.tr_ptr[m + 1]) F[S.asmt_pos[e]] += (T)S.asmt_val[e];
         }
     g.sync();
+    if (G::size > 32 && S.pa_base && S.pa_base[s] >= 0) {
+        // CTA fronts: every entry sums its children's contributions (host
+        // lists, child order) without a barrier between children; four
+        // entries a thread per round, their loads issued together
+        const int *pp = S.pa_ptr + S.pa_base[s];
+        const int n2 = mm * mm;
+        for (int p0 = idx; p0 < n2; p0 += 4 * step) {
+            T acc[4];
+            int e0[4], e1[4], kmax = 0;
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int p = p0 + u * step;
+                e0[u] = p < n2 ? pp[p] : 0;
+                e1[u] = p < n2 ? pp[p + 1] : 0;
+                acc[u] = p < n2 ? F[p] : T(0);
+                kmax = max(kmax, e1[u] - e0[u]);
+            }
+            for (int k = 0; k < kmax; k++)
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (e0[u] + k < e1[u]) acc[u] += ldcg(fr + S.pa_src[e0[u] + k]);
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (p0 + u * step < n2) F[p0 + u * step] = acc[u];
+        }
+        if (RHS) {
+            const int *rp = S.pr_ptr + S.pr_base[s];
+            for (int i = idx; i < mm; i += step) {
+                T acc = F[mm * mm + i];
+                for (int e = rp[i]; e < rp[i + 1]; e++) acc += (T)ldcg(uv + S.pr_src[e]);
+                F[mm * mm + i] = acc;
+            }
+        }
+        g.sync();
+    } else
     for (int q = S.child_ptr[s]; q < S.child_ptr[s + 1]; q++) {
         const int c = S.children[q];
         const int ncc = S.sup_start[c + 1] - S.sup_start[c];

@@ -19,9 +19,9 @@ struct DTab {
 struct DevProblem {
     int n_bus, n_diff, n_alg, n_ctrl, n_par, n_sys, net, n_red;
     int M;
-    // complex Ybus, CSR
+    // complex Ybus, CSR; each entry's (G, B) in one 16-byte pair
     const int *y_rowptr, *y_colidx;
-    const double *y_re, *y_im;
+    const double2 *y_val;
     DTab dev[8];
     const uint8_t *is_diff;
     // clusters (non-trivial only are processed by the cluster kernel)
@@ -89,6 +89,13 @@ struct DevSym {
     double *fronts;                   // [M][front_total]
     double *uvec;                     // [M][uvec_total]
     int *ipiv;                        // [M][n] pivot row within the supernode, per column
+    // extend-add of the CTA-sized fronts, by entry ("pull"): for supernode s
+    // (-1 when a warp factors it), pa_ptr[pa_base[s] + p] .. [.. + p + 1]
+    // are the children's update-matrix entries (offsets in a scenario's
+    // fronts) that add into front entry p, in child order; pr_* likewise
+    // for the right-hand side (offsets in a scenario's update vectors)
+    const int *pa_base, *pa_ptr, *pa_src;
+    const int *pr_base, *pr_ptr, *pr_src;
 };
 
 // Sparse cluster factorisation plan: clusters grouped into classes with

@@ -467,7 +467,8 @@ __global__ void __launch_bounds__(256) network_kernel(DevProblem P, DevWork W, D
         double fr = 0.0, fi = 0.0, d00 = 0.0, d01 = 0.0, d10 = 0.0, d11 = 0.0, rr = 0.0, ri = 0.0;
         for (int q = P.y_rowptr[b]; q < P.y_rowptr[b + 1]; q++) {
             const int j = P.y_colidx[q];
-            const double g = P.y_re[q], bb = P.y_im[q];
+            const double2 y = P.y_val[q];   // one 16-byte load
+            const double g = y.x, bb = y.y;
             const double vrj = z[net + 2 * j], vij = z[net + 2 * j + 1];
             // -(g + j bb)(vrj + j vij), two FMAs per part
             fr = fma(-g, vrj, fma(bb, vij, fr));

@@ -58,7 +58,7 @@ constexpr int kTopStage = 20 * 1024;         // shared memory for a task's facto
 constexpr int kMaxJ = 8;       // register rows per lane: fronts up to 256 rows
 constexpr int kBlkFront = 64;  // largest front inside a block (two rows per lane)
 constexpr int kUpThreads = 512;           // threads of the upper kernel (one CTA per scenario)
-constexpr int kUpWidth = 48;              // a level of at most this many supernodes is upper
+constexpr int kUpWidth = 8;               // a level of at most this many supernodes is upper
 constexpr int kUpMaxRows = 8192;          // most pivot rows of the upper part (shared vector)
 constexpr int kUpSmem = 200 * 1024;       // most shared memory of the upper kernel
 
@@ -829,36 +829,22 @@ __host__ __device__ constexpr int up_bytes(int n_xu, int stage, int tmf) {
     return align16(n_xu * 8) + align16(stage * 8) + (kUpThreads / 32) * up_warp_bytes(tmf);
 }
 
-// The lanes of one warp copy columns [c0, c1) of rows [0, nrow) of the front F
-// (leading dimension mm) into Fs (leading dimension nrow).
-template <class T>
-__device__ void warp_stage_cols(T *Fs, const T *F, int mm, int nrow, int c0, int c1) {
-    const int lane = threadIdx.x & 31;
-    const int n = nrow * (c1 - c0);
-    int c = lane / nrow, i = lane - c * nrow;
-    const int dc = 32 / nrow, di = 32 - dc * nrow;
-    for (int e = lane; e < n; e += 32) {
-        cp_async(Fs + e, F + i + (size_t)(c0 + c) * mm, (int)sizeof(T));
-        i += di;
-        c += dc;
-        if (i >= nrow) { i -= nrow; c++; }
-    }
-}
-
 // Forward then backward solve of the upper supernodes of scenario m with
-// factors of type T, a level per step and a warp per supernode.  The warp
-// first copies its front's factor entries into the level's staging area
-// (cp.async; forward: the pivot columns, backward: the pivot rows), builds
-// the front vector while the copies are in flight (forward: the upper rows
-// plus the children's update vectors from global memory; backward: the
-// upper rows and the ancestors' solution, all in shared memory), then
-// sweeps from shared memory.  One CTA barrier per level.  The forward part
-// is skipped when the FP64 factorisation already did it.  Ends with the
-// upper rows written to xperm.
+// factors of type T, a level per step and a warp per supernode (a level has
+// at most kUpWidth <= warps supernodes).  Each step: all threads copy the
+// level's factor entries into shared memory (cp.async; forward: the pivot
+// columns of each front, backward: its pivot rows); while the copies are in
+// flight each warp builds its front vector (forward: the upper rows plus
+// the children's update vectors from global memory; backward: the upper
+// rows and the ancestors' solution, both in shared memory); one barrier;
+// the sweeps from shared memory; another barrier.  The forward part is
+// skipped when the FP64 factorisation already did it.  Ends with the upper
+// rows written to xperm.
 template <class T>
 __device__ void upper_solve(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B,
                             const FrontSel &fs, int m, bool do_fwd, unsigned char *smem) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    static_assert(kUpWidth <= kUpThreads / 32, "one supernode a warp per level");
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int tmf = B.top_max_front;
     T *xu = reinterpret_cast<T *>(smem);
     T *stg = reinterpret_cast<T *>(smem + align16(B.n_xu * 8));
@@ -875,14 +861,25 @@ __device__ void upper_solve(const DevProblem &P, const DevWork &W, const DevSym 
     for (int step = do_fwd ? 0 : B.up_nlev; step < 2 * B.up_nlev; step++) {
         const bool fwd = step < B.up_nlev;
         const int l = fwd ? step : 2 * B.up_nlev - 1 - step;
-        for (int q = B.up_lev_ptr[l] + warp; q < B.up_lev_ptr[l + 1]; q += nwarp) {
-            const int rank = B.n_lower_top + q, s = B.top_order[rank];
-            const int start = S.sup_start[s], ns = S.sup_start[s + 1] - start;
+        const int q0 = B.up_lev_ptr[l], q1 = B.up_lev_ptr[l + 1];
+        for (int q = q0; q < q1; q++) {
+            const int s = B.top_order[B.n_lower_top + q];
+            const int ns = S.sup_start[s + 1] - S.sup_start[s];
             const int mm = ns + S.row_ptr[s + 1] - S.row_ptr[s];
-            const int xo = B.up_xoff[q];
-            T *Fs = stg + B.up_soff[q];
+            if (fwd) stage_cols<T>(stg + B.up_soff[q], fr + S.front_off[s], mm, mm, 0, ns);
+            else stage_cols<T>(stg + B.up_soff[q], fr + S.front_off[s], mm, ns, 0, mm);
+        }
+        const int q = q0 + warp;
+        const bool mine = q < q1;
+        int rank = 0, s = 0, start = 0, ns = 0, mm = 0, xo = 0;
+        if (mine) {
+            rank = B.n_lower_top + q;
+            s = B.top_order[rank];
+            start = S.sup_start[s];
+            ns = S.sup_start[s + 1] - start;
+            mm = ns + S.row_ptr[s + 1] - S.row_ptr[s];
+            xo = B.up_xoff[q];
             if (fwd) {
-                warp_stage_cols<T>(Fs, fr + S.front_off[s], mm, mm, 0, ns);
                 const int *xr = B.top_xrow + B.top_xptr[rank];
                 for (int i = lane; i < mm; i += 32) {
                     T acc = i < ns ? xu[xo + i] : T(0);
@@ -890,23 +887,25 @@ __device__ void upper_solve(const DevProblem &P, const DevWork &W, const DevSym 
                     v[i] = acc;
                 }
                 for (int i = lane; i < ns; i += 32) pi[i] = ip[start + i];
-                cp_async_wait_all();
-                __syncwarp();
+            } else {
+                const int *rm = B.up_rmap + B.up_rmap_ptr[q];
+                for (int i = lane; i < mm; i += 32) v[i] = i < ns ? xu[xo + i] : xu[rm[i - ns]];
+            }
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        if (mine) {
+            const T *Fs = stg + B.up_soff[q];
+            if (fwd) {
                 fwd_cols<T>(Fs, mm, 0, 0, ns, ns, mm, v, sc, [&](int i) { return pi[i]; }, true);
                 for (int i = lane; i < ns; i += 32) xu[xo + i] = v[i];
                 double *us = uv + S.uvec_off[s];
                 for (int a = lane; a < mm - ns; a += 32) us[a] = (double)v[ns + a];
             } else {
-                warp_stage_cols<T>(Fs, fr + S.front_off[s], mm, ns, 0, mm);
-                const int *rm = B.up_rmap + B.up_rmap_ptr[q];
-                for (int i = lane; i < mm; i += 32) v[i] = i < ns ? xu[xo + i] : xu[rm[i - ns]];
-                cp_async_wait_all();
-                __syncwarp();
                 if (mm > ns) bwd_u12<T>(Fs, ns, 0, ns, mm, ns, v);
                 bwd_cols<T>(Fs, ns, 0, 0, ns, ns, v);
                 for (int i = lane; i < ns; i += 32) xu[xo + i] = v[i];
             }
-            __syncwarp();
         }
         __syncthreads();
     }

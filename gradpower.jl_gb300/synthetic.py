@@ -377,10 +377,33 @@ def planar70k(seed=4, n_scenarios=8):
     return _planar("planar70k", seed, 70000, 5000, 0.55, n_scenarios, 1.0, "high_degree")
 
 
+def planar2k_stressed(seed=2, n_scenarios=256):
+    """planar2k with four times the loads (P ~ U[0.02, 0.12] pu) and line
+    charging b ~ U[0, 0.1] pu (a quarter of the 39-bus range): the heaviest
+    variant of the 2,000-bus grid that keeps a power-flow solution (b up to
+    0.2 also solves; 0.4 does not)."""
+    w = _planar("planar2k_stressed", seed, 2000, 400, 0.6, n_scenarios, 2.0, "random", b_range=(0.0, 0.1),
+                load_range=(0.02, 0.12))
+    w.notes.append("stressed variant: loads x4 (U[0.02, 0.12] pu), line charging b ~ U[0, 0.1] pu")
+    return w
+
+
+def planar70k_charged(seed=4, n_scenarios=8):
+    """planar70k with line charging b ~ U[0, 0.01] pu, the most the
+    70,000-bus grid takes: b up to 0.02, or loads 1.5 times heavier, leave
+    its power flow without a solution."""
+    w = _planar("planar70k_charged", seed, 70000, 5000, 0.55, n_scenarios, 1.0, "high_degree",
+                b_range=(0.0, 0.01))
+    w.notes.append("charged variant: line charging b ~ U[0, 0.01] pu")
+    return w
+
+
 WORKLOADS = {
     "two_bus": two_bus,
     "ring39": ring39,
     "planar2k": planar2k,
     "planar2k_adj": planar2k_adj,
     "planar70k": planar70k,
+    "planar2k_stressed": planar2k_stressed,
+    "planar70k_charged": planar70k_charged,
 }

@@ -96,3 +96,23 @@ def test_planar2k_256_scenarios_full_horizon(G, orc):
     assert np.array_equal(f64["iters"][:32], o["iters"])
     assert _rel(f64["traj"][:32], o["traj"]) <= RTOL
     assert max(_errors(c.PA, mx["traj"][:32], o["traj"])) <= TOL
+
+
+@pytest.mark.parametrize("name,M,n_or", [("planar2k_stressed", 64, 8), ("planar70k_charged", 2, 2)])
+def test_harder_grids(G, orc, name, M, n_or):
+    """The precision form on harder grids: planar2k with four times the loads
+    and line charging b ~ U[0, 0.1] pu (2 s), and planar70k with line
+    charging b ~ U[0, 0.01] pu (1 s).  The FP64 path against the oracle
+    (identical Newton counts, 1e-9), the mixed path against both (1e-6)."""
+    c, w = synthetic_case(name, M)
+    ns = int(round(w.tf / DT))
+    runs = _gpu_runs(G, c, ns, (LY.SOLVER_SCHUR_FP64, LY.SOLVER_SCHUR_MIXED))
+    f64, mx = runs[LY.SOLVER_SCHUR_FP64], runs[LY.SOLVER_SCHUR_MIXED]
+    assert np.all(f64["status"] == 0) and np.all(mx["status"] == 0)
+    assert max(_errors(c.PA, mx["traj"], f64["traj"])) <= TOL
+    sub = type(c)(c.ps, c.dp, c.faults[:n_or], n_or)
+    o = run_oracle(orc, sub, ns, itermax=30, nthreads=THREADS)
+    assert np.all(o["status"] == 0)
+    assert np.array_equal(f64["iters"][:n_or], o["iters"])
+    assert _rel(f64["traj"][:n_or], o["traj"]) <= RTOL
+    assert max(_errors(c.PA, mx["traj"][:n_or], o["traj"])) <= TOL
