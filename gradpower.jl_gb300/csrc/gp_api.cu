@@ -506,10 +506,6 @@ struct HostBlk {
     int n_top_levels = 0, top_max_front = 1, top_max_xent = 1;
     std::vector<int> top_order, top_rank;
     std::vector<int> top_xptr, top_xrow, top_xent;   // extend-add lists of the top region
-    // upper part of the top region (narrow levels near the root), solved by
-    // one CTA per scenario (gp_solve.cu, upper_kernel): ranks from n_lower_top
-    int n_lower_top = 0, up_nlev = 0, n_xu = 0, up_stage = 0;
-    std::vector<int> up_lev_ptr{0}, up_xoff, up_soff, up_xrow, up_rmap_ptr{0}, up_rmap;
 };
 
 void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
@@ -653,74 +649,6 @@ void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
         B.top_xptr.push_back((int)B.top_xrow.size());
         B.top_max_xent = std::max(B.top_max_xent, B.top_xrow.back() - B.top_xrow[B.top_xptr[B.top_xptr.size() - 2]]);
     }
-    // upper part: the levels near the root that have at most
-    // solve_upper_width() supernodes each, as long as their pivot
-    // rows fit the upper kernel's shared vector; every ancestor of an upper
-    // supernode is upper, so its update rows are upper rows
-    std::vector<int> lev_cnt(ntl, 0);
-    for (int s : B.top_order) lev_cnt[tlev[s]]++;
-    int U = ntl;
-    while (U > 0 && lev_cnt[U - 1] <= gp::solve_upper_width()) U--;
-    // and as long as the shared memory of the upper kernel holds its rows
-    // and the factor entries of its widest level (staged a level at a time:
-    // pivot columns forward, pivot rows backward, ns * mm entries a front)
-    std::vector<long> lev_stage(ntl, 0);
-    for (int s : B.top_order) lev_stage[tlev[s]] += (long)sym.front_n(s) * sym.front_m(s);
-    auto upper_rows = [&](int from) {
-        long n = 0;
-        for (int s : B.top_order)
-            if (tlev[s] >= from) n += sym.front_n(s);
-        return n;
-    };
-    auto upper_stage = [&](int from) {
-        long n = 0;
-        for (int d = from; d < ntl; d++) n = std::max(n, lev_stage[d]);
-        return n;
-    };
-    while (U < ntl && (upper_rows(U) > gp::solve_upper_max_rows() ||
-                       gp::solve_upper_bytes((int)upper_rows(U), (int)upper_stage(U), B.top_max_front) >
-                           gp::solve_upper_smem()))
-        U++;
-    B.n_lower_top = 0;
-    for (int s : B.top_order)
-        if (tlev[s] < U) B.n_lower_top++;
-    B.up_nlev = ntl - U;
-    B.up_lev_ptr.assign(1, 0);
-    B.up_xoff.clear();
-    B.up_soff.clear();
-    B.up_xrow.clear();
-    B.up_stage = U < ntl ? (int)upper_stage(U) : 0;
-    B.up_rmap_ptr.assign(1, 0);
-    B.up_rmap.clear();
-    std::vector<int> slot_of_row(sym.n, -1);
-    for (int q = B.n_lower_top; q < (int)B.top_order.size(); q++) {
-        const int s = B.top_order[q];
-        B.up_xoff.push_back((int)B.up_xrow.size());
-        for (int i = sym.sup_start[s]; i < sym.sup_start[s + 1]; i++) {
-            slot_of_row[i] = (int)B.up_xrow.size();
-            B.up_xrow.push_back(i);
-        }
-    }
-    for (int d = U; d < ntl; d++) {
-        int c = B.up_lev_ptr.back(), so = 0;
-        for (int s : B.top_order)
-            if (tlev[s] == d) {
-                c++;
-                B.up_soff.push_back(so);   // staging offset within the level (upper order is by level)
-                so += sym.front_n(s) * sym.front_m(s);
-            }
-        B.up_lev_ptr.push_back(c);
-    }
-    for (int q = B.n_lower_top; q < (int)B.top_order.size(); q++) {
-        const int s = B.top_order[q];
-        for (int a = 0; a < sym.front_r(s); a++) {
-            const int slot = slot_of_row[sym.rows[sym.row_ptr[s] + a]];
-            if (slot < 0) fail(GP_E_INTERNAL, "upper supernode %d: update row outside the upper rows", s);
-            B.up_rmap.push_back(slot);
-        }
-        B.up_rmap_ptr.push_back((int)B.up_rmap.size());
-    }
-    B.n_xu = (int)B.up_xrow.size();
 }
 
 // Host emulation of the device factorisation (gp_dag.cu): the same front
@@ -855,57 +783,16 @@ void host_fwd_front(const double *F, const int *perm, int ns, int mm, Staged &v,
     }
 }
 
-// ld: leading dimension of F (mm for a front, ns for its pivot rows alone).
-void host_bwd_front(const double *F, int ns, int mm, Staged &v, long o, int ld = -1) {
-    if (ld < 0) ld = mm;
+void host_bwd_front(const double *F, int ns, int mm, Staged &v, long o) {
     for (int i = 0; i < ns; i++) {
         double acc = 0.0;
-        for (int a = 0; a < mm - ns; a++) acc += F[i + (size_t)(ns + a) * ld] * v[o + ns + a];
+        for (int a = 0; a < mm - ns; a++) acc += F[i + (size_t)(ns + a) * mm] * v[o + ns + a];
         v[o + i] -= acc;
     }
     for (int k = ns - 1; k >= 0; k--) {
-        const double tk = v[o + k] * F[k + (size_t)k * ld];
+        const double tk = v[o + k] * F[k + (size_t)k * mm];
         v[o + k] = tk;
-        for (int i = 0; i < k; i++) v[o + i] -= F[i + (size_t)k * ld] * tk;
-    }
-}
-
-// Checks the upper part's maps against the symbolic structure, as the upper
-// kernel (gp_solve.cu) indexes them: every slot inside the shared vector,
-// pivot rows and update rows landing on their own rows, levels in order.
-void check_upper(const gp::Symbolic &S, const HostBlk &B) {
-    const int nu = (int)B.top_order.size() - B.n_lower_top;
-    if (nu < 0 || (int)B.up_xoff.size() != nu || (int)B.up_rmap_ptr.size() != nu + 1 ||
-        (int)B.up_lev_ptr.size() != B.up_nlev + 1 || B.up_lev_ptr.back() != nu || B.n_xu != (int)B.up_xrow.size())
-        fail(GP_E_INTERNAL, "upper part: inconsistent sizes");
-    if (B.n_xu > gp::solve_upper_max_rows()) fail(GP_E_INTERNAL, "upper part: %d rows above the limit", B.n_xu);
-    for (int l = 0; l < B.up_nlev; l++)
-        if (B.up_lev_ptr[l + 1] - B.up_lev_ptr[l] > gp::solve_upper_width())
-            fail(GP_E_INTERNAL, "upper part: level %d wider than %d", l, gp::solve_upper_width());
-    for (int q = 0; q < nu; q++) {
-        const int s = B.top_order[B.n_lower_top + q];
-        const int ns = S.front_n(s), r = S.front_r(s);
-        if (B.up_xoff[q] < 0 || B.up_xoff[q] + ns > B.n_xu) fail(GP_E_INTERNAL, "upper part: slots of %d", s);
-        if ((int)B.up_soff.size() != nu || B.up_soff[q] < 0 || B.up_soff[q] + ns * (ns + r) > B.up_stage)
-            fail(GP_E_INTERNAL, "upper part: staging area of %d", s);
-        for (int i = 0; i < ns; i++)
-            if (B.up_xrow[B.up_xoff[q] + i] != S.sup_start[s] + i) fail(GP_E_INTERNAL, "upper part: row of %d", s);
-        if (B.up_rmap_ptr[q + 1] - B.up_rmap_ptr[q] != r) fail(GP_E_INTERNAL, "upper part: update rows of %d", s);
-        for (int a = 0; a < r; a++) {
-            const int slot = B.up_rmap[B.up_rmap_ptr[q] + a];
-            if (slot < 0 || slot >= B.n_xu || B.up_xrow[slot] != S.rows[S.row_ptr[s] + a])
-                fail(GP_E_INTERNAL, "upper part: update row %d of %d", a, s);
-        }
-        // a parent of an upper supernode is upper, at a later level
-        const int p = S.parent[s];
-        if (p >= 0 && B.top_rank[p] <= B.n_lower_top + q) fail(GP_E_INTERNAL, "upper part: parent order of %d", s);
-    }
-    // a lower top supernode or a block root never has an upper child after
-    // it: the children of an upper supernode come before it in top order
-    for (int q = 0; q < B.n_lower_top; q++) {
-        const int s = B.top_order[q];
-        for (int c = S.child_ptr[s]; c < S.child_ptr[s + 1]; c++)
-            if (B.top_rank[S.children[c]] >= B.n_lower_top) fail(GP_E_INTERNAL, "upper child below a lower supernode");
+        for (int i = 0; i < k; i++) v[o + i] -= F[i + (size_t)k * mm] * tk;
     }
 }
 
@@ -966,54 +853,11 @@ void host_block_solve(const gp::Symbolic &S, const HostBlk &B, const std::vector
             for (int e = xr[i]; e < xr[i + 1]; e++) acc += uvec[B.top_xent[e]];
             tv[i] = acc;
         }
-        if (t >= B.n_lower_top) continue;   // the upper part below
         host_fwd_front(fronts.data() + S.front_off[s], ipiv.data() + start, ns, mm, tv, 0);
         for (int i = 0; i < ns; i++) x[start + i] = tv[i];
         for (int a = 0; a < r; a++) uvec[S.uvec_off[s] + a] = tv[ns + a];
     }
-    // the upper part as upper_kernel runs it: the upper rows in their own
-    // vector, forward level by level, then backward from the root
-    check_upper(S, B);
-    {
-        Staged xu(std::max(1, B.n_xu), "upper vector");
-        for (int k = 0; k < B.n_xu; k++) xu[k] = x[B.up_xrow[k]];
-        for (int l = 0; l < B.up_nlev; l++)
-            for (int q = B.up_lev_ptr[l]; q < B.up_lev_ptr[l + 1]; q++) {
-                const int rank = B.n_lower_top + q, s = B.top_order[rank];
-                const int start = S.sup_start[s], ns = S.front_n(s), r = S.front_r(s), mm = ns + r;
-                Staged tv(B.top_max_front, "upper front vector");
-                const int *xr = B.top_xrow.data() + B.top_xptr[rank];
-                for (int i = 0; i < mm; i++) {
-                    double acc = i < ns ? (double)xu[B.up_xoff[q] + i] : 0.0;
-                    for (int e = xr[i]; e < xr[i + 1]; e++) acc += uvec[B.top_xent[e]];
-                    tv[i] = acc;
-                }
-                // the pivot columns through the staging area, as the kernel copies them
-                Staged stg(std::max(1, B.up_stage), "upper staging");
-                const double *F = fronts.data() + S.front_off[s];
-                for (int e = 0; e < mm * ns; e++) stg[B.up_soff[q] + e] = F[e];
-                host_fwd_front(&stg[B.up_soff[q]], ipiv.data() + start, ns, mm, tv, 0);
-                for (int i = 0; i < ns; i++) xu[B.up_xoff[q] + i] = tv[i];
-                for (int a = 0; a < r; a++) uvec[S.uvec_off[s] + a] = tv[ns + a];
-            }
-        for (int l = B.up_nlev - 1; l >= 0; l--)
-            for (int q = B.up_lev_ptr[l]; q < B.up_lev_ptr[l + 1]; q++) {
-                const int s = B.top_order[B.n_lower_top + q];
-                const int ns = S.front_n(s), r = S.front_r(s), mm = ns + r;
-                Staged tv(B.top_max_front, "upper front vector");
-                for (int i = 0; i < mm; i++)
-                    tv[i] = i < ns ? (double)xu[B.up_xoff[q] + i] : (double)xu[B.up_rmap[B.up_rmap_ptr[q] + i - ns]];
-                // the pivot rows through the staging area (leading dimension ns)
-                Staged stg(std::max(1, B.up_stage), "upper staging");
-                const double *F = fronts.data() + S.front_off[s];
-                for (int c = 0; c < mm; c++)
-                    for (int i = 0; i < ns; i++) stg[B.up_soff[q] + i + (long)c * ns] = F[i + (size_t)c * mm];
-                host_bwd_front(&stg[B.up_soff[q]], ns, mm, tv, 0, ns);
-                for (int i = 0; i < ns; i++) xu[B.up_xoff[q] + i] = tv[i];
-            }
-        for (int k = 0; k < B.n_xu; k++) x[B.up_xrow[k]] = xu[k];
-    }
-    for (int t = B.n_lower_top - 1; t >= 0; t--) {
+    for (int t = ntop - 1; t >= 0; t--) {
         const int s = B.top_order[t];
         const int start = S.sup_start[s], ns = S.front_n(s), r = S.front_r(s), mm = ns + r;
         Staged tv(B.top_max_front, "top vector");
@@ -1164,16 +1008,6 @@ void build_blocks(gp_layout *L, const gp::Symbolic &sym) {
     B.top_xptr = A.upload(H.top_xptr);
     B.top_xrow = A.upload(H.top_xrow);
     B.top_xent = A.upload(H.top_xent);
-    B.n_lower_top = H.n_lower_top;
-    B.up_nlev = H.up_nlev;
-    B.n_xu = H.n_xu;
-    B.up_lev_ptr = A.upload(H.up_lev_ptr);
-    B.up_xoff = A.upload(H.up_xoff);
-    B.up_soff = A.upload(H.up_soff);
-    B.up_stage = H.up_stage;
-    B.up_xrow = A.upload(H.up_xrow);
-    B.up_rmap_ptr = A.upload(H.up_rmap_ptr);
-    B.up_rmap = A.upload(H.up_rmap);
     L->n_top_levels = H.n_top_levels;
     const int sc = gp::solve_configure(B, L->SG);
     if (sc == -2) fail(GP_E_INVALID, "front of %d rows exceeds the solve kernels' staging area", B.top_max_front);
@@ -1532,8 +1366,7 @@ int enqueue_solve(gp_layout *L, int variant, int *nfac_out) {
     const gp::DevDag &D = L->D;
     const int nfac = (D.n_small > 0) + (D.nsup > D.n_small);
     const gp::DevBlk &B = L->B;
-    const int nsolve = (B.nblk + B.n_lower_top) > 0;   // one dataflow kernel per direction
-    const int nupper = B.up_nlev > 0;                   // and the upper kernel before the backward one
+    const int nsolve = (B.nblk + B.n_top) > 0;   // one fused kernel per direction
     int launches = 2, facs = 0;   // dag_begin, update
     mark(L, 3);
     gp::launch_dag_begin(D, L->st);
@@ -1546,7 +1379,7 @@ int enqueue_solve(gp_layout *L, int variant, int *nfac_out) {
         mark(L, 5);
         gp::launch_solve_bwd(L->P, L->W, L->S, B, D, L->SG, fs, L->st);
         gp::launch_wb_correct(L->P, L->W, L->wb_W1, L->wb_W2, L->wb_Hinv, L->wb_s, L->st);
-        launches += 2 * nsolve + nupper + 2;
+        launches += 2 * nsolve + 2;
     } else if (variant < 0) {
         const gp::FrontSel fs{nullptr, L->S.fronts, nullptr, 1};
         gp::launch_dag_factor<double>(L->P, L->W, L->S, D, L->G64, L->S.fronts, L->W.active, 1, L->st);
@@ -1554,7 +1387,7 @@ int enqueue_solve(gp_layout *L, int variant, int *nfac_out) {
         mark(L, 5);
         gp::launch_solve_bwd(L->P, L->W, L->S, B, D, L->SG, fs, L->st);
         facs = nfac;
-        launches += nfac + nsolve + nupper;
+        launches += nfac + nsolve;
     } else {
         const gp::FrontSel fs{L->Mx.fronts, L->S.fronts, L->Mx.refac, 1};
         if (variant & 1) {
@@ -1575,7 +1408,7 @@ int enqueue_solve(gp_layout *L, int variant, int *nfac_out) {
         gp::launch_solve_fwd(L->P, L->W, L->S, B, D, L->SG, fs, L->st);
         mark(L, 5);
         gp::launch_solve_bwd(L->P, L->W, L->S, B, D, L->SG, fs, L->st);
-        launches += facs + 2 * nsolve + nupper;
+        launches += facs + 2 * nsolve;
     }
     mark(L, 6);
     gp::launch_update(L->P, L->W, L->S, L->d_state_maps, L->st);
@@ -1782,7 +1615,7 @@ void wb_prepare(gp_layout *L, double dt) {
            "woodbury column");
     }
     gp::launch_wb_setup(L->P, L->wb_W1, L->wb_W2, L->wb_Hinv, L->st);
-    L->launches += 14 + (L->D.n_small > 0) + (L->D.nsup > L->D.n_small) + 2 * (L->B.up_nlev > 0);
+    L->launches += 14 + (L->D.n_small > 0) + (L->D.nsup > L->D.n_small);
     L->factor_launches += (L->D.n_small > 0) + (L->D.nsup > L->D.n_small);
 }
 
@@ -2398,7 +2231,6 @@ int32_t gp_reduced_selftest(const gp_problem *prob, const int32_t *s_rowptr, con
     out[7] = hb.max_n;
     out[9] = hb.top_order.empty() ? 0 : hb.top_max_front;
     out[10] = hb.max_v;
-    out[11] = hb.n_xu;
     // S^T from the transposed assembly lists (the adjoint's system):
     // relative residual of S^T y = rhs
     {

@@ -216,16 +216,6 @@ struct DevBlk {
     const int *top_xptr;         // [n_top+1] first row pointer of each top supernode
     const int *top_xrow;         // row pointers into top_xent
     const int *top_xent;
-    // upper part of the top region: ranks [n_lower_top, n_top), solved by one
-    // CTA per scenario with the upper rows' solution in shared memory
-    int n_lower_top, up_nlev, n_xu;
-    int up_stage;                // factor entries of the widest upper level (staging area)
-    const int *up_lev_ptr;       // [up_nlev+1] upper supernodes (rank - n_lower_top) by level, leaves first
-    const int *up_xoff;          // [n_top - n_lower_top] first slot of the supernode's pivot rows
-    const int *up_soff;          // [n_top - n_lower_top] its staging offset within its level
-    const int *up_xrow;          // [n_xu] permuted row of each slot
-    const int *up_rmap_ptr;      // [n_top - n_lower_top + 1]
-    const int *up_rmap;          // slot of each update row of each upper supernode
 };
 
 // Factors of the triangular solves, per scenario: FP64 when f32 is null or
@@ -242,17 +232,7 @@ struct FrontSel {
 struct SolveGrid {
     int blk_bytes = 0, top_bytes = 0;   // dynamic shared memory per CTA
     int top_fwd = 0, top_bwd = 0;       // resident CTAs of the dataflow kernels
-    int up_bytes = 0;                   // dynamic shared memory of the upper kernel
 };
-
-// Narrowest top-region level (supernodes) and most pivot rows of the part
-// that the upper kernel solves.
-int solve_upper_width();
-int solve_upper_max_rows();
-// Shared memory of the upper kernel for n_xu rows, a level of `stage` factor
-// entries and fronts of at most tmf rows, and the most it may use.
-int solve_upper_bytes(int n_xu, int stage, int tmf);
-int solve_upper_smem();
 
 int solve_configure(const DevBlk &B, SolveGrid &g);
 void launch_solve_fwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B, const DevDag &D,

@@ -16,14 +16,6 @@
 //    the done flags of the tasks it depends on; one warp then sweeps the
 //    front from shared memory.  One launch per direction.
 // Forward: blocks, then top.  Backward: top, then blocks.
-//  - upper: the narrow levels of the top region near the root (at most
-//    solve_upper_width() supernodes per level).  One CTA per scenario solves
-//    them forward and then backward with the upper rows' solution in shared
-//    memory, a level per step and a CTA barrier between levels: no flags and
-//    no waits, where each level of the dataflow cost a flag round trip
-//    through L2.  It runs between the two dataflow kernels (at the start of
-//    the backward solve); the dataflow kernels take the top region's lower
-//    levels only and treat upper parents as done.
 //
 // Within a front, one warp holds up to kMaxJ rows per lane in registers
 // (row i in lane i % 32, register i / 32).  The unit-lower and upper
@@ -57,10 +49,6 @@ constexpr int kTopThreads = 128;             // threads of a top-region task
 constexpr int kTopStage = 20 * 1024;         // shared memory for a task's factor columns
 constexpr int kMaxJ = 8;       // register rows per lane: fronts up to 256 rows
 constexpr int kBlkFront = 64;  // largest front inside a block (two rows per lane)
-constexpr int kUpThreads = 512;           // threads of the upper kernel (one CTA per scenario)
-constexpr int kUpWidth = 8;               // a level of at most this many supernodes is upper
-constexpr int kUpMaxRows = 8192;          // most pivot rows of the upper part (shared vector)
-constexpr int kUpSmem = 200 * 1024;       // most shared memory of the upper kernel
 
 __host__ __device__ constexpr int align16(int b) { return (b + 15) & ~15; }
 
@@ -535,14 +523,9 @@ __device__ bool wait_top_children(const DevSym &S, const DevBlk &B, const DevDag
     return *s_ok != 0;
 }
 
-// Supernode s is in the upper part (solved before the backward dataflow
-// kernel starts).
-__device__ __forceinline__ bool is_upper(const DevBlk &B, int s) { return B.top_rank[s] >= B.n_lower_top; }
-
-__device__ bool wait_top_parent(const DevBlk &B, const DevDag &D, int s, int m, int M, int epoch, int *s_ok) {
+__device__ bool wait_top_parent(const DevDag &D, int s, int m, int M, int epoch, int *s_ok) {
     const int par = D.parent[s];
-    if (threadIdx.x == 0)
-        *s_ok = (par < 0 || is_upper(B, par)) ? 1 : (int)wait_epoch(D.bdone + (size_t)par * M + m, epoch, D.err, D.wait_limit);
+    if (threadIdx.x == 0) *s_ok = par < 0 ? 1 : (int)wait_epoch(D.bdone + (size_t)par * M + m, epoch, D.err, D.wait_limit);
     __syncthreads();
     return *s_ok != 0;
 }
@@ -626,7 +609,7 @@ __device__ void bwd_top_task(const DevProblem &P, const DevWork &W, const DevSym
     // then U11 from the last pivot column
     int c1 = t.mm, c0 = max(0, t.mm - cap);
     stage_cols<T>(Fs, F, t.mm, t.ns, c0, c1);
-    if (!wait_top_parent(B, D, t.s, t.m, P.M, epoch, s_ok) && threadIdx.x == 0) atomicOr(W.status + t.m, 8);
+    if (!wait_top_parent(D, t.s, t.m, P.M, epoch, s_ok) && threadIdx.x == 0) atomicOr(W.status + t.m, 8);
     for (int a = threadIdx.x; a < t.r; a += blockDim.x) v[t.ns + a] = (T)__ldcg(x + pi[a]);
     for (;;) {
         cp_async_wait_all();
@@ -724,7 +707,7 @@ __global__ void __launch_bounds__(kTopThreads, 8) fwd_solve_kernel(DevProblem P,
             }
         }
     }
-    const int n_tasks = B.n_lower_top * M;
+    const int n_tasks = B.n_top * M;
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) s_task = atomicAdd(D.ctr + 2, 1);
@@ -750,16 +733,16 @@ __global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P,
     const int lane = threadIdx.x & 31;
     const int M = P.M;
     const int epoch = *D.epoch;
-    const int n_tasks = B.n_lower_top * M;
+    const int n_tasks = B.n_top * M;
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) s_task = atomicAdd(D.ctr + 3, 1);
         __syncthreads();
         const int t = s_task;
         if (t >= n_tasks) break;
-        const int s = B.top_order[B.n_lower_top - 1 - t / M], m = t % M;
+        const int s = B.top_order[B.n_top - 1 - t / M], m = t % M;
         if (!W.active[m]) continue;
-        const TopCtx c = top_ctx(S, s, m, B.n_lower_top - 1 - t / M);
+        const TopCtx c = top_ctx(S, s, m, B.n_top - 1 - t / M);
         if (use64(fs, m)) bwd_top_task<double>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
         else bwd_top_task<float>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
         __syncthreads();
@@ -775,8 +758,7 @@ __global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P,
         t = __shfl_sync(FULL, t, 0);
         if (t >= n_blk) break;
         const int blk = (int)(t / MP), u = (int)(t % MP);
-        int par = D.parent[B.ent0[B.blk_ptr[blk + 1] - 1].x];
-        if (par >= 0 && is_upper(B, par)) par = -1;   // solved by the upper kernel, before this launch
+        const int par = D.parent[B.ent0[B.blk_ptr[blk + 1] - 1].x];
         if (MP != M) {
             const int m0 = 2 * u, m1 = 2 * u + 1;
             if (m1 < M && pair_ok(W, fs, m0) && pair_ok(W, fs, m1)) {
@@ -818,110 +800,6 @@ __global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P,
     }
 }
 
-
-// ---- upper part: one CTA per scenario ------------------------------------
-// Shared memory: the upper rows' vector (double slots, whatever the factor
-// type), the staging area of one level's factor entries (up_stage entries,
-// sized for double), then per warp a front vector, a gather scratch (both
-// sized for double) and the pivot permutation.
-__host__ __device__ constexpr int up_warp_bytes(int tmf) { return align16(tmf * (8 + 8 + 4)); }
-__host__ __device__ constexpr int up_bytes(int n_xu, int stage, int tmf) {
-    return align16(n_xu * 8) + align16(stage * 8) + (kUpThreads / 32) * up_warp_bytes(tmf);
-}
-
-// Forward then backward solve of the upper supernodes of scenario m with
-// factors of type T, a level per step and a warp per supernode (a level has
-// at most kUpWidth <= warps supernodes).  Each step: all threads copy the
-// level's factor entries into shared memory (cp.async; forward: the pivot
-// columns of each front, backward: its pivot rows); while the copies are in
-// flight each warp builds its front vector (forward: the upper rows plus
-// the children's update vectors from global memory; backward: the upper
-// rows and the ancestors' solution, both in shared memory); one barrier;
-// the sweeps from shared memory; another barrier.  The forward part is
-// skipped when the FP64 factorisation already did it.  Ends with the upper
-// rows written to xperm.
-template <class T>
-__device__ void upper_solve(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B,
-                            const FrontSel &fs, int m, bool do_fwd, unsigned char *smem) {
-    static_assert(kUpWidth <= kUpThreads / 32, "one supernode a warp per level");
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int tmf = B.top_max_front;
-    T *xu = reinterpret_cast<T *>(smem);
-    T *stg = reinterpret_cast<T *>(smem + align16(B.n_xu * 8));
-    unsigned char *wb = smem + align16(B.n_xu * 8) + align16(B.up_stage * 8) + (size_t)warp * up_warp_bytes(tmf);
-    T *v = reinterpret_cast<T *>(wb);
-    T *sc = reinterpret_cast<T *>(wb + tmf * 8);
-    int *pi = reinterpret_cast<int *>(wb + tmf * 16);
-    double *x = W.xperm + (size_t)m * P.n_red;
-    double *uv = S.uvec + (size_t)m * S.uvec_total;
-    const T *fr = front_base<T>(fs) + (size_t)(fs.shared ? 0 : m) * S.front_total;
-    const int *ip = S.ipiv + (size_t)(fs.shared ? 0 : m) * S.n;
-    for (int k = threadIdx.x; k < B.n_xu; k += blockDim.x) xu[k] = (T)x[B.up_xrow[k]];
-    __syncthreads();
-    for (int step = do_fwd ? 0 : B.up_nlev; step < 2 * B.up_nlev; step++) {
-        const bool fwd = step < B.up_nlev;
-        const int l = fwd ? step : 2 * B.up_nlev - 1 - step;
-        const int q0 = B.up_lev_ptr[l], q1 = B.up_lev_ptr[l + 1];
-        for (int q = q0; q < q1; q++) {
-            const int s = B.top_order[B.n_lower_top + q];
-            const int ns = S.sup_start[s + 1] - S.sup_start[s];
-            const int mm = ns + S.row_ptr[s + 1] - S.row_ptr[s];
-            if (fwd) stage_cols<T>(stg + B.up_soff[q], fr + S.front_off[s], mm, mm, 0, ns);
-            else stage_cols<T>(stg + B.up_soff[q], fr + S.front_off[s], mm, ns, 0, mm);
-        }
-        const int q = q0 + warp;
-        const bool mine = q < q1;
-        int rank = 0, s = 0, start = 0, ns = 0, mm = 0, xo = 0;
-        if (mine) {
-            rank = B.n_lower_top + q;
-            s = B.top_order[rank];
-            start = S.sup_start[s];
-            ns = S.sup_start[s + 1] - start;
-            mm = ns + S.row_ptr[s + 1] - S.row_ptr[s];
-            xo = B.up_xoff[q];
-            if (fwd) {
-                const int *xr = B.top_xrow + B.top_xptr[rank];
-                for (int i = lane; i < mm; i += 32) {
-                    T acc = i < ns ? xu[xo + i] : T(0);
-                    for (int e = xr[i]; e < xr[i + 1]; e++) acc += (T)uv[B.top_xent[e]];
-                    v[i] = acc;
-                }
-                for (int i = lane; i < ns; i += 32) pi[i] = ip[start + i];
-            } else {
-                const int *rm = B.up_rmap + B.up_rmap_ptr[q];
-                for (int i = lane; i < mm; i += 32) v[i] = i < ns ? xu[xo + i] : xu[rm[i - ns]];
-            }
-        }
-        cp_async_wait_all();
-        __syncthreads();
-        if (mine) {
-            const T *Fs = stg + B.up_soff[q];
-            if (fwd) {
-                fwd_cols<T>(Fs, mm, 0, 0, ns, ns, mm, v, sc, [&](int i) { return pi[i]; }, true);
-                for (int i = lane; i < ns; i += 32) xu[xo + i] = v[i];
-                double *us = uv + S.uvec_off[s];
-                for (int a = lane; a < mm - ns; a += 32) us[a] = (double)v[ns + a];
-            } else {
-                if (mm > ns) bwd_u12<T>(Fs, ns, 0, ns, mm, ns, v);
-                bwd_cols<T>(Fs, ns, 0, 0, ns, ns, v);
-                for (int i = lane; i < ns; i += 32) xu[xo + i] = v[i];
-            }
-        }
-        __syncthreads();
-    }
-    for (int k = threadIdx.x; k < B.n_xu; k += blockDim.x) x[B.up_xrow[k]] = (double)xu[k];
-}
-
-__global__ void __launch_bounds__(kUpThreads) upper_kernel(DevProblem P, DevWork W, DevSym S, DevBlk B, FrontSel fs) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const int m = blockIdx.x;
-    if (!W.active[m]) return;
-    const bool d = use64(fs, m);
-    const bool do_fwd = !(d && fs.fused64);
-    if (d) upper_solve<double>(P, W, S, B, fs, m, do_fwd, smem);
-    else upper_solve<float>(P, W, S, B, fs, m, do_fwd, smem);
-}
-
 int grid_for(int resident, long long tasks, int per_block) {
     const long long need = (tasks + per_block - 1) / per_block;
     return (int)std::max<long long>(1, std::min<long long>(need, resident));
@@ -930,10 +808,6 @@ int grid_for(int resident, long long tasks, int per_block) {
 }  // namespace
 
 int solve_block_front_limit() { return kBlkFront; }
-int solve_upper_width() { return kUpWidth; }
-int solve_upper_max_rows() { return kUpMaxRows; }
-int solve_upper_bytes(int n_xu, int stage, int tmf) { return up_bytes(n_xu, stage, std::max(1, tmf)); }
-int solve_upper_smem() { return kUpSmem; }
 
 int solve_configure(const DevBlk &B, SolveGrid &g) {
     int dev = 0, nsm = 0, occ = 0;
@@ -961,27 +835,20 @@ int solve_configure(const DevBlk &B, SolveGrid &g) {
             cudaSuccess || occ < 1)
         return -1;
     g.top_bwd = nsm * occ;
-    g.up_bytes = up_bytes(B.n_xu, B.up_stage, std::max(1, B.top_max_front));
-    if (B.up_nlev > 0 &&
-        cudaFuncSetAttribute(upper_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, g.up_bytes) != cudaSuccess) {
-        cudaGetLastError();
-        return -1;
-    }
     return 0;
 }
 
 void launch_solve_fwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B, const DevDag &D,
                       const SolveGrid &g, FrontSel fs, cudaStream_t st) {
-    const long long work = std::max((long long)B.nblk * P.M / kBlkWarps + 1, (long long)B.n_lower_top * P.M);
-    if (B.nblk + B.n_lower_top > 0)
+    const long long work = std::max((long long)B.nblk * P.M / kBlkWarps + 1, (long long)B.n_top * P.M);
+    if (B.nblk + B.n_top > 0)
         fwd_solve_kernel<<<grid_for(g.top_fwd, work, 1), kTopThreads, g.top_bytes, st>>>(P, W, S, B, D, fs);
 }
 
 void launch_solve_bwd(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B, const DevDag &D,
                       const SolveGrid &g, FrontSel fs, cudaStream_t st) {
-    if (B.up_nlev > 0) upper_kernel<<<P.M, kUpThreads, g.up_bytes, st>>>(P, W, S, B, fs);
-    const long long work = std::max((long long)B.nblk * P.M / kBlkWarps + 1, (long long)B.n_lower_top * P.M);
-    if (B.nblk + B.n_lower_top > 0)
+    const long long work = std::max((long long)B.nblk * P.M / kBlkWarps + 1, (long long)B.n_top * P.M);
+    if (B.nblk + B.n_top > 0)
         bwd_solve_kernel<<<grid_for(g.top_bwd, work, 1), kTopThreads, g.top_bytes, st>>>(P, W, S, B, D, fs);
 }
 

@@ -413,8 +413,7 @@ int32_t gp_residual_static(gp_layout *L, const double *zold, double dt, double *
  * supernodes in one block, out[8] max |S^T y - rhs| / max |y| for S^T
  * factored from the transposed assembly lists of the adjoint, out[9]
  * largest front of the top region (0 when every supernode is in a block),
- * out[10] most vector entries one block stages, out[11] pivot rows of the
- * top region's upper part (the levels one CTA per scenario solves).
+ * out[10] most vector entries one block stages, out[11] zero.
  * No counterpart in the reference: a test hook for the analysis that
  * replaces cuDSS's. */
 int32_t gp_reduced_selftest(const gp_problem *prob, const int32_t *s_rowptr, const int32_t *s_colidx,

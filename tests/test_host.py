@@ -88,10 +88,6 @@ def test_reduced_factorisation_matches_scipy(lib, name):
     assert out[8] <= 1e-10
     xr = spla.spsolve(S.tocsc(), rhs)
     assert np.max(np.abs(x - xr)) <= 1e-12 * np.max(np.abs(xr))
-    if name in ("planar2k", "planar70k"):
-        # the narrow levels near the root go to the upper kernel
-        assert out[11] > 0
-    print(name, "upper rows", out[11], "top levels", out[6])
 
 
 def test_reduced_factorisation_with_static_generators(lib, golden_cases, orc):
