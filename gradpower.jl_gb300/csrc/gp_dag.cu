@@ -150,11 +150,119 @@ constexpr int kPanel = 8;
 // The front is left in the layout of the other paths: multipliers below the
 // diagonal, U above it, the pivots' reciprocals on it, piv[k] the row
 // swapped with row k at step k.
+// Rows a lane holds in the register panel (rows of the panel beyond
+// 32 * kPanelRows take the shared-memory path).
+constexpr int kPanelRows = 5;
+
+// Value of register slot j (a runtime index) of a per-lane array.
+template <int J>
+__device__ __forceinline__ float slot(const float (&r)[J], int j) {
+    float v = r[0];
+#pragma unroll
+    for (int q = 1; q < J; q++)
+        if (j == q) v = r[q];
+    return v;
+}
+
+// Panel [kb, ke) of an FP32 front factored by one warp in registers: lane l
+// holds rows kb + l + 32 j (j < J) of the panel's columns.  Per column: the
+// pivot among the pivot rows by a max and a min reduction, the pivot row and
+// row k exchanged through shuffles, the multipliers, the rank-1 update of
+// the panel's later columns; no barrier.  Same operations, in the same
+// order, as the shared-memory path.
+template <int J>
+__device__ void panel_warp32(float *F, int mm, int ns, int kb, int ke, int *piv, int *status) {
+    const int lane = threadIdx.x & 31, nb = ke - kb;
+    float P[J][kPanel];
+#pragma unroll
+    for (int j = 0; j < J; j++) {
+        const int i = kb + lane + 32 * j;
+#pragma unroll
+        for (int c = 0; c < kPanel; c++) P[j][c] = (i < mm && c < nb) ? F[i + (kb + c) * mm] : 0.0f;
+    }
+#pragma unroll
+    for (int c = 0; c < kPanel; c++) {
+        if (c >= nb) break;
+        const int k = kb + c;
+        // pivot among rows k..ns-1
+        unsigned key = 0u;
+        int bi = k;
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            const int i = kb + lane + 32 * j;
+            const unsigned v = __float_as_uint(P[j][c]) & 0x7fffffffu;
+            if (i >= k && i < ns && v > key) { key = v; bi = i; }
+        }
+        const unsigned kmax = __reduce_max_sync(FULL, key);
+        const int pv = (int)__reduce_min_sync(FULL, key == kmax ? (unsigned)bi : 0xffffffffu);
+        if (lane == 0) {
+            piv[k] = pv;
+            if (kmax == 0u) atomicOr(status, 4);
+        }
+        // the pivot row (u) and row k (w), broadcast
+        const int lp = (pv - kb) & 31, jp = (pv - kb) >> 5, lk = (k - kb) & 31, jk = (k - kb) >> 5;
+        float u[kPanel], w[kPanel];
+#pragma unroll
+        for (int q = 0; q < kPanel; q++) {
+            float col[J];
+#pragma unroll
+            for (int j = 0; j < J; j++) col[j] = P[j][q];
+            u[q] = __shfl_sync(FULL, slot(col, jp), lp);
+            w[q] = __shfl_sync(FULL, slot(col, jk), lk);
+        }
+        const float inv = 1.0f / u[c];
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            const int i = kb + lane + 32 * j;
+            if (i == pv && pv != k) {
+#pragma unroll
+                for (int q = 0; q < kPanel; q++) P[j][q] = w[q];
+            }
+            if (i == k) {
+#pragma unroll
+                for (int q = 0; q < kPanel; q++) P[j][q] = u[q];
+                P[j][c] = inv;
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            const int i = kb + lane + 32 * j;
+            if (i > k && i < mm) {
+                const float l = P[j][c] * inv;
+                P[j][c] = l;
+#pragma unroll
+                for (int q = 0; q < kPanel; q++)
+                    if (q > c) P[j][q] -= l * u[q];
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < J; j++) {
+        const int i = kb + lane + 32 * j;
+#pragma unroll
+        for (int c = 0; c < kPanel; c++)
+            if (i < mm && c < nb) F[i + (kb + c) * mm] = P[j][c];
+    }
+    __syncwarp();
+}
+
 __device__ void eliminate_cta32(float *F, int mm, int ns, int nc, int *piv, int *status) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
     for (int kb = 0; kb < ns; kb += kPanel) {
         const int ke = min(ns, kb + kPanel), nb = ke - kb;
         // ---- (a) the panel ----
+        if (mm - kb <= 32 * kPanelRows) {
+            if (warp == 0) {
+                switch ((mm - kb + 31) >> 5) {
+                case 1: panel_warp32<1>(F, mm, ns, kb, ke, piv, status); break;
+                case 2: panel_warp32<2>(F, mm, ns, kb, ke, piv, status); break;
+                case 3: panel_warp32<3>(F, mm, ns, kb, ke, piv, status); break;
+                case 4: panel_warp32<4>(F, mm, ns, kb, ke, piv, status); break;
+                default: panel_warp32<5>(F, mm, ns, kb, ke, piv, status); break;
+                }
+            }
+            __syncthreads();
+        } else
         for (int k = kb; k < ke; k++) {
             if (warp == 0) {
                 unsigned key = 0u;
