@@ -1209,6 +1209,10 @@ void build_work(gp_layout *L, const double *z0, const double *u0, const double *
     D.fdone = A.alloc<int>(M * D.nsup);
     D.xdone = A.alloc<int>(M * D.nsup);
     D.bdone = A.alloc<int>(M * D.nsup);
+    D.utag = A.alloc<unsigned long long>(M * std::max<int64_t>(1, S.uvec_total));
+    D.xtag = A.alloc<unsigned long long>(M * std::max(1, P.n_red));
+    fill(L, D.utag, 0, M * std::max<int64_t>(1, S.uvec_total) * sizeof(unsigned long long));
+    fill(L, D.xtag, 0, M * std::max(1, P.n_red) * sizeof(unsigned long long));
     fill(L, D.ctr, 0, 8 * sizeof(int));
     fill(L, D.epoch, 0, sizeof(int));
     fill(L, D.err, 0, sizeof(int));

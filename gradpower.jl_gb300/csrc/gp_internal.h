@@ -170,6 +170,12 @@ struct DevDag {
     int *epoch;             // [1] current solve
     int *err;               // [1] a wait gave up (sticky until the host clears it)
     int *fdone, *xdone, *bdone;   // [nsup][M] epoch at which the task finished
+    // Solves on FP32 factors hand values between tasks as tagged words
+    // (value, epoch) instead of done flags: utag mirrors uvec (the forward
+    // solve's update vectors), xtag mirrors xperm (the backward solve's
+    // entries of the top region).  Zero-filled at creation; epochs start at 1.
+    unsigned long long *utag;     // [M][uvec_total]
+    unsigned long long *xtag;     // [M][n_red]
     int wait_limit = 1 << 20;     // polls before a wait gives up (gp_set_wait_limit)
 };
 

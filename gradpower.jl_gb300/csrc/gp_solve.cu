@@ -6,16 +6,27 @@
 //  - blocks: subtrees whose fronts are small.  One warp per (block,
 //    scenario) keeps the block's right-hand-side vector, index maps and
 //    pivot permutations in shared memory and runs the whole block: children
-//    before parents forward, parents before children backward.  Blocks are
-//    independent: no flags, no waits.  One launch per direction.
-//  - top: the supernodes above the blocks.  A persistent dataflow kernel
-//    whose CTAs claim (supernode, scenario) tasks in a topological order
-//    (children first forward, parents first backward).  A task copies the
-//    part of the front it needs into shared memory (cp.async, all threads)
-//    and loads its own right-hand-side entries before it waits, bounded, on
-//    the done flags of the tasks it depends on; one warp then sweeps the
-//    front from shared memory.  One launch per direction.
-// Forward: blocks, then top.  Backward: top, then blocks.
+//    before parents forward, parents before children backward.  Inside a
+//    block nothing waits; a block hands its root's update vector to the top
+//    region (forward) and takes the entries of its external rows from it
+//    (backward).
+//  - top: the supernodes above the blocks, tasks (supernode, scenario)
+//    claimed in a topological order (children first forward, parents first
+//    backward).  A task copies the part of the front it needs into shared
+//    memory (cp.async, all threads) and loads its own right-hand-side
+//    entries before it waits, bounded, on the tasks it depends on; one warp
+//    then sweeps the front from shared memory.
+// One persistent kernel per direction runs both: forward, the warps claim
+// the block tasks first and the CTAs then the top tasks; backward, the top
+// tasks first and then the block tasks.
+//
+// Hand-offs between tasks.  On FP64 factors a task signals a done flag
+// (release store after a barrier) and its dependants poll the flag, then
+// read the values.  On FP32 factors the values themselves carry the epoch
+// (tagged 64-bit words, gp_warp.cuh): a block root or top task stores its
+// update vector (forward) or its solved pivot entries (backward) as tagged
+// words, and the tasks that consume them poll those words directly, so that
+// a hand-off costs one store and the polls that see it, with no fence.
 //
 // Within a front, one warp holds up to kMaxJ rows per lane in registers
 // (row i in lane i % 32, register i / 32).  The unit-lower and upper
@@ -35,6 +46,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "gp_internal.h"
 #include "gp_warp.cuh"
@@ -65,6 +77,40 @@ __device__ __forceinline__ void cp_async(void *dst, const void *src, int bytes) 
 }
 
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Solves on FP32 factors pass values between tasks as tagged words
+// (gp_warp.cuh); solves on FP64 factors keep the done flags.
+template <class T>
+struct Tagged {
+    static constexpr bool value = std::is_same<T, float>::value;
+};
+
+// Thread tid of nthr polls the tagged words src[idx(e)], e = tid, tid +
+// nthr, ... < n, until each carries epoch, and hands each value to put(e,
+// v); four loads in flight per thread before the first poll.  False when a
+// wait gave up.
+template <class Idx, class Put>
+__device__ bool poll_tagged(const unsigned long long *src, int n, int tid, int nthr, int epoch, const DevDag &D,
+                            Idx idx, Put put) {
+    bool ok = true;
+    for (int e0 = tid; e0 < n; e0 += 4 * nthr) {
+        unsigned long long w[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int e = e0 + q * nthr;
+            w[q] = e < n ? ld_relaxed_u64(src + idx(e)) : 0ull;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int e = e0 + q * nthr;
+            if (e < n) {
+                if (!tag_ok(w[q], epoch)) w[q] = wait_tag(src + idx(e), epoch, D.err, D.wait_limit, ok);
+                put(e, tag_val(w[q]));
+            }
+        }
+    }
+    return ok;
+}
 
 __device__ __forceinline__ bool use64(const FrontSel &fs, int m) {
     return fs.f32 == nullptr || (fs.mode != nullptr && fs.mode[m] == MX_EXACT);
@@ -415,8 +461,8 @@ __device__ void stage_piv_pair(const DevSym &S, const BlkTask &t, int m0, int m1
 // scenario, pivots in t.pv; LW = 16: each half-warp on its own scenario
 // (same block, so the same control flow), pivots in pvb.
 template <class T, int LW = 32>
-__device__ void fwd_block(const DevProblem &P, const DevWork &W, const DevSym &S, const FrontSel &fs,
-                          const BlkTask &t, int m, T *vs, const unsigned char *pvb = nullptr) {
+__device__ void fwd_block(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, int epoch,
+                          const FrontSel &fs, const BlkTask &t, int m, T *vs, const unsigned char *pvb = nullptr) {
     const int lane = threadIdx.x & (LW - 1), seg = (threadIdx.x >> 4) & 1;
     const double *x = W.xperm + (size_t)m * P.n_red;
     for (int q = 0; q < t.n; q++) {
@@ -442,6 +488,9 @@ __device__ void fwd_block(const DevProblem &P, const DevWork &W, const DevSym &S
         if (q < t.n - 1) {
             const int *pm = t.mp + b.z;
             for (int i = lane; i < r; i += LW) vs[pm[i]] += v[ns + i];
+        } else if constexpr (Tagged<T>::value) {
+            unsigned long long *ut = D.utag + (size_t)m * S.uvec_total + S.uvec_off[a.x];
+            for (int i = lane; i < r; i += LW) st_relaxed_u64(ut + i, tag_f32(v[ns + i], epoch));
         } else {
             double *us = uv + S.uvec_off[a.x];
             for (int i = lane; i < r; i += LW) us[i] = (double)v[ns + i];
@@ -450,9 +499,12 @@ __device__ void fwd_block(const DevProblem &P, const DevWork &W, const DevSym &S
     }
 }
 
+// FP32 factors: the entries of rows outside the block (pivots of top
+// supernodes) are polled as tagged words; FP64: the caller has waited on the
+// parent's done flag.
 template <class T, int LW = 32>
-__device__ void bwd_block(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B,
-                          const FrontSel &fs, const BlkTask &t, int blk, int m, T *vs) {
+__device__ void bwd_block(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B, const DevDag &D,
+                          int epoch, const FrontSel &fs, const BlkTask &t, int blk, int m, T *vs) {
     const int lane = threadIdx.x & (LW - 1);
     double *x = W.xperm + (size_t)m * P.n_red;
     for (int q = 0; q < t.n; q++) {
@@ -460,7 +512,15 @@ __device__ void bwd_block(const DevProblem &P, const DevWork &W, const DevSym &S
         for (int i = lane; i < a.z; i += LW) vs[b.y + i] = (T)x[a.y + i];
     }
     const int xb = B.ext_ptr[blk], next = B.ext_ptr[blk + 1] - xb;
-    for (int k = lane; k < next; k += LW) vs[B.ext_pos[xb + k]] = (T)x[B.ext_row[xb + k]];
+    if constexpr (Tagged<T>::value) {
+        const unsigned long long *xt = D.xtag + (size_t)m * P.n_red;
+        const bool ok = poll_tagged(
+            xt, next, lane, LW, epoch, D, [&](int k) { return B.ext_row[xb + k]; },
+            [&](int k, float v) { vs[B.ext_pos[xb + k]] = v; });
+        if (!ok) atomicOr(W.status + m, 8);
+    } else {
+        for (int k = lane; k < next; k += LW) vs[B.ext_pos[xb + k]] = (T)x[B.ext_row[xb + k]];
+    }
     __syncwarp();
     const T *fr = front_base<T>(fs) + (size_t)(fs.shared ? 0 : m) * S.front_total;
     for (int q = t.n - 1; q >= 0; q--) {
@@ -556,11 +616,21 @@ __device__ void fwd_top_task(const DevProblem &P, const DevWork &W, const DevSym
     int k1 = min(t.ns, cap);
     stage_cols<T>(Fs, F, t.mm, t.mm, 0, k1);
     __syncthreads();
-    {
-        const int e0 = sxr[0], ne = sxr[t.mm] - e0;
-        for (int e = threadIdx.x; e < ne; e += blockDim.x) sxe[e] = B.top_xent[e0 + e];
+    const int ne = sxr[t.mm] - sxr[0];
+    for (int e = threadIdx.x; e < ne; e += blockDim.x) sxe[e] = B.top_xent[sxr[0] + e];
+    if constexpr (Tagged<T>::value) {
+        // the children's entries, polled as tagged words by the thread that
+        // staged their offsets, replace the offsets in sxe
+        const unsigned long long *ut = D.utag + (size_t)t.m * S.uvec_total;
+        const bool ok = poll_tagged(
+            ut, ne, threadIdx.x, blockDim.x, epoch, D, [&](int e) { return sxe[e]; },
+            [&](int e, float val) { sxe[e] = __float_as_int(val); });
+        if (!ok) atomicOr(W.status + t.m, 8);
+        __syncthreads();
+    } else {
+        if (!wait_top_children(S, B, D, t.s, t.m, P.M, epoch, s_ok) && threadIdx.x == 0)
+            atomicOr(W.status + t.m, 8);
     }
-    if (!wait_top_children(S, B, D, t.s, t.m, P.M, epoch, s_ok) && threadIdx.x == 0) atomicOr(W.status + t.m, 8);
     // extend-add: one thread per front row sums the children's entries in
     // child order (the update vectors of the children were written by other
     // CTAs: read through L2)
@@ -568,7 +638,10 @@ __device__ void fwd_top_task(const DevProblem &P, const DevWork &W, const DevSym
         const int e0 = sxr[0];
         for (int i = threadIdx.x; i < t.mm; i += blockDim.x) {
             T acc = v[i];
-            for (int e = sxr[i] - e0; e < sxr[i + 1] - e0; e++) acc += (T)__ldcg(uv + sxe[e]);
+            for (int e = sxr[i] - e0; e < sxr[i + 1] - e0; e++) {
+                if constexpr (Tagged<T>::value) acc += __int_as_float(sxe[e]);
+                else acc += (T)__ldcg(uv + sxe[e]);
+            }
             v[i] = acc;
         }
     }
@@ -587,8 +660,13 @@ __device__ void fwd_top_task(const DevProblem &P, const DevWork &W, const DevSym
         stage_cols<T>(Fs, F, t.mm, t.mm, k0, k1);
     }
     for (int i = threadIdx.x; i < t.ns; i += blockDim.x) x[t.start + i] = (double)v[i];
-    double *us = uv + S.uvec_off[t.s];
-    for (int i = threadIdx.x; i < t.r; i += blockDim.x) us[i] = (double)v[t.ns + i];
+    if constexpr (Tagged<T>::value) {
+        unsigned long long *ut = D.utag + (size_t)t.m * S.uvec_total + S.uvec_off[t.s];
+        for (int i = threadIdx.x; i < t.r; i += blockDim.x) st_relaxed_u64(ut + i, tag_f32(v[t.ns + i], epoch));
+    } else {
+        double *us = uv + S.uvec_off[t.s];
+        for (int i = threadIdx.x; i < t.r; i += blockDim.x) us[i] = (double)v[t.ns + i];
+    }
 }
 
 template <class T>
@@ -609,8 +687,18 @@ __device__ void bwd_top_task(const DevProblem &P, const DevWork &W, const DevSym
     // then U11 from the last pivot column
     int c1 = t.mm, c0 = max(0, t.mm - cap);
     stage_cols<T>(Fs, F, t.mm, t.ns, c0, c1);
-    if (!wait_top_parent(D, t.s, t.m, P.M, epoch, s_ok) && threadIdx.x == 0) atomicOr(W.status + t.m, 8);
-    for (int a = threadIdx.x; a < t.r; a += blockDim.x) v[t.ns + a] = (T)__ldcg(x + pi[a]);
+    if constexpr (Tagged<T>::value) {
+        // the entries of the front's rows (pivots of ancestors), polled as
+        // tagged words by the thread that staged their row indices
+        const unsigned long long *xt = D.xtag + (size_t)t.m * P.n_red;
+        const bool ok = poll_tagged(
+            xt, t.r, threadIdx.x, blockDim.x, epoch, D, [&](int a) { return pi[a]; },
+            [&](int a, float val) { v[t.ns + a] = val; });
+        if (!ok) atomicOr(W.status + t.m, 8);
+    } else {
+        if (!wait_top_parent(D, t.s, t.m, P.M, epoch, s_ok) && threadIdx.x == 0) atomicOr(W.status + t.m, 8);
+        for (int a = threadIdx.x; a < t.r; a += blockDim.x) v[t.ns + a] = (T)__ldcg(x + pi[a]);
+    }
     for (;;) {
         cp_async_wait_all();
         __syncthreads();
@@ -626,6 +714,10 @@ __device__ void bwd_top_task(const DevProblem &P, const DevWork &W, const DevSym
         stage_cols<T>(Fs, F, t.mm, t.ns, c0, c1);
     }
     for (int i = threadIdx.x; i < t.ns; i += blockDim.x) x[t.start + i] = (double)v[i];
+    if constexpr (Tagged<T>::value) {
+        unsigned long long *xt = D.xtag + (size_t)t.m * P.n_red + t.start;
+        for (int i = threadIdx.x; i < t.ns; i += blockDim.x) st_relaxed_u64(xt + i, tag_f32(v[i], epoch));
+    }
 }
 
 // ---- the solves: one persistent kernel per direction ------------------------
@@ -683,10 +775,9 @@ __global__ void __launch_bounds__(kTopThreads, 8) fwd_solve_kernel(DevProblem P,
                     stage_piv_pair(S, bt, m0, m1, pvb);
                     prefetch_block<float, 16>(S, fs, bt, m, true);
                     __syncwarp();
-                    fwd_block<float, 16>(P, W, S, fs, bt, m, reinterpret_cast<float *>(base + lay.v) + seg * B.max_v,
-                                         pvb);
+                    fwd_block<float, 16>(P, W, S, D, epoch, fs, bt, m,
+                                         reinterpret_cast<float *>(base + lay.v) + seg * B.max_v, pvb);
                     __syncwarp();
-                    if ((threadIdx.x & 15) == 0) signal_done(D.xdone + (size_t)root * M + m, epoch);
                     continue;
                 }
             }
@@ -699,10 +790,10 @@ __global__ void __launch_bounds__(kTopThreads, 8) fwd_solve_kernel(DevProblem P,
                 __syncwarp();
                 if (d) prefetch_block<double>(S, fs, bt, m, true);
                 else prefetch_block<float>(S, fs, bt, m, true);
-                if (d) fwd_block<double>(P, W, S, fs, bt, m, reinterpret_cast<double *>(base + lay.v));
-                else fwd_block<float>(P, W, S, fs, bt, m, reinterpret_cast<float *>(base + lay.v));
+                if (d) fwd_block<double>(P, W, S, D, epoch, fs, bt, m, reinterpret_cast<double *>(base + lay.v));
+                else fwd_block<float>(P, W, S, D, epoch, fs, bt, m, reinterpret_cast<float *>(base + lay.v));
                 __syncwarp();
-                if (lane == 0) signal_done(D.xdone + (size_t)root * M + m, epoch);
+                if (d && lane == 0) signal_done(D.xdone + (size_t)root * M + m, epoch);
                 __syncwarp();
             }
         }
@@ -719,10 +810,13 @@ __global__ void __launch_bounds__(kTopThreads, 8) fwd_solve_kernel(DevProblem P,
         const bool d = use64(fs, m);
         if (d && fs.fused64) continue;
         const TopCtx c = top_ctx(S, s, m, t / M);
-        if (d) fwd_top_task<double>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
-        else fwd_top_task<float>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
-        __syncthreads();
-        if (threadIdx.x == 0) signal_done(D.xdone + (size_t)s * M + m, epoch);
+        if (d) {
+            fwd_top_task<double>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
+            __syncthreads();
+            if (threadIdx.x == 0) signal_done(D.xdone + (size_t)s * M + m, epoch);
+        } else {
+            fwd_top_task<float>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
+        }
     }
 }
 
@@ -743,10 +837,13 @@ __global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P,
         const int s = B.top_order[B.n_top - 1 - t / M], m = t % M;
         if (!W.active[m]) continue;
         const TopCtx c = top_ctx(S, s, m, B.n_top - 1 - t / M);
-        if (use64(fs, m)) bwd_top_task<double>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
-        else bwd_top_task<float>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
-        __syncthreads();
-        if (threadIdx.x == 0) signal_done(D.bdone + (size_t)s * M + m, epoch);
+        if (use64(fs, m)) {
+            bwd_top_task<double>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
+            __syncthreads();
+            if (threadIdx.x == 0) signal_done(D.bdone + (size_t)s * M + m, epoch);
+        } else {
+            bwd_top_task<float>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
+        }
     }
     const int MP = pair_mode(fs) ? (M + 1) / 2 : M;
     const long long n_blk = (long long)B.nblk * MP;
@@ -766,14 +863,8 @@ __global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P,
                 const BlkTask bt = stage_block(S, B, blk, 0, base, lay, B.map_bwd, false);
                 __syncwarp();
                 prefetch_block<float, 16>(S, fs, bt, m, false);
-                if (par >= 0) {
-                    bool ok = true;
-                    if ((threadIdx.x & 15) == 0) ok = wait_epoch(D.bdone + (size_t)par * M + m, epoch, D.err, D.wait_limit);
-                    ok = __shfl_sync(FULL, ok, threadIdx.x & 16);
-                    if (!ok && (threadIdx.x & 15) == 0) atomicOr(W.status + m, 8);
-                }
                 __syncwarp();
-                bwd_block<float, 16>(P, W, S, B, fs, bt, blk, m,
+                bwd_block<float, 16>(P, W, S, B, D, epoch, fs, bt, blk, m,
                                      reinterpret_cast<float *>(base + lay.v) + seg * B.max_v);
                 __syncwarp();
                 continue;
@@ -784,17 +875,18 @@ __global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P,
             if (m >= M || !W.active[m]) continue;
             const BlkTask bt = stage_block(S, B, blk, fs.shared ? 0 : m, base, lay, B.map_bwd, false);
             __syncwarp();
-            if (use64(fs, m)) prefetch_block<double>(S, fs, bt, m, false);
+            const bool d = use64(fs, m);
+            if (d) prefetch_block<double>(S, fs, bt, m, false);
             else prefetch_block<float>(S, fs, bt, m, false);
-            if (par >= 0) {
+            if (d && par >= 0) {
                 bool ok = true;
                 if (lane == 0) ok = wait_epoch(D.bdone + (size_t)par * M + m, epoch, D.err, D.wait_limit);
                 ok = __shfl_sync(FULL, ok, 0);
                 if (!ok && lane == 0) atomicOr(W.status + m, 8);
             }
             __syncwarp();
-            if (use64(fs, m)) bwd_block<double>(P, W, S, B, fs, bt, blk, m, reinterpret_cast<double *>(base + lay.v));
-            else bwd_block<float>(P, W, S, B, fs, bt, blk, m, reinterpret_cast<float *>(base + lay.v));
+            if (d) bwd_block<double>(P, W, S, B, D, epoch, fs, bt, blk, m, reinterpret_cast<double *>(base + lay.v));
+            else bwd_block<float>(P, W, S, B, D, epoch, fs, bt, blk, m, reinterpret_cast<float *>(base + lay.v));
             __syncwarp();
         }
     }

@@ -45,6 +45,47 @@ __device__ inline bool wait_epoch(const int *flag, int epoch, int *err, int limi
 // writes before it; the release store makes them visible with the flag.
 __device__ __forceinline__ void signal_done(int *flag, int epoch) { st_release(flag, epoch); }
 
+// ---- tagged words: a value that carries its own epoch ------------------
+// An FP32 value and the epoch of the solve that wrote it in one 64-bit word
+// (value in the low half, epoch in the high half), stored and loaded as one
+// single-copy-atomic access.  A reader polls the word itself: no flag, no
+// release fence on the writer's side, no second load after the flag.
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long tag_f32(float v, int epoch) {
+    return ((unsigned long long)(unsigned)epoch << 32) | __float_as_uint(v);
+}
+
+__device__ __forceinline__ bool tag_ok(unsigned long long w, int epoch) { return (int)(w >> 32) == epoch; }
+
+__device__ __forceinline__ float tag_val(unsigned long long w) { return __uint_as_float((unsigned)w); }
+
+// Polls *p until it carries epoch, bounded like wait_epoch; clears ok when
+// the wait gave up.
+__device__ inline unsigned long long wait_tag(const unsigned long long *p, int epoch, int *err, int limit, bool &ok) {
+    for (int it = 0; it < limit; ++it) {
+        const unsigned long long w = ld_relaxed_u64(p);
+        if (tag_ok(w, epoch)) return w;
+        if ((it & 31) == 31 && ld_relaxed(err)) {
+            ok = false;
+            return w;
+        }
+        __nanosleep(32);
+    }
+    atomicExch(err, 1);
+    ok = false;
+    return 0ull;
+}
+
 // Next power of two >= n, for 1 <= n <= 32.
 __device__ __forceinline__ int np2(int n) { return n <= 1 ? 1 : 1 << (32 - __clz(n - 1)); }
 
