@@ -506,7 +506,19 @@ struct HostBlk {
     int n_top_levels = 0, top_max_front = 1, top_max_xent = 1;
     std::vector<int> top_order, top_rank;
     std::vector<int> top_xptr, top_xrow, top_xent;   // extend-add lists of the top region
+    // solve-ordered factor copies: supernode s's L panel (mm x ns, leading
+    // dimension mm) and U rows (ns x mm, leading dimension ns) both start at
+    // lu_off[s]; the supernodes of a block follow one another in the block's
+    // order, every block and every top supernode starts on a multiple of
+    // kLuAlign entries
+    std::vector<int64_t> lu_off;
+    int64_t lu_total = 0;
+    int max_seg = 1;   // entries of the largest block (aligned)
 };
+
+constexpr int kLuAlign = 4;   // 16 bytes of FP32, 32 of FP64
+
+int64_t lu_align(int64_t x) { return (x + kLuAlign - 1) / kLuAlign * kLuAlign; }
 
 void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
     constexpr long kLimSlices = 2048, kLimRows = 512, kLimSups = 64;
@@ -628,6 +640,24 @@ void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
                 B.top_order.push_back(s);
             }
     B.n_top_levels = ntl;
+    // solve-ordered factor copies: the blocks in the order they are claimed,
+    // then the top supernodes
+    B.lu_off.assign(ns, -1);
+    int64_t lo = 0;
+    for (int b : emit) {
+        const int64_t b0 = lo;
+        for (int s : members[b]) {
+            B.lu_off[s] = lo;
+            lo += (int64_t)sym.front_m(s) * sym.front_n(s);
+        }
+        lo = lu_align(lo);
+        B.max_seg = (int)std::max<int64_t>(B.max_seg, lo - b0);
+    }
+    for (int s : B.top_order) {
+        B.lu_off[s] = lo;
+        lo = lu_align(lo + (int64_t)sym.front_m(s) * sym.front_n(s));
+    }
+    B.lu_total = std::max<int64_t>(lo, kLuAlign);
     // extend-add lists: for every front row of a top supernode, the
     // children's update-vector entries that add into it, in child order
     B.top_xptr.assign(1, 0);
@@ -783,16 +813,54 @@ void host_fwd_front(const double *F, const int *perm, int ns, int mm, Staged &v,
     }
 }
 
-void host_bwd_front(const double *F, int ns, int mm, Staged &v, long o) {
+// U: the front's U rows (ns x mm, leading dimension ns).
+void host_bwd_front(const double *U, int ns, int mm, Staged &v, long o) {
     for (int i = 0; i < ns; i++) {
         double acc = 0.0;
-        for (int a = 0; a < mm - ns; a++) acc += F[i + (size_t)(ns + a) * mm] * v[o + ns + a];
+        for (int a = 0; a < mm - ns; a++) acc += U[i + (size_t)(ns + a) * ns] * v[o + ns + a];
         v[o + i] -= acc;
     }
     for (int k = ns - 1; k >= 0; k--) {
-        const double tk = v[o + k] * F[k + (size_t)k * mm];
+        const double tk = v[o + k] * U[k + (size_t)k * ns];
         v[o + k] = tk;
-        for (int i = 0; i < k; i++) v[o + i] -= F[i + (size_t)k * mm] * tk;
+        for (int i = 0; i < k; i++) v[o + i] -= U[i + (size_t)k * ns] * tk;
+    }
+}
+
+// The factorisation's solve-ordered copies (gp_dag.cu, store): L panel and
+// U rows of every supernode at B.lu_off, each range checked against the
+// arrays, each block's supernodes consecutive and aligned as the solve
+// kernels' prefetch of a block's range assumes.
+void host_solve_copies(const gp::Symbolic &S, const HostBlk &B, const std::vector<double> &fronts,
+                       std::vector<double> &lf, std::vector<double> &uf) {
+    lf.assign(B.lu_total, 0.0);
+    uf.assign(B.lu_total, 0.0);
+    std::vector<int> seen(B.lu_total, 0);
+    for (int s = 0; s < S.nsup; s++) {
+        const int64_t o = B.lu_off[s];
+        const int ns = S.front_n(s), mm = S.front_m(s);
+        if (o < 0 || o + (int64_t)mm * ns > B.lu_total || o % kLuAlign && B.top_rank[s] >= 0)
+            fail(GP_E_INTERNAL, "solve copies: supernode %d at %lld", s, (long long)o);
+        const double *F = fronts.data() + S.front_off[s];
+        for (int k = 0; k < ns; k++)
+            for (int i = 0; i < mm; i++) {
+                if (seen[o + i + (int64_t)k * mm]++) fail(GP_E_INTERNAL, "solve copies: overlap at supernode %d", s);
+                lf[o + i + (int64_t)k * mm] = F[i + (size_t)k * mm];
+            }
+        for (int c = 0; c < mm; c++)
+            for (int i = 0; i < ns; i++) uf[o + i + (int64_t)c * ns] = F[i + (size_t)c * mm];
+    }
+    for (int blk = 0; blk < B.nblk; blk++) {
+        const int e0 = B.blk_ptr[blk], n = B.blk_ptr[blk + 1] - e0;
+        int64_t at = B.lu_off[B.ent0[e0].x];
+        if (at % kLuAlign) fail(GP_E_INTERNAL, "solve copies: block %d not aligned", blk);
+        const int64_t b0 = at;
+        for (int q = 0; q < n; q++) {
+            const int4 a = B.ent0[e0 + q];
+            if (B.lu_off[a.x] != at) fail(GP_E_INTERNAL, "solve copies: block %d not contiguous", blk);
+            at += (int64_t)(a.z + a.w) * a.z;
+        }
+        if (lu_align(at) - b0 > B.max_seg) fail(GP_E_INTERNAL, "solve copies: block %d above max_seg", blk);
     }
 }
 
@@ -803,6 +871,8 @@ void host_bwd_front(const double *F, int ns, int mm, Staged &v, long o) {
 void host_block_solve(const gp::Symbolic &S, const HostBlk &B, const std::vector<double> &fronts,
                       const std::vector<int> &ipiv, std::vector<double> &x) {
     std::vector<double> uvec(std::max<int64_t>(1, S.uvec_off[S.nsup]), 0.0);
+    std::vector<double> lf, uf;
+    host_solve_copies(S, B, fronts, lf, uf);
     auto ent = [&](int e, int4 &a, int4 &b) {
         a = B.ent0[e];
         b = B.ent1[e];
@@ -829,7 +899,7 @@ void host_block_solve(const gp::Symbolic &S, const HostBlk &B, const std::vector
             const int s = a.x, ns = a.z, r = a.w;
             std::vector<int> perm(ns);
             for (int i = 0; i < ns; i++) perm[i] = (int)pv[b.w + i];
-            host_fwd_front(fronts.data() + S.front_off[s], perm.data(), ns, ns + r, vs, b.y);
+            host_fwd_front(lf.data() + B.lu_off[s], perm.data(), ns, ns + r, vs, b.y);
             for (int i = 0; i < ns; i++) x[a.y + i] = vs[b.y + i];
             if (q < n - 1)
                 for (int i = 0; i < r; i++) vs[(long)mp[b.z + i]] += vs[b.y + ns + i];
@@ -853,7 +923,7 @@ void host_block_solve(const gp::Symbolic &S, const HostBlk &B, const std::vector
             for (int e = xr[i]; e < xr[i + 1]; e++) acc += uvec[B.top_xent[e]];
             tv[i] = acc;
         }
-        host_fwd_front(fronts.data() + S.front_off[s], ipiv.data() + start, ns, mm, tv, 0);
+        host_fwd_front(lf.data() + B.lu_off[s], ipiv.data() + start, ns, mm, tv, 0);
         for (int i = 0; i < ns; i++) x[start + i] = tv[i];
         for (int a = 0; a < r; a++) uvec[S.uvec_off[s] + a] = tv[ns + a];
     }
@@ -863,7 +933,7 @@ void host_block_solve(const gp::Symbolic &S, const HostBlk &B, const std::vector
         Staged tv(B.top_max_front, "top vector");
         const int *rows = S.rows.data() + S.row_ptr[s];
         for (int i = 0; i < mm; i++) tv[i] = i < ns ? x[start + i] : x[rows[i - ns]];
-        host_bwd_front(fronts.data() + S.front_off[s], ns, mm, tv, 0);
+        host_bwd_front(uf.data() + B.lu_off[s], ns, mm, tv, 0);
         for (int i = 0; i < ns; i++) x[start + i] = tv[i];
     }
     for (int blk = 0; blk < B.nblk; blk++) {
@@ -888,7 +958,7 @@ void host_block_solve(const gp::Symbolic &S, const HostBlk &B, const std::vector
                 if (g >= b.y && g < b.y + ns + r) fail(GP_E_INTERNAL, "block solve: map into the front's own rows");
                 vs[b.y + ns + c] = vs[g];
             }
-            host_bwd_front(fronts.data() + S.front_off[a.x], ns, ns + r, vs, b.y);
+            host_bwd_front(uf.data() + B.lu_off[a.x], ns, ns + r, vs, b.y);
             for (int i = 0; i < ns; i++) x[a.y + i] = vs[b.y + i];
         }
     }
@@ -927,10 +997,58 @@ void build_dag(gp_layout *L, const gp::Symbolic &sym) {
     D.nsup = ns;
     D.n_small = n_small;
     D.max_front = sym.max_front;
-    D.max_big_front = max_big;
     D.order = A.upload(order);
     D.rank = A.upload(rank);
     D.parent = A.upload(sym.parent);
+    // split fronts (FP64): in the last kSplitTail ranks of the order (the
+    // narrow top of the tree), a front of at least kSplitMin rows is factored
+    // by about one part per 24 columns, at most kMaxParts
+    {
+        constexpr int kSplitTail = gp::kSplitTailMax, kSplitMin = 48, kColsPerPart = 24;
+        const size_t M = L->M;
+        D.tail0 = std::max(n_small, ns - kSplitTail);
+        D.n_tail = ns - D.tail0;
+        std::vector<uint8_t> nparts(ns, 1);
+        std::vector<int> tail_units(1, 0);
+        std::vector<int64_t> pb_off;
+        int64_t pbt = 0;
+        for (int r = D.tail0; r < ns; r++) {
+            const int s = order[r], mm = sym.front_m(s), n = sym.front_n(s);
+            const int np = mm >= kSplitMin ? std::min(gp::kMaxParts, std::max(2, (mm + kColsPerPart) / kColsPerPart))
+                                           : 1;
+            nparts[s] = (uint8_t)np;
+            tail_units.push_back(tail_units.back() + np);
+            pb_off.push_back(pbt);
+            if (np > 1) {
+                const int npan = (n + gp::kSplitPanel - 1) / gp::kSplitPanel;
+                pbt += (int64_t)npan * mm * gp::kSplitPanel;
+                D.max_panels = std::max(D.max_panels, npan);
+                D.max_split_ns = std::max(D.max_split_ns, n);
+                // local columns of a part: whole panels of the nc = mm + 1
+                // columns (the FP64 right-hand side included), dealt in turn
+                const int per = gp::kSplitPanel * np;
+                const int ncl = (mm + 1 + per - 1) / per * gp::kSplitPanel;
+                D.max_part_entries = std::max(D.max_part_entries, mm * (ncl + gp::kSplitPanel));
+                D.max_part_ints = std::max(D.max_part_ints, 2 * mm);
+            }
+        }
+        D.max_big_whole = 0;
+        for (int r = n_small; r < ns; r++)
+            if (nparts[order[r]] == 1) D.max_big_whole = std::max(D.max_big_whole, sym.front_m(order[r]));
+        D.big_units = (D.tail0 - n_small) + tail_units.back();
+        D.nparts = A.upload(nparts);
+        D.tail_units = A.upload(tail_units);
+        D.pb_off = A.upload(pb_off);
+        D.pb_total = std::max<int64_t>(pbt, 1);
+        const size_t nt = std::max(1, D.n_tail);
+        D.pdone = A.alloc<int>(nt * M * gp::kMaxParts);
+        D.pflag = A.alloc<int>(nt * M * D.max_panels);
+        D.ppiv = A.alloc<int>(nt * M * D.max_split_ns);
+        D.pbuf = A.alloc<double>(M * D.pb_total);
+        fill(L, D.pdone, 0, nt * M * gp::kMaxParts * sizeof(int));
+        fill(L, D.pflag, 0, nt * M * D.max_panels * sizeof(int));
+    }
+    D.max_big_front = max_big;
     // extend-add lists of the fronts the CTA kernel factors: per front entry
     // (and right-hand-side row) its children's contributions, in child order
     {
@@ -1008,6 +1126,10 @@ void build_blocks(gp_layout *L, const gp::Symbolic &sym) {
     B.top_xptr = A.upload(H.top_xptr);
     B.top_xrow = A.upload(H.top_xrow);
     B.top_xent = A.upload(H.top_xent);
+    L->S.lu_off = A.upload(H.lu_off);
+    L->S.lu_total = H.lu_total;
+    L->ST.lu_off = L->S.lu_off;
+    L->ST.lu_total = L->S.lu_total;
     L->n_top_levels = H.n_top_levels;
     const int sc = gp::solve_configure(B, L->SG);
     if (sc == -2) fail(GP_E_INVALID, "front of %d rows exceeds the solve kernels' staging area", B.top_max_front);
@@ -1186,10 +1308,16 @@ void build_work(gp_layout *L, const double *z0, const double *u0, const double *
     W.dt = A.alloc<double>(1);
     DevSym &S = L->S;
     S.fronts = A.alloc<double>(M * S.front_total);
+    S.lfac = A.alloc<double>(M * S.lu_total);
+    S.ufac = A.alloc<double>(M * S.lu_total);
+    fill(L, S.lfac, 0, M * S.lu_total * sizeof(double));
+    fill(L, S.ufac, 0, M * S.lu_total * sizeof(double));
     S.uvec = A.alloc<double>(M * std::max<int64_t>(1, S.uvec_total));
     S.ipiv = A.alloc<int>(M * S.n);
     // S^T (the adjoint) factors into the same buffers
     L->ST.fronts = S.fronts;
+    L->ST.lfac = S.lfac;
+    L->ST.ufac = S.ufac;
     L->ST.uvec = S.uvec;
     L->ST.ipiv = S.ipiv;
     {
@@ -1377,7 +1505,7 @@ int enqueue_solve(gp_layout *L, int variant, int *nfac_out) {
     if (variant == -2) {
         // shared-factor Woodbury: the factors of P (scenario 0's slot), the
         // fault's rank-2 correction, no factorisation
-        const gp::FrontSel fs{nullptr, L->S.fronts, nullptr, 0, 1};
+        const gp::FrontSel fs{nullptr, nullptr, L->S.lfac, L->S.ufac, nullptr, 0, 1};
         mark(L, 4);
         gp::launch_solve_fwd(L->P, L->W, L->S, B, D, L->SG, fs, L->st);
         mark(L, 5);
@@ -1385,17 +1513,19 @@ int enqueue_solve(gp_layout *L, int variant, int *nfac_out) {
         gp::launch_wb_correct(L->P, L->W, L->wb_W1, L->wb_W2, L->wb_Hinv, L->wb_s, L->st);
         launches += 2 * nsolve + 2;
     } else if (variant < 0) {
-        const gp::FrontSel fs{nullptr, L->S.fronts, nullptr, 1};
-        gp::launch_dag_factor<double>(L->P, L->W, L->S, D, L->G64, L->S.fronts, L->W.active, 1, L->st);
+        const gp::FrontSel fs{nullptr, nullptr, L->S.lfac, L->S.ufac, nullptr, 1};
+        gp::launch_dag_factor<double>(L->P, L->W, L->S, D, L->G64, L->S.fronts, nullptr, L->S.ufac, L->W.active, 1,
+                                      L->st);
         mark(L, 4);   // the FP64 factorisation includes the forward solve
         mark(L, 5);
         gp::launch_solve_bwd(L->P, L->W, L->S, B, D, L->SG, fs, L->st);
         facs = nfac;
         launches += nfac + nsolve;
     } else {
-        const gp::FrontSel fs{L->Mx.fronts, L->S.fronts, L->Mx.refac, 1};
+        const gp::FrontSel fs{L->Mx.lfac, L->Mx.ufac, L->S.lfac, L->S.ufac, L->Mx.refac, 1};
         if (variant & 1) {
-            gp::launch_dag_factor<float>(L->P, L->W, L->S, D, L->G32, L->Mx.fronts, L->Mx.refac, gp::MX_FP32, L->st);
+            gp::launch_dag_factor<float>(L->P, L->W, L->S, D, L->G32, L->Mx.fronts, L->Mx.lfac, L->Mx.ufac,
+                                         L->Mx.refac, gp::MX_FP32, L->st);
             facs += nfac;
         }
         if (variant & 2) {
@@ -1405,7 +1535,8 @@ int enqueue_solve(gp_layout *L, int variant, int *nfac_out) {
                 gp::launch_dag_begin(D, L->st);
                 launches += 1;
             }
-            gp::launch_dag_factor<double>(L->P, L->W, L->S, D, L->G64, L->S.fronts, L->Mx.refac, gp::MX_EXACT, L->st);
+            gp::launch_dag_factor<double>(L->P, L->W, L->S, D, L->G64, L->S.fronts, nullptr, L->S.ufac, L->Mx.refac,
+                                          gp::MX_EXACT, L->st);
             facs += nfac;
         }
         mark(L, 4);
@@ -1557,6 +1688,8 @@ void ensure_mixed(gp_layout *L) {
     X.lu = A.alloc<float>(M * std::max(1, L->C.n_tasks) * n_lu * 32);
     X.cc = A.alloc<float>(M * std::max(1, L->P.n_cl) * 6);
     X.fronts = A.alloc<float>(M * L->S.front_total);
+    X.lfac = A.alloc<float>(M * L->S.lu_total);
+    X.ufac = A.alloc<float>(M * L->S.lu_total);
     X.kc = A.alloc<double>(M * std::max(1, L->C.n_tasks) * gp::kConstSlots * 32);
     L->zprev = A.alloc<double>(M * L->n_sys);
     L->zprev2 = A.alloc<double>(M * L->n_sys);
@@ -1572,6 +1705,8 @@ void ensure_mixed(gp_layout *L) {
     fill(L, X.lu, 0, M * std::max(1, L->C.n_tasks) * n_lu * 32 * sizeof(float));
     fill(L, X.cc, 0, M * std::max(1, L->P.n_cl) * 6 * sizeof(float));
     fill(L, X.fronts, 0, M * L->S.front_total * sizeof(float));
+    fill(L, X.lfac, 0, M * L->S.lu_total * sizeof(float));
+    fill(L, X.ufac, 0, M * L->S.lu_total * sizeof(float));
     if (gp::dag_configure(L->D, 1, L->G32) != 0) fail(GP_E_CUDA, "could not configure the FP32 dataflow kernels");
     L->mixed_ready = true;
 }
@@ -1606,8 +1741,9 @@ void wb_prepare(gp_layout *L, double dt) {
     gp::launch_cluster(L->P, L->W, L->C, L->Mx, 0, L->st);
     gp::launch_network(L->P, L->W, L->Mx, 0, L->st);
     gp::launch_dag_begin(L->D, L->st);
-    gp::launch_dag_factor<double>(L->P, L->W, L->S, L->D, L->G64, L->S.fronts, L->d_only0, 1, L->st);
-    const gp::FrontSel fs{nullptr, L->S.fronts, nullptr, 0, 1};
+    gp::launch_dag_factor<double>(L->P, L->W, L->S, L->D, L->G64, L->S.fronts, L->S.lfac, L->S.ufac, L->d_only0, 1,
+                                  L->st);
+    const gp::FrontSel fs{nullptr, nullptr, L->S.lfac, L->S.ufac, nullptr, 0, 1};
     double *cols[2] = {L->wb_W1, L->wb_W2};
     for (int c = 0; c < 2; c++) {
         gp::launch_wb_unit(L->P, L->W, c, L->st);
@@ -1755,8 +1891,10 @@ void adj_solve(gp_layout *L, const gp::DevAdj &A, const gp::DevClu &Csave, doubl
     launch_network(L->P, L->W, exact, 0, L->st);
     launch_adj_rhs(L->P, L->W, Csave, A, L->st);
     launch_dag_begin(L->D, L->st);
-    launch_dag_factor<double>(L->P, L->W, L->ST, L->D, L->G64, L->ST.fronts, L->W.active, 1, L->st);
-    launch_solve_bwd(L->P, L->W, L->ST, L->B, L->D, L->SG, FrontSel{nullptr, L->ST.fronts, nullptr, 1}, L->st);
+    launch_dag_factor<double>(L->P, L->W, L->ST, L->D, L->G64, L->ST.fronts, nullptr, L->ST.ufac, L->W.active, 1,
+                              L->st);
+    launch_solve_bwd(L->P, L->W, L->ST, L->B, L->D, L->SG, FrontSel{nullptr, nullptr, L->ST.lfac, L->ST.ufac, nullptr, 1},
+                     L->st);
     launch_adj_back(L->P, L->W, Csave, A, L->d_state_maps, L->st);
     ck(cudaGetLastError(), "adjoint launch");
 }

@@ -20,9 +20,11 @@
 // Partial pivoting is restricted to a supernode's pivot rows.  The FP32
 // elimination is blocked (the pivot panel column by column, then one
 // triangular solve and one update of the rest of the front); the FP64 one
-// is right-looking.  The front
-// (column-major, leading dimension = front rows) keeps L, U and the update
-// matrix that the parent's extend-add reads.
+// is right-looking.  The front is column-major (leading dimension = front
+// rows) in shared memory; of it, the factorisation stores the update matrix
+// that the parent's extend-add reads (in `fronts`, at the front's offset)
+// and, for the triangular solves, the L panel and the U rows in the
+// solve-ordered arrays lfac and ufac (DevSym::lu_off).
 //
 // The factor type T is double (exact Newton) or float (factors kept and
 // reused across Newton iterations).  The FP64 factorisation also does the
@@ -59,15 +61,24 @@ __device__ __forceinline__ T ldcg(const T *p) {
 }
 
 // One warp waits for the children of supernode s (scenario m) whose
-// schedule rank is at least `from_rank`.
+// schedule rank is at least `from_rank`; with `split`, on each part of a
+// split child.
 __device__ bool warp_wait_children(const DevSym &S, const DevDag &D, const int *done, int s, int m, int M,
-                                   int epoch, int from_rank) {
+                                   int epoch, int from_rank, bool split = false) {
     const int lane = threadIdx.x & 31;
     const int c0 = S.child_ptr[s], nc = S.child_ptr[s + 1] - c0;
     bool ok = true;
     for (int q = lane; q < nc; q += 32) {
         const int c = S.children[c0 + q];
-        if (D.rank[c] >= from_rank) ok = wait_epoch(done + (size_t)c * M + m, epoch, D.err, D.wait_limit) && ok;
+        const int rc = D.rank[c];
+        if (rc < from_rank) continue;
+        const int np = split ? D.nparts[c] : 1;
+        if (np == 1) {
+            ok = wait_epoch(done + (size_t)c * M + m, epoch, D.err, D.wait_limit) && ok;
+        } else {
+            const int *pd = D.pdone + ((size_t)(rc - D.tail0) * M + m) * kMaxParts;
+            for (int p = 0; p < np; p++) ok = wait_epoch(pd + p, epoch, D.err, D.wait_limit) && ok;
+        }
     }
     ok = __all_sync(FULL, ok);
     __syncwarp();
@@ -130,97 +141,124 @@ struct BlockGroup {
     __device__ void sync() const { __syncthreads(); }
 };
 
-// Columns per panel of the blocked FP32 elimination of CTA-sized fronts.
-constexpr int kPanel = 8;
+// Columns per panel of the blocked elimination of CTA-sized fronts.
+template <class T>
+struct PanelOf {
+    static constexpr int cols = 8;
+};
 
-// Elimination of an FP32 front by the whole CTA (fronts above the warp
-// size), blocked right-looking in panels of kPanel pivot columns:
+// Elimination of a front by the whole CTA (fronts above the warp size),
+// blocked right-looking in panels of PanelOf<T>::cols pivot columns:
 //  (a) the panel, column by column: warp 0 finds the pivot among the pivot
-//      rows (one max and one min reduction), swaps the two rows within the
-//      panel, stores the multipliers and the pivot's reciprocal; the CTA then
-//      updates the panel's later columns (a rank-1 update kPanel columns
-//      wide, not the whole front);
+//      rows, swaps the two rows within the panel, stores the multipliers
+//      and the pivot's reciprocal, and updates the panel's later columns;
+//      in registers (lane l holds rows kb + l + 32 j) when the panel has at
+//      most 32 * kPanelRows rows, else in shared memory with the CTA
+//      updating the panel's later columns;
 //  (b) the panel's row interchanges applied to every other column;
 //  (c) U of the panel rows right of it, by a forward substitution per
 //      column with the panel's unit lower block (values in registers);
-//  (d) the trailing update A -= L U (rank kPanel): a warp takes four
+//  (d) the trailing update A -= L U (rank = panel width): a warp takes four
 //      columns and its lanes the rows, each lane the same four columns of
 //      up to five rows, sums in registers; the U entries are broadcasts and
 //      the L and A entries consecutive across lanes (no bank conflicts).
-// The front is left in the layout of the other paths: multipliers below the
-// diagonal, U above it, the pivots' reciprocals on it, piv[k] the row
-// swapped with row k at step k.
-// Rows a lane holds in the register panel (rows of the panel beyond
-// 32 * kPanelRows take the shared-memory path).
+// Every entry receives the same operations in the same order as in the
+// column-by-column right-looking elimination (each update one FMA, the
+// updates of an entry in pivot order), so the factors are the same.  The
+// columns beyond the front (nc > mm: the right-hand side of the FP64
+// factorisation) are carried through (b)-(d) like any other column.  The
+// front is left with the multipliers below the diagonal, U above it, the
+// pivots' reciprocals on it, piv[k] the row swapped with row k at step k.
+// Rows a lane holds in the register panel.
 constexpr int kPanelRows = 5;
 
 // Value of register slot j (a runtime index) of a per-lane array.
-template <int J>
-__device__ __forceinline__ float slot(const float (&r)[J], int j) {
-    float v = r[0];
+template <class T, int J>
+__device__ __forceinline__ T slot(const T (&r)[J], int j) {
+    T v = r[0];
 #pragma unroll
     for (int q = 1; q < J; q++)
         if (j == q) v = r[q];
     return v;
 }
 
-// Panel [kb, ke) of an FP32 front factored by one warp in registers: lane l
-// holds rows kb + l + 32 j (j < J) of the panel's columns.  Per column: the
-// pivot among the pivot rows by a max and a min reduction, the pivot row and
+// The warp's largest key and, among the lanes holding it, the smallest
+// index; every lane returns both.
+__device__ __forceinline__ void warp_argmax(unsigned &key, int &bi) {
+    const unsigned kmax = __reduce_max_sync(FULL, key);
+    bi = (int)__reduce_min_sync(FULL, key == kmax ? (unsigned)bi : 0xffffffffu);
+    key = kmax;
+}
+__device__ __forceinline__ void warp_argmax(unsigned long long &key, int &bi) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const unsigned long long ok = __shfl_xor_sync(FULL, key, off);
+        const int oi = __shfl_xor_sync(FULL, bi, off);
+        if (ok > key || (ok == key && oi < bi)) {
+            key = ok;
+            bi = oi;
+        }
+    }
+}
+
+// Panel [kb, ke) factored by one warp in registers: lane l holds rows kb +
+// l + 32 j (j < J) of the panel's columns.  Per column: the pivot among the
+// pivot rows (largest magnitude, smallest row on ties), the pivot row and
 // row k exchanged through shuffles, the multipliers, the rank-1 update of
-// the panel's later columns; no barrier.  Same operations, in the same
-// order, as the shared-memory path.
-template <int J>
-__device__ void panel_warp32(float *F, int mm, int ns, int kb, int ke, int *piv, int *status) {
+// the panel's later columns; no barrier.
+template <class T, int J>
+__device__ void panel_warp(T *F, int mm, int ns, int kb, int ke, int *piv, int *status) {
+    constexpr int NP = PanelOf<T>::cols;
+    using K = typename KeyOf<T>::type;
     const int lane = threadIdx.x & 31, nb = ke - kb;
-    float P[J][kPanel];
+    T P[J][NP];
 #pragma unroll
     for (int j = 0; j < J; j++) {
         const int i = kb + lane + 32 * j;
 #pragma unroll
-        for (int c = 0; c < kPanel; c++) P[j][c] = (i < mm && c < nb) ? F[i + (kb + c) * mm] : 0.0f;
+        for (int c = 0; c < NP; c++) P[j][c] = (i < mm && c < nb) ? F[i + (kb + c) * mm] : T(0);
     }
 #pragma unroll
-    for (int c = 0; c < kPanel; c++) {
+    for (int c = 0; c < NP; c++) {
         if (c >= nb) break;
         const int k = kb + c;
         // pivot among rows k..ns-1
-        unsigned key = 0u;
+        K key = 0;
         int bi = k;
 #pragma unroll
         for (int j = 0; j < J; j++) {
             const int i = kb + lane + 32 * j;
-            const unsigned v = __float_as_uint(P[j][c]) & 0x7fffffffu;
+            const K v = (K)mag_key(P[j][c]);
             if (i >= k && i < ns && v > key) { key = v; bi = i; }
         }
-        const unsigned kmax = __reduce_max_sync(FULL, key);
-        const int pv = (int)__reduce_min_sync(FULL, key == kmax ? (unsigned)bi : 0xffffffffu);
+        warp_argmax(key, bi);
+        const int pv = bi;
         if (lane == 0) {
             piv[k] = pv;
-            if (kmax == 0u) atomicOr(status, 4);
+            if (key == 0) atomicOr(status, 4);
         }
         // the pivot row (u) and row k (w), broadcast
         const int lp = (pv - kb) & 31, jp = (pv - kb) >> 5, lk = (k - kb) & 31, jk = (k - kb) >> 5;
-        float u[kPanel], w[kPanel];
+        T u[NP], w[NP];
 #pragma unroll
-        for (int q = 0; q < kPanel; q++) {
-            float col[J];
+        for (int q = 0; q < NP; q++) {
+            T col[J];
 #pragma unroll
             for (int j = 0; j < J; j++) col[j] = P[j][q];
             u[q] = __shfl_sync(FULL, slot(col, jp), lp);
             w[q] = __shfl_sync(FULL, slot(col, jk), lk);
         }
-        const float inv = 1.0f / u[c];
+        const T inv = T(1) / u[c];
 #pragma unroll
         for (int j = 0; j < J; j++) {
             const int i = kb + lane + 32 * j;
             if (i == pv && pv != k) {
 #pragma unroll
-                for (int q = 0; q < kPanel; q++) P[j][q] = w[q];
+                for (int q = 0; q < NP; q++) P[j][q] = w[q];
             }
             if (i == k) {
 #pragma unroll
-                for (int q = 0; q < kPanel; q++) P[j][q] = u[q];
+                for (int q = 0; q < NP; q++) P[j][q] = u[q];
                 P[j][c] = inv;
             }
         }
@@ -228,10 +266,10 @@ __device__ void panel_warp32(float *F, int mm, int ns, int kb, int ke, int *piv,
         for (int j = 0; j < J; j++) {
             const int i = kb + lane + 32 * j;
             if (i > k && i < mm) {
-                const float l = P[j][c] * inv;
+                const T l = P[j][c] * inv;
                 P[j][c] = l;
 #pragma unroll
-                for (int q = 0; q < kPanel; q++)
+                for (int q = 0; q < NP; q++)
                     if (q > c) P[j][q] -= l * u[q];
             }
         }
@@ -240,50 +278,46 @@ __device__ void panel_warp32(float *F, int mm, int ns, int kb, int ke, int *piv,
     for (int j = 0; j < J; j++) {
         const int i = kb + lane + 32 * j;
 #pragma unroll
-        for (int c = 0; c < kPanel; c++)
+        for (int c = 0; c < NP; c++)
             if (i < mm && c < nb) F[i + (kb + c) * mm] = P[j][c];
     }
     __syncwarp();
 }
 
-__device__ void eliminate_cta32(float *F, int mm, int ns, int nc, int *piv, int *status) {
+template <class T>
+__device__ void eliminate_cta(T *F, int mm, int ns, int nc, int *piv, int *status) {
+    constexpr int NP = PanelOf<T>::cols;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
-    for (int kb = 0; kb < ns; kb += kPanel) {
-        const int ke = min(ns, kb + kPanel), nb = ke - kb;
+    for (int kb = 0; kb < ns; kb += NP) {
+        const int ke = min(ns, kb + NP), nb = ke - kb;
         // ---- (a) the panel ----
         if (mm - kb <= 32 * kPanelRows) {
             if (warp == 0) {
                 switch ((mm - kb + 31) >> 5) {
-                case 1: panel_warp32<1>(F, mm, ns, kb, ke, piv, status); break;
-                case 2: panel_warp32<2>(F, mm, ns, kb, ke, piv, status); break;
-                case 3: panel_warp32<3>(F, mm, ns, kb, ke, piv, status); break;
-                case 4: panel_warp32<4>(F, mm, ns, kb, ke, piv, status); break;
-                default: panel_warp32<5>(F, mm, ns, kb, ke, piv, status); break;
+                case 1: panel_warp<T, 1>(F, mm, ns, kb, ke, piv, status); break;
+                case 2: panel_warp<T, 2>(F, mm, ns, kb, ke, piv, status); break;
+                case 3: panel_warp<T, 3>(F, mm, ns, kb, ke, piv, status); break;
+                case 4: panel_warp<T, 4>(F, mm, ns, kb, ke, piv, status); break;
+                default: panel_warp<T, 5>(F, mm, ns, kb, ke, piv, status); break;
                 }
             }
             __syncthreads();
         } else
         for (int k = kb; k < ke; k++) {
             if (warp == 0) {
-                unsigned key = 0u;
-                int bi = k;
-                for (int i = k + lane; i < ns; i += 32) {
-                    const unsigned v = __float_as_uint(F[i + k * mm]) & 0x7fffffffu;
-                    if (v > key) { key = v; bi = i; }
-                }
-                const unsigned kmax = __reduce_max_sync(FULL, key);
-                const int pv = (int)__reduce_min_sync(FULL, key == kmax ? (unsigned)bi : 0xffffffffu);
+                bool zero;
+                const int pv = warp_pivot(F, mm, k, ns, zero);
                 if (lane == 0) {
                     piv[k] = pv;
-                    if (kmax == 0u) atomicOr(status, 4);
+                    if (zero) atomicOr(status, 4);
                 }
                 if (pv != k && lane < nb) {
-                    const float a = F[k + (kb + lane) * mm];
+                    const T a = F[k + (kb + lane) * mm];
                     F[k + (kb + lane) * mm] = F[pv + (kb + lane) * mm];
                     F[pv + (kb + lane) * mm] = a;
                 }
                 __syncwarp();
-                const float inv = 1.0f / F[k + k * mm];
+                const T inv = T(1) / F[k + k * mm];
                 for (int i = k + 1 + lane; i < mm; i += 32) F[i + k * mm] *= inv;
                 __syncwarp();
                 if (lane == 0) F[k + k * mm] = inv;
@@ -293,7 +327,7 @@ __device__ void eliminate_cta32(float *F, int mm, int ns, int nc, int *piv, int 
             // threads over rows, the columns split between the CTA's halves
             const int half = blockDim.x >> 1, h = tid >= half, rt = tid - h * half;
             for (int j = k + 1 + h; j < ke; j += 2) {
-                const float u = F[k + j * mm];
+                const T u = F[k + j * mm];
                 for (int i = k + 1 + rt; i < mm; i += half) F[i + j * mm] -= F[i + k * mm] * u;
             }
             __syncthreads();
@@ -304,7 +338,7 @@ __device__ void eliminate_cta32(float *F, int mm, int ns, int nc, int *piv, int 
             for (int k = kb; k < ke; k++) {
                 const int pv = piv[k];
                 if (pv != k) {
-                    const float a = F[k + j * mm];
+                    const T a = F[k + j * mm];
                     F[k + j * mm] = F[pv + j * mm];
                     F[pv + j * mm] = a;
                 }
@@ -314,16 +348,16 @@ __device__ void eliminate_cta32(float *F, int mm, int ns, int nc, int *piv, int 
         if (ke >= nc) break;
         // ---- (c) U of the panel rows, columns ke..nc-1 ----
         for (int j = ke + tid; j < nc; j += blockDim.x) {
-            float u[kPanel];
+            T u[NP];
 #pragma unroll
-            for (int q = 0; q < kPanel; q++) u[q] = q < nb ? F[kb + q + j * mm] : 0.0f;
+            for (int q = 0; q < NP; q++) u[q] = q < nb ? F[kb + q + j * mm] : T(0);
 #pragma unroll
-            for (int q = 0; q < kPanel; q++)
+            for (int q = 0; q < NP; q++)
 #pragma unroll
-                for (int p = q + 1; p < kPanel; p++)
+                for (int p = q + 1; p < NP; p++)
                     if (p < nb) u[p] -= F[kb + p + (kb + q) * mm] * u[q];
 #pragma unroll
-            for (int q = 0; q < kPanel; q++)
+            for (int q = 0; q < NP; q++)
                 if (q < nb) F[kb + q + j * mm] = u[q];
         }
         __syncthreads();
@@ -332,26 +366,26 @@ __device__ void eliminate_cta32(float *F, int mm, int ns, int nc, int *piv, int 
         const int nq = (nc - ke + 3) >> 2, nr = (mm - ke + 159) / 160;
         for (int t = warp; t < nq * nr; t += nwarp) {
             const int c0 = ke + 4 * (t % nq), r0 = ke + 160 * (t / nq);
-            float acc[5][4];
+            T acc[5][4];
 #pragma unroll
             for (int q = 0; q < 5; q++) {
                 const int i = r0 + lane + 32 * q;
 #pragma unroll
-                for (int c = 0; c < 4; c++) acc[q][c] = (i < mm && c0 + c < nc) ? F[i + (c0 + c) * mm] : 0.0f;
+                for (int c = 0; c < 4; c++) acc[q][c] = (i < mm && c0 + c < nc) ? F[i + (c0 + c) * mm] : T(0);
             }
             for (int k = kb; k < ke; k++) {
-                float u[4], l[5];
+                T u[4], l[5];
 #pragma unroll
-                for (int c = 0; c < 4; c++) u[c] = c0 + c < nc ? F[k + (c0 + c) * mm] : 0.0f;
+                for (int c = 0; c < 4; c++) u[c] = c0 + c < nc ? F[k + (c0 + c) * mm] : T(0);
 #pragma unroll
                 for (int q = 0; q < 5; q++) {
                     const int i = r0 + lane + 32 * q;
-                    l[q] = i < mm ? F[i + k * mm] : 0.0f;
+                    l[q] = i < mm ? F[i + k * mm] : T(0);
                 }
 #pragma unroll
                 for (int q = 0; q < 5; q++)
 #pragma unroll
-                    for (int c = 0; c < 4; c++) acc[q][c] = fmaf(-l[q], u[c], acc[q][c]);
+                    for (int c = 0; c < 4; c++) acc[q][c] = fma(-l[q], u[c], acc[q][c]);
             }
 #pragma unroll
             for (int q = 0; q < 5; q++) {
@@ -376,8 +410,8 @@ __device__ void eliminate_cta32(float *F, int mm, int ns, int nc, int *piv, int 
 //    also the forward solve.  It leaves the forward-solved entries in xperm
 //    and this supernode's update vector in uvec.
 template <class T, bool RHS, class G>
-__device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym &S, T *fronts, int s, int m, T *F,
-                             int *piv, G g) {
+__device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym &S, T *fronts, T *lfac, T *ufac,
+                             int s, int m, T *F, int *piv, G g) {
     const int start = S.sup_start[s];
     const int ns = S.sup_start[s + 1] - start;
     const int mm = ns + S.row_ptr[s + 1] - S.row_ptr[s];
@@ -476,17 +510,21 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
         g.sync();
     }
     // ---- elimination ----
-    // FP64: right-looking, column by column over the whole front (every
-    // update of a column is an independent FMA, which keeps GB300's long
-    // FP64 pipeline busy).  FP32: blocked; the pivot panel (columns
-    // 0..ns-1) column by column, then the right part (columns ns..nc-1) once:
-    // U12 = L11^-1 A12 by forward substitution, one column per thread, and
-    // A22 -= L21 U12, four entries per thread with the sums in registers.
-    // Both give every entry the same operations in the same order.
+    // FP64: right-looking, column by column over the whole front, each
+    // column's updates spread evenly over every thread of the group (FP64
+    // runs at two FMAs a clock per SM on GB300: the elimination is bound by
+    // the FP64 pipe, and this keeps all four of its SM sub-partitions busy,
+    // where a panel factored by one warp would idle three of them).  FP32:
+    // blocked; CTA fronts in panels (eliminate_cta), warp fronts with the
+    // pivot panel (columns 0..ns-1) column by column, then the right part
+    // (columns ns..nc-1) once: U12 = L11^-1 A12 by forward substitution, one
+    // column per thread, and A22 -= L21 U12, four entries per thread with the
+    // sums in registers.  All of them give every entry the same operations
+    // in the same order.
     constexpr bool kBlocked = sizeof(T) == 4;
     if constexpr (kBlocked && G::size > 32) {
         static_assert(!RHS, "the FP32 factorisation carries no right-hand side");
-        eliminate_cta32(F, mm, ns, nc, piv, W.status + m);
+        eliminate_cta<T>(F, mm, ns, nc, piv, W.status + m);
     } else {
     for (int k = 0; k < ns; k++) {
         if (g.lead_warp()) {
@@ -585,8 +623,29 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
             perm[p] = t;
         }
     }
-    T *out = fr + S.front_off[s];
-    for (int i = idx; i < mm * mm; i += step) out[i] = F[i];
+    // the columns ns..mm-1 (their rows ns..mm-1 are the update matrix the
+    // parent's assembly reads) as one contiguous range, and the
+    // solve-ordered copies of the factors: the L panel (columns 0..ns-1,
+    // contiguous as in F; skipped when lfac is null) and the U rows (rows
+    // 0..ns-1, leading dimension ns; the 2D index advances by the stride,
+    // one division per thread)
+    {
+        T *out = fr + S.front_off[s];
+        for (int i = ns * mm + idx; i < mm * mm; i += step) out[i] = F[i];
+        if (lfac) {
+            T *lo = lfac + (size_t)m * S.lu_total + S.lu_off[s];
+            for (int i = idx; i < mm * ns; i += step) lo[i] = F[i];
+        }
+        T *uo = ufac + (size_t)m * S.lu_total + S.lu_off[s];
+        int i = idx % ns, c = idx / ns;
+        const int di = step % ns, dc = step / ns;
+        for (int e = idx; e < ns * mm; e += step) {
+            uo[e] = F[i + c * mm];
+            i += di;
+            c += dc;
+            if (i >= ns) { i -= ns; c++; }
+        }
+    }
     g.sync();
     int *ipiv = S.ipiv + (size_t)m * S.n + start;
     for (int i = idx; i < ns; i += step) ipiv[i] = piv[ns + i];
@@ -596,6 +655,293 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
         for (int a = idx; a < mm - ns; a += step) us[a] = (double)F[mm * mm + ns + a];
     }
     g.sync();
+}
+
+// ---- split fronts ----------------------------------------------------------
+// One part of a front factored by np CTAs together (np parts, each a task of
+// the CTA kernel).  The front's columns are dealt in blocks of kSplitPanel:
+// column j belongs to part (j / kSplitPanel) % np, which keeps its columns
+// in shared memory (local index jl, leading dimension mm).  Each part
+// assembles its own columns.  Panel p (pivot columns p*kSplitPanel ..) is
+// factored by its part, column by column (pivot among the pivot rows,
+// largest magnitude, smallest row on ties; multipliers; rank-1 update of the
+// panel's later columns), and published: its columns and pivot rows to
+// global memory, then a flag set to the epoch.  Every part (the owner
+// included) then applies the panel's row interchanges to its other columns,
+// computes the U rows of its columns right of the panel and updates them
+// below it (rank kSplitPanel).  Every entry receives the same operations in
+// the same order as in the one-CTA elimination, so the factors are the same.
+// A part waits (bounded) only on the panels of the other parts of its own
+// front, which are the tasks next to it in the claim order, so with at
+// least kMaxParts resident CTAs the kernel cannot deadlock.
+// Shared memory: the local columns (mm x ncl_cap), the panel read from
+// global memory (mm x kSplitPanel), the pivot rows and their composition.
+__host__ __device__ inline int part_cols_cap(int nc, int np) {
+    const int per = kSplitPanel * np;
+    return (nc + per - 1) / per * kSplitPanel;
+}
+
+template <class T, bool RHS>
+__device__ void factor_part(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, T *fronts,
+                            T *lfac, T *ufac, int s, int m, int k, int part, int np, int epoch,
+                            unsigned char *smem) {
+    constexpr int B = kSplitPanel;
+    using K = typename KeyOf<T>::type;
+    const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
+    const int start = S.sup_start[s];
+    const int ns = S.sup_start[s + 1] - start;
+    const int mm = ns + S.row_ptr[s + 1] - S.row_ptr[s];
+    const int nc = mm + (RHS ? 1 : 0);
+    const int per = B * np;
+    // the part's columns below column j (they come first in local order)
+    auto owned_below = [&](int j) {
+        const int full = j / per, rem = j - full * per;
+        return full * B + min(B, max(0, rem - part * B));
+    };
+    auto jof = [&](int jl) { return ((jl / B) * np + part) * B + jl % B; };
+    const int ncl = owned_below(nc);
+    T *Fl = reinterpret_cast<T *>(smem);
+    T *Pn = Fl + (size_t)mm * part_cols_cap(nc, np);
+    int *piv = reinterpret_cast<int *>(Pn + (size_t)mm * B);
+    int *perm = piv + mm;
+    T *fr = fronts + (size_t)m * S.front_total;
+    double *x = W.xperm + (size_t)m * P.n_red;
+    double *uv = S.uvec + (size_t)m * S.uvec_total;
+    // front position p = i + j * mm -> local entry, -1 when another part's
+    auto local = [&](int p) {
+        const int j = p / mm;
+        return ((j / B) % np != part) ? -1 : (p - j * mm) + ((j / per) * B + j % B) * mm;
+    };
+    const int jr = ((mm / B) % np == part) ? (mm / per) * B + mm % B : -1;   // local right-hand side
+    // ---- assembly of the part's columns ----
+    for (int e = tid; e < mm * ncl; e += nthr) Fl[e] = T(0);
+    __syncthreads();
+    for (int q = S.asmc_ptr[s] + tid; q < S.asmc_ptr[s + 1]; q += nthr) {
+        const int e = local(S.asmc_pos[q]);
+        if (e >= 0) Fl[e] += (T)S.asmc_val[q];
+    }
+    if (RHS && jr >= 0)
+        for (int i = tid; i < ns; i += nthr) Fl[i + jr * mm] = (T)x[start + i];
+    __syncthreads();
+    const double *sv = W.svar + (size_t)m * P.n_var;
+    for (int q = S.asmv_ptr[s] + tid; q < S.asmv_ptr[s + 1]; q += nthr) {
+        const int e = local(S.asmv_pos[q]);
+        if (e >= 0) Fl[e] += (T)sv[S.asmv_idx[q]];
+    }
+    if (S.asmt_ptr)
+        for (int q = S.asmt_ptr[s] + tid; q < S.asmt_ptr[s + 1]; q += nthr) {
+            const int t = S.asmt_tr[q];
+            if (P.tr_on[t] && t >= P.tr_ptr[m] && t < P.tr_ptr[m + 1]) {
+                const int e = local(S.asmt_pos[q]);
+                if (e >= 0) Fl[e] += (T)S.asmt_val[q];
+            }
+        }
+    __syncthreads();
+    {
+        // the children's update matrices, entry by entry from the host lists
+        // (child order), four entries a thread with their loads together
+        const int *pp = S.pa_ptr + S.pa_base[s];
+        for (int e0 = tid; e0 < mm * ncl; e0 += 4 * nthr) {
+            T acc[4];
+            int a0[4], a1[4], kmax = 0;
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int e = e0 + u * nthr;
+                a0[u] = a1[u] = 0;
+                acc[u] = T(0);
+                if (e < mm * ncl) {
+                    const int jl = e / mm, i = e - jl * mm;
+                    acc[u] = Fl[e];
+                    if (jl != jr) {
+                        const int p = i + jof(jl) * mm;
+                        a0[u] = pp[p];
+                        a1[u] = pp[p + 1];
+                    }
+                }
+                kmax = max(kmax, a1[u] - a0[u]);
+            }
+            for (int kk = 0; kk < kmax; kk++)
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (a0[u] + kk < a1[u]) acc[u] += ldcg(fr + S.pa_src[a0[u] + kk]);
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (e0 + u * nthr < mm * ncl) Fl[e0 + u * nthr] = acc[u];
+        }
+        // (the loop above also wrote the right-hand-side column back as it
+        // found it: its children's update vectors are added after a barrier)
+        __syncthreads();
+        if (RHS && jr >= 0) {
+            const int *rp = S.pr_ptr + S.pr_base[s];
+            for (int i = tid; i < mm; i += nthr) {
+                T acc = Fl[i + jr * mm];
+                for (int e = rp[i]; e < rp[i + 1]; e++) acc += (T)ldcg(uv + S.pr_src[e]);
+                Fl[i + jr * mm] = acc;
+            }
+        }
+    }
+    __syncthreads();
+    // ---- elimination, panel by panel ----
+    const int npan = (ns + B - 1) / B;
+    int *ppv = D.ppiv + ((size_t)k * P.M + m) * D.max_split_ns;
+    T *pb = reinterpret_cast<T *>(D.pbuf) + (size_t)m * D.pb_total + D.pb_off[k];
+    int *pfl = D.pflag + ((size_t)k * P.M + m) * D.max_panels;
+    for (int pn = 0; pn < npan; pn++) {
+        const int kb = pn * B, ke = min(ns, kb + B), nb = ke - kb;
+        const bool own = pn % np == part;
+        const int jlp = own ? owned_below(kb) : -1;   // local index of column kb
+        const T *L;                                    // panel column c at L + c * mm
+        if (own) {
+            T *Fp = Fl + (size_t)jlp * mm;
+            for (int kk = kb; kk < ke; kk++) {
+                T *col = Fp + (size_t)(kk - kb) * mm;
+                if (warp == 0) {
+                    K key = 0;
+                    int bi = kk;
+                    for (int i = kk + lane; i < ns; i += 32) {
+                        const K v = (K)mag_key(col[i]);
+                        if (v > key) { key = v; bi = i; }
+                    }
+                    warp_argmax(key, bi);
+                    if (lane == 0) {
+                        piv[kk] = bi;
+                        if (key == 0) atomicOr(W.status + m, 4);
+                    }
+                    if (bi != kk && lane < nb) {
+                        const T a = Fp[kk + lane * mm];
+                        Fp[kk + lane * mm] = Fp[bi + lane * mm];
+                        Fp[bi + lane * mm] = a;
+                    }
+                    __syncwarp();
+                    const T inv = T(1) / col[kk];
+                    for (int i = kk + 1 + lane; i < mm; i += 32) col[i] *= inv;
+                    __syncwarp();
+                    if (lane == 0) col[kk] = inv;
+                }
+                __syncthreads();
+                const int lr = mm - kk - 1, lc = ke - kk - 1;
+                for (int t = tid; t < lr * lc; t += nthr) {
+                    const int c = t / lr, i = t - c * lr;
+                    Fp[(kk + 1 + i) + (kk - kb + 1 + c) * mm] -= col[kk + 1 + i] * Fp[kk + (kk - kb + 1 + c) * mm];
+                }
+                __syncthreads();
+            }
+            T *dst = pb + (size_t)pn * mm * B;
+            for (int e = tid; e < mm * nb; e += nthr) dst[e] = Fp[e];
+            for (int i = tid; i < nb; i += nthr) ppv[kb + i] = piv[kb + i];
+            __syncthreads();
+            if (tid == 0) signal_done(pfl + pn, epoch);
+            L = Fp;
+        } else {
+            if (warp == 0) {
+                if (lane == 0 && !wait_epoch(pfl + pn, epoch, D.err, D.wait_limit)) atomicOr(W.status + m, 8);
+            }
+            __syncthreads();
+            const T *src = pb + (size_t)pn * mm * B;
+            for (int e = tid; e < mm * nb; e += nthr) Pn[e] = ldcg(src + e);
+            for (int i = tid; i < nb; i += nthr) piv[kb + i] = __ldcg(ppv + kb + i);
+            __syncthreads();
+            L = Pn;
+        }
+        // ---- the panel's row interchanges on the part's other columns ----
+        for (int jl = tid; jl < ncl; jl += nthr) {
+            if (own && jl >= jlp && jl < jlp + nb) continue;
+            for (int kk = kb; kk < ke; kk++) {
+                const int pv = piv[kk];
+                if (pv != kk) {
+                    const T a = Fl[kk + jl * mm];
+                    Fl[kk + jl * mm] = Fl[pv + jl * mm];
+                    Fl[pv + jl * mm] = a;
+                }
+            }
+        }
+        __syncthreads();
+        // ---- U rows of the part's columns right of the panel ----
+        const int jl0 = owned_below(ke);
+        for (int jl = jl0 + tid; jl < ncl; jl += nthr) {
+            T u[B];
+#pragma unroll
+            for (int q = 0; q < B; q++) u[q] = q < nb ? Fl[kb + q + jl * mm] : T(0);
+#pragma unroll
+            for (int q = 0; q < B; q++)
+#pragma unroll
+                for (int p = q + 1; p < B; p++)
+                    if (p < nb) u[p] -= L[kb + p + q * mm] * u[q];
+#pragma unroll
+            for (int q = 0; q < B; q++)
+                if (q < nb) Fl[kb + q + jl * mm] = u[q];
+        }
+        __syncthreads();
+        // ---- their update below the panel, rank nb: a warp takes four
+        // columns and up to 160 rows, the sums in registers ----
+        const int nq = (ncl - jl0 + 3) >> 2, nr = (mm - ke + 159) / 160;
+        for (int t = warp; t < nq * nr; t += nwarp) {
+            const int c0 = jl0 + 4 * (t % nq), r0 = ke + 160 * (t / nq);
+            T acc[5][4];
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                const int i = r0 + lane + 32 * q;
+#pragma unroll
+                for (int c = 0; c < 4; c++) acc[q][c] = (i < mm && c0 + c < ncl) ? Fl[i + (c0 + c) * mm] : T(0);
+            }
+            for (int q = 0; q < nb; q++) {
+                T u[4], l[5];
+#pragma unroll
+                for (int c = 0; c < 4; c++) u[c] = c0 + c < ncl ? Fl[kb + q + (c0 + c) * mm] : T(0);
+#pragma unroll
+                for (int r = 0; r < 5; r++) {
+                    const int i = r0 + lane + 32 * r;
+                    l[r] = i < mm ? L[i + q * mm] : T(0);
+                }
+#pragma unroll
+                for (int r = 0; r < 5; r++)
+#pragma unroll
+                    for (int c = 0; c < 4; c++) acc[r][c] = fma(-l[r], u[c], acc[r][c]);
+            }
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                const int i = r0 + lane + 32 * q;
+#pragma unroll
+                for (int c = 0; c < 4; c++)
+                    if (i < mm && c0 + c < ncl) Fl[i + (c0 + c) * mm] = acc[q][c];
+            }
+        }
+        __syncthreads();
+    }
+    // ---- store: columns ns..mm-1 whole (the update matrix for the parent),
+    // the L panel columns and the U rows of the part's columns ----
+    {
+        T *out = fr + S.front_off[s];
+        T *lo = lfac ? lfac + (size_t)m * S.lu_total + S.lu_off[s] : nullptr;
+        T *uo = ufac + (size_t)m * S.lu_total + S.lu_off[s];
+        for (int e = tid; e < mm * ncl; e += nthr) {
+            const int jl = e / mm, i = e - jl * mm, j = jof(jl);
+            if (j >= mm) continue;
+            const T v = Fl[e];
+            if (j >= ns) out[i + (size_t)j * mm] = v;
+            else if (lo) lo[i + (size_t)j * mm] = v;
+            if (i < ns) uo[i + (size_t)j * ns] = v;
+        }
+        if (RHS && jr >= 0) {
+            for (int i = tid; i < ns; i += nthr) x[start + i] = (double)Fl[i + jr * mm];
+            double *us = uv + S.uvec_off[s];
+            for (int a = tid; a < mm - ns; a += nthr) us[a] = (double)Fl[ns + a + jr * mm];
+        }
+        if (part == 0) {
+            if (tid == 0) {
+                for (int i = 0; i < ns; i++) perm[i] = i;
+                for (int kk = 0; kk < ns; kk++) {
+                    const int pv = piv[kk], t = perm[kk];
+                    perm[kk] = perm[pv];
+                    perm[pv] = t;
+                }
+            }
+            __syncthreads();
+            int *ipiv = S.ipiv + (size_t)m * S.n + start;
+            for (int i = tid; i < ns; i += nthr) ipiv[i] = perm[i];
+        }
+    }
+    __syncthreads();
 }
 
 // Shared memory of the factorisation kernels: the front (with the
@@ -616,7 +962,8 @@ __host__ __device__ inline int big_front_bytes(int max_front) {
 
 template <class T, bool RHS>
 __global__ void __launch_bounds__(kThreads, 6) factor_small_kernel(DevProblem P, DevWork W, DevSym S, DevDag D,
-                                                                T *fronts, const uint8_t *mask, int want) {
+                                                                T *fronts, T *lfac, T *ufac, const uint8_t *mask,
+                                                                int want) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned char *wbase = smem_raw + (size_t)warp * small_warp_bytes<T>();
@@ -633,38 +980,74 @@ __global__ void __launch_bounds__(kThreads, 6) factor_small_kernel(DevProblem P,
         const int s = D.order[t / M], m = t % M;
         if (mask[m] != want) continue;
         if (!warp_wait_children(S, D, D.fdone, s, m, M, epoch, 0) && lane == 0) atomicOr(W.status + m, 8);
-        factor_front<T, RHS>(P, W, S, fronts, s, m, F, piv, WarpGroup{});
+        factor_front<T, RHS>(P, W, S, fronts, lfac, ufac, s, m, F, piv, WarpGroup{});
         if (lane == 0) signal_done(D.fdone + (size_t)s * M + m, epoch);
     }
 }
 
 template <class T, bool RHS>
 __global__ void __launch_bounds__(kThreads, 3) factor_big_kernel(DevProblem P, DevWork W, DevSym S, DevDag D,
-                                                              T *fronts, const uint8_t *mask, int want) {
+                                                              T *fronts, T *lfac, T *ufac, const uint8_t *mask,
+                                                              int want) {
+    // FP64 factorisations split the large fronts of the tail (factor_part);
+    // FP32 ones factor every front with one CTA (eliminate_cta)
+    constexpr bool kSplit = sizeof(T) == 8;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *F = reinterpret_cast<T *>(smem_raw);
-    int *piv = reinterpret_cast<int *>(smem_raw + big_front_bytes<T>(D.max_big_front));
+    int *piv = reinterpret_cast<int *>(smem_raw + big_front_bytes<T>(kSplit ? D.max_big_whole : D.max_big_front));
     __shared__ int s_task, s_ok;
     const int tid = threadIdx.x, lane = tid & 31;
     const int M = P.M;
     const int epoch = *D.epoch;
-    const int n_tasks = (D.nsup - D.n_small) * M;
+    const int n_tasks = kSplit ? D.big_units * M : (D.nsup - D.n_small) * M;
+    const int t_tail = kSplit ? (D.tail0 - D.n_small) * M : n_tasks;   // first task of the tail
+    // the tail's cumulative part counts, for the task decoding
+    __shared__ int s_units[kSplitTailMax + 1];
+    if (kSplit)
+        for (int i = tid; i <= D.n_tail; i += blockDim.x) s_units[i] = D.tail_units[i];
     for (;;) {
         __syncthreads();
         if (tid == 0) s_task = atomicAdd(D.ctr + 1, 1);
         __syncthreads();
         const int t = s_task;
         if (t >= n_tasks) break;
-        const int s = D.order[D.n_small + t / M], m = t % M;
+        // task -> (rank, scenario, part): below the tail one task per
+        // (rank, scenario); in the tail the parts of one (rank, scenario)
+        // are consecutive tasks
+        int rank, m, part = 0, np = 1;
+        if (!kSplit || t < t_tail) {
+            rank = D.n_small + t / M;
+            m = t % M;
+        } else {
+            const int u = t - t_tail;
+            int lo = 0, hi = D.n_tail - 1;   // the tail rank k with s_units[k] * M <= u
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s_units[mid] * M <= u) lo = mid;
+                else hi = mid - 1;
+            }
+            np = s_units[lo + 1] - s_units[lo];
+            const int w = u - s_units[lo] * M;
+            m = w / np;
+            part = w - m * np;
+            rank = D.tail0 + lo;
+        }
+        const int s = D.order[rank];
         if (mask[m] != want) continue;
         if (tid < 32) {
-            const bool ok = warp_wait_children(S, D, D.fdone, s, m, M, epoch, D.n_small);
+            const bool ok = warp_wait_children(S, D, D.fdone, s, m, M, epoch, D.n_small, kSplit);
             if (lane == 0) s_ok = ok;
         }
         __syncthreads();
         if (!s_ok && tid == 0) atomicOr(W.status + m, 8);
-        factor_front<T, RHS>(P, W, S, fronts, s, m, F, piv, BlockGroup{});
-        if (tid == 0) signal_done(D.fdone + (size_t)s * M + m, epoch);
+        if (np == 1) {
+            factor_front<T, RHS>(P, W, S, fronts, lfac, ufac, s, m, F, piv, BlockGroup{});
+            if (tid == 0) signal_done(D.fdone + (size_t)s * M + m, epoch);
+        } else if constexpr (kSplit) {
+            const int k = rank - D.tail0;
+            factor_part<T, RHS>(P, W, S, D, fronts, lfac, ufac, s, m, k, part, np, epoch, smem_raw);
+            if (tid == 0) signal_done(D.pdone + ((size_t)k * M + m) * kMaxParts + part, epoch);
+        }
     }
 }
 
@@ -717,9 +1100,13 @@ int dag_configure(const DevDag &D, int fp32, DagGrid &g) {
     int dev = 0, nsm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return -1;
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -1;
-    const int mb = std::max(1, D.max_big_front);
+    // FP32: every front of the CTA kernel whole; FP64: the fronts that are
+    // not split whole, and the parts of the split ones
+    const int mb = std::max(1, fp32 ? D.max_big_front : D.max_big_whole);
     const int small_bytes = kWarps * (fp32 ? small_warp_bytes<float>() : small_warp_bytes<double>());
-    const int big_bytes = (fp32 ? big_front_bytes<float>(mb) : big_front_bytes<double>(mb)) + 2 * mb * 4;
+    const int whole = (fp32 ? big_front_bytes<float>(mb) : big_front_bytes<double>(mb)) + 2 * mb * 4;
+    const int part = fp32 ? 0 : ((D.max_part_entries * 8 + 15) & ~15) + D.max_part_ints * 4;
+    const int big_bytes = std::max(whole, part);
     const int rc = fp32 ? configure_one<float>(g, nsm, small_bytes, big_bytes)
                         : configure_one<double>(g, nsm, small_bytes, big_bytes);
     if (rc != 0) {
@@ -737,19 +1124,23 @@ void launch_dag_begin(const DevDag &D, cudaStream_t st) { dag_begin_kernel<<<1, 
 
 template <class T>
 void launch_dag_factor(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, const DagGrid &g,
-                       T *fronts, const uint8_t *mask, int want, cudaStream_t st) {
+                       T *fronts, T *lfac, T *ufac, const uint8_t *mask, int want, cudaStream_t st) {
     constexpr bool R = FusedRhs<T>::value;
-    const long long ts = (long long)D.n_small * P.M, tb = (long long)(D.nsup - D.n_small) * P.M;
+    const long long ts = (long long)D.n_small * P.M,
+                    tb = (long long)(sizeof(T) == 8 ? D.big_units : D.nsup - D.n_small) * P.M;
     if (ts > 0)
-        factor_small_kernel<T, R><<<blocks_for(g.small, ts, kWarps), kThreads, g.small_bytes, st>>>(P, W, S, D,
-                                                                                                   fronts, mask, want);
+        factor_small_kernel<T, R><<<blocks_for(g.small, ts, kWarps), kThreads, g.small_bytes, st>>>(
+            P, W, S, D, fronts, lfac, ufac, mask, want);
     if (tb > 0)
-        factor_big_kernel<T, R><<<blocks_for(g.big, tb, 1), kThreads, g.big_bytes, st>>>(P, W, S, D, fronts, mask, want);
+        factor_big_kernel<T, R><<<blocks_for(g.big, tb, 1), kThreads, g.big_bytes, st>>>(P, W, S, D, fronts, lfac,
+                                                                                          ufac, mask, want);
 }
 
 template void launch_dag_factor<double>(const DevProblem &, const DevWork &, const DevSym &, const DevDag &,
-                                        const DagGrid &, double *, const uint8_t *, int, cudaStream_t);
+                                        const DagGrid &, double *, double *, double *, const uint8_t *, int,
+                                        cudaStream_t);
 template void launch_dag_factor<float>(const DevProblem &, const DevWork &, const DevSym &, const DevDag &,
-                                       const DagGrid &, float *, const uint8_t *, int, cudaStream_t);
+                                       const DagGrid &, float *, float *, float *, const uint8_t *, int,
+                                       cudaStream_t);
 
 }  // namespace gp

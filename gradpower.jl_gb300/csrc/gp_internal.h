@@ -87,6 +87,16 @@ struct DevSym {
     const int *asmt_ptr, *asmt_pos, *asmt_tr;
     const double *asmt_val;
     double *fronts;                   // [M][front_total]
+    // solve-ordered copies of the factors, written by the factorisation for
+    // the triangular solves: supernode s's L panel (mm x ns, leading
+    // dimension mm: unit-lower L below the diagonal, the reciprocal pivots
+    // on it, U11 above) in lfac and its U rows (ns x mm, leading dimension
+    // ns: U11 and U12) in ufac, both at lu_off[s].  The supernodes of a
+    // solve block are consecutive; blocks and top supernodes start on a
+    // multiple of 4 entries
+    const int64_t *lu_off;
+    int64_t lu_total;
+    double *lfac, *ufac;              // [M][lu_total] FP64 factors
     double *uvec;                     // [M][uvec_total]
     int *ipiv;                        // [M][n] pivot row within the supernode, per column
     // extend-add of the CTA-sized fronts, by entry ("pull"): for supernode s
@@ -151,7 +161,8 @@ struct DevMixed {
     double *prev_norm;     // [M] residual norm of the previous iteration
     float *lu;             // [M][n_tasks][n_lu][32] cluster LU values and pivot reciprocals
     float *cc;             // [M][n_cl][6] coupling rows of the network equations
-    float *fronts;         // [M][front_total] reduced-system factors
+    float *fronts;         // [M][front_total] reduced-system fronts (update matrices for the assembly)
+    float *lfac, *ufac;    // [M][lu_total] solve-ordered FP32 factors (DevSym::lu_off)
     double *kc;            // [M][n_tasks][kConstSlots][32] parameter constants of the cluster devices
 };
 
@@ -162,6 +173,7 @@ struct DevMixed {
 struct DevDag {
     int nsup, n_small;
     int max_front, max_big_front;
+    int max_big_whole;            // largest front of the CTA kernel that is not split (FP64)
     const int *order;       // [nsup]
     const int *rank;        // [nsup] position in order
     const int *parent;      // [nsup] parent supernode or -1
@@ -177,7 +189,32 @@ struct DevDag {
     unsigned long long *utag;     // [M][uvec_total]
     unsigned long long *xtag;     // [M][n_red]
     int wait_limit = 1 << 20;     // polls before a wait gives up (gp_set_wait_limit)
+    // Split fronts (FP64 factorisations): the large fronts near the root of
+    // the assembly tree, where few tasks can run at once, are factored by
+    // several CTAs together (gp_dag.cu, factor_part).  The last n_tail ranks of `order`
+    // (from rank tail0) form the tail; a tail supernode s has nparts[s]
+    // parts (1: one CTA as elsewhere), each part a task of its own, the
+    // parts of one (supernode, scenario) claimed one after the other.
+    int tail0 = 0, n_tail = 0;
+    int big_units = 0;            // tasks of the CTA kernel per scenario: ranks below the tail, tail parts
+    const int *tail_units;        // [n_tail+1] cumulative parts of the tail ranks
+    const uint8_t *nparts;        // [nsup] parts of each front
+    int *pdone;                   // [n_tail][M][kMaxParts] epoch at which each part finished
+    int *pflag;                   // [n_tail][M][max_panels] epoch at which each panel was published
+    int *ppiv;                    // [n_tail][M][max_split_ns] the panels' pivot rows
+    void *pbuf;                   // [M][pb_total] published panels (factor type, sized for double)
+    const int64_t *pb_off;        // [n_tail] offset of a supernode's panels in a scenario's pbuf
+    int64_t pb_total = 0;
+    int max_panels = 1, max_split_ns = 1;
+    int max_part_entries = 0;     // factor entries of the largest part's shared memory
+    int max_part_ints = 0;        // and its pivot integers
 };
+
+// Split fronts: at most kMaxParts parts; panels of kSplitPanel pivot
+// columns, owned by the parts in turn (block-cyclic columns).
+constexpr int kMaxParts = 8;
+constexpr int kSplitPanel = 8;
+constexpr int kSplitTailMax = 96;   // ranks of the tail
 
 struct DagGrid {
     int small = 0, big = 0;                  // resident blocks
@@ -189,10 +226,13 @@ int dag_configure(const DevDag &D, int fp32, DagGrid &g);
 // rides along as an extra front column); launch_dag_factor<float> does not.
 int dag_small_front();
 void launch_dag_begin(const DevDag &D, cudaStream_t st);
-// Factors the scenarios m with mask[m] == want.
+// Factors the scenarios m with mask[m] == want: fronts (update matrices) and
+// the solve-ordered copies lfac, ufac ([M][lu_total]); lfac may be null when
+// no forward solve will read it (the FP64 factorisation's own forward solve
+// is fused).
 template <class T>
 void launch_dag_factor(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, const DagGrid &g,
-                       T *fronts, const uint8_t *mask, int want, cudaStream_t st);
+                       T *fronts, T *lfac, T *ufac, const uint8_t *mask, int want, cudaStream_t st);
 // Split of the assembly tree for the triangular solves (gp_solve.cu).
 // Blocks are subtrees solved by one warp each from shared memory; their
 // entries are the block's supernodes, children before parents, the last
@@ -228,8 +268,8 @@ struct DevBlk {
 // the scenario's mode is MX_EXACT, else FP32.  With fused64 set, the forward
 // solve skips the FP64 scenarios (their factorisation did it).
 struct FrontSel {
-    const float *f32;
-    const double *f64;
+    const float *l32, *u32;     // solve-ordered FP32 factors (DevSym::lu_off), null: FP64 only
+    const double *l64, *u64;    // solve-ordered FP64 factors
     const uint8_t *mode;
     int fused64;
     int shared;    // every scenario solves with scenario 0's factors (shared-factor Woodbury path)

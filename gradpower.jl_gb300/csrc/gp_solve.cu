@@ -35,13 +35,17 @@
 // arithmetic.  The U12 product of the backward solve is a row-dot product
 // spread over all lanes.
 //
-// Front layout (column-major, leading dimension mm = ns + r): columns
-// 0..ns-1 hold L (unit lower, below the diagonal), U11 above it and the
-// reciprocal of each pivot on the diagonal; rows 0..ns-1 of columns
-// ns..mm-1 hold U12.  ipiv holds per supernode the composed row permutation
-// (pivot row i = assembled row ipiv[start + i]).  Arithmetic is in the
-// factor type, chosen per scenario (FrontSel): double for exact Newton,
-// float for the kept factors of the mixed solver; xperm and uvec are double.
+// Factor layout: the factorisation writes each supernode's factors twice,
+// in solve order (DevSym::lu_off; a block's supernodes are consecutive, so a
+// block's factors are one contiguous range).  The forward pass reads the L
+// panel (mm x ns, column-major, leading dimension mm = ns + r: unit-lower L
+// below the diagonal), the backward pass the U rows (ns x mm, leading
+// dimension ns: U11 with the reciprocal of each pivot on its diagonal, then
+// U12), so that each pass streams only the entries it uses, contiguously.
+// ipiv holds per supernode the composed row permutation (pivot row i =
+// assembled row ipiv[start + i]).  Arithmetic is in the factor type, chosen
+// per scenario (FrontSel): double for exact Newton, float for the kept
+// factors of the mixed solver; xperm and uvec are double.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -113,18 +117,30 @@ __device__ bool poll_tagged(const unsigned long long *src, int n, int tid, int n
 }
 
 __device__ __forceinline__ bool use64(const FrontSel &fs, int m) {
-    return fs.f32 == nullptr || (fs.mode != nullptr && fs.mode[m] == MX_EXACT);
+    return fs.l32 == nullptr || (fs.mode != nullptr && fs.mode[m] == MX_EXACT);
 }
 
+// The solve-ordered factors of scenario m in the factor type: the L panels
+// (forward) and the U rows (backward), both indexed by DevSym::lu_off.
 template <class T>
-__device__ __forceinline__ const T *front_base(const FrontSel &fs);
+struct Fac;
 template <>
-__device__ __forceinline__ const float *front_base<float>(const FrontSel &fs) {
-    return fs.f32;
+struct Fac<float> {
+    static __device__ __forceinline__ const float *l(const FrontSel &fs) { return fs.l32; }
+    static __device__ __forceinline__ const float *u(const FrontSel &fs) { return fs.u32; }
+};
+template <>
+struct Fac<double> {
+    static __device__ __forceinline__ const double *l(const FrontSel &fs) { return fs.l64; }
+    static __device__ __forceinline__ const double *u(const FrontSel &fs) { return fs.u64; }
+};
+template <class T>
+__device__ __forceinline__ const T *lfac(const FrontSel &fs, const DevSym &S, int m) {
+    return Fac<T>::l(fs) + (size_t)(fs.shared ? 0 : m) * S.lu_total;
 }
-template <>
-__device__ __forceinline__ const double *front_base<double>(const FrontSel &fs) {
-    return fs.f64;
+template <class T>
+__device__ __forceinline__ const T *ufac(const FrontSel &fs, const DevSym &S, int m) {
+    return Fac<T>::u(fs) + (size_t)(fs.shared ? 0 : m) * S.lu_total;
 }
 
 template <class T, int J>
@@ -340,14 +356,15 @@ __device__ void fwd_front_blk(const T *F, Perm perm, int ns, int mm, T *v) {
     }
 }
 
+// U: the front's U rows (ns x mm, leading dimension ns).
 template <class T, int LW = 32>
-__device__ void bwd_front_blk(const T *F, int ns, int mm, T *v) {
-    bwd_u12<T, LW>(F, mm, 0, ns, mm, ns, v);
-    if (ns <= LW) bwd_cols_j<T, 1, 4, LW>(F, mm, 0, 0, ns, ns, v);
-    else if (ns <= 2 * LW) bwd_cols_j<T, 2, 4, LW>(F, mm, 0, 0, ns, ns, v);
+__device__ void bwd_front_blk(const T *U, int ns, int mm, T *v) {
+    bwd_u12<T, LW>(U, ns, 0, ns, mm, ns, v);
+    if (ns <= LW) bwd_cols_j<T, 1, 4, LW>(U, ns, 0, 0, ns, ns, v);
+    else if (ns <= 2 * LW) bwd_cols_j<T, 2, 4, LW>(U, ns, 0, 0, ns, ns, v);
     else if constexpr (LW < 32) {
-        if (ns <= 3 * LW) bwd_cols_j<T, 3, 2, LW>(F, mm, 0, 0, ns, ns, v);
-        else bwd_cols_j<T, 4, 2, LW>(F, mm, 0, 0, ns, ns, v);
+        if (ns <= 3 * LW) bwd_cols_j<T, 3, 2, LW>(U, ns, 0, 0, ns, ns, v);
+        else bwd_cols_j<T, 4, 2, LW>(U, ns, 0, 0, ns, ns, v);
     }
 }
 
@@ -395,7 +412,7 @@ __device__ BlkTask stage_block(const DevSym &S, const DevBlk &B, int blk, int mf
         const int4 a = B.ent0[e0 + q];
         E0[q] = a;
         E1[q] = B.ent1[e0 + q];
-        FO[q] = (long long)S.front_off[a.x];
+        FO[q] = (long long)S.lu_off[a.x];
     }
     const int mb = B.map_ptr[blk], nmap = B.map_ptr[blk + 1] - mb;
     for (int i = lane; i < nmap; i += 32) mp[i] = map[mb + i];
@@ -413,30 +430,18 @@ __device__ BlkTask stage_block(const DevSym &S, const DevBlk &B, int blk, int mf
 __device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
 
 // Pulls the factor entries a block task's sweep will read into L1 before
-// the sweep (and, backward, before the wait on the parent), so that the
-// sweep's column chunks do not each wait on L2.  Forward: columns [0, ns) of
-// every front, one contiguous range; backward: rows [0, ns) of every column.
-// Every address lies inside the front.
+// the sweep (and, backward, before the waits on the top region), so that
+// the sweep's column chunks do not each wait on L2.  The block's L panels
+// (forward) or U rows (backward) are one contiguous range of the
+// solve-ordered factors; every address lies inside it.
 template <class T, int LW = 32>
-__device__ void prefetch_block(const DevSym &S, const FrontSel &fs, const BlkTask &t, int m, bool fwd) {
+__device__ void prefetch_block(const T *fac, const BlkTask &t) {
     const int lane = threadIdx.x & (LW - 1);
-    const T *fr = front_base<T>(fs) + (size_t)(fs.shared ? 0 : m) * S.front_total;
-    for (int q = 0; q < t.n; q++) {
-        const int4 a = t.E0[q];
-        const int ns = a.z, mm = a.z + a.w;
-        const T *f = fr + t.FO[q];
-        if (fwd) {
-            const uintptr_t l0 = (uintptr_t)f & ~(uintptr_t)127, l1 = (uintptr_t)(f + (size_t)mm * ns - 1);
-            for (uintptr_t ad = l0 + (uintptr_t)lane * 128; ad <= l1; ad += LW * 128)
-                prefetch_l1(reinterpret_cast<const void *>(ad));
-        } else {
-            for (int c = lane; c < mm; c += LW) {
-                const T *col = f + (size_t)c * mm;
-                prefetch_l1(col);
-                if ((((uintptr_t)col) >> 7) != (((uintptr_t)(col + ns - 1)) >> 7)) prefetch_l1(col + ns - 1);
-            }
-        }
-    }
+    const int4 a = t.E0[t.n - 1];
+    const T *f0 = fac + t.FO[0], *f1 = fac + t.FO[t.n - 1] + (size_t)(a.z + a.w) * a.z - 1;
+    const uintptr_t l0 = (uintptr_t)f0 & ~(uintptr_t)127, l1 = (uintptr_t)f1;
+    for (uintptr_t ad = l0 + (uintptr_t)lane * 128; ad <= l1; ad += LW * 128)
+        prefetch_l1(reinterpret_cast<const void *>(ad));
 }
 
 // Pivot rows of one segment in the interleaved byte table.
@@ -470,7 +475,7 @@ __device__ void fwd_block(const DevProblem &P, const DevWork &W, const DevSym &S
         for (int i = lane; i < a.z + a.w; i += LW) vs[b.y + i] = i < a.z ? (T)x[a.y + i] : T(0);
     }
     __syncwarp();
-    const T *fr = front_base<T>(fs) + (size_t)(fs.shared ? 0 : m) * S.front_total;
+    const T *fr = lfac<T>(fs, S, m);
     double *xo = W.xperm + (size_t)m * P.n_red;
     double *uv = S.uvec + (size_t)m * S.uvec_total;
     for (int q = 0; q < t.n; q++) {
@@ -522,7 +527,7 @@ __device__ void bwd_block(const DevProblem &P, const DevWork &W, const DevSym &S
         for (int k = lane; k < next; k += LW) vs[B.ext_pos[xb + k]] = (T)x[B.ext_row[xb + k]];
     }
     __syncwarp();
-    const T *fr = front_base<T>(fs) + (size_t)(fs.shared ? 0 : m) * S.front_total;
+    const T *fr = ufac<T>(fs, S, m);
     for (int q = t.n - 1; q >= 0; q--) {
         const int4 a = t.E0[q], b = t.E1[q];
         const int ns = a.z, r = a.w;
@@ -537,15 +542,10 @@ __device__ void bwd_block(const DevProblem &P, const DevWork &W, const DevSym &S
 
 // ---- top region: dataflow of CTA tasks ------------------------------------
 
-// All threads of the CTA copy columns [c0, c1) of rows [0, nrow) of the
-// front F (leading dimension mm) into Fs (leading dimension nrow).
+// All threads of the CTA copy n consecutive factor entries into Fs.
 template <class T>
-__device__ void stage_cols(T *Fs, const T *F, int mm, int nrow, int c0, int c1) {
-    const int n = nrow * (c1 - c0);
-    for (int e = threadIdx.x; e < n; e += blockDim.x) {
-        const int c = e / nrow, i = e - c * nrow;
-        cp_async(Fs + e, F + i + (size_t)(c0 + c) * mm, (int)sizeof(T));
-    }
+__device__ void stage_range(T *Fs, const T *F, int n) {
+    for (int e = threadIdx.x; e < n; e += blockDim.x) cp_async(Fs + e, F + e, (int)sizeof(T));
 }
 
 struct TopCtx {
@@ -601,7 +601,7 @@ __device__ void fwd_top_task(const DevProblem &P, const DevWork &W, const DevSym
     int *sxr = reinterpret_cast<int *>(smem + top_vec_bytes(tmf));
     int *sxe = sxr + align16((tmf + 1) * 4) / 4;
     T *Fs = reinterpret_cast<T *>(smem + top_vec_bytes(tmf) + top_idx_bytes(tmf, B.top_max_xent));
-    const T *F = front_base<T>(fs) + (size_t)(fs.shared ? 0 : t.m) * S.front_total + S.front_off[t.s];
+    const T *F = lfac<T>(fs, S, t.m) + S.lu_off[t.s];   // L panel, leading dimension mm
     const int cap = kTopStage / ((int)sizeof(T) * t.mm);   // columns per staged chunk
     double *x = W.xperm + (size_t)t.m * P.n_red;
     double *uv = S.uvec + (size_t)t.m * S.uvec_total;
@@ -614,7 +614,7 @@ __device__ void fwd_top_task(const DevProblem &P, const DevWork &W, const DevSym
     for (int i = threadIdx.x; i < t.mm; i += blockDim.x) v[i] = i < t.ns ? (T)x[t.start + i] : T(0);
     for (int i = threadIdx.x; i < t.ns; i += blockDim.x) pi[i] = ip[i];
     int k1 = min(t.ns, cap);
-    stage_cols<T>(Fs, F, t.mm, t.mm, 0, k1);
+    stage_range<T>(Fs, F, k1 * t.mm);
     __syncthreads();
     const int ne = sxr[t.mm] - sxr[0];
     for (int e = threadIdx.x; e < ne; e += blockDim.x) sxe[e] = B.top_xent[sxr[0] + e];
@@ -657,7 +657,7 @@ __device__ void fwd_top_task(const DevProblem &P, const DevWork &W, const DevSym
         if (k1 >= t.ns) break;
         k0 = k1;
         k1 = min(t.ns, k0 + cap);
-        stage_cols<T>(Fs, F, t.mm, t.mm, k0, k1);
+        stage_range<T>(Fs, F + (size_t)k0 * t.mm, (k1 - k0) * t.mm);
     }
     for (int i = threadIdx.x; i < t.ns; i += blockDim.x) x[t.start + i] = (double)v[i];
     if constexpr (Tagged<T>::value) {
@@ -677,7 +677,7 @@ __device__ void bwd_top_task(const DevProblem &P, const DevWork &W, const DevSym
     T *v = reinterpret_cast<T *>(smem);
     int *pi = reinterpret_cast<int *>(smem + tmf * 16);
     T *Fs = reinterpret_cast<T *>(smem + top_vec_bytes(tmf));
-    const T *F = front_base<T>(fs) + (size_t)(fs.shared ? 0 : t.m) * S.front_total + S.front_off[t.s];
+    const T *F = ufac<T>(fs, S, t.m) + S.lu_off[t.s];   // U rows, leading dimension ns
     const int cap = kTopStage / ((int)sizeof(T) * max(1, t.ns));   // columns per staged chunk
     double *x = W.xperm + (size_t)t.m * P.n_red;
     const int *rows = S.rows + S.row_ptr[t.s];
@@ -686,7 +686,7 @@ __device__ void bwd_top_task(const DevProblem &P, const DevWork &W, const DevSym
     // chunks run over the front's columns from mm - 1 down to 0: U12 first,
     // then U11 from the last pivot column
     int c1 = t.mm, c0 = max(0, t.mm - cap);
-    stage_cols<T>(Fs, F, t.mm, t.ns, c0, c1);
+    stage_range<T>(Fs, F + (size_t)c0 * t.ns, (c1 - c0) * t.ns);
     if constexpr (Tagged<T>::value) {
         // the entries of the front's rows (pivots of ancestors), polled as
         // tagged words by the thread that staged their row indices
@@ -711,7 +711,7 @@ __device__ void bwd_top_task(const DevProblem &P, const DevWork &W, const DevSym
         if (c0 == 0) break;
         c1 = c0;
         c0 = max(0, c1 - cap);
-        stage_cols<T>(Fs, F, t.mm, t.ns, c0, c1);
+        stage_range<T>(Fs, F + (size_t)c0 * t.ns, (c1 - c0) * t.ns);
     }
     for (int i = threadIdx.x; i < t.ns; i += blockDim.x) x[t.start + i] = (double)v[i];
     if constexpr (Tagged<T>::value) {
@@ -734,7 +734,7 @@ __device__ void bwd_top_task(const DevProblem &P, const DevWork &W, const DevSym
 // Mixed solves pair the scenarios in the block phase (two per warp); a pair
 // runs in the two half-warps when both scenarios are active and on FP32
 // factors (the FP32 vector of each fits half of the area sized for FP64).
-__device__ __forceinline__ bool pair_mode(const FrontSel &fs) { return fs.f32 != nullptr && !fs.shared; }
+__device__ __forceinline__ bool pair_mode(const FrontSel &fs) { return fs.l32 != nullptr && !fs.shared; }
 __device__ __forceinline__ bool pair_ok(const DevWork &W, const FrontSel &fs, int m) {
     return W.active[m] && !use64(fs, m);
 }
@@ -773,7 +773,7 @@ __global__ void __launch_bounds__(kTopThreads, 8) fwd_solve_kernel(DevProblem P,
                     __syncwarp();
                     unsigned char *pvb = base + lay.piv;
                     stage_piv_pair(S, bt, m0, m1, pvb);
-                    prefetch_block<float, 16>(S, fs, bt, m, true);
+                    prefetch_block<float, 16>(lfac<float>(fs, S, m), bt);
                     __syncwarp();
                     fwd_block<float, 16>(P, W, S, D, epoch, fs, bt, m,
                                          reinterpret_cast<float *>(base + lay.v) + seg * B.max_v, pvb);
@@ -788,8 +788,8 @@ __global__ void __launch_bounds__(kTopThreads, 8) fwd_solve_kernel(DevProblem P,
                 if (d && fs.fused64) continue;
                 const BlkTask bt = stage_block(S, B, blk, fs.shared ? 0 : m, base, lay, B.map_fwd, true);
                 __syncwarp();
-                if (d) prefetch_block<double>(S, fs, bt, m, true);
-                else prefetch_block<float>(S, fs, bt, m, true);
+                if (d) prefetch_block<double>(lfac<double>(fs, S, m), bt);
+                else prefetch_block<float>(lfac<float>(fs, S, m), bt);
                 if (d) fwd_block<double>(P, W, S, D, epoch, fs, bt, m, reinterpret_cast<double *>(base + lay.v));
                 else fwd_block<float>(P, W, S, D, epoch, fs, bt, m, reinterpret_cast<float *>(base + lay.v));
                 __syncwarp();
@@ -862,7 +862,7 @@ __global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P,
                 const int seg = (threadIdx.x >> 4) & 1, m = seg ? m1 : m0;
                 const BlkTask bt = stage_block(S, B, blk, 0, base, lay, B.map_bwd, false);
                 __syncwarp();
-                prefetch_block<float, 16>(S, fs, bt, m, false);
+                prefetch_block<float, 16>(ufac<float>(fs, S, m), bt);
                 __syncwarp();
                 bwd_block<float, 16>(P, W, S, B, D, epoch, fs, bt, blk, m,
                                      reinterpret_cast<float *>(base + lay.v) + seg * B.max_v);
@@ -876,8 +876,8 @@ __global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P,
             const BlkTask bt = stage_block(S, B, blk, fs.shared ? 0 : m, base, lay, B.map_bwd, false);
             __syncwarp();
             const bool d = use64(fs, m);
-            if (d) prefetch_block<double>(S, fs, bt, m, false);
-            else prefetch_block<float>(S, fs, bt, m, false);
+            if (d) prefetch_block<double>(ufac<double>(fs, S, m), bt);
+            else prefetch_block<float>(ufac<float>(fs, S, m), bt);
             if (d && par >= 0) {
                 bool ok = true;
                 if (lane == 0) ok = wait_epoch(D.bdone + (size_t)par * M + m, epoch, D.err, D.wait_limit);
