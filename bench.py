@@ -68,15 +68,17 @@ def load_oracle():
 
 
 def solve_traffic():
-    """DRAM bytes (read + write) of one forward + backward solve launch pair
-    of the mixed path on this workload, from the committed summary of an ncu
-    capture (profiles/), with the capture's command as its source; (None,
-    None) when there is no such summary."""
+    """DRAM bytes (read + write) per scenario of one forward + backward
+    solve launch pair of the mixed path on this workload, from the
+    committed summary of an ncu capture (profiles/): the pair's bytes over
+    the scenarios active in the captured launches, with the capture's
+    command as its source; (None, None) when there is no such summary."""
     path = os.path.join(ROOT, "profiles", "planar70k_solve_dram.json")
     try:
         with open(path) as f:
             d = json.load(f)
-        return float(d["dram_bytes_per_launch_pair"]), "ncu capture: " + d["command"]
+        return (float(d["dram_bytes_per_launch_pair"]) / float(d["active_scenarios"]),
+                "ncu capture (%d active scenarios): %s" % (d["active_scenarios"], d["command"]))
     except Exception:
         return None, None
 
@@ -528,14 +530,17 @@ def gpu_arm(args):
     ms, bytes_per_scen, scen_passes = phases[dom]
     achieved = bytes_per_scen * scen_passes / (ms / 1e3) / 1e9 if ms > 0 else 0.0
     launches = accp["linear_solves"] if dom == "solve" else None
-    traffic, traffic_src = solve_traffic() if dom == "solve" else (None, None)
+    traffic_scen, traffic_src = solve_traffic() if dom == "solve" else (None, None)
     alg_per_launch = bytes_per_scen * scen_passes / launches if launches else None
+    # the capture's bytes per scenario, scaled to this run's average launch
+    # pair (scenarios drop out of a solve as they converge)
+    traffic = traffic_scen * scen_passes / launches if traffic_scen and launches else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per launch pair",
                 "traffic_source": traffic_src, "kernel": dom,
                 "algorithmic_bytes_per_scenario_pass": bytes_per_scen,
                 "algorithmic_bytes_per_launch_pair": alg_per_launch,
-                "traffic_over_algorithmic": traffic / alg_per_launch if traffic and alg_per_launch else None,
+                "traffic_over_algorithmic": traffic_scen / bytes_per_scen if traffic_scen else None,
                 "peak_source": peak_kind,
                 "timing": "phase times from one pass with the host-driven Newton loop and CUDA events on the "
                           "library stream around every phase (same kernels as the timed region)",
