@@ -502,6 +502,9 @@ struct HostBlk {
     int nblk = 0;
     int max_n = 1, max_v = 1, max_p = 1, max_map = 1, max_ext = 1;
     std::vector<int> blk_ptr{0}, map_ptr{0}, ext_ptr{0}, map_fwd, map_bwd, ext_pos, ext_row;
+    // the block's pivot columns in member order (entry e of a block is its
+    // pivot slot e) and each one's position in the block's vector
+    std::vector<int> pcol_ptr{0}, pcol, pvs;
     std::vector<int4> ent0, ent1;
     int n_top_levels = 0, top_max_front = 1, top_max_xent = 1;
     std::vector<int> top_order, top_rank;
@@ -582,6 +585,10 @@ void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
             const int m = sym.front_m(s), n = sym.front_n(s), r = sym.front_r(s);
             B.ent0.push_back(make_int4(s, sym.sup_start[s], n, r));
             B.ent1.push_back(make_int4(0, vo, mo, po));
+            for (int i = 0; i < n; i++) {
+                B.pcol.push_back(sym.sup_start[s] + i);
+                B.pvs.push_back(vo + i);
+            }
             voff_of[s] = vo;
             vo += m;
             mo += r;
@@ -615,6 +622,7 @@ void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
         B.blk_ptr.push_back((int)B.ent0.size());
         B.map_ptr.push_back((int)B.map_fwd.size());
         B.ext_ptr.push_back((int)B.ext_pos.size());
+        B.pcol_ptr.push_back((int)B.pcol.size());
     }
     B.nblk = nblk;
     // top region by level (leaves of the region first)
@@ -887,10 +895,18 @@ void host_block_solve(const gp::Symbolic &S, const HostBlk &B, const std::vector
         if (n > B.max_n) fail(GP_E_INTERNAL, "block solve: %d entries above max_n", n);
         const int mb = B.map_ptr[blk], nmap = B.map_ptr[blk + 1] - mb;
         for (int i = 0; i < nmap; i++) mp[i] = B.map_fwd[mb + i];
+        // the device stages pivots and right-hand side through the block's
+        // flat pivot list: entry b.w + i is column a.y + i at vector b.y + i
+        const int p0 = B.pcol_ptr[blk];
+        if (B.pcol_ptr[blk + 1] - p0 > B.max_p) fail(GP_E_INTERNAL, "block solve: pivot list above max_p");
         for (int q = 0; q < n; q++) {
             int4 a, b;
             ent(e0 + q, a, b);
-            for (int i = 0; i < a.z; i++) pv[b.w + i] = ipiv[a.y + i];
+            for (int i = 0; i < a.z; i++) {
+                if (B.pcol[p0 + b.w + i] != a.y + i || B.pvs[p0 + b.w + i] != b.y + i)
+                    fail(GP_E_INTERNAL, "block solve: pivot list of block %d", blk);
+                pv[b.w + i] = ipiv[B.pcol[p0 + b.w + i]];
+            }
             for (int i = 0; i < a.z + a.w; i++) vs[b.y + i] = i < a.z ? x[a.y + i] : 0.0;
         }
         for (int q = 0; q < n; q++) {
@@ -1118,6 +1134,9 @@ void build_blocks(gp_layout *L, const gp::Symbolic &sym) {
     B.ext_ptr = A.upload(H.ext_ptr);
     B.ext_pos = A.upload(H.ext_pos);
     B.ext_row = A.upload(H.ext_row);
+    B.pcol_ptr = A.upload(H.pcol_ptr);
+    B.pcol = A.upload(H.pcol);
+    B.pvs = A.upload(H.pvs);
     B.n_top = (int)H.top_order.size();
     B.top_max_front = H.top_max_front;
     B.top_max_xent = H.top_max_xent;

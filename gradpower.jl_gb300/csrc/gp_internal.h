@@ -252,6 +252,10 @@ struct DevBlk {
     const int *map_bwd;          // per update row: vector position of that row's solution
     const int *ext_ptr;          // [nblk+1]
     const int *ext_pos, *ext_row;   // solution entries above the block: vector position, xperm row
+    // per block, its pivot columns in member order (entry e is pivot slot
+    // e) and each one's position in the block's vector
+    const int *pcol_ptr;         // [nblk+1]
+    const int *pcol, *pvs;
     int n_top, top_max_front;
     int top_max_xent;            // most extend-add entries of one top supernode
     const int *top_order;        // [n_top] top supernodes, children before parents

@@ -408,23 +408,77 @@ __device__ BlkTask stage_block(const DevSym &S, const DevBlk &B, int blk, int mf
     int *mp = reinterpret_cast<int *>(base + lay.map);
     int *pv = reinterpret_cast<int *>(base + lay.piv);
     const int e0 = B.blk_ptr[blk], n = B.blk_ptr[blk + 1] - e0;
-    for (int q = lane; q < n; q += 32) {
-        const int4 a = B.ent0[e0 + q];
-        E0[q] = a;
-        E1[q] = B.ent1[e0 + q];
-        FO[q] = (long long)S.lu_off[a.x];
+    for (int q0 = lane; q0 < n; q0 += 64) {
+        int4 a[2], b[2];
+        long long f[2];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int q = q0 + 32 * u;
+            a[u] = q < n ? B.ent0[e0 + q] : make_int4(0, 0, 0, 0);
+            b[u] = q < n ? B.ent1[e0 + q] : make_int4(0, 0, 0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < 2; u++) f[u] = q0 + 32 * u < n ? (long long)S.lu_off[a[u].x] : 0;
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int q = q0 + 32 * u;
+            if (q < n) {
+                E0[q] = a[u];
+                E1[q] = b[u];
+                FO[q] = f[u];
+            }
+        }
     }
+    // (the loops below keep four loads a lane in flight: a store waiting on
+    // its load would otherwise hold back the next iteration's load)
     const int mb = B.map_ptr[blk], nmap = B.map_ptr[blk + 1] - mb;
-    for (int i = lane; i < nmap; i += 32) mp[i] = map[mb + i];
-    __syncwarp();
+    for (int i0 = lane; i0 < nmap; i0 += 4 * 32) {
+        int v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) v[u] = i0 + 32 * u < nmap ? map[mb + i0 + 32 * u] : 0;
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (i0 + 32 * u < nmap) mp[i0 + 32 * u] = v[u];
+    }
     if (with_piv) {
         const int *ip = S.ipiv + (size_t)mf * S.n;
-        for (int q = 0; q < n; q++) {
-            const int4 a = E0[q], b = E1[q];
-            for (int i = lane; i < a.z; i += 32) pv[b.w + i] = ip[a.y + i];
+        const int p0 = B.pcol_ptr[blk], np = B.pcol_ptr[blk + 1] - p0;
+        for (int e0 = lane; e0 < np; e0 += 4 * 32) {
+            int c[4], v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) c[u] = e0 + 32 * u < np ? B.pcol[p0 + e0 + 32 * u] : 0;
+#pragma unroll
+            for (int u = 0; u < 4; u++) v[u] = e0 + 32 * u < np ? ip[c[u]] : 0;
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (e0 + 32 * u < np) pv[e0 + 32 * u] = v[u];
         }
     }
     return BlkTask{e0, n, E0, E1, FO, mp, pv};
+}
+
+// The pivot rows' entries of x into a block's vector vs (entry e of the
+// block's pivot list at vs[pvs[e]]), four loads a lane in flight; LW-lane
+// segments each on their own vector.
+template <class T, int LW>
+__device__ void gather_pivot_rows(const DevBlk &B, int blk, const double *x, T *vs) {
+    const int lane = threadIdx.x & (LW - 1);
+    const int p0 = B.pcol_ptr[blk], np = B.pcol_ptr[blk + 1] - p0;
+    for (int e0 = lane; e0 < np; e0 += 4 * LW) {
+        int c[4], q[4];
+        T v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const bool in = e0 + LW * u < np;
+            c[u] = in ? B.pcol[p0 + e0 + LW * u] : 0;
+            q[u] = in ? B.pvs[p0 + e0 + LW * u] : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) v[u] = e0 + LW * u < np ? (T)x[c[u]] : T(0);
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (e0 + LW * u < np) vs[q[u]] = v[u];
+    }
 }
 
 __device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
@@ -453,12 +507,19 @@ struct PermBytes {
 // Two scenarios per warp (LW = 16, segment seg = 0, 1 of the warp): the
 // pivots of both, one byte each (pivot rows are within the supernode's
 // pivot block, fewer than kBlkFront), interleaved in the pivot area.
-__device__ void stage_piv_pair(const DevSym &S, const BlkTask &t, int m0, int m1, unsigned char *pvb) {
+__device__ void stage_piv_pair(const DevSym &S, const DevBlk &B, int blk, int m0, int m1, unsigned char *pvb) {
     const int lane = threadIdx.x & 15, seg = (threadIdx.x >> 4) & 1;
     const int *ip = S.ipiv + (size_t)(seg ? m1 : m0) * S.n;
-    for (int q = 0; q < t.n; q++) {
-        const int4 a = t.E0[q], b = t.E1[q];
-        for (int i = lane; i < a.z; i += 16) pvb[2 * (b.w + i) + seg] = (unsigned char)ip[a.y + i];
+    const int p0 = B.pcol_ptr[blk], np = B.pcol_ptr[blk + 1] - p0;
+    for (int e0 = lane; e0 < np; e0 += 4 * 16) {
+        int c[4], v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) c[u] = e0 + 16 * u < np ? B.pcol[p0 + e0 + 16 * u] : 0;
+#pragma unroll
+        for (int u = 0; u < 4; u++) v[u] = e0 + 16 * u < np ? ip[c[u]] : 0;
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (e0 + 16 * u < np) pvb[2 * (e0 + 16 * u) + seg] = (unsigned char)v[u];
     }
 }
 
@@ -466,13 +527,18 @@ __device__ void stage_piv_pair(const DevSym &S, const BlkTask &t, int m0, int m1
 // scenario, pivots in t.pv; LW = 16: each half-warp on its own scenario
 // (same block, so the same control flow), pivots in pvb.
 template <class T, int LW = 32>
-__device__ void fwd_block(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, int epoch,
-                          const FrontSel &fs, const BlkTask &t, int m, T *vs, const unsigned char *pvb = nullptr) {
+__device__ void fwd_block(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B, int blk,
+                          const DevDag &D, int epoch, const FrontSel &fs, const BlkTask &t, int m, T *vs,
+                          const unsigned char *pvb = nullptr) {
     const int lane = threadIdx.x & (LW - 1), seg = (threadIdx.x >> 4) & 1;
     const double *x = W.xperm + (size_t)m * P.n_red;
-    for (int q = 0; q < t.n; q++) {
-        const int4 a = t.E0[q], b = t.E1[q];
-        for (int i = lane; i < a.z + a.w; i += LW) vs[b.y + i] = i < a.z ? (T)x[a.y + i] : T(0);
+    // the block's vector: zero, then the pivot rows' right-hand side
+    {
+        const int4 al = t.E0[t.n - 1], bl = t.E1[t.n - 1];
+        const int nv = bl.y + al.z + al.w;
+        for (int i = lane; i < nv; i += LW) vs[i] = T(0);
+        __syncwarp();
+        gather_pivot_rows<T, LW>(B, blk, x, vs);
     }
     __syncwarp();
     const T *fr = lfac<T>(fs, S, m);
@@ -512,10 +578,7 @@ __device__ void bwd_block(const DevProblem &P, const DevWork &W, const DevSym &S
                           int epoch, const FrontSel &fs, const BlkTask &t, int blk, int m, T *vs) {
     const int lane = threadIdx.x & (LW - 1);
     double *x = W.xperm + (size_t)m * P.n_red;
-    for (int q = 0; q < t.n; q++) {
-        const int4 a = t.E0[q], b = t.E1[q];
-        for (int i = lane; i < a.z; i += LW) vs[b.y + i] = (T)x[a.y + i];
-    }
+    gather_pivot_rows<T, LW>(B, blk, x, vs);
     const int xb = B.ext_ptr[blk], next = B.ext_ptr[blk + 1] - xb;
     if constexpr (Tagged<T>::value) {
         const unsigned long long *xt = D.xtag + (size_t)m * P.n_red;
@@ -764,7 +827,6 @@ __global__ void __launch_bounds__(kTopThreads, 8) fwd_solve_kernel(DevProblem P,
             t = __shfl_sync(FULL, t, 0);
             if (t >= n_blk) break;
             const int blk = (int)(t / MP), u = (int)(t % MP);
-            const int root = B.ent0[B.blk_ptr[blk + 1] - 1].x;
             if (MP != M) {
                 const int m0 = 2 * u, m1 = 2 * u + 1;
                 if (m1 < M && pair_ok(W, fs, m0) && pair_ok(W, fs, m1)) {
@@ -772,10 +834,10 @@ __global__ void __launch_bounds__(kTopThreads, 8) fwd_solve_kernel(DevProblem P,
                     const BlkTask bt = stage_block(S, B, blk, 0, base, lay, B.map_fwd, false);
                     __syncwarp();
                     unsigned char *pvb = base + lay.piv;
-                    stage_piv_pair(S, bt, m0, m1, pvb);
+                    stage_piv_pair(S, B, blk, m0, m1, pvb);
                     prefetch_block<float, 16>(lfac<float>(fs, S, m), bt);
                     __syncwarp();
-                    fwd_block<float, 16>(P, W, S, D, epoch, fs, bt, m,
+                    fwd_block<float, 16>(P, W, S, B, blk, D, epoch, fs, bt, m,
                                          reinterpret_cast<float *>(base + lay.v) + seg * B.max_v, pvb);
                     __syncwarp();
                     continue;
@@ -790,10 +852,10 @@ __global__ void __launch_bounds__(kTopThreads, 8) fwd_solve_kernel(DevProblem P,
                 __syncwarp();
                 if (d) prefetch_block<double>(lfac<double>(fs, S, m), bt);
                 else prefetch_block<float>(lfac<float>(fs, S, m), bt);
-                if (d) fwd_block<double>(P, W, S, D, epoch, fs, bt, m, reinterpret_cast<double *>(base + lay.v));
-                else fwd_block<float>(P, W, S, D, epoch, fs, bt, m, reinterpret_cast<float *>(base + lay.v));
+                if (d) fwd_block<double>(P, W, S, B, blk, D, epoch, fs, bt, m, reinterpret_cast<double *>(base + lay.v));
+                else fwd_block<float>(P, W, S, B, blk, D, epoch, fs, bt, m, reinterpret_cast<float *>(base + lay.v));
                 __syncwarp();
-                if (d && lane == 0) signal_done(D.xdone + (size_t)root * M + m, epoch);
+                if (d && lane == 0) signal_done(D.xdone + (size_t)bt.E0[bt.n - 1].x * M + m, epoch);
                 __syncwarp();
             }
         }
@@ -855,7 +917,6 @@ __global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P,
         t = __shfl_sync(FULL, t, 0);
         if (t >= n_blk) break;
         const int blk = (int)(t / MP), u = (int)(t % MP);
-        const int par = D.parent[B.ent0[B.blk_ptr[blk + 1] - 1].x];
         if (MP != M) {
             const int m0 = 2 * u, m1 = 2 * u + 1;
             if (m1 < M && pair_ok(W, fs, m0) && pair_ok(W, fs, m1)) {
@@ -878,7 +939,8 @@ __global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P,
             const bool d = use64(fs, m);
             if (d) prefetch_block<double>(ufac<double>(fs, S, m), bt);
             else prefetch_block<float>(ufac<float>(fs, S, m), bt);
-            if (d && par >= 0) {
+            const int par = d ? D.parent[bt.E0[bt.n - 1].x] : -1;   // (FP64 factors wait on it)
+            if (par >= 0) {
                 bool ok = true;
                 if (lane == 0) ok = wait_epoch(D.bdone + (size_t)par * M + m, epoch, D.err, D.wait_limit);
                 ok = __shfl_sync(FULL, ok, 0);

@@ -8,6 +8,12 @@
 - A non-finite parameter in one scenario: that scenario stops with status
   bit 2 (non-finite residual) where the oracle stops unconverged; the other
   scenarios are untouched and still match the oracle.
+- A singular reduced network matrix in one scenario: tripping the only line
+  of a bus without load or machine leaves its rows of S empty.  That
+  scenario's FP64 factorisation meets a zero pivot (status bit 4) where the
+  oracle's sparse LU fails; the other scenarios still match the oracle.
+  (The mixed solver may go on with factors kept from before the trip, which
+  are not singular, so it is not part of this check.)
 
 The reference is silent on both (src/batched.jl:459, src/numerics.jl:146-166).
 """
@@ -16,7 +22,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from helpers import DT, LY, run_oracle, synthetic_case
+from helpers import DT, LY, M, run_oracle, synthetic_case
 
 pytestmark = pytest.mark.gpu
 
@@ -96,3 +102,35 @@ def test_nan_parameter_stops_only_its_scenario(G, orc, solver):
     assert np.all(o["status"][good] == 0) and np.all(r["status"][good] == 0)
     err = np.max(np.abs(r["traj"][good] - o["traj"][good]) / np.maximum(1.0, np.abs(o["traj"][good])))
     assert err <= (1e-9 if solver == LY.SOLVER_SCHUR_FP64 else 1e-6)
+
+
+def _isolating_trip(ps):
+    """The branch of the first bus with one line and neither load nor
+    machine (tripping it isolates the bus)."""
+    deg = {}
+    for b in ps.branches:
+        deg[b.fr] = deg.get(b.fr, 0) + 1
+        deg[b.to] = deg.get(b.to, 0) + 1
+    busy = {l.bus for l in ps.loads} | {g.bus for g in ps.gens}
+    bus = next(b for b in range(ps.nbus) if deg.get(b, 0) == 1 and b not in busy)
+    return next(br for br in ps.branches if bus in (br.fr, br.to))
+
+
+def test_isolated_bus_zero_pivot_stops_only_its_scenario(G, orc):
+    c, w = synthetic_case("planar2k", 4)
+    per = [[], [M.trip_branch_event(_isolating_trip(c.ps), 0.05)], [], []]
+    gbl = G.GpuBatchedLayout(c.dp, c.ps, c.M)
+    try:
+        r = gbl.integrate(20 * DT, DT, scenario_faults=c.faults, solver=LY.SOLVER_SCHUR_FP64, scenario_trips=per)
+    finally:
+        gbl.close()
+    z, u, p = c.arrays()
+    fa, nf = c.fault_array(DT)
+    ta, nt = LY.trip_array(per, DT, ())
+    o = orc.integrate(c.PA, z, u, p, fa, nf, DT, 20, itermax=30, nthreads=4, trips=ta, n_trips=nt)
+    assert o["status"][1] != 0 and r["status"][1] & 4
+    good = [0, 2, 3]
+    assert np.all(o["status"][good] == 0) and np.all(r["status"][good] == 0)
+    assert np.array_equal(r["iters"][good], o["iters"][good])
+    err = np.max(np.abs(r["traj"][good] - o["traj"][good]) / np.maximum(1.0, np.abs(o["traj"][good])))
+    assert err <= 1e-9
