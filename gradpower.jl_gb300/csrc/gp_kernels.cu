@@ -76,18 +76,27 @@ __device__ __forceinline__ DevRef devref(const DTab &T, int k) {
     return d;
 }
 
+// The cluster's device table entries are read first, all together, so that
+// their round trips overlap instead of each device's starting after the
+// previous device's equations.
 template <class Sink, class KP = ComputeK>
 __device__ __forceinline__ void eval_cluster(const DevProblem &P, int c, const double *z, const double *u0,
                                              const double *p, Sink &sink, double Cc[6], double Ic[2],
                                              const KP &kc = KP(), bool exc_on = true) {
-    genrou_eval(devref(P.dev[0], P.cl_gen[c]), P.net, z, u0, p, sink, Cc, Ic, kc);
-    const int gt = P.cl_gov_type[c];
-    if (gt == 1) ieesgo_eval(devref(P.dev[1], P.cl_gov[c]), z, p, sink, kc);
-    else if (gt == 2) tgov1_eval(devref(P.dev[2], P.cl_gov[c]), z, p, sink, kc);
-    const int et = exc_on ? P.cl_exc_type[c] : -1;   // an offline exciter's states hold
-    if (et == 3) sexs_eval(devref(P.dev[3], P.cl_exc[c]), P.net, z, p, sink, kc);
-    else if (et == 4) esdc1a_eval(devref(P.dev[4], P.cl_exc[c]), P.net, z, p, sink, kc);
-    if (P.cl_pss[c] >= 0) ieeest_eval(devref(P.dev[5], P.cl_pss[c]), z, p, sink, kc);
+    const int gt = P.cl_gov_type[c], et0 = P.cl_exc_type[c], ip = P.cl_pss[c];
+    const int ig = P.cl_gen[c], igv = P.cl_gov[c], iex = P.cl_exc[c];
+    const int et = exc_on ? et0 : -1;   // an offline exciter's states hold
+    const DevRef dg = devref(P.dev[0], ig);
+    DevRef dgv{}, dex{}, dps{};
+    if (gt == 1 || gt == 2) dgv = devref(P.dev[gt], igv);
+    if (et == 3 || et == 4) dex = devref(P.dev[et], iex);
+    if (ip >= 0) dps = devref(P.dev[5], ip);
+    genrou_eval(dg, P.net, z, u0, p, sink, Cc, Ic, kc);
+    if (gt == 1) ieesgo_eval(dgv, z, p, sink, kc);
+    else if (gt == 2) tgov1_eval(dgv, z, p, sink, kc);
+    if (et == 3) sexs_eval(dex, P.net, z, p, sink, kc);
+    else if (et == 4) esdc1a_eval(dex, P.net, z, p, sink, kc);
+    if (ip >= 0) ieeest_eval(dps, z, p, sink, kc);
 }
 
 // Sink that drops every entry (the evaluation of the parameter constants).
@@ -185,13 +194,26 @@ __global__ void __launch_bounds__(32) cluster_kernel(DevProblem P, DevWork W, De
     const double dt = *W.dt;
     const int rb = Cl.rhs_base[cls];
     double *R0 = vals + (size_t)rb * 32, *R1 = R0 + (size_t)Wn * 32, *R2 = R1 + (size_t)Wn * 32;
-    // backward-Euler scaling
-    for (int q = q0; q < qm; q++) {
-        const CluOp o = ops[q];
-        double *vd = vals + o.d * 32 + lane;
-        if (o.code == OP_SCL) *vd *= -dt;
-        else if (o.code == OP_DIAG) *vd += 1.0;
-        else if (o.code == OP_BEF) *vd = act ? z[ws + o.a] - zold[ws + o.a] - dt * *vd : 0.0;
+    // backward-Euler scaling, eight ops and their state loads in flight
+    for (int q = q0; q < qm; q += 8) {
+        CluOp o[8];
+        double zn[8], zo[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) o[u] = ops[min(q + u, qm - 1)];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const bool ld = act && q + u < qm && o[u].code == OP_BEF;
+            zn[u] = ld ? z[ws + o[u].a] : 0.0;
+            zo[u] = ld ? zold[ws + o[u].a] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            if (q + u >= qm) break;
+            double *vd = vals + o[u].d * 32 + lane;
+            if (o[u].code == OP_SCL) *vd *= -dt;
+            else if (o[u].code == OP_DIAG) *vd += 1.0;
+            else if (o[u].code == OP_BEF) *vd = act ? zn[u] - zo[u] - dt * *vd : 0.0;
+        }
     }
     // residual norm (and the residual itself for the parity probe)
     const int *pc = Cl.perm_col + cls * 32;
@@ -336,12 +358,24 @@ __global__ void __launch_bounds__(32, 16) cluster_keep_kernel(DevProblem P, DevW
     const double dt = *W.dt;
     const CluOp *ops = Cl.ops;
     const int q0 = Cl.prog_ptr[cls], qm = Cl.prog_mid[cls], qs = Cl.prog_sol[cls], q1 = Cl.prog_ptr[cls + 1];
-    for (int q = q0; q < qm; q++) {
-        const CluOp o = ops[q];
-        if (o.code == OP_BEF) {
-            double *vd = R2 + (o.d - base) * 32 + lane;
-            *vd = act ? z[ws + o.a] - zold[ws + o.a] - dt * *vd : 0.0;
+    // backward-Euler rows, eight ops and their state loads in flight
+    for (int q = q0; q < qm; q += 8) {
+        CluOp o[8];
+        double zn[8], zo[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) o[u] = ops[min(q + u, qm - 1)];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const bool ld = act && q + u < qm && o[u].code == OP_BEF;
+            zn[u] = ld ? z[ws + o[u].a] : 0.0;
+            zo[u] = ld ? zold[ws + o[u].a] : 0.0;
         }
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            if (q + u < qm && o[u].code == OP_BEF) {
+                double *vd = R2 + (o[u].d - base) * 32 + lane;
+                *vd = act ? zn[u] - zo[u] - dt * *vd : 0.0;
+            }
     }
     unsigned long long nb = 0ull;
     for (int j = 0; j < Wn; j++) {
