@@ -507,6 +507,11 @@ struct HostBlk {
     std::vector<int> pcol_ptr{0}, pcol, pvs;
     std::vector<int4> ent0, ent1;
     int n_top_levels = 0, top_max_front = 1, top_max_xent = 1;
+    // the first n_lower_top entries of top_order (whole levels, each front
+    // of at most solve_block_front_limit() rows) are forward-solved by one
+    // warp per task, the rest (and the whole backward pass) by one CTA per
+    // task
+    int n_lower_top = 0;
     std::vector<int> top_order, top_rank;
     std::vector<int> top_xptr, top_xrow, top_xent;   // extend-add lists of the top region
     // solve-ordered factor copies: supernode s's L panel (mm x ns, leading
@@ -648,6 +653,19 @@ void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
                 B.top_order.push_back(s);
             }
     B.n_top_levels = ntl;
+    {
+        int lv = 0;   // the lower region: the levels below the first with a front too large for a warp
+        while (lv < ntl) {
+            bool fits_warp = true;
+            for (int s = 0; s < ns; s++)
+                if (tlev[s] == lv && sym.front_m(s) > kLimFront) fits_warp = false;
+            if (!fits_warp) break;
+            lv++;
+        }
+        B.n_lower_top = 0;
+        for (int s : B.top_order)
+            if (tlev[s] < lv) B.n_lower_top++;
+    }
     // solve-ordered factor copies: the blocks in the order they are claimed,
     // then the top supernodes
     B.lu_off.assign(ns, -1);
@@ -1138,6 +1156,7 @@ void build_blocks(gp_layout *L, const gp::Symbolic &sym) {
     B.pcol = A.upload(H.pcol);
     B.pvs = A.upload(H.pvs);
     B.n_top = (int)H.top_order.size();
+    B.n_lower_top = H.n_lower_top;
     B.top_max_front = H.top_max_front;
     B.top_max_xent = H.top_max_xent;
     B.top_order = A.upload(H.top_order);

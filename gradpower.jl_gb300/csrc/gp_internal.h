@@ -257,6 +257,7 @@ struct DevBlk {
     const int *pcol_ptr;         // [nblk+1]
     const int *pcol, *pvs;
     int n_top, top_max_front;
+    int n_lower_top;             // the first n_lower_top entries of top_order: one warp per forward task
     int top_max_xent;            // most extend-add entries of one top supernode
     const int *top_order;        // [n_top] top supernodes, children before parents
     const int *top_rank;         // [nsup] position in top_order, -1 inside a block

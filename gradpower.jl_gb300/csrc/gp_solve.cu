@@ -16,9 +16,13 @@
 //    memory (cp.async, all threads) and loads its own right-hand-side
 //    entries before it waits, bounded, on the tasks it depends on; one warp
 //    then sweeps the front from shared memory.
-// One persistent kernel per direction runs both: forward, the warps claim
-// the block tasks first and the CTAs then the top tasks; backward, the top
-// tasks first and then the block tasks.
+//  - in the forward pass the top region's first levels (fronts of at most
+//    kBlkFront rows) are tasks of one warp each, a supernode per task
+//    waiting on its children.
+// One persistent kernel per direction runs them all: forward, the warps
+// claim the block tasks, then the lower top tasks, and the CTAs then the
+// rest of the top region; backward, the CTAs claim the top tasks, then the
+// warps the block tasks.
 //
 // Hand-offs between tasks.  On FP64 factors a task signals a done flag
 // (release store after a barrier) and its dependants poll the flag, then
@@ -603,6 +607,86 @@ __device__ void bwd_block(const DevProblem &P, const DevWork &W, const DevSym &S
     }
 }
 
+// ---- lower top region, forward: one warp per task ---------------------------
+// In the forward pass the top supernodes of the first levels (fronts of at
+// most kBlkFront rows) are tasks of one warp each, like a block of one
+// supernode that waits on its children: through tagged words on FP32
+// factors, through done flags on FP64 factors.  The warp keeps the front's
+// vector in its shared-memory area and reads the factors through L1 (pulled
+// in before the waits).  (The backward pass keeps CTA tasks there: warp
+// tasks measured slower, 97.8 against 101.2 ms of solves per mixed run.)
+
+template <class T>
+__device__ void fwd_top_warp(const DevProblem &P, const DevWork &W, const DevSym &S, const DevBlk &B,
+                             const DevDag &D, const FrontSel &fs, int s, int rank, int m, int epoch, T *v) {
+    const int lane = threadIdx.x & 31;
+    const int start = S.sup_start[s], ns = S.sup_start[s + 1] - start;
+    const int r = S.row_ptr[s + 1] - S.row_ptr[s], mm = ns + r;
+    const T *L = lfac<T>(fs, S, m) + S.lu_off[s];
+    {
+        const uintptr_t l0 = (uintptr_t)L & ~(uintptr_t)127, l1 = (uintptr_t)(L + (size_t)mm * ns - 1);
+        for (uintptr_t ad = l0 + (uintptr_t)lane * 128; ad <= l1; ad += 32 * 128)
+            prefetch_l1(reinterpret_cast<const void *>(ad));
+    }
+    double *x = W.xperm + (size_t)m * P.n_red;
+    const int *xr = B.top_xrow + B.top_xptr[rank];
+    bool ok = true;
+    if constexpr (!Tagged<T>::value) {
+        // FP64 factors: the children's done flags, then their update vectors
+        const int c0 = S.child_ptr[s], nch = S.child_ptr[s + 1] - c0;
+        for (int q = lane; q < nch; q += 32)
+            ok = wait_epoch(D.xdone + (size_t)S.children[c0 + q] * P.M + m, epoch, D.err, D.wait_limit) && ok;
+        ok = __all_sync(FULL, ok);
+    }
+    const double *uv = S.uvec + (size_t)m * S.uvec_total;
+    const unsigned long long *ut = D.utag + (size_t)m * S.uvec_total;
+    // rows over lanes; each row sums its children's entries in child order
+    // (the CTA tasks' order), four loads in flight
+    for (int i = lane; i < mm; i += 32) {
+        T acc = i < ns ? (T)x[start + i] : T(0);
+        const int e1 = xr[i + 1];
+        for (int e = xr[i]; e < e1; e += 4) {
+            int off[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) off[u] = e + u < e1 ? B.top_xent[e + u] : 0;
+            if constexpr (Tagged<T>::value) {
+                unsigned long long w[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) w[u] = e + u < e1 ? ld_relaxed_u64(ut + off[u]) : 0ull;
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (e + u < e1) {
+                        if (!tag_ok(w[u], epoch)) w[u] = wait_tag(ut + off[u], epoch, D.err, D.wait_limit, ok);
+                        acc += tag_val(w[u]);
+                    }
+            } else {
+                double w[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) w[u] = e + u < e1 ? __ldcg(uv + off[u]) : 0.0;
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (e + u < e1) acc += (T)w[u];
+            }
+        }
+        v[i] = acc;
+    }
+    if (!__all_sync(FULL, ok) && lane == 0) atomicOr(W.status + m, 8);
+    __syncwarp();
+    const int *ip = S.ipiv + (size_t)(fs.shared ? 0 : m) * S.n + start;
+    fwd_front_blk<T>(L, [&](int i) { return ip[i]; }, ns, mm, v);
+    for (int i = lane; i < ns; i += 32) x[start + i] = (double)v[i];
+    if constexpr (Tagged<T>::value) {
+        unsigned long long *uo = D.utag + (size_t)m * S.uvec_total + S.uvec_off[s];
+        for (int i = lane; i < r; i += 32) st_relaxed_u64(uo + i, tag_f32(v[ns + i], epoch));
+    } else {
+        double *us = S.uvec + (size_t)m * S.uvec_total + S.uvec_off[s];
+        for (int i = lane; i < r; i += 32) us[i] = (double)v[ns + i];
+        __syncwarp();
+        if (lane == 0) signal_done(D.xdone + (size_t)s * P.M + m, epoch);
+    }
+    __syncwarp();
+}
+
 // ---- top region: dataflow of CTA tasks ------------------------------------
 
 // All threads of the CTA copy n consecutive factor entries into Fs.
@@ -784,15 +868,15 @@ __device__ void bwd_top_task(const DevProblem &P, const DevWork &W, const DevSym
 }
 
 // ---- the solves: one persistent kernel per direction ------------------------
-// Forward: the warps first claim block tasks (no waits); each block signals
-// its root's done flag.  Once every block task is claimed, the CTAs claim the
-// top-region tasks, which wait only on their own children (block roots or
-// top supernodes), so the top region starts as soon as the blocks below it
-// are done.  Backward: the CTAs first claim the top-region tasks (parents
-// first), then the warps claim block tasks, each waiting only on the top
-// supernode above its root.  A task only ever waits on tasks claimed before
-// it by running warps or CTAs, so the kernels cannot deadlock; every wait is
-// bounded.
+// Forward: the warps first claim block tasks (no waits); each block hands
+// its root's update vector on.  Once every block task is claimed, the warps
+// claim the lower top tasks (children first), and once those are claimed the
+// CTAs claim the rest of the top region; every task waits only on its own
+// children, so the top region starts as soon as the blocks below it are
+// done.  Backward: the CTAs first claim the top tasks (parents first), then
+// the warps the block tasks, each waiting only on the entries above it.  A task only ever waits on
+// tasks claimed before it by running warps or CTAs, so the kernels cannot
+// deadlock; every wait is bounded.
 
 // Mixed solves pair the scenarios in the block phase (two per warp); a pair
 // runs in the two half-warps when both scenarios are active and on FP32
@@ -859,19 +943,36 @@ __global__ void __launch_bounds__(kTopThreads, 8) fwd_solve_kernel(DevProblem P,
                 __syncwarp();
             }
         }
+        // the lower top region, one warp per task, children first
+        const long long n_lt = (long long)B.n_lower_top * M;
+        for (;;) {
+            long long t = 0;
+            if (lane == 0) t = atomicAdd(D.ctr + 6, 1);
+            t = __shfl_sync(FULL, t, 0);
+            if (t >= n_lt) break;
+            const int rank = (int)(t / M), m = (int)(t % M);
+            if (!W.active[m]) continue;
+            const bool d = use64(fs, m);
+            if (d && fs.fused64) continue;
+            const int s = B.top_order[rank];
+            if (d) fwd_top_warp<double>(P, W, S, B, D, fs, s, rank, m, epoch, reinterpret_cast<double *>(base + lay.v));
+            else fwd_top_warp<float>(P, W, S, B, D, fs, s, rank, m, epoch, reinterpret_cast<float *>(base + lay.v));
+        }
     }
-    const int n_tasks = B.n_top * M;
+    // the rest of the top region, one CTA per task
+    const int n_tasks = (B.n_top - B.n_lower_top) * M;
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) s_task = atomicAdd(D.ctr + 2, 1);
         __syncthreads();
         const int t = s_task;
         if (t >= n_tasks) break;
-        const int s = B.top_order[t / M], m = t % M;
+        const int rank = B.n_lower_top + t / M, m = t % M;
+        const int s = B.top_order[rank];
         if (!W.active[m]) continue;
         const bool d = use64(fs, m);
         if (d && fs.fused64) continue;
-        const TopCtx c = top_ctx(S, s, m, t / M);
+        const TopCtx c = top_ctx(S, s, m, rank);
         if (d) {
             fwd_top_task<double>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
             __syncthreads();
@@ -889,6 +990,7 @@ __global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P,
     const int lane = threadIdx.x & 31;
     const int M = P.M;
     const int epoch = *D.epoch;
+    // the top region, one CTA per task, parents first
     const int n_tasks = B.n_top * M;
     for (;;) {
         __syncthreads();
@@ -896,9 +998,10 @@ __global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P,
         __syncthreads();
         const int t = s_task;
         if (t >= n_tasks) break;
-        const int s = B.top_order[B.n_top - 1 - t / M], m = t % M;
+        const int rank = B.n_top - 1 - t / M, m = t % M;
+        const int s = B.top_order[rank];
         if (!W.active[m]) continue;
-        const TopCtx c = top_ctx(S, s, m, B.n_top - 1 - t / M);
+        const TopCtx c = top_ctx(S, s, m, rank);
         if (use64(fs, m)) {
             bwd_top_task<double>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
             __syncthreads();
@@ -907,10 +1010,10 @@ __global__ void __launch_bounds__(kTopThreads, 8) bwd_solve_kernel(DevProblem P,
             bwd_top_task<float>(P, W, S, B, D, fs, c, epoch, smem, &s_ok);
         }
     }
-    const int MP = pair_mode(fs) ? (M + 1) / 2 : M;
-    const long long n_blk = (long long)B.nblk * MP;
     const BlkLayout lay = blk_layout(B);
     unsigned char *base = warp_area(smem, lay);
+    const int MP = pair_mode(fs) ? (M + 1) / 2 : M;
+    const long long n_blk = (long long)B.nblk * MP;
     for (;;) {
         long long t = 0;
         if (lane == 0) t = atomicAdd(D.ctr + 5, 1);
