@@ -712,8 +712,81 @@ void make_blocks(const gp::Symbolic &sym, HostBlk &B) {
 // keeps the reciprocal of each pivot and ipiv the composed row permutation
 // of each supernode (pivot row i = assembled row ipiv[start + i]), as on the
 // device.  Returns the number of zero pivots.
+// Host emulation of factor_part (gp_dag.cu) on an assembled front of mm
+// rows and ns pivots split in np parts (no right-hand side): each part's
+// columns in its own storage (gp::split_col / split_owned_below, every
+// mapping checked), each panel factored by its part and copied out, every
+// part applying the panel's interchanges, U rows and rank-nb update to its
+// own columns; the factored front goes back into F, the pivot rows to piv.
+void host_split_eliminate(double *F, int ns, int mm, int np, std::vector<int> &piv) {
+    const int nc = mm, B = gp::kSplitPanel;
+    std::vector<std::vector<double>> Fl(np);
+    std::vector<int> ncl(np);
+    int total = 0;
+    for (int part = 0; part < np; part++) {
+        ncl[part] = gp::split_owned_below(nc, part, np);
+        if (ncl[part] > gp::split_cols_cap(nc, np)) fail(GP_E_INTERNAL, "split front: part above its column bound");
+        Fl[part].assign((size_t)mm * ncl[part], 0.0);
+        for (int jl = 0; jl < ncl[part]; jl++) {
+            const int j = gp::split_col(jl, part, np);
+            if (j >= nc || gp::split_owner(j, np) != part || gp::split_owned_below(j, part, np) != jl)
+                fail(GP_E_INTERNAL, "split front: column map of part %d", part);
+            std::copy(F + (size_t)j * mm, F + (size_t)(j + 1) * mm, Fl[part].begin() + (size_t)jl * mm);
+        }
+        total += ncl[part];
+    }
+    if (total != nc) fail(GP_E_INTERNAL, "split front: %d of %d columns dealt", total, nc);
+    piv.assign(ns, 0);
+    std::vector<double> Pn((size_t)mm * B);
+    for (int kb = 0; kb < ns; kb += B) {
+        const int ke = std::min(ns, kb + B), nb = ke - kb, o = gp::split_owner(kb, np);
+        double *Fo = Fl[o].data() + (size_t)gp::split_owned_below(kb, o, np) * mm;
+        for (int k = kb; k < ke; k++) {
+            double *col = Fo + (size_t)(k - kb) * mm;
+            double best = -1.0;
+            int bi = k;
+            for (int i = k; i < ns; i++)
+                if (std::fabs(col[i]) > best) { best = std::fabs(col[i]); bi = i; }
+            piv[k] = bi;
+            if (bi != k)
+                for (int c = 0; c < nb; c++) std::swap(Fo[k + (size_t)c * mm], Fo[bi + (size_t)c * mm]);
+            const double inv = 1.0 / col[k];
+            for (int i = k + 1; i < mm; i++) col[i] *= inv;
+            col[k] = inv;
+            for (int c = k - kb + 1; c < nb; c++)
+                for (int i = k + 1; i < mm; i++) Fo[i + (size_t)c * mm] -= col[i] * Fo[k + (size_t)c * mm];
+        }
+        std::copy(Fo, Fo + (size_t)mm * nb, Pn.begin());
+        for (int part = 0; part < np; part++) {
+            double *Fp = Fl[part].data();
+            const int jlp = gp::split_owned_below(kb, part, np);
+            for (int jl = 0; jl < ncl[part]; jl++) {
+                if (part == o && jl >= jlp && jl < jlp + nb) continue;
+                for (int k = kb; k < ke; k++)
+                    if (piv[k] != k) std::swap(Fp[k + (size_t)jl * mm], Fp[piv[k] + (size_t)jl * mm]);
+            }
+            for (int jl = gp::split_owned_below(ke, part, np); jl < ncl[part]; jl++) {
+                double *cj = Fp + (size_t)jl * mm;
+                for (int q = 0; q < nb; q++)
+                    for (int p = q + 1; p < nb; p++) cj[kb + p] -= Pn[kb + p + (size_t)q * mm] * cj[kb + q];
+                for (int i = ke; i < mm; i++) {
+                    double acc = cj[i];
+                    for (int q = 0; q < nb; q++) acc -= Pn[i + (size_t)q * mm] * cj[kb + q];
+                    cj[i] = acc;
+                }
+            }
+        }
+    }
+    for (int part = 0; part < np; part++)
+        for (int jl = 0; jl < ncl[part]; jl++)
+            std::copy(Fl[part].begin() + (size_t)jl * mm, Fl[part].begin() + (size_t)(jl + 1) * mm,
+                      F + (size_t)gp::split_col(jl, part, np) * mm);
+}
+
+// split: parts per supernode (DagPlan::nparts); a front with more than one
+// is eliminated by host_split_eliminate.
 int host_factor(const Plan &pl, const std::vector<double> &svar, std::vector<double> &fronts, std::vector<int> &ipiv,
-                bool transpose = false) {
+                bool transpose = false, const std::vector<uint8_t> *split = nullptr) {
     const std::vector<int> &acp = transpose ? pl.t_acp : pl.acp, &acpos = transpose ? pl.t_acpos : pl.acpos;
     const std::vector<double> &acval = transpose ? pl.t_acval : pl.acval;
     const std::vector<int> &avp = transpose ? pl.t_avp : pl.avp, &avpos = transpose ? pl.t_avpos : pl.avpos;
@@ -739,6 +812,16 @@ int host_factor(const Plan &pl, const std::vector<double> &svar, std::vector<dou
             }
             std::vector<int> perm(ns);
             for (int i = 0; i < ns; i++) perm[i] = i;
+            if (split && (*split)[s] > 1) {
+                std::vector<int> pv;
+                host_split_eliminate(F, ns, mm, (*split)[s], pv);
+                for (int k = 0; k < ns; k++) {
+                    if (F[k + k * mm] == 0.0 || !std::isfinite(F[k + k * mm])) zero_pivots++;
+                    std::swap(perm[k], perm[pv[k]]);
+                }
+                for (int i = 0; i < ns; i++) ipiv[start + i] = perm[i];
+                continue;
+            }
             for (int k = 0; k < ns; k++) {
                 double best = -1.0;
                 int bi = k;
@@ -1001,32 +1084,82 @@ void host_block_solve(const gp::Symbolic &S, const HostBlk &B, const std::vector
 // Task order of the dataflow kernels: supernodes whose whole subtree has
 // fronts of at most dag_small_front() rows first (by level), then the rest
 // (by level).  Both parts list children before parents.
-void build_dag(gp_layout *L, const gp::Symbolic &sym) {
-    DeviceArena &A = L->arena;
+// The dataflow schedule (host side): the topological order of the
+// factorisation tasks (the small region, subtrees whose fronts have at most
+// dag_small_front() rows, by level; then the rest by level) and the split of
+// the tail's large FP64 fronts into parts.
+struct DagPlan {
+    std::vector<int> order, rank, submax;
+    int n_small = 0, max_big = 0, max_big_whole = 0;
+    int tail0 = 0;
+    std::vector<uint8_t> nparts;
+    std::vector<int> tail_units{0};
+    std::vector<int64_t> pb_off;
+    int64_t pb_total = 0;
+    int max_panels = 1, max_split_ns = 1, max_part_entries = 0, max_part_ints = 0;
+};
+
+void make_dag_plan(const gp::Symbolic &sym, DagPlan &dp) {
     const int ns = sym.nsup;
-    std::vector<int> submax(ns, 0);
+    dp.submax.assign(ns, 0);
     for (int l = 0; l < sym.nlevels; l++)
         for (int q = sym.level_ptr[l]; q < sym.level_ptr[l + 1]; q++) {
             const int s = sym.level_sups[q];
             int mx = sym.front_m(s);
-            for (int c = sym.child_ptr[s]; c < sym.child_ptr[s + 1]; c++) mx = std::max(mx, submax[sym.children[c]]);
-            submax[s] = mx;
+            for (int c = sym.child_ptr[s]; c < sym.child_ptr[s + 1]; c++) mx = std::max(mx, dp.submax[sym.children[c]]);
+            dp.submax[s] = mx;
         }
     const int lim = gp::dag_small_front();
-    std::vector<int> order, rank(ns);
-    int max_big = 0;
+    dp.order.clear();
+    dp.rank.assign(ns, 0);
     for (int pass = 0; pass < 2; pass++)
         for (int l = 0; l < sym.nlevels; l++)
             for (int q = sym.level_ptr[l]; q < sym.level_ptr[l + 1]; q++) {
                 const int s = sym.level_sups[q];
-                const bool small = submax[s] <= lim;
+                const bool small = dp.submax[s] <= lim;
                 if (small != (pass == 0)) continue;
-                rank[s] = (int)order.size();
-                order.push_back(s);
-                if (!small) max_big = std::max(max_big, sym.front_m(s));
+                dp.rank[s] = (int)dp.order.size();
+                dp.order.push_back(s);
+                if (!small) dp.max_big = std::max(dp.max_big, sym.front_m(s));
             }
-    int n_small = 0;
-    for (int s = 0; s < ns; s++) n_small += submax[s] <= lim;
+    dp.n_small = 0;
+    for (int s = 0; s < ns; s++) dp.n_small += dp.submax[s] <= lim;
+    // split fronts (FP64): in the last kSplitTail ranks of the order (the
+    // narrow top of the tree), a front of at least kSplitMin rows is factored
+    // by about one part per 24 columns, at most kMaxParts
+    constexpr int kSplitTail = gp::kSplitTailMax, kSplitMin = 48, kColsPerPart = 24;
+    dp.tail0 = std::max(dp.n_small, ns - kSplitTail);
+    dp.nparts.assign(ns, 1);
+    for (int r = dp.tail0; r < ns; r++) {
+        const int s = dp.order[r], mm = sym.front_m(s), n = sym.front_n(s);
+        const int np =
+            mm >= kSplitMin ? std::min(gp::kMaxParts, std::max(2, (mm + kColsPerPart) / kColsPerPart)) : 1;
+        dp.nparts[s] = (uint8_t)np;
+        dp.tail_units.push_back(dp.tail_units.back() + np);
+        dp.pb_off.push_back(dp.pb_total);
+        if (np > 1) {
+            const int npan = (n + gp::kSplitPanel - 1) / gp::kSplitPanel;
+            dp.pb_total += (int64_t)npan * mm * gp::kSplitPanel;
+            dp.max_panels = std::max(dp.max_panels, npan);
+            dp.max_split_ns = std::max(dp.max_split_ns, n);
+            // a part's columns: whole panels of the nc = mm + 1 columns (the
+            // FP64 right-hand side included), dealt in turn
+            dp.max_part_entries = std::max(dp.max_part_entries, mm * (gp::split_cols_cap(mm + 1, np) + gp::kSplitPanel));
+            dp.max_part_ints = std::max(dp.max_part_ints, 2 * mm);
+        }
+    }
+    for (int r = dp.n_small; r < ns; r++)
+        if (dp.nparts[dp.order[r]] == 1) dp.max_big_whole = std::max(dp.max_big_whole, sym.front_m(dp.order[r]));
+}
+
+void build_dag(gp_layout *L, const gp::Symbolic &sym) {
+    DeviceArena &A = L->arena;
+    const int ns = sym.nsup;
+    DagPlan dp;
+    make_dag_plan(sym, dp);
+    const std::vector<int> &order = dp.order, &rank = dp.rank, &submax = dp.submax;
+    const int lim = gp::dag_small_front();
+    const int n_small = dp.n_small;
     gp::DevDag &D = L->D;
     D.nsup = ns;
     D.n_small = n_small;
@@ -1034,46 +1167,20 @@ void build_dag(gp_layout *L, const gp::Symbolic &sym) {
     D.order = A.upload(order);
     D.rank = A.upload(rank);
     D.parent = A.upload(sym.parent);
-    // split fronts (FP64): in the last kSplitTail ranks of the order (the
-    // narrow top of the tree), a front of at least kSplitMin rows is factored
-    // by about one part per 24 columns, at most kMaxParts
     {
-        constexpr int kSplitTail = gp::kSplitTailMax, kSplitMin = 48, kColsPerPart = 24;
         const size_t M = L->M;
-        D.tail0 = std::max(n_small, ns - kSplitTail);
-        D.n_tail = ns - D.tail0;
-        std::vector<uint8_t> nparts(ns, 1);
-        std::vector<int> tail_units(1, 0);
-        std::vector<int64_t> pb_off;
-        int64_t pbt = 0;
-        for (int r = D.tail0; r < ns; r++) {
-            const int s = order[r], mm = sym.front_m(s), n = sym.front_n(s);
-            const int np = mm >= kSplitMin ? std::min(gp::kMaxParts, std::max(2, (mm + kColsPerPart) / kColsPerPart))
-                                           : 1;
-            nparts[s] = (uint8_t)np;
-            tail_units.push_back(tail_units.back() + np);
-            pb_off.push_back(pbt);
-            if (np > 1) {
-                const int npan = (n + gp::kSplitPanel - 1) / gp::kSplitPanel;
-                pbt += (int64_t)npan * mm * gp::kSplitPanel;
-                D.max_panels = std::max(D.max_panels, npan);
-                D.max_split_ns = std::max(D.max_split_ns, n);
-                // local columns of a part: whole panels of the nc = mm + 1
-                // columns (the FP64 right-hand side included), dealt in turn
-                const int per = gp::kSplitPanel * np;
-                const int ncl = (mm + 1 + per - 1) / per * gp::kSplitPanel;
-                D.max_part_entries = std::max(D.max_part_entries, mm * (ncl + gp::kSplitPanel));
-                D.max_part_ints = std::max(D.max_part_ints, 2 * mm);
-            }
-        }
-        D.max_big_whole = 0;
-        for (int r = n_small; r < ns; r++)
-            if (nparts[order[r]] == 1) D.max_big_whole = std::max(D.max_big_whole, sym.front_m(order[r]));
-        D.big_units = (D.tail0 - n_small) + tail_units.back();
-        D.nparts = A.upload(nparts);
-        D.tail_units = A.upload(tail_units);
-        D.pb_off = A.upload(pb_off);
-        D.pb_total = std::max<int64_t>(pbt, 1);
+        D.tail0 = dp.tail0;
+        D.n_tail = ns - dp.tail0;
+        D.big_units = (D.tail0 - n_small) + dp.tail_units.back();
+        D.max_panels = dp.max_panels;
+        D.max_split_ns = dp.max_split_ns;
+        D.max_part_entries = dp.max_part_entries;
+        D.max_part_ints = dp.max_part_ints;
+        D.max_big_whole = dp.max_big_whole;
+        D.nparts = A.upload(dp.nparts);
+        D.tail_units = A.upload(dp.tail_units);
+        D.pb_off = A.upload(dp.pb_off);
+        D.pb_total = std::max<int64_t>(dp.pb_total, 1);
         const size_t nt = std::max(1, D.n_tail);
         D.pdone = A.alloc<int>(nt * M * gp::kMaxParts);
         D.pflag = A.alloc<int>(nt * M * D.max_panels);
@@ -1082,7 +1189,7 @@ void build_dag(gp_layout *L, const gp::Symbolic &sym) {
         fill(L, D.pdone, 0, nt * M * gp::kMaxParts * sizeof(int));
         fill(L, D.pflag, 0, nt * M * D.max_panels * sizeof(int));
     }
-    D.max_big_front = max_big;
+    D.max_big_front = dp.max_big;
     // extend-add lists of the fronts the CTA kernel factors: per front entry
     // (and right-hand-side row) its children's contributions, in child order
     {
@@ -2401,6 +2508,20 @@ int32_t gp_reduced_selftest(const gp_problem *prob, const int32_t *s_rowptr, con
         xmax = std::max(xmax, std::fabs(xl[k]));
     }
     for (int k = 0; k < n; k++) x[pl.sym.perm[k]] = xp[k];
+    // the split fronts' elimination (factor_part, emulated) against the
+    // one-front one: the same operations in the same order, so the same bits
+    {
+        DagPlan dp;
+        make_dag_plan(pl.sym, dp);
+        std::vector<double> fs;
+        std::vector<int> ps;
+        host_factor(pl, svar, fs, ps, false, &dp.nparts);
+        double d = 0.0;
+        for (size_t i = 0; i < fs.size(); i++) d = std::max(d, std::fabs(fs[i] - fronts[i]));
+        for (int k = 0; k < n; k++)
+            if (ps[k] != ipiv[k]) d = std::max(d, 1.0);
+        out[11] = d;
+    }
     out[0] = mism;
     out[1] = zp;
     out[2] = (double)pl.sym.nnz_lu;

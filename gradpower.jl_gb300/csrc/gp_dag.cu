@@ -676,11 +676,6 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
 // least kMaxParts resident CTAs the kernel cannot deadlock.
 // Shared memory: the local columns (mm x ncl_cap), the panel read from
 // global memory (mm x kSplitPanel), the pivot rows and their composition.
-__host__ __device__ inline int part_cols_cap(int nc, int np) {
-    const int per = kSplitPanel * np;
-    return (nc + per - 1) / per * kSplitPanel;
-}
-
 template <class T, bool RHS>
 __device__ void factor_part(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, T *fronts,
                             T *lfac, T *ufac, int s, int m, int k, int part, int np, int epoch,
@@ -692,16 +687,11 @@ __device__ void factor_part(const DevProblem &P, const DevWork &W, const DevSym 
     const int ns = S.sup_start[s + 1] - start;
     const int mm = ns + S.row_ptr[s + 1] - S.row_ptr[s];
     const int nc = mm + (RHS ? 1 : 0);
-    const int per = B * np;
-    // the part's columns below column j (they come first in local order)
-    auto owned_below = [&](int j) {
-        const int full = j / per, rem = j - full * per;
-        return full * B + min(B, max(0, rem - part * B));
-    };
-    auto jof = [&](int jl) { return ((jl / B) * np + part) * B + jl % B; };
+    auto owned_below = [&](int j) { return split_owned_below(j, part, np); };
+    auto jof = [&](int jl) { return split_col(jl, part, np); };
     const int ncl = owned_below(nc);
     T *Fl = reinterpret_cast<T *>(smem);
-    T *Pn = Fl + (size_t)mm * part_cols_cap(nc, np);
+    T *Pn = Fl + (size_t)mm * split_cols_cap(nc, np);
     int *piv = reinterpret_cast<int *>(Pn + (size_t)mm * B);
     int *perm = piv + mm;
     T *fr = fronts + (size_t)m * S.front_total;
@@ -710,9 +700,9 @@ __device__ void factor_part(const DevProblem &P, const DevWork &W, const DevSym 
     // front position p = i + j * mm -> local entry, -1 when another part's
     auto local = [&](int p) {
         const int j = p / mm;
-        return ((j / B) % np != part) ? -1 : (p - j * mm) + ((j / per) * B + j % B) * mm;
+        return split_owner(j, np) != part ? -1 : (p - j * mm) + owned_below(j) * mm;
     };
-    const int jr = ((mm / B) % np == part) ? (mm / per) * B + mm % B : -1;   // local right-hand side
+    const int jr = split_owner(mm, np) == part ? owned_below(mm) : -1;   // local right-hand side
     // ---- assembly of the part's columns ----
     for (int e = tid; e < mm * ncl; e += nthr) Fl[e] = T(0);
     __syncthreads();

@@ -216,6 +216,24 @@ constexpr int kMaxParts = 8;
 constexpr int kSplitPanel = 8;
 constexpr int kSplitTailMax = 96;   // ranks of the tail
 
+// Column j of a front split in np parts belongs to part (j / kSplitPanel) %
+// np.  A part keeps its columns in increasing order: split_owned_below(j)
+// of them lie left of column j, and its local column jl is front column
+// split_col(jl).  split_cols_cap(nc, np) bounds a part's columns.
+__host__ __device__ inline int split_owner(int j, int np) { return (j / kSplitPanel) % np; }
+__host__ __device__ inline int split_owned_below(int j, int part, int np) {
+    const int per = kSplitPanel * np, full = j / per, rem = j - full * per;
+    const int t = rem - part * kSplitPanel;
+    return full * kSplitPanel + (t < 0 ? 0 : (t > kSplitPanel ? kSplitPanel : t));
+}
+__host__ __device__ inline int split_col(int jl, int part, int np) {
+    return ((jl / kSplitPanel) * np + part) * kSplitPanel + jl % kSplitPanel;
+}
+__host__ __device__ inline int split_cols_cap(int nc, int np) {
+    const int per = kSplitPanel * np;
+    return (nc + per - 1) / per * kSplitPanel;
+}
+
 struct DagGrid {
     int small = 0, big = 0;                  // resident blocks
     int small_bytes = 0, big_bytes = 0;      // dynamic shared memory

@@ -413,7 +413,10 @@ int32_t gp_residual_static(gp_layout *L, const double *zold, double dt, double *
  * supernodes in one block, out[8] max |S^T y - rhs| / max |y| for S^T
  * factored from the transposed assembly lists of the adjoint, out[9]
  * largest front of the top region (0 when every supernode is in a block),
- * out[10] most vector entries one block stages, out[11] zero.
+ * out[10] most vector entries one block stages, out[11] max |difference|
+ * between the factors with the large fronts near the root split over
+ * several CTAs (the FP64 factorisation's parts, emulated on the host) and
+ * without (0: the same bits).
  * No counterpart in the reference: a test hook for the analysis that
  * replaces cuDSS's. */
 int32_t gp_reduced_selftest(const gp_problem *prob, const int32_t *s_rowptr, const int32_t *s_colidx,

@@ -86,6 +86,8 @@ def test_reduced_factorisation_matches_scipy(lib, name):
     assert out[4] <= 1e-13 and out[5] >= 1
     # S^T from the transposed assembly lists (the adjoint's system)
     assert out[8] <= 1e-10
+    # the split-front elimination (parts emulated) gives the same bits
+    assert out[11] == 0.0
     xr = spla.spsolve(S.tocsc(), rhs)
     assert np.max(np.abs(x - xr)) <= 1e-12 * np.max(np.abs(xr))
 
