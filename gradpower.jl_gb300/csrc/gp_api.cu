@@ -1085,12 +1085,13 @@ void host_block_solve(const gp::Symbolic &S, const HostBlk &B, const std::vector
 // fronts of at most dag_small_front() rows first (by level), then the rest
 // (by level).  Both parts list children before parents.
 // The dataflow schedule (host side): the topological order of the
-// factorisation tasks (the small region, subtrees whose fronts have at most
-// dag_small_front() rows, by level; then the rest by level) and the split of
-// the tail's large FP64 fronts into parts.
+// factorisation tasks (the tiny region, subtrees whose fronts have at most
+// dag_tiny_front() rows, by level; the rest of the small region, at most
+// dag_small_front() rows; then the rest by level) and the split of the
+// tail's large FP64 fronts into parts.
 struct DagPlan {
     std::vector<int> order, rank, submax;
-    int n_small = 0, max_big = 0, max_big_whole = 0;
+    int n_tiny = 0, n_small = 0, max_big = 0, max_big_whole = 0;
     int tail0 = 0;
     std::vector<uint8_t> nparts;
     std::vector<int> tail_units{0};
@@ -1109,21 +1110,24 @@ void make_dag_plan(const gp::Symbolic &sym, DagPlan &dp) {
             for (int c = sym.child_ptr[s]; c < sym.child_ptr[s + 1]; c++) mx = std::max(mx, dp.submax[sym.children[c]]);
             dp.submax[s] = mx;
         }
-    const int lim = gp::dag_small_front();
+    const int lim = gp::dag_small_front(), tiny = gp::dag_tiny_front();
     dp.order.clear();
     dp.rank.assign(ns, 0);
-    for (int pass = 0; pass < 2; pass++)
+    auto region = [&](int s) { return dp.submax[s] <= tiny ? 0 : (dp.submax[s] <= lim ? 1 : 2); };
+    for (int pass = 0; pass < 3; pass++)
         for (int l = 0; l < sym.nlevels; l++)
             for (int q = sym.level_ptr[l]; q < sym.level_ptr[l + 1]; q++) {
                 const int s = sym.level_sups[q];
-                const bool small = dp.submax[s] <= lim;
-                if (small != (pass == 0)) continue;
+                if (region(s) != pass) continue;
                 dp.rank[s] = (int)dp.order.size();
                 dp.order.push_back(s);
-                if (!small) dp.max_big = std::max(dp.max_big, sym.front_m(s));
+                if (pass == 2) dp.max_big = std::max(dp.max_big, sym.front_m(s));
             }
-    dp.n_small = 0;
-    for (int s = 0; s < ns; s++) dp.n_small += dp.submax[s] <= lim;
+    dp.n_tiny = dp.n_small = 0;
+    for (int s = 0; s < ns; s++) {
+        dp.n_tiny += region(s) == 0;
+        dp.n_small += region(s) <= 1;
+    }
     // split fronts (FP64): in the last kSplitTail ranks of the order (the
     // narrow top of the tree), a front of at least kSplitMin rows is factored
     // by about one part per 24 columns, at most kMaxParts
@@ -1163,6 +1167,7 @@ void build_dag(gp_layout *L, const gp::Symbolic &sym) {
     gp::DevDag &D = L->D;
     D.nsup = ns;
     D.n_small = n_small;
+    D.n_tiny = dp.n_tiny;
     D.max_front = sym.max_front;
     D.order = A.upload(order);
     D.rank = A.upload(rank);
@@ -1641,7 +1646,10 @@ void mark(gp_layout *L, int i) {
 // own factors), and the update.
 int enqueue_solve(gp_layout *L, int variant, int *nfac_out) {
     const gp::DevDag &D = L->D;
+    // factorisation launches: FP32 the warp and CTA kernels; FP64 also the
+    // tiny region's warp launch
     const int nfac = (D.n_small > 0) + (D.nsup > D.n_small);
+    const int nfac64 = (D.n_tiny > 0) + (D.n_small > D.n_tiny) + (D.nsup > D.n_small);
     const gp::DevBlk &B = L->B;
     const int nsolve = (B.nblk + B.n_top) > 0;   // one fused kernel per direction
     int launches = 2, facs = 0;   // dag_begin, update
@@ -1664,8 +1672,8 @@ int enqueue_solve(gp_layout *L, int variant, int *nfac_out) {
         mark(L, 4);   // the FP64 factorisation includes the forward solve
         mark(L, 5);
         gp::launch_solve_bwd(L->P, L->W, L->S, B, D, L->SG, fs, L->st);
-        facs = nfac;
-        launches += nfac + nsolve;
+        facs = nfac64;
+        launches += nfac64 + nsolve;
     } else {
         const gp::FrontSel fs{L->Mx.lfac, L->Mx.ufac, L->S.lfac, L->S.ufac, L->Mx.refac, 1};
         if (variant & 1) {
@@ -1682,7 +1690,7 @@ int enqueue_solve(gp_layout *L, int variant, int *nfac_out) {
             }
             gp::launch_dag_factor<double>(L->P, L->W, L->S, D, L->G64, L->S.fronts, nullptr, L->S.ufac, L->Mx.refac,
                                           gp::MX_EXACT, L->st);
-            facs += nfac;
+            facs += nfac64;
         }
         mark(L, 4);
         gp::launch_solve_fwd(L->P, L->W, L->S, B, D, L->SG, fs, L->st);
@@ -1900,8 +1908,12 @@ void wb_prepare(gp_layout *L, double dt) {
            "woodbury column");
     }
     gp::launch_wb_setup(L->P, L->wb_W1, L->wb_W2, L->wb_Hinv, L->st);
-    L->launches += 14 + (L->D.n_small > 0) + (L->D.nsup > L->D.n_small);
-    L->factor_launches += (L->D.n_small > 0) + (L->D.nsup > L->D.n_small);
+    {
+        const gp::DevDag &D = L->D;
+        const int nfac64 = (D.n_tiny > 0) + (D.n_small > D.n_tiny) + (D.nsup > D.n_small);
+        L->launches += 14 + nfac64;
+        L->factor_launches += nfac64;
+    }
 }
 
 void ensure_graphs(gp_layout *L, double tol, int itermax, int solver) {

@@ -48,6 +48,14 @@ constexpr unsigned FULL = kFullMask;
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kSmallFront = 32;
+// FP64 factorisations run the subtrees whose fronts have at most
+// kTinyFront rows first, in a launch of their own with a smaller front
+// buffer per warp: twice the resident warps, where the 32-row buffers hold
+// an SM to 24 (factorisation 693 -> 670 ms per FP64 run).  FP32 ones keep
+// one launch: their 32-row buffers already allow 48 warps, and the launch
+// boundary would cost the overlap of the two regions (74 -> 81 ms per mixed
+// run).
+constexpr int kTinyFront = 20;
 // update-matrix entries a thread loads ahead in the extend-add: none in the
 // warp kernel, which runs at 40 registers a thread and many warps a SM
 template <class G>
@@ -936,38 +944,41 @@ __device__ void factor_part(const DevProblem &P, const DevWork &W, const DevSym 
 
 // Shared memory of the factorisation kernels: the front (with the
 // right-hand-side column) and 2 * front rows ints for the pivot indices and
-// their composed permutation, each part 16-byte aligned.
+// their composed permutation, each part 16-byte aligned; per warp of the
+// warp kernel, for fronts of at most cap rows.
 template <class T>
-__host__ __device__ constexpr int small_front_bytes() {
-    return (kSmallFront * (kSmallFront + 1) * (int)sizeof(T) + 15) & ~15;
+__host__ __device__ constexpr int warp_front_bytes(int cap) {
+    return (cap * (cap + 1) * (int)sizeof(T) + 15) & ~15;
 }
 template <class T>
-__host__ __device__ constexpr int small_warp_bytes() {
-    return small_front_bytes<T>() + 2 * kSmallFront * 4;
+__host__ __device__ constexpr int warp_area_bytes(int cap) {
+    return warp_front_bytes<T>(cap) + 2 * cap * 4;
 }
 template <class T>
 __host__ __device__ inline int big_front_bytes(int max_front) {
     return (max_front * (max_front + 1) * (int)sizeof(T) + 15) & ~15;
 }
 
+// Ranks [r0, r1) of the order, one warp per task, fronts of at most cap
+// rows; tasks claimed from counter ctr.
 template <class T, bool RHS>
 __global__ void __launch_bounds__(kThreads, 6) factor_small_kernel(DevProblem P, DevWork W, DevSym S, DevDag D,
                                                                 T *fronts, T *lfac, T *ufac, const uint8_t *mask,
-                                                                int want) {
+                                                                int want, int r0, int r1, int cap, int ctr) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned char *wbase = smem_raw + (size_t)warp * small_warp_bytes<T>();
+    unsigned char *wbase = smem_raw + (size_t)warp * warp_area_bytes<T>(cap);
     T *F = reinterpret_cast<T *>(wbase);
-    int *piv = reinterpret_cast<int *>(wbase + small_front_bytes<T>());
+    int *piv = reinterpret_cast<int *>(wbase + warp_front_bytes<T>(cap));
     const int M = P.M;
     const int epoch = *D.epoch;
-    const int n_tasks = D.n_small * M;
+    const int n_tasks = (r1 - r0) * M;
     for (;;) {
         int t = 0;
-        if (lane == 0) t = atomicAdd(D.ctr + 0, 1);
+        if (lane == 0) t = atomicAdd(D.ctr + ctr, 1);
         t = __shfl_sync(FULL, t, 0);
         if (t >= n_tasks) break;
-        const int s = D.order[t / M], m = t % M;
+        const int s = D.order[r0 + t / M], m = t % M;
         if (mask[m] != want) continue;
         if (!warp_wait_children(S, D, D.fdone, s, m, M, epoch, 0) && lane == 0) atomicOr(W.status + m, 8);
         factor_front<T, RHS>(P, W, S, fronts, lfac, ufac, s, m, F, piv, WarpGroup{});
@@ -1061,7 +1072,7 @@ struct FusedRhs<double> {
 };
 
 template <class T>
-int configure_one(DagGrid &g, int nsm, int small_bytes, int big_bytes) {
+int configure_one(DagGrid &g, int nsm, int tiny_bytes, int small_bytes, int big_bytes) {
     constexpr bool R = FusedRhs<T>::value;
     int occ = 0;
     if (cudaFuncSetAttribute(factor_small_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, small_bytes) !=
@@ -1070,6 +1081,10 @@ int configure_one(DagGrid &g, int nsm, int small_bytes, int big_bytes) {
             cudaSuccess || occ < 1)
         return -1;
     g.small = nsm * occ;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, factor_small_kernel<T, R>, kThreads, tiny_bytes) !=
+            cudaSuccess || occ < 1)
+        return -1;
+    g.tiny = nsm * occ;
     if (cudaFuncSetAttribute(factor_big_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, big_bytes) !=
             cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, factor_big_kernel<T, R>, kThreads, big_bytes) !=
@@ -1093,22 +1108,25 @@ int dag_configure(const DevDag &D, int fp32, DagGrid &g) {
     // FP32: every front of the CTA kernel whole; FP64: the fronts that are
     // not split whole, and the parts of the split ones
     const int mb = std::max(1, fp32 ? D.max_big_front : D.max_big_whole);
-    const int small_bytes = kWarps * (fp32 ? small_warp_bytes<float>() : small_warp_bytes<double>());
+    const int small_bytes = kWarps * (fp32 ? warp_area_bytes<float>(kSmallFront) : warp_area_bytes<double>(kSmallFront));
+    const int tiny_bytes = kWarps * (fp32 ? warp_area_bytes<float>(kTinyFront) : warp_area_bytes<double>(kTinyFront));
     const int whole = (fp32 ? big_front_bytes<float>(mb) : big_front_bytes<double>(mb)) + 2 * mb * 4;
     const int part = fp32 ? 0 : ((D.max_part_entries * 8 + 15) & ~15) + D.max_part_ints * 4;
     const int big_bytes = std::max(whole, part);
-    const int rc = fp32 ? configure_one<float>(g, nsm, small_bytes, big_bytes)
-                        : configure_one<double>(g, nsm, small_bytes, big_bytes);
+    const int rc = fp32 ? configure_one<float>(g, nsm, tiny_bytes, small_bytes, big_bytes)
+                        : configure_one<double>(g, nsm, tiny_bytes, small_bytes, big_bytes);
     if (rc != 0) {
         cudaGetLastError();
         return -1;
     }
+    g.tiny_bytes = tiny_bytes;
     g.small_bytes = small_bytes;
     g.big_bytes = big_bytes;
     return 0;
 }
 
 int dag_small_front() { return kSmallFront; }
+int dag_tiny_front() { return kTinyFront; }
 
 void launch_dag_begin(const DevDag &D, cudaStream_t st) { dag_begin_kernel<<<1, 32, 0, st>>>(D); }
 
@@ -1116,11 +1134,15 @@ template <class T>
 void launch_dag_factor(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, const DagGrid &g,
                        T *fronts, T *lfac, T *ufac, const uint8_t *mask, int want, cudaStream_t st) {
     constexpr bool R = FusedRhs<T>::value;
-    const long long ts = (long long)D.n_small * P.M,
+    const int n_tiny = sizeof(T) == 8 ? D.n_tiny : 0;
+    const long long tt = (long long)n_tiny * P.M, ts = (long long)(D.n_small - n_tiny) * P.M,
                     tb = (long long)(sizeof(T) == 8 ? D.big_units : D.nsup - D.n_small) * P.M;
+    if (tt > 0)
+        factor_small_kernel<T, R><<<blocks_for(g.tiny, tt, kWarps), kThreads, g.tiny_bytes, st>>>(
+            P, W, S, D, fronts, lfac, ufac, mask, want, 0, n_tiny, kTinyFront, 7);
     if (ts > 0)
         factor_small_kernel<T, R><<<blocks_for(g.small, ts, kWarps), kThreads, g.small_bytes, st>>>(
-            P, W, S, D, fronts, lfac, ufac, mask, want);
+            P, W, S, D, fronts, lfac, ufac, mask, want, n_tiny, D.n_small, kSmallFront, 0);
     if (tb > 0)
         factor_big_kernel<T, R><<<blocks_for(g.big, tb, 1), kThreads, g.big_bytes, st>>>(P, W, S, D, fronts, lfac,
                                                                                           ufac, mask, want);

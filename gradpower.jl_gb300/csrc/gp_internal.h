@@ -172,13 +172,14 @@ struct DevMixed {
 // order of the assembly tree.
 struct DevDag {
     int nsup, n_small;
+    int n_tiny;                   // the first n_tiny ranks: subtrees with fronts of at most dag_tiny_front() rows
     int max_front, max_big_front;
     int max_big_whole;            // largest front of the CTA kernel that is not split (FP64)
     const int *order;       // [nsup]
     const int *rank;        // [nsup] position in order
     const int *parent;      // [nsup] parent supernode or -1
     int *ctr;               // [8] claim counters: small factor, big factor, forward top, backward top,
-                            //     forward blocks, backward blocks
+                            //     forward blocks, backward blocks, forward lower top, tiny factor
     int *epoch;             // [1] current solve
     int *err;               // [1] a wait gave up (sticky until the host clears it)
     int *fdone, *xdone, *bdone;   // [nsup][M] epoch at which the task finished
@@ -235,14 +236,15 @@ __host__ __device__ inline int split_cols_cap(int nc, int np) {
 }
 
 struct DagGrid {
-    int small = 0, big = 0;                  // resident blocks
-    int small_bytes = 0, big_bytes = 0;      // dynamic shared memory
+    int tiny = 0, small = 0, big = 0;                    // resident blocks
+    int tiny_bytes = 0, small_bytes = 0, big_bytes = 0;  // dynamic shared memory
 };
 
 int dag_configure(const DevDag &D, int fp32, DagGrid &g);
 // launch_dag_factor<double> also does the forward solve (the right-hand side
 // rides along as an extra front column); launch_dag_factor<float> does not.
 int dag_small_front();
+int dag_tiny_front();
 void launch_dag_begin(const DevDag &D, cudaStream_t st);
 // Factors the scenarios m with mask[m] == want: fronts (update matrices) and
 // the solve-ordered copies lfac, ufac ([M][lu_total]); lfac may be null when
