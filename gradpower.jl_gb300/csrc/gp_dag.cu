@@ -417,9 +417,9 @@ __device__ void eliminate_cta(T *F, int mm, int ns, int nc, int *piv, int *statu
 //    xperm plus the children's update vectors), so that the elimination is
 //    also the forward solve.  It leaves the forward-solved entries in xperm
 //    and this supernode's update vector in uvec.
-template <class T, bool RHS, class G>
+template <class T, bool RHS, class G, class Wait, class Done>
 __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym &S, T *fronts, T *lfac, T *ufac,
-                             int s, int m, T *F, int *piv, G g) {
+                             int s, int m, T *F, int *piv, G g, Wait wait, Done done) {
     const int start = S.sup_start[s];
     const int ns = S.sup_start[s + 1] - start;
     const int mm = ns + S.row_ptr[s + 1] - S.row_ptr[s];
@@ -443,17 +443,22 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
             if (P.tr_on[t] && t >= P.tr_ptr[m] && t < P.tr_ptr[m + 1]) F[S.asmt_pos[e]] += (T)S.asmt_val[e];
         }
     g.sync();
+    // the entries above need nothing from the children: only now wait for
+    // them (bounded; wait() ends with a barrier of the group)
+    wait();
     if (G::size > 32 && S.pa_base && S.pa_base[s] >= 0) {
         // CTA fronts: every entry sums its children's contributions (host
-        // lists, child order) without a barrier between children; four
-        // entries a thread per round, their loads issued together
+        // lists, child order) without a barrier between children; kPa
+        // entries a thread per round, their loads issued together (the
+        // round trips to L2 of a round overlap)
         const int *pp = S.pa_ptr + S.pa_base[s];
         const int n2 = mm * mm;
-        for (int p0 = idx; p0 < n2; p0 += 4 * step) {
-            T acc[4];
-            int e0[4], e1[4], kmax = 0;
+        constexpr int kPa = 8;
+        for (int p0 = idx; p0 < n2; p0 += kPa * step) {
+            T acc[kPa];
+            int e0[kPa], e1[kPa], kmax = 0;
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
+            for (int u = 0; u < kPa; u++) {
                 const int p = p0 + u * step;
                 e0[u] = p < n2 ? pp[p] : 0;
                 e1[u] = p < n2 ? pp[p + 1] : 0;
@@ -462,10 +467,10 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
             }
             for (int k = 0; k < kmax; k++)
 #pragma unroll
-                for (int u = 0; u < 4; u++)
+                for (int u = 0; u < kPa; u++)
                     if (e0[u] + k < e1[u]) acc[u] += ldcg(fr + S.pa_src[e0[u] + k]);
 #pragma unroll
-            for (int u = 0; u < 4; u++)
+            for (int u = 0; u < kPa; u++)
                 if (p0 + u * step < n2) F[p0 + u * step] = acc[u];
         }
         if (RHS) {
@@ -631,15 +636,26 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
             perm[p] = t;
         }
     }
-    // the columns ns..mm-1 (their rows ns..mm-1 are the update matrix the
-    // parent's assembly reads) as one contiguous range, and the
-    // solve-ordered copies of the factors: the L panel (columns 0..ns-1,
-    // contiguous as in F; skipped when lfac is null) and the U rows (rows
-    // 0..ns-1, leading dimension ns; the 2D index advances by the stride,
-    // one division per thread)
+    // first what the parent's assembly reads: the columns ns..mm-1 (their
+    // rows ns..mm-1 are the update matrix) as one contiguous range and, with
+    // RHS, the update vector (and the forward-solved entries); then done(),
+    // and only after it the solve-ordered copies of the factors, which
+    // nothing reads before the solves: the L panel (columns 0..ns-1,
+    // contiguous as in F; skipped when lfac is null), the U rows (rows
+    // 0..ns-1, leading dimension ns; the 2D index advances by the stride, one
+    // division per thread) and the composed pivots
     {
         T *out = fr + S.front_off[s];
         for (int i = ns * mm + idx; i < mm * mm; i += step) out[i] = F[i];
+    }
+    if (RHS) {
+        for (int i = idx; i < ns; i += step) x[start + i] = (double)F[mm * mm + i];
+        double *us = uv + S.uvec_off[s];
+        for (int a = idx; a < mm - ns; a += step) us[a] = (double)F[mm * mm + ns + a];
+    }
+    g.sync();
+    done();
+    {
         if (lfac) {
             T *lo = lfac + (size_t)m * S.lu_total + S.lu_off[s];
             for (int i = idx; i < mm * ns; i += step) lo[i] = F[i];
@@ -654,14 +670,8 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
             if (i >= ns) { i -= ns; c++; }
         }
     }
-    g.sync();
     int *ipiv = S.ipiv + (size_t)m * S.n + start;
     for (int i = idx; i < ns; i += step) ipiv[i] = piv[ns + i];
-    if (RHS) {
-        for (int i = idx; i < ns; i += step) x[start + i] = (double)F[mm * mm + i];
-        double *us = uv + S.uvec_off[s];
-        for (int a = idx; a < mm - ns; a += step) us[a] = (double)F[mm * mm + ns + a];
-    }
     g.sync();
 }
 
@@ -684,10 +694,10 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
 // least kMaxParts resident CTAs the kernel cannot deadlock.
 // Shared memory: the local columns (mm x ncl_cap), the panel read from
 // global memory (mm x kSplitPanel), the pivot rows and their composition.
-template <class T, bool RHS>
+template <class T, bool RHS, class Wait, class Done>
 __device__ void factor_part(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, T *fronts,
                             T *lfac, T *ufac, int s, int m, int k, int part, int np, int epoch,
-                            unsigned char *smem) {
+                            unsigned char *smem, Wait wait, Done done) {
     constexpr int B = kSplitPanel;
     using K = typename KeyOf<T>::type;
     const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
@@ -735,6 +745,7 @@ __device__ void factor_part(const DevProblem &P, const DevWork &W, const DevSym 
             }
         }
     __syncthreads();
+    wait();
     {
         // the children's update matrices, entry by entry from the host lists
         // (child order), four entries a thread with their loads together
@@ -906,24 +917,31 @@ __device__ void factor_part(const DevProblem &P, const DevWork &W, const DevSym 
         }
         __syncthreads();
     }
-    // ---- store: columns ns..mm-1 whole (the update matrix for the parent),
-    // the L panel columns and the U rows of the part's columns ----
+    // ---- store: first what the parent reads (columns ns..mm-1 whole, the
+    // update matrix, and the part's share of the right-hand side), then
+    // done(), then the L panel columns and the U rows of the part's columns
+    // and the composed pivots, which nothing reads before the solves ----
     {
         T *out = fr + S.front_off[s];
+        for (int e = tid; e < mm * ncl; e += nthr) {
+            const int jl = e / mm, i = e - jl * mm, j = jof(jl);
+            if (j >= ns && j < mm) out[i + (size_t)j * mm] = Fl[e];
+        }
+        if (RHS && jr >= 0) {
+            for (int i = tid; i < ns; i += nthr) x[start + i] = (double)Fl[i + jr * mm];
+            double *us = uv + S.uvec_off[s];
+            for (int a = tid; a < mm - ns; a += nthr) us[a] = (double)Fl[ns + a + jr * mm];
+        }
+        __syncthreads();
+        done();
         T *lo = lfac ? lfac + (size_t)m * S.lu_total + S.lu_off[s] : nullptr;
         T *uo = ufac + (size_t)m * S.lu_total + S.lu_off[s];
         for (int e = tid; e < mm * ncl; e += nthr) {
             const int jl = e / mm, i = e - jl * mm, j = jof(jl);
             if (j >= mm) continue;
             const T v = Fl[e];
-            if (j >= ns) out[i + (size_t)j * mm] = v;
-            else if (lo) lo[i + (size_t)j * mm] = v;
+            if (j < ns && lo) lo[i + (size_t)j * mm] = v;
             if (i < ns) uo[i + (size_t)j * ns] = v;
-        }
-        if (RHS && jr >= 0) {
-            for (int i = tid; i < ns; i += nthr) x[start + i] = (double)Fl[i + jr * mm];
-            double *us = uv + S.uvec_off[s];
-            for (int a = tid; a < mm - ns; a += nthr) us[a] = (double)Fl[ns + a + jr * mm];
         }
         if (part == 0) {
             if (tid == 0) {
@@ -980,9 +998,14 @@ __global__ void __launch_bounds__(kThreads, 6) factor_small_kernel(DevProblem P,
         if (t >= n_tasks) break;
         const int s = D.order[r0 + t / M], m = t % M;
         if (mask[m] != want) continue;
-        if (!warp_wait_children(S, D, D.fdone, s, m, M, epoch, 0) && lane == 0) atomicOr(W.status + m, 8);
-        factor_front<T, RHS>(P, W, S, fronts, lfac, ufac, s, m, F, piv, WarpGroup{});
-        if (lane == 0) signal_done(D.fdone + (size_t)s * M + m, epoch);
+        factor_front<T, RHS>(
+            P, W, S, fronts, lfac, ufac, s, m, F, piv, WarpGroup{},
+            [&] {
+                if (!warp_wait_children(S, D, D.fdone, s, m, M, epoch, 0) && lane == 0) atomicOr(W.status + m, 8);
+            },
+            [&] {
+                if (lane == 0) signal_done(D.fdone + (size_t)s * M + m, epoch);
+            });
     }
 }
 
@@ -1035,19 +1058,25 @@ __global__ void __launch_bounds__(kThreads, 3) factor_big_kernel(DevProblem P, D
         }
         const int s = D.order[rank];
         if (mask[m] != want) continue;
-        if (tid < 32) {
-            const bool ok = warp_wait_children(S, D, D.fdone, s, m, M, epoch, D.n_small, kSplit);
-            if (lane == 0) s_ok = ok;
-        }
-        __syncthreads();
-        if (!s_ok && tid == 0) atomicOr(W.status + m, 8);
+        // the children (bounded wait), called by the assembly once the
+        // entries that need nothing from them are in place
+        auto wait = [&] {
+            if (tid < 32) {
+                const bool ok = warp_wait_children(S, D, D.fdone, s, m, M, epoch, D.n_small, kSplit);
+                if (lane == 0) s_ok = ok;
+            }
+            __syncthreads();
+            if (!s_ok && tid == 0) atomicOr(W.status + m, 8);
+        };
         if (np == 1) {
-            factor_front<T, RHS>(P, W, S, fronts, lfac, ufac, s, m, F, piv, BlockGroup{});
-            if (tid == 0) signal_done(D.fdone + (size_t)s * M + m, epoch);
+            factor_front<T, RHS>(P, W, S, fronts, lfac, ufac, s, m, F, piv, BlockGroup{}, wait, [&] {
+                if (tid == 0) signal_done(D.fdone + (size_t)s * M + m, epoch);
+            });
         } else if constexpr (kSplit) {
             const int k = rank - D.tail0;
-            factor_part<T, RHS>(P, W, S, D, fronts, lfac, ufac, s, m, k, part, np, epoch, smem_raw);
-            if (tid == 0) signal_done(D.pdone + ((size_t)k * M + m) * kMaxParts + part, epoch);
+            factor_part<T, RHS>(P, W, S, D, fronts, lfac, ufac, s, m, k, part, np, epoch, smem_raw, wait, [&] {
+                if (tid == 0) signal_done(D.pdone + ((size_t)k * M + m) * kMaxParts + part, epoch);
+            });
         }
     }
 }
