@@ -292,6 +292,18 @@ __device__ void panel_warp(T *F, int mm, int ns, int kb, int ke, int *piv, int *
     __syncwarp();
 }
 
+// The register panel for rows kb..mm-1 (at most 32 * kPanelRows of them).
+template <class T>
+__device__ __forceinline__ void panel_regs(T *F, int mm, int ns, int kb, int ke, int *piv, int *status) {
+    switch ((mm - kb + 31) >> 5) {
+    case 1: panel_warp<T, 1>(F, mm, ns, kb, ke, piv, status); break;
+    case 2: panel_warp<T, 2>(F, mm, ns, kb, ke, piv, status); break;
+    case 3: panel_warp<T, 3>(F, mm, ns, kb, ke, piv, status); break;
+    case 4: panel_warp<T, 4>(F, mm, ns, kb, ke, piv, status); break;
+    default: panel_warp<T, 5>(F, mm, ns, kb, ke, piv, status); break;
+    }
+}
+
 template <class T>
 __device__ void eliminate_cta(T *F, int mm, int ns, int nc, int *piv, int *status) {
     constexpr int NP = PanelOf<T>::cols;
@@ -300,15 +312,7 @@ __device__ void eliminate_cta(T *F, int mm, int ns, int nc, int *piv, int *statu
         const int ke = min(ns, kb + NP), nb = ke - kb;
         // ---- (a) the panel ----
         if (mm - kb <= 32 * kPanelRows) {
-            if (warp == 0) {
-                switch ((mm - kb + 31) >> 5) {
-                case 1: panel_warp<T, 1>(F, mm, ns, kb, ke, piv, status); break;
-                case 2: panel_warp<T, 2>(F, mm, ns, kb, ke, piv, status); break;
-                case 3: panel_warp<T, 3>(F, mm, ns, kb, ke, piv, status); break;
-                case 4: panel_warp<T, 4>(F, mm, ns, kb, ke, piv, status); break;
-                default: panel_warp<T, 5>(F, mm, ns, kb, ke, piv, status); break;
-                }
-            }
+            if (warp == 0) panel_regs<T>(F, mm, ns, kb, ke, piv, status);
             __syncthreads();
         } else
         for (int k = kb; k < ke; k++) {
@@ -370,10 +374,10 @@ __device__ void eliminate_cta(T *F, int mm, int ns, int nc, int *piv, int *statu
         }
         __syncthreads();
         // ---- (d) trailing update, rows ke..mm-1, columns ke..nc-1 ----
-        // (rows in chunks of 160: five per lane)
-        const int nq = (nc - ke + 3) >> 2, nr = (mm - ke + 159) / 160;
-        for (int t = warp; t < nq * nr; t += nwarp) {
-            const int c0 = ke + 4 * (t % nq), r0 = ke + 160 * (t / nq);
+        // (tiles of four columns and up to 160 rows, five per lane; a
+        // look-ahead, warp 0 factoring the next panel while the other warps
+        // update, measured no faster: the update keeps the SM busy)
+        auto tile = [&](int c0, int r0) {
             T acc[5][4];
 #pragma unroll
             for (int q = 0; q < 5; q++) {
@@ -381,7 +385,10 @@ __device__ void eliminate_cta(T *F, int mm, int ns, int nc, int *piv, int *statu
 #pragma unroll
                 for (int c = 0; c < 4; c++) acc[q][c] = (i < mm && c0 + c < nc) ? F[i + (c0 + c) * mm] : T(0);
             }
-            for (int k = kb; k < ke; k++) {
+#pragma unroll
+            for (int kk = 0; kk < NP; kk++) {
+                const int k = kb + kk;
+                if (k >= ke) break;
                 T u[4], l[5];
 #pragma unroll
                 for (int c = 0; c < 4; c++) u[c] = c0 + c < nc ? F[k + (c0 + c) * mm] : T(0);
@@ -402,7 +409,9 @@ __device__ void eliminate_cta(T *F, int mm, int ns, int nc, int *piv, int *statu
                 for (int c = 0; c < 4; c++)
                     if (i < mm && c0 + c < nc) F[i + (c0 + c) * mm] = acc[q][c];
             }
-        }
+        };
+        const int nq = (nc - ke + 3) >> 2, nr = (mm - ke + 159) / 160;
+        for (int t = warp; t < nq * nr; t += nwarp) tile(ke + 4 * (t % nq), ke + 160 * (t / nq));
         __syncthreads();
     }
 }
