@@ -2440,6 +2440,31 @@ int32_t gp_integrate(gp_layout *L, const gp_options *opt, int32_t n_faults, cons
     API_END
 }
 
+int32_t gp_recip_check(int32_t n, const double *x, double *r) {
+    API_BEGIN
+    if (n < 0 || (n > 0 && (!x || !r))) fail(GP_E_INVALID, "bad arguments");
+    if (n == 0) return GP_OK;
+    // the buffers and the stream go on every path out
+    struct Scope {
+        DeviceArena A;
+        cudaStream_t st = nullptr;
+        ~Scope() {
+            if (st) cudaStreamSynchronize(st);
+            A.release();
+            if (st) cudaStreamDestroy(st);
+        }
+    } sc;
+    ck(cudaStreamCreateWithFlags(&sc.st, cudaStreamNonBlocking), "cudaStreamCreate");
+    sc.A.st = sc.st;
+    const double *dx = sc.A.upload(x, (size_t)n);
+    double *dr = sc.A.alloc<double>((size_t)n);
+    gp::launch_recip_check(dx, dr, n, sc.st);
+    ck(cudaGetLastError(), "recip check launch");
+    ck(cudaMemcpyAsync(r, dr, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, sc.st), "cudaMemcpyAsync");
+    ck(cudaStreamSynchronize(sc.st), "recip check");
+    API_END
+}
+
 int32_t gp_cluster_selftest(const gp_problem *prob, const double *z, const double *zold, const double *u0,
                             const double *p, double dt, double *yx, double *clout, double *f, double out[4]) {
     API_BEGIN

@@ -13,7 +13,10 @@
 // D.wait_limit polls it raises the error flag, every other wait then returns
 // at once, and the kernel finishes with the scenario marked in `status`.
 //
-// Factorisation, in two launches:
+// Factorisation, in two launches (three for FP64):
+//  - factor_pair_kernel (FP64 only): supernodes whose whole subtree has
+//    fronts of at most kTinyFront rows, two scenarios a warp (a half-warp
+//    per front);
 //  - factor_small_kernel: supernodes whose whole subtree has fronts of at
 //    most 32 rows, one warp per task, the front in shared memory;
 //  - factor_big_kernel: the rest, one CTA per task.
@@ -50,11 +53,11 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kSmallFront = 32;
 // FP64 factorisations run the subtrees whose fronts have at most
 // kTinyFront rows first, in a launch of their own with a smaller front
-// buffer per warp: twice the resident warps, where the 32-row buffers hold
-// an SM to 24 (factorisation 693 -> 670 ms per FP64 run).  FP32 ones keep
-// one launch: their 32-row buffers already allow 48 warps, and the launch
-// boundary would cost the overlap of the two regions (74 -> 81 ms per mixed
-// run).
+// buffer: more fronts in flight, where the 32-row buffers hold an SM to 24
+// (factorisation 693 -> 670 ms per FP64 run), and two fronts a warp
+// (factor_pair_kernel).  FP32 ones keep one launch: their 32-row buffers
+// already allow 48 warps, and the launch boundary would cost the overlap of
+// the two regions (74 -> 81 ms per mixed run).
 constexpr int kTinyFront = 20;
 // update-matrix entries a thread loads ahead in the extend-add: none in the
 // warp kernel, which runs at 40 registers a thread and many warps a SM
@@ -93,6 +96,22 @@ __device__ bool warp_wait_children(const DevSym &S, const DevDag &D, const int *
     return ok;
 }
 
+// The same for two scenarios a warp: each half-warp waits for the children
+// of supernode s in its own scenario m (the whole warp calls it); true when
+// every wait of the caller's half succeeded.
+__device__ bool half_wait_children(const DevSym &S, const DevDag &D, const int *done, int s, int m, int M,
+                                   int epoch) {
+    const int c0 = S.child_ptr[s], nc = S.child_ptr[s + 1] - c0;
+    bool ok = true;
+    for (int q = threadIdx.x & 15; q < nc; q += 16) {
+        const int c = S.children[c0 + q];
+        ok = wait_epoch(done + (size_t)c * M + m, epoch, D.err, D.wait_limit) && ok;
+    }
+    const unsigned bad = __ballot_sync(FULL, !ok);
+    __syncwarp();
+    return (bad & (0xffffu << (threadIdx.x & 16))) == 0;
+}
+
 // Magnitude of a factor entry as an unsigned key that orders like |v|
 // (sign bit cleared; NaN above +inf), so that pivot search and reductions
 // run on the integer pipes instead of the (scarce) FP64 pipe.
@@ -115,38 +134,59 @@ struct KeyOf<float> {
     using type = unsigned;
 };
 
-template <class T>
+// LW < 32: the warp is LW-lane segments, each searching its own front (the
+// whole warp calls it).
+template <class T, int LW = 32>
 __device__ __forceinline__ int warp_pivot(const T *F, int mm, int k, int ns, bool &zero) {
     using K = typename KeyOf<T>::type;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & (LW - 1);
     K bk = 0;
     int bi = k;
-    for (int i = k + lane; i < ns; i += 32) {
+    for (int i = k + lane; i < ns; i += LW) {
         const K v = (K)mag_key(F[i + k * mm]);
         if (v > bk) { bk = v; bi = i; }
     }
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        const K ok = __shfl_xor_sync(FULL, bk, off);
-        const int oi = __shfl_xor_sync(FULL, bi, off);
+    for (int off = LW / 2; off > 0; off >>= 1) {
+        const K ok = __shfl_xor_sync(FULL, bk, off, LW);
+        const int oi = __shfl_xor_sync(FULL, bi, off, LW);
         if (ok > bk || (ok == bk && oi < bi)) { bk = ok; bi = oi; }
     }
     zero = bk == 0;
     return bi;
 }
 
-// Thread groups that factor one front: a warp, or the whole CTA.
+// Thread groups that factor one front: a warp, the whole CTA, or half a
+// warp (two fronts a warp, each half on its own front of the same
+// supernode).  size: threads of the group; lanes: threads of the lead
+// segment that searches pivots and scales the multipliers; active(): false
+// for a half that only follows its partner (it computes the partner's front
+// and stores nothing).
 struct WarpGroup {
-    static constexpr int size = 32;
+    static constexpr int size = 32, lanes = 32;
     __device__ int idx() const { return threadIdx.x & 31; }
+    __device__ int lane() const { return threadIdx.x & 31; }
     __device__ bool lead_warp() const { return true; }
+    __device__ bool active() const { return true; }
     __device__ void sync() const { __syncwarp(); }
 };
 struct BlockGroup {
-    static constexpr int size = kThreads;
+    static constexpr int size = kThreads, lanes = 32;
     __device__ int idx() const { return threadIdx.x; }
+    __device__ int lane() const { return threadIdx.x & 31; }
     __device__ bool lead_warp() const { return threadIdx.x < 32; }
+    __device__ bool active() const { return true; }
     __device__ void sync() const { __syncthreads(); }
+};
+struct HalfGroup {
+    static constexpr int size = 16, lanes = 16;
+    bool act;
+    __device__ int idx() const { return threadIdx.x & 15; }
+    __device__ int lane() const { return threadIdx.x & 15; }
+    __device__ bool lead_warp() const { return true; }
+    __device__ bool active() const { return act; }
+    // both halves run the same supernode, so they meet every barrier
+    __device__ void sync() const { __syncwarp(); }
 };
 
 // Columns per panel of the blocked elimination of CTA-sized fronts.
@@ -256,7 +296,7 @@ __device__ void panel_warp(T *F, int mm, int ns, int kb, int ke, int *piv, int *
             u[q] = __shfl_sync(FULL, slot(col, jp), lp);
             w[q] = __shfl_sync(FULL, slot(col, jk), lk);
         }
-        const T inv = T(1) / u[c];
+        const T inv = recip(u[c]);
 #pragma unroll
         for (int j = 0; j < J; j++) {
             const int i = kb + lane + 32 * j;
@@ -329,7 +369,7 @@ __device__ void eliminate_cta(T *F, int mm, int ns, int nc, int *piv, int *statu
                     F[pv + (kb + lane) * mm] = a;
                 }
                 __syncwarp();
-                const T inv = T(1) / F[k + k * mm];
+                const T inv = recip(F[k + k * mm]);
                 for (int i = k + 1 + lane; i < mm; i += 32) F[i + k * mm] *= inv;
                 __syncwarp();
                 if (lane == 0) F[k + k * mm] = inv;
@@ -550,22 +590,23 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
     } else {
     for (int k = 0; k < ns; k++) {
         if (g.lead_warp()) {
-            const int lane = threadIdx.x & 31;
+            constexpr int LW = G::lanes;
+            const int lane = g.lane();
             bool zero;
-            const int pv = warp_pivot(F, mm, k, ns, zero);
+            const int pv = warp_pivot<T, LW>(F, mm, k, ns, zero);
             if (lane == 0) {
                 piv[k] = pv;
-                if (zero) atomicOr(W.status + m, 4);
+                if (zero && g.active()) atomicOr(W.status + m, 4);
             }
             if (pv != k)
-                for (int j = lane; j < nc; j += 32) {
+                for (int j = lane; j < nc; j += LW) {
                     const T a = F[k + j * mm];
                     F[k + j * mm] = F[pv + j * mm];
                     F[pv + j * mm] = a;
                 }
             __syncwarp();
-            const T inv = T(1) / F[k + k * mm];
-            for (int i = k + 1 + lane; i < mm; i += 32) F[i + k * mm] *= inv;
+            const T inv = recip(F[k + k * mm]);
+            for (int i = k + 1 + lane; i < mm; i += LW) F[i + k * mm] *= inv;
             __syncwarp();
             if (lane == 0) F[k + k * mm] = inv;
         }
@@ -653,18 +694,19 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
     // contiguous as in F; skipped when lfac is null), the U rows (rows
     // 0..ns-1, leading dimension ns; the 2D index advances by the stride, one
     // division per thread) and the composed pivots
-    {
+    const bool act = g.active();
+    if (act) {
         T *out = fr + S.front_off[s];
         for (int i = ns * mm + idx; i < mm * mm; i += step) out[i] = F[i];
     }
-    if (RHS) {
+    if (RHS && act) {
         for (int i = idx; i < ns; i += step) x[start + i] = (double)F[mm * mm + i];
         double *us = uv + S.uvec_off[s];
         for (int a = idx; a < mm - ns; a += step) us[a] = (double)F[mm * mm + ns + a];
     }
     g.sync();
     done();
-    {
+    if (act) {
         if (lfac) {
             T *lo = lfac + (size_t)m * S.lu_total + S.lu_off[s];
             for (int i = idx; i < mm * ns; i += step) lo[i] = F[i];
@@ -679,8 +721,10 @@ __device__ void factor_front(const DevProblem &P, const DevWork &W, const DevSym
             if (i >= ns) { i -= ns; c++; }
         }
     }
-    int *ipiv = S.ipiv + (size_t)m * S.n + start;
-    for (int i = idx; i < ns; i += step) ipiv[i] = piv[ns + i];
+    if (act) {
+        int *ipiv = S.ipiv + (size_t)m * S.n + start;
+        for (int i = idx; i < ns; i += step) ipiv[i] = piv[ns + i];
+    }
     g.sync();
 }
 
@@ -831,7 +875,7 @@ __device__ void factor_part(const DevProblem &P, const DevWork &W, const DevSym 
                         Fp[bi + lane * mm] = a;
                     }
                     __syncwarp();
-                    const T inv = T(1) / col[kk];
+                    const T inv = recip(col[kk]);
                     for (int i = kk + 1 + lane; i < mm; i += 32) col[i] *= inv;
                     __syncwarp();
                     if (lane == 0) col[kk] = inv;
@@ -1018,6 +1062,50 @@ __global__ void __launch_bounds__(kThreads, 6) factor_small_kernel(DevProblem P,
     }
 }
 
+// Ranks [r0, r1) of the order, two scenarios a warp: a task is a
+// (supernode, scenario pair), and each half-warp factors the front of one
+// of the two scenarios (fronts of at most cap rows, a buffer per half).
+// Both fronts belong to the same supernode, so the halves run the same
+// loops, and each instruction of a pivot column's steps (pivot search,
+// reciprocal, multipliers) serves two fronts.  The FP64 elimination of
+// small fronts is bound by the FP64 pipe, which these steps, one per column
+// whatever the front's size, would otherwise occupy once per front.  A half
+// whose scenario this launch does not factor (M odd, or masked out) follows
+// its partner's front and stores nothing.
+template <class T, bool RHS>
+__global__ void __launch_bounds__(kThreads, 4) factor_pair_kernel(DevProblem P, DevWork W, DevSym S, DevDag D,
+                                                               T *fronts, T *lfac, T *ufac, const uint8_t *mask,
+                                                               int want, int r0, int r1, int cap, int ctr) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, half = lane >> 4;
+    unsigned char *hbase = smem_raw + (size_t)(2 * warp + half) * warp_area_bytes<T>(cap);
+    T *F = reinterpret_cast<T *>(hbase);
+    int *piv = reinterpret_cast<int *>(hbase + warp_front_bytes<T>(cap));
+    const int M = P.M, Mp = (M + 1) >> 1;
+    const int epoch = *D.epoch;
+    const int n_tasks = (r1 - r0) * Mp;
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(D.ctr + ctr, 1);
+        t = __shfl_sync(FULL, t, 0);
+        if (t >= n_tasks) break;
+        const int s = D.order[r0 + t / Mp], m0 = 2 * (t % Mp), m1 = m0 + 1;
+        const bool v0 = mask[m0] == want, v1 = m1 < M && mask[m1] == want;
+        if (!v0 && !v1) continue;
+        const bool act = half ? v1 : v0;
+        const int m = act ? m0 + half : (half ? m0 : m1);
+        factor_front<T, RHS>(
+            P, W, S, fronts, lfac, ufac, s, m, F, piv, HalfGroup{act},
+            [&] {
+                if (!half_wait_children(S, D, D.fdone, s, m, M, epoch) && (lane & 15) == 0 && act)
+                    atomicOr(W.status + m, 8);
+            },
+            [&] {
+                if ((lane & 15) == 0 && act) signal_done(D.fdone + (size_t)s * M + m, epoch);
+            });
+    }
+}
+
 template <class T, bool RHS>
 __global__ void __launch_bounds__(kThreads, 3) factor_big_kernel(DevProblem P, DevWork W, DevSym S, DevDag D,
                                                               T *fronts, T *lfac, T *ufac, const uint8_t *mask,
@@ -1119,10 +1207,17 @@ int configure_one(DagGrid &g, int nsm, int tiny_bytes, int small_bytes, int big_
             cudaSuccess || occ < 1)
         return -1;
     g.small = nsm * occ;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, factor_small_kernel<T, R>, kThreads, tiny_bytes) !=
-            cudaSuccess || occ < 1)
-        return -1;
-    g.tiny = nsm * occ;
+    if constexpr (sizeof(T) == 8) {
+        // the tiny fronts of FP64 factorisations: two scenarios a warp
+        if (cudaFuncSetAttribute(factor_pair_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 tiny_bytes) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, factor_pair_kernel<T, R>, kThreads, tiny_bytes) !=
+                cudaSuccess || occ < 1)
+            return -1;
+        g.tiny = nsm * occ;
+    } else {
+        g.tiny = 0;
+    }
     if (cudaFuncSetAttribute(factor_big_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, big_bytes) !=
             cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, factor_big_kernel<T, R>, kThreads, big_bytes) !=
@@ -1147,7 +1242,7 @@ int dag_configure(const DevDag &D, int fp32, DagGrid &g) {
     // not split whole, and the parts of the split ones
     const int mb = std::max(1, fp32 ? D.max_big_front : D.max_big_whole);
     const int small_bytes = kWarps * (fp32 ? warp_area_bytes<float>(kSmallFront) : warp_area_bytes<double>(kSmallFront));
-    const int tiny_bytes = kWarps * (fp32 ? warp_area_bytes<float>(kTinyFront) : warp_area_bytes<double>(kTinyFront));
+    const int tiny_bytes = fp32 ? 0 : 2 * kWarps * warp_area_bytes<double>(kTinyFront);   // two fronts a warp
     const int whole = (fp32 ? big_front_bytes<float>(mb) : big_front_bytes<double>(mb)) + 2 * mb * 4;
     const int part = fp32 ? 0 : ((D.max_part_entries * 8 + 15) & ~15) + D.max_part_ints * 4;
     const int big_bytes = std::max(whole, part);
@@ -1168,16 +1263,29 @@ int dag_tiny_front() { return kTinyFront; }
 
 void launch_dag_begin(const DevDag &D, cudaStream_t st) { dag_begin_kernel<<<1, 32, 0, st>>>(D); }
 
+namespace {
+__global__ void recip_check_kernel(const double *x, double *r, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) r[i] = recip(x[i]);
+}
+}  // namespace
+
+void launch_recip_check(const double *x, double *r, int n, cudaStream_t st) {
+    if (n > 0) recip_check_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, r, n);
+}
+
 template <class T>
 void launch_dag_factor(const DevProblem &P, const DevWork &W, const DevSym &S, const DevDag &D, const DagGrid &g,
                        T *fronts, T *lfac, T *ufac, const uint8_t *mask, int want, cudaStream_t st) {
     constexpr bool R = FusedRhs<T>::value;
     const int n_tiny = sizeof(T) == 8 ? D.n_tiny : 0;
-    const long long tt = (long long)n_tiny * P.M, ts = (long long)(D.n_small - n_tiny) * P.M,
+    const long long tt = (long long)n_tiny * ((P.M + 1) / 2), ts = (long long)(D.n_small - n_tiny) * P.M,
                     tb = (long long)(sizeof(T) == 8 ? D.big_units : D.nsup - D.n_small) * P.M;
-    if (tt > 0)
-        factor_small_kernel<T, R><<<blocks_for(g.tiny, tt, kWarps), kThreads, g.tiny_bytes, st>>>(
-            P, W, S, D, fronts, lfac, ufac, mask, want, 0, n_tiny, kTinyFront, 7);
+    if constexpr (sizeof(T) == 8) {
+        if (tt > 0)
+            factor_pair_kernel<T, R><<<blocks_for(g.tiny, tt, kWarps), kThreads, g.tiny_bytes, st>>>(
+                P, W, S, D, fronts, lfac, ufac, mask, want, 0, n_tiny, kTinyFront, 7);
+    }
     if (ts > 0)
         factor_small_kernel<T, R><<<blocks_for(g.small, ts, kWarps), kThreads, g.small_bytes, st>>>(
             P, W, S, D, fronts, lfac, ufac, mask, want, n_tiny, D.n_small, kSmallFront, 0);

@@ -246,6 +246,8 @@ int dag_configure(const DevDag &D, int fp32, DagGrid &g);
 int dag_small_front();
 int dag_tiny_front();
 void launch_dag_begin(const DevDag &D, cudaStream_t st);
+// r[i] = the factorisations' reciprocal of x[i] (device arrays), i < n.
+void launch_recip_check(const double *x, double *r, int n, cudaStream_t st);
 // Factors the scenarios m with mask[m] == want: fronts (update matrices) and
 // the solve-ordered copies lfac, ufac ([M][lu_total]); lfac may be null when
 // no forward solve will read it (the FP64 factorisation's own forward solve

@@ -28,6 +28,7 @@
 
 #include "gp_devices.cuh"
 #include "gp_internal.h"
+#include "gp_warp.cuh"
 
 namespace gp {
 
@@ -129,7 +130,7 @@ __device__ __forceinline__ void clu_program(T *vals, T *R0, T *R1, T *R2, const 
         const CluOp o = ops[q];
         switch (o.code) {
         case OP_RCP:
-            vals[o.d * 32 + lane] = T(1) / vals[o.a * 32 + lane];
+            vals[o.d * 32 + lane] = recip(vals[o.a * 32 + lane]);
             break;
         case OP_MUL:
             vals[o.d * 32 + lane] *= vals[o.a * 32 + lane];

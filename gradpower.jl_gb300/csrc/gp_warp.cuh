@@ -86,6 +86,31 @@ __device__ inline unsigned long long wait_tag(const unsigned long long *p, int e
     return 0ull;
 }
 
+// ---- reciprocal of a pivot ----------------------------------------------
+// float: the IEEE division.  double: the PTX approximate reciprocal
+// (rcp.approx.ftz.f64) refined by two Newton-Raphson steps r <- r + r (1 -
+// x r), each step two fused multiply-adds (the FMA form of the iteration in
+// P. Markstein, "Computation of elementary functions on the IBM RISC
+// System/6000 processor", IBM J. Res. Develop. 34 (1990) 111-119).  A step
+// squares the relative error, so from the seed's error two steps leave the
+// result within about one ulp of 1/x (the library's tests bound it against
+// the division).  Four FMAs on the FP64 pipe, which runs at two FMAs a clock
+// per SM on GB300 and is what the elimination of small fronts spends most
+// of its time on: a warp computes one reciprocal per pivot column.  Zero,
+// subnormal, very large, infinite and NaN pivots take the division, so
+// that they give the division's result exactly.
+__device__ __forceinline__ float recip(float x) { return 1.0f / x; }
+__device__ __forceinline__ double recip(double x) {
+    const unsigned e = ((unsigned)__double2hiint(x) >> 20) & 0x7ffu;
+    if (e == 0u || e > 0x7fcu) return 1.0 / x;
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    double t = fma(-x, r, 1.0);
+    r = fma(r, t, r);
+    t = fma(-x, r, 1.0);
+    return fma(r, t, r);
+}
+
 // Next power of two >= n, for 1 <= n <= 32.
 __device__ __forceinline__ int np2(int n) { return n <= 1 ? 1 : 1 << (32 - __clz(n - 1)); }
 

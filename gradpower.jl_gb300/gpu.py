@@ -60,12 +60,13 @@ def library():
         L.gp_set_device_disconnects.argtypes = [vp, C.c_int32, vp]
         L.gp_initialize.argtypes = [vp] * 7
         L.gp_adjoint.argtypes = [vp, vp, C.c_int32, vp, vp, C.c_int32, vp, vp, vp, vp]
+        L.gp_recip_check.argtypes = [C.c_int32, vp, vp]
         for f in ("gp_layout_create", "gp_layout_destroy", "gp_layout_stats", "gp_set_state",
                   "gp_get_state", "gp_integrate", "gp_residual", "gp_last_timing",
                   "gp_restore_initial_state", "gp_reduced_selftest", "gp_cluster_selftest",
                   "gp_residual_static", "gp_set_mixed_policy", "gp_set_profiling", "gp_set_wait_limit",
                   "gp_set_line_trips",
-                  "gp_set_device_disconnects", "gp_initialize", "gp_adjoint"):
+                  "gp_set_device_disconnects", "gp_initialize", "gp_adjoint", "gp_recip_check"):
             getattr(L, f).restype = C.c_int32
         _lib = L
     return _lib

@@ -422,6 +422,14 @@ int32_t gp_residual_static(gp_layout *L, const double *zold, double dt, double *
 int32_t gp_reduced_selftest(const gp_problem *prob, const int32_t *s_rowptr, const int32_t *s_colidx,
                             const double *s_val, const double *rhs, double *x, double out[12]);
 
+/* Device check of the reciprocal the FP64 factorisations take of each pivot
+ * (the hardware's approximate reciprocal refined by two Newton-Raphson
+ * steps, the division for zero, subnormal, very large, infinite and NaN
+ * pivots): r[i] = that reciprocal of x[i], i < n, computed on the current
+ * device.  No counterpart in the reference: a test hook that bounds the
+ * reciprocal against the correctly rounded 1/x. */
+int32_t gp_recip_check(int32_t n, const double *x, double *r);
+
 /* Host-only check of the cluster factorisation, needs no GPU: builds the
  * class plans of gp_layout_create from (z, u0, p) of one scenario and runs
  * every non-trivial cluster's program on the host in the device kernel's
