@@ -14,9 +14,9 @@
 // at once, and the kernel finishes with the scenario marked in `status`.
 //
 // Factorisation, in two launches (three for FP64):
-//  - factor_pair_kernel (FP64 only): supernodes whose whole subtree has
-//    fronts of at most kTinyFront rows, two scenarios a warp (a half-warp
-//    per front);
+//  - factor_group_kernel (FP64 only): supernodes whose whole subtree has
+//    fronts of at most kTinyFront rows, 32 / kTinyLanes scenarios a warp
+//    (kTinyLanes lanes per front);
 //  - factor_small_kernel: supernodes whose whole subtree has fronts of at
 //    most 32 rows, one warp per task, the front in shared memory;
 //  - factor_big_kernel: the rest, one CTA per task.
@@ -54,11 +54,17 @@ constexpr int kSmallFront = 32;
 // FP64 factorisations run the subtrees whose fronts have at most
 // kTinyFront rows first, in a launch of their own with a smaller front
 // buffer: more fronts in flight, where the 32-row buffers hold an SM to 24
-// (factorisation 693 -> 670 ms per FP64 run), and two fronts a warp
-// (factor_pair_kernel).  FP32 ones keep one launch: their 32-row buffers
+// (factorisation 693 -> 670 ms per FP64 run), and several fronts a warp
+// (factor_group_kernel).  FP32 ones keep one launch: their 32-row buffers
 // already allow 48 warps, and the launch boundary would cost the overlap of
 // the two regions (74 -> 81 ms per mixed run).
 constexpr int kTinyFront = 20;
+// lanes a tiny front gets in factor_group_kernel (32 / kTinyLanes fronts a
+// warp).  16: two fronts a warp.  8 (four fronts a warp, a quarter fewer
+// FP64 instructions by count) measured slower: the same shared memory then
+// holds half the warps, and the kernel also waits on its loads (FP64
+// factorisation 141.2 -> 144.7 ms over 0.3 s of the 70k-bus workload).
+constexpr int kTinyLanes = 16;
 // update-matrix entries a thread loads ahead in the extend-add: none in the
 // warp kernel, which runs at 40 registers a thread and many warps a SM
 template <class G>
@@ -96,20 +102,22 @@ __device__ bool warp_wait_children(const DevSym &S, const DevDag &D, const int *
     return ok;
 }
 
-// The same for two scenarios a warp: each half-warp waits for the children
-// of supernode s in its own scenario m (the whole warp calls it); true when
-// every wait of the caller's half succeeded.
-__device__ bool half_wait_children(const DevSym &S, const DevDag &D, const int *done, int s, int m, int M,
-                                   int epoch) {
+// The same for several scenarios a warp: each W-lane group (W = 8 or 16)
+// waits for the children of supernode s in its own scenario m (the whole
+// warp calls it); true when every wait of the caller's group succeeded.
+template <int W>
+__device__ bool group_wait_children(const DevSym &S, const DevDag &D, const int *done, int s, int m, int M,
+                                    int epoch) {
+    static_assert(W == 8 || W == 16, "lane groups of 8 or 16");
     const int c0 = S.child_ptr[s], nc = S.child_ptr[s + 1] - c0;
     bool ok = true;
-    for (int q = threadIdx.x & 15; q < nc; q += 16) {
+    for (int q = threadIdx.x & (W - 1); q < nc; q += W) {
         const int c = S.children[c0 + q];
         ok = wait_epoch(done + (size_t)c * M + m, epoch, D.err, D.wait_limit) && ok;
     }
     const unsigned bad = __ballot_sync(FULL, !ok);
     __syncwarp();
-    return (bad & (0xffffu << (threadIdx.x & 16))) == 0;
+    return (bad & (((1u << W) - 1u) << (threadIdx.x & 31 & ~(W - 1)))) == 0;
 }
 
 // Magnitude of a factor entry as an unsigned key that orders like |v|
@@ -156,11 +164,11 @@ __device__ __forceinline__ int warp_pivot(const T *F, int mm, int k, int ns, boo
     return bi;
 }
 
-// Thread groups that factor one front: a warp, the whole CTA, or half a
-// warp (two fronts a warp, each half on its own front of the same
-// supernode).  size: threads of the group; lanes: threads of the lead
+// Thread groups that factor one front: a warp, the whole CTA, or a W-lane
+// part of a warp (32 / W fronts a warp, each group on its own front of the
+// same supernode).  size: threads of the group; lanes: threads of the lead
 // segment that searches pivots and scales the multipliers; active(): false
-// for a half that only follows its partner (it computes the partner's front
+// for a group that only follows another's front (it computes that front
 // and stores nothing).
 struct WarpGroup {
     static constexpr int size = 32, lanes = 32;
@@ -178,14 +186,15 @@ struct BlockGroup {
     __device__ bool active() const { return true; }
     __device__ void sync() const { __syncthreads(); }
 };
-struct HalfGroup {
-    static constexpr int size = 16, lanes = 16;
+template <int W>
+struct LaneGroup {
+    static constexpr int size = W, lanes = W;
     bool act;
-    __device__ int idx() const { return threadIdx.x & 15; }
-    __device__ int lane() const { return threadIdx.x & 15; }
+    __device__ int idx() const { return threadIdx.x & (W - 1); }
+    __device__ int lane() const { return threadIdx.x & (W - 1); }
     __device__ bool lead_warp() const { return true; }
     __device__ bool active() const { return act; }
-    // both halves run the same supernode, so they meet every barrier
+    // every group runs the same supernode, so they meet every barrier
     __device__ void sync() const { __syncwarp(); }
 };
 
@@ -1062,46 +1071,55 @@ __global__ void __launch_bounds__(kThreads, 6) factor_small_kernel(DevProblem P,
     }
 }
 
-// Ranks [r0, r1) of the order, two scenarios a warp: a task is a
-// (supernode, scenario pair), and each half-warp factors the front of one
-// of the two scenarios (fronts of at most cap rows, a buffer per half).
-// Both fronts belong to the same supernode, so the halves run the same
-// loops, and each instruction of a pivot column's steps (pivot search,
-// reciprocal, multipliers) serves two fronts.  The FP64 elimination of
-// small fronts is bound by the FP64 pipe, which these steps, one per column
-// whatever the front's size, would otherwise occupy once per front.  A half
-// whose scenario this launch does not factor (M odd, or masked out) follows
-// its partner's front and stores nothing.
-template <class T, bool RHS>
-__global__ void __launch_bounds__(kThreads, 4) factor_pair_kernel(DevProblem P, DevWork W, DevSym S, DevDag D,
-                                                               T *fronts, T *lfac, T *ufac, const uint8_t *mask,
-                                                               int want, int r0, int r1, int cap, int ctr) {
+// Ranks [r0, r1) of the order, G = 32 / W scenarios a warp: a task is a
+// (supernode, group of G scenarios), and each W-lane group of the warp
+// factors the front of one of them (fronts of at most cap rows, a buffer per
+// group).  The fronts belong to the same supernode, so the groups run the
+// same loops, and each instruction of a pivot column's steps (pivot search,
+// reciprocal, multipliers) serves G fronts.  The FP64 elimination of small
+// fronts is bound by the FP64 pipe, which charges a warp instruction the
+// same whatever its active lanes, and these steps, one per column whatever
+// the front's size, would otherwise occupy it once per front.  A group
+// whose scenario this launch does not factor (M not a multiple of G, or
+// masked out) follows the task's first factored scenario and stores
+// nothing.
+template <class T, bool RHS, int W>
+__global__ void __launch_bounds__(kThreads, W == 16 ? 4 : 2) factor_group_kernel(DevProblem P, DevWork W_, DevSym S, DevDag D,
+                                                                T *fronts, T *lfac, T *ufac, const uint8_t *mask,
+                                                                int want, int r0, int r1, int cap, int ctr) {
+    constexpr int G = 32 / W;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, half = lane >> 4;
-    unsigned char *hbase = smem_raw + (size_t)(2 * warp + half) * warp_area_bytes<T>(cap);
-    T *F = reinterpret_cast<T *>(hbase);
-    int *piv = reinterpret_cast<int *>(hbase + warp_front_bytes<T>(cap));
-    const int M = P.M, Mp = (M + 1) >> 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, gi = lane / W;
+    unsigned char *gbase = smem_raw + (size_t)(G * warp + gi) * warp_area_bytes<T>(cap);
+    T *F = reinterpret_cast<T *>(gbase);
+    int *piv = reinterpret_cast<int *>(gbase + warp_front_bytes<T>(cap));
+    const int M = P.M, Mg = (M + G - 1) / G;
     const int epoch = *D.epoch;
-    const int n_tasks = (r1 - r0) * Mp;
+    const int n_tasks = (r1 - r0) * Mg;
     for (;;) {
         int t = 0;
         if (lane == 0) t = atomicAdd(D.ctr + ctr, 1);
         t = __shfl_sync(FULL, t, 0);
         if (t >= n_tasks) break;
-        const int s = D.order[r0 + t / Mp], m0 = 2 * (t % Mp), m1 = m0 + 1;
-        const bool v0 = mask[m0] == want, v1 = m1 < M && mask[m1] == want;
-        if (!v0 && !v1) continue;
-        const bool act = half ? v1 : v0;
-        const int m = act ? m0 + half : (half ? m0 : m1);
+        const int s = D.order[r0 + t / Mg], m0 = G * (t % Mg);
+        int first = -1;
+        bool act = false;
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            const bool v = m0 + g < M && mask[m0 + g] == want;
+            if (v && first < 0) first = m0 + g;
+            if (g == gi) act = v;
+        }
+        if (first < 0) continue;
+        const int m = act ? m0 + gi : first;
         factor_front<T, RHS>(
-            P, W, S, fronts, lfac, ufac, s, m, F, piv, HalfGroup{act},
+            P, W_, S, fronts, lfac, ufac, s, m, F, piv, LaneGroup<W>{act},
             [&] {
-                if (!half_wait_children(S, D, D.fdone, s, m, M, epoch) && (lane & 15) == 0 && act)
-                    atomicOr(W.status + m, 8);
+                if (!group_wait_children<W>(S, D, D.fdone, s, m, M, epoch) && (lane & (W - 1)) == 0 && act)
+                    atomicOr(W_.status + m, 8);
             },
             [&] {
-                if ((lane & 15) == 0 && act) signal_done(D.fdone + (size_t)s * M + m, epoch);
+                if ((lane & (W - 1)) == 0 && act) signal_done(D.fdone + (size_t)s * M + m, epoch);
             });
     }
 }
@@ -1209,9 +1227,10 @@ int configure_one(DagGrid &g, int nsm, int tiny_bytes, int small_bytes, int big_
     g.small = nsm * occ;
     if constexpr (sizeof(T) == 8) {
         // the tiny fronts of FP64 factorisations: two scenarios a warp
-        if (cudaFuncSetAttribute(factor_pair_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        if (cudaFuncSetAttribute(factor_group_kernel<T, R, kTinyLanes>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  tiny_bytes) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, factor_pair_kernel<T, R>, kThreads, tiny_bytes) !=
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, factor_group_kernel<T, R, kTinyLanes>, kThreads,
+                                                          tiny_bytes) !=
                 cudaSuccess || occ < 1)
             return -1;
         g.tiny = nsm * occ;
@@ -1242,7 +1261,7 @@ int dag_configure(const DevDag &D, int fp32, DagGrid &g) {
     // not split whole, and the parts of the split ones
     const int mb = std::max(1, fp32 ? D.max_big_front : D.max_big_whole);
     const int small_bytes = kWarps * (fp32 ? warp_area_bytes<float>(kSmallFront) : warp_area_bytes<double>(kSmallFront));
-    const int tiny_bytes = fp32 ? 0 : 2 * kWarps * warp_area_bytes<double>(kTinyFront);   // two fronts a warp
+    const int tiny_bytes = fp32 ? 0 : (32 / kTinyLanes) * kWarps * warp_area_bytes<double>(kTinyFront);
     const int whole = (fp32 ? big_front_bytes<float>(mb) : big_front_bytes<double>(mb)) + 2 * mb * 4;
     const int part = fp32 ? 0 : ((D.max_part_entries * 8 + 15) & ~15) + D.max_part_ints * 4;
     const int big_bytes = std::max(whole, part);
@@ -1279,11 +1298,12 @@ void launch_dag_factor(const DevProblem &P, const DevWork &W, const DevSym &S, c
                        T *fronts, T *lfac, T *ufac, const uint8_t *mask, int want, cudaStream_t st) {
     constexpr bool R = FusedRhs<T>::value;
     const int n_tiny = sizeof(T) == 8 ? D.n_tiny : 0;
-    const long long tt = (long long)n_tiny * ((P.M + 1) / 2), ts = (long long)(D.n_small - n_tiny) * P.M,
+    constexpr int G = 32 / kTinyLanes;
+    const long long tt = (long long)n_tiny * ((P.M + G - 1) / G), ts = (long long)(D.n_small - n_tiny) * P.M,
                     tb = (long long)(sizeof(T) == 8 ? D.big_units : D.nsup - D.n_small) * P.M;
     if constexpr (sizeof(T) == 8) {
         if (tt > 0)
-            factor_pair_kernel<T, R><<<blocks_for(g.tiny, tt, kWarps), kThreads, g.tiny_bytes, st>>>(
+            factor_group_kernel<T, R, kTinyLanes><<<blocks_for(g.tiny, tt, kWarps), kThreads, g.tiny_bytes, st>>>(
                 P, W, S, D, fronts, lfac, ufac, mask, want, 0, n_tiny, kTinyFront, 7);
     }
     if (ts > 0)
