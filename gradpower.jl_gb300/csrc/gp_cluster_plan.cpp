@@ -312,12 +312,17 @@ void make_cluster_plan(const gp_problem *pr, const double *z0, const double *u0,
         for (int t = 0; t < 3; t++) pl.pos3[(size_t)cls * 3 + t] = ipcol[cls_loc3[cls][t]];
         pl.lu_flops += fl * (int64_t)members[cls].size();
     }
-    // warp tasks: 32 clusters of one class
+    // warp tasks: 32 clusters of one class, the classes with the most slots
+    // (the longest programs) first, so that the warps that start last are
+    // the short ones
     pl.order.clear();
     pl.task_class.clear();
     pl.task_first.clear();
     pl.task_count.clear();
-    for (int cls = 0; cls < pl.n_class; cls++) {
+    std::vector<int> by_len(pl.n_class);
+    for (int cls = 0; cls < pl.n_class; cls++) by_len[cls] = cls;
+    std::stable_sort(by_len.begin(), by_len.end(), [&](int a, int b) { return pl.nslot[a] > pl.nslot[b]; });
+    for (int cls : by_len) {
         const int first = (int)pl.order.size();
         pl.order.insert(pl.order.end(), members[cls].begin(), members[cls].end());
         for (size_t s = 0; s < members[cls].size(); s += 32) {
