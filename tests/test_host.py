@@ -35,6 +35,15 @@ def test_library_exports_every_declared_symbol(lib):
     assert lib.gp_abi_version() == 1
 
 
+def test_recip_check_validates_its_arguments_before_any_device_call(lib):
+    """gp_recip_check refuses a negative count or missing arrays, and an
+    empty call succeeds, all without touching a device."""
+    assert lib.gp_recip_check(-1, None, None) == -1
+    assert "bad arguments" in lib_error(lib)
+    assert lib.gp_recip_check(3, None, None) == -1
+    assert lib.gp_recip_check(0, None, None) == 0
+
+
 def lib_error(lib):
     buf = C.create_string_buffer(1024)
     lib.gp_last_error(buf, 1024)
