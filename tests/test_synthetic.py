@@ -90,3 +90,25 @@ def test_planar_configuration(name, n_bus, n_gen, load_frac, scen, tf):
     _check_machines(gens, (3.0, 10.0), 0.2)
     _check_controls(w)
     assert w.n_scenarios == scen and len(w.faults) == scen and w.tf == tf and w.dt == 1.0 / 120.0
+
+
+def test_two_bus_configuration():
+    """Slack bus with one GENROU (H in [3, 6] s, the stated machine constants
+    exactly) and an IEESGO governor; a 0.8 + j0.3 pu load on bus 2 (its Q
+    stored negated, as the reference's case import stores it); one line of
+    r = 0.01, x = 0.1 pu; a 0.2 pu fault on bus 2 from 0.2 s to 0.3 s; 10 s
+    at dt = 1/120."""
+    w = synthetic.two_bus()
+    ps = w.ps
+    assert ps.nbus == 2 and ps.buses[0].type == 3
+    assert [(b.fr, b.to, b.r, b.x, b.sh) for b in ps.branches] == [(0, 1, 0.01, 0.1, 0.0)]
+    assert [(ld.bus, ld.pd, ld.qd) for ld in ps.loads] == [(1, 0.8, -0.3)]
+    assert _kinds(w) == {"genrou": 1, "ieesgo": 1, "zipload": 1}
+    g = _of(w, "genrou")[0]
+    assert 3.0 <= g.H <= 6.0 and g.D == 0.0
+    assert (g.x_d, g.x_q, g.x_dp, g.x_qp, g.x_ddp, g.xl) == (1.8, 1.7, 0.3, 0.55, 0.25, 0.2)
+    assert (g.T_d0p, g.T_q0p, g.T_d0dp, g.T_q0dp, g.S1, g.S2) == (6.0, 0.5, 0.03, 0.05, 0.09, 0.38)
+    _check_controls(w)
+    (f,), = w.faults
+    assert (f.bus, f.rfault, f.ton, f.toff) == (1, 0.2, 0.2, 0.3)
+    assert w.n_scenarios == 1 and w.tf == 10.0 and w.dt == 1.0 / 120.0
