@@ -63,3 +63,32 @@ def test_adjoint_initial_state_gradient_matches_fd(two_bus, orc):
     Jv = AO.objective_of_traj(PA, r["traj"], DT)
     fd = np.array([(Jv[2 * q] - Jv[2 * q + 1]) / (2 * hs[q]) for q in range(len(diff))])
     assert np.max(np.abs(c["gz"][diff] - fd)) <= 1e-6 * max(1e-3, np.max(np.abs(fd)))
+
+
+def test_adjoint_full_model_mix_with_voltage_term(orc):
+    """The differentiation workload's objective (speed deviation plus
+    10 * max(0, 0.9 - |V|)^2) on a small planar grid with every device type:
+    the adjoint's gradient with respect to the differentiated parameters
+    (machine H and D, SEXS K, ESDC1A KA, TGOV1 R, IEESGO K1) against central
+    differences, through a fault and its clearing."""
+    from helpers import synthetic
+    w = synthetic._planar("mix", 11, 120, 24, 0.6, 1, 0.5, "random")
+    PA = LY.ProblemArrays(w.ps)
+    kinds = {r.dtype.kind for r in w.ps.dynamic.devices}
+    assert {"genrou", "sexs", "esdc1a", "ieeest", "ieesgo", "tgov1", "zipload"} <= kinds
+    ev = w.faults[0]
+    ns = LY.jl_round(0.3 / DT)
+    fa, nf = LY.fault_array([ev], DT)
+    assert 0 < fa[0].on_step < fa[0].off_step <= ns
+    idx = AO.differentiated_params(PA)
+    kw = dict(w_speed=1.0, w_volt=10.0, v_min=0.9)
+    J, grad, _ = AO.adjoint(orc, PA, w.dp.zvec, w.dp.uvec, w.dp.pvec, ev, DT, ns, params=idx, **kw)
+    assert J > 0.0
+    # the voltage term is active: some bus dips below 0.9 during the fault
+    J_speed = AO.adjoint(orc, PA, w.dp.zvec, w.dp.uvec, w.dp.pvec, ev, DT, ns, params=[], **dict(kw, w_volt=0.0))[0]
+    assert J > J_speed * (1 + 1e-6)
+    fd = AO.fd_gradient(orc, PA, w.dp.zvec, w.dp.uvec, w.dp.pvec, ev, DT, ns, idx, **kw)
+    g = grad[idx]
+    scale = np.max(np.abs(fd))
+    assert scale > 0.0
+    assert np.all(np.abs(g - fd) <= 1e-5 * np.abs(fd) + 1e-7 * scale), np.max(np.abs(g - fd) / scale)
