@@ -112,3 +112,18 @@ def test_two_bus_configuration():
     (f,), = w.faults
     assert (f.bus, f.rfault, f.ton, f.toff) == (1, 0.2, 0.2, 0.3)
     assert w.n_scenarios == 1 and w.tf == 10.0 and w.dt == 1.0 / 120.0
+
+
+@pytest.mark.parametrize("name", ["two_bus", "ring39", "planar2k", "planar2k_adj", "planar2k_stressed",
+                                  "planar70k", "planar70k_charged"])
+def test_workloads_start_at_an_equilibrium(orc, name):
+    """Every workload's initial state is a steady state of its pre-fault
+    system: the oracle's backward-Euler residual vanishes there, the
+    check the reference makes of initialize_dynamics! (src/dynamics.jl:58,
+    test/test_integrate.jl:27-47)."""
+    from helpers import DT, Case
+    w = synthetic.WORKLOADS[name]()
+    c = Case(w.ps, w.dp)
+    fa, nf = c.fault_array()
+    f = orc.residual(c.PA, w.dp.zvec, w.dp.zvec, w.dp.uvec, w.dp.pvec, fa, nf, np.zeros(1), DT)
+    assert np.max(np.abs(f)) < 1e-9
