@@ -195,3 +195,31 @@ def test_oracle_shared_factor_path(orc):
     assert np.all(o3["status"] == 0) and np.all(o1["status"] == 0)
     assert o3["iters"].sum() > o1["iters"].sum()
     assert np.max(np.abs(o3["traj"] - o1["traj"]) / np.maximum(1.0, np.abs(o1["traj"]))) <= 1e-8
+
+
+def test_chained_windows_equal_one_horizon_and_threads_do_not_matter(orc):
+    """The reference arm of the benchmark integrates the horizon in chained
+    windows (each from the state the previous one ended in, the fault steps
+    shifted to the window's start): two windows of 24 steps give the bits of
+    one 48-step integration through the fault and its clearing, and the
+    oracle's OpenMP threads over scenarios do not change a bit."""
+    from helpers import synthetic_case
+    c, w = synthetic_case("planar2k", 2)
+    z0, u, p = c.arrays()
+    fa, nf = c.fault_array()
+    steps = [(fa[q].on_step, fa[q].off_step) for q in range(nf)]
+    assert all(0 < on < off <= 24 for on, off in steps)
+    whole = orc.integrate(c.PA, z0, u, p, fa, nf, DT, 48, itermax=30, solver=0, nthreads=2)
+    first = orc.integrate(c.PA, z0, u, p, fa, nf, DT, 24, itermax=30, solver=0, nthreads=1)
+    fb, nfb = c.fault_array()
+    for q in range(nfb):
+        fb[q].on_step -= 24
+        fb[q].off_step -= 24
+    second = orc.integrate(c.PA, np.ascontiguousarray(first["z"]), u, p, fb, nfb, DT, 24, itermax=30, solver=0,
+                           nthreads=2)
+    assert np.array_equal(second["z"], whole["z"])
+    assert np.array_equal(whole["traj"][:, 24], first["traj"][:, 24])
+    assert np.array_equal(whole["traj"][:, 48], second["traj"][:, 24])
+    # the same Newton iterations, step by step (two counts a step: the step
+    # and its event re-solve)
+    assert np.array_equal(whole["iters"], np.concatenate([first["iters"], second["iters"]], axis=1))
