@@ -154,7 +154,8 @@ typedef struct gp_line_trip {
  * at the end of step on_step the device's online flag is cleared
  * (_set_device_offline!, :672-698) for the rest of the call, followed by the
  * dt = 0 re-solve (src/dynamics.jl:612-646).  The batch kernels skip an
- * offline device (`table.online[k] || continue` in src/kernels/*.jl): its
+ * offline device (`table.online[k] || continue` in the device kernels of
+ * src/kernels/): its
  * differential states hold (their backward-Euler rows become z - zold) and
  * it injects nothing into the network.  A device that owns algebraic rows
  * (GENROU, IEESGO, TGOV1, IEEEST, a PV or slack static generator) would

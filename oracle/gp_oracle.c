@@ -1445,7 +1445,7 @@ static int integrate_one(const gp_problem *P0, const double *z0, const double *u
     /* device disconnections: a private copy of the problem whose online
      * flags this scenario's events clear, for the rest of the run
      * (_set_device_offline!, src/GradPower.jl:672-698; every kernel skips an
-     * offline device, src/kernels/*.jl) */
+     * offline device, the device kernels of src/kernels/) */
     gp_problem Pm = *P0;
     uint8_t *onl[GP_NTYPES] = {0};
     for (int e = 0; e < ndc; e++) {
