@@ -155,9 +155,8 @@ typedef struct gp_line_trip {
  * (_set_device_offline!, :672-698) for the rest of the call, followed by the
  * dt = 0 re-solve (src/dynamics.jl:612-646).  The batch kernels skip an
  * offline device (`table.online[k] || continue` in the device kernels of
- * src/kernels/): its
- * differential states hold (their backward-Euler rows become z - zold) and
- * it injects nothing into the network.  A device that owns algebraic rows
+ * src/kernels/): its differential states hold (their backward-Euler rows
+ * become z - zold) and it injects nothing into the network.  A device that owns algebraic rows
  * (GENROU, IEESGO, TGOV1, IEEEST, a PV or slack static generator) would
  * leave those rows without equations, a singular Jacobian: such events are
  * refused with GP_E_INVALID.  Every gp_integrate call starts and ends
