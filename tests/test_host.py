@@ -207,6 +207,19 @@ def _gloo_worker(rank, world, port, out_q):
     dist.destroy_process_group()
 
 
+def test_scenario_shard_partitions_the_scenarios():
+    """The ranks' ranges are contiguous, cover every scenario once, and
+    differ in size by at most one (more ranks than scenarios included)."""
+    from gradpower_gb300 import gpu as G
+    for Mtot in range(0, 21):
+        for world in range(1, 10):
+            r = [G.scenario_shard(Mtot, k, world) for k in range(world)]
+            assert r[0][0] == 0 and r[-1][1] == Mtot
+            assert all(r[k][1] == r[k + 1][0] for k in range(world - 1))
+            sizes = [hi - lo for lo, hi in r]
+            assert min(sizes) >= 0 and max(sizes) - min(sizes) <= 1
+
+
 def test_scenario_sharding_gloo(orc):
     """Scenarios shard across ranks with no exchange during the run; the
     gathered result equals the single-process run (world size 2, gloo)."""
